@@ -1,0 +1,265 @@
+"""btrc_gb300: GB300-native wavefront path tracer with Btrc's scene format.
+
+Python mirror of the C ABI in include/btrc.h (ctypes). The compute path is the in-tree
+CUDA library btrc_gb300/_build/libbtrc_gb300.so; there is no CPU fallback: when the
+library is missing or no GPU is present, the calls raise.
+
+Typical use (the reference's CLI flow, src/cli/main.cpp:17-81):
+
+    ctx = btrc_gb300.Context(0)
+    scene = ctx.load_scene("scene.json")   # parse JSON, load OBJ files
+    scene.build()                          # SAH BVH + upload
+    image = ctx.render(scene)              # float32 (H, W, 3) radiance / weight
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_build" / "libbtrc_gb300.so"
+
+OK = 0
+STATUS_NAMES = {
+    0: "OK", 1: "INVALID_ARG", 2: "IO", 3: "PARSE", 4: "CUDA", 5: "OOM",
+    6: "TIMEOUT", 7: "CANCELLED", 8: "UNSUPPORTED", 9: "INTERNAL",
+}
+HIT_BIT = 1 << 30
+
+# exported symbols and their ctypes signatures (kept in sync with include/btrc.h)
+_vp = C.c_void_p
+
+
+class SceneInfo(C.Structure):
+    _fields_ = [
+        ("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32),
+        ("min_depth", C.c_int32), ("max_depth", C.c_int32), ("state_count", C.c_int32),
+        ("sampler", C.c_int32), ("filter", C.c_int32),
+        ("instances", C.c_int32), ("geometries", C.c_int32), ("materials", C.c_int32),
+        ("area_lights", C.c_int32), ("media", C.c_int32), ("has_envir_light", C.c_int32),
+        ("triangles", C.c_uint64), ("bvh_nodes", C.c_int32), ("bvh_depth", C.c_int32),
+        ("bvh_bytes", C.c_uint64), ("world_min", C.c_float * 3), ("world_max", C.c_float * 3),
+        ("build_ms", C.c_double),
+    ]
+
+
+class BuildOpts(C.Structure):
+    _fields_ = [("threads", C.c_int32)]
+
+
+class RenderOpts(C.Structure):
+    _fields_ = [("spp", C.c_int32), ("state_count", C.c_int32), ("output_on_device", C.c_int32),
+                ("use_graphs", C.c_int32), ("profile", C.c_int32)]
+
+
+STAGES = ("control", "generate", "trace", "medium", "shade", "shadow")
+
+
+class Stats(C.Structure):
+    _fields_ = [("paths", C.c_uint64), ("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
+                ("bounces", C.c_uint32), ("traversal_errors", C.c_uint32), ("device_ms", C.c_double),
+                ("wall_ms", C.c_double), ("kernel_launches", C.c_uint64), ("stage_ms", C.c_double * 6),
+                ("stage_launches", C.c_uint64 * 6), ("node_visits", C.c_uint64), ("tri_tests", C.c_uint64)]
+
+    def as_dict(self) -> dict:
+        d = {}
+        for k, _ in self._fields_:
+            v = getattr(self, k)
+            d[k] = dict(zip(STAGES, list(v))) if k in ("stage_ms", "stage_launches") else v
+        return d
+
+
+SIGNATURES = {
+    "btrc_version": (C.c_char_p, []),
+    "btrc_ctx_create": (C.c_int, [C.c_int, C.POINTER(_vp)]),
+    "btrc_ctx_destroy": (None, [_vp]),
+    "btrc_last_error": (C.c_char_p, [_vp]),
+    "btrc_cancel": (None, [_vp]),
+    "btrc_scene_load_json": (C.c_int, [_vp, C.c_char_p, C.POINTER(_vp)]),
+    "btrc_scene_build": (C.c_int, [_vp, C.POINTER(BuildOpts)]),
+    "btrc_scene_info_get": (C.c_int, [_vp, C.POINTER(SceneInfo)]),
+    "btrc_scene_destroy": (None, [_vp]),
+    "btrc_scene_export_triangles": (C.c_int, [_vp, _vp, _vp, C.c_uint64]),
+    "btrc_scene_export_bvh": (C.c_int, [_vp, _vp, C.c_uint64, _vp, C.c_uint64]),
+    "btrc_render": (C.c_int, [_vp, _vp, C.POINTER(RenderOpts), _vp, C.POINTER(Stats)]),
+    "btrc_trace_closest": (C.c_int, [_vp, _vp, _vp, C.c_uint64, _vp, _vp, _vp]),
+    "btrc_trace_any": (C.c_int, [_vp, _vp, _vp, C.c_uint64, _vp, _vp]),
+    "btrc_trace_stats": (C.c_int, [_vp, _vp, _vp, C.c_uint64, _vp, _vp, _vp]),
+    "btrc_sampler_batch": (C.c_int, [_vp, C.c_int32, C.c_int32, C.c_int32, _vp, _vp, C.c_uint64, C.c_uint32,
+                                     _vp, _vp]),
+    "btrc_bsdf_batch": (C.c_int, [_vp, C.c_int32, _vp, _vp, _vp, C.c_uint64, _vp, _vp]),
+    "btrc_medium_tr_batch": (C.c_int, [_vp, _vp, C.c_int32, _vp, _vp, C.c_uint64, _vp, _vp]),
+}
+
+_lib = None
+
+
+class BtrcError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Load the CUDA library (built by btrc_gb300._build.build()). Raises if absent."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"native library {p} is missing: run btrc_gb300._build.build() first")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def version() -> str:
+    return load_library().btrc_version().decode()
+
+
+def _ptr(x) -> int | None:
+    """Raw address of a torch tensor / numpy array / int."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    raise TypeError(f"cannot take a pointer of {type(x)}")
+
+
+class Context:
+    """One CUDA device + stream (btrc_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = load_library()
+        h = _vp()
+        st = self._lib.btrc_ctx_create(device, C.byref(h))
+        if st != OK:
+            raise BtrcError(st, f"btrc_ctx_create(device={device}) failed")
+        self.handle = h
+        self.device = device
+
+    def _check(self, status: int):
+        if status != OK:
+            msg = self._lib.btrc_last_error(self.handle)
+            raise BtrcError(status, msg.decode() if msg else "")
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._lib.btrc_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def load_scene(self, path: str | os.PathLike) -> "Scene":
+        h = _vp()
+        self._check(self._lib.btrc_scene_load_json(self.handle, str(path).encode(), C.byref(h)))
+        return Scene(self, h)
+
+    def cancel(self):
+        self._lib.btrc_cancel(self.handle)
+
+    def render(self, scene: "Scene", spp: int = 0, state_count: int = 0, out=None, use_graphs: bool = True,
+               stats: dict | None = None, profile: int = 0) -> np.ndarray:
+        """Render the scene's frame. `out` may be a CUDA tensor (rendered in place) or None
+        (a new host float32 array of shape (H, W, 3) is returned)."""
+        info = scene.info()
+        on_dev = out is not None and hasattr(out, "is_cuda") and out.is_cuda
+        if out is None:
+            out = np.zeros((info.height, info.width, 3), np.float32)
+        opts = RenderOpts(spp, state_count, 1 if on_dev else 0, 1 if use_graphs else 0, profile)
+        st = Stats()
+        self._check(self._lib.btrc_render(self.handle, scene.handle, C.byref(opts), _ptr(out), C.byref(st)))
+        if stats is not None:
+            stats.update(st.as_dict())
+        return out
+
+    def trace_closest(self, scene: "Scene", rays, n: int, flags, hits, stream: int | None = None):
+        self._check(self._lib.btrc_trace_closest(self.handle, scene.handle, _ptr(rays), n, _ptr(flags),
+                                                 _ptr(hits), stream))
+
+    def trace_any(self, scene: "Scene", rays, n: int, occluded, stream: int | None = None):
+        self._check(self._lib.btrc_trace_any(self.handle, scene.handle, _ptr(rays), n, _ptr(occluded), stream))
+
+    def trace_stats(self, scene: "Scene", rays, n: int, node_visits, tri_tests, stream: int | None = None):
+        self._check(self._lib.btrc_trace_stats(self.handle, scene.handle, _ptr(rays), n, _ptr(node_visits),
+                                               _ptr(tri_tests), stream))
+
+    def sampler_batch(self, kind: int, width: int, height: int, pixel_xy, sample_index, n: int, dims: int, out,
+                      stream: int | None = None):
+        self._check(self._lib.btrc_sampler_batch(self.handle, kind, width, height, _ptr(pixel_xy),
+                                                 _ptr(sample_index), n, dims, _ptr(out), stream))
+
+    def bsdf_batch(self, op: int, material, wo, wi_or_u, n: int, out, stream: int | None = None):
+        self._check(self._lib.btrc_bsdf_batch(self.handle, op, _ptr(material), _ptr(wo), _ptr(wi_or_u), n,
+                                              _ptr(out), stream))
+
+    def medium_tr_batch(self, scene: "Scene", medium_id: int, seg, seeds, n: int, out, stream: int | None = None):
+        self._check(self._lib.btrc_medium_tr_batch(self.handle, scene.handle, medium_id, _ptr(seg), _ptr(seeds),
+                                                   n, _ptr(out), stream))
+
+
+class Scene:
+    """A loaded scene (btrc_scene). build() constructs the BVH and uploads to HBM."""
+
+    def __init__(self, ctx: Context, handle):
+        self.ctx = ctx
+        self.handle = handle
+
+    def build(self, threads: int = 0) -> "Scene":
+        opts = BuildOpts(threads)
+        self.ctx._check(self.ctx._lib.btrc_scene_build(self.handle, C.byref(opts)))
+        return self
+
+    def info(self) -> SceneInfo:
+        info = SceneInfo()
+        self.ctx._check(self.ctx._lib.btrc_scene_info_get(self.handle, C.byref(info)))
+        return info
+
+    def export_triangles(self) -> tuple[np.ndarray, np.ndarray]:
+        n = self.info().triangles
+        xyz = np.zeros((n, 9), np.float32)
+        ids = np.zeros((n, 2), np.uint32)
+        self.ctx._check(self.ctx._lib.btrc_scene_export_triangles(self.handle, xyz.ctypes.data, ids.ctypes.data, n))
+        return xyz, ids
+
+    def export_bvh(self) -> tuple[np.ndarray, np.ndarray]:
+        """(nodes, tris) as raw uint8 arrays of shape (N, 80) and (M, 48)."""
+        info = self.info()
+        nodes = np.zeros((info.bvh_nodes, 80), np.uint8)
+        tris = np.zeros((info.triangles, 48), np.uint8)
+        self.ctx._check(self.ctx._lib.btrc_scene_export_bvh(self.handle, nodes.ctypes.data, len(nodes),
+                                                            tris.ctypes.data, len(tris)))
+        return nodes, tris
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.ctx._lib.btrc_scene_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

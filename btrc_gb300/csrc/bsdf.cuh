@@ -1,0 +1,769 @@
+// Surface scattering for the wavefront shade stage. Each material follows the
+// reference's local-space component and the BSDFAggregate wrapper around it:
+//   aggregate / shading frame : builtin/btrc/builtin/material/utils/aggregate.cpp:32-229,
+//                               builtin/btrc/builtin/material/utils/shader_frame.cpp:5-95
+//   diffuse                   : builtin/btrc/builtin/material/component/diffuse.cpp:10-60
+//   GGX conductor (metal)     : builtin/btrc/builtin/material/component/microfacet_reflection.h:10-121
+//   Disney                    : builtin/btrc/builtin/material/disney.cpp:9-736
+//   mirror / invisible / black: builtin/btrc/builtin/material/{mirror,invisible,black}.cpp
+// Microfacet helpers: builtin/btrc/builtin/material/utils/microfacet.cpp:19-110,
+// Fresnel: builtin/btrc/builtin/material/utils/fresnel.cpp:5-49.
+#pragma once
+
+#include "bmath.h"
+#include "layout.h"
+
+namespace bt {
+
+struct CompSample
+{
+    V3 f;
+    V3 dir;
+    float pdf;
+    bool is_delta;
+};
+
+BT_HD CompSample comp_clear()
+{
+    CompSample s;
+    s.f = V3(0);
+    s.dir = V3(0);
+    s.pdf = 0;
+    s.is_delta = false;
+    return s;
+}
+
+BT_HD float sqrf(float x) { return x * x; }
+
+// ---------------------------------------------------------------- distributions
+
+BT_HD V3 sample_hemisphere_zweighted(float u1, float u2)
+{
+    float sx = 0, sy = 0;
+    u1 = 2.0f * u1 - 1.0f;
+    u2 = 2.0f * u2 - 1.0f;
+    if(u1 != 0.0f || u2 != 0.0f)
+    {
+        float theta, r;
+        if(fabsf(u1) > fabsf(u2))
+        {
+            r = u1;
+            theta = 0.25f * PI * (u2 / u1);
+        }
+        else
+        {
+            r = u2;
+            theta = 0.5f * PI - 0.25f * PI * (u1 / u2);
+        }
+        sx = r * cosf(theta);
+        sy = r * sinf(theta);
+    }
+    const float z = sqrtf(fmaxf(0.0f, 1.0f - (sx * sx + sy * sy)));
+    return V3(sx, sy, z);
+}
+
+BT_HD float pdf_hemisphere_zweighted(V3 v) { return v.z >= 0 ? v.z / PI : 0.0f; }
+
+BT_HD V3 sample_sphere_uniform(float u1, float u2)
+{
+    const float z = 1.0f - (u1 + u1);
+    const float phi = 2.0f * PI * u2;
+    const float r = sqrtf(fmaxf(0.0f, 1.0f - z * z));
+    return V3(r * cosf(phi), r * sinf(phi), z);
+}
+
+BT_HD float cos2sin(float c) { return sqrtf(fmaxf(0.0f, 1.0f - c * c)); }
+
+BT_HD float tan_theta(V3 w)
+{
+    const float t = 1.0f - w.z * w.z;
+    return t > 0 ? sqrtf(t) / w.z : 0.0f;
+}
+
+BT_HD float phi_of(V3 w)
+{
+    float r = 0.0f;
+    if(w.x != 0 || w.y != 0)
+    {
+        r = atan2f(w.y, w.x);
+        if(r < 0)
+            r += 2 * PI;
+    }
+    return r;
+}
+
+// ---------------------------------------------------------------- fresnel
+
+BT_HD float dielectric_fresnel(float eta_i, float eta_o, float cos_theta_i)
+{
+    if(cos_theta_i < 0)
+    {
+        const float t = eta_i;
+        eta_i = eta_o;
+        eta_o = t;
+        cos_theta_i = -cos_theta_i;
+    }
+    const float sin_theta_i = sqrtf(fmaxf(0.0f, 1.0f - cos_theta_i * cos_theta_i));
+    const float sin_theta_t = eta_o / eta_i * sin_theta_i;
+    if(sin_theta_t >= 1)
+        return 1.0f;
+    const float cos_theta_t = sqrtf(fmaxf(0.0f, 1.0f - sin_theta_t * sin_theta_t));
+    const float para = (eta_i * cos_theta_i - eta_o * cos_theta_t) / (eta_i * cos_theta_i + eta_o * cos_theta_t);
+    const float perp = (eta_o * cos_theta_i - eta_i * cos_theta_t) / (eta_o * cos_theta_i + eta_i * cos_theta_t);
+    return 0.5f * (para * para + perp * perp);
+}
+
+BT_HD float schlick(float R0, float c)
+{
+    const float t = 1.0f - c, t2 = t * t;
+    return R0 + (1.0f - R0) * (t2 * t2 * t);
+}
+
+BT_HD V3 schlick3(V3 R0, float c)
+{
+    const float t = 1.0f - c, t2 = t * t, t5 = t2 * t2 * t;
+    return R0 + (V3(1.0f) - R0) * t5;
+}
+
+// ---------------------------------------------------------------- microfacet
+
+BT_HD float mf_smith_gtr2(float tan_t, float alpha)
+{
+    if(tan_t == 0)
+        return 1.0f;
+    const float root = alpha * tan_t;
+    return 2.0f / (1.0f + sqrtf(1.0f + root * root));
+}
+
+BT_HD float mf_aniso_gtr2(float sin_phi_h, float cos_phi_h, float sin_theta_h, float cos_theta_h, float ax, float ay)
+{
+    const float A = sqrf(cos_phi_h / ax) + sqrf(sin_phi_h / ay);
+    const float RD = sqrf(sin_theta_h) * A + sqrf(cos_theta_h);
+    return 1.0f / (PI * ax * ay * sqrf(RD));
+}
+
+BT_HD float mf_smith_aniso_gtr2(float cos_phi, float sin_phi, float ax, float ay, float tan_t)
+{
+    const float t = sqrf(ax * cos_phi) + sqrf(ay * sin_phi);
+    const float sq = 1.0f + t * sqrf(tan_t);
+    const float lambda = -0.5f + 0.5f * sqrtf(sq);
+    return 1.0f / (1.0f + lambda);
+}
+
+BT_HD V3 mf_sample_aniso_gtr2(float ax, float ay, float s0, float s1)
+{
+    float sin_phi_h = ay * sinf(2 * PI * s0);
+    float cos_phi_h = ax * cosf(2 * PI * s0);
+    const float nor = 1.0f / sqrtf(sqrf(sin_phi_h) + sqrf(cos_phi_h));
+    sin_phi_h *= nor;
+    cos_phi_h *= nor;
+    const float A = sqrf(cos_phi_h / ax) + sqrf(sin_phi_h / ay);
+    const float cos_theta_h = sqrtf(A * (1.0f - s1) / ((1.0f - A) * s1 + A));
+    const float sin_theta_h = cos2sin(cos_theta_h);
+    return normalize(V3(sin_theta_h * cos_phi_h, sin_theta_h * sin_phi_h, cos_theta_h));
+}
+
+BT_HD float mf_gtr1(float sin_theta_h, float cos_theta_h, float alpha)
+{
+    const float U = sqrf(alpha) - 1;
+    const float LD = 2.0f * PI * logf(alpha);
+    const float RD = sqrf(alpha * cos_theta_h) + sqrf(sin_theta_h);
+    return U / (LD * RD);
+}
+
+BT_HD V3 mf_sample_gtr1(float alpha, float s0, float s1)
+{
+    const float phi = 2 * PI * s0;
+    const float cos_theta = sqrtf((powf(alpha, 2.0f - 2.0f * s1) - 1.0f) / (sqrf(alpha) - 1.0f));
+    const float sin_theta = cos2sin(cos_theta);
+    return normalize(V3(sin_theta * cosf(phi), sin_theta * sinf(phi), cos_theta));
+}
+
+BT_HD V3 mf_sample_vndf(V3 ve, float ax, float ay, float s0, float s1)
+{
+    const V3 vh = normalize(V3(ax * ve.x, ay * ve.y, ve.z));
+    const float lensq = vh.x * vh.x + vh.y * vh.y;
+    V3 t1(1, 0, 0);
+    if(lensq > 3e-4f)
+        t1 = V3(-vh.y, vh.x, 0) / sqrtf(lensq);
+    const V3 t2 = cross(vh, t1);
+    const float r = sqrtf(s0);
+    const float phi = 2 * PI * s1;
+    const float tt1 = r * cosf(phi);
+    const float tt2_ = r * sinf(phi);
+    const float s = 0.5f * (1.0f + vh.z);
+    const float tt2 = (1.0f - s) * sqrtf(1.0f - tt1 * tt1) + s * tt2_;
+    const V3 nh = tt1 * t1 + tt2 * t2 + sqrtf(fmaxf(0.0f, 1.0f - tt1 * tt1 - tt2 * tt2)) * vh;
+    return normalize(V3(ax * nh.x, ay * nh.y, fmaxf(0.0f, nh.z)));
+}
+
+// ---------------------------------------------------------------- diffuse component
+
+BT_HD CompSample diffuse_sample(V3 albedo, V3 lwo, float s1, float s2)
+{
+    if(lwo.z <= 0)
+        return comp_clear();
+    CompSample r;
+    r.dir = sample_hemisphere_zweighted(s1, s2);
+    r.f = albedo / PI;
+    r.pdf = pdf_hemisphere_zweighted(r.dir);
+    r.is_delta = false;
+    return r;
+}
+
+BT_HD V3 diffuse_eval(V3 albedo, V3 lwi, V3 lwo)
+{
+    return (lwi.z <= 0 || lwo.z <= 0) ? V3(0) : albedo / PI;
+}
+
+BT_HD float diffuse_pdf(V3 lwi, V3 lwo)
+{
+    return (lwi.z <= 0 || lwo.z <= 0) ? 0.0f : pdf_hemisphere_zweighted(lwi);
+}
+
+// ---------------------------------------------------------------- GGX conductor component
+
+struct MetalParams
+{
+    V3 R0;
+    float ax, ay;
+};
+
+BT_HD MetalParams metal_params(const float *p)
+{
+    MetalParams m;
+    m.R0 = V3(p[0], p[1], p[2]);
+    const float roughness = p[3], aniso = p[4];
+    float aspect = 1.0f;
+    if(aniso > 0)
+        aspect = sqrtf(1.0f - 0.9f * aniso);
+    m.ax = fmaxf(0.001f, roughness * roughness / aspect);
+    m.ay = fmaxf(0.001f, roughness * roughness * aspect);
+    return m;
+}
+
+BT_HD void metal_eval_pdf(const MetalParams &m, V3 lwi, V3 lwo, V3 &f, float &pdf)
+{
+    if(lwi.z <= 0 || lwo.z <= 0)
+    {
+        f = V3(0);
+        pdf = 0;
+        return;
+    }
+    const float cti = lwi.z, cto = lwo.z;
+    const V3 lwh = normalize(lwi + lwo);
+    const float ctd = dot(lwi, lwh);
+    const float phi_h = phi_of(lwh);
+    const float sph = sinf(phi_h), cph = cosf(phi_h);
+    const float cth = lwh.z, sth = cos2sin(cth);
+    const float D = mf_aniso_gtr2(sph, cph, sth, cth, m.ax, m.ay);
+    const float phi_i = phi_of(lwi), phi_o = phi_of(lwo);
+    const float Go = mf_smith_aniso_gtr2(cosf(phi_o), sinf(phi_o), m.ax, m.ay, tan_theta(lwo));
+    const float Gi = mf_smith_aniso_gtr2(cosf(phi_i), sinf(phi_i), m.ax, m.ay, tan_theta(lwi));
+    const V3 F = schlick3(m.R0, ctd);
+    f = F * (D * Gi * Go / fabsf(4.0f * cti * cto));
+    pdf = Go * D / (4.0f * lwo.z);
+}
+
+BT_HD CompSample metal_sample(const MetalParams &m, V3 lwo, float s1, float s2)
+{
+    CompSample r = comp_clear();
+    if(lwo.z > 0)
+    {
+        const V3 lwh = normalize(mf_sample_vndf(lwo, m.ax, m.ay, s1, s2));
+        if(lwh.z > 0)
+        {
+            const V3 lwi = normalize(2.0f * dot(lwo, lwh) * lwh - lwo);
+            if(lwi.z > 0)
+            {
+                r.dir = lwi;
+                metal_eval_pdf(m, lwi, lwo, r.f, r.pdf);
+            }
+        }
+    }
+    return r;
+}
+
+// ---------------------------------------------------------------- Disney component
+
+struct DisneyParams
+{
+    V3 C, C_tint;
+    float metallic, roughness, specular, specular_tint, anisotropic, sheen, sheen_tint;
+    float clearcoat, clearcoat_roughness, transmission, transmission_roughness, ior;
+    float trans_ax, trans_ay, ax, ay;
+    float w_diffuse, w_specular, w_clearcoat, w_transmission;
+};
+
+BT_HD float one_minus_5(float x)
+{
+    const float t = 1.0f - x, t2 = t * t;
+    return t2 * t2 * t;
+}
+
+BT_HD DisneyParams disney_params(const float *p)
+{
+    DisneyParams d;
+    d.C = V3(p[0], p[1], p[2]);
+    const float lum = luminance(d.C);
+    d.C_tint = lum > 0 ? d.C / lum : V3(1.0f);
+    d.metallic = p[3];
+    d.roughness = p[4];
+    d.specular = p[5];
+    d.specular_tint = p[6];
+    d.anisotropic = p[7];
+    d.sheen = p[8];
+    d.sheen_tint = p[9];
+    d.clearcoat = p[10];
+    const float clearcoat_gloss = p[11];
+    d.transmission = p[12];
+    d.transmission_roughness = p[13];
+    d.ior = fmaxf(1.01f, p[14]);
+    float aspect = 1.0f;
+    if(d.anisotropic > 0)
+        aspect = sqrtf(1.0f - 0.9f * d.anisotropic);
+    d.ax = fmaxf(0.001f, sqrf(d.roughness) / aspect);
+    d.ay = fmaxf(0.001f, sqrf(d.roughness) * aspect);
+    d.trans_ax = fmaxf(0.001f, sqrf(d.transmission_roughness) / aspect);
+    d.trans_ay = fmaxf(0.001f, sqrf(d.transmission_roughness) * aspect);
+    d.clearcoat_roughness = fmaxf(0.0001f, sqrf(lerpf(0.1f, 0.0f, clearcoat_gloss)));
+    const float A = clampf(lum * (1.0f - d.metallic), 0.3f, 0.7f);
+    const float B = 1.0f - A;
+    d.w_diffuse = A * (1.0f - d.transmission);
+    d.w_transmission = A * d.transmission;
+    d.w_specular = B * 2.0f / (2.0f + d.clearcoat);
+    d.w_clearcoat = B * d.clearcoat / (2.0f + d.clearcoat);
+    return d;
+}
+
+BT_HD bool disney_refract(V3 w, V3 n, float eta, V3 &out)
+{
+    const float cti = dot(w, n);
+    const float s2t = sqrf(eta) * (1.0f - sqrf(cti));
+    const float c2t = 1.0f - s2t;
+    if(c2t <= 0)
+        return false;
+    const float ctt = sqrtf(c2t);
+    out = normalize((eta * cti - ctt) * n - eta * w);
+    return true;
+}
+
+BT_HD V3 disney_eval_trans(const DisneyParams &d, V3 lwi, V3 lwo)
+{
+    const float cti = lwi.z, cto = lwo.z;
+    const float eta = cto > 0 ? d.ior : 1.0f / d.ior;
+    V3 lwh = normalize(lwo + eta * lwi);
+    if(lwh.z < 0)
+        lwh = -lwh;
+    const float ctd = dot(lwo, lwh);
+    const float F = dielectric_fresnel(d.ior, 1, ctd);
+    const float phi_h = phi_of(lwh);
+    const float cth = lwh.z, sth = cos2sin(cth);
+    const float D = mf_aniso_gtr2(sinf(phi_h), cosf(phi_h), sth, cth, d.trans_ax, d.trans_ay);
+    const float phi_i = phi_of(lwi), phi_o = phi_of(lwo);
+    const float G = mf_smith_aniso_gtr2(cosf(phi_i), sinf(phi_i), d.trans_ax, d.trans_ay, tan_theta(lwi)) *
+                    mf_smith_aniso_gtr2(cosf(phi_o), sinf(phi_o), d.trans_ax, d.trans_ay, tan_theta(lwo));
+    const float sdem = ctd + eta * dot(lwi, lwh);
+    const float corr = 1.0f / eta;  // radiance transport
+    const V3 sqrtC(sqrtf(d.C.x), sqrtf(d.C.y), sqrtf(d.C.z));
+    const float val = (1.0f - F) * D * G * eta * eta * dot(lwi, lwh) * dot(lwo, lwh) * corr * corr /
+                      (cti * cto * sdem * sdem);
+    const float trans_factor = cto > 0 ? d.transmission : 1.0f;
+    return sqrtC * ((1.0f - d.metallic) * trans_factor * fabsf(val));
+}
+
+BT_HD V3 disney_eval_inner_refl(const DisneyParams &d, V3 lwi, V3 lwo)
+{
+    const V3 lwh = -normalize(lwi + lwo);
+    const float ctd = dot(lwo, lwh);
+    const float F = dielectric_fresnel(d.ior, 1, ctd);
+    const float phi_h = phi_of(lwh);
+    const float cth = lwh.z, sth = cos2sin(cth);
+    const float D = mf_aniso_gtr2(sinf(phi_h), cosf(phi_h), sth, cth, d.trans_ax, d.trans_ay);
+    const float phi_i = phi_of(lwi), phi_o = phi_of(lwo);
+    const float G = mf_smith_aniso_gtr2(cosf(phi_i), sinf(phi_i), d.trans_ax, d.trans_ay, tan_theta(lwi)) *
+                    mf_smith_aniso_gtr2(cosf(phi_o), sinf(phi_o), d.trans_ax, d.trans_ay, tan_theta(lwo));
+    return d.C * (d.transmission * fabsf(F * D * G / (4.0f * lwi.z * lwo.z)));
+}
+
+BT_HD V3 disney_eval_specular(const DisneyParams &d, V3 lwi, V3 lwo)
+{
+    const float cti = lwi.z, cto = lwo.z;
+    const V3 lwh = normalize(lwi + lwo);
+    const float ctd = dot(lwi, lwh);
+    const V3 Cspec = lerp3(lerp3(V3(1.0f), d.C_tint, d.specular_tint), d.C, d.metallic);
+    const V3 dielectric = Cspec * dielectric_fresnel(d.ior, 1.0f, ctd);
+    const V3 conductor = schlick3(Cspec, ctd);
+    const V3 F = lerp3(d.specular * dielectric, conductor, d.metallic);
+    const float phi_h = phi_of(lwh);
+    const float cth = lwh.z, sth = cos2sin(cth);
+    const float D = mf_aniso_gtr2(sinf(phi_h), cosf(phi_h), sth, cth, d.ax, d.ay);
+    const float phi_i = phi_of(lwi), phi_o = phi_of(lwo);
+    const float G = mf_smith_aniso_gtr2(cosf(phi_i), sinf(phi_i), d.ax, d.ay, tan_theta(lwi)) *
+                    mf_smith_aniso_gtr2(cosf(phi_o), sinf(phi_o), d.ax, d.ay, tan_theta(lwo));
+    return F * (D * G / fabsf(4.0f * cti * cto));
+}
+
+BT_HD V3 disney_eval(const DisneyParams &d, V3 lwi, V3 lwo)
+{
+    if(fabsf(lwi.z) < 1e-4f || fabsf(lwo.z) < 1e-4f)
+        return V3(0);
+    if(lwi.z * lwo.z < 0)
+        return d.transmission == 0.0f ? V3(0) : disney_eval_trans(d, lwi, lwo);
+    if(lwi.z < 0 && lwo.z < 0)
+        return d.transmission == 0.0f ? V3(0) : disney_eval_inner_refl(d, lwi, lwo);
+    if(lwi.z <= 0 || lwo.z <= 0)
+        return V3(0);
+    const float cti = lwi.z, cto = lwo.z;
+    const V3 lwh = normalize(lwi + lwo);
+    const float ctd = dot(lwi, lwh);
+    V3 diffuse(0), sheen(0);
+    if(d.metallic < 1.0f)
+    {
+        const V3 lambert = d.C / PI;
+        const float fl = one_minus_5(cti), fv = one_minus_5(cto);
+        const float rr = 2.0f * d.roughness * ctd * ctd;
+        const V3 retro = d.C / PI * (rr * (fl + fv + fl * fv * (rr - 1)));
+        diffuse = lambert * ((1.0f - 0.5f * fl) * (1.0f - 0.5f * fv)) + retro;
+        if(d.sheen > 0.0f)
+            sheen = 4.0f * d.sheen * lerp3(V3(1.0f), d.C_tint, d.sheen_tint) * one_minus_5(ctd);
+    }
+    const V3 specular = disney_eval_specular(d, lwi, lwo);
+    V3 clearcoat(0);
+    if(d.clearcoat > 0.0f)
+    {
+        const float tti = tan_theta(lwi), tto = tan_theta(lwo);
+        const float cth = lwh.z, sth = cos2sin(cth);
+        const float D = mf_gtr1(sth, cth, d.clearcoat_roughness);
+        const float F = schlick(0.04f, ctd);
+        const float G = mf_smith_gtr2(tti, 0.25f) * mf_smith_gtr2(tto, 0.25f);
+        const float val = d.clearcoat * D * F * G / fabsf(4.0f * cti * cto);
+        clearcoat = V3(val);
+    }
+    return (diffuse + sheen) * ((1.0f - d.metallic) * (1.0f - d.transmission)) + specular + clearcoat;
+}
+
+BT_HD float disney_pdf_transmission(const DisneyParams &d, V3 lwi, V3 lwo)
+{
+    const float eta = lwo.z > 0 ? d.ior : 1.0f / d.ior;
+    V3 lwh = normalize(lwo + eta * lwi);
+    if(lwh.z < 0)
+        lwh = -lwh;
+    if(((lwo.z > 0) != (dot(lwh, lwo) > 0)) || ((lwi.z > 0) != (dot(lwh, lwi) > 0)))
+        return 0.0f;
+    const float sdem = dot(lwo, lwh) + eta * dot(lwi, lwh);
+    const float dwh_to_dwi = eta * eta * dot(lwi, lwh) / (sdem * sdem);
+    const float phi_h = phi_of(lwh);
+    const float cth = lwh.z, sth = cos2sin(cth);
+    const float D = mf_aniso_gtr2(sinf(phi_h), cosf(phi_h), sth, cth, d.trans_ax, d.trans_ay);
+    return fabsf(dot(lwi, lwh) * D * dwh_to_dwi);
+}
+
+BT_HD float disney_pdf_inner_refl(const DisneyParams &d, V3 lwi, V3 lwo)
+{
+    const V3 lwh = -normalize(lwi + lwo);
+    const float phi_h = phi_of(lwh);
+    const float cth = lwh.z, sth = cos2sin(cth);
+    const float ctd = dot(lwi, lwh);
+    const float D = mf_aniso_gtr2(sinf(phi_h), cosf(phi_h), sth, cth, d.trans_ax, d.trans_ay);
+    return fabsf(cth * D / (4.0f * ctd));
+}
+
+BT_HD float disney_pdf(const DisneyParams &d, V3 lwi, V3 lwo)
+{
+    if(fabsf(lwi.z) < 1e-4f || fabsf(lwo.z) < 1e-4f)
+        return 0.0f;
+    if(lwo.z < 0)
+    {
+        if(d.transmission == 0.0f)
+            return 0.0f;
+        const float macro_F = clampf(dielectric_fresnel(d.ior, 1, lwo.z), 0.1f, 0.9f);
+        if(lwi.z > 0)
+            return (1.0f - macro_F) * disney_pdf_transmission(d, lwi, lwo);
+        return macro_F * disney_pdf_inner_refl(d, lwi, lwo);
+    }
+    if(lwi.z < 0)
+        return d.w_transmission * disney_pdf_transmission(d, lwi, lwo);
+    const float diffuse = pdf_hemisphere_zweighted(lwi);
+    const V3 lwh = normalize(lwi + lwo);
+    const float phi_h = phi_of(lwh);
+    const float cth = lwh.z, sth = cos2sin(cth);
+    const float ctd = dot(lwi, lwh);
+    // the reference derives sin(phi_o) as sqrt(1 - cos^2), i.e. always non-negative
+    const float cpo = cosf(phi_of(lwo));
+    const float spo = cos2sin(cpo);
+    const float spec_D = mf_aniso_gtr2(sinf(phi_h), cosf(phi_h), sth, cth, d.ax, d.ay);
+    const float pdf_spec = mf_smith_aniso_gtr2(cpo, spo, d.ax, d.ay, tan_theta(lwo)) * spec_D / (4.0f * lwo.z);
+    const float cc_D = mf_gtr1(sth, cth, d.clearcoat_roughness);
+    const float pdf_cc = cth * cc_D / (4.0f * ctd);
+    return d.w_diffuse * diffuse + d.w_specular * pdf_spec + d.w_clearcoat * pdf_cc;
+}
+
+BT_HD V3 disney_sample_transmission(const DisneyParams &d, V3 lwo, float s0, float s1)
+{
+    const V3 lwh = mf_sample_aniso_gtr2(d.trans_ax, d.trans_ay, s0, s1);
+    if(lwh.z <= 0)
+        return V3(0);
+    if((lwo.z > 0) != (dot(lwh, lwo) > 0))
+        return V3(0);
+    const float eta = lwo.z > 0 ? 1.0f / d.ior : d.ior;
+    const V3 owh = dot(lwh, lwo) > 0 ? lwh : -lwh;
+    V3 lwi;
+    if(!disney_refract(lwo, owh, eta, lwi))
+        return V3(0);
+    if(lwi.z * lwo.z > 0 || ((lwi.z > 0) != (dot(lwh, lwi) > 0)))
+        return V3(0);
+    return normalize(lwi);
+}
+
+BT_HD V3 disney_sample_inner_refl(const DisneyParams &d, V3 lwo, float s0, float s1)
+{
+    const V3 lwh = mf_sample_aniso_gtr2(d.trans_ax, d.trans_ay, s0, s1);
+    if(lwh.z <= 0)
+        return V3(0);
+    const V3 lwi = 2.0f * dot(lwo, lwh) * lwh - lwo;
+    if(lwi.z > 0)
+        return V3(0);
+    return normalize(lwi);
+}
+
+BT_HD V3 disney_sample_specular(const DisneyParams &d, V3 lwo, float s0, float s1)
+{
+    const V3 lwh = mf_sample_vndf(lwo, d.ax, d.ay, s0, s1);
+    if(lwh.z <= 0)
+        return V3(0);
+    const V3 lwi = 2.0f * dot(lwo, lwh) * lwh - lwo;
+    if(lwi.z <= 0)
+        return V3(0);
+    return normalize(lwi);
+}
+
+BT_HD V3 disney_sample_clearcoat(const DisneyParams &d, V3 lwo, float s0, float s1)
+{
+    const V3 lwh = mf_sample_gtr1(d.clearcoat_roughness, s0, s1);
+    if(lwh.z <= 0)
+        return V3(0);
+    const V3 lwi = 2.0f * dot(lwo, lwh) * lwh - lwo;
+    if(lwi.z <= 0)
+        return V3(0);
+    return normalize(lwi);
+}
+
+BT_HD CompSample disney_sample(const DisneyParams &d, V3 lwo, float s0, float s1, float s2)
+{
+    CompSample r = comp_clear();
+    if(fabsf(lwo.z) < 1e-4f)
+        return r;
+    V3 lwi;
+    if(lwo.z < 0)
+    {
+        if(d.transmission == 0.0f)
+            return r;
+        const float macro_F = clampf(dielectric_fresnel(d.ior, 1, lwo.z), 0.1f, 0.9f);
+        lwi = s0 >= macro_F ? disney_sample_transmission(d, lwo, s1, s2) : disney_sample_inner_refl(d, lwo, s1, s2);
+    }
+    else
+    {
+        float sel = s0;
+        if(sel < d.w_diffuse)
+            lwi = sample_hemisphere_zweighted(s1, s2);
+        else
+        {
+            sel -= d.w_diffuse;
+            if(sel < d.w_transmission)
+                lwi = disney_sample_transmission(d, lwo, s1, s2);
+            else
+            {
+                sel -= d.w_transmission;
+                if(sel < d.w_specular)
+                    lwi = disney_sample_specular(d, lwo, s1, s2);
+                else
+                    lwi = disney_sample_clearcoat(d, lwo, s1, s2);
+            }
+        }
+    }
+    if(lwi.x == 0 && lwi.y == 0 && lwi.z == 0)
+        return r;
+    r.dir = lwi;
+    r.f = disney_eval(d, lwi, lwo);
+    r.pdf = disney_pdf(d, lwi, lwo);
+    // handle_bad_sample (disney.cpp:566-573)
+    const V3 v = r.f * (fabsf(r.dir.z) / r.pdf);
+    if(fmaxf(fmaxf(v.x, v.y), v.z) > 10)
+        return comp_clear();
+    return r;
+}
+
+// ---------------------------------------------------------------- shading frame + aggregate
+
+struct ShaderFrame
+{
+    Frame geometry;
+    Frame shading;
+
+    BT_HD bool is_black_fringes(V3 w) const
+    {
+        return geometry.in_positive_z_hemisphere(w) != shading.in_positive_z_hemisphere(w);
+    }
+    BT_HD ShaderFrame flip_for_black_fringes(V3 wo) const
+    {
+        ShaderFrame f;
+        f.geometry = geometry;
+        f.shading = is_black_fringes(wo) ? geometry : shading;
+        return f;
+    }
+    BT_HD float correct_shading_energy(V3 wi) const
+    {
+        const float down = fabsf(dot(geometry.z, wi));
+        if(down > 1e-4f)
+            return fabsf(dot(shading.z, wi)) / down;
+        return 1.0f;
+    }
+    BT_HD float shadow_terminator(V3 wi) const
+    {
+        const float wgwi = dot(geometry.z, wi);
+        const float wswi = dot(shading.z, wi);
+        const float wgws = dot(geometry.z, shading.z);
+        const float g = saturate(wgwi / (wswi * wgws));
+        return -g * g * g + g * g + g;
+    }
+};
+
+// Local-space component dispatch for the aggregate materials (diffuse, metal, disney).
+struct MaterialEval
+{
+    int type;
+    V3 albedo;           // diffuse
+    MetalParams metal;
+    DisneyParams disney;
+};
+
+BT_HD MaterialEval make_material_eval(const Material &m)
+{
+    MaterialEval e;
+    e.type = m.type;
+    e.albedo = V3(m.p[0], m.p[1], m.p[2]);
+    if(m.type == MAT_METAL)
+        e.metal = metal_params(m.p);
+    else if(m.type == MAT_DISNEY)
+        e.disney = disney_params(m.p);
+    return e;
+}
+
+BT_HD CompSample comp_sample(const MaterialEval &e, V3 lwo, float s0, float s1, float s2)
+{
+    if(e.type == MAT_DIFFUSE)
+        return diffuse_sample(e.albedo, lwo, s1, s2);
+    if(e.type == MAT_METAL)
+        return metal_sample(e.metal, lwo, s1, s2);
+    return disney_sample(e.disney, lwo, s0, s1, s2);
+}
+
+BT_HD V3 comp_eval(const MaterialEval &e, V3 lwi, V3 lwo)
+{
+    if(e.type == MAT_DIFFUSE)
+        return diffuse_eval(e.albedo, lwi, lwo);
+    if(e.type == MAT_METAL)
+    {
+        V3 f;
+        float pdf;
+        metal_eval_pdf(e.metal, lwi, lwo, f, pdf);
+        return f;
+    }
+    return disney_eval(e.disney, lwi, lwo);
+}
+
+BT_HD float comp_pdf(const MaterialEval &e, V3 lwi, V3 lwo)
+{
+    if(e.type == MAT_DIFFUSE)
+        return diffuse_pdf(lwi, lwo);
+    if(e.type == MAT_METAL)
+    {
+        V3 f;
+        float pdf;
+        metal_eval_pdf(e.metal, lwi, lwo, f, pdf);
+        return pdf;
+    }
+    return disney_pdf(e.disney, lwi, lwo);
+}
+
+// Full surface shader: aggregate materials go through the shading-frame logic with a
+// single component of weight 1; mirror / invisible / black are their own shaders.
+struct SurfaceShader
+{
+    ShaderFrame frame;
+    MaterialEval mat;
+    bool shadow_terminator;
+
+    BT_HD CompSample sample(V3 wo, float s0, float s1, float s2) const
+    {
+        CompSample r = comp_clear();
+        if(mat.type == MAT_BLACK)
+            return r;
+        if(mat.type == MAT_INVISIBLE)
+        {
+            r.f = V3(1.0f / fabsf(dot(frame.geometry.z, normalize(wo))));
+            r.dir = -wo;
+            r.pdf = 1;
+            r.is_delta = true;
+            return r;
+        }
+        const ShaderFrame fr = frame.flip_for_black_fringes(wo);
+        if(mat.type == MAT_MIRROR)
+        {
+            V3 lwo = fr.shading.global_to_local(wo);
+            if(lwo.z > 0)
+            {
+                lwo = normalize(lwo);
+                const V3 wi = fr.shading.local_to_global(V3(-lwo.x, -lwo.y, lwo.z));
+                if(!frame.is_black_fringes(wi))
+                {
+                    r.f = schlick3(mat.albedo, lwo.z) / lwo.z * fr.correct_shading_energy(wi);
+                    r.dir = wi;
+                    r.pdf = 1;
+                    r.is_delta = true;
+                }
+            }
+            return r;
+        }
+        const V3 lwo = normalize(fr.shading.global_to_local(wo));
+        const CompSample c = comp_sample(mat, lwo, s0, s1, s2);
+        if(c.pdf <= 0)
+            return r;
+        r.dir = fr.shading.local_to_global(c.dir);
+        if(frame.is_black_fringes(r.dir))
+            return comp_clear();
+        r.pdf = c.pdf;
+        float k = fr.correct_shading_energy(r.dir);
+        if(shadow_terminator)
+            k *= frame.shadow_terminator(r.dir);
+        r.f = c.f * k;
+        r.is_delta = false;
+        return r;
+    }
+
+    BT_HD V3 eval(V3 wi, V3 wo) const
+    {
+        if(mat.type == MAT_BLACK || mat.type == MAT_INVISIBLE || mat.type == MAT_MIRROR)
+            return V3(0);
+        const ShaderFrame fr = frame.flip_for_black_fringes(wo);
+        const V3 lwi = normalize(fr.shading.global_to_local(wi));
+        const V3 lwo = normalize(fr.shading.global_to_local(wo));
+        float k = fr.correct_shading_energy(wi);
+        if(shadow_terminator)
+            k *= frame.shadow_terminator(wi);
+        return comp_eval(mat, lwi, lwo) * k;
+    }
+
+    BT_HD float pdf(V3 wi, V3 wo) const
+    {
+        if(mat.type == MAT_BLACK || mat.type == MAT_INVISIBLE || mat.type == MAT_MIRROR)
+            return 0.0f;
+        const ShaderFrame fr = frame.flip_for_black_fringes(wo);
+        const V3 lwi = normalize(fr.shading.global_to_local(wi));
+        const V3 lwo = normalize(fr.shading.global_to_local(wo));
+        return comp_pdf(mat, lwi, lwo);
+    }
+};
+
+} // namespace bt

@@ -1,0 +1,798 @@
+// C-ABI implementation: host runtime around the CUDA kernels. No C++ exception
+// crosses this boundary; every failure becomes a btrc_status plus a message.
+#include <atomic>
+#include <chrono>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/btrc.h"
+#include "bvh.h"
+#include "kernels.h"
+#include "scene.h"
+
+using namespace bt;
+
+struct btrc_ctx
+{
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    std::atomic<bool> cancel{ false };
+    // render buffers, grown on demand and reused across renders
+    RenderBuffers buf{};
+    std::vector<void *> buf_allocs;
+    uint32_t buf_capacity = 0;
+    size_t film_pixels = 0;
+    bool has_media_buffers = false;
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+};
+
+struct btrc_scene
+{
+    btrc_ctx *ctx = nullptr;
+    HostScene host;
+    bool built = false;
+    DevScene dev{};
+    std::vector<void *> allocs;
+    int bvh_nodes = 0, bvh_depth = 0;
+    uint64_t bvh_bytes = 0;
+    double build_ms = 0;
+    std::vector<AliasEntry8> filter_table_host;
+    AliasEntry8 *filter_table = nullptr;
+    std::vector<float> export_xyz;
+    std::vector<uint32_t> export_ids;
+    std::vector<CWNode> host_nodes;  // kept for host-only contexts and small scenes
+    std::vector<TriRec> host_tris;
+};
+
+namespace {
+
+struct StatusError : std::runtime_error
+{
+    btrc_status status;
+    StatusError(btrc_status s, const std::string &m) : std::runtime_error(m), status(s) {}
+};
+
+void check_cuda(cudaError_t e, const char *what)
+{
+    if(e == cudaSuccess)
+        return;
+    const btrc_status s = e == cudaErrorMemoryAllocation ? BTRC_ERR_OOM : BTRC_ERR_CUDA;
+    throw StatusError(s, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template<typename F>
+btrc_status guarded(btrc_ctx *ctx, F &&f)
+{
+    try
+    {
+        f();
+        if(ctx)
+            ctx->last_error.clear();
+        return BTRC_OK;
+    }
+    catch(const StatusError &e)
+    {
+        if(ctx)
+            ctx->last_error = e.what();
+        return e.status;
+    }
+    catch(const json::ParseError &e)
+    {
+        if(ctx)
+            ctx->last_error = e.what();
+        return std::string(e.what()).find("cannot open") != std::string::npos ? BTRC_ERR_IO : BTRC_ERR_PARSE;
+    }
+    catch(const std::bad_alloc &)
+    {
+        if(ctx)
+            ctx->last_error = "host allocation failed";
+        return BTRC_ERR_OOM;
+    }
+    catch(const std::exception &e)
+    {
+        if(ctx)
+            ctx->last_error = e.what();
+        const std::string m = e.what();
+        if(m.find("cannot open") != std::string::npos || m.find("failed to open") != std::string::npos)
+            return BTRC_ERR_IO;
+        if(m.find("unsupported") != std::string::npos)
+            return BTRC_ERR_UNSUPPORTED;
+        return BTRC_ERR_PARSE;
+    }
+    catch(...)
+    {
+        if(ctx)
+            ctx->last_error = "unknown internal error";
+        return BTRC_ERR_INTERNAL;
+    }
+}
+
+template<typename T>
+T *dev_upload(std::vector<void *> &allocs, const T *src, size_t count)
+{
+    if(count == 0)
+        return nullptr;
+    void *p = nullptr;
+    check_cuda(cudaMalloc(&p, sizeof(T) * count), "cudaMalloc");
+    allocs.push_back(p);
+    check_cuda(cudaMemcpy(p, src, sizeof(T) * count, cudaMemcpyHostToDevice), "cudaMemcpy");
+    return static_cast<T *>(p);
+}
+
+void *dev_alloc(std::vector<void *> &allocs, size_t bytes)
+{
+    void *p = nullptr;
+    check_cuda(cudaMalloc(&p, bytes > 0 ? bytes : 16), "cudaMalloc");
+    allocs.push_back(p);
+    return p;
+}
+
+void free_all(std::vector<void *> &allocs)
+{
+    for(void *p : allocs)
+        cudaFree(p);
+    allocs.clear();
+}
+
+void extended_gcd(uint64_t a, uint64_t b, int64_t *x, int64_t *y)
+{
+    if(b == 0)
+    {
+        *x = 1;
+        *y = 0;
+        return;
+    }
+    const int64_t d = static_cast<int64_t>(a / b);
+    int64_t xp, yp;
+    extended_gcd(b, a % b, &xp, &yp);
+    *x = yp;
+    *y = xp - d * yp;
+}
+
+int64_t mult_inverse(int64_t a, int64_t n)
+{
+    int64_t x, y;
+    extended_gcd(static_cast<uint64_t>(a), static_cast<uint64_t>(n), &x, &y);
+    int64_t r = x - x / n * n;
+    return r < 0 ? r + n : r;
+}
+
+// HaltonSampler::initialize_consts (builtin/btrc/builtin/sampler/halton.cpp:140-160)
+HaltonConsts halton_consts(int width, int height)
+{
+    HaltonConsts hc{};
+    const int res[2] = { width, height };
+    for(int i = 0; i < 2; ++i)
+    {
+        const int base = i == 0 ? 2 : 3;
+        int scale = 1, e = 0;
+        while(scale < std::min(res[i], HALTON_MAX_RES))
+        {
+            scale *= base;
+            ++e;
+        }
+        hc.scale[i] = scale;
+        hc.exponent[i] = e;
+    }
+    hc.mult_inverse[0] = static_cast<int32_t>(mult_inverse(hc.scale[1], hc.scale[0]));
+    hc.mult_inverse[1] = static_cast<int32_t>(mult_inverse(hc.scale[0], hc.scale[1]));
+    hc.stride = hc.scale[0] * hc.scale[1];
+    return hc;
+}
+
+void build_scene(btrc_scene *sc, int threads)
+{
+    HostScene &H = sc->host;
+    const auto t0 = std::chrono::steady_clock::now();
+    const bool host_only = sc->ctx->device < 0;
+    if(!host_only)
+    {
+        check_cuda(cudaSetDevice(sc->ctx->device), "cudaSetDevice");
+        free_all(sc->allocs);
+    }
+
+    // flatten instances into world-space triangles (single-level BVH)
+    std::vector<TriRec> world;
+    world.reserve(H.triangle_count);
+    sc->export_xyz.clear();
+    sc->export_ids.clear();
+    for(size_t i = 0; i < H.instances.size(); ++i)
+    {
+        const HostGeometry &g = H.geometries[H.instances[i].geometry];
+        const Transform &xf = H.instance_xf[i];
+        const size_t nt = g.area.size();
+        for(size_t t = 0; t < nt; ++t)
+        {
+            const V3 a = xf.point(g.pos[t * 3 + 0]);
+            const V3 b = xf.point(g.pos[t * 3 + 1]);
+            const V3 c = xf.point(g.pos[t * 3 + 2]);
+            TriRec r{ a.x, a.y, a.z, static_cast<uint32_t>(i), b.x, b.y, b.z, static_cast<uint32_t>(t),
+                      c.x, c.y, c.z, 0u };
+            world.push_back(r);
+        }
+    }
+    CWBVH bvh = build_cwbvh(world, threads);
+    sc->export_xyz.resize(world.size() * 9);
+    sc->export_ids.resize(world.size() * 2);
+    for(size_t k = 0; k < world.size(); ++k)
+    {
+        const TriRec &r = world[k];
+        const float v[9] = { r.v0x, r.v0y, r.v0z, r.v1x, r.v1y, r.v1z, r.v2x, r.v2y, r.v2z };
+        std::memcpy(&sc->export_xyz[k * 9], v, sizeof(v));
+        sc->export_ids[k * 2] = r.inst;
+        sc->export_ids[k * 2 + 1] = r.prim;
+    }
+    world.clear();
+    world.shrink_to_fit();
+    sc->bvh_nodes = static_cast<int>(bvh.nodes.size());
+    sc->bvh_depth = bvh.depth;
+    sc->bvh_bytes = bvh.nodes.size() * sizeof(CWNode) + bvh.tris.size() * sizeof(TriRec);
+    if(host_only || H.triangle_count <= (1u << 20))
+    {
+        sc->host_nodes = bvh.nodes;
+        sc->host_tris = bvh.tris;
+    }
+    if(host_only)
+    {
+        sc->built = true;
+        sc->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        return;
+    }
+
+    DevScene &D = sc->dev;
+    D = DevScene{};
+    D.nodes = reinterpret_cast<const F4 *>(dev_upload(sc->allocs, bvh.nodes.data(), bvh.nodes.size()));
+    D.tris = reinterpret_cast<const F4 *>(dev_upload(sc->allocs, bvh.tris.data(), bvh.tris.size()));
+    D.node_count = static_cast<uint32_t>(bvh.nodes.size());
+    D.tri_count = static_cast<uint32_t>(bvh.tris.size());
+
+    // shading SoA + geometry table + light sampling data
+    std::vector<Geometry> geos(H.geometries.size());
+    std::vector<bool> is_light_geo(H.geometries.size(), false);
+    for(auto &L : H.area_lights)
+        is_light_geo[L.geometry] = true;
+    size_t total = 0, light_total = 0;
+    for(size_t g = 0; g < H.geometries.size(); ++g)
+    {
+        geos[g].tri_offset = static_cast<uint32_t>(total);
+        geos[g].tri_count = static_cast<uint32_t>(H.geometries[g].area.size());
+        geos[g].total_area = H.geometries[g].total_area;
+        uint32_t lo = 0xffffffffu;
+        if(is_light_geo[g])
+        {
+            lo = static_cast<uint32_t>(light_total);
+            light_total += H.geometries[g].area.size();
+        }
+        std::memcpy(&geos[g].pad, &lo, sizeof(lo));
+        total += H.geometries[g].area.size();
+    }
+    for(int k = 0; k < 6; ++k)
+    {
+        std::vector<F4> cat;
+        cat.reserve(total);
+        for(auto &g : H.geometries)
+            cat.insert(cat.end(), g.shade[k].begin(), g.shade[k].end());
+        D.shade[k] = dev_upload(sc->allocs, cat.data(), cat.size());
+    }
+    std::vector<F4> lpos;
+    std::vector<AliasEntry8> lalias;
+    lpos.reserve(light_total * 3);
+    lalias.reserve(light_total);
+    for(size_t g = 0; g < H.geometries.size(); ++g)
+    {
+        if(!is_light_geo[g])
+            continue;
+        const HostGeometry &G = H.geometries[g];
+        for(size_t t = 0; t < G.area.size(); ++t)
+        {
+            const V3 a = G.pos[t * 3], ba = G.pos[t * 3 + 1] - a, ca = G.pos[t * 3 + 2] - a;
+            lpos.push_back({ a.x, a.y, a.z, 0 });
+            lpos.push_back({ ba.x, ba.y, ba.z, 0 });
+            lpos.push_back({ ca.x, ca.y, ca.z, 0 });
+        }
+        auto tab = build_alias_table(G.area);
+        lalias.insert(lalias.end(), tab.begin(), tab.end());
+    }
+    D.geometries = dev_upload(sc->allocs, geos.data(), geos.size());
+    D.instances = dev_upload(sc->allocs, H.instances.data(), H.instances.size());
+    D.materials = dev_upload(sc->allocs, H.materials.data(), H.materials.size());
+    D.area_lights = dev_upload(sc->allocs, H.area_lights.data(), H.area_lights.size());
+    D.light_pos = dev_upload(sc->allocs, lpos.data(), lpos.size());
+    D.light_alias = dev_upload(sc->allocs, lalias.data(), lalias.size());
+    D.num_area_lights = static_cast<int32_t>(H.area_lights.size());
+    D.num_lights = D.num_area_lights + (H.env.type != ENV_NONE ? 1 : 0);
+    D.env = H.env;
+
+    // media and density grids
+    std::vector<Medium> meds;
+    std::vector<float> grids;
+    for(auto &m : H.media)
+    {
+        Medium md = m.dev;
+        md.grid_offset = static_cast<int32_t>(grids.size());
+        grids.insert(grids.end(), m.grid.begin(), m.grid.end());
+        meds.push_back(md);
+    }
+    D.media = dev_upload(sc->allocs, meds.data(), meds.size());
+    D.grids = grids.empty() ? nullptr : dev_upload(sc->allocs, grids.data(), grids.size());
+    D.num_media = static_cast<int32_t>(meds.size());
+    D.vacuum_medium = H.vacuum_medium;
+    D.has_media = 0;
+    for(auto &inst : H.instances)
+    {
+        const int inner = static_cast<int>(inst.media & 0xffffu), outer = static_cast<int>(inst.media >> 16);
+        if(H.media[inner].dev.type != MED_VACUUM || H.media[outer].dev.type != MED_VACUUM)
+            D.has_media = 1;
+    }
+    const V3 ext = H.world_max - H.world_min;
+    D.world_diagonal = length(ext);
+
+    // film filter table
+    if(H.params.filter == FILTER_GAUSSIAN)
+    {
+        sc->filter_table_host = build_gaussian_filter_table(H.params.filter_radius, H.params.filter_alpha);
+        sc->filter_table = dev_upload(sc->allocs, sc->filter_table_host.data(), sc->filter_table_host.size());
+    }
+    check_cuda(cudaDeviceSynchronize(), "scene upload");
+    sc->built = true;
+    sc->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void ensure_render_buffers(btrc_ctx *ctx, uint32_t capacity, size_t pixels)
+{
+    if(ctx->buf_capacity >= capacity && ctx->film_pixels == pixels)
+        return;
+    check_cuda(cudaStreamSynchronize(ctx->stream), "stream sync");
+    for(void *p : ctx->buf_allocs)
+        cudaFree(p);
+    ctx->buf_allocs.clear();
+    if(ctx->buf.host_counters)
+        cudaFreeHost(ctx->buf.host_counters);
+    ctx->buf = RenderBuffers{};
+    ctx->buf_capacity = 0;
+    RenderBuffers &B = ctx->buf;
+    auto A = [&](size_t bytes) { return dev_alloc(ctx->buf_allocs, bytes); };
+    for(int k = 0; k < 2; ++k)
+    {
+        B.path[k].beta_depth = static_cast<F4 *>(A(sizeof(F4) * capacity));
+        B.path[k].rad_pixel = static_cast<F4 *>(A(sizeof(F4) * capacity));
+        B.path[k].sampler = static_cast<SamplerState *>(A(sizeof(SamplerState) * capacity));
+        B.path[k].ray_o = static_cast<F4 *>(A(sizeof(F4) * capacity));
+        B.path[k].ray_d = static_cast<F4 *>(A(sizeof(F4) * capacity));
+        B.path[k].bsdf_le = static_cast<F4 *>(A(sizeof(F4) * capacity));
+    }
+    B.shadow.o = static_cast<F4 *>(A(sizeof(F4) * capacity));
+    B.shadow.d = static_cast<F4 *>(A(sizeof(F4) * capacity));
+    B.shadow.beta = static_cast<F4 *>(A(sizeof(F4) * capacity));
+    B.shadow.sampler = static_cast<SamplerState *>(A(sizeof(SamplerState) * capacity));
+    B.hit_flag = static_cast<uint32_t *>(A(sizeof(uint32_t) * capacity));
+    B.hit_detail = static_cast<HitDetail *>(A(sizeof(HitDetail) * capacity));
+    B.film = static_cast<float4 *>(A(sizeof(float4) * pixels));
+    B.counters = static_cast<Counters *>(A(sizeof(Counters)));
+    void *hc = nullptr;
+    check_cuda(cudaMallocHost(&hc, sizeof(Counters) * RING_SLOTS), "cudaMallocHost");
+    B.host_counters = static_cast<Counters *>(hc);
+    B.capacity = capacity;
+    ctx->buf_capacity = capacity;
+    ctx->film_pixels = pixels;
+}
+
+DevRender make_render_params(const btrc_scene *sc, int spp, uint32_t capacity)
+{
+    const HostScene &H = sc->host;
+    DevRender R{};
+    R.width = H.params.width;
+    R.height = H.params.height;
+    R.spp = spp;
+    R.min_depth = H.params.min_depth;
+    R.max_depth = H.params.max_depth;
+    R.rr_threshold = H.params.rr_threshold;
+    R.rr_cont_prob = H.params.rr_cont_prob;
+    R.sampler = H.params.sampler;
+    R.filter = H.params.filter;
+    R.filter_radius = H.params.filter_radius;
+    R.tile = H.params.tile ? 1 : 0;
+    R.capacity = capacity;
+    R.total_paths = static_cast<uint64_t>(spp) * H.params.width * H.params.height;
+    R.halton = halton_consts(H.params.width, H.params.height);
+    R.filter_table = sc->filter_table;
+    R.cam_eye = H.camera.eye;
+    R.cam_lbc = H.camera.lbc;
+    R.cam_fx = H.camera.film_x;
+    R.cam_fy = H.camera.film_y;
+    return R;
+}
+
+cudaStream_t pick_stream(btrc_ctx *ctx, void *stream)
+{
+    return stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+}
+
+void require_built(const btrc_scene *sc)
+{
+    if(!sc || !sc->built)
+        throw StatusError(BTRC_ERR_INVALID_ARG, "scene is not built (call btrc_scene_build)");
+    if(sc->ctx->device < 0)
+        throw StatusError(BTRC_ERR_INVALID_ARG, "host-only context (device -1) cannot run device work");
+}
+
+void require_device(const btrc_ctx *ctx)
+{
+    if(ctx->device < 0)
+        throw StatusError(BTRC_ERR_INVALID_ARG, "host-only context (device -1) cannot run device work");
+}
+
+uint32_t *ctx_scratch_err(btrc_ctx *ctx)
+{
+    if(!ctx->scratch)
+    {
+        check_cuda(cudaMalloc(&ctx->scratch, 256), "cudaMalloc");
+        check_cuda(cudaMemset(ctx->scratch, 0, 256), "cudaMemset");
+        ctx->scratch_bytes = 256;
+    }
+    return static_cast<uint32_t *>(ctx->scratch);
+}
+
+} // namespace
+
+extern "C" {
+
+const char *btrc_version(void) { return "btrc_gb300 0.1.0 (sm_103a)"; }
+
+btrc_status btrc_ctx_create(int device, btrc_ctx **out)
+{
+    if(!out)
+        return BTRC_ERR_INVALID_ARG;
+    *out = nullptr;
+    auto ctx = std::make_unique<btrc_ctx>();
+    btrc_status s = guarded(nullptr, [&] {
+        ctx->device = device;
+        if(device == -1)
+            return;  // host-only context: scene loading and BVH building, no device work
+        int n = 0;
+        check_cuda(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+        if(device < 0 || device >= n)
+            throw StatusError(BTRC_ERR_INVALID_ARG, "device index out of range");
+        ctx->device = device;
+        check_cuda(cudaSetDevice(device), "cudaSetDevice");
+        check_cuda(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        check_cuda(upload_primes(), "prime table upload");
+    });
+    if(s == BTRC_OK)
+        *out = ctx.release();
+    return s;
+}
+
+void btrc_ctx_destroy(btrc_ctx *ctx)
+{
+    if(!ctx)
+        return;
+    if(ctx->device < 0)
+    {
+        delete ctx;
+        return;
+    }
+    cudaSetDevice(ctx->device);
+    if(ctx->stream)
+        cudaStreamSynchronize(ctx->stream);
+    for(void *p : ctx->buf_allocs)
+        cudaFree(p);
+    if(ctx->buf.host_counters)
+        cudaFreeHost(ctx->buf.host_counters);
+    if(ctx->scratch)
+        cudaFree(ctx->scratch);
+    if(ctx->stream)
+        cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char *btrc_last_error(const btrc_ctx *ctx)
+{
+    return ctx ? ctx->last_error.c_str() : "null context";
+}
+
+void btrc_cancel(btrc_ctx *ctx)
+{
+    if(ctx)
+        ctx->cancel.store(true);
+}
+
+btrc_status btrc_scene_load_json(btrc_ctx *ctx, const char *path, btrc_scene **out)
+{
+    if(!ctx || !path || !out)
+        return BTRC_ERR_INVALID_ARG;
+    *out = nullptr;
+    auto sc = std::make_unique<btrc_scene>();
+    sc->ctx = ctx;
+    const btrc_status s = guarded(ctx, [&] { sc->host = load_scene(path); });
+    if(s == BTRC_OK)
+        *out = sc.release();
+    return s;
+}
+
+btrc_status btrc_scene_build(btrc_scene *scene, const btrc_build_opts *opts)
+{
+    if(!scene)
+        return BTRC_ERR_INVALID_ARG;
+    return guarded(scene->ctx, [&] { build_scene(scene, opts ? opts->threads : 0); });
+}
+
+btrc_status btrc_scene_info_get(const btrc_scene *sc, btrc_scene_info *out)
+{
+    if(!sc || !out)
+        return BTRC_ERR_INVALID_ARG;
+    const HostScene &H = sc->host;
+    btrc_scene_info i{};
+    i.width = H.params.width;
+    i.height = H.params.height;
+    i.spp = H.params.spp;
+    i.min_depth = H.params.min_depth;
+    i.max_depth = H.params.max_depth;
+    i.state_count = H.params.state_count;
+    i.sampler = H.params.sampler;
+    i.filter = H.params.filter;
+    i.instances = static_cast<int32_t>(H.instances.size());
+    i.geometries = static_cast<int32_t>(H.geometries.size());
+    i.materials = static_cast<int32_t>(H.materials.size());
+    i.area_lights = static_cast<int32_t>(H.area_lights.size());
+    i.media = static_cast<int32_t>(H.media.size());
+    i.has_envir_light = H.env.type != ENV_NONE ? 1 : 0;
+    i.triangles = H.triangle_count;
+    i.bvh_nodes = sc->bvh_nodes;
+    i.bvh_depth = sc->bvh_depth;
+    i.bvh_bytes = sc->bvh_bytes;
+    i.world_min[0] = H.world_min.x; i.world_min[1] = H.world_min.y; i.world_min[2] = H.world_min.z;
+    i.world_max[0] = H.world_max.x; i.world_max[1] = H.world_max.y; i.world_max[2] = H.world_max.z;
+    i.build_ms = sc->build_ms;
+    *out = i;
+    return BTRC_OK;
+}
+
+void btrc_scene_destroy(btrc_scene *scene)
+{
+    if(!scene)
+        return;
+    if(scene->ctx->device >= 0)
+    {
+        cudaSetDevice(scene->ctx->device);
+        cudaStreamSynchronize(scene->ctx->stream);
+        free_all(scene->allocs);
+    }
+    delete scene;
+}
+
+btrc_status btrc_scene_export_triangles(const btrc_scene *sc, float *xyz, uint32_t *ids, uint64_t capacity)
+{
+    if(!sc)
+        return BTRC_ERR_INVALID_ARG;
+    if(!sc->built)
+        return BTRC_ERR_INVALID_ARG;
+    const uint64_t n = sc->export_ids.size() / 2;
+    if(capacity < n)
+        return BTRC_ERR_INVALID_ARG;
+    if(xyz)
+        std::memcpy(xyz, sc->export_xyz.data(), sizeof(float) * n * 9);
+    if(ids)
+        std::memcpy(ids, sc->export_ids.data(), sizeof(uint32_t) * n * 2);
+    return BTRC_OK;
+}
+
+btrc_status btrc_scene_export_bvh(const btrc_scene *sc, void *nodes, uint64_t node_capacity, void *tris,
+                                  uint64_t tri_capacity)
+{
+    if(!sc || !sc->built)
+        return BTRC_ERR_INVALID_ARG;
+    if(sc->host_nodes.size() != static_cast<size_t>(sc->bvh_nodes))
+        return BTRC_ERR_UNSUPPORTED;
+    if(node_capacity < sc->host_nodes.size() || tri_capacity < sc->host_tris.size())
+        return BTRC_ERR_INVALID_ARG;
+    if(nodes)
+        std::memcpy(nodes, sc->host_nodes.data(), sc->host_nodes.size() * sizeof(CWNode));
+    if(tris)
+        std::memcpy(tris, sc->host_tris.data(), sc->host_tris.size() * sizeof(TriRec));
+    return BTRC_OK;
+}
+
+btrc_status btrc_render(btrc_ctx *ctx, btrc_scene *scene, const btrc_render_opts *opts, float *rgb_out,
+                        btrc_stats *stats)
+{
+    if(!ctx || !scene || !rgb_out)
+        return BTRC_ERR_INVALID_ARG;
+    bool cancelled = false;
+    const btrc_status s = guarded(ctx, [&] {
+        require_built(scene);
+        const auto w0 = std::chrono::steady_clock::now();
+        check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+        ctx->cancel.store(false);
+        const HostScene &H = scene->host;
+        const int spp = opts && opts->spp > 0 ? opts->spp : H.params.spp;
+        const int sc_count = opts && opts->state_count > 0 ? opts->state_count : H.params.state_count;
+        const uint64_t total = static_cast<uint64_t>(spp) * H.params.width * H.params.height;
+        const uint32_t capacity = static_cast<uint32_t>(std::min<uint64_t>(static_cast<uint64_t>(sc_count),
+                                                                            std::max<uint64_t>(total, 1)));
+        const size_t pixels = static_cast<size_t>(H.params.width) * H.params.height;
+        ensure_render_buffers(ctx, capacity, pixels);
+        check_cuda(cudaMemsetAsync(ctx->buf.film, 0, sizeof(float4) * pixels, ctx->stream), "film clear");
+        DevRender R = make_render_params(scene, spp, capacity);
+        ctx->buf.capacity = capacity;
+        RenderStats rs{};
+        const bool graphs = !opts || opts->use_graphs != 0;
+        const int profile = opts ? opts->profile : 0;
+        if(profile < 0 || profile > 2)
+            throw StatusError(BTRC_ERR_INVALID_ARG, "profile must be 0, 1 or 2");
+        check_cuda(render_wavefront(scene->dev, R, ctx->buf, ctx->stream, &ctx->cancel, graphs, profile, &rs,
+                                    &cancelled),
+                   "wavefront render");
+        const bool on_dev = opts && opts->output_on_device;
+        float *rgb_dev = rgb_out;
+        if(!on_dev)
+        {
+            if(ctx->scratch_bytes < pixels * 3 * sizeof(float) + 256)
+            {
+                if(ctx->scratch)
+                    cudaFree(ctx->scratch);
+                ctx->scratch = nullptr;
+                check_cuda(cudaMalloc(&ctx->scratch, pixels * 3 * sizeof(float) + 256), "cudaMalloc");
+                check_cuda(cudaMemset(ctx->scratch, 0, 256), "cudaMemset");
+                ctx->scratch_bytes = pixels * 3 * sizeof(float) + 256;
+            }
+            rgb_dev = reinterpret_cast<float *>(static_cast<char *>(ctx->scratch) + 256);
+        }
+        check_cuda(launch_resolve(ctx->buf.film, rgb_dev, static_cast<uint32_t>(pixels), ctx->stream), "resolve");
+        if(!on_dev)
+            check_cuda(cudaMemcpyAsync(rgb_out, rgb_dev, pixels * 3 * sizeof(float), cudaMemcpyDeviceToHost,
+                                       ctx->stream),
+                       "image download");
+        check_cuda(cudaStreamSynchronize(ctx->stream), "render sync");
+        if(stats)
+        {
+            stats->paths = rs.paths;
+            stats->extension_rays = rs.ext_rays;
+            stats->shadow_rays = rs.shadow_rays;
+            stats->bounces = rs.iterations;
+            stats->traversal_errors = rs.err;
+            stats->device_ms = rs.device_ms;
+            stats->wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
+            stats->kernel_launches = rs.kernel_launches + 1;  // + resolve
+            for(int k = 0; k < 6; ++k)
+            {
+                stats->stage_ms[k] = rs.stage_ms[k];
+                stats->stage_launches[k] = rs.stage_launches[k];
+            }
+            stats->node_visits = rs.node_visits;
+            stats->tri_tests = rs.tri_tests;
+        }
+        if(rs.err)
+            throw StatusError(BTRC_ERR_INTERNAL, "traversal stack overflow reported by the device");
+    });
+    if(s == BTRC_OK && cancelled)
+    {
+        ctx->last_error = "render cancelled";
+        return BTRC_ERR_CANCELLED;
+    }
+    return s;
+}
+
+btrc_status btrc_trace_closest(btrc_ctx *ctx, const btrc_scene *scene, const btrc_ray *d_rays, uint64_t n,
+                               uint32_t *d_flags, btrc_hit *d_hits, void *stream)
+{
+    if(!ctx || !scene || (n > 0 && (!d_rays || !d_flags || !d_hits)) || n > 0xffffffffull)
+        return BTRC_ERR_INVALID_ARG;
+    return guarded(ctx, [&] {
+        require_built(scene);
+        check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+        check_cuda(launch_trace_closest(scene->dev, reinterpret_cast<const Ray *>(d_rays), static_cast<uint32_t>(n),
+                                        d_flags, reinterpret_cast<HitDetail *>(d_hits), ctx_scratch_err(ctx),
+                                        pick_stream(ctx, stream)),
+                   "trace_closest launch");
+    });
+}
+
+btrc_status btrc_trace_any(btrc_ctx *ctx, const btrc_scene *scene, const btrc_ray *d_rays, uint64_t n,
+                           uint32_t *d_occluded, void *stream)
+{
+    if(!ctx || !scene || (n > 0 && (!d_rays || !d_occluded)) || n > 0xffffffffull)
+        return BTRC_ERR_INVALID_ARG;
+    return guarded(ctx, [&] {
+        require_built(scene);
+        check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+        check_cuda(launch_trace_any(scene->dev, reinterpret_cast<const Ray *>(d_rays), static_cast<uint32_t>(n),
+                                    d_occluded, ctx_scratch_err(ctx), pick_stream(ctx, stream)),
+                   "trace_any launch");
+    });
+}
+
+btrc_status btrc_trace_stats(btrc_ctx *ctx, const btrc_scene *scene, const btrc_ray *d_rays, uint64_t n,
+                             uint32_t *d_node_visits, uint32_t *d_tri_tests, void *stream)
+{
+    if(!ctx || !scene || (n > 0 && (!d_rays || !d_node_visits || !d_tri_tests)) || n > 0xffffffffull)
+        return BTRC_ERR_INVALID_ARG;
+    return guarded(ctx, [&] {
+        require_built(scene);
+        check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+        check_cuda(launch_trace_stats(scene->dev, reinterpret_cast<const Ray *>(d_rays), static_cast<uint32_t>(n),
+                                      d_node_visits, d_tri_tests, ctx_scratch_err(ctx), pick_stream(ctx, stream)),
+                   "trace_stats launch");
+    });
+}
+
+btrc_status btrc_sampler_batch(btrc_ctx *ctx, int32_t type, int32_t width, int32_t height, const uint32_t *d_pixel_xy,
+                               const uint32_t *d_sample_index, uint64_t n, uint32_t dims, float *d_out, void *stream)
+{
+    if(!ctx || (type != SAMPLER_INDEPENDENT && type != SAMPLER_HALTON) || width <= 0 || height <= 0 ||
+       n > 0xffffffffull || (n > 0 && (!d_pixel_xy || !d_sample_index || !d_out)))
+        return BTRC_ERR_INVALID_ARG;
+    return guarded(ctx, [&] {
+        require_device(ctx);
+        check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+        check_cuda(launch_sampler_batch(type, width, height, halton_consts(width, height), d_pixel_xy, d_sample_index,
+                                        static_cast<uint32_t>(n), dims, d_out, pick_stream(ctx, stream)),
+                   "sampler batch");
+    });
+}
+
+btrc_status btrc_bsdf_batch(btrc_ctx *ctx, int32_t op, const float *d_material, const float *d_wo,
+                            const float *d_wi_or_u, uint64_t n, float *d_out, void *stream)
+{
+    if(!ctx || (op != 0 && op != 1) || n > 0xffffffffull || (n > 0 && (!d_material || !d_wo || !d_wi_or_u || !d_out)))
+        return BTRC_ERR_INVALID_ARG;
+    return guarded(ctx, [&] {
+        require_device(ctx);
+        check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+        // convert the 16-float records into Material structs on the device
+        std::vector<void *> tmp;
+        Material *mats = nullptr;
+        if(n > 0)
+        {
+            std::vector<float> hrec(n * 16);
+            check_cuda(cudaMemcpy(hrec.data(), d_material, sizeof(float) * n * 16, cudaMemcpyDeviceToHost),
+                       "material download");
+            std::vector<Material> hm(n);
+            for(uint64_t i = 0; i < n; ++i)
+            {
+                Material m{};
+                m.type = static_cast<int32_t>(hrec[i * 16 + 15]);
+                if(m.type != MAT_DIFFUSE && m.type != MAT_METAL && m.type != MAT_DISNEY)
+                    throw StatusError(BTRC_ERR_INVALID_ARG, "bsdf batch supports diffuse, metal and disney");
+                m.shadow_terminator = 0;
+                for(int k = 0; k < 15; ++k)
+                    m.p[k] = hrec[i * 16 + k];
+                hm[i] = m;
+            }
+            mats = dev_upload(tmp, hm.data(), hm.size());
+        }
+        cudaError_t e = launch_bsdf_batch(op, mats, d_wo, d_wi_or_u, static_cast<uint32_t>(n), d_out,
+                                          pick_stream(ctx, stream));
+        if(e == cudaSuccess)
+            e = cudaStreamSynchronize(pick_stream(ctx, stream));
+        free_all(tmp);
+        check_cuda(e, "bsdf batch");
+    });
+}
+
+btrc_status btrc_medium_tr_batch(btrc_ctx *ctx, const btrc_scene *scene, int32_t medium_id, const float *d_seg,
+                                 const uint64_t *d_seeds, uint64_t n, float *d_out, void *stream)
+{
+    if(!ctx || !scene || n > 0xffffffffull || (n > 0 && (!d_seg || !d_seeds || !d_out)))
+        return BTRC_ERR_INVALID_ARG;
+    return guarded(ctx, [&] {
+        require_built(scene);
+        if(medium_id < 0 || medium_id >= scene->dev.num_media)
+            throw StatusError(BTRC_ERR_INVALID_ARG, "medium id out of range");
+        check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+        check_cuda(launch_medium_tr_batch(scene->dev, medium_id, d_seg, d_seeds, static_cast<uint32_t>(n), d_out,
+                                          pick_stream(ctx, stream)),
+                   "medium tr batch");
+    });
+}
+
+} // extern "C"

@@ -1,0 +1,91 @@
+// Device-resident scene and per-render parameters (plain pointers into HBM).
+#pragma once
+
+#include <cstdint>
+
+#include "layout.h"
+#include "sampler.cuh"
+
+namespace bt {
+
+struct DevScene
+{
+    const F4 *nodes;          // CWNode array viewed as float4 (5 per node)
+    const F4 *tris;           // TriRec array viewed as float4 (3 per triangle)
+    uint32_t node_count;
+    uint32_t tri_count;
+
+    const F4 *shade[6];       // per-geometry shading SoA, concatenated over geometries
+    const Geometry *geometries;
+    const Instance *instances;
+    const Material *materials;
+    const AreaLight *area_lights;
+    const F4 *light_pos;      // a, b-a, c-a per triangle of light geometries (local space)
+    const AliasEntry8 *light_alias;
+    int32_t num_area_lights;
+    int32_t num_lights;       // area lights + environment (if any)
+    EnvLight env;
+
+    const Medium *media;
+    const float *grids;
+    int32_t num_media;
+    int32_t vacuum_medium;
+    int32_t has_media;        // any non-vacuum medium referenced by an instance
+    float world_diagonal;
+};
+
+struct DevRender
+{
+    int32_t width, height, spp;
+    int32_t min_depth, max_depth;
+    float rr_threshold, rr_cont_prob;
+    int32_t sampler;
+    int32_t filter;
+    float filter_radius;
+    int32_t tile;
+    uint32_t capacity;
+    uint64_t total_paths;
+    HaltonConsts halton;
+    const AliasEntry8 *filter_table;
+    V3 cam_eye, cam_lbc, cam_fx, cam_fy;
+};
+
+// Queue counters, resident in device memory for the whole render.
+struct Counters
+{
+    uint32_t active;       // states in the current queue (survivors + new)
+    uint32_t slot_base;    // first slot written by generate this iteration
+    uint32_t n_new;        // paths generated this iteration
+    uint32_t next_active;  // survivors appended by shade/medium
+    uint32_t shadow;       // shadow records appended this iteration
+    uint32_t err;          // traversal stack overflow flag
+    uint32_t iterations;
+    uint32_t pad;
+    uint64_t generated;    // total camera paths generated
+    uint64_t gen_base;     // global path index of slot_base
+    uint64_t ext_rays;     // extension rays traced
+    uint64_t shadow_rays;  // shadow rays traced
+    uint64_t node_visits;  // closest-hit node visits (counting mode only)
+    uint64_t tri_tests;    // closest-hit triangle tests (counting mode only)
+};
+
+// Structure-of-arrays path state. Two copies (current / next) per render.
+struct PathSoA
+{
+    F4 *beta_depth;    // beta.xyz, depth (int bits)
+    F4 *rad_pixel;     // path radiance.xyz, pixel (x | y << 16)
+    SamplerState *sampler;
+    F4 *ray_o;         // o.xyz, medium id (bits)
+    F4 *ray_d;         // d.xyz, t1
+    F4 *bsdf_le;       // beta_le.xyz, bsdf pdf (negative: delta)
+};
+
+struct ShadowSoA
+{
+    F4 *o;             // o.xyz, pixel (bits)
+    F4 *d;             // d.xyz, t1
+    F4 *beta;          // beta_li.xyz, medium id (bits)
+    SamplerState *sampler;
+};
+
+} // namespace bt

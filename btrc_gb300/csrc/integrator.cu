@@ -1,0 +1,1208 @@
+// Wavefront path tracer: per-bounce stage kernels over SoA path queues.
+// Stage order per bounce follows WavefrontPathTracer::render
+// (builtin/btrc/builtin/renderer/wavefront.cpp:205-325): generate -> trace -> [medium]
+// -> shade -> shadow. Differences that are GB300-specific:
+//   * queue counters stay in device memory; a one-thread control kernel advances them,
+//     so there is no blocking device-to-host copy per bounce (the reference reads the
+//     counters back every bounce, wavefront.cpp:284);
+//   * the queue is topped up with new camera paths every bounce (the reference refills
+//     only when half empty, generate.cpp:148-156); the estimator is unchanged;
+//   * queue appends are warp-aggregated (one atomic per warp instead of per thread);
+//   * two bounces (ping and pong buffers) are captured into one CUDA graph and relaunched.
+#include <algorithm>
+#include <cstdio>
+#include <vector>
+
+#include "bsdf.cuh"
+#include "kernels.h"
+#include "traverse.cuh"
+
+namespace bt {
+
+__constant__ uint32_t c_primes[PRIME_COUNT];
+
+namespace {
+
+constexpr int BLOCK = 256;
+constexpr uint32_t MAX_TRACKING_STEPS = 1u << 20;
+
+// ---------------------------------------------------------------- small helpers
+
+__device__ __forceinline__ V3 v3(const F4 &f) { return V3(f.x, f.y, f.z); }
+__device__ __forceinline__ F4 f4(V3 v, float w) { return F4{ v.x, v.y, v.z, w }; }
+__device__ __forceinline__ F4 ldf4(const F4 *p) { const float4 v = __ldg(reinterpret_cast<const float4 *>(p)); return F4{ v.x, v.y, v.z, v.w }; }
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+
+// warp-aggregated queue append: one atomic per converged group of callers
+__device__ __forceinline__ uint32_t queue_append(uint32_t *counter)
+{
+    const uint32_t mask = __activemask();
+    const uint32_t leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if(lane_id() == leader)
+        base = atomicAdd(counter, static_cast<uint32_t>(__popc(mask)));
+    base = __shfl_sync(mask, base, leader);
+    return base + __popc(mask & ((1u << lane_id()) - 1u));
+}
+
+// Film::splat_atomic (core/btrc/core/film.cpp:131-165): non-finite values are dropped
+__device__ __forceinline__ void splat(float4 *film, uint32_t pixel, int width, V3 v)
+{
+    if(!all_finite(v))
+        return;
+    const uint32_t x = pixel & 0xffffu, y = pixel >> 16;
+    atomicAdd(film + (static_cast<size_t>(y) * width + x), make_float4(v.x, v.y, v.z, 0.0f));
+}
+
+// intersection_offset (common/btrc/utils/intersection.cpp:5-37)
+__device__ __forceinline__ V3 offset_point(V3 pos, V3 nor)
+{
+    const float ORIGIN = 1.0f / 32.0f, FLOAT_SCALE = 1.0f / 65536.0f, INT_SCALE = 256.0f;
+    const int ox = static_cast<int>(2 * INT_SCALE * nor.x);
+    const int oy = static_cast<int>(2 * INT_SCALE * nor.y);
+    const int oz = static_cast<int>(2 * INT_SCALE * nor.z);
+    const float px = __int_as_float(__float_as_int(pos.x) + (pos.x < 0 ? -ox : ox));
+    const float py = __int_as_float(__float_as_int(pos.y) + (pos.y < 0 ? -oy : oy));
+    const float pz = __int_as_float(__float_as_int(pos.z) + (pos.z < 0 ? -oz : oz));
+    return V3(fabsf(pos.x) < ORIGIN ? pos.x + FLOAT_SCALE * nor.x : px,
+              fabsf(pos.y) < ORIGIN ? pos.y + FLOAT_SCALE * nor.y : py,
+              fabsf(pos.z) < ORIGIN ? pos.z + FLOAT_SCALE * nor.z : pz);
+}
+
+__device__ __forceinline__ V3 offset_dir(V3 pos, V3 nor, V3 dir)
+{
+    return offset_point(pos, dot(nor, dir) > 0 ? nor : -nor);
+}
+
+__device__ __forceinline__ V3 aff_point(const float *m, V3 p)
+{
+    return V3(m[0] * p.x + m[1] * p.y + m[2] * p.z + m[3], m[4] * p.x + m[5] * p.y + m[6] * p.z + m[7],
+              m[8] * p.x + m[9] * p.y + m[10] * p.z + m[11]);
+}
+__device__ __forceinline__ V3 aff_vector(const float *m, V3 v)
+{
+    return V3(m[0] * v.x + m[1] * v.y + m[2] * v.z, m[4] * v.x + m[5] * v.y + m[6] * v.z,
+              m[8] * v.x + m[9] * v.y + m[10] * v.z);
+}
+// normal transform from the inverse matrix (core ctransform.cpp apply_to_normal)
+__device__ __forceinline__ V3 aff_normal(const float *inv, V3 n)
+{
+    return V3(inv[0] * n.x + inv[4] * n.y + inv[8] * n.z, inv[1] * n.x + inv[5] * n.y + inv[9] * n.z,
+              inv[2] * n.x + inv[6] * n.y + inv[10] * n.z);
+}
+
+// ---------------------------------------------------------------- sampler
+
+struct DSampler
+{
+    SamplerState s;
+    int type;
+
+    __device__ __forceinline__ float halton(uint32_t dim) const
+    {
+        return owen_scrambled_radical_inverse(c_primes[dim], s.a, mix_bits(static_cast<uint64_t>(1u + (dim << 4))));
+    }
+    __device__ __forceinline__ float get1d()
+    {
+        if(type == SAMPLER_INDEPENDENT)
+            return pcg32_uniform(s.a, s.b);
+        uint32_t dim = static_cast<uint32_t>(s.b);
+        if(dim >= PRIME_COUNT)
+            dim = 2;
+        const float v = halton(dim);
+        s.b = dim + 1;
+        return v;
+    }
+    __device__ __forceinline__ void get2d(float &x, float &y)
+    {
+        if(type == SAMPLER_INDEPENDENT)
+        {
+            x = pcg32_uniform(s.a, s.b);
+            y = pcg32_uniform(s.a, s.b);
+            return;
+        }
+        uint32_t dim = static_cast<uint32_t>(s.b);
+        if(dim + 1 >= PRIME_COUNT)
+            dim = 2;
+        x = halton(dim);
+        y = halton(dim + 1);
+        s.b = dim + 2;
+    }
+    __device__ __forceinline__ void get3d(float &x, float &y, float &z)
+    {
+        if(type == SAMPLER_INDEPENDENT)
+        {
+            x = pcg32_uniform(s.a, s.b);
+            y = pcg32_uniform(s.a, s.b);
+            z = pcg32_uniform(s.a, s.b);
+            return;
+        }
+        uint32_t dim = static_cast<uint32_t>(s.b);
+        if(dim + 2 >= PRIME_COUNT)
+            dim = 2;
+        x = halton(dim);
+        y = halton(dim + 1);
+        z = halton(dim + 2);
+        s.b = dim + 3;
+    }
+};
+
+__device__ __forceinline__ SamplerState sampler_init(int type, const HaltonConsts &hc, uint32_t px, uint32_t py,
+                                                     uint32_t sample_index)
+{
+    SamplerState st;
+    if(type == SAMPLER_INDEPENDENT)
+    {
+        pcg32_seed(st.a, st.b, murmur64a_2x32(px, py), PCG_STREAM);
+        pcg32_advance(st.a, st.b, static_cast<uint64_t>(sample_index) * 65536u);
+        return st;
+    }
+    uint64_t index = 0;
+    if(hc.stride > 1)
+    {
+        const uint32_t pm[2] = { px % HALTON_MAX_RES, py % HALTON_MAX_RES };
+        for(int i = 0; i < 2; ++i)
+        {
+            const uint64_t off = inverse_radical_inverse(pm[i], i == 0 ? 2u : 3u, hc.exponent[i]);
+            index += off * static_cast<uint64_t>((hc.stride / hc.scale[i]) * hc.mult_inverse[i]);
+        }
+        index %= static_cast<uint64_t>(hc.stride);
+    }
+    index += static_cast<uint64_t>(sample_index) * static_cast<uint64_t>(hc.stride);
+    st.a = index;
+    st.b = 2;
+    return st;
+}
+
+// ---------------------------------------------------------------- geometry helpers
+
+struct SurfacePoint
+{
+    V3 position;
+    Frame frame;
+    V3 interp_z;
+};
+
+// get_hitinfo (core/btrc/core/scene.cpp:9-64)
+__device__ SurfacePoint get_hitinfo(const DevScene &S, V3 o, V3 d, const Instance &inst, uint32_t idx, float t,
+                                    float b1, float b2)
+{
+    SurfacePoint sp;
+    sp.position = o + t * d;
+    const F4 gx = ldf4(S.shade[0] + idx), gy = ldf4(S.shade[1] + idx), gz = ldf4(S.shade[2] + idx);
+    const F4 sa = ldf4(S.shade[3] + idx), sba = ldf4(S.shade[4] + idx), sca = ldf4(S.shade[5] + idx);
+    Frame f(v3(gx), v3(gy), v3(gz));
+    f.x = normalize(aff_vector(inst.l2w, f.x));
+    f.y = normalize(aff_vector(inst.l2w, f.y));
+    f.z = normalize(aff_normal(inst.w2l, f.z));
+    sp.frame = f;
+    const V3 in = v3(sa) + v3(sba) * b1 + v3(sca) * b2;
+    sp.interp_z = normalize(aff_normal(inst.w2l, in));
+    return sp;
+}
+
+// ---------------------------------------------------------------- lights
+
+__device__ __forceinline__ uint32_t alias_sample(const AliasEntry8 *table, uint32_t n, float u)
+{
+    const float nu = static_cast<float>(n) * u;
+    const uint32_t i = min(static_cast<uint32_t>(nu), n - 1);
+    const float s = nu - static_cast<float>(i);
+    const AliasEntry8 e = table[i];
+    return s <= e.accept ? i : e.alias;
+}
+
+__device__ __forceinline__ V3 env_le(const EnvLight &env, V3 to_light)
+{
+    const V3 up(env.up[0], env.up[1], env.up[2]);
+    const float c = dot(up, normalize(to_light));
+    const float s = saturate(0.5f * (c + 1.0f));
+    return V3(env.lower[0], env.lower[1], env.lower[2]) * (1.0f - s) + V3(env.upper[0], env.upper[1], env.upper[2]) * s;
+}
+
+struct LightSample
+{
+    bool success;
+    V3 o, d;
+    float t1, light_pdf;
+    V3 li;
+};
+
+// sample_light_li_impl (builtin/.../wavefront/helper.cpp:9-61); offset_origin selects the
+// surface form (origin offset along the normal) or the medium form (origin = ref_pos)
+__device__ LightSample sample_light(const DevScene &S, V3 ref_pos, V3 ref_nor, bool offset_origin, DSampler &smp)
+{
+    LightSample r;
+    float s0, s1, s2;
+    smp.get3d(s0, s1, s2);
+    const float sel = smp.get1d();
+    r.success = false;
+    if(S.num_lights == 0)
+        return r;
+    const int idx = min(static_cast<int>(sel * static_cast<float>(S.num_lights)), S.num_lights - 1);
+    const float select_pdf = 1.0f / static_cast<float>(S.num_lights);
+    if(idx < S.num_area_lights)
+    {
+        // MeshLight::sample_li_inline (builtin/btrc/builtin/light/mesh_light.cpp:31-58)
+        const AreaLight L = S.area_lights[idx];
+        const Geometry g = S.geometries[L.geometry];
+        const Instance &inst = S.instances[L.instance];
+        const uint32_t base = __float_as_uint(g.pad);
+        const uint32_t prim = alias_sample(S.light_alias + base, g.tri_count, s0);
+        const float tq = sqrtf(s1);
+        const float u = 1.0f - tq, v = tq * s2;
+        const V3 a = v3(S.light_pos[(base + prim) * 3 + 0]);
+        const V3 ba = v3(S.light_pos[(base + prim) * 3 + 1]);
+        const V3 ca = v3(S.light_pos[(base + prim) * 3 + 2]);
+        const V3 pos = a + ba * u + ca * v;
+        const V3 ez = normalize(v3(ldf4(S.shade[2] + g.tri_offset + prim)));
+        const V3 spos = aff_point(inst.l2w, pos);
+        const V3 snor = normalize(aff_normal(inst.w2l, ez));
+        const V3 pos_to_ref = ref_pos - spos;
+        const float dist2 = length_square(pos_to_ref);
+        const float pdf_sa = 1.0f / (L.scale * L.scale) * (1.0f / g.total_area) * dist2 /
+                             fabsf(dot(snor, normalize(pos_to_ref)));
+        const V3 rad = dot(pos_to_ref, snor) > 0 ? V3(L.intensity[0], L.intensity[1], L.intensity[2]) : V3(0);
+        const V3 diff = spos - ref_pos;
+        const V3 dst = offset_dir(spos, snor, -diff);
+        r.o = offset_origin ? offset_dir(ref_pos, ref_nor, diff) : ref_pos;
+        r.d = dst - r.o;
+        r.t1 = 1.0f;
+        r.li = rad;
+        r.light_pdf = select_pdf * pdf_sa;
+    }
+    else
+    {
+        // GradientSky::sample_li_inline (builtin/btrc/builtin/light/gradient_sky.cpp:28-35)
+        const V3 dir = sample_sphere_uniform(s0, s1);
+        r.o = offset_origin ? offset_dir(ref_pos, ref_nor, dir) : ref_pos;
+        r.d = dir;
+        r.t1 = MAX_FLOAT;
+        r.li = env_le(S.env, dir);
+        r.light_pdf = select_pdf * (1.0f / (4.0f * PI));
+    }
+    r.success = true;
+    return r;
+}
+
+// eval_miss_le (helper.cpp:144-172)
+__device__ __forceinline__ V3 miss_le(const DevScene &S, V3 d, V3 beta_le, float bsdf_pdf)
+{
+    if(S.env.type == ENV_NONE)
+        return V3(0);
+    const V3 le = env_le(S.env, d);
+    if(bsdf_pdf < 0)
+        return beta_le * le / -bsdf_pdf;
+    const float light_pdf = (1.0f / static_cast<float>(S.num_lights)) * (1.0f / (4.0f * PI));
+    return beta_le * le / (bsdf_pdf + light_pdf);
+}
+
+// handle_intersected_light (helper.cpp:174-207) with MeshLight::eval_le / pdf_li
+__device__ __forceinline__ V3 hit_light_le(const DevScene &S, V3 o, V3 d, const SurfacePoint &sp, V3 beta_le,
+                                           float bsdf_pdf, int light)
+{
+    if(light < 0)
+        return V3(0);
+    const AreaLight L = S.area_lights[light];
+    const V3 le = dot(sp.frame.z, -d) >= 0 ? V3(L.intensity[0], L.intensity[1], L.intensity[2]) : V3(0);
+    if(bsdf_pdf < 0)
+        return beta_le * le / -bsdf_pdf;
+    float pdf_li = 0;
+    const V3 to_ref = o - sp.position;
+    if(dot(sp.frame.z, to_ref) > 0)
+    {
+        const float total_area = S.geometries[L.geometry].total_area;
+        const float dist2 = length_square(to_ref);
+        const float dist3 = sqrtf(dist2) * dist2;
+        pdf_li = 1.0f / (L.scale * L.scale) * (1.0f / total_area) * dist3 / fabsf(dot(sp.frame.z, to_ref));
+    }
+    const float light_pdf = (1.0f / static_cast<float>(S.num_lights)) * pdf_li;
+    return beta_le * le / (bsdf_pdf + light_pdf);
+}
+
+// simple_russian_roulette (helper.cpp:67-97); returns true when the path ends
+__device__ __forceinline__ bool russian_roulette(V3 &beta, int depth, DSampler &smp, const DevRender &R)
+{
+    if(depth < R.min_depth)
+        return false;
+    if(depth >= R.max_depth)
+        return true;
+    const float sam = smp.get1d();
+    if(luminance(beta) < R.rr_threshold)
+    {
+        if(sam > R.rr_cont_prob)
+            return true;
+        beta = beta / R.rr_cont_prob;
+    }
+    return false;
+}
+
+// ---------------------------------------------------------------- media
+
+// software trilinear lookup, normalised coordinates, clamp addressing
+__device__ __forceinline__ float grid_lookup(const float *grid, const Medium &m, V3 uvw)
+{
+    const float fx = uvw.x * m.res_x - 0.5f, fy = uvw.y * m.res_y - 0.5f, fz = uvw.z * m.res_z - 0.5f;
+    const float flx = floorf(fx), fly = floorf(fy), flz = floorf(fz);
+    const float tx = fx - flx, ty = fy - fly, tz = fz - flz;
+    const int x0 = static_cast<int>(flx), y0 = static_cast<int>(fly), z0 = static_cast<int>(flz);
+    const int xa = min(max(x0, 0), m.res_x - 1), xb = min(max(x0 + 1, 0), m.res_x - 1);
+    const int ya = min(max(y0, 0), m.res_y - 1), yb = min(max(y0 + 1, 0), m.res_y - 1);
+    const int za = min(max(z0, 0), m.res_z - 1), zb = min(max(z0 + 1, 0), m.res_z - 1);
+    const float *g = grid + m.grid_offset;
+    const size_t sx = 1, sy = static_cast<size_t>(m.res_x), sz = static_cast<size_t>(m.res_x) * m.res_y;
+    const float c000 = __ldg(g + za * sz + ya * sy + xa * sx), c100 = __ldg(g + za * sz + ya * sy + xb * sx);
+    const float c010 = __ldg(g + za * sz + yb * sy + xa * sx), c110 = __ldg(g + za * sz + yb * sy + xb * sx);
+    const float c001 = __ldg(g + zb * sz + ya * sy + xa * sx), c101 = __ldg(g + zb * sz + ya * sy + xb * sx);
+    const float c011 = __ldg(g + zb * sz + yb * sy + xa * sx), c111 = __ldg(g + zb * sz + yb * sy + xb * sx);
+    const float c00 = c000 + (c100 - c000) * tx, c10 = c010 + (c110 - c010) * tx;
+    const float c01 = c001 + (c101 - c001) * tx, c11 = c011 + (c111 - c011) * tx;
+    const float c0 = c00 + (c10 - c00) * ty, c1 = c01 + (c11 - c01) * ty;
+    return c0 + (c1 - c0) * tz;
+}
+
+struct MediumSample
+{
+    bool scattered;
+    V3 position;
+};
+
+// HetergeneousMedium::sample (builtin/btrc/builtin/medium/hetergeneous.cpp:25-73) and the
+// homogeneous variant; TransformMedium maps a, b to the medium's local frame first
+// (core/btrc/core/medium.cpp:98-129)
+__device__ MediumSample medium_sample(const DevScene &S, const Medium &m, V3 a, V3 b, DSampler &smp)
+{
+    MediumSample r;
+    r.scattered = false;
+    if(m.type == MED_VACUUM)
+        return r;
+    const float t_max = length(b - a);
+    if(m.type == MED_HOMOGENEOUS)
+    {
+        const float st = -logf(1.0f - smp.get1d()) / m.sigma_t_const;
+        if(st < t_max)
+        {
+            r.scattered = true;
+            r.position = a + normalize(b - a) * st;
+        }
+        return r;
+    }
+    const float inv_max = 1.0f / m.sigma_max;
+    const V3 la = V3(0.5f) + 0.5f * aff_point(m.w2l, a);
+    const V3 lb = V3(0.5f) + 0.5f * aff_point(m.w2l, b);
+    const V3 lstep = (lb - la) / t_max;
+    const V3 wstep = (b - a) / t_max;
+    float t = 0.0f;
+    for(uint32_t it = 0; it < MAX_TRACKING_STEPS; ++it)
+    {
+        t += -logf(1.0f - smp.get1d()) * inv_max;
+        if(t >= t_max)
+            break;
+        const V3 uvw = la + t * lstep;
+        const float density = grid_lookup(S.grids, m, uvw);
+        if(smp.get1d() < density * inv_max)
+        {
+            r.scattered = true;
+            r.position = a + t * wstep;
+            break;
+        }
+    }
+    return r;
+}
+
+// ratio-tracking transmittance (hetergeneous.cpp:75-106); homogeneous is analytic
+__device__ V3 medium_tr(const DevScene &S, const Medium &m, V3 a, V3 b, DSampler &smp)
+{
+    if(m.type == MED_VACUUM)
+        return V3(1.0f);
+    const float t_max = length(b - a);
+    if(m.type == MED_HOMOGENEOUS)
+    {
+        // the reference attenuates by absorption only (homogeneous.cpp:49-62)
+        const V3 sigma_a = m.sigma_t_const * (V3(1.0f) - V3(m.albedo[0], m.albedo[1], m.albedo[2]));
+        const V3 e = -t_max * sigma_a;
+        return V3(expf(e.x), expf(e.y), expf(e.z));
+    }
+    const float inv_max = 1.0f / m.sigma_max;
+    const V3 la = V3(0.5f) + 0.5f * aff_point(m.w2l, a);
+    const V3 lb = V3(0.5f) + 0.5f * aff_point(m.w2l, b);
+    const V3 lstep = (lb - la) / t_max;
+    float result = 1.0f, t = 0.0f;
+    for(uint32_t it = 0; it < MAX_TRACKING_STEPS; ++it)
+    {
+        t += -logf(1.0f - smp.get1d()) * inv_max;
+        if(t >= t_max)
+            break;
+        const V3 uvw = la + t * lstep;
+        result *= 1.0f - grid_lookup(S.grids, m, uvw) * inv_max;
+    }
+    return V3(result);
+}
+
+__device__ __forceinline__ float henyey_greenstein(float g, float u)
+{
+    const float g2 = g * g;
+    const float dem = 1.0f + g2 - 2.0f * (g * u);
+    return (1.0f - g2) / (4.0f * PI * dem * sqrtf(dem));
+}
+
+// ---------------------------------------------------------------- kernels
+
+__global__ void k_control(Counters *c, uint32_t capacity, uint64_t total)
+{
+    Counters k = *c;
+    k.shadow_rays += k.shadow;
+    const uint32_t survivors = k.next_active;
+    const uint64_t remaining = total - k.generated;
+    const uint64_t room = capacity - survivors;
+    const uint32_t n_new = static_cast<uint32_t>(remaining < room ? remaining : room);
+    k.slot_base = survivors;
+    k.n_new = n_new;
+    k.gen_base = k.generated;
+    k.generated += n_new;
+    k.active = survivors + n_new;
+    k.ext_rays += k.active;
+    k.next_active = 0;
+    k.shadow = 0;
+    if(k.active > 0)
+        ++k.iterations;
+    *c = k;
+}
+
+__global__ void __launch_bounds__(BLOCK) k_generate(DevRender R, PathSoA P, float4 *film, const Counters *cnt,
+                                                    int vacuum_medium)
+{
+    const uint32_t n = cnt->n_new;
+    const uint32_t slot_base = cnt->slot_base;
+    const uint64_t gen_base = cnt->gen_base;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint64_t pixel_count = static_cast<uint64_t>(R.width) * R.height;
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    {
+        const uint64_t g = gen_base + i;
+        uint64_t pixel, sample;
+        if(!R.tile)
+        {
+            pixel = g % pixel_count;
+            sample = g / pixel_count;
+        }
+        else
+        {
+            pixel = g / R.spp;
+            sample = g % R.spp;
+        }
+        const uint32_t px = static_cast<uint32_t>(pixel % R.width);
+        const uint32_t py = static_cast<uint32_t>(pixel / R.width);
+        DSampler smp;
+        smp.type = R.sampler;
+        smp.s = sampler_init(R.sampler, R.halton, px, py, static_cast<uint32_t>(sample));
+        float fx, fy;
+        if(R.filter == FILTER_GAUSSIAN)
+        {
+            // GaussianFilter::sample (builtin/btrc/builtin/film_filter/gaussian.cpp:54-66)
+            const uint32_t cell = alias_sample(R.filter_table, FILTER_GRID * FILTER_GRID, smp.get1d());
+            const uint32_t gy = cell / FILTER_GRID, gx = cell % FILTER_GRID;
+            const float r = R.filter_radius, w = 2 * r / FILTER_GRID;
+            const float x0 = -r + w * static_cast<float>(gx), x1 = -r + w * static_cast<float>(gx + 1);
+            const float y0 = -r + w * static_cast<float>(gy), y1 = -r + w * static_cast<float>(gy + 1);
+            fx = lerpf(x0, x1, smp.get1d());
+            fy = lerpf(y0, y1, smp.get1d());
+        }
+        else
+        {
+            fx = smp.get1d() - 0.5f;
+            fy = smp.get1d() - 0.5f;
+        }
+        const float film_x = (static_cast<float>(px) + 0.5f + fx) / static_cast<float>(R.width);
+        const float film_y = (static_cast<float>(py) + 0.5f + fy) / static_cast<float>(R.height);
+        (void)smp.get1d();  // time sample
+        // PinholeCamera::generate_ray_inline (builtin/btrc/builtin/camera/pinhole.cpp:84-99)
+        const V3 dst = R.cam_lbc + film_x * R.cam_fx + film_y * R.cam_fy;
+        const V3 dir = normalize(dst - R.cam_eye);
+        const uint32_t pix = px | (py << 16);
+        atomicAdd(&film[static_cast<size_t>(py) * R.width + px].w, 1.0f);
+        const uint32_t s = slot_base + i;
+        P.beta_depth[s] = F4{ 1.0f, 1.0f, 1.0f, __int_as_float(0) };
+        P.rad_pixel[s] = F4{ 0.0f, 0.0f, 0.0f, __uint_as_float(pix) };
+        P.sampler[s] = smp.s;
+        P.ray_o[s] = F4{ R.cam_eye.x, R.cam_eye.y, R.cam_eye.z, __int_as_float(vacuum_medium) };
+        P.ray_d[s] = F4{ dir.x, dir.y, dir.z, MAX_FLOAT };
+        P.bsdf_le[s] = F4{ 1.0f, 1.0f, 1.0f, -1.0f };
+    }
+}
+
+template<bool COUNT>
+__global__ void __launch_bounds__(128) k_trace(DevScene S, PathSoA P, uint32_t *flags, HitDetail *hits,
+                                               Counters *cnt)
+{
+    const uint32_t n = cnt->active;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    uint64_t nv = 0, tv = 0;
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    {
+        const F4 o = P.ray_o[i], d = P.ray_d[i];
+        const TravRay tr = make_trav_ray(o.x, o.y, o.z, d.x, d.y, d.z);
+        uint32_t a = 0, b = 0;
+        const ClosestResult c = trace_closest(tr, d.w, reinterpret_cast<const float4 *>(S.nodes),
+                                              reinterpret_cast<const float4 *>(S.tris), S.node_count, &cnt->err,
+                                              COUNT ? &a : nullptr, COUNT ? &b : nullptr);
+        nv += a;
+        tv += b;
+        flags[i] = c.hit ? (c.inst | HIT_BIT) : 0u;
+        hits[i] = HitDetail{ c.t, c.prim, c.b1, c.b2 };
+    }
+    if(COUNT)
+    {
+        for(int off = 16; off > 0; off >>= 1)
+        {
+            nv += __shfl_down_sync(0xffffffffu, nv, off);
+            tv += __shfl_down_sync(0xffffffffu, tv, off);
+        }
+        if(lane_id() == 0)
+        {
+            atomicAdd(reinterpret_cast<unsigned long long *>(&cnt->node_visits), static_cast<unsigned long long>(nv));
+            atomicAdd(reinterpret_cast<unsigned long long *>(&cnt->tri_tests), static_cast<unsigned long long>(tv));
+        }
+    }
+}
+
+// MediumPipeline (builtin/btrc/builtin/renderer/wavefront/medium.cpp:28-249)
+__global__ void __launch_bounds__(BLOCK) k_medium(DevScene S, DevRender R, PathSoA P, PathSoA N, ShadowSoA SH,
+                                                  uint32_t *flags, const HitDetail *hits, float4 *film, Counters *cnt)
+{
+    const uint32_t n = cnt->active;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    {
+        const uint32_t flag = flags[i];
+        const F4 ro = P.ray_o[i], rd = P.ray_d[i];
+        const V3 o = v3(ro), d = v3(rd);
+        const int ray_medium = __float_as_int(ro.w);
+        int medium_id;
+        V3 end;
+        if(flag & HIT_BIT)
+        {
+            const HitDetail h = hits[i];
+            const Instance &inst = S.instances[flag & INST_MASK];
+            const Geometry g = S.geometries[inst.geometry];
+            const V3 ln = v3(ldf4(S.shade[2] + g.tri_offset + h.prim));
+            const V3 nor = aff_normal(inst.w2l, ln);
+            const int inner = static_cast<int>(inst.media & 0xffffu), outer = static_cast<int>(inst.media >> 16);
+            const int inct_medium = dot(d, nor) < 0 ? outer : inner;
+            medium_id = min(inct_medium, ray_medium);
+            end = offset_dir(o + h.t * d, nor, -d);
+        }
+        else
+        {
+            medium_id = S.vacuum_medium;
+            end = o + normalize(d) * S.world_diagonal;
+        }
+        P.ray_o[i].w = __int_as_float(medium_id);
+        const Medium &m = S.media[medium_id];
+        if(m.type == MED_VACUUM)
+            continue;
+
+        DSampler smp;
+        smp.type = R.sampler;
+        smp.s = P.sampler[i];
+        const MediumSample ms = medium_sample(S, m, o, end, smp);
+        const V3 tr = medium_tr(S, m, o, end, smp);
+        F4 ble = P.bsdf_le[i];
+        ble.x *= tr.x;
+        ble.y *= tr.y;
+        ble.z *= tr.z;
+        P.bsdf_le[i] = ble;
+        if(!ms.scattered)
+        {
+            P.sampler[i] = smp.s;
+            continue;
+        }
+        flags[i] = flag | SCATTER_BIT;
+        const F4 bd = P.beta_depth[i], rp = P.rad_pixel[i];
+        V3 beta = v3(bd);
+        const int depth = __float_as_int(bd.w);
+        const uint32_t pixel = __float_as_uint(rp.w);
+        const V3 path_rad = v3(rp);
+        if(russian_roulette(beta, depth, smp, R))
+        {
+            splat(film, pixel, R.width, path_rad);
+            continue;
+        }
+        const V3 albedo(m.albedo[0], m.albedo[1], m.albedo[2]);
+        LightSample ls = sample_light(S, ms.position, V3(0, 0, 1), false, smp);
+        if(ls.success)
+        {
+            // HG eval/pdf with u = -cos(wi, wo)
+            const V3 wo = -d;
+            const float u = -dot(normalize(ls.d), normalize(wo));
+            const float ph = henyey_greenstein(m.g, u);
+            ls.li = ls.li * beta * (albedo * ph) / (ph + ls.light_pdf);
+        }
+        // HenyeyGreensteinPhaseShader::sample (core/btrc/core/medium.cpp:32-64)
+        float s0, s1, s2;
+        smp.get3d(s0, s1, s2);
+        const float g = m.g;
+        const float s = s0 + s0 - 1;
+        float u;
+        if(fabsf(g) < 0.001f)
+            u = s;
+        else
+        {
+            const float g2 = g * g;
+            u = (1.0f + g2 - sqrf((1.0f - g2) / (1.0f + g * s))) / (g + g);
+        }
+        const float cos_theta = -u;
+        const float sin_theta = cos2sin(cos_theta);
+        const float phi = 2 * PI * s1;
+        const V3 lwi(sin_theta * sinf(phi), sin_theta * cosf(phi), cos_theta);
+        const float phase_val = henyey_greenstein(g, u);
+        const V3 phase = albedo * phase_val;
+        V3 ndir = Frame::from_z(-d).local_to_global(lwi);
+        (void)s2;
+        if(ls.success)
+        {
+            const uint32_t k = queue_append(&cnt->shadow);
+            const int smed = ls.t1 > 1 ? S.vacuum_medium : medium_id;
+            SH.o[k] = f4(ls.o, __uint_as_float(pixel));
+            SH.d[k] = f4(ls.d, ls.t1);
+            SH.beta[k] = f4(ls.li, __int_as_float(smed));
+            SamplerState ss;
+            pcg32_seed(ss.a, ss.b, mix_bits((static_cast<uint64_t>(cnt->iterations) << 32) ^ i) ^ pixel, PCG_STREAM);
+            SH.sampler[k] = ss;
+        }
+        if(!is_zero(phase))
+        {
+            ndir = normalize(ndir);
+            const V3 beta_le = beta * phase;
+            beta = beta_le / phase_val;
+            const uint32_t k = queue_append(&cnt->next_active);
+            N.beta_depth[k] = f4(beta, __int_as_float(depth + 1));
+            N.rad_pixel[k] = f4(path_rad, __uint_as_float(pixel));
+            N.sampler[k] = smp.s;
+            N.ray_o[k] = f4(ms.position, __int_as_float(medium_id));
+            N.ray_d[k] = f4(ndir, MAX_FLOAT);
+            N.bsdf_le[k] = f4(beta_le, phase_val);
+        }
+        else
+            splat(film, pixel, R.width, path_rad);
+    }
+}
+
+// ShadePipeline (builtin/btrc/builtin/renderer/wavefront/shade.cpp:29-235)
+__global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, DevRender R, PathSoA P, PathSoA N, ShadowSoA SH,
+                                                 const uint32_t *flags, const HitDetail *hits, float4 *film,
+                                                 Counters *cnt)
+{
+    const uint32_t n = cnt->active;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    {
+        const uint32_t flag = flags[i];
+        const F4 bd = P.beta_depth[i], rp = P.rad_pixel[i];
+        const F4 ro = P.ray_o[i], rd = P.ray_d[i], ble = P.bsdf_le[i];
+        const uint32_t pixel = __float_as_uint(rp.w);
+        const V3 o = v3(ro), d = v3(rd), beta_le = v3(ble);
+        const float bsdf_pdf = ble.w;
+        V3 path_rad = v3(rp);
+        const bool scattered = (flag & SCATTER_BIT) != 0;
+
+        if(!(flag & HIT_BIT))
+        {
+            V3 rad = miss_le(S, d, beta_le, bsdf_pdf);
+            if(!scattered)
+                rad = rad + path_rad;
+            splat(film, pixel, R.width, rad);
+            continue;
+        }
+
+        const HitDetail h = hits[i];
+        const Instance &inst = S.instances[flag & INST_MASK];
+        const Geometry geo = S.geometries[inst.geometry];
+        const SurfacePoint sp = get_hitinfo(S, o, d, inst, geo.tri_offset + h.prim, h.t, h.b1, h.b2);
+        const V3 le = hit_light_le(S, o, d, sp, beta_le, bsdf_pdf, inst.light);
+        if(scattered)
+        {
+            splat(film, pixel, R.width, le);
+            continue;
+        }
+        path_rad = path_rad + le;
+
+        V3 beta = v3(bd);
+        const int depth = __float_as_int(bd.w);
+        DSampler smp;
+        smp.type = R.sampler;
+        smp.s = P.sampler[i];
+        if(russian_roulette(beta, depth, smp, R))
+        {
+            splat(film, pixel, R.width, path_rad);
+            continue;
+        }
+
+        LightSample ls = sample_light(S, sp.position, sp.frame.z, true, smp);
+
+        const Material mat = S.materials[inst.material];
+        SurfaceShader sh;
+        sh.frame.geometry = sp.frame;
+        sh.frame.shading = sp.frame.rotate_to_new_z(sp.interp_z);
+        sh.mat = make_material_eval(mat);
+        sh.shadow_terminator = mat.shadow_terminator != 0;
+
+        float u0, u1, u2;
+        smp.get3d(u0, u1, u2);
+        const V3 wo = -d;
+        CompSample bs = sh.sample(wo, u0, u1, u2);
+        V3 shadow_f(0);
+        float shadow_pdf = 0;
+        if(ls.success)
+        {
+            shadow_f = sh.eval(ls.d, wo);
+            ls.success = !is_zero(shadow_f);
+            if(ls.success)
+                shadow_pdf = sh.pdf(ls.d, wo);
+        }
+
+        if(ls.success)
+        {
+            const bool shadow_out = dot(sp.frame.z, ls.d) > 0;
+            const bool last_out = dot(sp.frame.z, d) < 0;
+            const int inner = static_cast<int>(inst.media & 0xffffu), outer = static_cast<int>(inst.media >> 16);
+            const int smed = shadow_out == last_out ? __float_as_int(ro.w) : (shadow_out ? outer : inner);
+            const float c = fabsf(dot(normalize(ls.d), sp.frame.z));
+            const V3 beta_li = ls.li * beta * shadow_f * c / (shadow_pdf + ls.light_pdf);
+            const uint32_t k = queue_append(&cnt->shadow);
+            SH.o[k] = f4(ls.o, __uint_as_float(pixel));
+            SH.d[k] = f4(ls.d, ls.t1);
+            SH.beta[k] = f4(beta_li, __int_as_float(smed));
+            if(S.has_media)
+            {
+                SamplerState ss;
+                pcg32_seed(ss.a, ss.b, mix_bits((static_cast<uint64_t>(cnt->iterations) << 32) ^ i) ^ pixel,
+                           PCG_STREAM);
+                SH.sampler[k] = ss;
+            }
+        }
+
+        if(!is_zero(bs.f))
+        {
+            const V3 ndir = normalize(bs.dir);
+            const float c = fabsf(dot(ndir, sp.frame.z));
+            const V3 new_beta_le = beta * c * bs.f;
+            beta = new_beta_le / bs.pdf;
+            const V3 no = offset_dir(sp.position, sp.frame.z, ndir);
+            const bool nout = dot(sp.frame.z, ndir) > 0;
+            const int nmed = nout ? static_cast<int>(inst.media >> 16) : static_cast<int>(inst.media & 0xffffu);
+            const float stored_pdf = bs.is_delta ? -bs.pdf : bs.pdf;
+            const uint32_t k = queue_append(&cnt->next_active);
+            N.beta_depth[k] = f4(beta, __int_as_float(depth + 1));
+            N.rad_pixel[k] = f4(path_rad, __uint_as_float(pixel));
+            N.sampler[k] = smp.s;
+            N.ray_o[k] = f4(no, __int_as_float(nmed));
+            N.ray_d[k] = f4(ndir, MAX_FLOAT);
+            N.bsdf_le[k] = f4(new_beta_le, stored_pdf);
+        }
+        else
+            splat(film, pixel, R.width, path_rad);
+    }
+}
+
+// ShadowPipeline (builtin/btrc/builtin/renderer/wavefront/shadow.cpp:24-76)
+__global__ void __launch_bounds__(128) k_shadow(DevScene S, DevRender R, ShadowSoA SH, float4 *film, Counters *cnt)
+{
+    const uint32_t n = cnt->shadow;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    {
+        const F4 o = SH.o[i], d = SH.d[i];
+        const TravRay tr = make_trav_ray(o.x, o.y, o.z, d.x, d.y, d.z);
+        if(trace_any(tr, d.w, reinterpret_cast<const float4 *>(S.nodes), reinterpret_cast<const float4 *>(S.tris),
+                     S.node_count, &cnt->err))
+            continue;
+        const F4 b = SH.beta[i];
+        V3 beta = v3(b);
+        if(S.has_media)
+        {
+            DSampler smp;
+            smp.type = SAMPLER_INDEPENDENT;
+            smp.s = SH.sampler[i];
+            const V3 ro = v3(o), rdv = v3(d);
+            if(d.w > 1)
+            {
+                const Medium &m = S.media[S.vacuum_medium];
+                beta = beta * medium_tr(S, m, ro, ro + normalize(rdv) * S.world_diagonal, smp);
+            }
+            else
+            {
+                const Medium &m = S.media[__float_as_int(b.w)];
+                beta = beta * medium_tr(S, m, ro, ro + rdv * d.w, smp);
+            }
+        }
+        splat(film, __float_as_uint(o.w), R.width, beta);
+    }
+}
+
+__global__ void k_resolve(const float4 *film, float *rgb, uint32_t pixels)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= pixels)
+        return;
+    const float4 f = film[i];
+    const float inv = f.w > 0 ? 1.0f / f.w : 0.0f;
+    rgb[i * 3 + 0] = f.x * inv;
+    rgb[i * 3 + 1] = f.y * inv;
+    rgb[i * 3 + 2] = f.z * inv;
+}
+
+uint64_t *launches_by_stage_ptr(uint64_t *p) { return p; }
+
+int persistent_grid(int block, const void *kernel)
+{
+    int dev = 0, sms = 152, per_sm = 4;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+    return sms * (per_sm > 0 ? per_sm : 1);
+}
+
+// Per-stage event timing for profile mode 1: a pair of events around every launch.
+struct StageTimer
+{
+    std::vector<cudaEvent_t> pool;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
+    size_t used = 0;
+    cudaEvent_t get()
+    {
+        if(used == pool.size())
+        {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            pool.push_back(e);
+        }
+        return pool[used++];
+    }
+    ~StageTimer()
+    {
+        for(auto e : pool)
+            cudaEventDestroy(e);
+    }
+};
+
+template<typename Launch>
+void timed(StageTimer *T, int stage, cudaStream_t st, uint64_t *launches, Launch &&fn)
+{
+    ++launches[stage];
+    if(!T)
+    {
+        fn();
+        return;
+    }
+    cudaEvent_t a = T->get(), b = T->get();
+    cudaEventRecord(a, st);
+    fn();
+    cudaEventRecord(b, st);
+    T->marks.push_back({ stage, { a, b } });
+}
+
+cudaError_t enqueue_bounce(const DevScene &S, const DevRender &R, RenderBuffers &B, int parity, cudaStream_t st,
+                           const int grids[5], int profile, StageTimer *T, uint64_t *launches)
+{
+    PathSoA &P = B.path[parity];
+    PathSoA &N = B.path[1 - parity];
+    timed(T, STAGE_CONTROL, st, launches, [&] { k_control<<<1, 1, 0, st>>>(B.counters, B.capacity, R.total_paths); });
+    timed(T, STAGE_GENERATE, st, launches,
+          [&] { k_generate<<<grids[0], BLOCK, 0, st>>>(R, P, B.film, B.counters, S.vacuum_medium); });
+    timed(T, STAGE_TRACE, st, launches, [&] {
+        if(profile == 2)
+            k_trace<true><<<grids[1], 128, 0, st>>>(S, P, B.hit_flag, B.hit_detail, B.counters);
+        else
+            k_trace<false><<<grids[1], 128, 0, st>>>(S, P, B.hit_flag, B.hit_detail, B.counters);
+    });
+    if(S.has_media)
+        timed(T, STAGE_MEDIUM, st, launches, [&] {
+            k_medium<<<grids[2], BLOCK, 0, st>>>(S, R, P, N, B.shadow, B.hit_flag, B.hit_detail, B.film, B.counters);
+        });
+    timed(T, STAGE_SHADE, st, launches, [&] {
+        k_shade<<<grids[3], BLOCK, 0, st>>>(S, R, P, N, B.shadow, B.hit_flag, B.hit_detail, B.film, B.counters);
+    });
+    timed(T, STAGE_SHADOW, st, launches,
+          [&] { k_shadow<<<grids[4], 128, 0, st>>>(S, R, B.shadow, B.film, B.counters); });
+    return cudaGetLastError();
+}
+
+} // namespace
+
+cudaError_t upload_primes()
+{
+    std::vector<uint32_t> primes;
+    for(uint32_t v = 2; primes.size() < PRIME_COUNT; ++v)
+    {
+        bool is_prime = true;
+        for(uint32_t p : primes)
+        {
+            if(p * p > v)
+                break;
+            if(v % p == 0)
+            {
+                is_prime = false;
+                break;
+            }
+        }
+        if(is_prime)
+            primes.push_back(v);
+    }
+    return cudaMemcpyToSymbol(c_primes, primes.data(), sizeof(uint32_t) * PRIME_COUNT);
+}
+
+cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffers &B, cudaStream_t st,
+                             const std::atomic<bool> *cancel, bool use_graphs, int profile, RenderStats *stats,
+                             bool *cancelled)
+{
+    *cancelled = false;
+    if(profile != 0)
+        use_graphs = false;
+    uint64_t launches[STAGE_COUNT] = {};
+    uint64_t graph_launches = 0;
+    StageTimer timer;
+    StageTimer *T = profile == 1 ? &timer : nullptr;
+    // every path ends within D + 1 bounces of its generation, and while the queue is full
+    // at least `capacity` paths finish every D + 1 bounces: bound the loop so that a
+    // malformed configuration cannot spin forever
+    const uint64_t depth_bound = static_cast<uint64_t>(std::max(R.max_depth, R.min_depth)) + 2;
+    const uint64_t bounce_bound = ((R.total_paths + R.capacity - 1) / R.capacity + 2) * depth_bound;
+    const uint64_t max_launches = bounce_bound + RING_SLOTS + 64;  // a launch runs two bounces: 2x slack
+    cudaError_t e = cudaMemsetAsync(B.counters, 0, sizeof(Counters), st);
+    if(e != cudaSuccess)
+        return e;
+    const int grids[5] = {
+        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_generate)),
+        persistent_grid(128, reinterpret_cast<const void *>(k_trace<false>)),
+        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_medium)),
+        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_shade)),
+        persistent_grid(128, reinterpret_cast<const void *>(k_shadow)),
+    };
+
+    cudaGraphExec_t exec = nullptr;
+    if(use_graphs)
+    {
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+        if(e != cudaSuccess)
+            return e;
+        uint64_t dummy[STAGE_COUNT] = {};
+        enqueue_bounce(S, R, B, 0, st, grids, 0, nullptr, dummy);
+        enqueue_bounce(S, R, B, 1, st, grids, 0, nullptr, dummy);
+        e = cudaStreamEndCapture(st, &graph);
+        if(e != cudaSuccess)
+            return e;
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if(e != cudaSuccess)
+            return e;
+    }
+
+    cudaEvent_t ev[RING_SLOTS];
+    for(int k = 0; k < RING_SLOTS; ++k)
+        cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming);
+    cudaEvent_t t0, t1;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    cudaEventRecord(t0, st);
+
+    // Launch pairs of bounces; read the counters back asynchronously and test completion
+    // RING_SLOTS-1 launches behind, so the GPU never idles waiting for the host.
+    uint64_t launches_total = 0;
+    for(;;)
+    {
+        const uint64_t launches_now = launches_total;
+        const int slot = static_cast<int>(launches_now % RING_SLOTS);
+        if(launches_now >= RING_SLOTS - 1)
+        {
+            const int old = static_cast<int>((launches_now - (RING_SLOTS - 1)) % RING_SLOTS);
+            e = cudaEventSynchronize(ev[old]);
+            if(e != cudaSuccess)
+                break;
+            const Counters &c = B.host_counters[old];
+            if(c.generated >= R.total_paths && c.next_active == 0)
+                break;
+            if(cancel && cancel->load())
+            {
+                *cancelled = true;
+                break;
+            }
+        }
+        if(launches_now >= max_launches)
+        {
+            e = cudaErrorLaunchTimeout;
+            break;
+        }
+        if(use_graphs)
+        {
+            e = cudaGraphLaunch(exec, st);
+            ++graph_launches;
+        }
+        else
+        {
+            e = enqueue_bounce(S, R, B, 0, st, grids, profile, T, launches_by_stage_ptr(launches));
+            if(e == cudaSuccess)
+                e = enqueue_bounce(S, R, B, 1, st, grids, profile, T, launches_by_stage_ptr(launches));
+        }
+        if(e != cudaSuccess)
+            break;
+        cudaMemcpyAsync(&B.host_counters[slot], B.counters, sizeof(Counters), cudaMemcpyDeviceToHost, st);
+        cudaEventRecord(ev[slot], st);
+        ++launches_total;
+    }
+    cudaEventRecord(t1, st);
+    cudaError_t se = cudaEventSynchronize(t1);
+    if(e == cudaSuccess)
+        e = se;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, t0, t1);
+    Counters fin{};
+    cudaMemcpy(&fin, B.counters, sizeof(Counters), cudaMemcpyDeviceToHost);
+    for(int k = 0; k < RING_SLOTS; ++k)
+        cudaEventDestroy(ev[k]);
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    if(exec)
+        cudaGraphExecDestroy(exec);
+    if(stats)
+    {
+        *stats = RenderStats{};
+        stats->paths = fin.generated;
+        stats->ext_rays = fin.ext_rays;
+        stats->shadow_rays = fin.shadow_rays + fin.shadow;
+        stats->iterations = fin.iterations;
+        stats->err = fin.err;
+        stats->device_ms = ms;
+        stats->node_visits = fin.node_visits;
+        stats->tri_tests = fin.tri_tests;
+        const uint64_t per_bounce = S.has_media ? 6 : 5;
+        for(int k = 0; k < STAGE_COUNT; ++k)
+            stats->stage_launches[k] = launches[k];
+        if(use_graphs)
+        {
+            for(int k = 0; k < STAGE_COUNT; ++k)
+                stats->stage_launches[k] = (k == STAGE_MEDIUM && !S.has_media) ? 0 : graph_launches * 2;
+            stats->kernel_launches = graph_launches * 2 * per_bounce;
+        }
+        else
+        {
+            uint64_t total = 0;
+            for(int k = 0; k < STAGE_COUNT; ++k)
+                total += launches[k];
+            stats->kernel_launches = total;
+        }
+        for(auto &m : timer.marks)
+        {
+            float t = 0;
+            cudaEventElapsedTime(&t, m.second.first, m.second.second);
+            stats->stage_ms[m.first] += t;
+        }
+    }
+    return e;
+}
+
+cudaError_t launch_resolve(const float4 *film, float *rgb, uint32_t pixels, cudaStream_t st)
+{
+    if(pixels == 0)
+        return cudaSuccess;
+    k_resolve<<<(pixels + 255) / 256, 256, 0, st>>>(film, rgb, pixels);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- test hooks
+
+namespace {
+
+__global__ void k_sampler_batch(int type, int width, int height, HaltonConsts hc, const uint32_t *pix,
+                                const uint32_t *sidx, uint32_t n, uint32_t dims, float *out)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= n)
+        return;
+    (void)width;
+    (void)height;
+    DSampler smp;
+    smp.type = type;
+    const uint32_t p = pix[i];
+    smp.s = sampler_init(type, hc, p & 0xffffu, p >> 16, sidx[i]);
+    for(uint32_t k = 0; k < dims; ++k)
+        out[static_cast<size_t>(i) * dims + k] = smp.get1d();
+}
+
+__global__ void k_bsdf_batch(int op, const Material *mats, const float *wo, const float *wu, uint32_t n, float *out)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= n)
+        return;
+    Material m = mats[i];
+    const V3 lwo(wo[i * 3 + 0], wo[i * 3 + 1], wo[i * 3 + 2]);
+    const MaterialEval e = make_material_eval(m);
+    if(op == 0)
+    {
+        const V3 lwi(wu[i * 3 + 0], wu[i * 3 + 1], wu[i * 3 + 2]);
+        const V3 f = comp_eval(e, lwi, lwo);
+        const float pdf = comp_pdf(e, lwi, lwo);
+        out[i * 4 + 0] = f.x;
+        out[i * 4 + 1] = f.y;
+        out[i * 4 + 2] = f.z;
+        out[i * 4 + 3] = pdf;
+    }
+    else
+    {
+        const CompSample s = comp_sample(e, lwo, wu[i * 3 + 0], wu[i * 3 + 1], wu[i * 3 + 2]);
+        out[i * 7 + 0] = s.f.x;
+        out[i * 7 + 1] = s.f.y;
+        out[i * 7 + 2] = s.f.z;
+        out[i * 7 + 3] = s.pdf;
+        out[i * 7 + 4] = s.dir.x;
+        out[i * 7 + 5] = s.dir.y;
+        out[i * 7 + 6] = s.dir.z;
+    }
+}
+
+__global__ void k_medium_tr_batch(DevScene S, int medium_id, const float *seg, const uint64_t *seeds, uint32_t n,
+                                  float *out)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= n)
+        return;
+    DSampler smp;
+    smp.type = SAMPLER_INDEPENDENT;
+    pcg32_seed(smp.s.a, smp.s.b, seeds[i], PCG_STREAM);
+    const V3 a(seg[i * 6 + 0], seg[i * 6 + 1], seg[i * 6 + 2]);
+    const V3 b(seg[i * 6 + 3], seg[i * 6 + 4], seg[i * 6 + 5]);
+    out[i] = medium_tr(S, S.media[medium_id], a, b, smp).x;
+}
+
+} // namespace
+
+cudaError_t launch_sampler_batch(int type, int width, int height, const HaltonConsts &hc, const uint32_t *pixel_xy,
+                                 const uint32_t *sample_index, uint32_t n, uint32_t dims, float *out, cudaStream_t st)
+{
+    if(n == 0)
+        return cudaSuccess;
+    k_sampler_batch<<<(n + 127) / 128, 128, 0, st>>>(type, width, height, hc, pixel_xy, sample_index, n, dims, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bsdf_batch(int op, const Material *mats, const float *wo, const float *wi_or_u, uint32_t n,
+                              float *out, cudaStream_t st)
+{
+    if(n == 0)
+        return cudaSuccess;
+    k_bsdf_batch<<<(n + 127) / 128, 128, 0, st>>>(op, mats, wo, wi_or_u, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_medium_tr_batch(const DevScene &S, int medium_id, const float *seg, const uint64_t *seeds,
+                                   uint32_t n, float *out, cudaStream_t st)
+{
+    if(n == 0)
+        return cudaSuccess;
+    k_medium_tr_batch<<<(n + 127) / 128, 128, 0, st>>>(S, medium_id, seg, seeds, n, out);
+    return cudaGetLastError();
+}
+
+} // namespace bt

@@ -1,0 +1,84 @@
+// Host-callable launchers for the CUDA kernels (implemented in the .cu files).
+#pragma once
+
+#include <atomic>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "device.h"
+
+namespace bt {
+
+// upload the first 1000 primes to constant memory (once per device)
+cudaError_t upload_primes();
+
+cudaError_t launch_trace_closest(const DevScene &S, const Ray *rays, uint32_t n, uint32_t *flags,
+                                 HitDetail *hits, uint32_t *err, cudaStream_t st);
+cudaError_t launch_trace_any(const DevScene &S, const Ray *rays, uint32_t n, uint32_t *occluded,
+                             uint32_t *err, cudaStream_t st);
+// per-ray node visits and triangle tests of the closest-hit traversal
+cudaError_t launch_trace_stats(const DevScene &S, const Ray *rays, uint32_t n, uint32_t *node_visits,
+                               uint32_t *tri_tests, uint32_t *err, cudaStream_t st);
+
+struct RenderBuffers
+{
+    PathSoA path[2];
+    ShadowSoA shadow;
+    uint32_t *hit_flag;
+    HitDetail *hit_detail;
+    float4 *film;          // radiance.rgb, weight per pixel
+    Counters *counters;
+    Counters *host_counters;  // pinned, ring of RING_SLOTS
+    uint32_t capacity;
+};
+
+constexpr int RING_SLOTS = 4;
+
+enum Stage
+{
+    STAGE_CONTROL = 0,
+    STAGE_GENERATE = 1,
+    STAGE_TRACE = 2,
+    STAGE_MEDIUM = 3,
+    STAGE_SHADE = 4,
+    STAGE_SHADOW = 5,
+    STAGE_COUNT = 6
+};
+
+struct RenderStats
+{
+    uint64_t paths;
+    uint64_t ext_rays;
+    uint64_t shadow_rays;
+    uint32_t iterations;
+    uint32_t err;
+    float device_ms;
+    uint64_t kernel_launches;
+    double stage_ms[STAGE_COUNT];        // profile mode 1: CUDA events around every launch
+    uint64_t stage_launches[STAGE_COUNT];
+    uint64_t node_visits, tri_tests;     // profile mode 2: traversal counters
+};
+
+// Runs the wavefront loop to completion on stream st. The film must be cleared by the
+// caller. Returns cudaSuccess or the first CUDA error; *cancelled is set when the cancel
+// flag stopped the loop early.
+// profile: 0 none (graphs allowed), 1 per-stage CUDA events (no graphs),
+//          2 traversal counters in the closest-hit stage (no graphs, slower)
+cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffers &B, cudaStream_t st,
+                             const std::atomic<bool> *cancel, bool use_graphs, int profile, RenderStats *stats,
+                             bool *cancelled);
+
+// radiance / weight -> rgb (3 floats per pixel)
+cudaError_t launch_resolve(const float4 *film, float *rgb, uint32_t pixels, cudaStream_t st);
+
+// test hooks
+cudaError_t launch_sampler_batch(int type, int width, int height, const HaltonConsts &hc,
+                                 const uint32_t *pixel_xy, const uint32_t *sample_index, uint32_t n,
+                                 uint32_t dims, float *out, cudaStream_t st);
+cudaError_t launch_bsdf_batch(int op, const Material *mats, const float *wo, const float *wi_or_u,
+                              uint32_t n, float *out, cudaStream_t st);
+cudaError_t launch_medium_tr_batch(const DevScene &S, int medium_id, const float *seg, const uint64_t *seeds,
+                                   uint32_t n, float *out, cudaStream_t st);
+
+} // namespace bt

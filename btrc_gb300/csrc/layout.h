@@ -1,0 +1,182 @@
+// HBM data layout shared by the host builder and the CUDA kernels.
+//
+// Acceleration structure (single level, instances baked to world space at build time):
+//   CWNode  80 B  8-wide compressed node: origin, per-axis power-of-two scale, child
+//                 boxes quantised to 8 bits, child/triangle base indices, per-slot meta.
+//   TriRec  48 B  world-space triangle v0,v1,v2 (xyz) with the instance index in v0.w
+//                 and the primitive index within its geometry in v1.w.
+// Shading data (per geometry, shared by all instances of a geometry), 6 x float4 per
+// triangle exactly as builtin/btrc/builtin/geometry/triangle_mesh.cpp:40-71 lays it out:
+//   ex|u_a, ey|u_ba, ez|u_ca, sn_a|v_a, sn_ba|v_ba, sn_ca|v_ca.
+#pragma once
+
+#include <cstdint>
+
+#include "bmath.h"
+
+namespace bt {
+
+struct alignas(16) F4
+{
+    float x, y, z, w;
+};
+
+struct alignas(16) CWNode
+{
+    float px, py, pz;
+    uint8_t ex, ey, ez, imask;
+    uint32_t child_base;
+    uint32_t tri_base;
+    uint8_t meta[8];
+    uint8_t qlo_x[8], qlo_y[8], qlo_z[8];
+    uint8_t qhi_x[8], qhi_y[8], qhi_z[8];
+};
+static_assert(sizeof(CWNode) == 80, "CWNode must be 80 bytes");
+
+struct alignas(16) TriRec
+{
+    float v0x, v0y, v0z;
+    uint32_t inst;
+    float v1x, v1y, v1z;
+    uint32_t prim;
+    float v2x, v2y, v2z;
+    uint32_t pad;
+};
+static_assert(sizeof(TriRec) == 48, "TriRec must be 48 bytes");
+
+// Ray as stored in the wavefront queues and passed through btrc_trace_*:
+// o.xyz + medium id, d.xyz + t1 (reference: builtin/.../wavefront/soa.h:8-38).
+struct alignas(16) Ray
+{
+    float ox, oy, oz;
+    uint32_t medium_id;
+    float dx, dy, dz;
+    float t1;
+};
+
+// Closest-hit result: flag word (instance | HIT_BIT) plus (t, prim, b1, b2).
+constexpr uint32_t HIT_BIT = 1u << 30;
+constexpr uint32_t SCATTER_BIT = 1u << 29;
+constexpr uint32_t INST_MASK = (1u << 29) - 1;
+
+struct alignas(16) HitDetail
+{
+    float t;
+    uint32_t prim;
+    float b1, b2;
+};
+
+enum MaterialType : int32_t
+{
+    MAT_DIFFUSE = 0,
+    MAT_METAL = 1,
+    MAT_DISNEY = 2,
+    MAT_BLACK = 3,
+    MAT_INVISIBLE = 4,
+    MAT_MIRROR = 5,
+};
+
+// Material parameters (constant textures only).
+//   diffuse: p[0..2] albedo
+//   metal  : p[0..2] R0, p[3] roughness, p[4] anisotropic
+//   disney : p[0..2] base color, p[3] metallic, p[4] roughness, p[5] specular,
+//            p[6] specular_tint, p[7] anisotropic, p[8] sheen, p[9] sheen_tint,
+//            p[10] clearcoat, p[11] clearcoat_gloss, p[12] transmission,
+//            p[13] transmission_roughness, p[14] ior
+//   mirror : p[0..2] color
+struct alignas(16) Material
+{
+    int32_t type;
+    int32_t shadow_terminator;
+    float p[16];
+    int32_t pad[2];
+};
+
+struct alignas(16) Instance
+{
+    float l2w[12];
+    float w2l[12];
+    int32_t geometry;
+    int32_t material;
+    int32_t light;
+    uint32_t media;  // inner medium id (low 16) | outer medium id (high 16)
+};
+
+struct alignas(16) Geometry
+{
+    uint32_t tri_offset;  // into the shading SoA and light-sampling arrays
+    uint32_t tri_count;
+    float total_area;
+    float pad;
+};
+
+struct alignas(8) AliasEntry8
+{
+    float accept;
+    uint32_t alias;
+};
+
+struct alignas(16) AreaLight
+{
+    int32_t instance;
+    int32_t geometry;
+    float scale;
+    float pad;
+    float intensity[3];
+    float pad2;
+};
+
+enum EnvType : int32_t
+{
+    ENV_NONE = 0,
+    ENV_GRADIENT_SKY = 1,
+};
+
+struct alignas(16) EnvLight
+{
+    int32_t type;
+    float lower[3];
+    float upper[3];
+    float up[3];
+    float pad[2];
+};
+
+enum MediumType : int32_t
+{
+    MED_VACUUM = 0,
+    MED_HOMOGENEOUS = 1,
+    MED_HETEROGENEOUS = 2,
+};
+
+// Participating medium. Heterogeneous media are a density grid behind a transform
+// (reference: builtin/btrc/builtin/medium/hetergeneous.cpp, core/btrc/core/medium.cpp:98-129).
+struct alignas(16) Medium
+{
+    int32_t type;
+    int32_t priority;
+    int32_t grid_offset;     // float index into the density pool
+    int32_t res_x, res_y, res_z;
+    float sigma_max;
+    float g;
+    float sigma_t_const;     // homogeneous sigma_t (grey) or scale when constant
+    float albedo[3];
+    float w2l[12];           // world -> medium local ([-1,1]^3) transform
+    float l2w[12];
+};
+
+enum SamplerType : int32_t
+{
+    SAMPLER_INDEPENDENT = 0,
+    SAMPLER_HALTON = 1,
+};
+
+// Gaussian filter importance-sampling grid resolution (film_filter/gaussian.cpp:8)
+constexpr int FILTER_GRID = 256;
+
+enum FilterType : int32_t
+{
+    FILTER_BOX = 0,
+    FILTER_GAUSSIAN = 1,
+};
+
+} // namespace bt

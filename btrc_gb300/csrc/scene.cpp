@@ -1,0 +1,999 @@
+#include "scene.h"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <filesystem>
+#include <fstream>
+#include <map>
+#include <numeric>
+#include <stdexcept>
+
+namespace bt {
+
+// ---------------------------------------------------------------- Mat4 / Transform
+
+Mat4 Mat4::identity() { return rows(1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1); }
+
+Mat4 Mat4::rows(float m00, float m01, float m02, float m03,
+                float m10, float m11, float m12, float m13,
+                float m20, float m21, float m22, float m23,
+                float m30, float m31, float m32, float m33)
+{
+    Mat4 r;
+    r.a[0][0] = m00; r.a[0][1] = m01; r.a[0][2] = m02; r.a[0][3] = m03;
+    r.a[1][0] = m10; r.a[1][1] = m11; r.a[1][2] = m12; r.a[1][3] = m13;
+    r.a[2][0] = m20; r.a[2][1] = m21; r.a[2][2] = m22; r.a[2][3] = m23;
+    r.a[3][0] = m30; r.a[3][1] = m31; r.a[3][2] = m32; r.a[3][3] = m33;
+    return r;
+}
+
+Mat4 Mat4::translate(float x, float y, float z)
+{
+    return rows(1, 0, 0, x, 0, 1, 0, y, 0, 0, 1, z, 0, 0, 0, 1);
+}
+
+Mat4 Mat4::scale(float x, float y, float z)
+{
+    return rows(x, 0, 0, 0, 0, y, 0, 0, 0, 0, z, 0, 0, 0, 0, 1);
+}
+
+// The reference fills its column-major storage with the textbook Rodrigues entries
+// (common/btrc/utils/math/mat4.cpp:117-145), so at(r, c) holds entry [c][r] of the
+// textbook matrix. That is reproduced here: R below is the textbook matrix, stored
+// transposed.
+Mat4 Mat4::rotate(V3 axis, float rad)
+{
+    const V3 a = normalize(axis);
+    const float s = std::sin(rad), c = std::cos(rad);
+    float R[3][3];
+    R[0][0] = a.x * a.x + (1 - a.x * a.x) * c;
+    R[0][1] = a.x * a.y * (1 - c) - a.z * s;
+    R[0][2] = a.x * a.z * (1 - c) + a.y * s;
+    R[1][0] = a.x * a.y * (1 - c) + a.z * s;
+    R[1][1] = a.y * a.y + (1 - a.y * a.y) * c;
+    R[1][2] = a.y * a.z * (1 - c) - a.x * s;
+    R[2][0] = a.x * a.z * (1 - c) - a.y * s;
+    R[2][1] = a.y * a.z * (1 - c) + a.x * s;
+    R[2][2] = a.z * a.z + (1 - a.z * a.z) * c;
+    return rows(R[0][0], R[1][0], R[2][0], 0,
+                R[0][1], R[1][1], R[2][1], 0,
+                R[0][2], R[1][2], R[2][2], 0,
+                0, 0, 0, 1);
+}
+
+Mat4 Mat4::rotate_x(float rad)
+{
+    const float S = std::sin(rad), C = std::cos(rad);
+    return rows(1, 0, 0, 0, 0, C, -S, 0, 0, S, C, 0, 0, 0, 0, 1);
+}
+
+Mat4 Mat4::rotate_y(float rad)
+{
+    const float S = std::sin(rad), C = std::cos(rad);
+    return rows(C, 0, S, 0, 0, 1, 0, 0, -S, 0, C, 0, 0, 0, 0, 1);
+}
+
+Mat4 Mat4::rotate_z(float rad)
+{
+    const float S = std::sin(rad), C = std::cos(rad);
+    return rows(C, -S, 0, 0, S, C, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1);
+}
+
+Mat4 operator*(const Mat4 &a, const Mat4 &b)
+{
+    Mat4 r;
+    for(int i = 0; i < 4; ++i)
+        for(int j = 0; j < 4; ++j)
+            r.a[i][j] = a.a[i][0] * b.a[0][j] + a.a[i][1] * b.a[1][j] +
+                        a.a[i][2] * b.a[2][j] + a.a[i][3] * b.a[3][j];
+    return r;
+}
+
+Transform operator*(const Transform &a, const Transform &b)
+{
+    Transform r;
+    r.mat = a.mat * b.mat;
+    r.inv = b.inv * a.inv;
+    return r;
+}
+
+V3 Transform::point(V3 p) const
+{
+    return V3(mat.a[0][0] * p.x + mat.a[0][1] * p.y + mat.a[0][2] * p.z + mat.a[0][3],
+              mat.a[1][0] * p.x + mat.a[1][1] * p.y + mat.a[1][2] * p.z + mat.a[1][3],
+              mat.a[2][0] * p.x + mat.a[2][1] * p.y + mat.a[2][2] * p.z + mat.a[2][3]);
+}
+
+V3 Transform::vector(V3 v) const
+{
+    return V3(mat.a[0][0] * v.x + mat.a[0][1] * v.y + mat.a[0][2] * v.z,
+              mat.a[1][0] * v.x + mat.a[1][1] * v.y + mat.a[1][2] * v.z,
+              mat.a[2][0] * v.x + mat.a[2][1] * v.y + mat.a[2][2] * v.z);
+}
+
+V3 Transform::normal(V3 n) const
+{
+    return V3(inv.a[0][0] * n.x + inv.a[1][0] * n.y + inv.a[2][0] * n.z,
+              inv.a[0][1] * n.x + inv.a[1][1] * n.y + inv.a[2][1] * n.z,
+              inv.a[0][2] * n.x + inv.a[1][2] * n.y + inv.a[2][2] * n.z);
+}
+
+void Transform::to_affine(float l2w[12], float w2l[12]) const
+{
+    for(int r = 0; r < 3; ++r)
+        for(int c = 0; c < 4; ++c)
+        {
+            l2w[r * 4 + c] = mat.a[r][c];
+            w2l[r * 4 + c] = inv.a[r][c];
+        }
+}
+
+// factory/btrc/factory/node/node.cpp:166-214. An array composes later elements on the
+// left: ret = elem * ret. rotate_z keeps the reference's (mat, inv) pair as written
+// (common/btrc/utils/math/transform.cpp:111-114: both use rotate_z(-rad)).
+Transform parse_transform(const json::NodeP &n)
+{
+    Transform t;
+    if(n->is_array())
+    {
+        for(auto &e : n->elems)
+            t = parse_transform(e) * t;
+        return t;
+    }
+    if(auto c = n->find("translate"))
+    {
+        const V3 v = json::as_vec3(c);
+        t.mat = Mat4::translate(v.x, v.y, v.z);
+        t.inv = Mat4::translate(-v.x, -v.y, -v.z);
+        return t;
+    }
+    if(auto c = n->find("rotate"))
+    {
+        const V3 axis = json::as_vec3(c->child("axis"));
+        const float rad = json::as_radian(c->child("angle"));
+        t.mat = Mat4::rotate(axis, rad);
+        t.inv = Mat4::rotate(axis, -rad);
+        return t;
+    }
+    if(auto c = n->find("rotate_x"))
+    {
+        const float rad = json::as_radian(c);
+        t.mat = Mat4::rotate_x(rad);
+        t.inv = Mat4::rotate_x(-rad);
+        return t;
+    }
+    if(auto c = n->find("rotate_y"))
+    {
+        const float rad = json::as_radian(c);
+        t.mat = Mat4::rotate_y(rad);
+        t.inv = Mat4::rotate_y(-rad);
+        return t;
+    }
+    if(auto c = n->find("rotate_z"))
+    {
+        const float rad = json::as_radian(c);
+        t.mat = Mat4::rotate_z(-rad);
+        t.inv = Mat4::rotate_z(-rad);
+        return t;
+    }
+    if(auto c = n->find("scale"))
+    {
+        const V3 s = json::as_vec3(c);
+        t.mat = Mat4::scale(s.x, s.y, s.z);
+        t.inv = Mat4::scale(1 / s.x, 1 / s.y, 1 / s.z);
+        return t;
+    }
+    throw json::ParseError("unknown transform3d type");
+}
+
+// ---------------------------------------------------------------- alias tables
+
+std::vector<AliasEntry8> build_alias_table(const std::vector<float> &probs)
+{
+    if(probs.empty())
+        throw std::runtime_error("alias table over an empty distribution");
+    double dsum = 0;
+    for(float p : probs)
+        dsum += p;
+    const float sum = static_cast<float>(dsum);
+    if(!(sum > 0))
+        throw std::runtime_error("alias table over a zero distribution");
+    const float ratio = static_cast<float>(probs.size()) / sum;
+    std::vector<AliasEntry8> units(probs.size());
+    std::vector<uint32_t> overs, unders;
+    for(uint32_t i = 0; i < units.size(); ++i)
+    {
+        const float p = probs[i] * ratio;
+        units[i].accept = p;
+        units[i].alias = i;
+        if(p > 1)
+            overs.push_back(i);
+        else if(p < 1)
+            unders.push_back(i);
+    }
+    while(!overs.empty() && !unders.empty())
+    {
+        const uint32_t over = overs.back();
+        const uint32_t under = unders.back();
+        overs.pop_back();
+        unders.pop_back();
+        units[over].accept -= 1 - units[under].accept;
+        units[under].alias = over;
+        if(units[over].accept > 1)
+            overs.push_back(over);
+        else if(units[over].accept < 1)
+            unders.push_back(over);
+    }
+    for(auto i : overs)
+        units[i].accept = 1;
+    for(auto i : unders)
+        units[i].accept = 1;
+    return units;
+}
+
+std::vector<AliasEntry8> build_gaussian_filter_table(float radius, float alpha)
+{
+    const float expv = std::exp(-alpha * radius * radius);
+    auto gaussian = [&](float d) { return std::max(0.0f, std::exp(-alpha * d * d) - expv); };
+    std::vector<float> values(FILTER_GRID * FILTER_GRID, 0.0f);
+    for(int y = 0; y < FILTER_GRID; ++y)
+    {
+        const float yf = 2 * radius * (y + 0.5f) / FILTER_GRID - radius;
+        for(int x = 0; x < FILTER_GRID; ++x)
+        {
+            const float xf = 2 * radius * (x + 0.5f) / FILTER_GRID - radius;
+            if(xf * xf + yf * yf < radius * radius)
+                values[y * FILTER_GRID + x] = gaussian(xf) * gaussian(yf);
+        }
+    }
+    return build_alias_table(values);
+}
+
+// ---------------------------------------------------------------- camera
+
+Camera make_pinhole(V3 eye, V3 dst, V3 up, float fov_y_deg, float w_over_h)
+{
+    const V3 forward = normalize(dst - eye);
+    const V3 ex = normalize(cross(forward, up));
+    const V3 ey = normalize(cross(forward, ex));
+    const float y_len = 2 * std::tan(0.5f * fov_y_deg * PI / 180);
+    const float x_len = w_over_h * y_len;
+    Camera c;
+    c.eye = eye;
+    c.lbc = eye + forward - 0.5f * (x_len * ex + y_len * ey);
+    c.film_x = x_len * ex;
+    c.film_y = y_len * ey;
+    return c;
+}
+
+// ---------------------------------------------------------------- OBJ loading
+
+namespace {
+
+struct ObjIndex { int v, vt, vn; };
+
+inline const char *skip_spaces(const char *p)
+{
+    while(*p == ' ' || *p == '\t')
+        ++p;
+    return p;
+}
+
+bool parse_obj_index(const char *&p, ObjIndex &out)
+{
+    out = { 0, 0, 0 };
+    char *end;
+    long v = std::strtol(p, &end, 10);
+    if(end == p)
+        return false;
+    out.v = static_cast<int>(v);
+    p = end;
+    if(*p == '/')
+    {
+        ++p;
+        if(*p != '/')
+        {
+            long t = std::strtol(p, &end, 10);
+            if(end != p)
+            {
+                out.vt = static_cast<int>(t);
+                p = end;
+            }
+        }
+        if(*p == '/')
+        {
+            ++p;
+            long n = std::strtol(p, &end, 10);
+            if(end != p)
+            {
+                out.vn = static_cast<int>(n);
+                p = end;
+            }
+        }
+    }
+    return true;
+}
+
+inline int resolve_obj(int idx, size_t count)
+{
+    // 1-based positive, or negative relative to the end; 0 means absent
+    if(idx > 0)
+        return idx - 1;
+    if(idx < 0)
+        return static_cast<int>(count) + idx;
+    return -1;
+}
+
+// common/btrc/utils/math/triangle.h: triangle_dpdu
+V3 triangle_dpdu(V3 B_A, V3 C_A, float bax, float bay, float cax, float cay, V3 nor)
+{
+    const float m00 = bax, m01 = bay, m10 = cax, m11 = cay;
+    const float det = m00 * m11 - m01 * m10;
+    if(det == 0.0f)
+        return Frame::from_z(nor).x;
+    const float inv_det = 1 / det;
+    return normalize(m11 * inv_det * B_A - m01 * inv_det * C_A);
+}
+
+} // namespace
+
+HostGeometry load_obj(const std::string &filename, bool to_unit_cube)
+{
+    std::ifstream fin(filename, std::ios::binary);
+    if(!fin)
+        throw std::runtime_error("cannot open obj file '" + filename + "'");
+    std::string text((std::istreambuf_iterator<char>(fin)), std::istreambuf_iterator<char>());
+
+    std::vector<V3> positions, normals;
+    std::vector<float> uvs;
+    std::vector<ObjIndex> corners;  // 3 per triangle, already resolved to 0-based (-1 absent)
+    positions.reserve(text.size() / 64);
+    corners.reserve(text.size() / 16);
+
+    const char *p = text.c_str();
+    const char *end = p + text.size();
+    std::vector<ObjIndex> face;
+    while(p < end)
+    {
+        const char *line = skip_spaces(p);
+        const char *eol = static_cast<const char *>(std::memchr(line, '\n', end - line));
+        if(!eol)
+            eol = end;
+        if(line[0] == 'v' && (line[1] == ' ' || line[1] == '\t'))
+        {
+            char *e;
+            float x = std::strtof(line + 2, &e);
+            float y = std::strtof(e, &e);
+            float z = std::strtof(e, &e);
+            positions.emplace_back(x, y, z);
+        }
+        else if(line[0] == 'v' && line[1] == 'n')
+        {
+            char *e;
+            float x = std::strtof(line + 3, &e);
+            float y = std::strtof(e, &e);
+            float z = std::strtof(e, &e);
+            normals.emplace_back(x, y, z);
+        }
+        else if(line[0] == 'v' && line[1] == 't')
+        {
+            char *e;
+            float u = std::strtof(line + 3, &e);
+            float v = std::strtof(e, &e);
+            uvs.push_back(u);
+            uvs.push_back(v);
+        }
+        else if(line[0] == 'f' && (line[1] == ' ' || line[1] == '\t'))
+        {
+            face.clear();
+            const char *q = line + 2;
+            for(;;)
+            {
+                q = skip_spaces(q);
+                if(q >= eol || *q == '\r' || *q == '\n')
+                    break;
+                ObjIndex oi;
+                if(!parse_obj_index(q, oi))
+                    throw std::runtime_error("bad face in obj file '" + filename + "'");
+                oi.v = resolve_obj(oi.v, positions.size());
+                oi.vt = resolve_obj(oi.vt, uvs.size() / 2);
+                oi.vn = resolve_obj(oi.vn, normals.size());
+                face.push_back(oi);
+            }
+            if(face.size() < 3)
+                throw std::runtime_error("invalid obj face vertex count in '" + filename + "'");
+            for(size_t k = 1; k + 1 < face.size(); ++k)
+            {
+                corners.push_back(face[0]);
+                corners.push_back(face[k]);
+                corners.push_back(face[k + 1]);
+            }
+        }
+        p = eol + 1;
+    }
+
+    for(auto &c : corners)
+    {
+        if(c.v < 0 || static_cast<size_t>(c.v) >= positions.size())
+            throw std::runtime_error("invalid obj vertex index: out of range");
+        if(c.vn >= 0 && static_cast<size_t>(c.vn) >= normals.size())
+            throw std::runtime_error("invalid obj normal index: out of range");
+        if(c.vt >= 0 && static_cast<size_t>(c.vt) * 2 + 1 >= uvs.size())
+            throw std::runtime_error("invalid obj tex coord index: out of range");
+    }
+
+    if(to_unit_cube && !positions.empty())
+    {
+        // common/btrc/utils/triangle_mesh_loader.cpp:195-213
+        V3 lo(MAX_FLOAT), hi(-MAX_FLOAT);
+        for(auto &q : positions)
+        {
+            lo = vmin(lo, q);
+            hi = vmax(hi, q);
+        }
+        const V3 ext = hi - lo;
+        const float emax = std::max(ext.x, std::max(ext.y, ext.z));
+        const float s = emax > 0 ? 1 / emax : 1.0f;
+        for(auto &q : positions)
+            q = s * (q - 0.5f * (lo + hi));
+    }
+
+    HostGeometry g;
+    g.filename = filename;
+    const size_t ntri = corners.size() / 3;
+    g.pos.resize(ntri * 3);
+    for(auto &s : g.shade)
+        s.resize(ntri);
+    g.area.resize(ntri);
+    g.bmin = V3(MAX_FLOAT);
+    g.bmax = V3(-MAX_FLOAT);
+    for(auto &q : positions)
+    {
+        g.bmin = vmin(g.bmin, q);
+        g.bmax = vmax(g.bmax, q);
+    }
+    double total = 0;
+    for(size_t i = 0; i < ntri; ++i)
+    {
+        const ObjIndex *c = &corners[i * 3];
+        const V3 a = positions[c[0].v], b = positions[c[1].v], cc = positions[c[2].v];
+        g.pos[i * 3 + 0] = a;
+        g.pos[i * 3 + 1] = b;
+        g.pos[i * 3 + 2] = cc;
+        const V3 geo_z = normalize(cross(b - a, cc - a));
+        V3 sz[3];
+        float tu[3], tv[3];
+        for(int k = 0; k < 3; ++k)
+        {
+            if(c[k].vn < 0)
+                sz[k] = geo_z;
+            else
+            {
+                sz[k] = normals[c[k].vn];
+                if(sz[k].x == 0.0f && sz[k].y == 0.0f && sz[k].z == 0.0f)
+                    sz[k] = geo_z;
+            }
+            if(c[k].vt < 0)
+            {
+                tu[k] = 0;
+                tv[k] = 0;
+            }
+            else
+            {
+                tu[k] = uvs[c[k].vt * 2];
+                tv[k] = uvs[c[k].vt * 2 + 1];
+            }
+        }
+        const V3 gx = triangle_dpdu(b - a, cc - a, tu[1] - tu[0], tv[1] - tv[0],
+                                    tu[2] - tu[0], tv[2] - tv[0], geo_z);
+        const V3 gz = geo_z;
+        const V3 gy = normalize(cross(gz, gx));
+        g.shade[0][i] = { gx.x, gx.y, gx.z, tu[0] };
+        g.shade[1][i] = { gy.x, gy.y, gy.z, tu[1] - tu[0] };
+        g.shade[2][i] = { gz.x, gz.y, gz.z, tu[2] - tu[0] };
+        g.shade[3][i] = { sz[0].x, sz[0].y, sz[0].z, tv[0] };
+        const V3 sba = sz[1] - sz[0], sca = sz[2] - sz[0];
+        g.shade[4][i] = { sba.x, sba.y, sba.z, tv[1] - tv[0] };
+        g.shade[5][i] = { sca.x, sca.y, sca.z, tv[2] - tv[0] };
+        g.area[i] = 0.5f * length(cross(b - a, cc - a));
+        total += g.area[i];
+    }
+    g.total_area = static_cast<float>(total);
+    return g;
+}
+
+// ---------------------------------------------------------------- scene file
+
+namespace {
+
+using json::NodeP;
+
+std::string resolve_path(const std::string &p, const std::string &scene_dir)
+{
+    std::string r = p;
+    const std::string key = "$env{scene_directory}";
+    for(size_t k = r.find(key); k != std::string::npos; k = r.find(key))
+        r.replace(k, key.size(), scene_dir);
+    std::filesystem::path fp(r);
+    if(fp.is_relative())
+        fp = std::filesystem::absolute(fp);
+    return fp.lexically_normal().string();
+}
+
+float tex_float(const NodeP &n, float def_if_null)
+{
+    if(!n)
+        return def_if_null;
+    if(n->is_value() || n->is_array())
+        return json::as_spectrum(n).x;  // Constant2D::sample_float returns .r
+    const std::string type = json::as_string(n->child("type"));
+    if(type == "constant")
+        return json::as_spectrum(n->child("value")).x;
+    throw std::runtime_error("unsupported texture2d type '" + type + "' (only constant textures)");
+}
+
+V3 tex_spectrum(const NodeP &n)
+{
+    if(n->is_value() || n->is_array())
+        return json::as_spectrum(n);
+    const std::string type = json::as_string(n->child("type"));
+    if(type == "constant")
+        return json::as_spectrum(n->child("value"));
+    throw std::runtime_error("unsupported texture2d type '" + type + "' (only constant textures)");
+}
+
+Material make_material(const NodeP &n)
+{
+    Material m{};
+    const std::string type = json::as_string(n->child("type"));
+    m.shadow_terminator = json::bool_or(n, "shadow_terminator_term", true) ? 1 : 0;
+    if(n->find("normal_map") || n->find("normal"))
+    {
+        // normal maps need image textures, which are not supported yet
+        auto nm = n->find("normal_map") ? n->find("normal_map") : n->find("normal");
+        if(!nm->is_value() || !nm->str.empty())
+            throw std::runtime_error("normal maps are not supported");
+    }
+    if(type == "diffuse")
+    {
+        m.type = MAT_DIFFUSE;
+        const V3 c = tex_spectrum(n->child("color"));
+        m.p[0] = c.x; m.p[1] = c.y; m.p[2] = c.z;
+    }
+    else if(type == "metal")
+    {
+        m.type = MAT_METAL;
+        const V3 c = tex_spectrum(n->child("color"));
+        m.p[0] = c.x; m.p[1] = c.y; m.p[2] = c.z;
+        m.p[3] = tex_float(n->child("roughness"), 0);
+        m.p[4] = tex_float(n->find("anisotropic"), 0);
+    }
+    else if(type == "disney")
+    {
+        // builtin/btrc/builtin/material/disney.cpp:844-894 creator defaults
+        m.type = MAT_DISNEY;
+        const V3 c = tex_spectrum(n->child("color"));
+        m.p[0] = c.x; m.p[1] = c.y; m.p[2] = c.z;
+        m.p[3] = tex_float(n->child("metallic"), 0);
+        m.p[4] = tex_float(n->child("roughness"), 0);
+        m.p[5] = tex_float(n->find("specular"), 1);
+        m.p[6] = tex_float(n->find("specular_tint"), 0);
+        m.p[7] = tex_float(n->find("anisotropic"), 0);
+        m.p[8] = tex_float(n->find("sheen"), 0);
+        m.p[9] = tex_float(n->find("sheen_tint"), 0);
+        m.p[10] = tex_float(n->find("clearcoat"), 0);
+        m.p[11] = tex_float(n->find("clearcoat_gloss"), 1);
+        m.p[12] = tex_float(n->find("transmission"), 0);
+        m.p[13] = n->find("transmission_roughness") ? tex_float(n->find("transmission_roughness"), 0) : m.p[4];
+        m.p[14] = tex_float(n->find("ior"), 1.5f);
+    }
+    else if(type == "black")
+        m.type = MAT_BLACK;
+    else if(type == "invisible")
+        m.type = MAT_INVISIBLE;
+    else if(type == "mirror")
+    {
+        m.type = MAT_MIRROR;
+        const V3 c = tex_spectrum(n->child("color"));
+        m.p[0] = c.x; m.p[1] = c.y; m.p[2] = c.z;
+    }
+    else
+        throw std::runtime_error("unsupported material type '" + type + "'");
+    return m;
+}
+
+struct GridData
+{
+    int w = 1, h = 1, d = 1;
+    std::vector<float> v;
+    float constant = 0;
+    bool is_constant = true;
+};
+
+// Texture3D: constant value / array of 1 or 3, {"type":"constant","value":...} or
+// {"type":"array","text":file} (common/btrc/utils/cuda/array.cpp:313-384, channel 0 only),
+// plus {"type":"array","binary":file}: raw header "BTG1" int32 w h d then float32 x-fastest.
+GridData load_texture3d(const NodeP &n, const std::string &scene_dir)
+{
+    GridData g;
+    if(n->is_value() || n->is_array())
+    {
+        g.constant = json::as_spectrum(n).x;
+        return g;
+    }
+    const std::string type = json::as_string(n->child("type"));
+    if(type == "constant")
+    {
+        g.constant = json::as_spectrum(n->child("value")).x;
+        return g;
+    }
+    if(type != "array")
+        throw std::runtime_error("unsupported texture3d type '" + type + "'");
+    g.is_constant = false;
+    if(auto b = n->find("binary"))
+    {
+        const std::string fn = resolve_path(json::as_string(b), scene_dir);
+        std::ifstream f(fn, std::ios::binary);
+        if(!f)
+            throw std::runtime_error("failed to open file: " + fn);
+        char magic[4];
+        int32_t dims[3];
+        f.read(magic, 4);
+        f.read(reinterpret_cast<char *>(dims), sizeof(dims));
+        if(!f || std::memcmp(magic, "BTG1", 4) != 0 || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0)
+            throw std::runtime_error("bad binary grid header: " + fn);
+        g.w = dims[0]; g.h = dims[1]; g.d = dims[2];
+        g.v.resize(static_cast<size_t>(g.w) * g.h * g.d);
+        f.read(reinterpret_cast<char *>(g.v.data()), g.v.size() * sizeof(float));
+        if(!f)
+            throw std::runtime_error("truncated binary grid: " + fn);
+        return g;
+    }
+    const std::string fn = resolve_path(json::as_string(n->child("text")), scene_dir);
+    std::ifstream f(fn);
+    if(!f)
+        throw std::runtime_error("failed to open file: " + fn);
+    std::string comp;
+    int ch;
+    f >> comp >> ch >> g.w >> g.h >> g.d;
+    if(!f || (ch != 1 && ch != 3 && ch != 4) || g.w <= 0 || g.h <= 0 || g.d <= 0)
+        throw std::runtime_error("Array::load_from_text: failed to parse file head");
+    g.v.resize(static_cast<size_t>(g.w) * g.h * g.d);
+    for(size_t i = 0; i < g.v.size(); ++i)
+    {
+        for(int c = 0; c < ch; ++c)
+        {
+            float val;
+            if(comp == "float")
+                f >> val;
+            else if(comp == "byte")
+            {
+                int b;
+                f >> b;
+                val = static_cast<float>(b) / 127.0f;
+            }
+            else
+                throw std::runtime_error("unknown component type: " + comp);
+            if(c == 0)
+                g.v[i] = val;
+        }
+    }
+    if(!f)
+        throw std::runtime_error("failed to load " + fn);
+    return g;
+}
+
+struct MediumBuilder
+{
+    std::string scene_dir;
+    std::vector<HostMedium> media;
+    std::map<const json::Node *, int> pool;
+
+    int create(const NodeP &n)
+    {
+        auto it = pool.find(n.get());
+        if(it != pool.end())
+            return it->second;
+        HostMedium m{};
+        build(n, Transform{}, false, m);
+        media.push_back(std::move(m));
+        const int id = static_cast<int>(media.size()) - 1;
+        pool[n.get()] = id;
+        return id;
+    }
+
+    void build(const NodeP &n, const Transform &w2l, bool has_xf, HostMedium &m)
+    {
+        const std::string type = json::as_string(n->child("type"));
+        if(type == "transform")
+        {
+            Transform t;
+            if(auto tn = n->find("world_to_local"))
+                t = parse_transform(tn);
+            else
+            {
+                Transform l2w = parse_transform(n->child("local_to_world"));
+                t.mat = l2w.inv;
+                t.inv = l2w.mat;
+            }
+            // nested transforms compose: the outer one is applied first
+            build(n->child("medium"), has_xf ? t * w2l : t, true, m);
+            return;
+        }
+        float l2w_a[12], w2l_a[12];
+        w2l.to_affine(w2l_a, l2w_a);
+        std::memcpy(m.dev.w2l, w2l_a, sizeof(w2l_a));
+        std::memcpy(m.dev.l2w, l2w_a, sizeof(l2w_a));
+        m.dev.priority = static_cast<int32_t>(json::float_or(n, "priority", 0.0f));
+        if(type == "homogeneous")
+        {
+            m.dev.type = MED_HOMOGENEOUS;
+            m.dev.sigma_t_const = json::as_float(n->child("sigma_t"));
+            const V3 a = json::as_spectrum(n->child("albedo"));
+            m.dev.albedo[0] = a.x; m.dev.albedo[1] = a.y; m.dev.albedo[2] = a.z;
+            m.dev.g = json::float_or(n, "g", 0.0f);
+        }
+        else if(type == "hetergeneous" || type == "heterogeneous")
+        {
+            m.dev.type = MED_HETEROGENEOUS;
+            GridData sig = load_texture3d(n->child("sigma_t"), scene_dir);
+            GridData alb = load_texture3d(n->child("albedo"), scene_dir);
+            if(!alb.is_constant)
+                throw std::runtime_error("only constant medium albedo is supported");
+            const V3 a = n->child("albedo")->is_group() && n->child("albedo")->find("value")
+                             ? json::as_spectrum(n->child("albedo")->child("value"))
+                             : (n->child("albedo")->is_group() ? V3(alb.constant) : json::as_spectrum(n->child("albedo")));
+            m.dev.albedo[0] = a.x; m.dev.albedo[1] = a.y; m.dev.albedo[2] = a.z;
+            if(auto gn = n->find("g"))
+            {
+                GridData gg = load_texture3d(gn, scene_dir);
+                if(!gg.is_constant)
+                    throw std::runtime_error("only constant phase g is supported");
+                m.dev.g = gg.constant;
+            }
+            if(sig.is_constant)
+            {
+                m.grid.assign(1, sig.constant);
+                m.dev.res_x = m.dev.res_y = m.dev.res_z = 1;
+            }
+            else
+            {
+                m.grid = std::move(sig.v);
+                m.dev.res_x = sig.w; m.dev.res_y = sig.h; m.dev.res_z = sig.d;
+            }
+            float mx = 0;
+            for(float v : m.grid)
+                mx = std::max(mx, v);
+            m.dev.sigma_max = std::max(mx, 0.001f);
+        }
+        else
+            throw std::runtime_error("unsupported medium type '" + type + "'");
+    }
+};
+
+} // namespace
+
+HostScene load_scene(const std::string &path)
+{
+    HostScene S;
+    S.path = path;
+    const std::string scene_dir = std::filesystem::absolute(std::filesystem::path(path)).parent_path().string();
+    NodeP root = json::parse_scene_file(path, scene_dir);
+
+    S.params.width = json::as_int(root->child("width"));
+    S.params.height = json::as_int(root->child("height"));
+    if(S.params.width <= 0 || S.params.height <= 0 || S.params.width > 65535 || S.params.height > 65535)
+        throw std::runtime_error("film size out of range");
+
+    // camera (builtin/btrc/builtin/camera/pinhole.cpp:101-114)
+    {
+        NodeP cam = root->child("camera");
+        const std::string type = json::as_string(cam->child("type"));
+        if(type != "pinhole")
+            throw std::runtime_error("unsupported camera type '" + type + "'");
+        S.camera = make_pinhole(json::as_vec3(cam->child("eye")), json::as_vec3(cam->child("dst")),
+                                json::as_vec3(cam->child("up")), json::as_degree(cam->child("fov_y")),
+                                static_cast<float>(S.params.width) / S.params.height);
+    }
+
+    // renderer (builtin/btrc/builtin/renderer/wavefront.cpp:375-397)
+    {
+        NodeP r = root->child("renderer");
+        RenderParams &P = S.params;
+        P.renderer_type = json::as_string(r->child("type"));
+        if(P.renderer_type != "wfpt" && P.renderer_type != "pt")
+            throw std::runtime_error("unsupported renderer type '" + P.renderer_type + "'");
+        P.tile = json::bool_or(r, "tile", P.tile);
+        P.spp = json::int_or(r, "spp", P.spp);
+        P.min_depth = json::int_or(r, "min_depth", P.min_depth);
+        P.max_depth = json::int_or(r, "max_depth", P.max_depth);
+        P.rr_threshold = json::float_or(r, "rr_threshold", P.rr_threshold);
+        P.rr_cont_prob = json::float_or(r, "rr_cont_prob", P.rr_cont_prob);
+        P.state_count = json::int_or(r, "state_count", P.state_count);
+        P.albedo = json::bool_or(r, "albedo", P.albedo);
+        P.normal = json::bool_or(r, "normal", P.normal);
+        if(P.spp <= 0 || P.state_count <= 0)
+            throw std::runtime_error("spp and state_count must be positive");
+        if(auto f = r->find("filter"))
+        {
+            const std::string ft = json::as_string(f->child("type"));
+            if(ft == "box")
+                P.filter = FILTER_BOX;
+            else if(ft == "gaussian")
+            {
+                P.filter = FILTER_GAUSSIAN;
+                P.filter_radius = json::float_or(f, "radius", 1.3f);
+                P.filter_alpha = json::float_or(f, "alpha", 1.6f);
+            }
+            else
+                throw std::runtime_error("unsupported filter type '" + ft + "'");
+        }
+        if(auto s = r->find("sampler"))
+        {
+            const std::string st = s->is_group() ? json::as_string(s->child("type")) : json::as_string(s);
+            if(st == "independent")
+                P.sampler = SAMPLER_INDEPENDENT;
+            else if(st == "halton")
+                P.sampler = SAMPLER_HALTON;
+            else
+                throw std::runtime_error("unsupported sampler type '" + st + "'");
+        }
+    }
+
+    // scene entities (factory/btrc/factory/scene.cpp:9-55)
+    NodeP scene = root->child("scene");
+    NodeP ents = scene->child("entities");
+    if(!ents->is_array())
+        throw std::runtime_error("entity array expected");
+
+    std::map<const json::Node *, int> geo_pool, mat_pool;
+    MediumBuilder mb;
+    mb.scene_dir = scene_dir;
+    struct PendingInstance { int geo, mat, light; int inner, outer; Transform xf; V3 intensity; };
+    std::vector<PendingInstance> pend;
+    for(auto &e : ents->elems)
+    {
+        if(!e->is_group())
+            throw std::runtime_error("entity group expected");
+        PendingInstance pi{};
+        NodeP gn = e->child("geometry");
+        auto git = geo_pool.find(gn.get());
+        if(git == geo_pool.end())
+        {
+            const std::string gt = json::as_string(gn->child("type"));
+            if(gt != "triangle_mesh")
+                throw std::runtime_error("unsupported geometry type '" + gt + "'");
+            const std::string fn = resolve_path(json::as_string(gn->child("filename")), scene_dir);
+            S.geometries.push_back(load_obj(fn, json::bool_or(gn, "transform_to_unit_cube", false)));
+            pi.geo = static_cast<int>(S.geometries.size()) - 1;
+            geo_pool[gn.get()] = pi.geo;
+        }
+        else
+            pi.geo = git->second;
+        NodeP mn = e->child("material");
+        auto mit = mat_pool.find(mn.get());
+        if(mit == mat_pool.end())
+        {
+            S.materials.push_back(make_material(mn));
+            pi.mat = static_cast<int>(S.materials.size()) - 1;
+            mat_pool[mn.get()] = pi.mat;
+        }
+        else
+            pi.mat = mit->second;
+        if(auto tn = e->find("local_to_world"))
+            pi.xf = parse_transform(tn);
+        pi.inner = e->find("inner_medium") ? mb.create(e->find("inner_medium")) : -1;
+        pi.outer = e->find("outer_medium") ? mb.create(e->find("outer_medium")) : -1;
+        pi.light = -1;
+        if(auto ln = e->find("light"))
+        {
+            const std::string lt = json::as_string(ln->child("type"));
+            if(lt != "mesh_light")
+                throw std::runtime_error("area light expected");
+            pi.light = 1;
+            pi.intensity = json::as_spectrum(ln->child("intensity"));
+        }
+        pend.push_back(pi);
+    }
+    if(auto vols = scene->find("volumes"))
+    {
+        if(!vols->is_array())
+            throw std::runtime_error("'volumes' is not an array node");
+        if(!vols->elems.empty())
+            throw std::runtime_error("volume primitives are not supported yet");
+    }
+    if(auto en = scene->find("envir_light"))
+    {
+        const std::string et = json::as_string(en->child("type"));
+        if(et != "gradient_sky")
+            throw std::runtime_error("unsupported environment light '" + et + "'");
+        S.env.type = ENV_GRADIENT_SKY;
+        const V3 up = normalize(json::as_vec3(en->child("up")));
+        const V3 lo = json::as_spectrum(en->child("lower"));
+        const V3 hi = json::as_spectrum(en->child("upper"));
+        S.env.lower[0] = lo.x; S.env.lower[1] = lo.y; S.env.lower[2] = lo.z;
+        S.env.upper[0] = hi.x; S.env.upper[1] = hi.y; S.env.upper[2] = hi.z;
+        S.env.up[0] = up.x; S.env.up[1] = up.y; S.env.up[2] = up.z;
+    }
+
+    // medium id table (core/btrc/core/scene.cpp:136-161): media sorted by priority
+    // descending (stable), the volume-primitive medium (vacuum here) last; entities
+    // without a medium refer to it.
+    {
+        std::vector<int> order(mb.media.size());
+        std::iota(order.begin(), order.end(), 0);
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+            return mb.media[a].dev.priority > mb.media[b].dev.priority;
+        });
+        std::vector<int> remap(mb.media.size());
+        for(size_t i = 0; i < order.size(); ++i)
+        {
+            remap[order[i]] = static_cast<int>(i);
+            S.media.push_back(std::move(mb.media[order[i]]));
+        }
+        HostMedium vac{};
+        vac.dev.type = MED_VACUUM;
+        vac.dev.priority = -(1 << 30);
+        S.media.push_back(vac);
+        S.vacuum_medium = static_cast<int>(S.media.size()) - 1;
+        for(auto &pi : pend)
+        {
+            pi.inner = pi.inner < 0 ? S.vacuum_medium : remap[pi.inner];
+            pi.outer = pi.outer < 0 ? S.vacuum_medium : remap[pi.outer];
+        }
+    }
+
+    // instances and lights in entity order (core/btrc/core/scene.cpp:92-101, 163-190)
+    int next_light = 0;
+    for(size_t i = 0; i < pend.size(); ++i)
+    {
+        auto &pi = pend[i];
+        Instance inst{};
+        pi.xf.to_affine(inst.l2w, inst.w2l);
+        inst.geometry = pi.geo;
+        inst.material = pi.mat;
+        inst.light = -1;
+        inst.media = static_cast<uint32_t>(pi.inner) | (static_cast<uint32_t>(pi.outer) << 16);
+        if(pi.light >= 0)
+        {
+            inst.light = next_light++;
+            AreaLight L{};
+            L.instance = static_cast<int>(i);
+            L.geometry = pi.geo;
+            // builtin/btrc/builtin/light/mesh_light.cpp:10-15
+            L.scale = length(pi.xf.point(V3(1, 0, 0)) - pi.xf.point(V3(0, 0, 0)));
+            L.intensity[0] = pi.intensity.x; L.intensity[1] = pi.intensity.y; L.intensity[2] = pi.intensity.z;
+            S.area_lights.push_back(L);
+        }
+        S.instances.push_back(inst);
+        S.instance_xf.push_back(pi.xf);
+        S.triangle_count += S.geometries[pi.geo].area.size();
+    }
+
+    // world bounds (core/btrc/core/scene.cpp:224-236) from transformed geometry boxes
+    S.world_min = V3(MAX_FLOAT);
+    S.world_max = V3(-MAX_FLOAT);
+    for(size_t i = 0; i < S.instances.size(); ++i)
+    {
+        const HostGeometry &g = S.geometries[S.instances[i].geometry];
+        if(g.area.empty())
+            continue;
+        for(int c = 0; c < 8; ++c)
+        {
+            const V3 p((c & 1) ? g.bmax.x : g.bmin.x, (c & 2) ? g.bmax.y : g.bmin.y, (c & 4) ? g.bmax.z : g.bmin.z);
+            const V3 w = S.instance_xf[i].point(p);
+            S.world_min = vmin(S.world_min, w);
+            S.world_max = vmax(S.world_max, w);
+        }
+    }
+    if(S.world_min.x > S.world_max.x)
+    {
+        S.world_min = V3(0);
+        S.world_max = V3(0);
+    }
+    return S;
+}
+
+} // namespace bt

@@ -1,0 +1,342 @@
+// 8-wide compressed-BVH traversal for sm_103a (closest hit and any hit).
+//
+// Node groups: a traversal entry is (base index, bit mask). Bits 24..31 mark child
+// nodes still to visit (their slot XOR the ray octant, so the highest set bit is
+// roughly the nearest child), bits 0..23 mark triangles of the current node. One
+// group is pushed per tree level at most, so the per-thread stack needs no more
+// entries than the tree has levels (the builder guarantees <= TRAVERSAL_STACK_SIZE).
+//
+// Triangle test: watertight ray/triangle intersection (Woop, Benthin, Wald, JCGT 2013)
+// in FP32 with every multiply/add written as an explicitly rounded intrinsic, so the
+// CPU oracle (compiled without FP contraction) reproduces t and the barycentrics bit
+// for bit. Candidate order is a strict total order on (t, instance, primitive), which
+// makes the closest hit independent of traversal order. Box tests are conservative:
+// quantised boxes round outwards and the box interval is widened by 2^-20 relative.
+#pragma once
+
+#include <cstdint>
+
+#include "bmath.h"
+#include "layout.h"
+
+namespace bt {
+
+constexpr int STACK_SIZE = 32;
+constexpr float BOX_EPS = 1.0f + 1.0f / 1048576.0f;
+
+struct TravRay
+{
+    float ox, oy, oz;
+    float dx, dy, dz;
+    float idx, idy, idz;   // reciprocal direction, zero components replaced by +-1e-20
+    uint32_t oct_inv;      // 7 - octant, octant bit k set when d[k] < 0
+    int kx, ky, kz;        // watertight axis permutation
+    float Sx, Sy, Sz;      // watertight shear
+};
+
+__device__ __forceinline__ float pick3(float x, float y, float z, int k)
+{
+    return k == 0 ? x : (k == 1 ? y : z);
+}
+
+__device__ __forceinline__ TravRay make_trav_ray(float ox, float oy, float oz, float dx, float dy, float dz)
+{
+    TravRay r;
+    r.ox = ox; r.oy = oy; r.oz = oz;
+    r.dx = dx; r.dy = dy; r.dz = dz;
+    const float tiny = 1e-20f;
+    const float sx = fabsf(dx) < tiny ? copysignf(tiny, dx) : dx;
+    const float sy = fabsf(dy) < tiny ? copysignf(tiny, dy) : dy;
+    const float sz = fabsf(dz) < tiny ? copysignf(tiny, dz) : dz;
+    r.idx = 1.0f / sx;
+    r.idy = 1.0f / sy;
+    r.idz = 1.0f / sz;
+    const uint32_t octant = (dx < 0.0f ? 1u : 0u) | (dy < 0.0f ? 2u : 0u) | (dz < 0.0f ? 4u : 0u);
+    r.oct_inv = 7u - octant;
+
+    const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
+    int kz = (ax >= ay) ? ((ax >= az) ? 0 : 2) : ((ay >= az) ? 1 : 2);
+    int kx = kz + 1 == 3 ? 0 : kz + 1;
+    int ky = kx + 1 == 3 ? 0 : kx + 1;
+    const float dkz = pick3(dx, dy, dz, kz);
+    if(dkz < 0.0f)
+    {
+        const int t = kx;
+        kx = ky;
+        ky = t;
+    }
+    r.kx = kx; r.ky = ky; r.kz = kz;
+    r.Sx = __fdiv_rn(pick3(dx, dy, dz, kx), dkz);
+    r.Sy = __fdiv_rn(pick3(dx, dy, dz, ky), dkz);
+    r.Sz = __frcp_rn(dkz);
+    return r;
+}
+
+struct TriHit
+{
+    float t, b1, b2;
+};
+
+// Returns true and fills h when the ray crosses the triangle at 0 < t <= tmax.
+__device__ __forceinline__ bool watertight(const TravRay &r, float4 a, float4 b, float4 c, float tmax, TriHit &h)
+{
+    const float Axw = __fsub_rn(a.x, r.ox), Ayw = __fsub_rn(a.y, r.oy), Azw = __fsub_rn(a.z, r.oz);
+    const float Bxw = __fsub_rn(b.x, r.ox), Byw = __fsub_rn(b.y, r.oy), Bzw = __fsub_rn(b.z, r.oz);
+    const float Cxw = __fsub_rn(c.x, r.ox), Cyw = __fsub_rn(c.y, r.oy), Czw = __fsub_rn(c.z, r.oz);
+    const float Akx = pick3(Axw, Ayw, Azw, r.kx), Aky = pick3(Axw, Ayw, Azw, r.ky), Akz = pick3(Axw, Ayw, Azw, r.kz);
+    const float Bkx = pick3(Bxw, Byw, Bzw, r.kx), Bky = pick3(Bxw, Byw, Bzw, r.ky), Bkz = pick3(Bxw, Byw, Bzw, r.kz);
+    const float Ckx = pick3(Cxw, Cyw, Czw, r.kx), Cky = pick3(Cxw, Cyw, Czw, r.ky), Ckz = pick3(Cxw, Cyw, Czw, r.kz);
+
+    const float Ax = __fsub_rn(Akx, __fmul_rn(r.Sx, Akz));
+    const float Ay = __fsub_rn(Aky, __fmul_rn(r.Sy, Akz));
+    const float Bx = __fsub_rn(Bkx, __fmul_rn(r.Sx, Bkz));
+    const float By = __fsub_rn(Bky, __fmul_rn(r.Sy, Bkz));
+    const float Cx = __fsub_rn(Ckx, __fmul_rn(r.Sx, Ckz));
+    const float Cy = __fsub_rn(Cky, __fmul_rn(r.Sy, Ckz));
+
+    float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if(U == 0.0f || V == 0.0f || W == 0.0f)
+    {
+        // exact products of floats in FP64, one rounding for the difference
+        U = __double2float_rn(__dsub_rn(__dmul_rn((double)Cx, (double)By), __dmul_rn((double)Cy, (double)Bx)));
+        V = __double2float_rn(__dsub_rn(__dmul_rn((double)Ax, (double)Cy), __dmul_rn((double)Ay, (double)Cx)));
+        W = __double2float_rn(__dsub_rn(__dmul_rn((double)Bx, (double)Ay), __dmul_rn((double)By, (double)Ax)));
+    }
+    if((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f))
+        return false;
+    const float det = __fadd_rn(__fadd_rn(U, V), W);
+    if(det == 0.0f)
+        return false;
+    const float Az = __fmul_rn(r.Sz, Akz);
+    const float Bz = __fmul_rn(r.Sz, Bkz);
+    const float Cz = __fmul_rn(r.Sz, Ckz);
+    const float T = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
+    const float rcp = __frcp_rn(det);
+    const float t = __fmul_rn(T, rcp);
+    if(!(t > 0.0f && t <= tmax))
+        return false;
+    h.t = t;
+    h.b1 = __fmul_rn(V, rcp);
+    h.b2 = __fmul_rn(W, rcp);
+    return true;
+}
+
+__device__ __forceinline__ float byte_f(uint32_t w, int j)
+{
+    return static_cast<float>((w >> (8 * j)) & 0xffu);
+}
+
+// Intersects the 8 children of a node. Returns the hit mask: bits 24..31 child nodes
+// (slot ^ oct_inv), bits 0..23 triangles relative to tri_base.
+__device__ __forceinline__ uint32_t intersect_children(const TravRay &r, const float4 *__restrict__ nodes4,
+                                                      uint32_t ni, float tcur, uint32_t &child_base,
+                                                      uint32_t &tri_base, uint32_t &imask)
+{
+    const float4 n0 = __ldg(nodes4 + ni * 5 + 0);
+    const uint4 n1 = __ldg(reinterpret_cast<const uint4 *>(nodes4) + ni * 5 + 1);
+    const uint4 n2 = __ldg(reinterpret_cast<const uint4 *>(nodes4) + ni * 5 + 2);
+    const uint4 n3 = __ldg(reinterpret_cast<const uint4 *>(nodes4) + ni * 5 + 3);
+    const uint4 n4 = __ldg(reinterpret_cast<const uint4 *>(nodes4) + ni * 5 + 4);
+    const uint32_t ew = __float_as_uint(n0.w);
+    imask = ew >> 24;
+    child_base = n1.x;
+    tri_base = n1.y;
+    const float adjx = __uint_as_float((ew & 0xffu) << 23) * r.idx;
+    const float adjy = __uint_as_float(((ew >> 8) & 0xffu) << 23) * r.idy;
+    const float adjz = __uint_as_float(((ew >> 16) & 0xffu) << 23) * r.idz;
+    const float orgx = (n0.x - r.ox) * r.idx;
+    const float orgy = (n0.y - r.oy) * r.idy;
+    const float orgz = (n0.z - r.oz) * r.idz;
+    const bool nx = r.idx < 0.0f, ny = r.idy < 0.0f, nz = r.idz < 0.0f;
+
+    uint32_t hitmask = 0;
+#pragma unroll
+    for(int half = 0; half < 2; ++half)
+    {
+        const uint32_t meta4 = half ? n1.w : n1.z;
+        const uint32_t qlox = half ? n2.y : n2.x, qloy = half ? n2.w : n2.z, qloz = half ? n3.y : n3.x;
+        const uint32_t qhix = half ? n3.w : n3.z, qhiy = half ? n4.y : n4.x, qhiz = half ? n4.w : n4.z;
+        const uint32_t xn = nx ? qhix : qlox, xf = nx ? qlox : qhix;
+        const uint32_t yn = ny ? qhiy : qloy, yf = ny ? qloy : qhiy;
+        const uint32_t zn = nz ? qhiz : qloz, zf = nz ? qloz : qhiz;
+#pragma unroll
+        for(int j = 0; j < 4; ++j)
+        {
+            const uint32_t m = (meta4 >> (8 * j)) & 0xffu;
+            const float tnx = fmaf(byte_f(xn, j), adjx, orgx);
+            const float tny = fmaf(byte_f(yn, j), adjy, orgy);
+            const float tnz = fmaf(byte_f(zn, j), adjz, orgz);
+            const float tfx = fmaf(byte_f(xf, j), adjx, orgx);
+            const float tfy = fmaf(byte_f(yf, j), adjy, orgy);
+            const float tfz = fmaf(byte_f(zf, j), adjz, orgz);
+            const float tmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
+            const float tmax = fminf(fminf(tfx, tfy), fminf(tfz, tcur)) * BOX_EPS;
+            if(m != 0u && tmin <= tmax)
+            {
+                const bool inner = (m & 0x18u) == 0x18u;
+                const uint32_t bit = inner ? ((m & 0x1fu) ^ r.oct_inv) : (m & 0x1fu);
+                hitmask |= (m >> 5) << bit;
+            }
+        }
+    }
+    return hitmask;
+}
+
+// Lexicographic (t, inst, prim) comparison used for closest-hit ties.
+__device__ __forceinline__ bool closer(float t, uint32_t inst, uint32_t prim, float bt, uint32_t binst, uint32_t bprim)
+{
+    if(t != bt)
+        return t < bt;
+    if(inst != binst)
+        return inst < binst;
+    return prim < bprim;
+}
+
+struct ClosestResult
+{
+    float t, b1, b2;
+    uint32_t inst, prim;
+    bool hit;
+};
+
+// Closest hit in (0, t1]. err is set when the stack would overflow (never for trees
+// accepted by the builder).
+__device__ __forceinline__ ClosestResult trace_closest(const TravRay &r, float t1, const float4 *__restrict__ nodes4,
+                                                       const float4 *__restrict__ tris4, uint32_t node_count,
+                                                       uint32_t *err, uint32_t *stats_nodes = nullptr,
+                                                       uint32_t *stats_tris = nullptr)
+{
+    ClosestResult best;
+    best.hit = false;
+    best.t = t1;
+    best.b1 = best.b2 = 0.0f;
+    best.inst = best.prim = 0xffffffffu;
+    if(node_count == 0)
+        return best;
+
+    uint2 stack[STACK_SIZE];
+    int sp = 0;
+    uint2 ngroup = make_uint2(0u, 0x80000000u);
+    uint2 tgroup = make_uint2(0u, 0u);
+    uint32_t n_nodes = 0, n_tris = 0;
+    for(;;)
+    {
+        if(ngroup.y > 0x00ffffffu)
+        {
+            const int bit = 31 - __clz(ngroup.y);
+            const uint32_t slot = (static_cast<uint32_t>(bit) - 24u) ^ r.oct_inv;
+            const uint32_t rel = __popc(ngroup.y & ~(0xffffffffu << slot));
+            const uint32_t ni = ngroup.x + rel;
+            ngroup.y &= ~(1u << bit);
+            if(ngroup.y > 0x00ffffffu)
+            {
+                if(sp >= STACK_SIZE)
+                {
+                    atomicOr(err, 1u);
+                    break;
+                }
+                stack[sp++] = ngroup;
+            }
+            uint32_t cbase, tbase, imask;
+            const uint32_t hm = intersect_children(r, nodes4, ni, best.t, cbase, tbase, imask);
+            ++n_nodes;
+            ngroup = make_uint2(cbase, (hm & 0xff000000u) | imask);
+            tgroup = make_uint2(tbase, hm & 0x00ffffffu);
+        }
+        while(tgroup.y != 0u)
+        {
+            const int tb = 31 - __clz(tgroup.y);
+            tgroup.y &= ~(1u << tb);
+            const uint32_t ti = tgroup.x + static_cast<uint32_t>(tb);
+            const float4 a = __ldg(tris4 + ti * 3 + 0);
+            const float4 b = __ldg(tris4 + ti * 3 + 1);
+            const float4 c = __ldg(tris4 + ti * 3 + 2);
+            ++n_tris;
+            TriHit h;
+            if(watertight(r, a, b, c, best.t, h))
+            {
+                const uint32_t inst = __float_as_uint(a.w), prim = __float_as_uint(b.w);
+                if(!best.hit || closer(h.t, inst, prim, best.t, best.inst, best.prim))
+                {
+                    best.hit = true;
+                    best.t = h.t;
+                    best.b1 = h.b1;
+                    best.b2 = h.b2;
+                    best.inst = inst;
+                    best.prim = prim;
+                }
+            }
+        }
+        if(ngroup.y <= 0x00ffffffu)
+        {
+            if(sp == 0)
+                break;
+            ngroup = stack[--sp];
+        }
+    }
+    if(stats_nodes)
+    {
+        *stats_nodes = n_nodes;
+        *stats_tris = n_tris;
+    }
+    return best;
+}
+
+// Any hit in (0, t1].
+__device__ __forceinline__ bool trace_any(const TravRay &r, float t1, const float4 *__restrict__ nodes4,
+                                          const float4 *__restrict__ tris4, uint32_t node_count, uint32_t *err)
+{
+    if(node_count == 0)
+        return false;
+    uint2 stack[STACK_SIZE];
+    int sp = 0;
+    uint2 ngroup = make_uint2(0u, 0x80000000u);
+    uint2 tgroup = make_uint2(0u, 0u);
+    for(;;)
+    {
+        if(ngroup.y > 0x00ffffffu)
+        {
+            const int bit = 31 - __clz(ngroup.y);
+            const uint32_t slot = (static_cast<uint32_t>(bit) - 24u) ^ r.oct_inv;
+            const uint32_t rel = __popc(ngroup.y & ~(0xffffffffu << slot));
+            const uint32_t ni = ngroup.x + rel;
+            ngroup.y &= ~(1u << bit);
+            if(ngroup.y > 0x00ffffffu)
+            {
+                if(sp >= STACK_SIZE)
+                {
+                    atomicOr(err, 1u);
+                    return false;
+                }
+                stack[sp++] = ngroup;
+            }
+            uint32_t cbase, tbase, imask;
+            const uint32_t hm = intersect_children(r, nodes4, ni, t1, cbase, tbase, imask);
+            ngroup = make_uint2(cbase, (hm & 0xff000000u) | imask);
+            tgroup = make_uint2(tbase, hm & 0x00ffffffu);
+        }
+        while(tgroup.y != 0u)
+        {
+            const int tb = 31 - __clz(tgroup.y);
+            tgroup.y &= ~(1u << tb);
+            const uint32_t ti = tgroup.x + static_cast<uint32_t>(tb);
+            const float4 a = __ldg(tris4 + ti * 3 + 0);
+            const float4 b = __ldg(tris4 + ti * 3 + 1);
+            const float4 c = __ldg(tris4 + ti * 3 + 2);
+            TriHit h;
+            if(watertight(r, a, b, c, t1, h))
+                return true;
+        }
+        if(ngroup.y <= 0x00ffffffu)
+        {
+            if(sp == 0)
+                break;
+            ngroup = stack[--sp];
+        }
+    }
+    return false;
+}
+
+} // namespace bt

@@ -1,0 +1,358 @@
+"""Seeded synthetic scenes in Btrc's scene-JSON schema (OBJ geometry + JSON).
+
+The reference ships no scenes, so the benchmark and parity workloads are generated:
+
+  cornell  : closed box of unit cross-section (12 triangles in three entities, normals
+             facing inwards, deepened towards the camera), two level-3
+             icospheres (1280 triangles, radius 0.3) at seeded positions, a 0.25 x 0.25
+             quad light of radiance 15 under the ceiling, Lambertian albedos U[0.2, 0.8]^3,
+             pinhole 40 degrees, 256x256, 16 spp, max depth 8, Russian roulette from depth 3,
+             Halton sampler, Gaussian filter of radius 1.5.
+  terrain  : 1024x1024-vertex fBm heightfield (8 octaves, amplitude 0.2, lacunarity 2,
+             Perlin gradient noise), 200 instances of one level-4 icosphere, Disney
+             materials (base colour U[0,1]^3, roughness U[0.05,1], metallic Bernoulli(0.3),
+             specular 0.5, clearcoat U[0,1]), gradient sky + 8 quad lights, 1920x1080,
+             64 spp, depth 16.
+  volume   : the cornell box with a 256^3 fBm density grid (sigma_t max 20, albedo 0.9,
+             g 0.6) inside an invisible cube, plus a noise-displaced level-7 icosphere with
+             a GGX conductor of roughness 0.2; 1024x1024, 64 spp, depth 32.
+
+Every random choice draws from numpy's PCG64 seeded with the scene seed.
+"""
+from __future__ import annotations
+
+import json
+import os
+from pathlib import Path
+
+import numpy as np
+
+CACHE_ENV = "BTRC_SCENE_CACHE"
+
+
+def cache_dir() -> Path:
+    d = Path(os.environ.get(CACHE_ENV, "/tmp/btrc_gb300_scenes"))
+    d.mkdir(parents=True, exist_ok=True)
+    return d
+
+
+# ------------------------------------------------------------------ geometry helpers
+
+def icosphere(level: int) -> tuple[np.ndarray, np.ndarray]:
+    """Unit icosphere: (V, 3) float64 vertices and (F, 3) int faces, 20 * 4^level faces."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+         (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+         (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    verts = [np.array(p, np.float64) / np.linalg.norm(p) for p in v]
+    faces = list(f)
+    for _ in range(level):
+        cache: dict[tuple[int, int], int] = {}
+
+        def mid(a: int, b: int) -> int:
+            key = (a, b) if a < b else (b, a)
+            if key not in cache:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                cache[key] = len(verts) - 1
+            return cache[key]
+
+        nf = []
+        for a, b, c in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = nf
+    return np.array(verts), np.array(faces, np.int64)
+
+
+def write_obj(path: Path, verts: np.ndarray, faces: np.ndarray, normals: np.ndarray | None = None) -> None:
+    """OBJ with 1-based indices; with normals, faces are written as a//a."""
+    verts = np.asarray(verts, np.float64)
+    faces = np.asarray(faces, np.int64) + 1
+    parts = [("v %.7g %.7g %.7g\n" * len(verts)) % tuple(verts.ravel())]
+    if normals is not None:
+        normals = np.asarray(normals, np.float64)
+        parts.append(("vn %.6g %.6g %.6g\n" * len(normals)) % tuple(normals.ravel()))
+        ff = np.repeat(faces, 2, axis=1)
+        parts.append(("f %d//%d %d//%d %d//%d\n" * len(faces)) % tuple(ff.ravel()))
+    else:
+        parts.append(("f %d %d %d\n" * len(faces)) % tuple(faces.ravel()))
+    tmp = path.with_suffix(path.suffix + ".tmp")
+    with open(tmp, "w") as fobj:
+        for p in parts:
+            fobj.write(p)
+    os.replace(tmp, path)
+
+
+def quad(size: float = 1.0) -> tuple[np.ndarray, np.ndarray]:
+    """Square in the xz plane, centred at the origin, normal +y."""
+    h = size / 2
+    v = np.array([[-h, 0, -h], [h, 0, -h], [h, 0, h], [-h, 0, h]], np.float64)
+    f = np.array([[0, 2, 1], [0, 3, 2]], np.int64)
+    return v, f
+
+
+def flip(faces: np.ndarray) -> np.ndarray:
+    return faces[:, [0, 2, 1]]
+
+
+def box_inward(lo, hi) -> tuple[np.ndarray, np.ndarray]:
+    """Closed axis-aligned box [lo, hi] of 12 triangles with normals facing inwards.
+    Faces in order: x-, x+, y-, y+, z-, z+ (two triangles each)."""
+    v = np.array([[x, y, z] for x in (lo[0], hi[0]) for y in (lo[1], hi[1]) for z in (lo[2], hi[2])], np.float64)
+    # vertex index = 4*ix + 2*iy + iz
+    quads = [
+        (0, 1, 3, 2),  # x = -h
+        (4, 6, 7, 5),  # x = +h
+        (0, 4, 5, 1),  # y = -h
+        (2, 3, 7, 6),  # y = +h
+        (0, 2, 6, 4),  # z = -h
+        (1, 5, 7, 3),  # z = +h
+    ]
+    f = []
+    for a, b, c, d in quads:
+        f += [(a, b, c), (a, c, d)]
+    f = np.array(f, np.int64)
+    # orient every face towards the centre
+    tri = v[f]
+    n = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    c = tri.mean(axis=1) - 0.5 * (np.asarray(lo) + np.asarray(hi))
+    wrong = np.einsum("ij,ij->i", n, -c) < 0
+    f[wrong] = f[wrong][:, [0, 2, 1]]
+    return v, f
+
+
+# ------------------------------------------------------------------ noise
+
+class Perlin:
+    """Improved gradient noise (Perlin 2002) with a seeded permutation table."""
+
+    def __init__(self, rng: np.random.Generator):
+        p = rng.permutation(256)
+        self.p = np.concatenate([p, p]).astype(np.int64)
+
+    @staticmethod
+    def _fade(t):
+        return t * t * t * (t * (t * 6 - 15) + 10)
+
+    @staticmethod
+    def _grad(h, x, y, z):
+        h = h & 15
+        u = np.where(h < 8, x, y)
+        v = np.where(h < 4, y, np.where((h == 12) | (h == 14), x, z))
+        return np.where(h & 1, -u, u) + np.where(h & 2, -v, v)
+
+    def noise3(self, x, y, z):
+        X = np.floor(x).astype(np.int64) & 255
+        Y = np.floor(y).astype(np.int64) & 255
+        Z = np.floor(z).astype(np.int64) & 255
+        x = x - np.floor(x)
+        y = y - np.floor(y)
+        z = z - np.floor(z)
+        u, v, w = self._fade(x), self._fade(y), self._fade(z)
+        p = self.p
+        A = p[X] + Y
+        AA = p[A] + Z
+        AB = p[A + 1] + Z
+        B = p[X + 1] + Y
+        BA = p[B] + Z
+        BB = p[B + 1] + Z
+        g = self._grad
+        lerp = lambda t, a, b: a + t * (b - a)
+        return lerp(w,
+                    lerp(v, lerp(u, g(p[AA], x, y, z), g(p[BA], x - 1, y, z)),
+                         lerp(u, g(p[AB], x, y - 1, z), g(p[BB], x - 1, y - 1, z))),
+                    lerp(v, lerp(u, g(p[AA + 1], x, y, z - 1), g(p[BA + 1], x - 1, y, z - 1)),
+                         lerp(u, g(p[AB + 1], x, y - 1, z - 1), g(p[BB + 1], x - 1, y - 1, z - 1))))
+
+    def fbm3(self, x, y, z, octaves=8, lacunarity=2.0, gain=0.5):
+        total = np.zeros_like(np.asarray(x, np.float64))
+        amp, freq = 1.0, 1.0
+        for _ in range(octaves):
+            total += amp * self.noise3(x * freq, y * freq, z * freq)
+            amp *= gain
+            freq *= lacunarity
+        return total
+
+
+# ------------------------------------------------------------------ scene JSON helpers
+
+def _entity(geometry, material, transform=None, light=None, inner=None, outer=None) -> dict:
+    e = {"geometry": geometry, "material": material}
+    if transform is not None:
+        e["local_to_world"] = transform
+    if inner is not None:
+        e["inner_medium"] = inner
+    if outer is not None:
+        e["outer_medium"] = outer
+    if light is not None:
+        e["light"] = light
+    return e
+
+
+def _diffuse(rgb) -> dict:
+    return {"type": "diffuse", "color": [float(c) for c in rgb]}
+
+
+def _write_scene(path: Path, scene: dict) -> Path:
+    tmp = path.with_suffix(".json.tmp")
+    tmp.write_text(json.dumps(scene, indent=1))
+    os.replace(tmp, path)
+    return path
+
+
+# ------------------------------------------------------------------ configurations
+
+def cornell(seed: int = 1000, width: int = 256, height: int = 256, spp: int = 16, sampler: str = "halton",
+            out_dir: Path | None = None, force: bool = False) -> Path:
+    """Config 0: closed unit box, two icospheres, one quad light (see module docstring)."""
+    out = Path(out_dir or cache_dir() / f"cornell-{seed}")
+    out.mkdir(parents=True, exist_ok=True)
+    name = f"scene-{width}x{height}-{spp}-{sampler}.json"
+    if (out / name).exists() and not force:
+        return out / name
+    rng = np.random.default_rng(seed)
+    half = 0.5
+    # unit cross-section, deepened towards the camera so that a 40 degree view from inside
+    # sees the side walls; left wall, right wall and the rest are separate entities
+    bv, bf = box_inward((-half, -half, -half), (half, half, 1.4))
+    write_obj(out / "box_left.obj", bv, bf[0:2])
+    write_obj(out / "box_right.obj", bv, bf[2:4])
+    write_obj(out / "box_rest.obj", bv, bf[4:12])
+    sv, sf = icosphere(3)
+    write_obj(out / "sphere3.obj", sv, sf, normals=sv)
+    qv, qf = quad(0.25)
+    write_obj(out / "light.obj", qv, flip(qf))  # normal -y: facing down into the box
+    eye = np.array([0.0, 0.0, 1.3])
+    radius = 0.3
+    centers = []
+    while len(centers) < 2:
+        c = rng.uniform(-half + radius, half - radius, 3)
+        if np.linalg.norm(c - eye) > radius + 0.08:
+            centers.append(c)
+    albedos = rng.uniform(0.2, 0.8, (6, 3))
+    ents = [_entity({"type": "triangle_mesh", "filename": "${" + part + "}"}, _diffuse(albedos[k]))
+            for k, part in enumerate(("box_left", "box_right", "box_rest"))]
+    for k, c in enumerate(centers):
+        ents.append(_entity({"type": "triangle_mesh", "filename": "${sphere}"}, _diffuse(albedos[3 + k]),
+                            [{"scale": [radius] * 3}, {"translate": [float(x) for x in c]}]))
+    ents.append(_entity({"type": "triangle_mesh", "filename": "${light}"}, _diffuse(albedos[5]),
+                        [{"translate": [0.0, half - 0.005, 0.0]}],
+                        light={"type": "mesh_light", "intensity": [15.0, 15.0, 15.0]}))
+    scene = {
+        "width": width, "height": height,
+        "camera": {"type": "pinhole", "eye": eye.tolist(), "dst": [0.0, 0.0, -half], "up": [0.0, 1.0, 0.0],
+                   "fov_y": {"deg": 40.0}},
+        "renderer": {"type": "wfpt", "spp": spp, "min_depth": 3, "max_depth": 8, "rr_threshold": 0.1,
+                     "rr_cont_prob": 0.5, "state_count": 1000000, "sampler": sampler,
+                     "filter": {"type": "gaussian", "radius": 1.5, "alpha": 1.6}},
+        "scene": {"entities": ents},
+    }
+    text = json.dumps(scene, indent=1)
+    for key, fn in (("${box_left}", "box_left.obj"), ("${box_right}", "box_right.obj"),
+                    ("${box_rest}", "box_rest.obj"), ("${sphere}", "sphere3.obj"), ("${light}", "light.obj")):
+        text = text.replace(key, "$env{scene_directory}/" + fn)
+    (out / name).write_text(text)
+    return out / name
+
+
+def terrain(seed: int = 1001, width: int = 1920, height: int = 1080, spp: int = 64, grid: int = 1024,
+            instances: int = 200, out_dir: Path | None = None, force: bool = False,
+            state_count: int = 2 * 1024 * 1024) -> Path:
+    """Config 1: fBm terrain + instanced icospheres + Disney + sky + 8 quad lights."""
+    out = Path(out_dir or cache_dir() / f"terrain-{seed}-{grid}-{instances}")
+    out.mkdir(parents=True, exist_ok=True)
+    name = f"scene-{width}x{height}-{spp}.json"
+    if (out / name).exists() and not force:
+        return out / name
+    rng = np.random.default_rng(seed)
+    perlin = Perlin(rng)
+    # heightfield over [-1, 1]^2 in xz
+    xs = np.linspace(-1.0, 1.0, grid)
+    X, Z = np.meshgrid(xs, xs, indexing="xy")
+    H = 0.2 * perlin.fbm3(X * 2.0 + 0.5, Z * 2.0 + 0.5, np.full_like(X, 0.37), octaves=8, lacunarity=2.0)
+    V = np.stack([X, H, Z], axis=-1).reshape(-1, 3)
+    # smooth vertex normals from central differences
+    dhdx = np.gradient(H, xs, axis=1)
+    dhdz = np.gradient(H, xs, axis=0)
+    N = np.stack([-dhdx, np.ones_like(H), -dhdz], axis=-1)
+    N /= np.linalg.norm(N, axis=-1, keepdims=True)
+    idx = np.arange(grid * grid).reshape(grid, grid)
+    a, b, c, d = idx[:-1, :-1], idx[:-1, 1:], idx[1:, :-1], idx[1:, 1:]
+    F = np.concatenate([np.stack([a, c, b], -1).reshape(-1, 3), np.stack([b, c, d], -1).reshape(-1, 3)])
+    write_obj(out / "terrain.obj", V, F, normals=N.reshape(-1, 3))
+    sv, sf = icosphere(4)
+    write_obj(out / "sphere4.obj", sv, sf, normals=sv)
+    qv, qf = quad(1.0)
+    write_obj(out / "quad.obj", qv, flip(qf))
+
+    def height_at(x, z):
+        return float(0.2 * perlin.fbm3(np.array([x * 2.0 + 0.5]), np.array([z * 2.0 + 0.5]),
+                                       np.array([0.37]), octaves=8)[0])
+
+    def disney():
+        return {"type": "disney", "color": [float(v) for v in rng.uniform(0, 1, 3)],
+                "roughness": float(rng.uniform(0.05, 1.0)),
+                "metallic": float(rng.random() < 0.3), "specular": 0.5,
+                "clearcoat": float(rng.uniform(0, 1))}
+
+    ents = [_entity({"type": "triangle_mesh", "filename": "$env{scene_directory}/terrain.obj"}, disney())]
+    sphere_node = {"type": "triangle_mesh", "filename": "$env{scene_directory}/sphere4.obj"}
+    for k in range(instances):
+        x, z = rng.uniform(-0.9, 0.9, 2)
+        r = float(rng.uniform(0.02, 0.06))
+        y = height_at(x, z) + r * float(rng.uniform(0.3, 1.0))
+        geo = sphere_node if k == 0 else "$reference{$root/scene/entities/1/geometry}"
+        ents.append(_entity(geo, disney(), [{"scale": [r, r, r]}, {"translate": [float(x), y, float(z)]}]))
+    for k in range(8):
+        x, z = rng.uniform(-0.8, 0.8, 2)
+        s = float(rng.uniform(0.05, 0.15))
+        y = height_at(x, z) + float(rng.uniform(0.15, 0.4))
+        inten = [float(v) for v in rng.uniform(2.0, 10.0) * rng.uniform(0.6, 1.0, 3)]
+        geo = {"type": "triangle_mesh", "filename": "$env{scene_directory}/quad.obj"} if k == 0 else \
+            f"$reference{{$root/scene/entities/{instances + 1}/geometry}}"
+        ents.append(_entity(geo, _diffuse([0.0, 0.0, 0.0]), [{"scale": [s, 1.0, s]}, {"translate": [float(x), y, float(z)]}],
+                            light={"type": "mesh_light", "intensity": inten}))
+    scene = {
+        "width": width, "height": height,
+        "camera": {"type": "pinhole", "eye": [0.0, 0.75, 1.55], "dst": [0.0, 0.0, 0.0], "up": [0.0, 1.0, 0.0],
+                   "fov_y": {"deg": 45.0}},
+        "renderer": {"type": "wfpt", "spp": spp, "min_depth": 5, "max_depth": 16, "rr_threshold": 0.1,
+                     "rr_cont_prob": 0.5, "state_count": state_count, "sampler": "independent",
+                     "filter": {"type": "gaussian", "radius": 1.5, "alpha": 1.6}},
+        "scene": {"entities": ents,
+                  "envir_light": {"type": "gradient_sky", "lower": [0.1, 0.1, 0.12], "upper": [0.6, 0.75, 1.0],
+                                  "up": [0.0, 1.0, 0.0]}},
+    }
+    return _write_scene(out / name, scene)
+
+
+def random_soup(path_dir: Path, seed: int, n_tris: int, n_instances: int = 3) -> Path:
+    """Small traversal-test scene: random triangles in a few translated/scaled instances
+    sharing one geometry, plus a ground quad."""
+    out = Path(path_dir)
+    out.mkdir(parents=True, exist_ok=True)
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(-1, 1, (n_tris, 3))
+    v = c[:, None, :] + rng.normal(0, 0.08, (n_tris, 3, 3))
+    write_obj(out / "soup.obj", v.reshape(-1, 3), np.arange(n_tris * 3).reshape(-1, 3))
+    qv, qf = quad(4.0)
+    write_obj(out / "ground.obj", qv, qf)
+    ents = [_entity({"type": "triangle_mesh", "filename": "$env{scene_directory}/ground.obj"}, _diffuse([0.5] * 3),
+                    [{"translate": [0.0, -1.5, 0.0]}])]
+    for k in range(n_instances):
+        geo = {"type": "triangle_mesh", "filename": "$env{scene_directory}/soup.obj"} if k == 0 else \
+            "$reference{$root/scene/entities/1/geometry}"
+        s = float(rng.uniform(0.5, 1.0))
+        t = [float(x) for x in rng.uniform(-1, 1, 3)]
+        ents.append(_entity(geo, _diffuse(rng.uniform(0.2, 0.8, 3)), [{"scale": [s, s, s]}, {"translate": t}]))
+    scene = {
+        "width": 64, "height": 64,
+        "camera": {"type": "pinhole", "eye": [0.0, 0.0, 4.0], "dst": [0.0, 0.0, 0.0], "up": [0.0, 1.0, 0.0],
+                   "fov_y": {"deg": 50.0}},
+        "renderer": {"type": "wfpt", "spp": 4},
+        "scene": {"entities": ents},
+    }
+    return _write_scene(out / "scene.json", scene)

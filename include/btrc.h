@@ -1,0 +1,195 @@
+/*
+ * btrc_gb300 C ABI: a GB300-native wavefront path tracer that loads the same scene JSON
+ * as AirGuanZ/Btrc and replaces its wavefront renderer, OptiX traversal and stage
+ * kernels. Plain pointers and sizes only; no exceptions cross this boundary.
+ *
+ * Conventions
+ *   - Every entry point returns a btrc_status; btrc_last_error(ctx) gives the message.
+ *   - The caller owns ray / hit / image buffers; the library owns scene and BVH memory.
+ *   - Functions taking `void *stream` enqueue on that cudaStream_t (NULL: the context's
+ *     stream) and return without synchronising; all others are synchronous.
+ *   - A context is bound to one CUDA device; calls on one context must not overlap.
+ *
+ * Reference interfaces each entry point replaces (paths inside the Btrc source tree):
+ *   btrc_scene_load_json   factory::JSONParser::parse (src/factory/btrc/factory/node/parser.cpp:59-72)
+ *                          + factory::create_scene (src/factory/btrc/factory/scene.cpp:5-94)
+ *                          + camera/renderer creation in src/cli/main.cpp:45-66
+ *   btrc_scene_build       TriangleMesh::commit / Scene::commit acceleration-structure builds
+ *                          (src/builtin/btrc/builtin/geometry/triangle_mesh.cpp:24-171,
+ *                           src/core/btrc/core/scene.cpp:92-238,
+ *                           src/common/btrc/utils/optix/context.cpp:106-215)
+ *   btrc_render            WavefrontPathTracer::render (src/builtin/btrc/builtin/renderer/wavefront.cpp:205-325)
+ *                          followed by the preview resolve radiance/weight (wavefront/preview.cpp:28-80)
+ *   btrc_trace_closest     TracePipeline::trace (src/builtin/btrc/builtin/renderer/wavefront/trace.cpp:118-166)
+ *   btrc_trace_any         ShadowPipeline::test occlusion query (wavefront/shadow.cpp:24-76, 140-158)
+ *   btrc_cancel            Renderer::stop_async (src/core/btrc/core/renderer.h)
+ */
+#ifndef BTRC_GB300_H
+#define BTRC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum btrc_status
+{
+    BTRC_OK = 0,
+    BTRC_ERR_INVALID_ARG = 1,
+    BTRC_ERR_IO = 2,
+    BTRC_ERR_PARSE = 3,
+    BTRC_ERR_CUDA = 4,
+    BTRC_ERR_OOM = 5,
+    BTRC_ERR_TIMEOUT = 6,
+    BTRC_ERR_CANCELLED = 7,
+    BTRC_ERR_UNSUPPORTED = 8,
+    BTRC_ERR_INTERNAL = 9
+} btrc_status;
+
+typedef struct btrc_ctx btrc_ctx;
+typedef struct btrc_scene btrc_scene;
+
+/* 32 bytes: origin + medium id, direction (not necessarily normalised) + t1.
+   Hits are accepted for 0 < t <= t1 (reference SoA layout: wavefront/soa.h:8-38). */
+typedef struct btrc_ray
+{
+    float o[3];
+    uint32_t medium_id;
+    float d[3];
+    float t1;
+} btrc_ray;
+
+/* 16 bytes: closest-hit detail (reference: trace.cpp:64-78 writes t, prim_id, b1, b2).
+   The matching flag word is instance_id | BTRC_HIT_BIT, or 0 on a miss. */
+typedef struct btrc_hit
+{
+    float t;
+    uint32_t prim_id;
+    float b1;
+    float b2;
+} btrc_hit;
+
+#define BTRC_HIT_BIT (1u << 30)
+
+typedef struct btrc_scene_info
+{
+    int32_t width, height, spp;
+    int32_t min_depth, max_depth, state_count;
+    int32_t sampler;          /* 0 independent (PCG), 1 halton */
+    int32_t filter;           /* 0 box, 1 gaussian */
+    int32_t instances, geometries, materials, area_lights, media;
+    int32_t has_envir_light;
+    uint64_t triangles;       /* after instance flattening */
+    int32_t bvh_nodes, bvh_depth;
+    uint64_t bvh_bytes;       /* nodes + triangle records */
+    float world_min[3], world_max[3];
+    double build_ms;
+} btrc_scene_info;
+
+typedef struct btrc_build_opts
+{
+    int32_t threads;          /* host threads for the BVH build; <= 0: all */
+} btrc_build_opts;
+
+typedef struct btrc_render_opts
+{
+    int32_t spp;              /* 0: use the scene's renderer.spp */
+    int32_t state_count;      /* 0: use the scene's renderer.state_count */
+    int32_t output_on_device; /* 1: rgb_out is a device pointer, 0: host pointer */
+    int32_t use_graphs;       /* 1: capture bounces in CUDA graphs (default behaviour) */
+    int32_t profile;          /* 0 off; 1 CUDA events around every stage launch (no graphs);
+                                 2 closest-hit traversal counters (no graphs, slower) */
+} btrc_render_opts;
+
+/* stage indices of btrc_stats.stage_ms / stage_launches */
+#define BTRC_STAGE_CONTROL 0
+#define BTRC_STAGE_GENERATE 1
+#define BTRC_STAGE_TRACE 2
+#define BTRC_STAGE_MEDIUM 3
+#define BTRC_STAGE_SHADE 4
+#define BTRC_STAGE_SHADOW 5
+
+typedef struct btrc_stats
+{
+    uint64_t paths;           /* camera paths completed */
+    uint64_t extension_rays;  /* closest-hit rays traced */
+    uint64_t shadow_rays;     /* occlusion rays traced */
+    uint32_t bounces;         /* wavefront iterations */
+    uint32_t traversal_errors;
+    double device_ms;         /* GPU time of the wavefront loop (CUDA events) */
+    double wall_ms;           /* host wall time of btrc_render, copies included */
+    uint64_t kernel_launches; /* kernels launched by the wavefront loop */
+    double stage_ms[6];       /* profile 1: summed CUDA-event time per stage */
+    uint64_t stage_launches[6];
+    uint64_t node_visits;     /* profile 2: closest-hit node visits over the render */
+    uint64_t tri_tests;       /* profile 2: closest-hit triangle tests over the render */
+} btrc_stats;
+
+const char *btrc_version(void);
+
+/* device >= 0: CUDA device index. device == -1: host-only context that can load scenes
+   and build BVHs (btrc_scene_build skips the upload) but runs no device work. */
+btrc_status btrc_ctx_create(int device, btrc_ctx **out);
+void btrc_ctx_destroy(btrc_ctx *ctx);
+const char *btrc_last_error(const btrc_ctx *ctx);
+/* Ask a running btrc_render on this context to stop between bounces (thread safe). */
+void btrc_cancel(btrc_ctx *ctx);
+
+btrc_status btrc_scene_load_json(btrc_ctx *ctx, const char *path, btrc_scene **out);
+btrc_status btrc_scene_build(btrc_scene *scene, const btrc_build_opts *opts);
+btrc_status btrc_scene_info_get(const btrc_scene *scene, btrc_scene_info *out);
+void btrc_scene_destroy(btrc_scene *scene);
+
+/* World-space triangles in flattened (instance, primitive) order: 9 floats each, plus
+   the (instance, primitive) pair in ids (2 uint32 each). Either output may be NULL. */
+btrc_status btrc_scene_export_triangles(const btrc_scene *scene, float *xyz, uint32_t *ids, uint64_t capacity);
+
+/* Copy of the flattened acceleration structure: 80-byte compressed 8-wide nodes and
+   48-byte triangle records (layout in btrc_gb300/csrc/layout.h). Available for host-only
+   contexts and scenes of up to 2^20 triangles; BTRC_ERR_UNSUPPORTED otherwise. */
+btrc_status btrc_scene_export_bvh(const btrc_scene *scene, void *nodes, uint64_t node_capacity, void *tris,
+                                  uint64_t tri_capacity);
+
+/* Render the whole frame: rgb_out receives width*height*3 floats (radiance / weight). */
+btrc_status btrc_render(btrc_ctx *ctx, btrc_scene *scene, const btrc_render_opts *opts, float *rgb_out,
+                        btrc_stats *stats);
+
+/* Closest hit for n device-resident rays. flags[i] = instance | BTRC_HIT_BIT or 0. */
+btrc_status btrc_trace_closest(btrc_ctx *ctx, const btrc_scene *scene, const btrc_ray *d_rays, uint64_t n,
+                               uint32_t *d_flags, btrc_hit *d_hits, void *stream);
+
+/* Occlusion for n device-resident rays: d_occluded[i] = 1 when any hit in (0, t1]. */
+btrc_status btrc_trace_any(btrc_ctx *ctx, const btrc_scene *scene, const btrc_ray *d_rays, uint64_t n,
+                           uint32_t *d_occluded, void *stream);
+
+/* Per-ray node visits and triangle tests of the closest-hit traversal (measurement). */
+btrc_status btrc_trace_stats(btrc_ctx *ctx, const btrc_scene *scene, const btrc_ray *d_rays, uint64_t n,
+                             uint32_t *d_node_visits, uint32_t *d_tri_tests, void *stream);
+
+/* Test hook: sampler streams. For each of n (pixel, sample) pairs write `dims` values
+   drawn with get1d from a fresh sampler of the given type (0 independent, 1 halton) for
+   a film of width x height. pixel_xy holds x | y << 16. All pointers are device memory. */
+btrc_status btrc_sampler_batch(btrc_ctx *ctx, int32_t type, int32_t width, int32_t height,
+                               const uint32_t *d_pixel_xy, const uint32_t *d_sample_index, uint64_t n,
+                               uint32_t dims, float *d_out, void *stream);
+
+/* Test hook: local-space BSDF component evaluation, device pointers.
+   material: 16 floats per record, layout of the scene's material parameters with the
+   material type in record[15] (0 diffuse, 1 metal, 2 disney).
+   op 0 (eval/pdf): wo, wi: 3 floats each; out: 4 floats (f.rgb, pdf)
+   op 1 (sample)  : wo: 3 floats, u: 3 floats; out: 7 floats (f.rgb, pdf, wi.xyz) */
+btrc_status btrc_bsdf_batch(btrc_ctx *ctx, int32_t op, const float *d_material, const float *d_wo,
+                            const float *d_wi_or_u, uint64_t n, float *d_out, void *stream);
+
+/* Test hook: transmittance estimates of medium `medium_id` of a built scene along n
+   world-space segments (6 floats: a.xyz, b.xyz); one PCG seed per segment. */
+btrc_status btrc_medium_tr_batch(btrc_ctx *ctx, const btrc_scene *scene, int32_t medium_id, const float *d_seg,
+                                 const uint64_t *d_seeds, uint64_t n, float *d_out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BTRC_GB300_H */

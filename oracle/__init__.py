@@ -1,0 +1,157 @@
+"""ORACLE — test infrastructure only (CPU restatement of the reference path).
+
+Loaded by tests/, __graft_entry__.smoke() and bench.py's CPU baseline as the checker;
+never by the product package. See oracle/oracle.cpp for what is restated and how each
+part is pinned.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+_vp = C.c_void_p
+_lib = None
+_ref = None
+
+
+class OracleScene(C.Structure):
+    _fields_ = [
+        ("tris", _vp), ("ids", _vp), ("ntri", C.c_uint64),
+        ("ninst", C.c_int32), ("inst_l2w", _vp), ("inst_w2l", _vp), ("inst_geo", _vp), ("inst_mat", _vp),
+        ("inst_light", _vp), ("inst_inner", _vp), ("inst_outer", _vp),
+        ("ngeo", C.c_int32), ("geo_offset", _vp), ("geo_count", _vp), ("geo_area_total", _vp), ("shade", _vp),
+        ("total_geo_tris", C.c_uint64), ("tri_area", _vp), ("local_pos", _vp),
+        ("nmat", C.c_int32), ("mat", _vp),
+        ("nlight", C.c_int32), ("light_inst", _vp), ("light_geo", _vp), ("light_scale", _vp),
+        ("light_intensity", _vp),
+        ("env_type", C.c_int32), ("env_lower", C.c_float * 3), ("env_upper", C.c_float * 3),
+        ("env_up", C.c_float * 3),
+        ("vacuum_medium", C.c_int32), ("world_diagonal", C.c_float),
+        ("eye", C.c_float * 3), ("lbc", C.c_float * 3), ("film_x", C.c_float * 3), ("film_y", C.c_float * 3),
+        ("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("min_depth", C.c_int32),
+        ("max_depth", C.c_int32), ("rr_threshold", C.c_float), ("rr_cont_prob", C.c_float),
+        ("sampler", C.c_int32), ("filter", C.c_int32), ("filter_radius", C.c_float), ("filter_alpha", C.c_float),
+    ]
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        L = C.CDLL(str(path))
+        L.oracle_bvh_build.restype = _vp
+        L.oracle_bvh_build.argtypes = [_vp, _vp, C.c_uint64]
+        L.oracle_bvh_free.argtypes = [_vp]
+        L.oracle_trace_closest.argtypes = [_vp, _vp, C.c_uint64, _vp, _vp, C.c_int]
+        L.oracle_trace_any.argtypes = [_vp, _vp, C.c_uint64, _vp, C.c_int]
+        L.oracle_sampler_batch.argtypes = [C.c_int, C.c_int, C.c_int, _vp, _vp, C.c_uint64, C.c_uint32, _vp]
+        L.oracle_pcg32_stream.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, _vp]
+        L.oracle_murmur64a.restype = C.c_uint64
+        L.oracle_murmur64a.argtypes = [_vp, C.c_uint64, C.c_uint64]
+        L.oracle_bsdf_batch.argtypes = [C.c_int, _vp, _vp, _vp, C.c_uint64, _vp]
+        L.oracle_prepare.restype = _vp
+        L.oracle_prepare.argtypes = [C.POINTER(OracleScene)]
+        L.oracle_release.argtypes = [_vp]
+        L.oracle_render.argtypes = [_vp, C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, _vp, C.c_int]
+        _lib = L
+    return _lib
+
+
+def ref_lib() -> C.CDLL | None:
+    """The reference tree's vendored lib/bvh (oracle/_ref), or None when not built."""
+    global _ref
+    if _ref is None:
+        path = _build.build_ref()
+        if path is None or not Path(path).exists():
+            return None
+        L = C.CDLL(str(path))
+        L.ref_build.restype = _vp
+        L.ref_build.argtypes = [_vp, C.c_uint64]
+        L.ref_free.argtypes = [_vp]
+        L.ref_closest.argtypes = [_vp, _vp, C.c_uint64, _vp, _vp]
+        _ref = L
+    return _ref
+
+
+def _p(a: np.ndarray) -> int:
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data
+
+
+class OracleBvh:
+    """Closest / any hit over world-space triangles (9 floats) with (inst, prim) ids."""
+
+    def __init__(self, tris: np.ndarray, ids: np.ndarray):
+        self.tris = np.ascontiguousarray(tris, np.float32)
+        self.ids = np.ascontiguousarray(ids, np.uint32)
+        self.h = lib().oracle_bvh_build(_p(self.tris), _p(self.ids), len(self.tris))
+
+    def closest(self, rays: np.ndarray, threads: int = 0) -> tuple[np.ndarray, np.ndarray]:
+        rays = np.ascontiguousarray(rays, np.float32)
+        flags = np.zeros(len(rays), np.uint32)
+        hits = np.zeros((len(rays), 4), np.float32)
+        lib().oracle_trace_closest(self.h, _p(rays), len(rays), _p(flags), _p(hits), threads)
+        return flags, hits
+
+    def any(self, rays: np.ndarray, threads: int = 0) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, np.float32)
+        occ = np.zeros(len(rays), np.uint32)
+        lib().oracle_trace_any(self.h, _p(rays), len(rays), _p(occ), threads)
+        return occ
+
+    def __del__(self):
+        try:
+            lib().oracle_bvh_free(self.h)
+        except Exception:
+            pass
+
+
+def sampler_batch(kind: int, width: int, height: int, pixel_xy: np.ndarray, sample_index: np.ndarray,
+                  dims: int) -> np.ndarray:
+    pixel_xy = np.ascontiguousarray(pixel_xy, np.uint32)
+    sample_index = np.ascontiguousarray(sample_index, np.uint32)
+    out = np.zeros((len(pixel_xy), dims), np.float32)
+    lib().oracle_sampler_batch(kind, width, height, _p(pixel_xy), _p(sample_index), len(pixel_xy), dims, _p(out))
+    return out
+
+
+def pcg32_stream(initstate: int, initseq: int, n: int) -> np.ndarray:
+    out = np.zeros(n, np.uint32)
+    lib().oracle_pcg32_stream(initstate, initseq, n, _p(out))
+    return out
+
+
+def murmur64a(data: bytes, seed: int = 0) -> int:
+    buf = np.frombuffer(data, np.uint8).copy() if data else np.zeros(1, np.uint8)
+    return int(lib().oracle_murmur64a(_p(buf), len(data), seed))
+
+
+def bsdf_batch(op: int, material: np.ndarray, wo: np.ndarray, wi_or_u: np.ndarray) -> np.ndarray:
+    """FP64 local-space BSDF. material: (n, 16) float32, type in column 15."""
+    material = np.ascontiguousarray(material, np.float32)
+    wo = np.ascontiguousarray(wo, np.float64)
+    wu = np.ascontiguousarray(wi_or_u, np.float64)
+    out = np.zeros((len(material), 4 if op == 0 else 7), np.float64)
+    lib().oracle_bsdf_batch(op, _p(material), _p(wo), _p(wu), len(material), _p(out))
+    return out
+
+
+def ref_closest(tris: np.ndarray, rays: np.ndarray) -> tuple[np.ndarray, np.ndarray] | None:
+    """Closest hit with the reference tree's lib/bvh; None when it is not built."""
+    L = ref_lib()
+    if L is None:
+        return None
+    tris = np.ascontiguousarray(tris, np.float32)
+    rays = np.ascontiguousarray(rays, np.float32)
+    h = L.ref_build(_p(tris), len(tris))
+    prim = np.zeros(len(rays), np.int64)
+    t = np.zeros(len(rays), np.float32)
+    try:
+        L.ref_closest(h, _p(rays), len(rays), _p(prim), _p(t))
+    finally:
+        L.ref_free(h)
+    return prim, t

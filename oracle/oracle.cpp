@@ -1,0 +1,1862 @@
+// ORACLE — test infrastructure only. A CPU restatement of the reference (AirGuanZ/Btrc)
+// hot path, used by tests/, __graft_entry__.smoke() and bench.py's CPU baseline as the
+// checker. The product (btrc_gb300) never includes, links or calls this file.
+//
+// Parity status: the reference cannot be built or run (its eDSL submodule and the OptiX
+// SDK are absent), so this restatement is pinned where a published or vendored answer
+// exists: PCG32 against O'Neill's published pcg32 demo output, closest-hit traversal
+// against the vendored madmann91/bvh library compiled from the reference tree
+// (oracle/ref_bvh.cpp), and the samplers/BSDFs against closed-form properties in the tests.
+// Elsewhere parity is unpinned: the restatement follows the reference source line by line.
+//
+// Build: g++ -O2 -std=c++17 -ffp-contract=off -fPIC -shared -pthread (oracle/build.py).
+// -ffp-contract=off matters: the watertight test must round every product and sum
+// separately, exactly like the CUDA kernel's explicitly rounded intrinsics.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <thread>
+#include <vector>
+
+namespace orc {
+
+constexpr float PIf = 3.14159265358979323846f;
+constexpr float FMAX = std::numeric_limits<float>::max();
+
+template<class T>
+struct V
+{
+    T x, y, z;
+    V() : x(0), y(0), z(0) {}
+    V(T v) : x(v), y(v), z(v) {}
+    V(T a, T b, T c) : x(a), y(b), z(c) {}
+    T operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+};
+template<class T> V<T> operator+(V<T> a, V<T> b) { return V<T>(a.x + b.x, a.y + b.y, a.z + b.z); }
+template<class T> V<T> operator-(V<T> a, V<T> b) { return V<T>(a.x - b.x, a.y - b.y, a.z - b.z); }
+template<class T> V<T> operator*(V<T> a, V<T> b) { return V<T>(a.x * b.x, a.y * b.y, a.z * b.z); }
+template<class T> V<T> operator*(V<T> a, T s) { return V<T>(a.x * s, a.y * s, a.z * s); }
+template<class T> V<T> operator*(T s, V<T> a) { return V<T>(a.x * s, a.y * s, a.z * s); }
+template<class T> V<T> operator/(V<T> a, T s) { return V<T>(a.x / s, a.y / s, a.z / s); }
+template<class T> V<T> operator-(V<T> a) { return V<T>(-a.x, -a.y, -a.z); }
+template<class T> T dot(V<T> a, V<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template<class T> V<T> cross(V<T> a, V<T> b) { return V<T>(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+template<class T> T len(V<T> a) { return std::sqrt(dot(a, a)); }
+template<class T> V<T> nrm(V<T> a) { return a * (T(1) / len(a)); }
+template<class T> bool zero3(V<T> a) { return a.x == 0 && a.y == 0 && a.z == 0; }
+template<class T> T lum(V<T> c) { return T(0.2126) * c.x + T(0.7152) * c.y + T(0.0722) * c.z; }
+template<class T> V<T> lerp(V<T> a, V<T> b, T t) { return a * (T(1) - t) + b * t; }
+template<class T> T lerp1(T a, T b, T t) { return a * (T(1) - t) + b * t; }
+template<class T> T clampv(T v, T lo, T hi) { return std::min(hi, std::max(lo, v)); }
+template<class T> T sq(T v) { return v * v; }
+
+using V3f = V<float>;
+
+// ------------------------------------------------------------------ frames (cframe.cpp:13-83)
+
+template<class T>
+struct Frame
+{
+    V<T> x, y, z;
+    Frame() : x(1, 0, 0), y(0, 1, 0), z(0, 0, 1) {}
+    Frame(V<T> a, V<T> b, V<T> c) : x(nrm(a)), y(nrm(b)), z(nrm(c)) {}
+    static Frame from_z(V<T> zz)
+    {
+        V<T> nz = nrm(zz), ny;
+        if(T(1) - std::abs(nz.x) < T(0.1))
+            ny = cross(nz, V<T>(0, 1, 0));
+        else
+            ny = cross(nz, V<T>(1, 0, 0));
+        return Frame(cross(ny, nz), ny, nz);
+    }
+    V<T> l2g(V<T> l) const { return x * l.x + y * l.y + z * l.z; }
+    V<T> g2l(V<T> g) const { return V<T>(dot(g, x), dot(g, y), dot(g, z)); }
+    Frame rotate_to_new_z(V<T> nz) const
+    {
+        V<T> nx = cross(y, nz);
+        V<T> ny = cross(nz, nx);
+        return Frame(nx, ny, nz);
+    }
+    bool upper(V<T> v) const { return dot(v, z) > 0; }
+};
+
+// ------------------------------------------------------------------ watertight triangle test
+// Woop, Benthin, Wald (JCGT 2013), FP32, every operation rounded separately.
+
+struct WRay
+{
+    float o[3], d[3];
+    int kx, ky, kz;
+    float Sx, Sy, Sz;
+};
+
+inline WRay make_wray(const float *o, const float *d)
+{
+    WRay r;
+    for(int k = 0; k < 3; ++k)
+    {
+        r.o[k] = o[k];
+        r.d[k] = d[k];
+    }
+    const float ax = std::fabs(d[0]), ay = std::fabs(d[1]), az = std::fabs(d[2]);
+    int kz = (ax >= ay) ? ((ax >= az) ? 0 : 2) : ((ay >= az) ? 1 : 2);
+    int kx = (kz + 1) % 3, ky = (kx + 1) % 3;
+    if(d[kz] < 0.0f)
+        std::swap(kx, ky);
+    r.kx = kx;
+    r.ky = ky;
+    r.kz = kz;
+    r.Sx = d[kx] / d[kz];
+    r.Sy = d[ky] / d[kz];
+    r.Sz = 1.0f / d[kz];
+    return r;
+}
+
+// returns true with t, b1 (weight of v1), b2 (weight of v2) when 0 < t <= tmax
+inline bool watertight(const WRay &r, const float *v0, const float *v1, const float *v2, float tmax, float &t,
+                       float &b1, float &b2)
+{
+    const float A[3] = { v0[0] - r.o[0], v0[1] - r.o[1], v0[2] - r.o[2] };
+    const float B[3] = { v1[0] - r.o[0], v1[1] - r.o[1], v1[2] - r.o[2] };
+    const float Cc[3] = { v2[0] - r.o[0], v2[1] - r.o[1], v2[2] - r.o[2] };
+    const float Ax = A[r.kx] - r.Sx * A[r.kz];
+    const float Ay = A[r.ky] - r.Sy * A[r.kz];
+    const float Bx = B[r.kx] - r.Sx * B[r.kz];
+    const float By = B[r.ky] - r.Sy * B[r.kz];
+    const float Cx = Cc[r.kx] - r.Sx * Cc[r.kz];
+    const float Cy = Cc[r.ky] - r.Sy * Cc[r.kz];
+    float U = Cx * By - Cy * Bx;
+    float Vv = Ax * Cy - Ay * Cx;
+    float W = Bx * Ay - By * Ax;
+    if(U == 0.0f || Vv == 0.0f || W == 0.0f)
+    {
+        U = static_cast<float>(static_cast<double>(Cx) * By - static_cast<double>(Cy) * Bx);
+        Vv = static_cast<float>(static_cast<double>(Ax) * Cy - static_cast<double>(Ay) * Cx);
+        W = static_cast<float>(static_cast<double>(Bx) * Ay - static_cast<double>(By) * Ax);
+    }
+    if((U < 0.0f || Vv < 0.0f || W < 0.0f) && (U > 0.0f || Vv > 0.0f || W > 0.0f))
+        return false;
+    const float det = (U + Vv) + W;
+    if(det == 0.0f)
+        return false;
+    const float Az = r.Sz * A[r.kz];
+    const float Bz = r.Sz * B[r.kz];
+    const float Cz = r.Sz * Cc[r.kz];
+    const float T = (U * Az + Vv * Bz) + W * Cz;
+    const float rcp = 1.0f / det;
+    const float tt = T * rcp;
+    if(!(tt > 0.0f && tt <= tmax))
+        return false;
+    t = tt;
+    b1 = Vv * rcp;
+    b2 = W * rcp;
+    return true;
+}
+
+// ------------------------------------------------------------------ oracle BVH (binary, SAH)
+
+struct Box
+{
+    float lo[3] = { FMAX, FMAX, FMAX }, hi[3] = { -FMAX, -FMAX, -FMAX };
+    void grow(const float *p)
+    {
+        for(int k = 0; k < 3; ++k)
+        {
+            lo[k] = std::min(lo[k], p[k]);
+            hi[k] = std::max(hi[k], p[k]);
+        }
+    }
+    void grow(const Box &b)
+    {
+        for(int k = 0; k < 3; ++k)
+        {
+            lo[k] = std::min(lo[k], b.lo[k]);
+            hi[k] = std::max(hi[k], b.hi[k]);
+        }
+    }
+    double area() const
+    {
+        if(lo[0] > hi[0])
+            return 0;
+        double dx = double(hi[0]) - lo[0], dy = double(hi[1]) - lo[1], dz = double(hi[2]) - lo[2];
+        return 2 * (dx * dy + dy * dz + dz * dx);
+    }
+};
+
+struct Node
+{
+    Box box;
+    int left = -1, right = -1;
+    uint32_t first = 0, count = 0;
+};
+
+struct Bvh
+{
+    std::vector<float> tri;       // 9 floats per triangle, leaf order
+    std::vector<uint32_t> ids;    // inst, prim per triangle, leaf order
+    std::vector<Node> nodes;
+
+    void build(const float *tris, const uint32_t *idsin, uint64_t n)
+    {
+        std::vector<Box> boxes(n);
+        std::vector<float> cen(n * 3);
+        std::vector<uint32_t> idx(n);
+        for(uint64_t i = 0; i < n; ++i)
+        {
+            for(int v = 0; v < 3; ++v)
+                boxes[i].grow(tris + i * 9 + v * 3);
+            for(int k = 0; k < 3; ++k)
+                cen[i * 3 + k] = 0.5f * (boxes[i].lo[k] + boxes[i].hi[k]);
+            idx[i] = static_cast<uint32_t>(i);
+        }
+        nodes.clear();
+        nodes.reserve(2 * n + 1);
+        nodes.emplace_back();
+        if(n > 0)
+            split(0, 0, static_cast<uint32_t>(n), boxes, cen, idx, 0);
+        tri.resize(n * 9);
+        ids.resize(n * 2);
+        for(uint64_t i = 0; i < n; ++i)
+        {
+            std::memcpy(&tri[i * 9], tris + idx[i] * 9, 9 * sizeof(float));
+            ids[i * 2] = idsin[idx[i] * 2];
+            ids[i * 2 + 1] = idsin[idx[i] * 2 + 1];
+        }
+    }
+
+    void split(int ni, uint32_t b, uint32_t e, const std::vector<Box> &boxes, const std::vector<float> &cen,
+               std::vector<uint32_t> &idx, int depth)
+    {
+        Box box, cb;
+        for(uint32_t i = b; i < e; ++i)
+        {
+            box.grow(boxes[idx[i]]);
+            cb.grow(&cen[idx[i] * 3]);
+        }
+        nodes[ni].box = box;
+        const uint32_t n = e - b;
+        if(n <= 4 || depth > 60)
+        {
+            nodes[ni].first = b;
+            nodes[ni].count = n;
+            return;
+        }
+        constexpr int NB = 16;
+        double best = std::numeric_limits<double>::infinity();
+        int ba = -1, bb = -1;
+        for(int a = 0; a < 3; ++a)
+        {
+            if(!(cb.hi[a] > cb.lo[a]))
+                continue;
+            const double sc = NB / (double(cb.hi[a]) - cb.lo[a]);
+            Box bins[NB];
+            uint32_t cnt[NB] = {};
+            for(uint32_t i = b; i < e; ++i)
+            {
+                int k = std::min(NB - 1, std::max(0, int((cen[idx[i] * 3 + a] - double(cb.lo[a])) * sc)));
+                bins[k].grow(boxes[idx[i]]);
+                ++cnt[k];
+            }
+            for(int s = 0; s < NB - 1; ++s)
+            {
+                Box l, r;
+                uint32_t nl = 0, nr = 0;
+                for(int k = 0; k <= s; ++k)
+                {
+                    l.grow(bins[k]);
+                    nl += cnt[k];
+                }
+                for(int k = s + 1; k < NB; ++k)
+                {
+                    r.grow(bins[k]);
+                    nr += cnt[k];
+                }
+                if(!nl || !nr)
+                    continue;
+                const double c = l.area() * nl + r.area() * nr;
+                if(c < best)
+                {
+                    best = c;
+                    ba = a;
+                    bb = s;
+                }
+            }
+        }
+        uint32_t mid;
+        if(ba < 0)
+            mid = b + n / 2;
+        else
+        {
+            const double sc = NB / (double(cb.hi[ba]) - cb.lo[ba]);
+            auto it = std::partition(idx.begin() + b, idx.begin() + e, [&](uint32_t p) {
+                int k = std::min(NB - 1, std::max(0, int((cen[p * 3 + ba] - double(cb.lo[ba])) * sc)));
+                return k <= bb;
+            });
+            mid = static_cast<uint32_t>(it - idx.begin());
+            if(mid == b || mid == e)
+                mid = b + n / 2;
+        }
+        const int l = static_cast<int>(nodes.size());
+        nodes.emplace_back();
+        nodes.emplace_back();
+        nodes[ni].left = l;
+        nodes[ni].right = l + 1;
+        split(l, b, mid, boxes, cen, idx, depth + 1);
+        split(l + 1, mid, e, boxes, cen, idx, depth + 1);
+    }
+
+    // conservative slab test in FP64
+    static bool slab(const Box &bx, const double *o, const double *inv, double tmax, double &tnear)
+    {
+        double t0 = 0.0, t1 = tmax;
+        for(int k = 0; k < 3; ++k)
+        {
+            double a = (double(bx.lo[k]) - o[k]) * inv[k];
+            double b = (double(bx.hi[k]) - o[k]) * inv[k];
+            if(a > b)
+                std::swap(a, b);
+            t0 = std::max(t0, a);
+            t1 = std::min(t1, b);
+        }
+        tnear = t0;
+        return t0 <= t1 * (1 + 1e-6) + 1e-30;
+    }
+
+    struct Hit
+    {
+        bool hit = false;
+        float t = 0, b1 = 0, b2 = 0;
+        uint32_t inst = 0, prim = 0;
+    };
+
+    Hit closest(const float *o, const float *d, float t1) const
+    {
+        Hit best;
+        best.t = t1;
+        if(nodes.empty() || tri.empty())
+            return best;
+        const WRay wr = make_wray(o, d);
+        double od[3], inv[3];
+        for(int k = 0; k < 3; ++k)
+        {
+            od[k] = o[k];
+            inv[k] = 1.0 / (std::fabs(d[k]) < 1e-30 ? std::copysign(1e-30, d[k]) : double(d[k]));
+        }
+        int stack[128];
+        int sp = 0;
+        stack[sp++] = 0;
+        while(sp)
+        {
+            const Node &nd = nodes[stack[--sp]];
+            double tn;
+            if(!slab(nd.box, od, inv, double(best.t), tn))
+                continue;
+            if(nd.left < 0)
+            {
+                for(uint32_t i = nd.first; i < nd.first + nd.count; ++i)
+                {
+                    float t, b1, b2;
+                    if(watertight(wr, &tri[i * 9], &tri[i * 9 + 3], &tri[i * 9 + 6], best.t, t, b1, b2))
+                    {
+                        const uint32_t inst = ids[i * 2], prim = ids[i * 2 + 1];
+                        bool better = !best.hit || t < best.t ||
+                                      (t == best.t && (inst < best.inst || (inst == best.inst && prim < best.prim)));
+                        if(better)
+                        {
+                            best.hit = true;
+                            best.t = t;
+                            best.b1 = b1;
+                            best.b2 = b2;
+                            best.inst = inst;
+                            best.prim = prim;
+                        }
+                    }
+                }
+                continue;
+            }
+            stack[sp++] = nd.left;
+            stack[sp++] = nd.right;
+        }
+        return best;
+    }
+
+    bool any(const float *o, const float *d, float t1) const
+    {
+        if(nodes.empty() || tri.empty())
+            return false;
+        const WRay wr = make_wray(o, d);
+        double od[3], inv[3];
+        for(int k = 0; k < 3; ++k)
+        {
+            od[k] = o[k];
+            inv[k] = 1.0 / (std::fabs(d[k]) < 1e-30 ? std::copysign(1e-30, d[k]) : double(d[k]));
+        }
+        int stack[128];
+        int sp = 0;
+        stack[sp++] = 0;
+        while(sp)
+        {
+            const Node &nd = nodes[stack[--sp]];
+            double tn;
+            if(!slab(nd.box, od, inv, double(t1), tn))
+                continue;
+            if(nd.left < 0)
+            {
+                for(uint32_t i = nd.first; i < nd.first + nd.count; ++i)
+                {
+                    float t, b1, b2;
+                    if(watertight(wr, &tri[i * 9], &tri[i * 9 + 3], &tri[i * 9 + 6], t1, t, b1, b2))
+                        return true;
+                }
+                continue;
+            }
+            stack[sp++] = nd.left;
+            stack[sp++] = nd.right;
+        }
+        return false;
+    }
+};
+
+template<class F>
+void parallel_for(uint64_t n, int threads, F &&f)
+{
+    if(threads <= 0)
+        threads = std::max(1u, std::thread::hardware_concurrency());
+    std::atomic<uint64_t> next{ 0 };
+    const uint64_t chunk = 256;
+    auto work = [&] {
+        for(;;)
+        {
+            const uint64_t b = next.fetch_add(chunk);
+            if(b >= n)
+                break;
+            const uint64_t e = std::min(n, b + chunk);
+            for(uint64_t i = b; i < e; ++i)
+                f(i);
+        }
+    };
+    std::vector<std::thread> pool;
+    for(int k = 1; k < threads; ++k)
+        pool.emplace_back(work);
+    work();
+    for(auto &t : pool)
+        t.join();
+}
+
+// ------------------------------------------------------------------ samplers
+// independent.cpp:11-24 (PCG32 seeded with murmur64A(pixel), advanced by sample*65536),
+// halton.cpp:46-116 and low_discrepancy.cpp:10-99.
+
+constexpr uint64_t PCG_MULT = 6364136223846793005ull;
+constexpr uint64_t PCG_STREAM = 0xda3e39cb94b95bdbull;
+constexpr float ONE_M_EPS = 0x1.fffffep-1f;
+
+struct Pcg
+{
+    uint64_t state = 0, inc = 1;
+    uint32_t next()
+    {
+        const uint64_t old = state;
+        state = old * PCG_MULT + inc;
+        const uint32_t xs = static_cast<uint32_t>(((old >> 18u) ^ old) >> 27u);
+        const uint32_t rot = static_cast<uint32_t>(old >> 59u);
+        return (xs >> rot) | (xs << ((0u - rot) & 31u));
+    }
+    void seed(uint64_t initstate, uint64_t initseq)
+    {
+        state = 0;
+        inc = (initseq << 1u) | 1u;
+        next();
+        state += initstate;
+        next();
+    }
+    void advance(uint64_t delta)
+    {
+        uint64_t cm = PCG_MULT, cp = inc, am = 1, ap = 0;
+        while(delta)
+        {
+            if(delta & 1)
+            {
+                am *= cm;
+                ap = ap * cm + cp;
+            }
+            cp = (cm + 1) * cp;
+            cm *= cm;
+            delta >>= 1;
+        }
+        state = am * state + ap;
+    }
+    float uniform()
+    {
+        const float v = static_cast<float>(next()) * 0x1p-32f;
+        return std::min(v, ONE_M_EPS);
+    }
+};
+
+inline uint64_t murmur64a(const uint8_t *key, uint64_t len, uint64_t seed)
+{
+    const uint64_t m = 0xc6a4a7935bd1e995ull;
+    const int r = 47;
+    uint64_t h = seed ^ (len * m);
+    const uint8_t *end = key + 8 * (len / 8);
+    while(key != end)
+    {
+        uint64_t k;
+        std::memcpy(&k, key, 8);
+        key += 8;
+        k *= m;
+        k ^= k >> r;
+        k *= m;
+        h ^= k;
+        h *= m;
+    }
+    switch(len & 7)
+    {
+    case 7: h ^= uint64_t(key[6]) << 48; [[fallthrough]];
+    case 6: h ^= uint64_t(key[5]) << 40; [[fallthrough]];
+    case 5: h ^= uint64_t(key[4]) << 32; [[fallthrough]];
+    case 4: h ^= uint64_t(key[3]) << 24; [[fallthrough]];
+    case 3: h ^= uint64_t(key[2]) << 16; [[fallthrough]];
+    case 2: h ^= uint64_t(key[1]) << 8; [[fallthrough]];
+    case 1: h ^= uint64_t(key[0]); h *= m;
+    }
+    h ^= h >> r;
+    h *= m;
+    h ^= h >> r;
+    return h;
+}
+
+inline uint64_t mix_bits(uint64_t v)
+{
+    v ^= v >> 31;
+    v *= 0x7fb5d329728ea185ull;
+    v ^= v >> 27;
+    v *= 0x81dadef4bc2dd44dull;
+    v ^= v >> 33;
+    return v;
+}
+
+inline uint32_t perm_element(uint32_t i, uint32_t l, uint32_t p)
+{
+    uint32_t w = l - 1;
+    w |= w >> 1;
+    w |= w >> 2;
+    w |= w >> 4;
+    w |= w >> 8;
+    w |= w >> 16;
+    for(;;)
+    {
+        i ^= p;
+        i *= 0xe170893du;
+        i ^= p >> 16;
+        i ^= (i & w) >> 4;
+        i ^= p >> 8;
+        i *= 0x0929eb3fu;
+        i ^= p >> 23;
+        i ^= (i & w) >> 1;
+        i *= 1u | p >> 27;
+        i *= 0x6935fa69u;
+        i ^= (i & w) >> 11;
+        i *= 0x74dcb303u;
+        i ^= (i & w) >> 2;
+        i *= 0x9e501cc3u;
+        i ^= (i & w) >> 2;
+        i *= 0xc860a3dfu;
+        i &= w;
+        i ^= i >> 5;
+        if(i < l)
+            break;
+    }
+    return (i + p) % l;
+}
+
+struct Primes
+{
+    uint32_t v[1000];
+    Primes()
+    {
+        int n = 0;
+        for(uint32_t c = 2; n < 1000; ++c)
+        {
+            bool ok = true;
+            for(int k = 0; k < n && v[k] * v[k] <= c; ++k)
+                if(c % v[k] == 0)
+                {
+                    ok = false;
+                    break;
+                }
+            if(ok)
+                v[n++] = c;
+        }
+    }
+};
+static const Primes PRIMES;
+
+inline float owen_radical_inverse(int base_index, uint64_t a, uint64_t hash)
+{
+    const uint64_t base = PRIMES.v[base_index];
+    const float inv_base = 1.0f / static_cast<float>(base);
+    float inv_base_m = 1.0f;
+    uint64_t reversed = 0;
+    while(1.0f - inv_base_m < 1)
+    {
+        const uint64_t next = a / base;
+        uint64_t digit = a - next * base;
+        const uint64_t digit_hash = mix_bits(hash ^ reversed);
+        digit = perm_element(static_cast<uint32_t>(digit), static_cast<uint32_t>(base), static_cast<uint32_t>(digit_hash));
+        reversed = reversed * base + digit;
+        inv_base_m = inv_base_m * inv_base;
+        a = next;
+    }
+    return std::min(inv_base_m * static_cast<float>(reversed), ONE_M_EPS);
+}
+
+inline uint64_t inverse_radical_inverse(uint64_t inverse, uint64_t base, int digits)
+{
+    uint64_t index = 0;
+    for(int i = 0; i < digits; ++i)
+    {
+        const uint64_t digit = inverse % base;
+        inverse /= base;
+        index = index * base + digit;
+    }
+    return index;
+}
+
+inline int64_t modi(int64_t a, int64_t b)
+{
+    const int64_t r = a - a / b * b;
+    return r < 0 ? r + b : r;
+}
+
+inline void egcd(uint64_t a, uint64_t b, int64_t *x, int64_t *y)
+{
+    if(b == 0)
+    {
+        *x = 1;
+        *y = 0;
+        return;
+    }
+    int64_t d = a / b, xp, yp;
+    egcd(b, a % b, &xp, &yp);
+    *x = yp;
+    *y = xp - d * yp;
+}
+
+struct Sampler
+{
+    int type = 0;  // 0 independent, 1 halton
+    Pcg pcg;
+    uint32_t dim = 0;
+    uint64_t index = 0;
+
+    struct HC
+    {
+        int scale[2], exp[2], mult[2], stride;
+    };
+    static HC consts(int w, int h)
+    {
+        HC c{};
+        const int res[2] = { w, h };
+        for(int i = 0; i < 2; ++i)
+        {
+            const int base = i == 0 ? 2 : 3;
+            int s = 1, e = 0;
+            while(s < std::min(res[i], 128))
+            {
+                s *= base;
+                ++e;
+            }
+            c.scale[i] = s;
+            c.exp[i] = e;
+        }
+        int64_t x, y;
+        egcd(c.scale[1], c.scale[0], &x, &y);
+        c.mult[0] = static_cast<int>(modi(x, c.scale[0]));
+        egcd(c.scale[0], c.scale[1], &x, &y);
+        c.mult[1] = static_cast<int>(modi(x, c.scale[1]));
+        c.stride = c.scale[0] * c.scale[1];
+        return c;
+    }
+
+    void init(int t, const HC &hc, uint32_t px, uint32_t py, uint32_t sample)
+    {
+        type = t;
+        if(t == 0)
+        {
+            uint8_t buf[8];
+            std::memcpy(buf, &px, 4);
+            std::memcpy(buf + 4, &py, 4);
+            pcg.seed(murmur64a(buf, 8, 0), PCG_STREAM);
+            pcg.advance(static_cast<uint64_t>(sample) * 65536u);
+            return;
+        }
+        index = 0;
+        if(hc.stride > 1)
+        {
+            const uint64_t pm[2] = { px % 128u, py % 128u };
+            for(int i = 0; i < 2; ++i)
+            {
+                const uint64_t off = inverse_radical_inverse(pm[i], i == 0 ? 2 : 3, hc.exp[i]);
+                index = index + off * static_cast<uint64_t>((hc.stride / hc.scale[i]) * hc.mult[i]);
+            }
+            index = index % static_cast<uint64_t>(hc.stride);
+        }
+        index = index + static_cast<uint64_t>(sample) * static_cast<uint64_t>(hc.stride);
+        dim = 2;
+    }
+    float halton(uint32_t d) const
+    {
+        return owen_radical_inverse(static_cast<int>(d), index, mix_bits(static_cast<uint64_t>(1u + (d << 4))));
+    }
+    float get1d()
+    {
+        if(type == 0)
+            return pcg.uniform();
+        if(dim >= 1000)
+            dim = 2;
+        const float v = halton(dim);
+        dim += 1;
+        return v;
+    }
+    void get3d(float &a, float &b, float &c)
+    {
+        if(type == 0)
+        {
+            a = pcg.uniform();
+            b = pcg.uniform();
+            c = pcg.uniform();
+            return;
+        }
+        if(dim + 2 >= 1000)
+            dim = 2;
+        a = halton(dim);
+        b = halton(dim + 1);
+        c = halton(dim + 2);
+        dim += 3;
+    }
+};
+
+// ------------------------------------------------------------------ alias tables (alias.cpp:13-50)
+
+struct Alias
+{
+    std::vector<float> accept;
+    std::vector<uint32_t> other;
+    void init(const std::vector<float> &p)
+    {
+        double s = 0;
+        for(float v : p)
+            s += v;
+        const float ratio = static_cast<float>(p.size()) / static_cast<float>(s);
+        accept.resize(p.size());
+        other.resize(p.size());
+        std::vector<uint32_t> overs, unders;
+        for(uint32_t i = 0; i < p.size(); ++i)
+        {
+            accept[i] = p[i] * ratio;
+            other[i] = i;
+            if(accept[i] > 1)
+                overs.push_back(i);
+            else if(accept[i] < 1)
+                unders.push_back(i);
+        }
+        while(!overs.empty() && !unders.empty())
+        {
+            const uint32_t o = overs.back(), u = unders.back();
+            overs.pop_back();
+            unders.pop_back();
+            accept[o] -= 1 - accept[u];
+            other[u] = o;
+            if(accept[o] > 1)
+                overs.push_back(o);
+            else if(accept[o] < 1)
+                unders.push_back(o);
+        }
+        for(auto i : overs)
+            accept[i] = 1;
+        for(auto i : unders)
+            accept[i] = 1;
+    }
+    uint32_t sample(float u) const
+    {
+        const uint32_t n = static_cast<uint32_t>(accept.size());
+        const float nu = static_cast<float>(n) * u;
+        const uint32_t i = std::min(static_cast<uint32_t>(nu), n - 1);
+        const float s = nu - static_cast<float>(i);
+        return s <= accept[i] ? i : other[i];
+    }
+};
+
+// ------------------------------------------------------------------ BSDFs (templated: FP32 render, FP64 check)
+
+template<class T> struct CS
+{
+    V<T> f, dir;
+    T pdf = 0;
+    bool delta = false;
+};
+
+template<class T> T PI_T() { return T(3.14159265358979323846); }
+
+template<class T> V<T> hemi_zw(T u1, T u2)
+{
+    T sx = 0, sy = 0;
+    u1 = T(2) * u1 - T(1);
+    u2 = T(2) * u2 - T(1);
+    if(u1 != 0 || u2 != 0)
+    {
+        T theta, r;
+        if(std::abs(u1) > std::abs(u2))
+        {
+            r = u1;
+            theta = T(0.25) * PI_T<T>() * (u2 / u1);
+        }
+        else
+        {
+            r = u2;
+            theta = T(0.5) * PI_T<T>() - T(0.25) * PI_T<T>() * (u1 / u2);
+        }
+        sx = r * std::cos(theta);
+        sy = r * std::sin(theta);
+    }
+    return V<T>(sx, sy, std::sqrt(std::max(T(0), T(1) - (sx * sx + sy * sy))));
+}
+template<class T> T pdf_hemi_zw(V<T> v) { return v.z >= 0 ? v.z / PI_T<T>() : T(0); }
+template<class T> T cos2sin(T c) { return std::sqrt(std::max(T(0), T(1) - c * c)); }
+template<class T> T tan_th(V<T> w)
+{
+    T t = T(1) - w.z * w.z;
+    return t > 0 ? std::sqrt(t) / w.z : T(0);
+}
+template<class T> T phi_of(V<T> w)
+{
+    T r = 0;
+    if(w.x != 0 || w.y != 0)
+    {
+        r = std::atan2(w.y, w.x);
+        if(r < 0)
+            r += 2 * PI_T<T>();
+    }
+    return r;
+}
+template<class T> T diel_fresnel(T ei, T eo, T ci)
+{
+    if(ci < 0)
+    {
+        std::swap(ei, eo);
+        ci = -ci;
+    }
+    const T si = std::sqrt(std::max(T(0), T(1) - ci * ci));
+    const T st = eo / ei * si;
+    if(st >= 1)
+        return T(1);
+    const T ct = std::sqrt(std::max(T(0), T(1) - st * st));
+    const T para = (ei * ci - eo * ct) / (ei * ci + eo * ct);
+    const T perp = (eo * ci - ei * ct) / (eo * ci + ei * ct);
+    return T(0.5) * (para * para + perp * perp);
+}
+template<class T> T schlick1(T r0, T c)
+{
+    T t = T(1) - c, t2 = t * t;
+    return r0 + (T(1) - r0) * (t2 * t2 * t);
+}
+template<class T> V<T> schlick3(V<T> r0, T c)
+{
+    T t = T(1) - c, t2 = t * t, t5 = t2 * t2 * t;
+    return r0 + (V<T>(T(1)) - r0) * t5;
+}
+template<class T> T smith_gtr2(T tt, T a)
+{
+    if(tt == 0)
+        return T(1);
+    T root = a * tt;
+    return T(2) / (T(1) + std::sqrt(T(1) + root * root));
+}
+template<class T> T aniso_gtr2(T sph, T cph, T sth, T cth, T ax, T ay)
+{
+    T A = sq(cph / ax) + sq(sph / ay);
+    T RD = sq(sth) * A + sq(cth);
+    return T(1) / (PI_T<T>() * ax * ay * sq(RD));
+}
+template<class T> T smith_aniso(T cp, T sp, T ax, T ay, T tt)
+{
+    T t = sq(ax * cp) + sq(ay * sp);
+    T lambda = T(-0.5) + T(0.5) * std::sqrt(T(1) + t * sq(tt));
+    return T(1) / (T(1) + lambda);
+}
+template<class T> V<T> sample_aniso_gtr2(T ax, T ay, T s0, T s1)
+{
+    T sph = ay * std::sin(2 * PI_T<T>() * s0);
+    T cph = ax * std::cos(2 * PI_T<T>() * s0);
+    T nor = T(1) / std::sqrt(sq(sph) + sq(cph));
+    sph *= nor;
+    cph *= nor;
+    T A = sq(cph / ax) + sq(sph / ay);
+    T cth = std::sqrt(A * (T(1) - s1) / ((T(1) - A) * s1 + A));
+    T sth = cos2sin(cth);
+    return nrm(V<T>(sth * cph, sth * sph, cth));
+}
+template<class T> T gtr1(T sth, T cth, T a)
+{
+    return (sq(a) - 1) / (T(2) * PI_T<T>() * std::log(a) * (sq(a * cth) + sq(sth)));
+}
+template<class T> V<T> sample_gtr1(T a, T s0, T s1)
+{
+    T phi = 2 * PI_T<T>() * s0;
+    T cth = std::sqrt((std::pow(a, T(2) - T(2) * s1) - T(1)) / (sq(a) - T(1)));
+    T sth = cos2sin(cth);
+    return nrm(V<T>(sth * std::cos(phi), sth * std::sin(phi), cth));
+}
+template<class T> V<T> sample_vndf(V<T> ve, T ax, T ay, T s0, T s1)
+{
+    V<T> vh = nrm(V<T>(ax * ve.x, ay * ve.y, ve.z));
+    T lensq = vh.x * vh.x + vh.y * vh.y;
+    V<T> t1(1, 0, 0);
+    if(lensq > T(3e-4))
+        t1 = V<T>(-vh.y, vh.x, 0) / std::sqrt(lensq);
+    V<T> t2 = cross(vh, t1);
+    T r = std::sqrt(s0), phi = 2 * PI_T<T>() * s1;
+    T a1 = r * std::cos(phi), a2_ = r * std::sin(phi);
+    T s = T(0.5) * (T(1) + vh.z);
+    T a2 = (T(1) - s) * std::sqrt(T(1) - a1 * a1) + s * a2_;
+    V<T> nh = a1 * t1 + a2 * t2 + std::sqrt(std::max(T(0), T(1) - a1 * a1 - a2 * a2)) * vh;
+    return nrm(V<T>(ax * nh.x, ay * nh.y, std::max(T(0), nh.z)));
+}
+
+// material record: type, p[0..14]
+template<class T>
+struct Mat
+{
+    int type = 0;
+    V<T> C;
+    // metal
+    T ax = 0, ay = 0;
+    // disney
+    V<T> Ct;
+    T metallic = 0, rough = 0, spec = 0, spec_tint = 0, aniso = 0, sheen = 0, sheen_tint = 0, cc = 0, cc_rough = 0,
+      trans = 0, trans_rough = 0, ior = 1.5, tax = 0, tay = 0, wd = 0, ws = 0, wc = 0, wt = 0;
+
+    void init(int tp, const float *p)
+    {
+        type = tp;
+        C = V<T>(T(p[0]), T(p[1]), T(p[2]));
+        if(tp == 1)
+        {
+            // MicrofacetReflectionComponentImpl ctor (microfacet_reflection.h:20-33)
+            const T r = T(p[3]), an = T(p[4]);
+            T aspect = 1;
+            if(an > 0)
+                aspect = std::sqrt(T(1) - T(0.9) * an);
+            ax = std::max(T(0.001), r * r / aspect);
+            ay = std::max(T(0.001), r * r * aspect);
+        }
+        else if(tp == 2)
+        {
+            // DisneyBSDF ctor (disney.cpp:426-475)
+            const T l = lum(C);
+            Ct = l > 0 ? C / l : V<T>(T(1));
+            metallic = T(p[3]);
+            rough = T(p[4]);
+            spec = T(p[5]);
+            spec_tint = T(p[6]);
+            aniso = T(p[7]);
+            sheen = T(p[8]);
+            sheen_tint = T(p[9]);
+            cc = T(p[10]);
+            const T gloss = T(p[11]);
+            trans = T(p[12]);
+            trans_rough = T(p[13]);
+            ior = std::max(T(1.01), T(p[14]));
+            T aspect = 1;
+            if(aniso > 0)
+                aspect = std::sqrt(T(1) - T(0.9) * aniso);
+            ax = std::max(T(0.001), sq(rough) / aspect);
+            ay = std::max(T(0.001), sq(rough) * aspect);
+            tax = std::max(T(0.001), sq(trans_rough) / aspect);
+            tay = std::max(T(0.001), sq(trans_rough) * aspect);
+            cc_rough = std::max(T(0.0001), sq(lerp1(T(0.1), T(0), gloss)));
+            const T A = clampv(l * (T(1) - metallic), T(0.3), T(0.7));
+            const T B = T(1) - A;
+            wd = A * (T(1) - trans);
+            wt = A * trans;
+            ws = B * T(2) / (T(2) + cc);
+            wc = B * cc / (T(2) + cc);
+        }
+    }
+
+    // ---- metal (microfacet_reflection.h:78-121)
+    void metal_ep(V<T> wi, V<T> wo, V<T> &f, T &pdf) const
+    {
+        if(wi.z <= 0 || wo.z <= 0)
+        {
+            f = V<T>(0);
+            pdf = 0;
+            return;
+        }
+        V<T> wh = nrm(wi + wo);
+        T ctd = dot(wi, wh);
+        T ph = phi_of(wh);
+        T D = aniso_gtr2(std::sin(ph), std::cos(ph), cos2sin(wh.z), wh.z, ax, ay);
+        T pi_ = phi_of(wi), po = phi_of(wo);
+        T Go = smith_aniso(std::cos(po), std::sin(po), ax, ay, tan_th(wo));
+        T Gi = smith_aniso(std::cos(pi_), std::sin(pi_), ax, ay, tan_th(wi));
+        f = schlick3(C, ctd) * (D * Gi * Go / std::abs(T(4) * wi.z * wo.z));
+        pdf = Go * D / (T(4) * wo.z);
+    }
+
+    // ---- disney lobes (disney.cpp:76-422)
+    static T om5(T x)
+    {
+        T t = T(1) - x, t2 = t * t;
+        return t2 * t2 * t;
+    }
+    V<T> d_trans(V<T> wi, V<T> wo) const
+    {
+        T ci = wi.z, co = wo.z;
+        T eta = co > 0 ? ior : T(1) / ior;
+        V<T> wh = nrm(wo + eta * wi);
+        if(wh.z < 0)
+            wh = -wh;
+        T ctd = dot(wo, wh);
+        T F = diel_fresnel(ior, T(1), ctd);
+        T ph = phi_of(wh);
+        T D = aniso_gtr2(std::sin(ph), std::cos(ph), cos2sin(wh.z), wh.z, tax, tay);
+        T pi_ = phi_of(wi), po = phi_of(wo);
+        T G = smith_aniso(std::cos(pi_), std::sin(pi_), tax, tay, tan_th(wi)) *
+              smith_aniso(std::cos(po), std::sin(po), tax, tay, tan_th(wo));
+        T sdem = ctd + eta * dot(wi, wh);
+        T corr = T(1) / eta;
+        V<T> sqrtC(std::sqrt(C.x), std::sqrt(C.y), std::sqrt(C.z));
+        T val = (T(1) - F) * D * G * eta * eta * dot(wi, wh) * dot(wo, wh) * corr * corr / (ci * co * sdem * sdem);
+        T tf = co > 0 ? trans : T(1);
+        return (T(1) - metallic) * tf * sqrtC * std::abs(val);
+    }
+    V<T> d_inner(V<T> wi, V<T> wo) const
+    {
+        V<T> wh = -nrm(wi + wo);
+        T ctd = dot(wo, wh);
+        T F = diel_fresnel(ior, T(1), ctd);
+        T ph = phi_of(wh);
+        T D = aniso_gtr2(std::sin(ph), std::cos(ph), cos2sin(wh.z), wh.z, tax, tay);
+        T pi_ = phi_of(wi), po = phi_of(wo);
+        T G = smith_aniso(std::cos(pi_), std::sin(pi_), tax, tay, tan_th(wi)) *
+              smith_aniso(std::cos(po), std::sin(po), tax, tay, tan_th(wo));
+        return trans * C * std::abs(F * D * G / (T(4) * wi.z * wo.z));
+    }
+    V<T> d_spec(V<T> wi, V<T> wo) const
+    {
+        T ci = wi.z, co = wo.z;
+        V<T> wh = nrm(wi + wo);
+        T ctd = dot(wi, wh);
+        V<T> Cs = lerp(lerp(V<T>(T(1)), Ct, spec_tint), C, metallic);
+        V<T> Fd = Cs * diel_fresnel(ior, T(1), ctd);
+        V<T> Fc = schlick3(Cs, ctd);
+        V<T> F = lerp(spec * Fd, Fc, metallic);
+        T ph = phi_of(wh);
+        T D = aniso_gtr2(std::sin(ph), std::cos(ph), cos2sin(wh.z), wh.z, ax, ay);
+        T pi_ = phi_of(wi), po = phi_of(wo);
+        T G = smith_aniso(std::cos(pi_), std::sin(pi_), ax, ay, tan_th(wi)) *
+              smith_aniso(std::cos(po), std::sin(po), ax, ay, tan_th(wo));
+        return F * D * G / std::abs(T(4) * ci * co);
+    }
+    V<T> disney_eval(V<T> wi, V<T> wo) const
+    {
+        if(std::abs(wi.z) < T(1e-4) || std::abs(wo.z) < T(1e-4))
+            return V<T>(0);
+        if(wi.z * wo.z < 0)
+            return trans == 0 ? V<T>(0) : d_trans(wi, wo);
+        if(wi.z < 0 && wo.z < 0)
+            return trans == 0 ? V<T>(0) : d_inner(wi, wo);
+        if(wi.z <= 0 || wo.z <= 0)
+            return V<T>(0);
+        T ci = wi.z, co = wo.z;
+        V<T> wh = nrm(wi + wo);
+        T ctd = dot(wi, wh);
+        V<T> diffuse(0), sh(0);
+        if(metallic < 1)
+        {
+            V<T> lam = C / PI_T<T>();
+            T fl = om5(ci), fv = om5(co);
+            T rr = T(2) * rough * ctd * ctd;
+            V<T> retro = C / PI_T<T>() * rr * (fl + fv + fl * fv * (rr - 1));
+            diffuse = lam * (T(1) - T(0.5) * fl) * (T(1) - T(0.5) * fv) + retro;
+            if(sheen > 0)
+                sh = T(4) * sheen * lerp(V<T>(T(1)), Ct, sheen_tint) * om5(ctd);
+        }
+        V<T> specular = d_spec(wi, wo);
+        V<T> clear(0);
+        if(cc > 0)
+        {
+            T D = gtr1(cos2sin(wh.z), wh.z, cc_rough);
+            T F = schlick1(T(0.04), ctd);
+            T G = smith_gtr2(tan_th(wi), T(0.25)) * smith_gtr2(tan_th(wo), T(0.25));
+            T v = cc * D * F * G / std::abs(T(4) * ci * co);
+            clear = V<T>(v);
+        }
+        return (T(1) - metallic) * (T(1) - trans) * (diffuse + sh) + specular + clear;
+    }
+    T p_trans(V<T> wi, V<T> wo) const
+    {
+        T eta = wo.z > 0 ? ior : T(1) / ior;
+        V<T> wh = nrm(wo + eta * wi);
+        if(wh.z < 0)
+            wh = -wh;
+        if(((wo.z > 0) != (dot(wh, wo) > 0)) || ((wi.z > 0) != (dot(wh, wi) > 0)))
+            return 0;
+        T sdem = dot(wo, wh) + eta * dot(wi, wh);
+        T dd = eta * eta * dot(wi, wh) / (sdem * sdem);
+        T ph = phi_of(wh);
+        T D = aniso_gtr2(std::sin(ph), std::cos(ph), cos2sin(wh.z), wh.z, tax, tay);
+        return std::abs(dot(wi, wh) * D * dd);
+    }
+    T p_inner(V<T> wi, V<T> wo) const
+    {
+        V<T> wh = -nrm(wi + wo);
+        T ph = phi_of(wh);
+        T D = aniso_gtr2(std::sin(ph), std::cos(ph), cos2sin(wh.z), wh.z, tax, tay);
+        return std::abs(wh.z * D / (T(4) * dot(wi, wh)));
+    }
+    T disney_pdf(V<T> wi, V<T> wo) const
+    {
+        if(std::abs(wi.z) < T(1e-4) || std::abs(wo.z) < T(1e-4))
+            return 0;
+        if(wo.z < 0)
+        {
+            if(trans == 0)
+                return 0;
+            T mF = clampv(diel_fresnel(ior, T(1), wo.z), T(0.1), T(0.9));
+            if(wi.z > 0)
+                return (T(1) - mF) * p_trans(wi, wo);
+            return mF * p_inner(wi, wo);
+        }
+        if(wi.z < 0)
+            return wt * p_trans(wi, wo);
+        T diffuse = pdf_hemi_zw(wi);
+        V<T> wh = nrm(wi + wo);
+        T ph = phi_of(wh);
+        T cth = wh.z, sth = cos2sin(cth);
+        T ctd = dot(wi, wh);
+        T cpo = std::cos(phi_of(wo));
+        T spo = cos2sin(cpo);  // the reference uses sqrt(1 - cos^2) here (disney.cpp:335)
+        T sD = aniso_gtr2(std::sin(ph), std::cos(ph), sth, cth, ax, ay);
+        T ps = smith_aniso(cpo, spo, ax, ay, tan_th(wo)) * sD / (T(4) * wo.z);
+        T cD = gtr1(sth, cth, cc_rough);
+        T pc = cth * cD / (T(4) * ctd);
+        return wd * diffuse + ws * ps + wc * pc;
+    }
+    V<T> s_trans(V<T> wo, T s0, T s1) const
+    {
+        V<T> wh = sample_aniso_gtr2(tax, tay, s0, s1);
+        if(wh.z <= 0)
+            return V<T>(0);
+        if((wo.z > 0) != (dot(wh, wo) > 0))
+            return V<T>(0);
+        T eta = wo.z > 0 ? T(1) / ior : ior;
+        V<T> owh = dot(wh, wo) > 0 ? wh : -wh;
+        T cti = dot(wo, owh);
+        T s2t = eta * eta * (T(1) - cti * cti);
+        T c2t = T(1) - s2t;
+        if(c2t <= 0)
+            return V<T>(0);
+        V<T> wi = nrm((eta * cti - std::sqrt(c2t)) * owh - eta * wo);
+        if(wi.z * wo.z > 0 || ((wi.z > 0) != (dot(wh, wi) > 0)))
+            return V<T>(0);
+        return nrm(wi);
+    }
+    V<T> s_inner(V<T> wo, T s0, T s1) const
+    {
+        V<T> wh = sample_aniso_gtr2(tax, tay, s0, s1);
+        if(wh.z <= 0)
+            return V<T>(0);
+        V<T> wi = T(2) * dot(wo, wh) * wh - wo;
+        if(wi.z > 0)
+            return V<T>(0);
+        return nrm(wi);
+    }
+    V<T> s_spec(V<T> wo, T s0, T s1) const
+    {
+        V<T> wh = sample_vndf(wo, ax, ay, s0, s1);
+        if(wh.z <= 0)
+            return V<T>(0);
+        V<T> wi = T(2) * dot(wo, wh) * wh - wo;
+        if(wi.z <= 0)
+            return V<T>(0);
+        return nrm(wi);
+    }
+    V<T> s_clear(V<T> wo, T s0, T s1) const
+    {
+        V<T> wh = sample_gtr1(cc_rough, s0, s1);
+        if(wh.z <= 0)
+            return V<T>(0);
+        V<T> wi = T(2) * dot(wo, wh) * wh - wo;
+        if(wi.z <= 0)
+            return V<T>(0);
+        return nrm(wi);
+    }
+    CS<T> disney_sample(V<T> wo, T s0, T s1, T s2) const
+    {
+        CS<T> r;
+        if(std::abs(wo.z) < T(1e-4))
+            return r;
+        V<T> wi;
+        if(wo.z < 0)
+        {
+            if(trans == 0)
+                return r;
+            T mF = clampv(diel_fresnel(ior, T(1), wo.z), T(0.1), T(0.9));
+            wi = s0 >= mF ? s_trans(wo, s1, s2) : s_inner(wo, s1, s2);
+        }
+        else
+        {
+            T sel = s0;
+            if(sel < wd)
+                wi = hemi_zw(s1, s2);
+            else
+            {
+                sel -= wd;
+                if(sel < wt)
+                    wi = s_trans(wo, s1, s2);
+                else
+                {
+                    sel -= wt;
+                    wi = sel < ws ? s_spec(wo, s1, s2) : s_clear(wo, s1, s2);
+                }
+            }
+        }
+        if(zero3(wi))
+            return r;
+        r.dir = wi;
+        r.f = disney_eval(wi, wo);
+        r.pdf = disney_pdf(wi, wo);
+        V<T> v = r.f * (std::abs(wi.z) / r.pdf);
+        if(std::max(std::max(v.x, v.y), v.z) > T(10))
+            return CS<T>();
+        return r;
+    }
+
+    // ---- component dispatch (diffuse.cpp:10-60, metal, disney)
+    CS<T> sample(V<T> wo, T s0, T s1, T s2) const
+    {
+        CS<T> r;
+        if(type == 0)
+        {
+            if(wo.z <= 0)
+                return r;
+            r.dir = hemi_zw(s1, s2);
+            r.f = C / PI_T<T>();
+            r.pdf = pdf_hemi_zw(r.dir);
+            return r;
+        }
+        if(type == 1)
+        {
+            if(wo.z > 0)
+            {
+                V<T> wh = nrm(sample_vndf(wo, ax, ay, s1, s2));
+                if(wh.z > 0)
+                {
+                    V<T> wi = nrm(T(2) * dot(wo, wh) * wh - wo);
+                    if(wi.z > 0)
+                    {
+                        r.dir = wi;
+                        metal_ep(wi, wo, r.f, r.pdf);
+                    }
+                }
+            }
+            return r;
+        }
+        return disney_sample(wo, s0, s1, s2);
+    }
+    V<T> eval(V<T> wi, V<T> wo) const
+    {
+        if(type == 0)
+            return (wi.z <= 0 || wo.z <= 0) ? V<T>(0) : C / PI_T<T>();
+        if(type == 1)
+        {
+            V<T> f;
+            T p;
+            metal_ep(wi, wo, f, p);
+            return f;
+        }
+        return disney_eval(wi, wo);
+    }
+    T pdf(V<T> wi, V<T> wo) const
+    {
+        if(type == 0)
+            return (wi.z <= 0 || wo.z <= 0) ? T(0) : pdf_hemi_zw(wi);
+        if(type == 1)
+        {
+            V<T> f;
+            T p;
+            metal_ep(wi, wo, f, p);
+            return p;
+        }
+        return disney_pdf(wi, wo);
+    }
+};
+
+} // namespace orc
+
+using namespace orc;
+
+// ------------------------------------------------------------------ scene for the renderer
+
+struct OracleScene
+{
+    const float *tris;      // 9 floats per flattened world triangle
+    const uint32_t *ids;    // (instance, primitive) per flattened triangle
+    uint64_t ntri;
+
+    int32_t ninst;
+    const float *inst_l2w;  // 12 per instance, rows of the 3x4 local-to-world matrix
+    const float *inst_w2l;  // 12 per instance, the reference's stored inverse
+    const int32_t *inst_geo, *inst_mat, *inst_light, *inst_inner, *inst_outer;
+
+    int32_t ngeo;
+    const uint64_t *geo_offset, *geo_count;
+    const float *geo_area_total;
+    const float *shade;     // [6][total_geo_tris][4]
+    uint64_t total_geo_tris;
+    const float *tri_area;  // per geometry triangle
+    const float *local_pos; // 9 per geometry triangle: a, b, c (object space)
+
+    int32_t nmat;
+    const float *mat;       // 20 per material: type, shadow_terminator, p[16], pad, pad
+
+    int32_t nlight;
+    const int32_t *light_inst, *light_geo;
+    const float *light_scale, *light_intensity;
+    int32_t env_type;
+    float env_lower[3], env_upper[3], env_up[3];
+
+    int32_t vacuum_medium;
+    float world_diagonal;
+
+    float eye[3], lbc[3], film_x[3], film_y[3];
+    int32_t width, height, spp, min_depth, max_depth;
+    float rr_threshold, rr_cont_prob;
+    int32_t sampler, filter;
+    float filter_radius, filter_alpha;
+};
+
+namespace {
+
+struct Prepared
+{
+    const OracleScene *S;
+    Bvh bvh;
+    std::vector<Alias> geo_alias;   // only for light geometries
+    Alias filter;
+    Sampler::HC hc;
+};
+
+V3f pt(const float *m, V3f p)
+{
+    return V3f(m[0] * p.x + m[1] * p.y + m[2] * p.z + m[3], m[4] * p.x + m[5] * p.y + m[6] * p.z + m[7],
+               m[8] * p.x + m[9] * p.y + m[10] * p.z + m[11]);
+}
+V3f vec(const float *m, V3f v)
+{
+    return V3f(m[0] * v.x + m[1] * v.y + m[2] * v.z, m[4] * v.x + m[5] * v.y + m[6] * v.z,
+               m[8] * v.x + m[9] * v.y + m[10] * v.z);
+}
+V3f nor(const float *inv, V3f n)
+{
+    return V3f(inv[0] * n.x + inv[4] * n.y + inv[8] * n.z, inv[1] * n.x + inv[5] * n.y + inv[9] * n.z,
+               inv[2] * n.x + inv[6] * n.y + inv[10] * n.z);
+}
+
+// intersection_offset (common/btrc/utils/intersection.cpp:5-37)
+V3f ioffset(V3f pos, V3f n)
+{
+    const float ORIGIN = 1.0f / 32.0f, FS = 1.0f / 65536.0f, IS = 256.0f;
+    auto one = [&](float p, float nn) {
+        const int of = static_cast<int>(2 * IS * nn);
+        int32_t pi;
+        std::memcpy(&pi, &p, 4);
+        pi += p < 0 ? -of : of;
+        float pf;
+        std::memcpy(&pf, &pi, 4);
+        return std::fabs(p) < ORIGIN ? p + FS * nn : pf;
+    };
+    return V3f(one(pos.x, n.x), one(pos.y, n.y), one(pos.z, n.z));
+}
+V3f ioffset_dir(V3f pos, V3f n, V3f d) { return ioffset(pos, dot(n, d) > 0 ? n : -n); }
+
+V3f sky(const OracleScene &S, V3f d)
+{
+    const V3f up(S.env_up[0], S.env_up[1], S.env_up[2]);
+    const float c = dot(up, nrm(d));
+    const float s = std::min(1.0f, std::max(0.0f, 0.5f * (c + 1.0f)));
+    return V3f(S.env_lower[0], S.env_lower[1], S.env_lower[2]) * (1.0f - s) +
+           V3f(S.env_upper[0], S.env_upper[1], S.env_upper[2]) * s;
+}
+
+int nlights_total(const OracleScene &S) { return S.nlight + (S.env_type ? 1 : 0); }
+
+struct ShadeFrame
+{
+    Frame<float> g, s;
+    bool black(V3f w) const { return g.upper(w) != s.upper(w); }
+    ShadeFrame flip(V3f wo) const
+    {
+        ShadeFrame f;
+        f.g = g;
+        f.s = black(wo) ? g : s;
+        return f;
+    }
+    float corr(V3f wi) const
+    {
+        const float down = std::fabs(dot(g.z, wi));
+        return down > 1e-4f ? std::fabs(dot(s.z, wi)) / down : 1.0f;
+    }
+    float term(V3f wi) const
+    {
+        const float a = dot(g.z, wi), b = dot(s.z, wi), c = dot(g.z, s.z);
+        const float t = std::min(1.0f, std::max(0.0f, a / (b * c)));
+        return -t * t * t + t * t + t;
+    }
+};
+
+void splat(double *film, int w, uint32_t px, uint32_t py, V3f v)
+{
+    if(!std::isfinite(v.x) || !std::isfinite(v.y) || !std::isfinite(v.z))
+        return;
+    double *p = film + (static_cast<size_t>(py) * w + px) * 4;
+    p[0] += v.x;
+    p[1] += v.y;
+    p[2] += v.z;
+}
+
+// One camera path with the wavefront integrator's semantics
+// (generate.cpp:33-87, shade.cpp:29-235, shadow.cpp:39-76, helper.cpp:9-207).
+void trace_path(const Prepared &P, uint64_t g, double *film)
+{
+    const OracleScene &S = *P.S;
+    const uint64_t pixels = static_cast<uint64_t>(S.width) * S.height;
+    const uint64_t pixel = g % pixels, sample = g / pixels;
+    const uint32_t px = static_cast<uint32_t>(pixel % S.width), py = static_cast<uint32_t>(pixel / S.width);
+    Sampler smp;
+    smp.init(S.sampler, P.hc, px, py, static_cast<uint32_t>(sample));
+    float fx, fy;
+    if(S.filter == 1)
+    {
+        const uint32_t cell = P.filter.sample(smp.get1d());
+        const uint32_t gy = cell / 256, gx = cell % 256;
+        const float r = S.filter_radius;
+        const float x0 = -r + 2 * r / 256 * static_cast<float>(gx), x1 = -r + 2 * r / 256 * static_cast<float>(gx + 1);
+        const float y0 = -r + 2 * r / 256 * static_cast<float>(gy), y1 = -r + 2 * r / 256 * static_cast<float>(gy + 1);
+        fx = lerp1(x0, x1, smp.get1d());
+        fy = lerp1(y0, y1, smp.get1d());
+    }
+    else
+    {
+        fx = smp.get1d() - 0.5f;
+        fy = smp.get1d() - 0.5f;
+    }
+    const float film_x = (static_cast<float>(px) + 0.5f + fx) / static_cast<float>(S.width);
+    const float film_y = (static_cast<float>(py) + 0.5f + fy) / static_cast<float>(S.height);
+    (void)smp.get1d();
+    const V3f eye(S.eye[0], S.eye[1], S.eye[2]);
+    const V3f dst = V3f(S.lbc[0], S.lbc[1], S.lbc[2]) + film_x * V3f(S.film_x[0], S.film_x[1], S.film_x[2]) +
+                    film_y * V3f(S.film_y[0], S.film_y[1], S.film_y[2]);
+    V3f o = eye, d = nrm(dst - eye);
+    film[(static_cast<size_t>(py) * S.width + px) * 4 + 3] += 1.0;
+
+    V3f beta(1.0f), rad(0.0f), beta_le(1.0f);
+    float bsdf_pdf = -1.0f;
+    int depth = 0;
+    const int NL = nlights_total(S);
+    for(;;)
+    {
+        float od[3] = { o.x, o.y, o.z }, dd[3] = { d.x, d.y, d.z };
+        const Bvh::Hit h = P.bvh.closest(od, dd, FMAX);
+        if(!h.hit)
+        {
+            V3f le(0.0f);
+            if(S.env_type)
+            {
+                const V3f L = sky(S, d);
+                if(bsdf_pdf < 0)
+                    le = beta_le * L / -bsdf_pdf;
+                else
+                    le = beta_le * L / (bsdf_pdf + (1.0f / NL) * (1.0f / (4.0f * PIf)));
+            }
+            splat(film, S.width, px, py, le + rad);
+            return;
+        }
+        const int inst = static_cast<int>(h.inst);
+        const float *l2w = S.inst_l2w + inst * 12, *w2l = S.inst_w2l + inst * 12;
+        const int geo = S.inst_geo[inst];
+        const uint64_t ti = S.geo_offset[geo] + h.prim;
+        auto sh = [&](int k) {
+            const float *p = S.shade + (static_cast<uint64_t>(k) * S.total_geo_tris + ti) * 4;
+            return V3f(p[0], p[1], p[2]);
+        };
+        // get_hitinfo (core/btrc/core/scene.cpp:9-64)
+        const V3f pos = o + h.t * d;
+        Frame<float> gf(sh(0), sh(1), sh(2));
+        gf.x = nrm(vec(l2w, gf.x));
+        gf.y = nrm(vec(l2w, gf.y));
+        gf.z = nrm(nor(w2l, gf.z));
+        const V3f interp = nrm(nor(w2l, sh(3) + sh(4) * h.b1 + sh(5) * h.b2));
+
+        // area light hit with MIS
+        const int light = S.inst_light[inst];
+        if(light >= 0)
+        {
+            const V3f I(S.light_intensity[light * 3], S.light_intensity[light * 3 + 1], S.light_intensity[light * 3 + 2]);
+            const V3f le = dot(gf.z, -d) >= 0 ? I : V3f(0.0f);
+            if(bsdf_pdf < 0)
+                rad = rad + beta_le * le / -bsdf_pdf;
+            else
+            {
+                float pdf_li = 0;
+                const V3f to_ref = o - pos;
+                if(dot(gf.z, to_ref) > 0)
+                {
+                    const float sc = S.light_scale[light];
+                    const float d2 = dot(to_ref, to_ref);
+                    const float d3 = std::sqrt(d2) * d2;
+                    pdf_li = 1.0f / (sc * sc) * (1.0f / S.geo_area_total[S.light_geo[light]]) * d3 /
+                             std::fabs(dot(gf.z, to_ref));
+                }
+                rad = rad + beta_le * le / (bsdf_pdf + (1.0f / NL) * pdf_li);
+            }
+        }
+
+        // Russian roulette (helper.cpp:67-97)
+        if(depth >= S.min_depth)
+        {
+            if(depth >= S.max_depth)
+            {
+                splat(film, S.width, px, py, rad);
+                return;
+            }
+            const float sam = smp.get1d();
+            if(lum(beta) < S.rr_threshold)
+            {
+                if(sam > S.rr_cont_prob)
+                {
+                    splat(film, S.width, px, py, rad);
+                    return;
+                }
+                beta = beta / S.rr_cont_prob;
+            }
+        }
+
+        // light sample (helper.cpp:9-61, 127-142)
+        float ls0, ls1, ls2;
+        smp.get3d(ls0, ls1, ls2);
+        const float lsel = smp.get1d();
+        bool ls_ok = false;
+        V3f ls_o, ls_d, ls_li;
+        float ls_t1 = 0, ls_pdf = 0;
+        if(NL > 0)
+        {
+            const int li = std::min(static_cast<int>(lsel * static_cast<float>(NL)), NL - 1);
+            const float spdf = 1.0f / static_cast<float>(NL);
+            if(li < S.nlight)
+            {
+                const int lg = S.light_geo[li];
+                const int linst = S.light_inst[li];
+                const uint32_t prim = P.geo_alias[lg].sample(ls0);
+                const float tq = std::sqrt(ls1);
+                const float u = 1.0f - tq, v = tq * ls2;
+                const float *lp = S.local_pos + (S.geo_offset[lg] + prim) * 9;
+                const V3f a(lp[0], lp[1], lp[2]), b(lp[3], lp[4], lp[5]), c(lp[6], lp[7], lp[8]);
+                const V3f lpos = a + (b - a) * u + (c - a) * v;
+                const float *ez = S.shade + (2 * S.total_geo_tris + S.geo_offset[lg] + prim) * 4;
+                const V3f spos = pt(S.inst_l2w + linst * 12, lpos);
+                const V3f snor = nrm(nor(S.inst_w2l + linst * 12, nrm(V3f(ez[0], ez[1], ez[2]))));
+                const V3f p2r = pos - spos;
+                const float d2 = dot(p2r, p2r);
+                const float sc = S.light_scale[li];
+                const float pdf_sa = 1.0f / (sc * sc) * (1.0f / S.geo_area_total[lg]) * d2 / std::fabs(dot(snor, nrm(p2r)));
+                const V3f I(S.light_intensity[li * 3], S.light_intensity[li * 3 + 1], S.light_intensity[li * 3 + 2]);
+                ls_li = dot(p2r, snor) > 0 ? I : V3f(0.0f);
+                const V3f diff = spos - pos;
+                const V3f dstp = ioffset_dir(spos, snor, -diff);
+                ls_o = ioffset_dir(pos, gf.z, diff);
+                ls_d = dstp - ls_o;
+                ls_t1 = 1.0f;
+                ls_pdf = spdf * pdf_sa;
+            }
+            else
+            {
+                const float z = 1.0f - (ls0 + ls0);
+                const float phi = 2.0f * PIf * ls1;
+                const float r = std::sqrt(std::max(0.0f, 1.0f - z * z));
+                const V3f dir(r * std::cos(phi), r * std::sin(phi), z);
+                ls_o = ioffset_dir(pos, gf.z, dir);
+                ls_d = dir;
+                ls_t1 = FMAX;
+                ls_li = sky(S, dir);
+                ls_pdf = spdf * (1.0f / (4.0f * PIf));
+            }
+            ls_ok = true;
+        }
+
+        // material
+        const float *mr = S.mat + S.inst_mat[inst] * 20;
+        const int mtype = static_cast<int>(mr[0]);
+        const bool term = mr[1] != 0.0f;
+        ShadeFrame fr;
+        fr.g = gf;
+        fr.s = gf.rotate_to_new_z(interp);
+        Mat<float> M;
+        if(mtype <= 2)
+            M.init(mtype, mr + 2);
+        float u0, u1, u2;
+        smp.get3d(u0, u1, u2);
+        const V3f wo = -d;
+        CS<float> bs;
+        auto eval = [&](V3f wi) -> V3f {
+            if(mtype > 2)
+                return V3f(0.0f);
+            const ShadeFrame f = fr.flip(wo);
+            const V3f lwi = nrm(f.s.g2l(wi)), lwo = nrm(f.s.g2l(wo));
+            float k = f.corr(wi);
+            if(term)
+                k *= fr.term(wi);
+            return M.eval(lwi, lwo) * k;
+        };
+        auto pdf = [&](V3f wi) -> float {
+            if(mtype > 2)
+                return 0.0f;
+            const ShadeFrame f = fr.flip(wo);
+            return M.pdf(nrm(f.s.g2l(wi)), nrm(f.s.g2l(wo)));
+        };
+        if(mtype == 4)
+        {
+            // invisible.cpp: pass straight through
+            bs.f = V3f(1.0f / std::fabs(dot(gf.z, nrm(wo))));
+            bs.dir = -wo;
+            bs.pdf = 1;
+            bs.delta = true;
+        }
+        else if(mtype == 5)
+        {
+            // mirror.cpp
+            const ShadeFrame f = fr.flip(wo);
+            V3f lwo = f.s.g2l(wo);
+            if(lwo.z > 0)
+            {
+                lwo = nrm(lwo);
+                const V3f wi = f.s.l2g(V3f(-lwo.x, -lwo.y, lwo.z));
+                if(!fr.black(wi))
+                {
+                    const V3f col(mr[2], mr[3], mr[4]);
+                    bs.f = schlick3(col, lwo.z) / lwo.z * f.corr(wi);
+                    bs.dir = wi;
+                    bs.pdf = 1;
+                    bs.delta = true;
+                }
+            }
+        }
+        else if(mtype <= 2)
+        {
+            // BSDFAggregate::sample (aggregate.cpp:32-105)
+            const ShadeFrame f = fr.flip(wo);
+            const V3f lwo = nrm(f.s.g2l(wo));
+            const CS<float> c = M.sample(lwo, u0, u1, u2);
+            if(c.pdf > 0)
+            {
+                const V3f wi = f.s.l2g(c.dir);
+                if(!fr.black(wi))
+                {
+                    float k = f.corr(wi);
+                    if(term)
+                        k *= fr.term(wi);
+                    bs.f = c.f * k;
+                    bs.dir = wi;
+                    bs.pdf = c.pdf;
+                }
+            }
+        }
+        V3f sf(0.0f);
+        float spdf = 0;
+        if(ls_ok)
+        {
+            sf = eval(ls_d);
+            ls_ok = !zero3(sf);
+            if(ls_ok)
+                spdf = pdf(ls_d);
+        }
+        if(ls_ok)
+        {
+            const float c = std::fabs(dot(nrm(ls_d), gf.z));
+            const V3f beta_li = ls_li * beta * sf * c / (spdf + ls_pdf);
+            const float so[3] = { ls_o.x, ls_o.y, ls_o.z }, sdir[3] = { ls_d.x, ls_d.y, ls_d.z };
+            if(!P.bvh.any(so, sdir, ls_t1))
+                splat(film, S.width, px, py, beta_li);
+        }
+        if(zero3(bs.f))
+        {
+            splat(film, S.width, px, py, rad);
+            return;
+        }
+        const V3f nd = nrm(bs.dir);
+        const float c = std::fabs(dot(nd, gf.z));
+        beta_le = beta * c * bs.f;
+        beta = beta_le / bs.pdf;
+        o = ioffset_dir(pos, gf.z, nd);
+        d = nd;
+        bsdf_pdf = bs.delta ? -bs.pdf : bs.pdf;
+        ++depth;
+    }
+}
+
+} // namespace
+
+extern "C" {
+
+void *oracle_bvh_build(const float *tris, const uint32_t *ids, uint64_t n)
+{
+    auto *b = new Bvh();
+    b->build(tris, ids, n);
+    return b;
+}
+
+void oracle_bvh_free(void *b) { delete static_cast<Bvh *>(b); }
+
+// rays: 8 floats each (o.xyz, medium, d.xyz, t1); hits: 4 floats (t, prim bits, b1, b2)
+void oracle_trace_closest(const void *bvh, const float *rays, uint64_t m, uint32_t *flags, float *hits, int threads)
+{
+    const Bvh &B = *static_cast<const Bvh *>(bvh);
+    parallel_for(m, threads, [&](uint64_t i) {
+        const float *r = rays + i * 8;
+        const Bvh::Hit h = B.closest(r, r + 4, r[7]);
+        flags[i] = h.hit ? (h.inst | (1u << 30)) : 0u;
+        float *o = hits + i * 4;
+        o[0] = h.hit ? h.t : 0.0f;
+        const uint32_t prim = h.hit ? h.prim : 0u;
+        std::memcpy(&o[1], &prim, 4);
+        o[2] = h.hit ? h.b1 : 0.0f;
+        o[3] = h.hit ? h.b2 : 0.0f;
+    });
+}
+
+void oracle_trace_any(const void *bvh, const float *rays, uint64_t m, uint32_t *occ, int threads)
+{
+    const Bvh &B = *static_cast<const Bvh *>(bvh);
+    parallel_for(m, threads, [&](uint64_t i) {
+        const float *r = rays + i * 8;
+        occ[i] = B.any(r, r + 4, r[7]) ? 1u : 0u;
+    });
+}
+
+void oracle_sampler_batch(int type, int width, int height, const uint32_t *pixel_xy, const uint32_t *sample_index,
+                          uint64_t n, uint32_t dims, float *out)
+{
+    const Sampler::HC hc = Sampler::consts(width, height);
+    for(uint64_t i = 0; i < n; ++i)
+    {
+        Sampler s;
+        s.init(type, hc, pixel_xy[i] & 0xffffu, pixel_xy[i] >> 16, sample_index[i]);
+        for(uint32_t k = 0; k < dims; ++k)
+            out[i * dims + k] = s.get1d();
+    }
+}
+
+// PCG32 raw output stream for the published known-answer test
+void oracle_pcg32_stream(uint64_t initstate, uint64_t initseq, uint32_t n, uint32_t *out)
+{
+    Pcg p;
+    p.seed(initstate, initseq);
+    for(uint32_t i = 0; i < n; ++i)
+        out[i] = p.next();
+}
+
+uint64_t oracle_murmur64a(const uint8_t *key, uint64_t len, uint64_t seed) { return murmur64a(key, len, seed); }
+
+// FP64 local-space BSDF: material records of 16 floats (p[0..14], type in [15])
+// op 0: out 4 doubles (f.rgb, pdf); op 1: out 7 doubles (f.rgb, pdf, wi.xyz)
+void oracle_bsdf_batch(int op, const float *mat, const double *wo, const double *wu, uint64_t n, double *out)
+{
+    for(uint64_t i = 0; i < n; ++i)
+    {
+        Mat<double> M;
+        M.init(static_cast<int>(mat[i * 16 + 15]), mat + i * 16);
+        const V<double> lwo(wo[i * 3], wo[i * 3 + 1], wo[i * 3 + 2]);
+        if(op == 0)
+        {
+            const V<double> lwi(wu[i * 3], wu[i * 3 + 1], wu[i * 3 + 2]);
+            const V<double> f = M.eval(lwi, lwo);
+            out[i * 4 + 0] = f.x;
+            out[i * 4 + 1] = f.y;
+            out[i * 4 + 2] = f.z;
+            out[i * 4 + 3] = M.pdf(lwi, lwo);
+        }
+        else
+        {
+            const CS<double> s = M.sample(lwo, wu[i * 3], wu[i * 3 + 1], wu[i * 3 + 2]);
+            out[i * 7 + 0] = s.f.x;
+            out[i * 7 + 1] = s.f.y;
+            out[i * 7 + 2] = s.f.z;
+            out[i * 7 + 3] = s.pdf;
+            out[i * 7 + 4] = s.dir.x;
+            out[i * 7 + 5] = s.dir.y;
+            out[i * 7 + 6] = s.dir.z;
+        }
+    }
+}
+
+void *oracle_prepare(const OracleScene *S)
+{
+    auto *P = new Prepared();
+    P->S = S;
+    P->bvh.build(S->tris, S->ids, S->ntri);
+    P->geo_alias.resize(S->ngeo);
+    for(int l = 0; l < S->nlight; ++l)
+    {
+        const int g = S->light_geo[l];
+        if(!P->geo_alias[g].accept.empty())
+            continue;
+        std::vector<float> a(S->tri_area + S->geo_offset[g], S->tri_area + S->geo_offset[g] + S->geo_count[g]);
+        P->geo_alias[g].init(a);
+    }
+    if(S->filter == 1)
+    {
+        // GaussianFilter::commit (film_filter/gaussian.cpp:27-52)
+        const float r = S->filter_radius, al = S->filter_alpha;
+        const float expv = std::exp(-al * r * r);
+        auto gau = [&](float x) { return std::max(0.0f, std::exp(-al * x * x) - expv); };
+        std::vector<float> v(256 * 256, 0.0f);
+        for(int y = 0; y < 256; ++y)
+        {
+            const float yf = 2 * r * (y + 0.5f) / 256 - r;
+            for(int x = 0; x < 256; ++x)
+            {
+                const float xf = 2 * r * (x + 0.5f) / 256 - r;
+                if(xf * xf + yf * yf < r * r)
+                    v[y * 256 + x] = gau(xf) * gau(yf);
+            }
+        }
+        P->filter.init(v);
+    }
+    P->hc = Sampler::consts(S->width, S->height);
+    return P;
+}
+
+void oracle_release(void *p) { delete static_cast<Prepared *>(p); }
+
+// Render the pixel range [pixel_begin, pixel_end) with samples [sample_begin, sample_end)
+// into film (4 doubles per pixel of the full image: rgb sum, weight). Threads split pixels.
+void oracle_render(const void *prepared, uint64_t pixel_begin, uint64_t pixel_end, uint32_t sample_begin,
+                   uint32_t sample_end, double *film, int threads)
+{
+    const Prepared &P = *static_cast<const Prepared *>(prepared);
+    const uint64_t pixels = static_cast<uint64_t>(P.S->width) * P.S->height;
+    parallel_for(pixel_end - pixel_begin, threads, [&](uint64_t k) {
+        const uint64_t pix = pixel_begin + k;
+        for(uint32_t s = sample_begin; s < sample_end; ++s)
+            trace_path(P, static_cast<uint64_t>(s) * pixels + pix, film);
+    });
+}
+
+} // extern "C"
