@@ -72,25 +72,44 @@ BT_HD V3 sample_sphere_uniform(float u1, float u2)
     return V3(r * cosf(phi), r * sinf(phi), z);
 }
 
-BT_HD float cos2sin(float c) { return sqrtf(fmaxf(0.0f, 1.0f - c * c)); }
+// Numerics. The reference evaluates these quantities as sqrt(1 - c*c), sin/cos of
+// atan2(y, x) and sqrt(1 - z*z) / z. The same quantities are computed here in forms that
+// stay accurate in FP32 near the specular peak, where 1 - c*c cancels catastrophically
+// and the microfacet distribution amplifies that error by ~1/alpha^2:
+//   sqrt(1 - c^2)        -> sqrt((1 - c)(1 + c))   (1 - c is exact for c in [0.5, 1])
+//   cos/sin(atan2(y, x)) -> x / r, y / r           (r = |(x, y)|; 1, 0 when r == 0)
+//   sin(theta_h)         -> |(h.x, h.y)|           (h a normalised half vector)
+// The values are mathematically identical; only the FP32 rounding differs.
+BT_HD float cos2sin(float c) { return sqrtf(fmaxf(0.0f, (1.0f - c) * (1.0f + c))); }
 
 BT_HD float tan_theta(V3 w)
 {
-    const float t = 1.0f - w.z * w.z;
+    const float t = (1.0f - w.z) * (1.0f + w.z);
     return t > 0 ? sqrtf(t) / w.z : 0.0f;
 }
 
-BT_HD float phi_of(V3 w)
+// cos(phi), sin(phi) of the azimuth of w
+BT_HD void phi_cs(V3 w, float &c, float &s)
 {
-    float r = 0.0f;
-    if(w.x != 0 || w.y != 0)
+    const float r2 = w.x * w.x + w.y * w.y;
+    if(r2 > 0.0f)
     {
-        r = atan2f(w.y, w.x);
-        if(r < 0)
-            r += 2 * PI;
+        const float inv = 1.0f / sqrtf(r2);
+        c = w.x * inv;
+        s = w.y * inv;
     }
-    return r;
+    else
+    {
+        c = 1.0f;
+        s = 0.0f;
+    }
 }
+
+// sin(theta) of a normalised vector
+BT_HD float sin_theta_n(V3 w) { return sqrtf(w.x * w.x + w.y * w.y); }
+
+// anisotropic GTR2 D of a normalised half vector
+BT_HD float gtr2_of(V3 h, float ax, float ay);
 
 // ---------------------------------------------------------------- fresnel
 
@@ -103,11 +122,11 @@ BT_HD float dielectric_fresnel(float eta_i, float eta_o, float cos_theta_i)
         eta_o = t;
         cos_theta_i = -cos_theta_i;
     }
-    const float sin_theta_i = sqrtf(fmaxf(0.0f, 1.0f - cos_theta_i * cos_theta_i));
+    const float sin_theta_i = cos2sin(cos_theta_i);
     const float sin_theta_t = eta_o / eta_i * sin_theta_i;
     if(sin_theta_t >= 1)
         return 1.0f;
-    const float cos_theta_t = sqrtf(fmaxf(0.0f, 1.0f - sin_theta_t * sin_theta_t));
+    const float cos_theta_t = cos2sin(sin_theta_t);
     const float para = (eta_i * cos_theta_i - eta_o * cos_theta_t) / (eta_i * cos_theta_i + eta_o * cos_theta_t);
     const float perp = (eta_o * cos_theta_i - eta_i * cos_theta_t) / (eta_o * cos_theta_i + eta_i * cos_theta_t);
     return 0.5f * (para * para + perp * perp);
@@ -140,6 +159,13 @@ BT_HD float mf_aniso_gtr2(float sin_phi_h, float cos_phi_h, float sin_theta_h, f
     const float A = sqrf(cos_phi_h / ax) + sqrf(sin_phi_h / ay);
     const float RD = sqrf(sin_theta_h) * A + sqrf(cos_theta_h);
     return 1.0f / (PI * ax * ay * sqrf(RD));
+}
+
+BT_HD float gtr2_of(V3 h, float ax, float ay)
+{
+    float c, s;
+    phi_cs(h, c, s);
+    return mf_aniso_gtr2(s, c, sin_theta_n(h), h.z, ax, ay);
 }
 
 BT_HD float mf_smith_aniso_gtr2(float cos_phi, float sin_phi, float ax, float ay, float tan_t)
@@ -253,13 +279,12 @@ BT_HD void metal_eval_pdf(const MetalParams &m, V3 lwi, V3 lwo, V3 &f, float &pd
     const float cti = lwi.z, cto = lwo.z;
     const V3 lwh = normalize(lwi + lwo);
     const float ctd = dot(lwi, lwh);
-    const float phi_h = phi_of(lwh);
-    const float sph = sinf(phi_h), cph = cosf(phi_h);
-    const float cth = lwh.z, sth = cos2sin(cth);
-    const float D = mf_aniso_gtr2(sph, cph, sth, cth, m.ax, m.ay);
-    const float phi_i = phi_of(lwi), phi_o = phi_of(lwo);
-    const float Go = mf_smith_aniso_gtr2(cosf(phi_o), sinf(phi_o), m.ax, m.ay, tan_theta(lwo));
-    const float Gi = mf_smith_aniso_gtr2(cosf(phi_i), sinf(phi_i), m.ax, m.ay, tan_theta(lwi));
+    const float D = gtr2_of(lwh, m.ax, m.ay);
+    float cpi, spi, cpo, spo;
+    phi_cs(lwi, cpi, spi);
+    phi_cs(lwo, cpo, spo);
+    const float Go = mf_smith_aniso_gtr2(cpo, spo, m.ax, m.ay, tan_theta(lwo));
+    const float Gi = mf_smith_aniso_gtr2(cpi, spi, m.ax, m.ay, tan_theta(lwi));
     const V3 F = schlick3(m.R0, ctd);
     f = F * (D * Gi * Go / fabsf(4.0f * cti * cto));
     pdf = Go * D / (4.0f * lwo.z);
@@ -357,12 +382,12 @@ BT_HD V3 disney_eval_trans(const DisneyParams &d, V3 lwi, V3 lwo)
         lwh = -lwh;
     const float ctd = dot(lwo, lwh);
     const float F = dielectric_fresnel(d.ior, 1, ctd);
-    const float phi_h = phi_of(lwh);
-    const float cth = lwh.z, sth = cos2sin(cth);
-    const float D = mf_aniso_gtr2(sinf(phi_h), cosf(phi_h), sth, cth, d.trans_ax, d.trans_ay);
-    const float phi_i = phi_of(lwi), phi_o = phi_of(lwo);
-    const float G = mf_smith_aniso_gtr2(cosf(phi_i), sinf(phi_i), d.trans_ax, d.trans_ay, tan_theta(lwi)) *
-                    mf_smith_aniso_gtr2(cosf(phi_o), sinf(phi_o), d.trans_ax, d.trans_ay, tan_theta(lwo));
+    const float D = gtr2_of(lwh, d.trans_ax, d.trans_ay);
+    float cpi, spi, cpo, spo;
+    phi_cs(lwi, cpi, spi);
+    phi_cs(lwo, cpo, spo);
+    const float G = mf_smith_aniso_gtr2(cpi, spi, d.trans_ax, d.trans_ay, tan_theta(lwi)) *
+                    mf_smith_aniso_gtr2(cpo, spo, d.trans_ax, d.trans_ay, tan_theta(lwo));
     const float sdem = ctd + eta * dot(lwi, lwh);
     const float corr = 1.0f / eta;  // radiance transport
     const V3 sqrtC(sqrtf(d.C.x), sqrtf(d.C.y), sqrtf(d.C.z));
@@ -377,12 +402,12 @@ BT_HD V3 disney_eval_inner_refl(const DisneyParams &d, V3 lwi, V3 lwo)
     const V3 lwh = -normalize(lwi + lwo);
     const float ctd = dot(lwo, lwh);
     const float F = dielectric_fresnel(d.ior, 1, ctd);
-    const float phi_h = phi_of(lwh);
-    const float cth = lwh.z, sth = cos2sin(cth);
-    const float D = mf_aniso_gtr2(sinf(phi_h), cosf(phi_h), sth, cth, d.trans_ax, d.trans_ay);
-    const float phi_i = phi_of(lwi), phi_o = phi_of(lwo);
-    const float G = mf_smith_aniso_gtr2(cosf(phi_i), sinf(phi_i), d.trans_ax, d.trans_ay, tan_theta(lwi)) *
-                    mf_smith_aniso_gtr2(cosf(phi_o), sinf(phi_o), d.trans_ax, d.trans_ay, tan_theta(lwo));
+    const float D = gtr2_of(lwh, d.trans_ax, d.trans_ay);
+    float cpi, spi, cpo, spo;
+    phi_cs(lwi, cpi, spi);
+    phi_cs(lwo, cpo, spo);
+    const float G = mf_smith_aniso_gtr2(cpi, spi, d.trans_ax, d.trans_ay, tan_theta(lwi)) *
+                    mf_smith_aniso_gtr2(cpo, spo, d.trans_ax, d.trans_ay, tan_theta(lwo));
     return d.C * (d.transmission * fabsf(F * D * G / (4.0f * lwi.z * lwo.z)));
 }
 
@@ -395,12 +420,12 @@ BT_HD V3 disney_eval_specular(const DisneyParams &d, V3 lwi, V3 lwo)
     const V3 dielectric = Cspec * dielectric_fresnel(d.ior, 1.0f, ctd);
     const V3 conductor = schlick3(Cspec, ctd);
     const V3 F = lerp3(d.specular * dielectric, conductor, d.metallic);
-    const float phi_h = phi_of(lwh);
-    const float cth = lwh.z, sth = cos2sin(cth);
-    const float D = mf_aniso_gtr2(sinf(phi_h), cosf(phi_h), sth, cth, d.ax, d.ay);
-    const float phi_i = phi_of(lwi), phi_o = phi_of(lwo);
-    const float G = mf_smith_aniso_gtr2(cosf(phi_i), sinf(phi_i), d.ax, d.ay, tan_theta(lwi)) *
-                    mf_smith_aniso_gtr2(cosf(phi_o), sinf(phi_o), d.ax, d.ay, tan_theta(lwo));
+    const float D = gtr2_of(lwh, d.ax, d.ay);
+    float cpi, spi, cpo, spo;
+    phi_cs(lwi, cpi, spi);
+    phi_cs(lwo, cpo, spo);
+    const float G = mf_smith_aniso_gtr2(cpi, spi, d.ax, d.ay, tan_theta(lwi)) *
+                    mf_smith_aniso_gtr2(cpo, spo, d.ax, d.ay, tan_theta(lwo));
     return F * (D * G / fabsf(4.0f * cti * cto));
 }
 
@@ -433,7 +458,7 @@ BT_HD V3 disney_eval(const DisneyParams &d, V3 lwi, V3 lwo)
     if(d.clearcoat > 0.0f)
     {
         const float tti = tan_theta(lwi), tto = tan_theta(lwo);
-        const float cth = lwh.z, sth = cos2sin(cth);
+        const float cth = lwh.z, sth = sin_theta_n(lwh);
         const float D = mf_gtr1(sth, cth, d.clearcoat_roughness);
         const float F = schlick(0.04f, ctd);
         const float G = mf_smith_gtr2(tti, 0.25f) * mf_smith_gtr2(tto, 0.25f);
@@ -453,19 +478,16 @@ BT_HD float disney_pdf_transmission(const DisneyParams &d, V3 lwi, V3 lwo)
         return 0.0f;
     const float sdem = dot(lwo, lwh) + eta * dot(lwi, lwh);
     const float dwh_to_dwi = eta * eta * dot(lwi, lwh) / (sdem * sdem);
-    const float phi_h = phi_of(lwh);
-    const float cth = lwh.z, sth = cos2sin(cth);
-    const float D = mf_aniso_gtr2(sinf(phi_h), cosf(phi_h), sth, cth, d.trans_ax, d.trans_ay);
+    const float D = gtr2_of(lwh, d.trans_ax, d.trans_ay);
     return fabsf(dot(lwi, lwh) * D * dwh_to_dwi);
 }
 
 BT_HD float disney_pdf_inner_refl(const DisneyParams &d, V3 lwi, V3 lwo)
 {
     const V3 lwh = -normalize(lwi + lwo);
-    const float phi_h = phi_of(lwh);
-    const float cth = lwh.z, sth = cos2sin(cth);
+    const float cth = lwh.z;
     const float ctd = dot(lwi, lwh);
-    const float D = mf_aniso_gtr2(sinf(phi_h), cosf(phi_h), sth, cth, d.trans_ax, d.trans_ay);
+    const float D = gtr2_of(lwh, d.trans_ax, d.trans_ay);
     return fabsf(cth * D / (4.0f * ctd));
 }
 
@@ -486,13 +508,13 @@ BT_HD float disney_pdf(const DisneyParams &d, V3 lwi, V3 lwo)
         return d.w_transmission * disney_pdf_transmission(d, lwi, lwo);
     const float diffuse = pdf_hemisphere_zweighted(lwi);
     const V3 lwh = normalize(lwi + lwo);
-    const float phi_h = phi_of(lwh);
-    const float cth = lwh.z, sth = cos2sin(cth);
+    const float cth = lwh.z, sth = sin_theta_n(lwh);
     const float ctd = dot(lwi, lwh);
     // the reference derives sin(phi_o) as sqrt(1 - cos^2), i.e. always non-negative
-    const float cpo = cosf(phi_of(lwo));
-    const float spo = cos2sin(cpo);
-    const float spec_D = mf_aniso_gtr2(sinf(phi_h), cosf(phi_h), sth, cth, d.ax, d.ay);
+    float cpo, spo;
+    phi_cs(lwo, cpo, spo);
+    spo = fabsf(spo);
+    const float spec_D = gtr2_of(lwh, d.ax, d.ay);
     const float pdf_spec = mf_smith_aniso_gtr2(cpo, spo, d.ax, d.ay, tan_theta(lwo)) * spec_D / (4.0f * lwo.z);
     const float cc_D = mf_gtr1(sth, cth, d.clearcoat_roughness);
     const float pdf_cc = cth * cc_D / (4.0f * ctd);

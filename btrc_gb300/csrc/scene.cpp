@@ -726,7 +726,8 @@ struct MediumBuilder
         w2l.to_affine(w2l_a, l2w_a);
         std::memcpy(m.dev.w2l, w2l_a, sizeof(w2l_a));
         std::memcpy(m.dev.l2w, l2w_a, sizeof(l2w_a));
-        m.dev.priority = static_cast<int32_t>(json::float_or(n, "priority", 0.0f));
+        m.priority = json::float_or(n, "priority", 0.0f);
+        m.dev.priority = static_cast<int32_t>(m.priority);
         if(type == "homogeneous")
         {
             m.dev.type = MED_HOMOGENEOUS;
@@ -925,7 +926,7 @@ HostScene load_scene(const std::string &path)
         std::vector<int> order(mb.media.size());
         std::iota(order.begin(), order.end(), 0);
         std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-            return mb.media[a].dev.priority > mb.media[b].dev.priority;
+            return mb.media[a].priority > mb.media[b].priority;
         });
         std::vector<int> remap(mb.media.size());
         for(size_t i = 0; i < order.size(); ++i)

@@ -77,6 +77,7 @@ struct RenderParams
 struct HostMedium
 {
     Medium dev{};
+    float priority = 0;       // sort key of the medium table (descending)
     std::vector<float> grid;  // heterogeneous density (x fastest)
 };
 

@@ -356,3 +356,105 @@ def random_soup(path_dir: Path, seed: int, n_tris: int, n_instances: int = 3) ->
         "scene": {"entities": ents},
     }
     return _write_scene(out / "scene.json", scene)
+
+
+def write_grid(path: Path, grid: np.ndarray) -> None:
+    """Binary density grid: b"BTG1", int32 width, height, depth, float32 values (x fastest)."""
+    d, h, w = grid.shape
+    tmp = path.with_suffix(path.suffix + ".tmp")
+    with open(tmp, "wb") as f:
+        f.write(b"BTG1")
+        f.write(np.array([w, h, d], np.int32).tobytes())
+        f.write(np.ascontiguousarray(grid, np.float32).tobytes())
+    os.replace(tmp, path)
+
+
+def write_grid_text(path: Path, grid: np.ndarray) -> None:
+    """The reference's text format: "float 1 W H D" then values, x fastest
+    (common/btrc/utils/cuda/array.cpp:313-384)."""
+    d, h, w = grid.shape
+    body = " ".join("%.6g" % v for v in grid.ravel())
+    path.write_text(f"float 1 {w} {h} {d}\n{body}\n")
+
+
+def fbm_grid(perlin: Perlin, res: int, freq: float = 4.0, slab: int = 16) -> np.ndarray:
+    """fBm (8 octaves, lacunarity 2) sampled at voxel centres of [0,1]^3, (res, res, res) z-major."""
+    out = np.zeros((res, res, res), np.float32)
+    c = (np.arange(res) + 0.5) / res
+    Y, X = np.meshgrid(c, c, indexing="ij")
+    for z0 in range(0, res, slab):
+        zs = c[z0:z0 + slab]
+        Z = np.broadcast_to(zs[:, None, None], (len(zs), res, res))
+        out[z0:z0 + len(zs)] = perlin.fbm3(np.broadcast_to(X, Z.shape) * freq + 0.31,
+                                           np.broadcast_to(Y, Z.shape) * freq + 0.17, Z * freq + 0.53, octaves=8)
+    return out
+
+
+def displaced_sphere(perlin: Perlin, level: int, radius: float, amp: float):
+    v, f = icosphere(level)
+    disp = perlin.fbm3(v[:, 0] * 3 + 11.1, v[:, 1] * 3 + 7.7, v[:, 2] * 3 + 3.3, octaves=4)
+    p = v * (radius + amp * disp)[:, None]
+    tri = p[f]
+    fn = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    vn = np.zeros_like(p)
+    for k in range(3):
+        np.add.at(vn, f[:, k], fn)
+    vn /= np.maximum(np.linalg.norm(vn, axis=1, keepdims=True), 1e-30)
+    return p, f, vn
+
+
+def volume(seed: int = 1002, width: int = 1024, height: int = 1024, spp: int = 64, grid_res: int = 256,
+           sphere_level: int = 7, text_grid: bool = False, out_dir: Path | None = None, force: bool = False,
+           state_count: int = 2 * 1024 * 1024) -> Path:
+    """Config 2: the cornell box with a heterogeneous fBm medium (sigma_t max 20, albedo 0.9,
+    HG g 0.6) behind a transform inside an invisible cube, plus a displaced icosphere with a
+    GGX conductor of roughness 0.2; depth 32."""
+    out = Path(out_dir or cache_dir() / f"volume-{seed}-{grid_res}-{sphere_level}")
+    out.mkdir(parents=True, exist_ok=True)
+    name = f"scene-{width}x{height}-{spp}.json"
+    if (out / name).exists() and not force:
+        return out / name
+    rng = np.random.default_rng(seed)
+    perlin = Perlin(rng)
+    half = 0.5
+    bv, bf = box_inward((-half, -half, -half), (half, half, 1.4))
+    write_obj(out / "box_left.obj", bv, bf[0:2])
+    write_obj(out / "box_right.obj", bv, bf[2:4])
+    write_obj(out / "box_rest.obj", bv, bf[4:12])
+    qv, qf = quad(0.25)
+    write_obj(out / "light.obj", qv, flip(qf))
+    ch = 0.475  # medium cube, 5% inside the box cross-section
+    cv, cf = box_inward((-ch, -ch, -ch), (ch, ch, ch))
+    write_obj(out / "cube.obj", cv, flip(cf))  # normals facing outwards
+    sv, sf, sn = displaced_sphere(perlin, sphere_level, 0.22, 0.03)
+    write_obj(out / "sphere.obj", sv, sf, normals=sn)
+    dens = np.clip(fbm_grid(perlin, grid_res), 0.0, 1.0) * 20.0
+    if text_grid:
+        write_grid_text(out / "density.txt", dens)
+        sigma = {"type": "array", "text": "$env{scene_directory}/density.txt"}
+    else:
+        write_grid(out / "density.bin", dens)
+        sigma = {"type": "array", "binary": "$env{scene_directory}/density.bin"}
+    albedos = rng.uniform(0.2, 0.8, (4, 3))
+    medium = {"type": "transform", "world_to_local": {"scale": [1.0 / ch] * 3},
+              "medium": {"type": "hetergeneous", "sigma_t": sigma, "albedo": 0.9, "g": 0.6}}
+    ents = [_entity({"type": "triangle_mesh", "filename": f"$env{{scene_directory}}/{part}.obj"}, _diffuse(albedos[k]))
+            for k, part in enumerate(("box_left", "box_right", "box_rest"))]
+    ents.append(_entity({"type": "triangle_mesh", "filename": "$env{scene_directory}/light.obj"}, _diffuse(albedos[3]),
+                        [{"translate": [0.0, half - 0.005, 0.0]}],
+                        light={"type": "mesh_light", "intensity": [15.0, 15.0, 15.0]}))
+    ents.append(_entity({"type": "triangle_mesh", "filename": "$env{scene_directory}/cube.obj"}, {"type": "invisible"},
+                        inner=medium))
+    ents.append(_entity({"type": "triangle_mesh", "filename": "$env{scene_directory}/sphere.obj"},
+                        {"type": "metal", "color": [0.95, 0.64, 0.54], "roughness": 0.2},
+                        outer="$reference{$root/scene/entities/4/inner_medium}"))
+    scene = {
+        "width": width, "height": height,
+        "camera": {"type": "pinhole", "eye": [0.0, 0.0, 1.3], "dst": [0.0, 0.0, -half], "up": [0.0, 1.0, 0.0],
+                   "fov_y": {"deg": 40.0}},
+        "renderer": {"type": "wfpt", "spp": spp, "min_depth": 5, "max_depth": 32, "rr_threshold": 0.1,
+                     "rr_cont_prob": 0.5, "state_count": state_count, "sampler": "independent",
+                     "filter": {"type": "gaussian", "radius": 1.5, "alpha": 1.6}},
+        "scene": {"entities": ents},
+    }
+    return _write_scene(out / name, scene)

@@ -31,6 +31,7 @@ class OracleScene(C.Structure):
         ("env_type", C.c_int32), ("env_lower", C.c_float * 3), ("env_upper", C.c_float * 3),
         ("env_up", C.c_float * 3),
         ("vacuum_medium", C.c_int32), ("world_diagonal", C.c_float),
+        ("nmed", C.c_int32), ("med", _vp), ("med_grid_offset", _vp), ("grids", _vp),
         ("eye", C.c_float * 3), ("lbc", C.c_float * 3), ("film_x", C.c_float * 3), ("film_y", C.c_float * 3),
         ("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("min_depth", C.c_int32),
         ("max_depth", C.c_int32), ("rr_threshold", C.c_float), ("rr_cont_prob", C.c_float),
@@ -53,6 +54,7 @@ def lib() -> C.CDLL:
         L.oracle_murmur64a.restype = C.c_uint64
         L.oracle_murmur64a.argtypes = [_vp, C.c_uint64, C.c_uint64]
         L.oracle_bsdf_batch.argtypes = [C.c_int, _vp, _vp, _vp, C.c_uint64, _vp]
+        L.oracle_bsdf_batch_f32.argtypes = [C.c_int, _vp, _vp, _vp, C.c_uint64, _vp]
         L.oracle_prepare.restype = _vp
         L.oracle_prepare.argtypes = [C.POINTER(OracleScene)]
         L.oracle_release.argtypes = [_vp]
@@ -130,13 +132,15 @@ def murmur64a(data: bytes, seed: int = 0) -> int:
     return int(lib().oracle_murmur64a(_p(buf), len(data), seed))
 
 
-def bsdf_batch(op: int, material: np.ndarray, wo: np.ndarray, wi_or_u: np.ndarray) -> np.ndarray:
-    """FP64 local-space BSDF. material: (n, 16) float32, type in column 15."""
+def bsdf_batch(op: int, material: np.ndarray, wo: np.ndarray, wi_or_u: np.ndarray, fp32: bool = False) -> np.ndarray:
+    """Local-space BSDF in FP64 (or the same code in FP32). material: (n, 16) float32,
+    type in column 15. op 0: (f.rgb, pdf); op 1: (f.rgb, pdf, wi.xyz)."""
     material = np.ascontiguousarray(material, np.float32)
     wo = np.ascontiguousarray(wo, np.float64)
     wu = np.ascontiguousarray(wi_or_u, np.float64)
     out = np.zeros((len(material), 4 if op == 0 else 7), np.float64)
-    lib().oracle_bsdf_batch(op, _p(material), _p(wo), _p(wu), len(material), _p(out))
+    fn = lib().oracle_bsdf_batch_f32 if fp32 else lib().oracle_bsdf_batch
+    fn(op, _p(material), _p(wo), _p(wu), len(material), _p(out))
     return out
 
 

@@ -1335,6 +1335,10 @@ struct OracleScene
 
     int32_t vacuum_medium;
     float world_diagonal;
+    int32_t nmed;
+    const float *med;       // 28 floats per medium (layout in medium() below)
+    const uint64_t *med_grid_offset;
+    const float *grids;
 
     float eye[3], lbc[3], film_x[3], film_y[3];
     int32_t width, height, spp, min_depth, max_depth;
@@ -1352,6 +1356,7 @@ struct Prepared
     std::vector<Alias> geo_alias;   // only for light geometries
     Alias filter;
     Sampler::HC hc;
+    bool has_media = false;
 };
 
 V3f pt(const float *m, V3f p)
@@ -1422,6 +1427,130 @@ struct ShadeFrame
     }
 };
 
+// ---- participating media (builtin/btrc/builtin/medium/{hetergeneous,homogeneous}.cpp,
+// core/btrc/core/medium.cpp, common/btrc/utils/henyey_greenstein.h)
+// medium record: [0] type (0 vacuum, 1 homogeneous, 2 heterogeneous), [1] priority,
+// [2..4] grid resolution, [5] unused (offsets in med_grid_offset), [6] sigma_max, [7] g, [8] homogeneous sigma_t,
+// [9..11] albedo, [12..23] world-to-local 3x4 rows
+struct Med
+{
+    int type;
+    int rx, ry, rz;
+    uint64_t off;
+    float sigma_max, g, sigma_t;
+    V3f albedo;
+    const float *w2l;
+};
+
+Med medium(const OracleScene &S, int id)
+{
+    const float *r = S.med + id * 28;
+    Med m;
+    m.type = static_cast<int>(r[0]);
+    m.rx = static_cast<int>(r[2]);
+    m.ry = static_cast<int>(r[3]);
+    m.rz = static_cast<int>(r[4]);
+    m.off = S.med_grid_offset[id];
+    m.sigma_max = r[6];
+    m.g = r[7];
+    m.sigma_t = r[8];
+    m.albedo = V3f(r[9], r[10], r[11]);
+    m.w2l = r + 12;
+    return m;
+}
+
+float grid_at(const OracleScene &S, const Med &m, V3f uvw)
+{
+    const float fx = uvw.x * m.rx - 0.5f, fy = uvw.y * m.ry - 0.5f, fz = uvw.z * m.rz - 0.5f;
+    const float flx = std::floor(fx), fly = std::floor(fy), flz = std::floor(fz);
+    const float tx = fx - flx, ty = fy - fly, tz = fz - flz;
+    auto cl = [](int v, int n) { return std::min(std::max(v, 0), n - 1); };
+    const int x0 = cl(int(flx), m.rx), x1 = cl(int(flx) + 1, m.rx);
+    const int y0 = cl(int(fly), m.ry), y1 = cl(int(fly) + 1, m.ry);
+    const int z0 = cl(int(flz), m.rz), z1 = cl(int(flz) + 1, m.rz);
+    const float *g = S.grids + m.off;
+    auto at = [&](int x, int y, int z) { return g[(static_cast<size_t>(z) * m.ry + y) * m.rx + x]; };
+    const float c00 = at(x0, y0, z0) + (at(x1, y0, z0) - at(x0, y0, z0)) * tx;
+    const float c10 = at(x0, y1, z0) + (at(x1, y1, z0) - at(x0, y1, z0)) * tx;
+    const float c01 = at(x0, y0, z1) + (at(x1, y0, z1) - at(x0, y0, z1)) * tx;
+    const float c11 = at(x0, y1, z1) + (at(x1, y1, z1) - at(x0, y1, z1)) * tx;
+    const float c0 = c00 + (c10 - c00) * ty, c1 = c01 + (c11 - c01) * ty;
+    return c0 + (c1 - c0) * tz;
+}
+
+template<class Smp>
+bool medium_sample(const OracleScene &S, const Med &m, V3f a, V3f b, Smp &smp, V3f &pos)
+{
+    if(m.type == 0)
+        return false;
+    const float t_max = len(b - a);
+    if(m.type == 1)
+    {
+        const float st = -std::log(1.0f - smp.get1d()) / m.sigma_t;
+        if(st < t_max)
+        {
+            pos = a + nrm(b - a) * st;
+            return true;
+        }
+        return false;
+    }
+    const float inv = 1.0f / m.sigma_max;
+    const V3f la = V3f(0.5f) + 0.5f * pt(m.w2l, a), lb = V3f(0.5f) + 0.5f * pt(m.w2l, b);
+    const V3f ls = (lb - la) / t_max, ws = (b - a) / t_max;
+    float t = 0;
+    for(int it = 0; it < (1 << 20); ++it)
+    {
+        t += -std::log(1.0f - smp.get1d()) * inv;
+        if(t >= t_max)
+            return false;
+        const float dens = grid_at(S, m, la + t * ls);
+        if(smp.get1d() < dens * inv)
+        {
+            pos = a + t * ws;
+            return true;
+        }
+    }
+    return false;
+}
+
+template<class Smp>
+V3f medium_tr(const OracleScene &S, const Med &m, V3f a, V3f b, Smp &smp)
+{
+    if(m.type == 0)
+        return V3f(1.0f);
+    const float t_max = len(b - a);
+    if(m.type == 1)
+    {
+        const V3f sa = m.sigma_t * (V3f(1.0f) - m.albedo);
+        return V3f(std::exp(-t_max * sa.x), std::exp(-t_max * sa.y), std::exp(-t_max * sa.z));
+    }
+    const float inv = 1.0f / m.sigma_max;
+    const V3f la = V3f(0.5f) + 0.5f * pt(m.w2l, a), lb = V3f(0.5f) + 0.5f * pt(m.w2l, b);
+    const V3f ls = (lb - la) / t_max;
+    float r = 1.0f, t = 0;
+    for(int it = 0; it < (1 << 20); ++it)
+    {
+        t += -std::log(1.0f - smp.get1d()) * inv;
+        if(t >= t_max)
+            break;
+        r *= 1.0f - grid_at(S, m, la + t * ls) * inv;
+    }
+    return V3f(r);
+}
+
+float hg(float g, float u)
+{
+    const float g2 = g * g;
+    const float dem = 1.0f + g2 - 2.0f * (g * u);
+    return (1.0f - g2) / (4.0f * PIf * dem * std::sqrt(dem));
+}
+
+struct PcgSmp
+{
+    Pcg p;
+    float get1d() { return p.uniform(); }
+};
+
 void splat(double *film, int w, uint32_t px, uint32_t py, V3f v)
 {
     if(!std::isfinite(v.x) || !std::isfinite(v.y) || !std::isfinite(v.z))
@@ -1432,8 +1561,95 @@ void splat(double *film, int w, uint32_t px, uint32_t py, V3f v)
     p[2] += v.z;
 }
 
-// One camera path with the wavefront integrator's semantics
-// (generate.cpp:33-87, shade.cpp:29-235, shadow.cpp:39-76, helper.cpp:9-207).
+// One camera path with the wavefront integrator's semantics, stage by stage as
+// WavefrontPathTracer::render runs them per bounce: trace -> medium -> shade -> shadow
+// (generate.cpp:33-87, medium.cpp:28-249, shade.cpp:29-235, shadow.cpp:39-76,
+// helper.cpp:9-207).
+struct LightSample
+{
+    bool ok = false;
+    V3f o, d, li;
+    float t1 = 0, pdf = 0;
+};
+
+LightSample sample_light(const Prepared &P, V3f ref, V3f ref_nor, bool offset_origin, Sampler &smp)
+{
+    const OracleScene &S = *P.S;
+    LightSample r;
+    float s0, s1, s2;
+    smp.get3d(s0, s1, s2);
+    const float sel = smp.get1d();
+    const int NL = nlights_total(S);
+    if(NL == 0)
+        return r;
+    const int li = std::min(static_cast<int>(sel * static_cast<float>(NL)), NL - 1);
+    const float spdf = 1.0f / static_cast<float>(NL);
+    if(li < S.nlight)
+    {
+        // MeshLight::sample_li_inline (builtin/btrc/builtin/light/mesh_light.cpp:31-58)
+        const int lg = S.light_geo[li], linst = S.light_inst[li];
+        const uint32_t prim = P.geo_alias[lg].sample(s0);
+        const float tq = std::sqrt(s1);
+        const float u = 1.0f - tq, v = tq * s2;
+        const float *lp = S.local_pos + (S.geo_offset[lg] + prim) * 9;
+        const V3f a(lp[0], lp[1], lp[2]), b(lp[3], lp[4], lp[5]), c(lp[6], lp[7], lp[8]);
+        const V3f lpos = a + (b - a) * u + (c - a) * v;
+        const float *ez = S.shade + (2 * S.total_geo_tris + S.geo_offset[lg] + prim) * 4;
+        const V3f spos = pt(S.inst_l2w + linst * 12, lpos);
+        const V3f snor = nrm(nor(S.inst_w2l + linst * 12, nrm(V3f(ez[0], ez[1], ez[2]))));
+        const V3f p2r = ref - spos;
+        const float d2 = dot(p2r, p2r);
+        const float sc = S.light_scale[li];
+        const float pdf_sa = 1.0f / (sc * sc) * (1.0f / S.geo_area_total[lg]) * d2 / std::fabs(dot(snor, nrm(p2r)));
+        const V3f I(S.light_intensity[li * 3], S.light_intensity[li * 3 + 1], S.light_intensity[li * 3 + 2]);
+        r.li = dot(p2r, snor) > 0 ? I : V3f(0.0f);
+        const V3f diff = spos - ref;
+        const V3f dstp = ioffset_dir(spos, snor, -diff);
+        r.o = offset_origin ? ioffset_dir(ref, ref_nor, diff) : ref;
+        r.d = dstp - r.o;
+        r.t1 = 1.0f;
+        r.pdf = spdf * pdf_sa;
+    }
+    else
+    {
+        const float z = 1.0f - (s0 + s0);
+        const float phi = 2.0f * PIf * s1;
+        const float rr = std::sqrt(std::max(0.0f, 1.0f - z * z));
+        const V3f dir(rr * std::cos(phi), rr * std::sin(phi), z);
+        r.o = offset_origin ? ioffset_dir(ref, ref_nor, dir) : ref;
+        r.d = dir;
+        r.t1 = FMAX;
+        r.li = sky(S, dir);
+        r.pdf = spdf * (1.0f / (4.0f * PIf));
+    }
+    r.ok = true;
+    return r;
+}
+
+bool russian_roulette(const OracleScene &S, V3f &beta, int depth, Sampler &smp)
+{
+    if(depth < S.min_depth)
+        return false;
+    if(depth >= S.max_depth)
+        return true;
+    const float sam = smp.get1d();
+    if(lum(beta) < S.rr_threshold)
+    {
+        if(sam > S.rr_cont_prob)
+            return true;
+        beta = beta / S.rr_cont_prob;
+    }
+    return false;
+}
+
+struct Shadow
+{
+    bool ok = false;
+    V3f o, d, beta;
+    float t1 = 0;
+    int medium = 0;
+};
+
 void trace_path(const Prepared &P, uint64_t g, double *film)
 {
     const OracleScene &S = *P.S;
@@ -1465,16 +1681,114 @@ void trace_path(const Prepared &P, uint64_t g, double *film)
     const V3f dst = V3f(S.lbc[0], S.lbc[1], S.lbc[2]) + film_x * V3f(S.film_x[0], S.film_x[1], S.film_x[2]) +
                     film_y * V3f(S.film_y[0], S.film_y[1], S.film_y[2]);
     V3f o = eye, d = nrm(dst - eye);
+    float t1 = FMAX;
+    int ray_medium = S.vacuum_medium;
     film[(static_cast<size_t>(py) * S.width + px) * 4 + 3] += 1.0;
 
     V3f beta(1.0f), rad(0.0f), beta_le(1.0f);
     float bsdf_pdf = -1.0f;
     int depth = 0;
     const int NL = nlights_total(S);
+    PcgSmp shadow_rng;
+    shadow_rng.p.seed(mix_bits(g), PCG_STREAM);
+
     for(;;)
     {
         float od[3] = { o.x, o.y, o.z }, dd[3] = { d.x, d.y, d.z };
-        const Bvh::Hit h = P.bvh.closest(od, dd, FMAX);
+        const Bvh::Hit h = P.bvh.closest(od, dd, t1);
+        bool alive = false;  // a next state was emitted this bounce
+        V3f n_o, n_d, n_beta, n_beta_le;
+        float n_pdf = 0;
+        int n_medium = 0;
+        Shadow sh;
+
+        // ---------------- medium stage (medium.cpp:28-164)
+        bool scattered = false;
+        if(P.has_media)
+        {
+            int medium_id;
+            V3f end;
+            if(h.hit)
+            {
+                const int inst = static_cast<int>(h.inst);
+                const int geo = S.inst_geo[inst];
+                const float *ez = S.shade + (2 * S.total_geo_tris + S.geo_offset[geo] + h.prim) * 4;
+                const V3f n = nor(S.inst_w2l + inst * 12, V3f(ez[0], ez[1], ez[2]));
+                const int im = dot(d, n) < 0 ? S.inst_outer[inst] : S.inst_inner[inst];
+                medium_id = std::min(im, ray_medium);
+                end = ioffset_dir(o + h.t * d, n, -d);
+            }
+            else
+            {
+                medium_id = S.vacuum_medium;
+                end = o + nrm(d) * S.world_diagonal;
+            }
+            ray_medium = medium_id;
+            const Med m = medium(S, medium_id);
+            if(m.type != 0)
+            {
+                V3f spos;
+                const bool sc = medium_sample(S, m, o, end, smp, spos);
+                const V3f tr = medium_tr(S, m, o, end, smp);
+                beta_le = beta_le * tr;
+                if(sc)
+                {
+                    scattered = true;
+                    if(russian_roulette(S, beta, depth, smp))
+                        splat(film, S.width, px, py, rad);
+                    else
+                    {
+                        LightSample ls = sample_light(P, spos, V3f(0, 0, 1), false, smp);
+                        if(ls.ok)
+                        {
+                            const float u = -dot(nrm(ls.d), nrm(-d));
+                            const float ph = hg(m.g, u);
+                            ls.li = ls.li * beta * (m.albedo * ph) / (ph + ls.pdf);
+                        }
+                        // HenyeyGreensteinPhaseShader::sample (core/btrc/core/medium.cpp:32-64)
+                        float a0, a1, a2;
+                        smp.get3d(a0, a1, a2);
+                        const float ss = a0 + a0 - 1;
+                        float u;
+                        if(std::fabs(m.g) < 0.001f)
+                            u = ss;
+                        else
+                        {
+                            const float g2 = m.g * m.g;
+                            u = (1.0f + g2 - sq((1.0f - g2) / (1.0f + m.g * ss))) / (m.g + m.g);
+                        }
+                        const float ct = -u, st = cos2sin(ct), phi = 2 * PIf * a1;
+                        const V3f lwi(st * std::sin(phi), st * std::cos(phi), ct);
+                        const float pv = hg(m.g, u);
+                        const V3f phase = m.albedo * pv;
+                        const V3f nd = Frame<float>::from_z(-d).l2g(lwi);
+                        if(ls.ok)
+                        {
+                            sh.ok = true;
+                            sh.o = ls.o;
+                            sh.d = ls.d;
+                            sh.t1 = ls.t1;
+                            sh.beta = ls.li;
+                            sh.medium = ls.t1 > 1 ? S.vacuum_medium : medium_id;
+                        }
+                        if(!zero3(phase))
+                        {
+                            alive = true;
+                            n_o = spos;
+                            n_d = nrm(nd);
+                            n_beta_le = beta * phase;
+                            n_beta = n_beta_le / pv;
+                            n_pdf = pv;
+                            n_medium = medium_id;
+                        }
+                        else
+                            splat(film, S.width, px, py, rad);
+                    }
+                }
+            }
+        }
+
+        // ---------------- shade stage (shade.cpp:29-235)
         if(!h.hit)
         {
             V3f le(0.0f);
@@ -1486,227 +1800,200 @@ void trace_path(const Prepared &P, uint64_t g, double *film)
                 else
                     le = beta_le * L / (bsdf_pdf + (1.0f / NL) * (1.0f / (4.0f * PIf)));
             }
-            splat(film, S.width, px, py, le + rad);
-            return;
+            splat(film, S.width, px, py, scattered ? le : le + rad);
         }
-        const int inst = static_cast<int>(h.inst);
-        const float *l2w = S.inst_l2w + inst * 12, *w2l = S.inst_w2l + inst * 12;
-        const int geo = S.inst_geo[inst];
-        const uint64_t ti = S.geo_offset[geo] + h.prim;
-        auto sh = [&](int k) {
-            const float *p = S.shade + (static_cast<uint64_t>(k) * S.total_geo_tris + ti) * 4;
-            return V3f(p[0], p[1], p[2]);
-        };
-        // get_hitinfo (core/btrc/core/scene.cpp:9-64)
-        const V3f pos = o + h.t * d;
-        Frame<float> gf(sh(0), sh(1), sh(2));
-        gf.x = nrm(vec(l2w, gf.x));
-        gf.y = nrm(vec(l2w, gf.y));
-        gf.z = nrm(nor(w2l, gf.z));
-        const V3f interp = nrm(nor(w2l, sh(3) + sh(4) * h.b1 + sh(5) * h.b2));
-
-        // area light hit with MIS
-        const int light = S.inst_light[inst];
-        if(light >= 0)
+        else
         {
-            const V3f I(S.light_intensity[light * 3], S.light_intensity[light * 3 + 1], S.light_intensity[light * 3 + 2]);
-            const V3f le = dot(gf.z, -d) >= 0 ? I : V3f(0.0f);
-            if(bsdf_pdf < 0)
-                rad = rad + beta_le * le / -bsdf_pdf;
+            const int inst = static_cast<int>(h.inst);
+            const float *l2w = S.inst_l2w + inst * 12, *w2l = S.inst_w2l + inst * 12;
+            const int geo = S.inst_geo[inst];
+            const uint64_t ti = S.geo_offset[geo] + h.prim;
+            auto shd = [&](int k) {
+                const float *q = S.shade + (static_cast<uint64_t>(k) * S.total_geo_tris + ti) * 4;
+                return V3f(q[0], q[1], q[2]);
+            };
+            // get_hitinfo (core/btrc/core/scene.cpp:9-64)
+            const V3f pos = o + h.t * d;
+            Frame<float> gf(shd(0), shd(1), shd(2));
+            gf.x = nrm(vec(l2w, gf.x));
+            gf.y = nrm(vec(l2w, gf.y));
+            gf.z = nrm(nor(w2l, gf.z));
+            const V3f interp = nrm(nor(w2l, shd(3) + shd(4) * h.b1 + shd(5) * h.b2));
+
+            V3f le(0.0f);
+            const int light = S.inst_light[inst];
+            if(light >= 0)
+            {
+                const V3f I(S.light_intensity[light * 3], S.light_intensity[light * 3 + 1], S.light_intensity[light * 3 + 2]);
+                const V3f e = dot(gf.z, -d) >= 0 ? I : V3f(0.0f);
+                if(bsdf_pdf < 0)
+                    le = beta_le * e / -bsdf_pdf;
+                else
+                {
+                    float pdf_li = 0;
+                    const V3f to_ref = o - pos;
+                    if(dot(gf.z, to_ref) > 0)
+                    {
+                        const float sc = S.light_scale[light];
+                        const float d2 = dot(to_ref, to_ref);
+                        const float d3 = std::sqrt(d2) * d2;
+                        pdf_li = 1.0f / (sc * sc) * (1.0f / S.geo_area_total[S.light_geo[light]]) * d3 /
+                                 std::fabs(dot(gf.z, to_ref));
+                    }
+                    le = beta_le * e / (bsdf_pdf + (1.0f / NL) * pdf_li);
+                }
+            }
+            if(scattered)
+                splat(film, S.width, px, py, le);
             else
             {
-                float pdf_li = 0;
-                const V3f to_ref = o - pos;
-                if(dot(gf.z, to_ref) > 0)
-                {
-                    const float sc = S.light_scale[light];
-                    const float d2 = dot(to_ref, to_ref);
-                    const float d3 = std::sqrt(d2) * d2;
-                    pdf_li = 1.0f / (sc * sc) * (1.0f / S.geo_area_total[S.light_geo[light]]) * d3 /
-                             std::fabs(dot(gf.z, to_ref));
-                }
-                rad = rad + beta_le * le / (bsdf_pdf + (1.0f / NL) * pdf_li);
-            }
-        }
-
-        // Russian roulette (helper.cpp:67-97)
-        if(depth >= S.min_depth)
-        {
-            if(depth >= S.max_depth)
-            {
-                splat(film, S.width, px, py, rad);
-                return;
-            }
-            const float sam = smp.get1d();
-            if(lum(beta) < S.rr_threshold)
-            {
-                if(sam > S.rr_cont_prob)
-                {
+                rad = rad + le;
+                if(russian_roulette(S, beta, depth, smp))
                     splat(film, S.width, px, py, rad);
-                    return;
+                else
+                {
+                    LightSample ls = sample_light(P, pos, gf.z, true, smp);
+                    const float *mr = S.mat + S.inst_mat[inst] * 20;
+                    const int mtype = static_cast<int>(mr[0]);
+                    const bool term = mr[1] != 0.0f;
+                    ShadeFrame fr;
+                    fr.g = gf;
+                    fr.s = gf.rotate_to_new_z(interp);
+                    Mat<float> M;
+                    if(mtype <= 2)
+                        M.init(mtype, mr + 2);
+                    float u0, u1, u2;
+                    smp.get3d(u0, u1, u2);
+                    const V3f wo = -d;
+                    CS<float> bs;
+                    auto eval = [&](V3f wi) -> V3f {
+                        if(mtype > 2)
+                            return V3f(0.0f);
+                        const ShadeFrame f = fr.flip(wo);
+                        const V3f lwi = nrm(f.s.g2l(wi)), lwo = nrm(f.s.g2l(wo));
+                        float k = f.corr(wi);
+                        if(term)
+                            k *= fr.term(wi);
+                        return M.eval(lwi, lwo) * k;
+                    };
+                    auto pdf = [&](V3f wi) -> float {
+                        if(mtype > 2)
+                            return 0.0f;
+                        const ShadeFrame f = fr.flip(wo);
+                        return M.pdf(nrm(f.s.g2l(wi)), nrm(f.s.g2l(wo)));
+                    };
+                    if(mtype == 4)
+                    {
+                        // invisible.cpp: pass straight through
+                        bs.f = V3f(1.0f / std::fabs(dot(gf.z, nrm(wo))));
+                        bs.dir = -wo;
+                        bs.pdf = 1;
+                        bs.delta = true;
+                    }
+                    else if(mtype == 5)
+                    {
+                        // mirror.cpp
+                        const ShadeFrame f = fr.flip(wo);
+                        V3f lwo = f.s.g2l(wo);
+                        if(lwo.z > 0)
+                        {
+                            lwo = nrm(lwo);
+                            const V3f wi = f.s.l2g(V3f(-lwo.x, -lwo.y, lwo.z));
+                            if(!fr.black(wi))
+                            {
+                                const V3f col(mr[2], mr[3], mr[4]);
+                                bs.f = schlick3(col, lwo.z) / lwo.z * f.corr(wi);
+                                bs.dir = wi;
+                                bs.pdf = 1;
+                                bs.delta = true;
+                            }
+                        }
+                    }
+                    else if(mtype <= 2)
+                    {
+                        // BSDFAggregate::sample (aggregate.cpp:32-105)
+                        const ShadeFrame f = fr.flip(wo);
+                        const V3f lwo = nrm(f.s.g2l(wo));
+                        const CS<float> c = M.sample(lwo, u0, u1, u2);
+                        if(c.pdf > 0)
+                        {
+                            const V3f wi = f.s.l2g(c.dir);
+                            if(!fr.black(wi))
+                            {
+                                float k = f.corr(wi);
+                                if(term)
+                                    k *= fr.term(wi);
+                                bs.f = c.f * k;
+                                bs.dir = wi;
+                                bs.pdf = c.pdf;
+                            }
+                        }
+                    }
+                    V3f sf(0.0f);
+                    float spdf = 0;
+                    if(ls.ok)
+                    {
+                        sf = eval(ls.d);
+                        ls.ok = !zero3(sf);
+                        if(ls.ok)
+                            spdf = pdf(ls.d);
+                    }
+                    if(ls.ok)
+                    {
+                        const bool sout = dot(gf.z, ls.d) > 0, lout = dot(gf.z, d) < 0;
+                        sh.ok = true;
+                        sh.o = ls.o;
+                        sh.d = ls.d;
+                        sh.t1 = ls.t1;
+                        sh.medium = sout == lout ? ray_medium : (sout ? S.inst_outer[inst] : S.inst_inner[inst]);
+                        const float c = std::fabs(dot(nrm(ls.d), gf.z));
+                        sh.beta = ls.li * beta * sf * c / (spdf + ls.pdf);
+                    }
+                    if(zero3(bs.f))
+                        splat(film, S.width, px, py, rad);
+                    else
+                    {
+                        const V3f nd = nrm(bs.dir);
+                        const float c = std::fabs(dot(nd, gf.z));
+                        alive = true;
+                        n_beta_le = beta * c * bs.f;
+                        n_beta = n_beta_le / bs.pdf;
+                        n_o = ioffset_dir(pos, gf.z, nd);
+                        n_d = nd;
+                        n_medium = dot(gf.z, nd) > 0 ? S.inst_outer[inst] : S.inst_inner[inst];
+                        n_pdf = bs.delta ? -bs.pdf : bs.pdf;
+                    }
                 }
-                beta = beta / S.rr_cont_prob;
             }
         }
 
-        // light sample (helper.cpp:9-61, 127-142)
-        float ls0, ls1, ls2;
-        smp.get3d(ls0, ls1, ls2);
-        const float lsel = smp.get1d();
-        bool ls_ok = false;
-        V3f ls_o, ls_d, ls_li;
-        float ls_t1 = 0, ls_pdf = 0;
-        if(NL > 0)
+        // ---------------- shadow stage (shadow.cpp:24-76)
+        if(sh.ok)
         {
-            const int li = std::min(static_cast<int>(lsel * static_cast<float>(NL)), NL - 1);
-            const float spdf = 1.0f / static_cast<float>(NL);
-            if(li < S.nlight)
+            const float so[3] = { sh.o.x, sh.o.y, sh.o.z }, sdir[3] = { sh.d.x, sh.d.y, sh.d.z };
+            if(!P.bvh.any(so, sdir, sh.t1))
             {
-                const int lg = S.light_geo[li];
-                const int linst = S.light_inst[li];
-                const uint32_t prim = P.geo_alias[lg].sample(ls0);
-                const float tq = std::sqrt(ls1);
-                const float u = 1.0f - tq, v = tq * ls2;
-                const float *lp = S.local_pos + (S.geo_offset[lg] + prim) * 9;
-                const V3f a(lp[0], lp[1], lp[2]), b(lp[3], lp[4], lp[5]), c(lp[6], lp[7], lp[8]);
-                const V3f lpos = a + (b - a) * u + (c - a) * v;
-                const float *ez = S.shade + (2 * S.total_geo_tris + S.geo_offset[lg] + prim) * 4;
-                const V3f spos = pt(S.inst_l2w + linst * 12, lpos);
-                const V3f snor = nrm(nor(S.inst_w2l + linst * 12, nrm(V3f(ez[0], ez[1], ez[2]))));
-                const V3f p2r = pos - spos;
-                const float d2 = dot(p2r, p2r);
-                const float sc = S.light_scale[li];
-                const float pdf_sa = 1.0f / (sc * sc) * (1.0f / S.geo_area_total[lg]) * d2 / std::fabs(dot(snor, nrm(p2r)));
-                const V3f I(S.light_intensity[li * 3], S.light_intensity[li * 3 + 1], S.light_intensity[li * 3 + 2]);
-                ls_li = dot(p2r, snor) > 0 ? I : V3f(0.0f);
-                const V3f diff = spos - pos;
-                const V3f dstp = ioffset_dir(spos, snor, -diff);
-                ls_o = ioffset_dir(pos, gf.z, diff);
-                ls_d = dstp - ls_o;
-                ls_t1 = 1.0f;
-                ls_pdf = spdf * pdf_sa;
-            }
-            else
-            {
-                const float z = 1.0f - (ls0 + ls0);
-                const float phi = 2.0f * PIf * ls1;
-                const float r = std::sqrt(std::max(0.0f, 1.0f - z * z));
-                const V3f dir(r * std::cos(phi), r * std::sin(phi), z);
-                ls_o = ioffset_dir(pos, gf.z, dir);
-                ls_d = dir;
-                ls_t1 = FMAX;
-                ls_li = sky(S, dir);
-                ls_pdf = spdf * (1.0f / (4.0f * PIf));
-            }
-            ls_ok = true;
-        }
-
-        // material
-        const float *mr = S.mat + S.inst_mat[inst] * 20;
-        const int mtype = static_cast<int>(mr[0]);
-        const bool term = mr[1] != 0.0f;
-        ShadeFrame fr;
-        fr.g = gf;
-        fr.s = gf.rotate_to_new_z(interp);
-        Mat<float> M;
-        if(mtype <= 2)
-            M.init(mtype, mr + 2);
-        float u0, u1, u2;
-        smp.get3d(u0, u1, u2);
-        const V3f wo = -d;
-        CS<float> bs;
-        auto eval = [&](V3f wi) -> V3f {
-            if(mtype > 2)
-                return V3f(0.0f);
-            const ShadeFrame f = fr.flip(wo);
-            const V3f lwi = nrm(f.s.g2l(wi)), lwo = nrm(f.s.g2l(wo));
-            float k = f.corr(wi);
-            if(term)
-                k *= fr.term(wi);
-            return M.eval(lwi, lwo) * k;
-        };
-        auto pdf = [&](V3f wi) -> float {
-            if(mtype > 2)
-                return 0.0f;
-            const ShadeFrame f = fr.flip(wo);
-            return M.pdf(nrm(f.s.g2l(wi)), nrm(f.s.g2l(wo)));
-        };
-        if(mtype == 4)
-        {
-            // invisible.cpp: pass straight through
-            bs.f = V3f(1.0f / std::fabs(dot(gf.z, nrm(wo))));
-            bs.dir = -wo;
-            bs.pdf = 1;
-            bs.delta = true;
-        }
-        else if(mtype == 5)
-        {
-            // mirror.cpp
-            const ShadeFrame f = fr.flip(wo);
-            V3f lwo = f.s.g2l(wo);
-            if(lwo.z > 0)
-            {
-                lwo = nrm(lwo);
-                const V3f wi = f.s.l2g(V3f(-lwo.x, -lwo.y, lwo.z));
-                if(!fr.black(wi))
+                V3f b = sh.beta;
+                if(P.has_media)
                 {
-                    const V3f col(mr[2], mr[3], mr[4]);
-                    bs.f = schlick3(col, lwo.z) / lwo.z * f.corr(wi);
-                    bs.dir = wi;
-                    bs.pdf = 1;
-                    bs.delta = true;
+                    if(sh.t1 > 1)
+                        b = b * medium_tr(S, medium(S, S.vacuum_medium), sh.o, sh.o + nrm(sh.d) * S.world_diagonal,
+                                          shadow_rng);
+                    else
+                        b = b * medium_tr(S, medium(S, sh.medium), sh.o, sh.o + sh.d * sh.t1, shadow_rng);
                 }
+                splat(film, S.width, px, py, b);
             }
         }
-        else if(mtype <= 2)
-        {
-            // BSDFAggregate::sample (aggregate.cpp:32-105)
-            const ShadeFrame f = fr.flip(wo);
-            const V3f lwo = nrm(f.s.g2l(wo));
-            const CS<float> c = M.sample(lwo, u0, u1, u2);
-            if(c.pdf > 0)
-            {
-                const V3f wi = f.s.l2g(c.dir);
-                if(!fr.black(wi))
-                {
-                    float k = f.corr(wi);
-                    if(term)
-                        k *= fr.term(wi);
-                    bs.f = c.f * k;
-                    bs.dir = wi;
-                    bs.pdf = c.pdf;
-                }
-            }
-        }
-        V3f sf(0.0f);
-        float spdf = 0;
-        if(ls_ok)
-        {
-            sf = eval(ls_d);
-            ls_ok = !zero3(sf);
-            if(ls_ok)
-                spdf = pdf(ls_d);
-        }
-        if(ls_ok)
-        {
-            const float c = std::fabs(dot(nrm(ls_d), gf.z));
-            const V3f beta_li = ls_li * beta * sf * c / (spdf + ls_pdf);
-            const float so[3] = { ls_o.x, ls_o.y, ls_o.z }, sdir[3] = { ls_d.x, ls_d.y, ls_d.z };
-            if(!P.bvh.any(so, sdir, ls_t1))
-                splat(film, S.width, px, py, beta_li);
-        }
-        if(zero3(bs.f))
-        {
-            splat(film, S.width, px, py, rad);
+        if(!alive)
             return;
-        }
-        const V3f nd = nrm(bs.dir);
-        const float c = std::fabs(dot(nd, gf.z));
-        beta_le = beta * c * bs.f;
-        beta = beta_le / bs.pdf;
-        o = ioffset_dir(pos, gf.z, nd);
-        d = nd;
-        bsdf_pdf = bs.delta ? -bs.pdf : bs.pdf;
+        o = n_o;
+        d = n_d;
+        t1 = FMAX;
+        beta = n_beta;
+        beta_le = n_beta_le;
+        bsdf_pdf = n_pdf;
+        ray_medium = n_medium;
         ++depth;
     }
 }
@@ -1806,6 +2093,38 @@ void oracle_bsdf_batch(int op, const float *mat, const double *wo, const double 
     }
 }
 
+// The same restatement instantiated in FP32 (inputs rounded to float first): the
+// spread between this and the FP64 result is the conditioning of the formula itself.
+void oracle_bsdf_batch_f32(int op, const float *mat, const double *wo, const double *wu, uint64_t n, double *out)
+{
+    for(uint64_t i = 0; i < n; ++i)
+    {
+        Mat<float> M;
+        M.init(static_cast<int>(mat[i * 16 + 15]), mat + i * 16);
+        const V<float> lwo(float(wo[i * 3]), float(wo[i * 3 + 1]), float(wo[i * 3 + 2]));
+        if(op == 0)
+        {
+            const V<float> lwi(float(wu[i * 3]), float(wu[i * 3 + 1]), float(wu[i * 3 + 2]));
+            const V<float> f = M.eval(lwi, lwo);
+            out[i * 4 + 0] = f.x;
+            out[i * 4 + 1] = f.y;
+            out[i * 4 + 2] = f.z;
+            out[i * 4 + 3] = M.pdf(lwi, lwo);
+        }
+        else
+        {
+            const CS<float> s = M.sample(lwo, float(wu[i * 3]), float(wu[i * 3 + 1]), float(wu[i * 3 + 2]));
+            out[i * 7 + 0] = s.f.x;
+            out[i * 7 + 1] = s.f.y;
+            out[i * 7 + 2] = s.f.z;
+            out[i * 7 + 3] = s.pdf;
+            out[i * 7 + 4] = s.dir.x;
+            out[i * 7 + 5] = s.dir.y;
+            out[i * 7 + 6] = s.dir.z;
+        }
+    }
+}
+
 void *oracle_prepare(const OracleScene *S)
 {
     auto *P = new Prepared();
@@ -1840,6 +2159,9 @@ void *oracle_prepare(const OracleScene *S)
         P->filter.init(v);
     }
     P->hc = Sampler::consts(S->width, S->height);
+    for(int i = 0; i < S->ninst && S->nmed > 0; ++i)
+        if(medium(*S, S->inst_inner[i]).type != 0 || medium(*S, S->inst_outer[i]).type != 0)
+            P->has_media = true;
     return P;
 }
 

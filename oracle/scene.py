@@ -461,6 +461,68 @@ def _material(n: Node) -> np.ndarray:
     return rec
 
 
+def _grid(n: Node, sdir: str):
+    """Texture3D: constant, {"type":"constant","value":..}, {"type":"array","text":f}
+    (common/btrc/utils/cuda/array.cpp:313-384, channel 0) or {"type":"array","binary":f}."""
+    if n.kind in ("value", "array"):
+        return float(vvec3(n)[0]), None
+    t = n.child("type").s
+    if t == "constant":
+        return float(vvec3(n.child("value"))[0]), None
+    if t != "array":
+        raise ValueError("texture3d type " + t)
+    if n.find("binary") is not None:
+        fn = n.child("binary").s.replace("$env{scene_directory}", sdir)
+        raw = Path(fn).read_bytes()
+        assert raw[:4] == b"BTG1"
+        w, h, d = np.frombuffer(raw[4:16], np.int32)
+        return None, np.frombuffer(raw[16:], np.float32, count=int(w) * int(h) * int(d)).reshape(int(d), int(h), int(w))
+    fn = n.child("text").s.replace("$env{scene_directory}", sdir)
+    toks = Path(fn).read_text().split()
+    comp, ch, w, h, d = toks[0], int(toks[1]), int(toks[2]), int(toks[3]), int(toks[4])
+    vals = np.array(toks[5:5 + ch * w * h * d], np.float64).reshape(-1, ch)[:, 0]
+    if comp == "byte":
+        vals = vals / 127.0
+    return None, vals.astype(np.float32).reshape(d, h, w)
+
+
+def _medium(n: Node, sdir: str, w2l=None):
+    """One medium record (28 floats) + grid; transform media compose their world-to-local."""
+    t = n.child("type").s
+    if t == "transform":
+        if n.find("world_to_local") is not None:
+            mat, _inv = parse_transform(n.child("world_to_local"))
+        else:
+            _m, mat = parse_transform(n.child("local_to_world"))
+        mat = mat if w2l is None else mat_mul(mat, w2l)
+        return _medium(n.child("medium"), sdir, mat)
+    rec = np.zeros(28, np.float32)
+    m = w2l if w2l is not None else np.eye(4, dtype=np.float32)
+    rec[12:24] = m[:3].reshape(-1)
+    pr = n.find("priority")
+    prio = float(vfloat(pr)) if pr is not None else 0.0
+    rec[1] = prio
+    grid = None
+    if t == "homogeneous":
+        rec[0] = 1
+        rec[8] = vfloat(n.child("sigma_t"))
+        rec[9:12] = vvec3(n.child("albedo"))
+        rec[7] = vfloat(n.child("g")) if n.find("g") is not None else 0.0
+    elif t in ("hetergeneous", "heterogeneous"):
+        rec[0] = 2
+        c, grid = _grid(n.child("sigma_t"), sdir)
+        if grid is None:
+            grid = np.array([[[c]]], np.float32)
+        rec[2], rec[3], rec[4] = grid.shape[2], grid.shape[1], grid.shape[0]
+        rec[6] = max(float(grid.max()), 0.001)
+        alb = n.child("albedo")
+        rec[9:12] = vvec3(alb.child("value")) if alb.kind == "group" else vvec3(alb)
+        rec[7] = _grid(n.child("g"), sdir)[0] if n.find("g") is not None else 0.0
+    else:
+        raise ValueError("medium type " + t)
+    return rec, grid, prio
+
+
 class Scene:
     """Flattened oracle scene; keeps every array alive for the C side."""
 
@@ -497,6 +559,8 @@ class Scene:
         mat_ids: dict[int, int] = {}
         geos, mats = [], []
         inst = []
+        med_ids: dict[int, int] = {}
+        meds = []
         for e in scene.child("entities").elems:
             gn = e.child("geometry")
             if id(gn) not in geo_ids:
@@ -512,7 +576,17 @@ class Scene:
                 (np.eye(4, dtype=np.float32), np.eye(4, dtype=np.float32))
             light = e.find("light")
             inten = vvec3(light.child("intensity")) if light is not None else None
-            inst.append((geo_ids[id(gn)], mat_ids[id(mn)], xf, inten))
+            media = []
+            for key in ("inner_medium", "outer_medium"):
+                mnode = e.find(key)
+                if mnode is None:
+                    media.append(-1)
+                    continue
+                if id(mnode) not in med_ids:
+                    meds.append(_medium(mnode, sdir))
+                    med_ids[id(mnode)] = len(meds) - 1
+                media.append(med_ids[id(mnode)])
+            inst.append((geo_ids[id(gn)], mat_ids[id(mn)], xf, inten, media))
 
         self.geos = geos
         counts = np.array([len(g[2]) for g in geos], np.uint64)
@@ -527,7 +601,31 @@ class Scene:
         tris, ids = [], []
         l2w, w2l, igeo, imat, ilight = [], [], [], [], []
         linst, lgeo, lscale, lint = [], [], [], []
-        for i, (g, m, (mat, inv), inten) in enumerate(inst):
+        # medium table (core/btrc/core/scene.cpp:136-161): priority descending, creation
+        # order on ties, the volume-primitive medium (vacuum) last
+        order = sorted(range(len(meds)), key=lambda k: -meds[k][2])
+        remap = {k: i for i, k in enumerate(order)}
+        recs, offs, grids, off = [], [], [], 0
+        for k in order:
+            rec, grid, _ = meds[k]
+            recs.append(rec)
+            offs.append(off)
+            if grid is not None:
+                grids.append(grid.reshape(-1))
+                off += grid.size
+        vac = np.zeros(28, np.float32)
+        vac[1] = -1e30
+        recs.append(vac)
+        offs.append(off)
+        self.vacuum = len(recs) - 1
+        self.med = np.ascontiguousarray(np.stack(recs), np.float32)
+        self.med_grid_offset = np.array(offs, np.uint64)
+        self.grids = np.ascontiguousarray(np.concatenate(grids) if grids else np.zeros(1, np.float32), np.float32)
+        inner, outer = [], []
+        for *_, media in inst:
+            inner.append(self.vacuum if media[0] < 0 else remap[media[0]])
+            outer.append(self.vacuum if media[1] < 0 else remap[media[1]])
+        for i, (g, m, (mat, inv), inten, _media) in enumerate(inst):
             pos = geos[g][0].reshape(-1, 3)
             w = apply_point(mat, pos).reshape(-1, 9)
             tris.append(w)
@@ -554,8 +652,21 @@ class Scene:
         self.inst_geo = np.array(igeo, np.int32)
         self.inst_mat = np.array(imat, np.int32)
         self.inst_light = np.array(ilight, np.int32)
-        self.inst_inner = np.zeros(len(inst), np.int32)
-        self.inst_outer = np.zeros(len(inst), np.int32)
+        self.inst_inner = np.array(inner, np.int32)
+        self.inst_outer = np.array(outer, np.int32)
+        # world bounds (core/btrc/core/scene.cpp:224-236): transformed geometry boxes
+        lo, hi = np.full(3, np.inf, np.float32), np.full(3, -np.inf, np.float32)
+        for i, (g, m, (mat, inv), inten, _media) in enumerate(inst):
+            pos = geos[g][0].reshape(-1, 3)
+            if not len(pos):
+                continue
+            bl, bh = pos.min(0), pos.max(0)
+            corners = np.array([[bh[0] if c & 1 else bl[0], bh[1] if c & 2 else bl[1], bh[2] if c & 4 else bl[2]]
+                                for c in range(8)], np.float32)
+            w = apply_point(mat, corners)
+            lo, hi = np.minimum(lo, w.min(0)), np.maximum(hi, w.max(0))
+        ext = (hi - lo).astype(np.float32)
+        self.world_diagonal = float(np.sqrt(np.float32((ext * ext).sum(dtype=np.float32))))
         self.light_inst = np.array(linst, np.int32)
         self.light_geo = np.array(lgeo, np.int32)
         self.light_scale = np.array(lscale, np.float32)
@@ -588,7 +699,9 @@ class Scene:
         if self.env is not None:
             s.env_type = 1
             s.env_lower[:], s.env_upper[:], s.env_up[:] = [list(map(float, v)) for v in self.env]
-        s.vacuum_medium = 0
+        s.vacuum_medium = self.vacuum
+        s.world_diagonal = self.world_diagonal
+        s.nmed, s.med, s.med_grid_offset, s.grids = len(self.med), _p(self.med), _p(self.med_grid_offset), _p(self.grids)
         eye, lbc, fx, fy = self.camera
         s.eye[:], s.lbc[:], s.film_x[:], s.film_y[:] = (list(map(float, v)) for v in (eye, lbc, fx, fy))
         s.width, s.height, s.spp = self.width, self.height, self.spp

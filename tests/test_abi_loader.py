@@ -1,0 +1,160 @@
+"""CPU tests of the C ABI surface and the scene loader (host-only context, no GPU).
+
+The loader must accept Btrc's scene schema with its quirks: scalars pass through
+std::to_string(float) (six decimals), "$include{}" splices text, "$reference{}" shares one
+node (so one geometry / one material object), transform arrays compose later elements on
+the left, and errors come back as status codes with a message."""
+import json
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import btrc_gb300 as B
+from btrc_gb300 import scenes
+from oracle import scene as OS
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def test_library_exports_every_declared_symbol(native_lib):
+    header = (ROOT / "include" / "btrc.h").read_text()
+    declared = set(re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*(btrc_[a-z_0-9]+)\s*\(", header, re.M))
+    assert len(declared) >= 18
+    out = subprocess.run(["nm", "-D", "--defined-only", str(B.LIB_PATH)], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (btrc_[a-z_0-9]+)$", out, re.M))
+    missing = declared - exported
+    assert not missing, f"declared but not exported: {sorted(missing)}"
+    # the Python mirror binds every declared entry point
+    assert declared <= set(B.SIGNATURES)
+
+
+def test_version_string(native_lib):
+    assert "sm_103a" in B.version()
+
+
+def _write(tmp, name, obj):
+    p = Path(tmp) / name
+    p.write_text(json.dumps(obj) if not isinstance(obj, str) else obj)
+    return p
+
+
+def _minimal(tmp, extra_entities=(), renderer=None, **root):
+    v, f = scenes.quad(2.0)
+    scenes.write_obj(Path(tmp) / "q.obj", v, f)
+    ents = [{"geometry": {"type": "triangle_mesh", "filename": "$env{scene_directory}/q.obj"},
+             "material": {"type": "diffuse", "color": [0.5, 0.5, 0.5]}}] + list(extra_entities)
+    scene = {"width": 8, "height": 6,
+             "camera": {"type": "pinhole", "eye": [0, 1, 3], "dst": [0, 0, 0], "up": [0, 1, 0], "fov_y": {"deg": 45}},
+             "renderer": renderer or {"type": "wfpt", "spp": 2},
+             "scene": {"entities": ents}}
+    scene.update(root)
+    return scene
+
+
+def test_host_only_context_loads_and_builds(native_lib, tmp_path):
+    p = _write(tmp_path, "s.json", _minimal(tmp_path))
+    ctx = B.Context(-1)
+    sc = ctx.load_scene(p).build()
+    info = sc.info()
+    assert (info.width, info.height, info.spp, info.triangles) == (8, 6, 2, 2)
+    with pytest.raises(B.BtrcError) as e:
+        ctx.render(sc)
+    assert e.value.status == 1 and "host-only" in str(e.value)
+
+
+@pytest.mark.parametrize("content,status", [
+    ("{ not json", 3),
+    ('{"width": 8}', 3),
+])
+def test_parse_errors(native_lib, tmp_path, content, status):
+    p = _write(tmp_path, "bad.json", content)
+    ctx = B.Context(-1)
+    with pytest.raises(B.BtrcError) as e:
+        ctx.load_scene(p)
+    assert e.value.status == status
+
+
+def test_missing_file_is_io_error(native_lib, tmp_path):
+    ctx = B.Context(-1)
+    with pytest.raises(B.BtrcError) as e:
+        ctx.load_scene(tmp_path / "nope.json")
+    assert e.value.status == 2
+    s = _minimal(tmp_path)
+    s["scene"]["entities"][0]["geometry"]["filename"] = "$env{scene_directory}/missing.obj"
+    with pytest.raises(B.BtrcError) as e:
+        ctx.load_scene(_write(tmp_path, "m.json", s))
+    assert e.value.status == 2
+
+
+def test_unsupported_material_is_reported(native_lib, tmp_path):
+    s = _minimal(tmp_path)
+    s["scene"]["entities"][0]["material"] = {"type": "velvet"}
+    ctx = B.Context(-1)
+    with pytest.raises(B.BtrcError) as e:
+        ctx.load_scene(_write(tmp_path, "u.json", s))
+    assert e.value.status == 8 and "velvet" in str(e.value)
+
+
+def test_bad_reference_is_parse_error(native_lib, tmp_path):
+    s = _minimal(tmp_path)
+    s["scene"]["entities"].append({"geometry": "$reference{$root/scene/entities/7/geometry}",
+                                   "material": {"type": "diffuse", "color": 0.5}})
+    ctx = B.Context(-1)
+    with pytest.raises(B.BtrcError) as e:
+        ctx.load_scene(_write(tmp_path, "r.json", s))
+    assert e.value.status == 3
+
+
+def test_reference_shares_geometry_and_include_splices(native_lib, tmp_path):
+    s = _minimal(tmp_path, extra_entities=[
+        {"geometry": "$reference{$root/scene/entities/0/geometry}", "material": "$include{mat.json}",
+         "local_to_world": [{"scale": [0.5, 1, 0.5]}, {"translate": [0, 1, 0]}]}])
+    (tmp_path / "mat.json").write_text('{"type": "diffuse", "color": [0.2, 0.3, 0.4]}')
+    text = json.dumps(s).replace('"$include{mat.json}"', '"$include{mat.json}"')
+    p = _write(tmp_path, "ref.json", text)
+    ctx = B.Context(-1)
+    sc = ctx.load_scene(p).build()
+    info = sc.info()
+    assert info.geometries == 1 and info.instances == 2 and info.materials == 2 and info.triangles == 4
+    xyz, ids = sc.export_triangles()
+    S = OS.Scene(p)
+    assert np.array_equal(xyz.view(np.uint32), S.tris.view(np.uint32))
+
+
+def test_scalars_pass_through_to_string(native_lib, tmp_path):
+    # 1e-7 becomes "0.000000" in the reference's node tree, i.e. zero
+    s = _minimal(tmp_path, extra_entities=[
+        {"geometry": "$reference{$root/scene/entities/0/geometry}", "material": {"type": "diffuse", "color": 0.5},
+         "local_to_world": {"translate": [1e-7, 0.1234567, 2.5]}}])
+    p = _write(tmp_path, "f.json", s)
+    ctx = B.Context(-1)
+    xyz, _ = ctx.load_scene(p).build().export_triangles()
+    quad = scenes.quad(2.0)[0]
+    moved = xyz[2:].reshape(-1, 3)
+    assert np.all(moved[:, 0] == np.float32(np.float32(quad[[0, 2, 1, 0, 3, 2], 0])))  # x unchanged
+    assert np.all(moved[:, 1] == np.float32(0.123457))
+
+
+def test_rotation_transforms_match_oracle(native_lib, tmp_path):
+    s = _minimal(tmp_path, extra_entities=[
+        {"geometry": "$reference{$root/scene/entities/0/geometry}", "material": {"type": "diffuse", "color": 0.5},
+         "local_to_world": [{"rotate": {"axis": [1, 2, 3], "angle": {"deg": 33}}}, {"rotate_x": {"deg": 20}},
+                            {"rotate_y": {"rad": 0.3}}, {"rotate_z": {"deg": 10}}, {"translate": [0.5, 0, 0]}]}])
+    p = _write(tmp_path, "rot.json", s)
+    ctx = B.Context(-1)
+    xyz, _ = ctx.load_scene(p).build().export_triangles()
+    S = OS.Scene(p)
+    # sin/cos come from two different libm implementations: allow a few ulps
+    assert np.allclose(xyz, S.tris, rtol=0, atol=4e-7)
+
+
+def test_wfpt_defaults_and_pt_renderer(native_lib, tmp_path):
+    s = _minimal(tmp_path, renderer={"type": "pt"})
+    ctx = B.Context(-1)
+    info = ctx.load_scene(_write(tmp_path, "pt.json", s)).info()
+    # WavefrontPathTracer::Params defaults (builtin/btrc/builtin/renderer/wavefront.h:13-27)
+    assert (info.spp, info.min_depth, info.max_depth, info.state_count) == (128, 5, 10, 1000000)
+    assert info.sampler == 0 and info.filter == 0

@@ -1,13 +1,15 @@
 """Local-space BSDF eval / pdf / sample on the GPU against the FP64 oracle.
 
-Tolerance: the benchmark spec's 1e-5 relative bound applies where FP32 evaluation is well
-conditioned. Near-specular lobes (alpha = roughness^2 down to 0.0025) amplify FP32
-rounding of the half vector by ~1/alpha^2, so the test asserts the 1e-5 bound on the
-bulk of the samples and a conditioning-aware bound on every sample:
-  * >= 99% of finite, non-negligible values within 1e-5 relative,
-  * every value within 1e-5 relative + 1e-5 * |value scale| / alpha^2 (the propagated
-    FP32 rounding bound), and directions within 1e-4.
-Samples within the reference's own |cos| < 1e-4 cut-offs are excluded."""
+Tolerance (1e-5 relative, the parity bar for BSDFs):
+  * >= 99.9% of the values above 1e-6 within 1e-5 relative of the FP64 oracle, and
+  * every value within 1e-5 relative or 1e-7 absolute. The absolute floor covers lobe
+    values of ~1e-6 in the transmission lobe near total internal reflection, where the
+    reference's (1 - F) cancels in any FP32 evaluation.
+  * sampled directions within 1e-4 (99.9th percentile), rejection flips < 1e-3.
+Directions within the reference's own |cos| < 1e-4 cut-offs are excluded. The kernel
+evaluates sqrt(1 - c^2), sin/cos(atan2(y, x)) and sin(theta_h) in cancellation-free forms
+(btrc_gb300/csrc/bsdf.cuh); an FP32 evaluation of the reference's literal expressions
+reaches only ~87% within 1e-5 on sampled directions."""
 import numpy as np
 import pytest
 
@@ -65,13 +67,15 @@ def _run(ctx, op, mats, wo, wu):
 
 
 def _check(g, o, scale_alpha, what):
-    ok = np.isfinite(o) & (np.abs(o) > 1e-6)
+    fin = np.isfinite(o)
+    assert np.array_equal(np.isfinite(g), fin), f"{what}: non-finite values differ"
+    ok = fin & (np.abs(o) > 1e-6)
     rel = np.abs(g[ok] - o[ok]) / np.abs(o[ok])
     frac = (rel <= 1e-5).mean()
-    bound = 1e-5 + 1e-5 / scale_alpha[ok]
-    assert frac >= 0.99, f"{what}: only {frac:.4f} within 1e-5 relative"
-    worst = np.max(rel / bound)
-    assert worst <= 1.0, f"{what}: worst error {worst:.3g} x the propagated bound"
+    assert frac >= 0.999, f"{what}: only {frac:.5f} within 1e-5 relative"
+    err = np.abs(g[fin] - o[fin])
+    worst = np.max(err / (1e-5 * np.abs(o[fin]) + 1e-7))
+    assert worst <= 1.0, f"{what}: worst error {worst:.3g} x (1e-5 relative + 1e-7 absolute)"
     return frac
 
 

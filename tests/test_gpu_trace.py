@@ -46,11 +46,13 @@ def _compare(ctx, path, rays):
 def test_closest_bitexact_cornell(gpu_ctx, scene_dir):
     p = scenes.cornell(out_dir=scene_dir / "cornell")
     rng = np.random.default_rng(11)
-    rays = np.concatenate([random_rays(rng, 200000, -0.45, 0.45)])
+    inside = random_rays(rng, 200000, -0.45, 0.45)
     S = OS.Scene(p)
-    rays = np.concatenate([rays, edge_rays(rng, S.tris, 50000)])
-    _, frac = _compare(gpu_ctx, p, rays)
-    assert frac > 0.99  # closed box
+    rays = np.concatenate([inside, edge_rays(rng, S.tris, 50000)])
+    sc, _ = _compare(gpu_ctx, p, rays)
+    # every ray that starts inside the closed box hits a wall
+    f, _, _ = _gpu_trace(gpu_ctx, sc, inside)
+    assert (f != 0).all()
 
 
 def test_closest_bitexact_instanced_soup(gpu_ctx, scene_dir):
