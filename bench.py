@@ -312,6 +312,7 @@ def run_ours(args, world, rank, local):
             "scene_load_s": load_s, "bvh_build_ms": info.build_ms,
         }
         print(json.dumps(line), flush=True)
+    sc.close()
     ctx.close()
 
 

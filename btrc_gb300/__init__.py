@@ -15,6 +15,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 from pathlib import Path
 
 import numpy as np
@@ -149,6 +150,7 @@ class Context:
             raise BtrcError(st, f"btrc_ctx_create(device={device}) failed")
         self.handle = h
         self.device = device
+        self._scenes = weakref.WeakSet()
 
     def _check(self, status: int):
         if status != OK:
@@ -156,7 +158,10 @@ class Context:
             raise BtrcError(status, msg.decode() if msg else "")
 
     def close(self):
+        """Destroy the context; scenes still open on it are destroyed with it."""
         if getattr(self, "handle", None):
+            for sc in list(getattr(self, "_scenes", ())):
+                sc.handle = None  # owned by the context from here on
             self._lib.btrc_ctx_destroy(self.handle)
             self.handle = None
 
@@ -175,7 +180,9 @@ class Context:
     def load_scene(self, path: str | os.PathLike) -> "Scene":
         h = _vp()
         self._check(self._lib.btrc_scene_load_json(self.handle, str(path).encode(), C.byref(h)))
-        return Scene(self, h)
+        sc = Scene(self, h)
+        self._scenes.add(sc)
+        return sc
 
     def cancel(self):
         self._lib.btrc_cancel(self.handle)
@@ -254,9 +261,9 @@ class Scene:
         return nodes, tris
 
     def close(self):
-        if getattr(self, "handle", None):
+        if getattr(self, "handle", None) and getattr(self.ctx, "handle", None):
             self.ctx._lib.btrc_scene_destroy(self.handle)
-            self.handle = None
+        self.handle = None
 
     def __del__(self):
         try:

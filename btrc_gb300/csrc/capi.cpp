@@ -6,6 +6,7 @@
 #include <memory>
 #include <mutex>
 #include <new>
+#include <set>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -33,6 +34,7 @@ struct btrc_ctx
     bool has_media_buffers = false;
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
+    std::set<btrc_scene *> scenes;  // live scenes, destroyed with the context
 };
 
 struct btrc_scene
@@ -476,6 +478,9 @@ void btrc_ctx_destroy(btrc_ctx *ctx)
 {
     if(!ctx)
         return;
+    // scenes still alive are destroyed with their context
+    while(!ctx->scenes.empty())
+        btrc_scene_destroy(*ctx->scenes.begin());
     if(ctx->device < 0)
     {
         delete ctx;
@@ -515,7 +520,10 @@ btrc_status btrc_scene_load_json(btrc_ctx *ctx, const char *path, btrc_scene **o
     sc->ctx = ctx;
     const btrc_status s = guarded(ctx, [&] { sc->host = load_scene(path); });
     if(s == BTRC_OK)
+    {
         *out = sc.release();
+        ctx->scenes.insert(*out);
+    }
     return s;
 }
 
@@ -561,10 +569,13 @@ void btrc_scene_destroy(btrc_scene *scene)
 {
     if(!scene)
         return;
-    if(scene->ctx->device >= 0)
+    btrc_ctx *ctx = scene->ctx;
+    if(ctx->scenes.erase(scene) == 0)
+        return;  // not a live scene of its context (already destroyed with it)
+    if(ctx->device >= 0)
     {
-        cudaSetDevice(scene->ctx->device);
-        cudaStreamSynchronize(scene->ctx->stream);
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
         free_all(scene->allocs);
     }
     delete scene;

@@ -132,6 +132,8 @@ const char *btrc_version(void);
 /* device >= 0: CUDA device index. device == -1: host-only context that can load scenes
    and build BVHs (btrc_scene_build skips the upload) but runs no device work. */
 btrc_status btrc_ctx_create(int device, btrc_ctx **out);
+/* Destroys the context and every scene still alive on it; scene handles of a destroyed
+   context must not be used again (not even with btrc_scene_destroy). */
 void btrc_ctx_destroy(btrc_ctx *ctx);
 const char *btrc_last_error(const btrc_ctx *ctx);
 /* Ask a running btrc_render on this context to stop between bounces (thread safe). */

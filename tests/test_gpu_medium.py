@@ -58,7 +58,8 @@ def test_ratio_tracking_constant_grid(gpu_ctx, tmp_path):
         se = tr.std() / np.sqrt(n)
         assert abs(tr.mean() - want) < 4 * se + 1e-6, (L, tr.mean(), want, se)
         # sigma_max == sigma: every tentative collision is real, so each estimate is 0 or 1
-        assert set(np.unique(tr)) <= {0.0, 1.0}
+        # up to the rounding of the interpolated density
+        assert np.all(np.minimum(np.abs(tr), np.abs(tr - 1.0)) < 1e-6)
 
 
 def test_homogeneous_closed_form(gpu_ctx, tmp_path):
