@@ -13,7 +13,7 @@
 
 #include <cuda_runtime.h>
 
-#include "../../include/btrc.h"
+#include "btrc.h"
 #include "bvh.h"
 #include "kernels.h"
 #include "scene.h"

@@ -123,9 +123,12 @@ __device__ __forceinline__ bool watertight(const TravRay &r, float4 a, float4 b,
     return true;
 }
 
+// Byte j of w as an exact float without the (quarter-rate) integer-to-float unit: one
+// byte permute builds 0x4B0000bb, i.e. the float 2^23 + b, and one full-rate add removes
+// 2^23. The result equals (float)b bit for bit.
 __device__ __forceinline__ float byte_f(uint32_t w, int j)
 {
-    return static_cast<float>((w >> (8 * j)) & 0xffu);
+    return __uint_as_float(__byte_perm(w, 0x4Bu, 0x4550u + static_cast<uint32_t>(j))) - 8388608.0f;
 }
 
 // Intersects the 8 children of a node. Returns the hit mask: bits 24..31 child nodes
