@@ -86,6 +86,7 @@ SIGNATURES = {
     "btrc_scene_export_triangles": (C.c_int, [_vp, _vp, _vp, C.c_uint64]),
     "btrc_scene_export_bvh": (C.c_int, [_vp, _vp, C.c_uint64, _vp, C.c_uint64]),
     "btrc_render": (C.c_int, [_vp, _vp, C.POINTER(RenderOpts), _vp, C.POINTER(Stats)]),
+    "btrc_render_noalloc": (C.c_int, [_vp, _vp, C.c_int32, _vp, C.POINTER(Stats)]),
     "btrc_trace_closest": (C.c_int, [_vp, _vp, _vp, C.c_uint64, _vp, _vp, _vp]),
     "btrc_trace_any": (C.c_int, [_vp, _vp, _vp, C.c_uint64, _vp, _vp]),
     "btrc_trace_stats": (C.c_int, [_vp, _vp, _vp, C.c_uint64, _vp, _vp, _vp]),
@@ -198,6 +199,15 @@ class Context:
         opts = RenderOpts(spp, state_count, 1 if on_dev else 0, 1 if use_graphs else 0, profile)
         st = Stats()
         self._check(self._lib.btrc_render(self.handle, scene.handle, C.byref(opts), _ptr(out), C.byref(st)))
+        if stats is not None:
+            stats.update(st.as_dict())
+        return out
+
+    def render_noalloc(self, scene: "Scene", out, spp: int = 0, stats: dict | None = None):
+        """Allocation-free render into a caller-owned CUDA tensor of shape (H, W, 3)
+        (btrc_render_noalloc: fixed scratch, film up to 512x512 pixels)."""
+        st = Stats()
+        self._check(self._lib.btrc_render_noalloc(self.handle, scene.handle, spp, _ptr(out), C.byref(st)))
         if stats is not None:
             stats.update(st.as_dict())
         return out

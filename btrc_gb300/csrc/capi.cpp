@@ -693,6 +693,56 @@ btrc_status btrc_render(btrc_ctx *ctx, btrc_scene *scene, const btrc_render_opts
     return s;
 }
 
+btrc_status btrc_render_noalloc(btrc_ctx *ctx, btrc_scene *scene, int32_t spp, float *d_rgb_out, btrc_stats *stats)
+{
+    if(!ctx || !scene || !d_rgb_out || spp < 0)
+        return BTRC_ERR_INVALID_ARG;
+    bool cancelled = false;
+    const btrc_status s = guarded(ctx, [&] {
+        require_built(scene);
+        const HostScene &H = scene->host;
+        const uint64_t pixels = static_cast<uint64_t>(H.params.width) * H.params.height;
+        if(pixels > noalloc_max_pixels())
+            throw StatusError(BTRC_ERR_INVALID_ARG,
+                              "btrc_render_noalloc: film of " + std::to_string(pixels) + " pixels exceeds the " +
+                                  std::to_string(noalloc_max_pixels()) + "-pixel limit of its fixed scratch");
+        check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+        void *scratch = nullptr;
+        check_cuda(noalloc_scratch_address(ctx->device, &scratch), "cudaGetSymbolAddress(scratch)");
+        ctx->cancel.store(false);
+        const int n_spp = spp > 0 ? spp : H.params.spp;
+        const uint64_t total = static_cast<uint64_t>(n_spp) * pixels;
+        const uint32_t capacity = static_cast<uint32_t>(std::min<uint64_t>(
+            std::min<uint64_t>(noalloc_max_states(), static_cast<uint64_t>(H.params.state_count)),
+            std::max<uint64_t>(total, 1)));
+        const DevRender R = make_render_params(scene, n_spp, capacity);
+        RenderStats rs{};
+        check_cuda(render_wavefront_noalloc(scene->dev, R, scratch, d_rgb_out, ctx->stream, &ctx->cancel, &rs,
+                                            &cancelled),
+                   "allocation-free render");
+        if(stats)
+        {
+            *stats = btrc_stats{};
+            stats->paths = rs.paths;
+            stats->extension_rays = rs.ext_rays;
+            stats->shadow_rays = rs.shadow_rays;
+            stats->bounces = rs.iterations;
+            stats->traversal_errors = rs.err;
+            stats->kernel_launches = rs.kernel_launches;
+            for(int k = 0; k < 6; ++k)
+                stats->stage_launches[k] = rs.stage_launches[k];
+        }
+        if(rs.err)
+            throw StatusError(BTRC_ERR_INTERNAL, "traversal stack overflow reported by the device");
+    });
+    if(s == BTRC_OK && cancelled)
+    {
+        ctx->last_error = "render cancelled";
+        return BTRC_ERR_CANCELLED;
+    }
+    return s;
+}
+
 btrc_status btrc_trace_closest(btrc_ctx *ctx, const btrc_scene *scene, const btrc_ray *d_rays, uint64_t n,
                                uint32_t *d_flags, btrc_hit *d_hits, void *stream)
 {

@@ -11,6 +11,7 @@
 //   * two bounces (ping and pong buffers) are captured into one CUDA graph and relaunched.
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 #include <vector>
 
 #include "bsdf.cuh"
@@ -1109,6 +1110,164 @@ cudaError_t launch_resolve(const float4 *film, float *rgb, uint32_t pixels, cuda
         return cudaSuccess;
     k_resolve<<<(pixels + 255) / 256, 256, 0, st>>>(film, rgb, pixels);
     return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- allocation-free render
+//
+// For callers that cannot allocate GPU memory while they render: engines that reserve
+// all device memory up front and hand out nothing afterwards, processes running under a
+// hard memory budget, or code that must not call cudaMalloc/cudaFree (which synchronise
+// the device) on a latency-critical thread. Everything the wavefront loop needs beyond
+// the scene and the caller's output image lives in one fixed array below, reserved when
+// the library's kernels are loaded on a device and kept until the process exits.
+
+namespace {
+
+constexpr uint32_t NOALLOC_MAX_STATES = 32768;   // path-queue capacity
+constexpr uint32_t NOALLOC_MAX_PIXELS = 512 * 512;
+constexpr size_t NOALLOC_PATH_BYTES = 6 * 16;    // one PathSoA slot
+constexpr size_t NOALLOC_BYTES =
+    2 * NOALLOC_PATH_BYTES * NOALLOC_MAX_STATES      // current + next queues
+    + 4 * 16 * NOALLOC_MAX_STATES                     // shadow queue (o, d, beta, sampler)
+    + (4 + 16) * NOALLOC_MAX_STATES                   // hit flags + details
+    + 16 * static_cast<size_t>(NOALLOC_MAX_PIXELS)    // film
+    + 256                                             // counters
+    + 32 * 256;                                       // 256-byte alignment of each buffer
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mutex;
+void *g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
+
+} // namespace
+
+size_t noalloc_scratch_bytes() { return NOALLOC_BYTES; }
+uint32_t noalloc_max_states() { return NOALLOC_MAX_STATES; }
+uint32_t noalloc_max_pixels() { return NOALLOC_MAX_PIXELS; }
+
+// Device address of the scratch array for the current device. The host-side name of a
+// __device__ variable is only a stand-in, so the address is looked up once per device
+// (with that device current) and cached.
+cudaError_t noalloc_scratch_address(int device, void **out)
+{
+    if(device < 0 || device >= NOALLOC_MAX_DEVICES)
+        return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if(!g_noalloc_addr[device])
+    {
+        void *ptr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if(e != cudaSuccess)
+            return e;
+        g_noalloc_addr[device] = ptr;
+    }
+    *out = g_noalloc_addr[device];
+    return cudaSuccess;
+}
+
+cudaError_t render_wavefront_noalloc(const DevScene &S, const DevRender &R, void *scratch, float *rgb_out,
+                                     cudaStream_t st, const std::atomic<bool> *cancel, RenderStats *stats,
+                                     bool *cancelled)
+{
+    *cancelled = false;
+    const uint32_t cap = R.capacity;
+    const size_t pixels = static_cast<size_t>(R.width) * R.height;
+    // carve the fixed array into the same buffers render_wavefront uses
+    unsigned char *p = static_cast<unsigned char *>(scratch);
+    auto take = [&](size_t bytes) {
+        unsigned char *r = p;
+        p += (bytes + 255) / 256 * 256;
+        return r;
+    };
+    RenderBuffers B{};
+    for(int k = 0; k < 2; ++k)
+    {
+        B.path[k].beta_depth = reinterpret_cast<F4 *>(take(16ull * cap));
+        B.path[k].rad_pixel = reinterpret_cast<F4 *>(take(16ull * cap));
+        B.path[k].sampler = reinterpret_cast<SamplerState *>(take(16ull * cap));
+        B.path[k].ray_o = reinterpret_cast<F4 *>(take(16ull * cap));
+        B.path[k].ray_d = reinterpret_cast<F4 *>(take(16ull * cap));
+        B.path[k].bsdf_le = reinterpret_cast<F4 *>(take(16ull * cap));
+    }
+    B.shadow.o = reinterpret_cast<F4 *>(take(16ull * cap));
+    B.shadow.d = reinterpret_cast<F4 *>(take(16ull * cap));
+    B.shadow.beta = reinterpret_cast<F4 *>(take(16ull * cap));
+    B.shadow.sampler = reinterpret_cast<SamplerState *>(take(16ull * cap));
+    B.hit_flag = reinterpret_cast<uint32_t *>(take(4ull * cap));
+    B.hit_detail = reinterpret_cast<HitDetail *>(take(16ull * cap));
+    B.film = reinterpret_cast<float4 *>(take(16ull * pixels));
+    B.counters = reinterpret_cast<Counters *>(take(sizeof(Counters)));
+    B.host_counters = nullptr;
+    B.capacity = cap;
+    if(static_cast<size_t>(p - static_cast<unsigned char *>(scratch)) > NOALLOC_BYTES)
+        return cudaErrorInvalidValue;
+
+    // the array keeps the previous call's contents: clear the film and the counters
+    cudaError_t e = cudaMemsetAsync(B.film, 0, 16ull * pixels, st);
+    if(e == cudaSuccess)
+        e = cudaMemsetAsync(B.counters, 0, sizeof(Counters), st);
+    if(e != cudaSuccess)
+        return e;
+    const int grids[5] = {
+        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_generate)),
+        persistent_grid(128, reinterpret_cast<const void *>(k_trace<false>)),
+        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_medium)),
+        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_shade)),
+        persistent_grid(128, reinterpret_cast<const void *>(k_shadow)),
+    };
+    const uint64_t depth_bound = static_cast<uint64_t>(std::max(R.max_depth, R.min_depth)) + 2;
+    const uint64_t max_launches = ((R.total_paths + cap - 1) / cap + 2) * depth_bound + 64;
+    uint64_t launches[STAGE_COUNT] = {};
+    Counters c{};
+    for(uint64_t launch = 0;; ++launch)
+    {
+        if(launch >= max_launches)
+        {
+            e = cudaErrorLaunchTimeout;
+            break;
+        }
+        e = enqueue_bounce(S, R, B, 0, st, grids, 0, nullptr, launches);
+        if(e == cudaSuccess)
+            e = enqueue_bounce(S, R, B, 1, st, grids, 0, nullptr, launches);
+        // counters come back synchronously into this stack variable: no pinned buffer
+        if(e == cudaSuccess)
+            e = cudaMemcpyAsync(&c, B.counters, sizeof(Counters), cudaMemcpyDeviceToHost, st);
+        if(e == cudaSuccess)
+            e = cudaStreamSynchronize(st);
+        if(e != cudaSuccess)
+            break;
+        if(c.generated >= R.total_paths && c.next_active == 0)
+            break;
+        if(cancel && cancel->load())
+        {
+            *cancelled = true;
+            break;
+        }
+    }
+    if(e == cudaSuccess)
+        e = launch_resolve(B.film, rgb_out, static_cast<uint32_t>(pixels), st);
+    if(e == cudaSuccess)
+        e = cudaMemcpyAsync(&c, B.counters, sizeof(Counters), cudaMemcpyDeviceToHost, st);
+    if(e == cudaSuccess)
+        e = cudaStreamSynchronize(st);
+    if(stats)
+    {
+        *stats = RenderStats{};
+        stats->paths = c.generated;
+        stats->ext_rays = c.ext_rays;
+        stats->shadow_rays = c.shadow_rays + c.shadow;
+        stats->iterations = c.iterations;
+        stats->err = c.err;
+        uint64_t total = 0;
+        for(int k = 0; k < STAGE_COUNT; ++k)
+        {
+            stats->stage_launches[k] = launches[k];
+            total += launches[k];
+        }
+        stats->kernel_launches = total + 1;
+    }
+    return e;
 }
 
 // ---------------------------------------------------------------- test hooks

@@ -69,6 +69,16 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
                              const std::atomic<bool> *cancel, bool use_graphs, int profile, RenderStats *stats,
                              bool *cancelled);
 
+// Allocation-free variant of render_wavefront: all scratch (queues, film, counters) lives
+// in a fixed device array; see the block comment above render_wavefront_noalloc.
+size_t noalloc_scratch_bytes();
+uint32_t noalloc_max_states();
+uint32_t noalloc_max_pixels();
+cudaError_t noalloc_scratch_address(int device, void **out);
+cudaError_t render_wavefront_noalloc(const DevScene &S, const DevRender &R, void *scratch, float *rgb_out,
+                                     cudaStream_t st, const std::atomic<bool> *cancel, RenderStats *stats,
+                                     bool *cancelled);
+
 // radiance / weight -> rgb (3 floats per pixel)
 cudaError_t launch_resolve(const float4 *film, float *rgb, uint32_t pixels, cudaStream_t st);
 

@@ -158,6 +158,22 @@ btrc_status btrc_scene_export_bvh(const btrc_scene *scene, void *nodes, uint64_t
 btrc_status btrc_render(btrc_ctx *ctx, btrc_scene *scene, const btrc_render_opts *opts, float *rgb_out,
                         btrc_stats *stats);
 
+/* Render the whole frame without allocating any GPU memory during the call (no
+   counterpart in the reference). For callers that cannot call cudaMalloc while they run:
+   engines that reserve all device memory up front and hand none out later, processes
+   under a hard memory budget, and latency-critical threads on which cudaMalloc/cudaFree
+   (which synchronise the device) are not allowed. The scene must already be built;
+   d_rgb_out is a caller-owned device buffer of width*height*3 floats.
+   All scratch (path queues of 32768 states, film, counters) lives in one fixed
+   ~13 MB __device__ array that every GPU loading this library reserves until the
+   process exits. Limits: width*height <= 262144 (e.g. 512x512), otherwise
+   BTRC_ERR_INVALID_ARG. Each call clears the film and counters it needs; calls share the
+   array, so calls that overlap on the GPU (other threads, other contexts on the same
+   device) race and must be serialised by the caller. The first call on a device looks
+   up the array's device address (cudaGetSymbolAddress); make that first call before any
+   stream capture. spp 0 uses the scene's renderer.spp. */
+btrc_status btrc_render_noalloc(btrc_ctx *ctx, btrc_scene *scene, int32_t spp, float *d_rgb_out, btrc_stats *stats);
+
 /* Closest hit for n device-resident rays. flags[i] = instance | BTRC_HIT_BIT or 0. */
 btrc_status btrc_trace_closest(btrc_ctx *ctx, const btrc_scene *scene, const btrc_ray *d_rays, uint64_t n,
                                uint32_t *d_flags, btrc_hit *d_hits, void *stream);
