@@ -67,6 +67,8 @@ struct Counters
     uint64_t shadow_rays;  // shadow rays traced
     uint64_t node_visits;  // closest-hit node visits (counting mode only)
     uint64_t tri_tests;    // closest-hit triangle tests (counting mode only)
+    uint32_t trace_cursor;   // next ray for the warp-refill traversal (reset every bounce)
+    uint32_t shadow_cursor;
 };
 
 // Structure-of-arrays path state. Two copies (current / next) per render.

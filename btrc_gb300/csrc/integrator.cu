@@ -466,6 +466,8 @@ __global__ void k_control(Counters *c, uint32_t capacity, uint64_t total)
     k.ext_rays += k.active;
     k.next_active = 0;
     k.shadow = 0;
+    k.trace_cursor = 0;
+    k.shadow_cursor = 0;
     if(k.active > 0)
         ++k.iterations;
     *c = k;
@@ -538,21 +540,21 @@ __global__ void __launch_bounds__(128) k_trace(DevScene S, PathSoA P, uint32_t *
                                                Counters *cnt)
 {
     const uint32_t n = cnt->active;
-    const uint32_t stride = gridDim.x * blockDim.x;
     uint64_t nv = 0, tv = 0;
-    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-    {
-        const F4 o = P.ray_o[i], d = P.ray_d[i];
-        const TravRay tr = make_trav_ray(o.x, o.y, o.z, d.x, d.y, d.z);
-        uint32_t a = 0, b = 0;
-        const ClosestResult c = trace_closest(tr, d.w, reinterpret_cast<const float4 *>(S.nodes),
-                                              reinterpret_cast<const float4 *>(S.tris), S.node_count, &cnt->err,
-                                              COUNT ? &a : nullptr, COUNT ? &b : nullptr);
-        nv += a;
-        tv += b;
-        flags[i] = c.hit ? (c.inst | HIT_BIT) : 0u;
-        hits[i] = HitDetail{ c.t, c.prim, c.b1, c.b2 };
-    }
+    traverse_refill<false, COUNT>(
+        reinterpret_cast<const float4 *>(S.nodes), reinterpret_cast<const float4 *>(S.tris), S.node_count,
+        &cnt->trace_cursor, n, REFILL_LANES, &cnt->err,
+        [&](uint32_t i, float *o, float *d, float &t1) {
+            const F4 ro = P.ray_o[i], rd = P.ray_d[i];
+            o[0] = ro.x; o[1] = ro.y; o[2] = ro.z;
+            d[0] = rd.x; d[1] = rd.y; d[2] = rd.z;
+            t1 = rd.w;
+        },
+        [&](uint32_t i, const ClosestResult &c) {
+            flags[i] = c.hit ? (c.inst | HIT_BIT) : 0u;
+            hits[i] = HitDetail{ c.t, c.prim, c.b1, c.b2 };
+        },
+        &nv, &tv);
     if(COUNT)
     {
         for(int off = 16; off > 0; off >>= 1)
@@ -807,39 +809,44 @@ __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, DevRender R, PathSo
     }
 }
 
-// ShadowPipeline (builtin/btrc/builtin/renderer/wavefront/shadow.cpp:24-76)
+// ShadowPipeline (builtin/btrc/builtin/renderer/wavefront/shadow.cpp:24-76): occlusion by
+// the warp-refill traversal; unoccluded records splat (times the medium transmittance)
 __global__ void __launch_bounds__(128) k_shadow(DevScene S, DevRender R, ShadowSoA SH, float4 *film, Counters *cnt)
 {
     const uint32_t n = cnt->shadow;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-    {
-        const F4 o = SH.o[i], d = SH.d[i];
-        const TravRay tr = make_trav_ray(o.x, o.y, o.z, d.x, d.y, d.z);
-        if(trace_any(tr, d.w, reinterpret_cast<const float4 *>(S.nodes), reinterpret_cast<const float4 *>(S.tris),
-                     S.node_count, &cnt->err))
-            continue;
-        const F4 b = SH.beta[i];
-        V3 beta = v3(b);
-        if(S.has_media)
-        {
-            DSampler smp;
-            smp.type = SAMPLER_INDEPENDENT;
-            smp.s = SH.sampler[i];
-            const V3 ro = v3(o), rdv = v3(d);
-            if(d.w > 1)
+    traverse_refill<true>(
+        reinterpret_cast<const float4 *>(S.nodes), reinterpret_cast<const float4 *>(S.tris), S.node_count,
+        &cnt->shadow_cursor, n, REFILL_LANES, &cnt->err,
+        [&](uint32_t i, float *o, float *d, float &t1) {
+            const F4 so = SH.o[i], sd = SH.d[i];
+            o[0] = so.x; o[1] = so.y; o[2] = so.z;
+            d[0] = sd.x; d[1] = sd.y; d[2] = sd.z;
+            t1 = sd.w;
+        },
+        [&](uint32_t i, const ClosestResult &c) {
+            if(c.hit)
+                return;
+            const F4 o = SH.o[i], d = SH.d[i], b = SH.beta[i];
+            V3 beta = v3(b);
+            if(S.has_media)
             {
-                const Medium &m = S.media[S.vacuum_medium];
-                beta = beta * medium_tr(S, m, ro, ro + normalize(rdv) * S.world_diagonal, smp);
+                DSampler smp;
+                smp.type = SAMPLER_INDEPENDENT;
+                smp.s = SH.sampler[i];
+                const V3 ro = v3(o), rdv = v3(d);
+                if(d.w > 1)
+                {
+                    const Medium &m = S.media[S.vacuum_medium];
+                    beta = beta * medium_tr(S, m, ro, ro + normalize(rdv) * S.world_diagonal, smp);
+                }
+                else
+                {
+                    const Medium &m = S.media[__float_as_int(b.w)];
+                    beta = beta * medium_tr(S, m, ro, ro + rdv * d.w, smp);
+                }
             }
-            else
-            {
-                const Medium &m = S.media[__float_as_int(b.w)];
-                beta = beta * medium_tr(S, m, ro, ro + rdv * d.w, smp);
-            }
-        }
-        splat(film, __float_as_uint(o.w), R.width, beta);
-    }
+            splat(film, __float_as_uint(o.w), R.width, beta);
+        });
 }
 
 __global__ void k_resolve(const float4 *film, float *rgb, uint32_t pixels)

@@ -10,45 +10,6 @@ namespace {
 
 constexpr int TRACE_BLOCK = 128;
 
-__global__ void __launch_bounds__(TRACE_BLOCK) k_trace_closest(DevScene S, const Ray *__restrict__ rays, uint32_t n,
-                                                               uint32_t *__restrict__ flags,
-                                                               HitDetail *__restrict__ hits, uint32_t *err)
-{
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-    {
-        const float4 ro = __ldg(reinterpret_cast<const float4 *>(rays) + i * 2);
-        const float4 rd = __ldg(reinterpret_cast<const float4 *>(rays) + i * 2 + 1);
-        const TravRay tr = make_trav_ray(ro.x, ro.y, ro.z, rd.x, rd.y, rd.z);
-        const ClosestResult c = trace_closest(tr, rd.w, reinterpret_cast<const float4 *>(S.nodes),
-                                              reinterpret_cast<const float4 *>(S.tris), S.node_count, err);
-        if(c.hit)
-        {
-            flags[i] = c.inst | HIT_BIT;
-            hits[i] = HitDetail{ c.t, c.prim, c.b1, c.b2 };
-        }
-        else
-        {
-            flags[i] = 0u;
-            hits[i] = HitDetail{ 0.0f, 0u, 0.0f, 0.0f };
-        }
-    }
-}
-
-__global__ void __launch_bounds__(TRACE_BLOCK) k_trace_any(DevScene S, const Ray *__restrict__ rays, uint32_t n,
-                                                           uint32_t *__restrict__ occluded, uint32_t *err)
-{
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-    {
-        const float4 ro = __ldg(reinterpret_cast<const float4 *>(rays) + i * 2);
-        const float4 rd = __ldg(reinterpret_cast<const float4 *>(rays) + i * 2 + 1);
-        const TravRay tr = make_trav_ray(ro.x, ro.y, ro.z, rd.x, rd.y, rd.z);
-        occluded[i] = trace_any(tr, rd.w, reinterpret_cast<const float4 *>(S.nodes),
-                                reinterpret_cast<const float4 *>(S.tris), S.node_count, err) ? 1u : 0u;
-    }
-}
-
 __global__ void __launch_bounds__(TRACE_BLOCK) k_trace_stats(DevScene S, const Ray *__restrict__ rays, uint32_t n,
                                                              uint32_t *__restrict__ nv, uint32_t *__restrict__ tv,
                                                              uint32_t *err)
@@ -65,6 +26,55 @@ __global__ void __launch_bounds__(TRACE_BLOCK) k_trace_stats(DevScene S, const R
         nv[i] = a;
         tv[i] = b;
     }
+}
+
+// persistent kernels with warp-level ray refill (traverse_refill); the cursor must be
+// zero at launch
+__global__ void __launch_bounds__(TRACE_BLOCK) k_trace_closest_dyn(DevScene S, const Ray *__restrict__ rays, uint32_t n,
+                                                                   uint32_t *__restrict__ flags,
+                                                                   HitDetail *__restrict__ hits, uint32_t *cursor,
+                                                                   uint32_t *err)
+{
+    traverse_refill<false>(
+        reinterpret_cast<const float4 *>(S.nodes), reinterpret_cast<const float4 *>(S.tris), S.node_count, cursor, n,
+        REFILL_LANES, err,
+        [&](uint32_t i, float *o, float *d, float &t1) {
+            const float4 ro = __ldg(reinterpret_cast<const float4 *>(rays) + i * 2);
+            const float4 rd = __ldg(reinterpret_cast<const float4 *>(rays) + i * 2 + 1);
+            o[0] = ro.x; o[1] = ro.y; o[2] = ro.z;
+            d[0] = rd.x; d[1] = rd.y; d[2] = rd.z;
+            t1 = rd.w;
+        },
+        [&](uint32_t i, const ClosestResult &c) {
+            flags[i] = c.hit ? (c.inst | HIT_BIT) : 0u;
+            hits[i] = c.hit ? HitDetail{ c.t, c.prim, c.b1, c.b2 } : HitDetail{ 0.0f, 0u, 0.0f, 0.0f };
+        });
+}
+
+__global__ void __launch_bounds__(TRACE_BLOCK) k_trace_any_dyn(DevScene S, const Ray *__restrict__ rays, uint32_t n,
+                                                               uint32_t *__restrict__ occluded, uint32_t *cursor,
+                                                               uint32_t *err)
+{
+    traverse_refill<true>(
+        reinterpret_cast<const float4 *>(S.nodes), reinterpret_cast<const float4 *>(S.tris), S.node_count, cursor, n,
+        REFILL_LANES, err,
+        [&](uint32_t i, float *o, float *d, float &t1) {
+            const float4 ro = __ldg(reinterpret_cast<const float4 *>(rays) + i * 2);
+            const float4 rd = __ldg(reinterpret_cast<const float4 *>(rays) + i * 2 + 1);
+            o[0] = ro.x; o[1] = ro.y; o[2] = ro.z;
+            d[0] = rd.x; d[1] = rd.y; d[2] = rd.z;
+            t1 = rd.w;
+        },
+        [&](uint32_t i, const ClosestResult &c) { occluded[i] = c.hit ? 1u : 0u; });
+}
+
+uint32_t persistent_blocks(const void *kernel)
+{
+    int dev = 0, sms = 152, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, TRACE_BLOCK, 0);
+    return static_cast<uint32_t>(sms * (per_sm > 0 ? per_sm : 1));
 }
 
 uint32_t grid_for(uint32_t n, int block)
@@ -84,7 +94,11 @@ cudaError_t launch_trace_closest(const DevScene &S, const Ray *rays, uint32_t n,
 {
     if(n == 0)
         return cudaSuccess;
-    k_trace_closest<<<grid_for(n, TRACE_BLOCK), TRACE_BLOCK, 0, st>>>(S, rays, n, flags, hits, err);
+    cudaError_t e = cudaMemsetAsync(err + 4, 0, sizeof(uint32_t), st);
+    if(e != cudaSuccess)
+        return e;
+    k_trace_closest_dyn<<<persistent_blocks(reinterpret_cast<const void *>(k_trace_closest_dyn)), TRACE_BLOCK, 0, st>>>(
+        S, rays, n, flags, hits, err + 4, err);
     return cudaGetLastError();
 }
 
@@ -93,7 +107,11 @@ cudaError_t launch_trace_any(const DevScene &S, const Ray *rays, uint32_t n, uin
 {
     if(n == 0)
         return cudaSuccess;
-    k_trace_any<<<grid_for(n, TRACE_BLOCK), TRACE_BLOCK, 0, st>>>(S, rays, n, occluded, err);
+    cudaError_t e = cudaMemsetAsync(err + 8, 0, sizeof(uint32_t), st);
+    if(e != cudaSuccess)
+        return e;
+    k_trace_any_dyn<<<persistent_blocks(reinterpret_cast<const void *>(k_trace_any_dyn)), TRACE_BLOCK, 0, st>>>(
+        S, rays, n, occluded, err + 8, err);
     return cudaGetLastError();
 }
 

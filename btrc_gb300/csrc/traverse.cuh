@@ -11,7 +11,8 @@
 // CPU oracle (compiled without FP contraction) reproduces t and the barycentrics bit
 // for bit. Candidate order is a strict total order on (t, instance, primitive), which
 // makes the closest hit independent of traversal order. Box tests are conservative:
-// quantised boxes round outwards and the box interval is widened by 2^-20 relative.
+// quantised boxes round outwards and the far distances (and the current closest t) are
+// widened by 2^-20 relative.
 #pragma once
 
 #include <cstdint>
@@ -123,6 +124,21 @@ __device__ __forceinline__ bool watertight(const TravRay &r, float4 a, float4 b,
     return true;
 }
 
+// Three-input FP32 min / max (sm_100 and later): one instruction instead of two.
+__device__ __forceinline__ float max3f(float a, float b, float c)
+{
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+__device__ __forceinline__ float min3f(float a, float b, float c)
+{
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
 // Byte j of w as an exact float without the (quarter-rate) integer-to-float unit: one
 // byte permute builds 0x4B0000bb, i.e. the float 2^23 + b, and one full-rate add removes
 // 2^23. The result equals (float)b bit for bit.
@@ -152,6 +168,11 @@ __device__ __forceinline__ uint32_t intersect_children(const TravRay &r, const f
     const float orgx = (n0.x - r.ox) * r.idx;
     const float orgy = (n0.y - r.oy) * r.idy;
     const float orgz = (n0.z - r.oz) * r.idz;
+    // far planes use coefficients pre-scaled by BOX_EPS, so every far distance comes out
+    // widened by 2^-20 relative without a multiply per child
+    const float fadjx = adjx * BOX_EPS, fadjy = adjy * BOX_EPS, fadjz = adjz * BOX_EPS;
+    const float forgx = orgx * BOX_EPS, forgy = orgy * BOX_EPS, forgz = orgz * BOX_EPS;
+    const float tcur_e = tcur * BOX_EPS;
     const bool nx = r.idx < 0.0f, ny = r.idy < 0.0f, nz = r.idz < 0.0f;
 
     uint32_t hitmask = 0;
@@ -171,11 +192,11 @@ __device__ __forceinline__ uint32_t intersect_children(const TravRay &r, const f
             const float tnx = fmaf(byte_f(xn, j), adjx, orgx);
             const float tny = fmaf(byte_f(yn, j), adjy, orgy);
             const float tnz = fmaf(byte_f(zn, j), adjz, orgz);
-            const float tfx = fmaf(byte_f(xf, j), adjx, orgx);
-            const float tfy = fmaf(byte_f(yf, j), adjy, orgy);
-            const float tfz = fmaf(byte_f(zf, j), adjz, orgz);
-            const float tmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
-            const float tmax = fminf(fminf(tfx, tfy), fminf(tfz, tcur)) * BOX_EPS;
+            const float tfx = fmaf(byte_f(xf, j), fadjx, forgx);
+            const float tfy = fmaf(byte_f(yf, j), fadjy, forgy);
+            const float tfz = fmaf(byte_f(zf, j), fadjz, forgz);
+            const float tmin = fmaxf(max3f(tnx, tny, tnz), 0.0f);
+            const float tmax = fminf(min3f(tfx, tfy, tfz), tcur_e);
             if(m != 0u && tmin <= tmax)
             {
                 const bool inner = (m & 0x18u) == 0x18u;
@@ -340,6 +361,164 @@ __device__ __forceinline__ bool trace_any(const TravRay &r, float t1, const floa
         }
     }
     return false;
+}
+
+} // namespace bt
+
+namespace bt {
+
+// Persistent traversal with warp-level ray refill. Every lane runs the same loop; a lane
+// whose ray has finished becomes idle, and once at least `refill` lanes of the warp are
+// idle (or no lane is busy) the idle lanes take the next rays from a global cursor with
+// one atomic per warp. Each loop iteration advances every busy lane by one node (plus
+// that node's triangles), so lanes never wait for the slowest ray of their warp.
+// All 32 lanes must enter (the warp-wide votes use the full mask).
+//   fetch(i, o, d, t1): load ray i;  emit(i, hit): store its result
+constexpr int REFILL_LANES = 8;  // idle lanes that trigger a warp refill (measured best of 8/16/24)
+
+template<bool ANY, bool COUNT = false, typename Fetch, typename Emit>
+__device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes4, const float4 *__restrict__ tris4,
+                                                uint32_t node_count, uint32_t *cursor, uint32_t n, int refill,
+                                                uint32_t *err, Fetch fetch, Emit emit,
+                                                uint64_t *node_visits = nullptr, uint64_t *tri_tests = nullptr)
+{
+    uint64_t visits = 0, tests = 0;
+    const uint32_t FULL = 0xffffffffu;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    int state = 0;  // 0 idle, 1 busy, 2 exhausted
+    uint32_t ray = 0;
+    TravRay r;
+    ClosestResult best;
+    uint2 stack[STACK_SIZE];
+    int sp = 0;
+    uint2 ngroup = make_uint2(0u, 0u);
+    uint2 tgroup = make_uint2(0u, 0u);
+    for(;;)
+    {
+        const uint32_t idle = __ballot_sync(FULL, state == 0);
+        const uint32_t busy = __ballot_sync(FULL, state == 1);
+        if(idle != 0u && (__popc(idle) >= refill || busy == 0u))
+        {
+            const uint32_t leader = __ffs(idle) - 1u;
+            uint32_t base = 0;
+            if(lane == leader)
+                base = atomicAdd(cursor, static_cast<uint32_t>(__popc(idle)));
+            base = __shfl_sync(FULL, base, leader);
+            if(state == 0)
+            {
+                const uint32_t mine = base + static_cast<uint32_t>(__popc(idle & lt_mask));
+                if(mine < n)
+                {
+                    float o[3], d[3], t1;
+                    fetch(mine, o, d, t1);
+                    r = make_trav_ray(o[0], o[1], o[2], d[0], d[1], d[2]);
+                    ray = mine;
+                    best.hit = false;
+                    best.t = t1;
+                    best.b1 = best.b2 = 0.0f;
+                    best.inst = best.prim = 0xffffffffu;
+                    sp = 0;
+                    ngroup = make_uint2(0u, node_count ? 0x80000000u : 0u);
+                    tgroup = make_uint2(0u, 0u);
+                    state = 1;
+                }
+                else
+                    state = 2;
+            }
+        }
+        if(__all_sync(FULL, state == 2))
+            break;
+        if(state != 1)
+            continue;
+        if(COUNT && ngroup.y > 0x00ffffffu)
+            ++visits;
+
+        if(ngroup.y > 0x00ffffffu)
+        {
+            const int bit = 31 - __clz(ngroup.y);
+            const uint32_t slot = (static_cast<uint32_t>(bit) - 24u) ^ r.oct_inv;
+            const uint32_t rel = __popc(ngroup.y & ~(0xffffffffu << slot));
+            const uint32_t ni = ngroup.x + rel;
+            ngroup.y &= ~(1u << bit);
+            bool overflow = false;
+            if(ngroup.y > 0x00ffffffu)
+            {
+                if(sp >= STACK_SIZE)
+                {
+                    atomicOr(err, 1u);
+                    overflow = true;
+                }
+                else
+                    stack[sp++] = ngroup;
+            }
+            if(overflow)
+            {
+                ngroup = make_uint2(0u, 0u);
+                tgroup = make_uint2(0u, 0u);
+                sp = 0;
+            }
+            else
+            {
+                uint32_t cbase, tbase, imask;
+                const uint32_t hm = intersect_children(r, nodes4, ni, best.t, cbase, tbase, imask);
+                ngroup = make_uint2(cbase, (hm & 0xff000000u) | imask);
+                tgroup = make_uint2(tbase, hm & 0x00ffffffu);
+            }
+        }
+        bool done_any = false;
+        while(tgroup.y != 0u)
+        {
+            const int tb = 31 - __clz(tgroup.y);
+            tgroup.y &= ~(1u << tb);
+            const uint32_t ti = tgroup.x + static_cast<uint32_t>(tb);
+            const float4 a = __ldg(tris4 + ti * 3 + 0);
+            const float4 b = __ldg(tris4 + ti * 3 + 1);
+            const float4 c = __ldg(tris4 + ti * 3 + 2);
+            if(COUNT)
+                ++tests;
+            TriHit h;
+            if(watertight(r, a, b, c, best.t, h))
+            {
+                const uint32_t inst = __float_as_uint(a.w), prim = __float_as_uint(b.w);
+                if(!best.hit || closer(h.t, inst, prim, best.t, best.inst, best.prim))
+                {
+                    best.hit = true;
+                    best.t = h.t;
+                    best.b1 = h.b1;
+                    best.b2 = h.b2;
+                    best.inst = inst;
+                    best.prim = prim;
+                }
+                if(ANY)
+                {
+                    done_any = true;
+                    tgroup.y = 0u;
+                }
+            }
+        }
+        if(done_any)
+        {
+            emit(ray, best);
+            state = 0;
+            continue;
+        }
+        if(ngroup.y <= 0x00ffffffu)
+        {
+            if(sp == 0)
+            {
+                emit(ray, best);
+                state = 0;
+            }
+            else
+                ngroup = stack[--sp];
+        }
+    }
+    if(COUNT)
+    {
+        *node_visits += visits;
+        *tri_tests += tests;
+    }
 }
 
 } // namespace bt
