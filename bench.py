@@ -134,22 +134,21 @@ class ClockSampler:
 
 def cpu_baseline(path: str, target_s: float, threads: int = 0) -> dict:
     """Oracle (CPU restatement of the reference renderer) on a bounded sample of the frame:
-    1 spp over a contiguous pixel range sized to about target_s seconds."""
+    the whole 1080p film at as many samples per pixel as fit in about target_s seconds."""
     from oracle import scene as OS
     S = OS.Scene(path)
     S.prepare()
     pixels = S.width * S.height
     threads = threads or os.cpu_count() or 1
-    n = min(pixels, 4096)
     t0 = time.perf_counter()
-    S.render(spp=1, pixel_begin=0, pixel_end=n, threads=threads)
+    S.render(spp=1, threads=threads)
     dt = time.perf_counter() - t0
-    n2 = int(min(pixels, max(n, n * target_s / max(dt, 1e-3))))
+    spp = int(max(1, min(64, target_s / max(dt, 1e-3))))
     t0 = time.perf_counter()
-    S.render(spp=1, pixel_begin=0, pixel_end=n2, threads=threads)
+    S.render(spp=spp, sample_begin=1, threads=threads)
     dt = time.perf_counter() - t0
-    return {"value": n2 / dt / 1e6, "unit": "Mpaths/s", "cores": threads, "kind": "port",
-            "sample": f"1 spp over pixels [0, {n2}) of the 1920x1080 frame ({n2} paths, {dt:.1f} s)",
+    return {"value": spp * pixels / dt / 1e6, "unit": "Mpaths/s", "cores": threads, "kind": "port",
+            "sample": f"{spp} spp over the full 1920x1080 film ({spp * pixels} paths, {dt:.1f} s)",
             "label": "CPU restatement of Btrc's wavefront integrator (the reference itself cannot be built)"}
 
 
@@ -264,11 +263,13 @@ def run_ours(args, world, rank, local):
     node_b, tri_b = 80, 48
     trace_bytes = ext_rays * (32 + 20) + cnt["node_visits"] * node_b + cnt["tri_tests"] * tri_b
     achieved = trace_bytes / (trace_ms / 1000) / 1e9 if trace_ms > 0 else None
+    # DRAM bytes per ray from the committed ncu capture, scaled to this run's average launch
     traffic_path = ROOT / "profiles" / "trace_traffic.json"
     traffic = None
     if traffic_path.exists():
         try:
-            traffic = json.loads(traffic_path.read_text()).get("bytes_per_launch")
+            per_ray = json.loads(traffic_path.read_text()).get("dram_bytes_per_ray")
+            traffic = per_ray * ext_rays / max(trace_launches, 1) if per_ray else None
         except ValueError:
             traffic = None
 
