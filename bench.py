@@ -178,7 +178,7 @@ def run_reference(args, world, rank):
     n_step = k_spp * pixels
     value = n_step * args.steps / total / 1e6
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": "Mpaths/s", "n_gpus": 0,
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Mpaths/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "width": args.width, "height": args.height, "spp": args.spp,

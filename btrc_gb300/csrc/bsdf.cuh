@@ -655,7 +655,8 @@ struct ShaderFrame
 struct MaterialEval
 {
     int type;
-    V3 albedo;           // diffuse
+    V3 albedo;           // diffuse / mirror / glass colour
+    float glass_ior;
     MetalParams metal;
     DisneyParams disney;
 };
@@ -665,6 +666,7 @@ BT_HD MaterialEval make_material_eval(const Material &m)
     MaterialEval e;
     e.type = m.type;
     e.albedo = V3(m.p[0], m.p[1], m.p[2]);
+    e.glass_ior = m.p[3];
     if(m.type == MAT_METAL)
         e.metal = metal_params(m.p);
     else if(m.type == MAT_DISNEY)
@@ -731,6 +733,8 @@ struct SurfaceShader
             return r;
         }
         const ShaderFrame fr = frame.flip_for_black_fringes(wo);
+        if(mat.type == MAT_GLASS)
+            return glass_sample(fr, wo, s0);
         if(mat.type == MAT_MIRROR)
         {
             V3 lwo = fr.shading.global_to_local(wo);
@@ -764,9 +768,51 @@ struct SurfaceShader
         return r;
     }
 
+    // GlassShaderImpl::sample_bidir (builtin/btrc/builtin/material/glass.cpp:34-95): delta
+    // reflection with probability F, else delta refraction; the refraction branch reports
+    // pdf = 1 - F(cos of the refracted direction), as the reference does
+    BT_HD CompSample glass_sample(const ShaderFrame &fr, V3 wo, float s0) const
+    {
+        CompSample r = comp_clear();
+        const V3 color = mat.albedo;
+        const float ior = mat.glass_ior;
+        const V3 nwo = normalize(fr.shading.global_to_local(wo));
+        const float F = dielectric_fresnel(ior, 1, nwo.z);
+        if(s0 < F)
+        {
+            const V3 lwi(-nwo.x, -nwo.y, nwo.z);
+            const V3 wi = fr.shading.local_to_global(lwi);
+            if(frame.is_black_fringes(wi))
+                return r;
+            r.f = color * (F / fabsf(lwi.z)) * fr.correct_shading_energy(wi);
+            r.dir = wi;
+            r.pdf = F;
+            r.is_delta = true;
+            return r;
+        }
+        const float nz = nwo.z > 0 ? 1.0f : -1.0f;
+        const float eta = nwo.z > 0 ? 1.0f / ior : ior;
+        const float cti = fabsf(nwo.z);
+        const float s2i = fmaxf(0.0f, 1.0f - cti * cti);
+        const float s2t = eta * eta * s2i;
+        if(s2t >= 1)
+            return r;
+        const float ctt = sqrtf(1.0f - s2t);
+        const V3 nwi = normalize((eta * cti - ctt) * V3(0, 0, nz) - eta * nwo);
+        const V3 wi = fr.shading.local_to_global(nwi);
+        if(frame.is_black_fringes(wi))
+            return r;
+        const float corr = eta * eta;  // radiance transport
+        r.f = color * (corr * (1.0f - F) / fabsf(nwi.z)) * fr.correct_shading_energy(wi);
+        r.dir = wi;
+        r.pdf = 1.0f - dielectric_fresnel(ior, 1, nwi.z);
+        r.is_delta = true;
+        return r;
+    }
+
     BT_HD V3 eval(V3 wi, V3 wo) const
     {
-        if(mat.type == MAT_BLACK || mat.type == MAT_INVISIBLE || mat.type == MAT_MIRROR)
+        if(mat.type == MAT_BLACK || mat.type == MAT_INVISIBLE || mat.type == MAT_MIRROR || mat.type == MAT_GLASS)
             return V3(0);
         const ShaderFrame fr = frame.flip_for_black_fringes(wo);
         const V3 lwi = normalize(fr.shading.global_to_local(wi));
@@ -779,7 +825,7 @@ struct SurfaceShader
 
     BT_HD float pdf(V3 wi, V3 wo) const
     {
-        if(mat.type == MAT_BLACK || mat.type == MAT_INVISIBLE || mat.type == MAT_MIRROR)
+        if(mat.type == MAT_BLACK || mat.type == MAT_INVISIBLE || mat.type == MAT_MIRROR || mat.type == MAT_GLASS)
             return 0.0f;
         const ShaderFrame fr = frame.flip_for_black_fringes(wo);
         const V3 lwi = normalize(fr.shading.global_to_local(wi));

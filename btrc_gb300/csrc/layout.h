@@ -74,6 +74,7 @@ enum MaterialType : int32_t
     MAT_BLACK = 3,
     MAT_INVISIBLE = 4,
     MAT_MIRROR = 5,
+    MAT_GLASS = 6,
 };
 
 // Material parameters (constant textures only).
@@ -84,6 +85,7 @@ enum MaterialType : int32_t
 //            p[10] clearcoat, p[11] clearcoat_gloss, p[12] transmission,
 //            p[13] transmission_roughness, p[14] ior
 //   mirror : p[0..2] color
+//   glass  : p[0..2] color, p[3] ior
 struct alignas(16) Material
 {
     int32_t type;

@@ -599,6 +599,14 @@ Material make_material(const NodeP &n)
         const V3 c = tex_spectrum(n->child("color"));
         m.p[0] = c.x; m.p[1] = c.y; m.p[2] = c.z;
     }
+    else if(type == "glass")
+    {
+        // builtin/btrc/builtin/material/glass.cpp:117-129
+        m.type = MAT_GLASS;
+        const V3 c = tex_spectrum(n->child("color"));
+        m.p[0] = c.x; m.p[1] = c.y; m.p[2] = c.z;
+        m.p[3] = tex_float(n->child("ior"), 1.5f);
+    }
     else
         throw std::runtime_error("unsupported material type '" + type + "'");
     return m;

@@ -205,12 +205,25 @@ def _write_scene(path: Path, scene: dict) -> Path:
 
 # ------------------------------------------------------------------ configurations
 
+SPHERE_VARIANTS = {
+    # materials of the two spheres; None = diffuse with a seeded albedo
+    "diffuse": (None, None),
+    # a smooth-shaded glass sphere (ior 1.5, builtin/btrc/builtin/material/glass.cpp) and a
+    # tinted mirror (mirror.cpp): delta reflection + refraction, no light sampling on either
+    "glass": ({"type": "glass", "color": [0.95, 0.97, 1.0], "ior": 1.5},
+              {"type": "mirror", "color": [0.9, 0.8, 0.6]}),
+}
+
+
 def cornell(seed: int = 1000, width: int = 256, height: int = 256, spp: int = 16, sampler: str = "halton",
-            out_dir: Path | None = None, force: bool = False) -> Path:
-    """Config 0: closed unit box, two icospheres, one quad light (see module docstring)."""
+            out_dir: Path | None = None, force: bool = False, variant: str = "diffuse") -> Path:
+    """Config 0: closed unit box, two icospheres, one quad light (see module docstring).
+    `variant` picks the spheres' materials from SPHERE_VARIANTS."""
+    mats = SPHERE_VARIANTS[variant]
     out = Path(out_dir or cache_dir() / f"cornell-{seed}")
     out.mkdir(parents=True, exist_ok=True)
-    name = f"scene-{width}x{height}-{spp}-{sampler}.json"
+    tag = "" if variant == "diffuse" else f"-{variant}"
+    name = f"scene-{width}x{height}-{spp}-{sampler}{tag}.json"
     if (out / name).exists() and not force:
         return out / name
     rng = np.random.default_rng(seed)
@@ -236,7 +249,8 @@ def cornell(seed: int = 1000, width: int = 256, height: int = 256, spp: int = 16
     ents = [_entity({"type": "triangle_mesh", "filename": "${" + part + "}"}, _diffuse(albedos[k]))
             for k, part in enumerate(("box_left", "box_right", "box_rest"))]
     for k, c in enumerate(centers):
-        ents.append(_entity({"type": "triangle_mesh", "filename": "${sphere}"}, _diffuse(albedos[3 + k]),
+        ents.append(_entity({"type": "triangle_mesh", "filename": "${sphere}"},
+                            mats[k] if mats[k] is not None else _diffuse(albedos[3 + k]),
                             [{"scale": [radius] * 3}, {"translate": [float(x) for x in c]}]))
     ents.append(_entity({"type": "triangle_mesh", "filename": "${light}"}, _diffuse(albedos[5]),
                         [{"translate": [0.0, half - 0.005, 0.0]}],

@@ -1890,6 +1890,48 @@ void trace_path(const Prepared &P, uint64_t g, double *film)
                         bs.pdf = 1;
                         bs.delta = true;
                     }
+                    else if(mtype == 6)
+                    {
+                        // glass.cpp:34-95
+                        const ShadeFrame f = fr.flip(wo);
+                        const V3f col(mr[2], mr[3], mr[4]);
+                        const float ior = mr[5];
+                        const V3f nwo = nrm(f.s.g2l(wo));
+                        const float F = diel_fresnel(ior, 1.0f, nwo.z);
+                        if(u0 < F)
+                        {
+                            const V3f lwi(-nwo.x, -nwo.y, nwo.z);
+                            const V3f wi = f.s.l2g(lwi);
+                            if(!fr.black(wi))
+                            {
+                                bs.f = col * F / std::fabs(lwi.z) * f.corr(wi);
+                                bs.dir = wi;
+                                bs.pdf = F;
+                                bs.delta = true;
+                            }
+                        }
+                        else
+                        {
+                            const float nz = nwo.z > 0 ? 1.0f : -1.0f;
+                            const float eta = nwo.z > 0 ? 1.0f / ior : ior;
+                            const float cti = std::fabs(nwo.z);
+                            const float s2i = std::max(0.0f, 1.0f - cti * cti);
+                            const float s2t = eta * eta * s2i;
+                            if(s2t < 1)
+                            {
+                                const float ctt = std::sqrt(1.0f - s2t);
+                                const V3f nwi = nrm((eta * cti - ctt) * V3f(0, 0, nz) - eta * nwo);
+                                const V3f wi = f.s.l2g(nwi);
+                                if(!fr.black(wi))
+                                {
+                                    bs.f = col * (eta * eta * (1.0f - F) / std::fabs(nwi.z)) * f.corr(wi);
+                                    bs.dir = wi;
+                                    bs.pdf = 1.0f - diel_fresnel(ior, 1.0f, nwi.z);
+                                    bs.delta = true;
+                                }
+                            }
+                        }
+                    }
                     else if(mtype == 5)
                     {
                         // mirror.cpp

@@ -416,7 +416,7 @@ def _obj_records(V, N, T, F, to_unit_cube):
 
 # ------------------------------------------------------------------ full scene
 
-MAT_TYPES = {"diffuse": 0, "metal": 1, "disney": 2, "black": 3, "invisible": 4, "mirror": 5}
+MAT_TYPES = {"diffuse": 0, "metal": 1, "disney": 2, "black": 3, "invisible": 4, "mirror": 5, "glass": 6}
 
 
 def _tex_rgb(n: Node) -> np.ndarray:
@@ -440,6 +440,9 @@ def _material(n: Node) -> np.ndarray:
     p = rec[2:18]
     if t in ("diffuse", "mirror"):
         p[0:3] = _tex_rgb(n.child("color"))
+    elif t == "glass":
+        p[0:3] = _tex_rgb(n.child("color"))
+        p[3] = _tex_float(n.child("ior"), 1.5)
     elif t == "metal":
         p[0:3] = _tex_rgb(n.child("color"))
         p[3] = _tex_float(n.child("roughness"), 0)

@@ -38,6 +38,20 @@ def test_cornell_halton_gaussian(gpu_ctx, scene_dir):
     assert z < 2.0, z
 
 
+def test_cornell_glass_and_mirror(gpu_ctx, scene_dir):
+    # delta dielectric (Fresnel-chosen reflection / refraction with the eta^2 radiance
+    # factor) and a Schlick-tinted mirror; caustics through the glass make this the
+    # noisiest scene, hence more spp
+    p = scenes.cornell(out_dir=scene_dir / "cornell", width=48, height=48, spp=512, variant="glass")
+    g, o, var, stats = _render_both(gpu_ctx, p, 512)
+    assert stats["traversal_errors"] == 0
+    assert np.isfinite(g).all()
+    err = rel_mse(g, o)
+    assert err < 2e-3, err
+    z = np.mean((g - o) ** 2 / (2 * var + 1e-8))
+    assert z < 2.0, z
+
+
 def test_terrain_disney_sky(gpu_ctx, scene_dir):
     p = scenes.terrain(out_dir=scene_dir / "terrain-small", width=96, height=54, spp=128, grid=96, instances=24)
     g, o, var, stats = _render_both(gpu_ctx, p, 128)
