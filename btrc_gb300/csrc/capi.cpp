@@ -324,6 +324,24 @@ void build_scene(btrc_scene *sc, int threads)
         grids.insert(grids.end(), m.grid.begin(), m.grid.end());
         meds.push_back(md);
     }
+    std::vector<VolumePrim> vols = H.volumes;
+    {
+        const int32_t base = static_cast<int32_t>(grids.size());
+        if(grids.size() + H.volume_grids.size() > static_cast<size_t>(INT32_MAX))
+            throw std::runtime_error("density grids exceed 2^31 floats");
+        for(VolumePrim &v : vols)
+        {
+            if(v.sigma_offset >= 0)
+                v.sigma_offset += base;
+            if(v.albedo_offset >= 0)
+                v.albedo_offset += base;
+        }
+        grids.insert(grids.end(), H.volume_grids.begin(), H.volume_grids.end());
+    }
+    D.volumes = vols.empty() ? nullptr : dev_upload(sc->allocs, vols.data(), vols.size());
+    D.volume_nodes = H.volume_nodes.empty() ? nullptr
+                                             : dev_upload(sc->allocs, H.volume_nodes.data(), H.volume_nodes.size());
+    D.num_volumes = static_cast<int32_t>(vols.size());
     D.media = dev_upload(sc->allocs, meds.data(), meds.size());
     D.grids = grids.empty() ? nullptr : dev_upload(sc->allocs, grids.data(), grids.size());
     D.num_media = static_cast<int32_t>(meds.size());
@@ -335,6 +353,8 @@ void build_scene(btrc_scene *sc, int threads)
         if(H.media[inner].dev.type != MED_VACUUM || H.media[outer].dev.type != MED_VACUUM)
             D.has_media = 1;
     }
+    if(!vols.empty())
+        D.has_media = 1;
     const V3 ext = H.world_max - H.world_min;
     D.world_diagonal = length(ext);
 

@@ -30,8 +30,11 @@ struct DevScene
     const float *grids;
     int32_t num_media;
     int32_t vacuum_medium;
-    int32_t has_media;        // any non-vacuum medium referenced by an instance
+    int32_t has_media;        // any non-vacuum medium referenced by an instance, or volumes[]
     float world_diagonal;
+    const VolumePrim *volumes;
+    const VolNode *volume_nodes;
+    int32_t num_volumes;
 };
 
 struct DevRender

@@ -341,18 +341,19 @@ __device__ __forceinline__ bool russian_roulette(V3 &beta, int depth, DSampler &
 
 // ---------------------------------------------------------------- media
 
-// software trilinear lookup, normalised coordinates, clamp addressing
-__device__ __forceinline__ float grid_lookup(const float *grid, const Medium &m, V3 uvw)
+// software trilinear lookup of channel c of an nch-channel grid (x fastest), normalised
+// coordinates, clamp addressing
+__device__ __forceinline__ float grid_trilinear(const float *g, int rx, int ry, int rz, int nch, int c, V3 uvw)
 {
-    const float fx = uvw.x * m.res_x - 0.5f, fy = uvw.y * m.res_y - 0.5f, fz = uvw.z * m.res_z - 0.5f;
+    const float fx = uvw.x * rx - 0.5f, fy = uvw.y * ry - 0.5f, fz = uvw.z * rz - 0.5f;
     const float flx = floorf(fx), fly = floorf(fy), flz = floorf(fz);
     const float tx = fx - flx, ty = fy - fly, tz = fz - flz;
     const int x0 = static_cast<int>(flx), y0 = static_cast<int>(fly), z0 = static_cast<int>(flz);
-    const int xa = min(max(x0, 0), m.res_x - 1), xb = min(max(x0 + 1, 0), m.res_x - 1);
-    const int ya = min(max(y0, 0), m.res_y - 1), yb = min(max(y0 + 1, 0), m.res_y - 1);
-    const int za = min(max(z0, 0), m.res_z - 1), zb = min(max(z0 + 1, 0), m.res_z - 1);
-    const float *g = grid + m.grid_offset;
-    const size_t sx = 1, sy = static_cast<size_t>(m.res_x), sz = static_cast<size_t>(m.res_x) * m.res_y;
+    const int xa = min(max(x0, 0), rx - 1), xb = min(max(x0 + 1, 0), rx - 1);
+    const int ya = min(max(y0, 0), ry - 1), yb = min(max(y0 + 1, 0), ry - 1);
+    const int za = min(max(z0, 0), rz - 1), zb = min(max(z0 + 1, 0), rz - 1);
+    g += c;
+    const size_t sx = nch, sy = static_cast<size_t>(rx) * nch, sz = static_cast<size_t>(rx) * ry * nch;
     const float c000 = __ldg(g + za * sz + ya * sy + xa * sx), c100 = __ldg(g + za * sz + ya * sy + xb * sx);
     const float c010 = __ldg(g + za * sz + yb * sy + xa * sx), c110 = __ldg(g + za * sz + yb * sy + xb * sx);
     const float c001 = __ldg(g + zb * sz + ya * sy + xa * sx), c101 = __ldg(g + zb * sz + ya * sy + xb * sx);
@@ -363,11 +364,320 @@ __device__ __forceinline__ float grid_lookup(const float *grid, const Medium &m,
     return c0 + (c1 - c0) * tz;
 }
 
+__device__ __forceinline__ float grid_lookup(const float *grid, const Medium &m, V3 uvw)
+{
+    return grid_trilinear(grid + m.grid_offset, m.res_x, m.res_y, m.res_z, 1, 0, uvw);
+}
+
 struct MediumSample
 {
     bool scattered;
     V3 position;
+    V3 color;      // phase-function colour at the scattering point (the medium's albedo)
+    float g;       // Henyey-Greenstein asymmetry
 };
+
+// ---------------------------------------------------------------- volume primitives
+// VolumePrimitiveMedium (core/btrc/core/volume.cpp:112-197) over the volume BVH
+// (core/btrc/core/volume/bvh.cpp:127-262) and the per-overlap delta / ratio tracking of
+// volume::Aggregate (core/btrc/core/volume/aggregate.cpp:131-252). The reference selects
+// an overlap through a trie of volume-id sequences only to reach code generated per
+// overlap set; here the set itself (at most 4 ids) is carried, so no trie is needed.
+
+constexpr uint32_t MAX_VOLUME_SEGMENTS = 1u << 16;
+
+__device__ __forceinline__ V3 vrow(const float *p)
+{
+    return V3(p[0], p[1], p[2]);
+}
+
+// VolumePrimitive::world_pos_to_uvw (core/btrc/core/volume.cpp:45-52)
+__device__ __forceinline__ V3 vol_uvw(const VolumePrim &v, V3 p)
+{
+    const V3 op = p - vrow(v.o);
+    return V3(dot(op, vrow(v.x)) * v.x_inv_len2, dot(op, vrow(v.y)) * v.y_inv_len2, dot(op, vrow(v.z)) * v.z_inv_len2);
+}
+
+// BVH::is_in_prim (core/btrc/core/volume/bvh.cpp:269-278)
+__device__ __forceinline__ bool vol_contains(const VolumePrim &v, V3 p)
+{
+    const V3 op = p - vrow(v.o);
+    const float u = dot(op, vrow(v.xd)), w = dot(op, vrow(v.yd)), x = dot(op, vrow(v.zd));
+    return 0.0f <= u && u <= 1.0f && 0.0f <= w && w <= 1.0f && 0.0f <= x && x <= 1.0f;
+}
+
+__device__ __forceinline__ bool vol_node_contains(const VolNode &n, V3 p)
+{
+    return n.lower[0] <= p.x && p.x <= n.upper[0] && n.lower[1] <= p.y && p.y <= n.upper[1] && n.lower[2] <= p.z &&
+           p.z <= n.upper[2];
+}
+
+// BVH::intersect_ray_aabb (core/btrc/core/volume/bvh.cpp:287-294)
+__device__ __forceinline__ bool vol_node_hit(const VolNode &n, V3 o, V3 inv_d, float t_max)
+{
+    const float nx = inv_d.x * (n.lower[0] - o.x), fx = inv_d.x * (n.upper[0] - o.x);
+    const float ny = inv_d.y * (n.lower[1] - o.y), fy = inv_d.y * (n.upper[1] - o.y);
+    const float nz = inv_d.z * (n.lower[2] - o.z), fz = inv_d.z * (n.upper[2] - o.z);
+    const float t0 = fmaxf(fmaxf(0.0f, fminf(nx, fx)), fmaxf(fminf(ny, fy), fminf(nz, fz)));
+    const float t1 = fminf(fminf(t_max, fmaxf(nx, fx)), fminf(fmaxf(ny, fy), fmaxf(nz, fz)));
+    return t0 <= t1;
+}
+
+// BVH::find_closest_intersection for one box (core/btrc/core/volume/bvh.cpp:296-327):
+// the first boundary crossing in (0, t_max) of the segment p + t d, or -1
+__device__ __forceinline__ float vol_box_crossing(const VolumePrim &v, V3 p, V3 d, float t_max)
+{
+    const V3 op = p - vrow(v.o);
+    float t0 = 0.0f, t1 = t_max;
+    const float *axes[3] = { v.xd, v.yd, v.zd };
+#pragma unroll
+    for(int a = 0; a < 3; ++a)
+    {
+        const V3 dd2 = vrow(axes[a]);
+        const float opd = dot(op, dd2), dd = dot(d, dd2);
+        const float nd = (0.0f - opd) / dd, fd = (1.0f - opd) / dd;
+        t0 = fmaxf(t0, fminf(nd, fd));
+        t1 = fminf(t1, fmaxf(nd, fd));
+    }
+    if(t0 > t1)
+        return -1.0f;
+    if(t0 > 0)
+        return t0;
+    if(t1 < t_max)
+        return t1;
+    return -1.0f;
+}
+
+// the nearest volume-box boundary strictly inside the segment a -> b
+__device__ bool vol_next_boundary(const DevScene &S, V3 a, V3 b, V3 &out)
+{
+    const V3 dir = b - a;
+    const V3 inv(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
+    float best = MAX_FLOAT, t_max = 1.0f;
+    uint32_t stack[VOL_STACK];
+    int top = 0;
+    stack[top++] = 0;
+    while(top > 0)
+    {
+        const VolNode &n = S.volume_nodes[stack[--top]];
+        if(n.prim_beg >= 0)
+        {
+            for(int i = n.prim_beg; i < n.prim_end; ++i)
+            {
+                const float t = vol_box_crossing(S.volumes[i], a, dir, t_max);
+                if(t >= 0.0f)
+                {
+                    best = fminf(best, t);
+                    t_max = best;
+                }
+            }
+        }
+        else
+        {
+            for(int c = 0; c < 2; ++c)
+                if(top < VOL_STACK && vol_node_hit(S.volume_nodes[n.prim_end + c], a, inv, t_max))
+                    stack[top++] = static_cast<uint32_t>(n.prim_end + c);
+        }
+    }
+    if(best > 10.0f)
+        return false;
+    out = a * (1.0f - best) + b * best;
+    return true;
+}
+
+// volumes containing p (BVH::get_overlap, core/btrc/core/volume/bvh.cpp:197-262): at most
+// VOL_MAX_OVERLAP of them, by ascending id; `slot` indexes S.volumes
+struct VolOverlap
+{
+    int count;
+    int slot[VOL_MAX_OVERLAP];
+};
+
+__device__ VolOverlap vol_overlap(const DevScene &S, V3 p)
+{
+    VolOverlap r;
+    r.count = 0;
+    int ids[VOL_MAX_OVERLAP];
+    uint32_t stack[VOL_STACK];
+    int top = 0;
+    stack[top++] = 0;
+    while(top > 0)
+    {
+        const VolNode &n = S.volume_nodes[stack[--top]];
+        if(n.prim_beg >= 0)
+        {
+            for(int i = n.prim_beg; i < n.prim_end; ++i)
+            {
+                const VolumePrim &v = S.volumes[i];
+                if(!vol_contains(v, p))
+                    continue;
+                const int id = v.id;
+                if(r.count == VOL_MAX_OVERLAP && id >= ids[VOL_MAX_OVERLAP - 1])
+                    continue;
+                int j = r.count < VOL_MAX_OVERLAP ? r.count++ : VOL_MAX_OVERLAP - 1;
+                while(j > 0 && ids[j - 1] > id)
+                {
+                    ids[j] = ids[j - 1];
+                    r.slot[j] = r.slot[j - 1];
+                    --j;
+                }
+                ids[j] = id;
+                r.slot[j] = i;
+            }
+        }
+        else
+        {
+            for(int c = 0; c < 2; ++c)
+                if(top < VOL_STACK && vol_node_contains(S.volume_nodes[n.prim_end + c], p))
+                    stack[top++] = static_cast<uint32_t>(n.prim_end + c);
+        }
+    }
+    return r;
+}
+
+__device__ __forceinline__ float vol_sigma(const DevScene &S, const VolumePrim &v, V3 uvw)
+{
+    if(v.sigma_offset < 0)
+        return v.sigma_const;
+    return grid_trilinear(S.grids + v.sigma_offset, v.sres[0], v.sres[1], v.sres[2], 1, 0, uvw);
+}
+
+// Texture3D::sample_spectrum: a 1-channel array texture reads back as (v, 0, 0), the
+// missing channels of a one-component CUDA texture fetch
+__device__ __forceinline__ V3 vol_albedo(const DevScene &S, const VolumePrim &v, V3 uvw)
+{
+    if(v.albedo_offset < 0)
+        return vrow(v.albedo_const);
+    const float *g = S.grids + v.albedo_offset;
+    if(v.albedo_channels == 1)
+        return V3(grid_trilinear(g, v.ares[0], v.ares[1], v.ares[2], 1, 0, uvw), 0.0f, 0.0f);
+    return V3(grid_trilinear(g, v.ares[0], v.ares[1], v.ares[2], 3, 0, uvw),
+              grid_trilinear(g, v.ares[0], v.ares[1], v.ares[2], 3, 1, uvw),
+              grid_trilinear(g, v.ares[0], v.ares[1], v.ares[2], 3, 2, uvw));
+}
+
+__device__ __forceinline__ float overlap_inv_max(const DevScene &S, const VolOverlap &ov)
+{
+    float m = 0.0f;
+    for(int k = 0; k < ov.count; ++k)
+        m += S.volumes[ov.slot[k]].sigma_max;
+    return 1.0f / fmaxf(m, 0.01f);
+}
+
+// Aggregate::sample_scattering_in_overlap (core/btrc/core/volume/aggregate.cpp:155-219)
+__device__ bool vol_sample_overlap(const DevScene &S, const VolOverlap &ov, V3 a, V3 b, DSampler &smp, V3 &pos,
+                                   V3 &color)
+{
+    const float inv_max = overlap_inv_max(S, ov);
+    V3 ua[VOL_MAX_OVERLAP], ub[VOL_MAX_OVERLAP];
+    for(int k = 0; k < ov.count; ++k)
+    {
+        ua[k] = vol_uvw(S.volumes[ov.slot[k]], a);
+        ub[k] = vol_uvw(S.volumes[ov.slot[k]], b);
+    }
+    const float t_max = length(b - a);
+    float t = 0.0f;
+    for(uint32_t it = 0; it < MAX_TRACKING_STEPS; ++it)
+    {
+        t += -logf(1.0f - smp.get1d()) * inv_max;
+        if(t >= t_max)
+            return false;
+        const float tf = t / t_max;
+        float dens[VOL_MAX_OVERLAP];
+        V3 uvw[VOL_MAX_OVERLAP];
+        float sum = 0.0f;
+        for(int k = 0; k < ov.count; ++k)
+        {
+            uvw[k] = ua[k] * (1.0f - tf) + ub[k] * tf;
+            dens[k] = vol_sigma(S, S.volumes[ov.slot[k]], uvw[k]);
+            sum += dens[k];
+        }
+        if(smp.get1d() < sum * inv_max)
+        {
+            pos = a * (1.0f - tf) + b * tf;
+            V3 alb(0.0f);
+            for(int k = 0; k < ov.count; ++k)
+                alb = alb + (dens[k] / sum) * vol_albedo(S, S.volumes[ov.slot[k]], uvw[k]);
+            color = alb;
+            return true;
+        }
+    }
+    return false;
+}
+
+// Aggregate::tr_in_overlap (core/btrc/core/volume/aggregate.cpp:221-252)
+__device__ float vol_tr_overlap(const DevScene &S, const VolOverlap &ov, V3 a, V3 b, DSampler &smp)
+{
+    const float inv_max = overlap_inv_max(S, ov);
+    V3 ua[VOL_MAX_OVERLAP], ub[VOL_MAX_OVERLAP];
+    for(int k = 0; k < ov.count; ++k)
+    {
+        ua[k] = vol_uvw(S.volumes[ov.slot[k]], a);
+        ub[k] = vol_uvw(S.volumes[ov.slot[k]], b);
+    }
+    const float t_max = length(b - a);
+    float result = 1.0f, t = 0.0f;
+    for(uint32_t it = 0; it < MAX_TRACKING_STEPS; ++it)
+    {
+        t += -logf(1.0f - smp.get1d()) * inv_max;
+        if(t >= t_max)
+            break;
+        const float tf = t / t_max;
+        float sum = 0.0f;
+        for(int k = 0; k < ov.count; ++k)
+            sum += vol_sigma(S, S.volumes[ov.slot[k]], ua[k] * (1.0f - tf) + ub[k] * tf);
+        result *= 1.0f - sum * inv_max;
+    }
+    return result;
+}
+
+// VolumePrimitiveMedium::sample (core/btrc/core/volume.cpp:112-160): walk the segment
+// from one box boundary to the next, tracking inside each overlap region; g = 0
+__device__ __noinline__ MediumSample volumes_sample(const DevScene &S, V3 a, V3 b, DSampler &smp)
+{
+    MediumSample r;
+    r.scattered = false;
+    r.g = 0.0f;
+    V3 o = a;
+    const V3 d = normalize(b - a);
+    for(uint32_t seg = 0; seg < MAX_VOLUME_SEGMENTS; ++seg)
+    {
+        if(dot(b - o, d) <= 0.0f || length_square(b - o) < 0.00001f)
+            break;
+        V3 inct;
+        if(!vol_next_boundary(S, o, b, inct))
+            inct = b;
+        const VolOverlap ov = vol_overlap(S, 0.5f * (o + inct));
+        if(ov.count != 0 && vol_sample_overlap(S, ov, o, inct, smp, r.position, r.color))
+        {
+            r.scattered = true;
+            break;
+        }
+        o = inct + 0.001f * d;
+    }
+    return r;
+}
+
+// VolumePrimitiveMedium::tr (core/btrc/core/volume.cpp:162-197)
+__device__ __noinline__ float volumes_tr(const DevScene &S, V3 a, V3 b, DSampler &smp)
+{
+    float result = 1.0f;
+    V3 o = a;
+    const V3 d = normalize(b - a);
+    for(uint32_t seg = 0; seg < MAX_VOLUME_SEGMENTS; ++seg)
+    {
+        if(dot(b - o, d) <= 0.0f || length_square(b - o) < 0.0001f)
+            break;
+        V3 inct;
+        if(!vol_next_boundary(S, o, b, inct))
+            inct = b;
+        const VolOverlap ov = vol_overlap(S, 0.5f * (o + inct));
+        if(ov.count != 0)
+            result *= vol_tr_overlap(S, ov, o, inct, smp);
+        o = inct + 0.001f * d;
+    }
+    return result;
+}
 
 // HetergeneousMedium::sample (builtin/btrc/builtin/medium/hetergeneous.cpp:25-73) and the
 // homogeneous variant; TransformMedium maps a, b to the medium's local frame first
@@ -378,6 +688,10 @@ __device__ MediumSample medium_sample(const DevScene &S, const Medium &m, V3 a, 
     r.scattered = false;
     if(m.type == MED_VACUUM)
         return r;
+    if(m.type == MED_VOLUMES)
+        return volumes_sample(S, a, b, smp);
+    r.color = V3(m.albedo[0], m.albedo[1], m.albedo[2]);
+    r.g = m.g;
     const float t_max = length(b - a);
     if(m.type == MED_HOMOGENEOUS)
     {
@@ -417,6 +731,8 @@ __device__ V3 medium_tr(const DevScene &S, const Medium &m, V3 a, V3 b, DSampler
 {
     if(m.type == MED_VACUUM)
         return V3(1.0f);
+    if(m.type == MED_VOLUMES)
+        return V3(volumes_tr(S, a, b, smp));
     const float t_max = length(b - a);
     if(m.type == MED_HOMOGENEOUS)
     {
@@ -632,20 +948,20 @@ __global__ void __launch_bounds__(BLOCK) k_medium(DevScene S, DevRender R, PathS
             splat(film, pixel, R.width, path_rad);
             continue;
         }
-        const V3 albedo(m.albedo[0], m.albedo[1], m.albedo[2]);
+        const V3 albedo = ms.color;
         LightSample ls = sample_light(S, ms.position, V3(0, 0, 1), false, smp);
         if(ls.success)
         {
             // HG eval/pdf with u = -cos(wi, wo)
             const V3 wo = -d;
             const float u = -dot(normalize(ls.d), normalize(wo));
-            const float ph = henyey_greenstein(m.g, u);
+            const float ph = henyey_greenstein(ms.g, u);
             ls.li = ls.li * beta * (albedo * ph) / (ph + ls.light_pdf);
         }
         // HenyeyGreensteinPhaseShader::sample (core/btrc/core/medium.cpp:32-64)
         float s0, s1, s2;
         smp.get3d(s0, s1, s2);
-        const float g = m.g;
+        const float g = ms.g;
         const float s = s0 + s0 - 1;
         float u;
         if(fabsf(g) < 0.001f)
@@ -811,6 +1127,9 @@ __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, DevRender R, PathSo
 
 // ShadowPipeline (builtin/btrc/builtin/renderer/wavefront/shadow.cpp:24-76): occlusion by
 // the warp-refill traversal; unoccluded records splat (times the medium transmittance)
+// MEDIA = false compiles the transmittance code out, so the traversal of scenes without
+// media keeps its registers
+template<bool MEDIA>
 __global__ void __launch_bounds__(128) k_shadow(DevScene S, DevRender R, ShadowSoA SH, float4 *film, Counters *cnt)
 {
     const uint32_t n = cnt->shadow;
@@ -828,7 +1147,7 @@ __global__ void __launch_bounds__(128) k_shadow(DevScene S, DevRender R, ShadowS
                 return;
             const F4 o = SH.o[i], d = SH.d[i], b = SH.beta[i];
             V3 beta = v3(b);
-            if(S.has_media)
+            if(MEDIA)
             {
                 DSampler smp;
                 smp.type = SAMPLER_INDEPENDENT;
@@ -933,7 +1252,12 @@ cudaError_t enqueue_bounce(const DevScene &S, const DevRender &R, RenderBuffers 
         k_shade<<<grids[3], BLOCK, 0, st>>>(S, R, P, N, B.shadow, B.hit_flag, B.hit_detail, B.film, B.counters);
     });
     timed(T, STAGE_SHADOW, st, launches,
-          [&] { k_shadow<<<grids[4], 128, 0, st>>>(S, R, B.shadow, B.film, B.counters); });
+          [&] {
+              if(S.has_media)
+                  k_shadow<true><<<grids[4], 128, 0, st>>>(S, R, B.shadow, B.film, B.counters);
+              else
+                  k_shadow<false><<<grids[4], 128, 0, st>>>(S, R, B.shadow, B.film, B.counters);
+          });
     return cudaGetLastError();
 }
 
@@ -986,7 +1310,8 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
         persistent_grid(128, reinterpret_cast<const void *>(k_trace<false>)),
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_medium)),
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_shade)),
-        persistent_grid(128, reinterpret_cast<const void *>(k_shadow)),
+        persistent_grid(128, S.has_media ? reinterpret_cast<const void *>(k_shadow<true>)
+                                         : reinterpret_cast<const void *>(k_shadow<false>)),
     };
 
     cudaGraphExec_t exec = nullptr;
@@ -1221,7 +1546,8 @@ cudaError_t render_wavefront_noalloc(const DevScene &S, const DevRender &R, void
         persistent_grid(128, reinterpret_cast<const void *>(k_trace<false>)),
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_medium)),
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_shade)),
-        persistent_grid(128, reinterpret_cast<const void *>(k_shadow)),
+        persistent_grid(128, S.has_media ? reinterpret_cast<const void *>(k_shadow<true>)
+                                         : reinterpret_cast<const void *>(k_shadow<false>)),
     };
     const uint64_t depth_bound = static_cast<uint64_t>(std::max(R.max_depth, R.min_depth)) + 2;
     const uint64_t max_launches = ((R.total_paths + cap - 1) / cap + 2) * depth_bound + 64;

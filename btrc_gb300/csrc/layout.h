@@ -148,6 +148,7 @@ enum MediumType : int32_t
     MED_VACUUM = 0,
     MED_HOMOGENEOUS = 1,
     MED_HETEROGENEOUS = 2,
+    MED_VOLUMES = 3,      // the volume-primitive medium when the scene has volumes[]
 };
 
 // Participating medium. Heterogeneous media are a density grid behind a transform
@@ -165,6 +166,46 @@ struct alignas(16) Medium
     float w2l[12];           // world -> medium local ([-1,1]^3) transform
     float l2w[12];
 };
+
+// Volume primitive (core/btrc/core/volume.h:9-49): the parallelepiped o + [0,1]^3 (x y z)
+// with a sigma_t and an albedo 3D texture over its uvw. Stored in volume-BVH leaf order;
+// `id` is its position in the scene's volumes[] array.
+struct alignas(16) VolumePrim
+{
+    float o[3];
+    int32_t id;
+    float x[3];
+    float x_inv_len2;        // world_pos_to_uvw: dot(p - o, x) * (1 / |x|^2) (volume.cpp:45-52)
+    float y[3];
+    float y_inv_len2;
+    float z[3];
+    float z_inv_len2;
+    float xd[3];             // x / |x|^2: containment and slab tests (volume/bvh.cpp:77-84)
+    float sigma_const;       // sigma_t when sigma_offset < 0
+    float yd[3];
+    float sigma_max;         // Texture3D::get_max_float of sigma_t
+    float zd[3];
+    int32_t sigma_offset;    // float index of the sigma_t grid in the grid pool, -1: constant
+    int32_t sres[3];
+    int32_t albedo_offset;   // float index of the albedo grid (3 floats per texel), -1: constant
+    int32_t ares[3];
+    int32_t albedo_channels; // texels of a 1-channel albedo array read as (v, 0, 0)
+    float albedo_const[3];
+    float pad;
+};
+
+// Binary BVH node over volume boxes: a leaf holds prims [prim_beg, prim_end), an
+// interior node has prim_beg = -1 and its children at prim_end and prim_end + 1.
+struct alignas(16) VolNode
+{
+    float lower[3];
+    int32_t prim_beg;
+    float upper[3];
+    int32_t prim_end;
+};
+
+constexpr int VOL_MAX_OVERLAP = 4;   // volume/bvh.h:10
+constexpr int VOL_STACK = 64;
 
 enum SamplerType : int32_t
 {

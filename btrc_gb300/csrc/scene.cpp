@@ -615,26 +615,33 @@ Material make_material(const NodeP &n)
 struct GridData
 {
     int w = 1, h = 1, d = 1;
-    std::vector<float> v;
-    float constant = 0;
+    int ch = 1;               // channels kept in v: 1, or 3 (rgb of a 3- or 4-channel array)
+    std::vector<float> v;     // x fastest, channels interleaved
+    V3 rgb = V3(0);           // the value of a constant texture
+    float constant = 0;       // rgb.x
     bool is_constant = true;
 };
 
-// Texture3D: constant value / array of 1 or 3, {"type":"constant","value":...} or
-// {"type":"array","text":file} (common/btrc/utils/cuda/array.cpp:313-384, channel 0 only),
-// plus {"type":"array","binary":file}: raw header "BTG1" int32 w h d then float32 x-fastest.
-GridData load_texture3d(const NodeP &n, const std::string &scene_dir)
+// Texture3D: constant value / spectrum, {"type":"constant","value":...} or
+// {"type":"array","text":file} (common/btrc/utils/cuda/array.cpp:313-384), plus
+// {"type":"array","binary":file}: raw header "BTG1" int32 w h d then float32 x-fastest.
+// Text arrays keep channel 0 unless keep_rgb; "byte" components are read as one
+// character each and mapped as signed 8-bit normalised values, as the reference's
+// `uint8_t comp; fin >> comp` + SNorm8 texture format do.
+GridData load_texture3d(const NodeP &n, const std::string &scene_dir, bool keep_rgb = false)
 {
     GridData g;
     if(n->is_value() || n->is_array())
     {
-        g.constant = json::as_spectrum(n).x;
+        g.rgb = json::as_spectrum(n);
+        g.constant = g.rgb.x;
         return g;
     }
     const std::string type = json::as_string(n->child("type"));
     if(type == "constant")
     {
-        g.constant = json::as_spectrum(n->child("value")).x;
+        g.rgb = json::as_spectrum(n->child("value"));
+        g.constant = g.rgb.x;
         return g;
     }
     if(type != "array")
@@ -666,31 +673,192 @@ GridData load_texture3d(const NodeP &n, const std::string &scene_dir)
     std::string comp;
     int ch;
     f >> comp >> ch >> g.w >> g.h >> g.d;
-    if(!f || (ch != 1 && ch != 3 && ch != 4) || g.w <= 0 || g.h <= 0 || g.d <= 0)
+    if(!f || g.w <= 0 || g.h <= 0 || g.d <= 0)
         throw std::runtime_error("Array::load_from_text: failed to parse file head");
-    g.v.resize(static_cast<size_t>(g.w) * g.h * g.d);
-    for(size_t i = 0; i < g.v.size(); ++i)
+    if(ch != 1 && ch != 3 && ch != 4)
+        throw std::runtime_error("unsupported channel count: " + std::to_string(ch));
+    if(comp != "float" && comp != "byte")
+        throw std::runtime_error("unknown component type: " + comp);
+    g.ch = keep_rgb && ch > 1 ? 3 : 1;
+    const size_t texels = static_cast<size_t>(g.w) * g.h * g.d;
+    g.v.resize(texels * g.ch);
+    for(size_t i = 0; i < texels; ++i)
     {
         for(int c = 0; c < ch; ++c)
         {
             float val;
             if(comp == "float")
                 f >> val;
-            else if(comp == "byte")
-            {
-                int b;
-                f >> b;
-                val = static_cast<float>(b) / 127.0f;
-            }
             else
-                throw std::runtime_error("unknown component type: " + comp);
-            if(c == 0)
-                g.v[i] = val;
+            {
+                char cc;
+                f >> cc;
+                const int u = static_cast<int>(static_cast<unsigned char>(cc));
+                const int sv = u >= 128 ? u - 256 : u;
+                val = std::max(static_cast<float>(sv) / 127.0f, -1.0f);
+            }
+            if(c < g.ch)
+                g.v[i * g.ch + c] = val;
         }
     }
     if(!f)
         throw std::runtime_error("failed to load " + fn);
     return g;
+}
+
+// VolumePrimitive::get_bounding_box (core/btrc/core/volume.cpp:54-68): the box of o and
+// o + x, o + y, o + z, as the reference computes it
+V3 volume_box_lower(const VolumePrim &v)
+{
+    const V3 o(v.o[0], v.o[1], v.o[2]), x(v.x[0], v.x[1], v.x[2]), y(v.y[0], v.y[1], v.y[2]),
+        z(v.z[0], v.z[1], v.z[2]);
+    return vmin(vmin(o, o + x), vmin(o + y, o + z));
+}
+
+V3 volume_box_upper(const VolumePrim &v)
+{
+    const V3 o(v.o[0], v.o[1], v.o[2]), x(v.x[0], v.x[1], v.x[2]), y(v.y[0], v.y[1], v.y[2]),
+        z(v.z[0], v.z[1], v.z[2]);
+    return vmax(vmax(o, o + x), vmax(o + y, o + z));
+}
+
+// all eight corners: the box the volume BVH is built over. The reference builds its BVH
+// over the four-point box above, which for a sheared volume leaves parts of it outside its
+// node bounds; bounding all corners makes the overlap set exactly the volumes containing
+// the point (the two boxes agree for axis-aligned volumes)
+void volume_corner_box(const VolumePrim &v, V3 &lo, V3 &hi)
+{
+    const V3 o(v.o[0], v.o[1], v.o[2]), x(v.x[0], v.x[1], v.x[2]), y(v.y[0], v.y[1], v.y[2]),
+        z(v.z[0], v.z[1], v.z[2]);
+    lo = V3(MAX_FLOAT);
+    hi = V3(-MAX_FLOAT);
+    for(int c = 0; c < 8; ++c)
+    {
+        const V3 p = o + ((c & 1) ? x : V3(0)) + ((c & 2) ? y : V3(0)) + ((c & 4) ? z : V3(0));
+        lo = vmin(lo, p);
+        hi = vmax(hi, p);
+    }
+}
+
+VolumePrim make_volume(const NodeP &n, int id, const std::string &scene_dir, std::vector<float> &pool)
+{
+    VolumePrim v{};
+    v.id = id;
+    const V3 o = json::as_vec3(n->child("o")), x = json::as_vec3(n->child("x")), y = json::as_vec3(n->child("y")),
+             z = json::as_vec3(n->child("z"));
+    const V3 *axes[3] = { &x, &y, &z };
+    float *dst[3] = { v.x, v.y, v.z };
+    float *dstd[3] = { v.xd, v.yd, v.zd };
+    float *inv[3] = { &v.x_inv_len2, &v.y_inv_len2, &v.z_inv_len2 };
+    v.o[0] = o.x; v.o[1] = o.y; v.o[2] = o.z;
+    for(int a = 0; a < 3; ++a)
+    {
+        const V3 e = *axes[a];
+        const float l2 = length_square(e);
+        if(!(l2 > 0))
+            throw std::runtime_error("degenerate volume axis");
+        dst[a][0] = e.x; dst[a][1] = e.y; dst[a][2] = e.z;
+        *inv[a] = 1.0f / l2;
+        const V3 ed = e / l2;
+        dstd[a][0] = ed.x; dstd[a][1] = ed.y; dstd[a][2] = ed.z;
+    }
+    GridData sig = load_texture3d(n->child("sigma_t"), scene_dir);
+    if(sig.is_constant)
+    {
+        v.sigma_offset = -1;
+        v.sigma_const = sig.constant;
+        v.sigma_max = sig.constant;
+        v.sres[0] = v.sres[1] = v.sres[2] = 1;
+    }
+    else
+    {
+        v.sigma_offset = static_cast<int32_t>(pool.size());
+        v.sres[0] = sig.w; v.sres[1] = sig.h; v.sres[2] = sig.d;
+        float mx = -MAX_FLOAT;
+        for(float s : sig.v)
+            mx = std::max(mx, s);
+        v.sigma_max = mx;
+        pool.insert(pool.end(), sig.v.begin(), sig.v.end());
+    }
+    GridData alb = load_texture3d(n->child("albedo"), scene_dir, true);
+    if(alb.is_constant)
+    {
+        v.albedo_offset = -1;
+        v.albedo_const[0] = alb.rgb.x; v.albedo_const[1] = alb.rgb.y; v.albedo_const[2] = alb.rgb.z;
+        v.ares[0] = v.ares[1] = v.ares[2] = 1;
+        v.albedo_channels = 3;
+    }
+    else
+    {
+        v.albedo_offset = static_cast<int32_t>(pool.size());
+        v.ares[0] = alb.w; v.ares[1] = alb.h; v.ares[2] = alb.d;
+        v.albedo_channels = alb.ch;
+        pool.insert(pool.end(), alb.v.begin(), alb.v.end());
+    }
+    if(pool.size() > static_cast<size_t>(INT32_MAX))
+        throw std::runtime_error("volume grids exceed 2^31 floats");
+    return v;
+}
+
+// Binary BVH over the volume boxes: object-median splits on the widest centroid axis,
+// leaves of at most 4 boxes, children of a node stored next to each other. The depth
+// stays below log2(n) + 1, far inside the traversal stack (VOL_STACK).
+void build_volume_bvh(const std::vector<VolumePrim> &in, std::vector<VolumePrim> &out, std::vector<VolNode> &nodes)
+{
+    out.clear();
+    nodes.clear();
+    if(in.empty())
+        return;
+    std::vector<V3> lo(in.size()), hi(in.size()), c(in.size());
+    for(size_t i = 0; i < in.size(); ++i)
+    {
+        volume_corner_box(in[i], lo[i], hi[i]);
+        c[i] = 0.5f * (lo[i] + hi[i]);
+    }
+    std::vector<int> idx(in.size());
+    std::iota(idx.begin(), idx.end(), 0);
+    nodes.emplace_back();
+    struct Task { int node, b, e; };
+    std::vector<Task> todo{ { 0, 0, static_cast<int>(in.size()) } };
+    while(!todo.empty())
+    {
+        const Task t = todo.back();
+        todo.pop_back();
+        V3 bl(MAX_FLOAT), bh(-MAX_FLOAT), cl(MAX_FLOAT), ch(-MAX_FLOAT);
+        for(int i = t.b; i < t.e; ++i)
+        {
+            bl = vmin(bl, lo[idx[i]]);
+            bh = vmax(bh, hi[idx[i]]);
+            cl = vmin(cl, c[idx[i]]);
+            ch = vmax(ch, c[idx[i]]);
+        }
+        VolNode &nd = nodes[t.node];
+        nd.lower[0] = bl.x; nd.lower[1] = bl.y; nd.lower[2] = bl.z;
+        nd.upper[0] = bh.x; nd.upper[1] = bh.y; nd.upper[2] = bh.z;
+        if(t.e - t.b <= 4)
+        {
+            nd.prim_beg = static_cast<int32_t>(out.size());
+            for(int i = t.b; i < t.e; ++i)
+                out.push_back(in[idx[i]]);
+            nd.prim_end = static_cast<int32_t>(out.size());
+            continue;
+        }
+        const V3 ext = ch - cl;
+        const int axis = ext.x >= ext.y && ext.x >= ext.z ? 0 : (ext.y >= ext.z ? 1 : 2);
+        const int mid = (t.b + t.e) / 2;
+        std::nth_element(idx.begin() + t.b, idx.begin() + mid, idx.begin() + t.e, [&](int a, int b) {
+            const float ca = axis == 0 ? c[a].x : (axis == 1 ? c[a].y : c[a].z);
+            const float cb = axis == 0 ? c[b].x : (axis == 1 ? c[b].y : c[b].z);
+            return ca < cb || (ca == cb && a < b);
+        });
+        const int left = static_cast<int>(nodes.size());
+        nd.prim_beg = -1;
+        nd.prim_end = left;
+        nodes.emplace_back();
+        nodes.emplace_back();
+        todo.push_back({ left + 1, mid, t.e });
+        todo.push_back({ left, t.b, mid });
+    }
 }
 
 struct MediumBuilder
@@ -748,12 +916,10 @@ struct MediumBuilder
         {
             m.dev.type = MED_HETEROGENEOUS;
             GridData sig = load_texture3d(n->child("sigma_t"), scene_dir);
-            GridData alb = load_texture3d(n->child("albedo"), scene_dir);
+            GridData alb = load_texture3d(n->child("albedo"), scene_dir, true);
             if(!alb.is_constant)
                 throw std::runtime_error("only constant medium albedo is supported");
-            const V3 a = n->child("albedo")->is_group() && n->child("albedo")->find("value")
-                             ? json::as_spectrum(n->child("albedo")->child("value"))
-                             : (n->child("albedo")->is_group() ? V3(alb.constant) : json::as_spectrum(n->child("albedo")));
+            const V3 a = alb.rgb;
             m.dev.albedo[0] = a.x; m.dev.albedo[1] = a.y; m.dev.albedo[2] = a.z;
             if(auto gn = n->find("g"))
             {
@@ -908,10 +1074,13 @@ HostScene load_scene(const std::string &path)
     }
     if(auto vols = scene->find("volumes"))
     {
+        // factory/btrc/factory/scene.cpp:57-79
         if(!vols->is_array())
             throw std::runtime_error("'volumes' is not an array node");
-        if(!vols->elems.empty())
-            throw std::runtime_error("volume primitives are not supported yet");
+        std::vector<VolumePrim> prims;
+        for(size_t i = 0; i < vols->elems.size(); ++i)
+            prims.push_back(make_volume(vols->elems[i], static_cast<int>(i), scene_dir, S.volume_grids));
+        build_volume_bvh(prims, S.volumes, S.volume_nodes);
     }
     if(auto en = scene->find("envir_light"))
     {
@@ -943,7 +1112,7 @@ HostScene load_scene(const std::string &path)
             S.media.push_back(std::move(mb.media[order[i]]));
         }
         HostMedium vac{};
-        vac.dev.type = MED_VACUUM;
+        vac.dev.type = S.volumes.empty() ? MED_VACUUM : MED_VOLUMES;
         vac.dev.priority = -(1 << 30);
         S.media.push_back(vac);
         S.vacuum_medium = static_cast<int>(S.media.size()) - 1;
@@ -996,6 +1165,13 @@ HostScene load_scene(const std::string &path)
             S.world_min = vmin(S.world_min, w);
             S.world_max = vmax(S.world_max, w);
         }
+    }
+    // volume boxes join the world bounds (core/btrc/core/scene.cpp:233-237)
+    for(const VolumePrim &v : S.volumes)
+    {
+        const V3 lo = volume_box_lower(v), hi = volume_box_upper(v);
+        S.world_min = vmin(S.world_min, lo);
+        S.world_max = vmax(S.world_max, hi);
     }
     if(S.world_min.x > S.world_max.x)
     {

@@ -92,6 +92,9 @@ struct HostScene
     EnvLight env{};
     std::vector<HostMedium> media;   // index 0 .. n-1; vacuum (volume-primitive medium) included
     int vacuum_medium = 0;
+    std::vector<VolumePrim> volumes; // volumes[] in volume-BVH leaf order
+    std::vector<VolNode> volume_nodes;
+    std::vector<float> volume_grids; // VolumePrim grid offsets index this pool
     Camera camera{};
     RenderParams params;
     V3 world_min, world_max;

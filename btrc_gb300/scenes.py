@@ -212,7 +212,30 @@ SPHERE_VARIANTS = {
     # tinted mirror (mirror.cpp): delta reflection + refraction, no light sampling on either
     "glass": ({"type": "glass", "color": [0.95, 0.97, 1.0], "ior": 1.5},
               {"type": "mirror", "color": [0.9, 0.8, 0.6]}),
+    # diffuse spheres inside three overlapping volume primitives (volumes[])
+    "fog": (None, None),
 }
+
+
+def _fog_volumes(out: Path, rng: np.random.Generator) -> list[dict]:
+    """Three overlapping volume primitives (core/btrc/core/volume.h): an axis-aligned box of
+    constant density, a sheared box with an 8^3 density grid and a coloured box whose albedo
+    is a 4^3 RGB grid (text array files, common/btrc/utils/cuda/array.cpp:313-384)."""
+    sig = rng.uniform(0.0, 4.0, (8, 8, 8)).astype(np.float32)
+    write_grid_text(out / "fog_sigma.txt", sig)
+    alb = rng.uniform(0.2, 0.95, (4, 4, 4, 3)).astype(np.float32)
+    lines = ["float 3 4 4 4"] + [" ".join(f"{v:.6f}" for v in t) for t in alb.reshape(-1, 3)]
+    (out / "fog_albedo.txt").write_text("\n".join(lines) + "\n")
+    return [
+        {"o": [-0.45, -0.45, 0.25], "x": [0.55, 0.0, 0.0], "y": [0.0, 0.5, 0.0], "z": [0.0, 0.0, 0.6],
+         "sigma_t": 2.0, "albedo": 0.8},
+        {"o": [-0.15, -0.35, 0.4], "x": [0.45, 0.12, 0.0], "y": [-0.1, 0.45, 0.05], "z": [0.0, 0.0, 0.5],
+         "sigma_t": {"type": "array", "text": "$env{scene_directory}/fog_sigma.txt"},
+         "albedo": [0.9, 0.5, 0.3]},
+        {"o": [-0.3, 0.0, 0.3], "x": [0.6, 0.0, 0.0], "y": [0.0, 0.35, 0.0], "z": [0.0, 0.0, 0.4],
+         "sigma_t": 1.0,
+         "albedo": {"type": "array", "text": "$env{scene_directory}/fog_albedo.txt"}},
+    ]
 
 
 def cornell(seed: int = 1000, width: int = 256, height: int = 256, spp: int = 16, sampler: str = "halton",
@@ -264,6 +287,8 @@ def cornell(seed: int = 1000, width: int = 256, height: int = 256, spp: int = 16
                      "filter": {"type": "gaussian", "radius": 1.5, "alpha": 1.6}},
         "scene": {"entities": ents},
     }
+    if variant == "fog":
+        scene["scene"]["volumes"] = _fog_volumes(out, rng)
     text = json.dumps(scene, indent=1)
     for key, fn in (("${box_left}", "box_left.obj"), ("${box_right}", "box_right.obj"),
                     ("${box_rest}", "box_rest.obj"), ("${sphere}", "sphere3.obj"), ("${light}", "light.obj")):

@@ -36,6 +36,7 @@ class OracleScene(C.Structure):
         ("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("min_depth", C.c_int32),
         ("max_depth", C.c_int32), ("rr_threshold", C.c_float), ("rr_cont_prob", C.c_float),
         ("sampler", C.c_int32), ("filter", C.c_int32), ("filter_radius", C.c_float), ("filter_alpha", C.c_float),
+        ("nvol", C.c_int32), ("vol", _vp), ("vol_off", _vp),
     ]
 
 
@@ -57,6 +58,7 @@ def lib() -> C.CDLL:
         L.oracle_bsdf_batch_f32.argtypes = [C.c_int, _vp, _vp, _vp, C.c_uint64, _vp]
         L.oracle_prepare.restype = _vp
         L.oracle_prepare.argtypes = [C.POINTER(OracleScene)]
+        L.oracle_medium_tr_batch.argtypes = [C.POINTER(OracleScene), C.c_int, _vp, _vp, C.c_uint64, _vp]
         L.oracle_release.argtypes = [_vp]
         L.oracle_render.argtypes = [_vp, C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, _vp, C.c_int]
         _lib = L

@@ -1345,6 +1345,10 @@ struct OracleScene
     float rr_threshold, rr_cont_prob;
     int32_t sampler, filter;
     float filter_radius, filter_alpha;
+
+    int32_t nvol;           // volumes[] in file order
+    const float *vol;       // 32 floats per volume (layout at volume() below)
+    const uint64_t *vol_off; // 2 per volume: sigma_t grid, albedo grid offsets into grids
 };
 
 namespace {
@@ -1478,11 +1482,283 @@ float grid_at(const OracleScene &S, const Med &m, V3f uvw)
     return c0 + (c1 - c0) * tz;
 }
 
+// ---- volume primitives: VolumePrimitiveMedium (core/btrc/core/volume.cpp:112-197),
+// volume::BVH queries (core/btrc/core/volume/bvh.cpp:127-327) answered by brute force over
+// all boxes (the nearest crossing and the containing set do not depend on the tree), and
+// volume::Aggregate tracking (core/btrc/core/volume/aggregate.cpp:131-252).
+// volume record: [0..2] o, [3..5] x, [6..8] y, [9..11] z, [12] constant sigma_t,
+// [13] max sigma_t, [14..16] sigma grid res, [17..19] albedo grid res, [20] albedo
+// channels (1 or 3), [21..23] constant albedo, [24] sigma is a grid, [25] albedo is a grid
+struct Vol
+{
+    V3f o, x, y, z, xd, yd, zd;
+    float xi, yi, zi;
+    float sigma_const, sigma_max;
+    int sres[3], ares[3], ach;
+    V3f albedo_const;
+    bool sgrid, agrid;
+    uint64_t soff, aoff;
+};
+
+Vol volume(const OracleScene &S, int k)
+{
+    const float *r = S.vol + k * 32;
+    Vol v;
+    v.o = V3f(r[0], r[1], r[2]);
+    v.x = V3f(r[3], r[4], r[5]);
+    v.y = V3f(r[6], r[7], r[8]);
+    v.z = V3f(r[9], r[10], r[11]);
+    v.xi = 1.0f / dot(v.x, v.x);
+    v.yi = 1.0f / dot(v.y, v.y);
+    v.zi = 1.0f / dot(v.z, v.z);
+    v.xd = v.x / dot(v.x, v.x);
+    v.yd = v.y / dot(v.y, v.y);
+    v.zd = v.z / dot(v.z, v.z);
+    v.sigma_const = r[12];
+    v.sigma_max = r[13];
+    for(int i = 0; i < 3; ++i)
+    {
+        v.sres[i] = static_cast<int>(r[14 + i]);
+        v.ares[i] = static_cast<int>(r[17 + i]);
+    }
+    v.ach = static_cast<int>(r[20]);
+    v.albedo_const = V3f(r[21], r[22], r[23]);
+    v.sgrid = r[24] != 0;
+    v.agrid = r[25] != 0;
+    v.soff = S.vol_off[k * 2];
+    v.aoff = S.vol_off[k * 2 + 1];
+    return v;
+}
+
+float grid_tri(const float *g, int rx, int ry, int rz, int nch, int c, V3f uvw)
+{
+    const float fx = uvw.x * rx - 0.5f, fy = uvw.y * ry - 0.5f, fz = uvw.z * rz - 0.5f;
+    const float flx = std::floor(fx), fly = std::floor(fy), flz = std::floor(fz);
+    const float tx = fx - flx, ty = fy - fly, tz = fz - flz;
+    auto cl = [](int v, int n) { return std::min(std::max(v, 0), n - 1); };
+    const int x0 = cl(int(flx), rx), x1 = cl(int(flx) + 1, rx);
+    const int y0 = cl(int(fly), ry), y1 = cl(int(fly) + 1, ry);
+    const int z0 = cl(int(flz), rz), z1 = cl(int(flz) + 1, rz);
+    auto at = [&](int x, int y, int z) { return g[((static_cast<size_t>(z) * ry + y) * rx + x) * nch + c]; };
+    const float c00 = at(x0, y0, z0) + (at(x1, y0, z0) - at(x0, y0, z0)) * tx;
+    const float c10 = at(x0, y1, z0) + (at(x1, y1, z0) - at(x0, y1, z0)) * tx;
+    const float c01 = at(x0, y0, z1) + (at(x1, y0, z1) - at(x0, y0, z1)) * tx;
+    const float c11 = at(x0, y1, z1) + (at(x1, y1, z1) - at(x0, y1, z1)) * tx;
+    const float c0 = c00 + (c10 - c00) * ty, c1 = c01 + (c11 - c01) * ty;
+    return c0 + (c1 - c0) * tz;
+}
+
+V3f vol_uvw(const Vol &v, V3f p)
+{
+    const V3f op = p - v.o;
+    return V3f(dot(op, v.x) * v.xi, dot(op, v.y) * v.yi, dot(op, v.z) * v.zi);
+}
+
+float vol_sigma(const OracleScene &S, const Vol &v, V3f uvw)
+{
+    if(!v.sgrid)
+        return v.sigma_const;
+    return grid_tri(S.grids + v.soff, v.sres[0], v.sres[1], v.sres[2], 1, 0, uvw);
+}
+
+// a one-channel array albedo reads back as (v, 0, 0)
+V3f vol_albedo(const OracleScene &S, const Vol &v, V3f uvw)
+{
+    if(!v.agrid)
+        return v.albedo_const;
+    const float *g = S.grids + v.aoff;
+    if(v.ach == 1)
+        return V3f(grid_tri(g, v.ares[0], v.ares[1], v.ares[2], 1, 0, uvw), 0.0f, 0.0f);
+    return V3f(grid_tri(g, v.ares[0], v.ares[1], v.ares[2], 3, 0, uvw),
+               grid_tri(g, v.ares[0], v.ares[1], v.ares[2], 3, 1, uvw),
+               grid_tri(g, v.ares[0], v.ares[1], v.ares[2], 3, 2, uvw));
+}
+
+float vol_crossing(const Vol &v, V3f p, V3f d)
+{
+    const V3f op = p - v.o;
+    float t0 = 0.0f, t1 = 1.0f;
+    const V3f ax[3] = { v.xd, v.yd, v.zd };
+    for(int a = 0; a < 3; ++a)
+    {
+        const float opd = dot(op, ax[a]), dd = dot(d, ax[a]);
+        const float nd = (0.0f - opd) / dd, fd = (1.0f - opd) / dd;
+        t0 = std::fmax(t0, std::fmin(nd, fd));
+        t1 = std::fmin(t1, std::fmax(nd, fd));
+    }
+    if(t0 > t1)
+        return -1.0f;
+    if(t0 > 0)
+        return t0;
+    if(t1 < 1.0f)
+        return t1;
+    return -1.0f;
+}
+
+bool vol_next_boundary(const OracleScene &S, V3f a, V3f b, V3f &out)
+{
+    const V3f dir = b - a;
+    float best = std::numeric_limits<float>::max();
+    for(int k = 0; k < S.nvol; ++k)
+    {
+        const float t = vol_crossing(volume(S, k), a, dir);
+        if(t >= 0.0f)
+            best = std::fmin(best, t);
+    }
+    if(best > 10.0f)
+        return false;
+    out = a * (1.0f - best) + b * best;
+    return true;
+}
+
+// the (at most 4) lowest-id volumes containing p
+int vol_overlap(const OracleScene &S, V3f p, int *ids)
+{
+    int n = 0;
+    for(int k = 0; k < S.nvol && n < 4; ++k)
+    {
+        const Vol v = volume(S, k);
+        const V3f op = p - v.o;
+        const float u = dot(op, v.xd), w = dot(op, v.yd), x = dot(op, v.zd);
+        if(0.0f <= u && u <= 1.0f && 0.0f <= w && w <= 1.0f && 0.0f <= x && x <= 1.0f)
+            ids[n++] = k;
+    }
+    return n;
+}
+
+float overlap_inv_max(const OracleScene &S, const int *ids, int n)
+{
+    float m = 0.0f;
+    for(int k = 0; k < n; ++k)
+        m += volume(S, ids[k]).sigma_max;
+    return 1.0f / std::max(m, 0.01f);
+}
+
 template<class Smp>
-bool medium_sample(const OracleScene &S, const Med &m, V3f a, V3f b, Smp &smp, V3f &pos)
+bool vol_sample_overlap(const OracleScene &S, const int *ids, int n, V3f a, V3f b, Smp &smp, V3f &pos, V3f &color)
+{
+    const float inv = overlap_inv_max(S, ids, n);
+    Vol vs[4];
+    V3f ua[4], ub[4];
+    for(int k = 0; k < n; ++k)
+    {
+        vs[k] = volume(S, ids[k]);
+        ua[k] = vol_uvw(vs[k], a);
+        ub[k] = vol_uvw(vs[k], b);
+    }
+    const float t_max = len(b - a);
+    float t = 0.0f;
+    for(int it = 0; it < (1 << 20); ++it)
+    {
+        t += -std::log(1.0f - smp.get1d()) * inv;
+        if(t >= t_max)
+            return false;
+        const float tf = t / t_max;
+        float dens[4], sum = 0.0f;
+        V3f uvw[4];
+        for(int k = 0; k < n; ++k)
+        {
+            uvw[k] = ua[k] * (1.0f - tf) + ub[k] * tf;
+            dens[k] = vol_sigma(S, vs[k], uvw[k]);
+            sum += dens[k];
+        }
+        if(smp.get1d() < sum * inv)
+        {
+            pos = a * (1.0f - tf) + b * tf;
+            V3f alb(0.0f);
+            for(int k = 0; k < n; ++k)
+                alb = alb + (dens[k] / sum) * vol_albedo(S, vs[k], uvw[k]);
+            color = alb;
+            return true;
+        }
+    }
+    return false;
+}
+
+template<class Smp>
+float vol_tr_overlap(const OracleScene &S, const int *ids, int n, V3f a, V3f b, Smp &smp)
+{
+    const float inv = overlap_inv_max(S, ids, n);
+    Vol vs[4];
+    V3f ua[4], ub[4];
+    for(int k = 0; k < n; ++k)
+    {
+        vs[k] = volume(S, ids[k]);
+        ua[k] = vol_uvw(vs[k], a);
+        ub[k] = vol_uvw(vs[k], b);
+    }
+    const float t_max = len(b - a);
+    float r = 1.0f, t = 0.0f;
+    for(int it = 0; it < (1 << 20); ++it)
+    {
+        t += -std::log(1.0f - smp.get1d()) * inv;
+        if(t >= t_max)
+            break;
+        const float tf = t / t_max;
+        float sum = 0.0f;
+        for(int k = 0; k < n; ++k)
+            sum += vol_sigma(S, vs[k], ua[k] * (1.0f - tf) + ub[k] * tf);
+        r *= 1.0f - sum * inv;
+    }
+    return r;
+}
+
+template<class Smp>
+bool volumes_sample(const OracleScene &S, V3f a, V3f b, Smp &smp, V3f &pos, V3f &color)
+{
+    V3f o = a;
+    const V3f d = nrm(b - a);
+    for(int seg = 0; seg < (1 << 16); ++seg)
+    {
+        if(dot(b - o, d) <= 0.0f || dot(b - o, b - o) < 0.00001f)
+            return false;
+        V3f inct;
+        if(!vol_next_boundary(S, o, b, inct))
+            inct = b;
+        int ids[4];
+        const int n = vol_overlap(S, 0.5f * (o + inct), ids);
+        if(n != 0 && vol_sample_overlap(S, ids, n, o, inct, smp, pos, color))
+            return true;
+        o = inct + 0.001f * d;
+    }
+    return false;
+}
+
+template<class Smp>
+float volumes_tr(const OracleScene &S, V3f a, V3f b, Smp &smp)
+{
+    float r = 1.0f;
+    V3f o = a;
+    const V3f d = nrm(b - a);
+    for(int seg = 0; seg < (1 << 16); ++seg)
+    {
+        if(dot(b - o, d) <= 0.0f || dot(b - o, b - o) < 0.0001f)
+            break;
+        V3f inct;
+        if(!vol_next_boundary(S, o, b, inct))
+            inct = b;
+        int ids[4];
+        const int n = vol_overlap(S, 0.5f * (o + inct), ids);
+        if(n != 0)
+            r *= vol_tr_overlap(S, ids, n, o, inct, smp);
+        o = inct + 0.001f * d;
+    }
+    return r;
+}
+
+// medium sampling; color / g are the phase function's (the medium's albedo and HG g)
+template<class Smp>
+bool medium_sample(const OracleScene &S, const Med &m, V3f a, V3f b, Smp &smp, V3f &pos, V3f &color, float &g)
 {
     if(m.type == 0)
         return false;
+    if(m.type == 3)
+    {
+        g = 0.0f;
+        return volumes_sample(S, a, b, smp, pos, color);
+    }
+    color = m.albedo;
+    g = m.g;
     const float t_max = len(b - a);
     if(m.type == 1)
     {
@@ -1518,6 +1794,8 @@ V3f medium_tr(const OracleScene &S, const Med &m, V3f a, V3f b, Smp &smp)
 {
     if(m.type == 0)
         return V3f(1.0f);
+    if(m.type == 3)
+        return V3f(volumes_tr(S, a, b, smp));
     const float t_max = len(b - a);
     if(m.type == 1)
     {
@@ -1727,8 +2005,9 @@ void trace_path(const Prepared &P, uint64_t g, double *film)
             const Med m = medium(S, medium_id);
             if(m.type != 0)
             {
-                V3f spos;
-                const bool sc = medium_sample(S, m, o, end, smp, spos);
+                V3f spos, pcolor;
+                float pg = 0.0f;
+                const bool sc = medium_sample(S, m, o, end, smp, spos, pcolor, pg);
                 const V3f tr = medium_tr(S, m, o, end, smp);
                 beta_le = beta_le * tr;
                 if(sc)
@@ -1742,25 +2021,25 @@ void trace_path(const Prepared &P, uint64_t g, double *film)
                         if(ls.ok)
                         {
                             const float u = -dot(nrm(ls.d), nrm(-d));
-                            const float ph = hg(m.g, u);
-                            ls.li = ls.li * beta * (m.albedo * ph) / (ph + ls.pdf);
+                            const float ph = hg(pg, u);
+                            ls.li = ls.li * beta * (pcolor * ph) / (ph + ls.pdf);
                         }
                         // HenyeyGreensteinPhaseShader::sample (core/btrc/core/medium.cpp:32-64)
                         float a0, a1, a2;
                         smp.get3d(a0, a1, a2);
                         const float ss = a0 + a0 - 1;
                         float u;
-                        if(std::fabs(m.g) < 0.001f)
+                        if(std::fabs(pg) < 0.001f)
                             u = ss;
                         else
                         {
-                            const float g2 = m.g * m.g;
-                            u = (1.0f + g2 - sq((1.0f - g2) / (1.0f + m.g * ss))) / (m.g + m.g);
+                            const float g2 = pg * pg;
+                            u = (1.0f + g2 - sq((1.0f - g2) / (1.0f + pg * ss))) / (pg + pg);
                         }
                         const float ct = -u, st = cos2sin(ct), phi = 2 * PIf * a1;
                         const V3f lwi(st * std::sin(phi), st * std::cos(phi), ct);
-                        const float pv = hg(m.g, u);
-                        const V3f phase = m.albedo * pv;
+                        const float pv = hg(pg, u);
+                        const V3f phase = pcolor * pv;
                         const V3f nd = Frame<float>::from_z(-d).l2g(lwi);
                         if(ls.ok)
                         {
@@ -2044,6 +2323,23 @@ void trace_path(const Prepared &P, uint64_t g, double *film)
 
 extern "C" {
 
+// transmittance of segments (a, b: 6 floats each) through one medium of the scene, each
+// with its own PCG stream seeded (seeds[i], PCG_STREAM): the independent-sampler stream
+// the library's medium test hook uses
+void oracle_medium_tr_batch(const OracleScene *S, int medium_id, const float *seg, const uint64_t *seeds, uint64_t n,
+                            float *out)
+{
+    const Med m = medium(*S, medium_id);
+    for(uint64_t i = 0; i < n; ++i)
+    {
+        PcgSmp smp;
+        smp.p.seed(seeds[i], PCG_STREAM);
+        const V3f a(seg[i * 6 + 0], seg[i * 6 + 1], seg[i * 6 + 2]);
+        const V3f b(seg[i * 6 + 3], seg[i * 6 + 4], seg[i * 6 + 5]);
+        out[i] = medium_tr(*S, m, a, b, smp).x;
+    }
+}
+
 void *oracle_bvh_build(const float *tris, const uint32_t *ids, uint64_t n)
 {
     auto *b = new Bvh();
@@ -2201,6 +2497,7 @@ void *oracle_prepare(const OracleScene *S)
         P->filter.init(v);
     }
     P->hc = Sampler::consts(S->width, S->height);
+    P->has_media = S->nvol > 0;
     for(int i = 0; i < S->ninst && S->nmed > 0; ++i)
         if(medium(*S, S->inst_inner[i]).type != 0 || medium(*S, S->inst_outer[i]).type != 0)
             P->has_media = true;

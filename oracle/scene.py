@@ -464,14 +464,19 @@ def _material(n: Node) -> np.ndarray:
     return rec
 
 
-def _grid(n: Node, sdir: str):
+def _grid(n: Node, sdir: str, rgb: bool = False):
     """Texture3D: constant, {"type":"constant","value":..}, {"type":"array","text":f}
-    (common/btrc/utils/cuda/array.cpp:313-384, channel 0) or {"type":"array","binary":f}."""
+    (common/btrc/utils/cuda/array.cpp:313-384) or {"type":"array","binary":f}.
+    Returns (constant, None) or (None, grid[d, h, w] or grid[d, h, w, 3] when rgb and the
+    array has 3 or 4 channels). The constant is the red channel, or [r, g, b] when rgb.
+    "byte" components are single characters read as signed 8-bit normalised values."""
     if n.kind in ("value", "array"):
-        return float(vvec3(n)[0]), None
+        v = vvec3(n)
+        return (v if rgb else float(v[0])), None
     t = n.child("type").s
     if t == "constant":
-        return float(vvec3(n.child("value"))[0]), None
+        v = vvec3(n.child("value"))
+        return (v if rgb else float(v[0])), None
     if t != "array":
         raise ValueError("texture3d type " + t)
     if n.find("binary") is not None:
@@ -483,10 +488,50 @@ def _grid(n: Node, sdir: str):
     fn = n.child("text").s.replace("$env{scene_directory}", sdir)
     toks = Path(fn).read_text().split()
     comp, ch, w, h, d = toks[0], int(toks[1]), int(toks[2]), int(toks[3]), int(toks[4])
-    vals = np.array(toks[5:5 + ch * w * h * d], np.float64).reshape(-1, ch)[:, 0]
+    count = ch * w * h * d
     if comp == "byte":
-        vals = vals / 127.0
-    return None, vals.astype(np.float32).reshape(d, h, w)
+        chars = "".join(toks[5:]).encode("latin-1")[:count]
+        vals = np.frombuffer(chars, np.int8).astype(np.float64) / 127.0
+        vals = np.maximum(vals, -1.0)
+    else:
+        vals = np.array(toks[5:5 + count], np.float64)
+    vals = vals.reshape(-1, ch)
+    if rgb and ch > 1:
+        return None, vals[:, :3].astype(np.float32).reshape(d, h, w, 3)
+    return None, vals[:, 0].astype(np.float32).reshape(d, h, w)
+
+
+def _volume(n: Node, sdir: str):
+    """One volume primitive (factory/btrc/factory/scene.cpp:57-79): the 32-float record of
+    oracle.cpp's volume() and its sigma_t / albedo grids (or None)."""
+    rec = np.zeros(32, np.float32)
+    for k, key in enumerate(("o", "x", "y", "z")):
+        rec[3 * k:3 * k + 3] = vvec3(n.child(key))
+    c, sg = _grid(n.child("sigma_t"), sdir)
+    if sg is None:
+        rec[12] = rec[13] = c
+        rec[14:17] = 1
+    else:
+        rec[13] = float(sg.max())
+        rec[14], rec[15], rec[16] = sg.shape[2], sg.shape[1], sg.shape[0]
+        rec[24] = 1
+    ca, ag = _grid(n.child("albedo"), sdir, rgb=True)
+    if ag is None:
+        rec[21:24] = ca
+        rec[17:20] = 1
+        rec[20] = 3
+    else:
+        rec[17], rec[18], rec[19] = ag.shape[2], ag.shape[1], ag.shape[0]
+        rec[20] = 3 if ag.ndim == 4 else 1
+        rec[25] = 1
+    return rec, sg, ag
+
+
+def volume_box(rec: np.ndarray):
+    """VolumePrimitive::get_bounding_box (core/btrc/core/volume.cpp:54-68)."""
+    o, x, y, z = rec[0:3], rec[3:6], rec[6:9], rec[9:12]
+    pts = np.stack([o, (o + x).astype(np.float32), (o + y).astype(np.float32), (o + z).astype(np.float32)])
+    return pts.min(0), pts.max(0)
 
 
 def _medium(n: Node, sdir: str, w2l=None):
@@ -616,7 +661,27 @@ class Scene:
             if grid is not None:
                 grids.append(grid.reshape(-1))
                 off += grid.size
+        # volume primitives: their grids follow the media grids in the same pool
+        vol_recs, vol_offs = [], []
+        vnode = scene.find("volumes")
+        for vn in (vnode.elems if vnode is not None else []):
+            rec, sg, ag = _volume(vn, sdir)
+            so = ao = 0
+            if sg is not None:
+                so = off
+                grids.append(sg.reshape(-1))
+                off += sg.size
+            if ag is not None:
+                ao = off
+                grids.append(ag.reshape(-1))
+                off += ag.size
+            vol_recs.append(rec)
+            vol_offs += [so, ao]
+        self.vol = np.ascontiguousarray(np.stack(vol_recs) if vol_recs else np.zeros((1, 32)), np.float32)
+        self.vol_off = np.array(vol_offs if vol_offs else [0, 0], np.uint64)
+        self.nvol = len(vol_recs)
         vac = np.zeros(28, np.float32)
+        vac[0] = 3 if self.nvol else 0
         vac[1] = -1e30
         recs.append(vac)
         offs.append(off)
@@ -668,6 +733,12 @@ class Scene:
                                 for c in range(8)], np.float32)
             w = apply_point(mat, corners)
             lo, hi = np.minimum(lo, w.min(0)), np.maximum(hi, w.max(0))
+        # volume boxes join the world bounds (core/btrc/core/scene.cpp:233-237)
+        for k in range(self.nvol):
+            bl, bh = volume_box(self.vol[k])
+            lo, hi = np.minimum(lo, bl), np.maximum(hi, bh)
+        if not np.all(lo <= hi):
+            lo, hi = np.zeros(3, np.float32), np.zeros(3, np.float32)
         ext = (hi - lo).astype(np.float32)
         self.world_diagonal = float(np.sqrt(np.float32((ext * ext).sum(dtype=np.float32))))
         self.light_inst = np.array(linst, np.int32)
@@ -712,7 +783,18 @@ class Scene:
         s.rr_threshold, s.rr_cont_prob = self.rr_threshold, self.rr_cont_prob
         s.sampler, s.filter = self.sampler, self.filter
         s.filter_radius, s.filter_alpha = self.filter_radius, self.filter_alpha
+        s.nvol, s.vol, s.vol_off = self.nvol, _p(self.vol), _p(self.vol_off)
         return s
+
+    def medium_tr(self, medium_id: int, seg: np.ndarray, seeds: np.ndarray) -> np.ndarray:
+        """Ratio-tracking transmittance of segments (n, 6) through one medium, one PCG
+        stream per segment seeded (seeds[i], PCG_STREAM)."""
+        seg = np.ascontiguousarray(seg, np.float32)
+        seeds = np.ascontiguousarray(seeds, np.uint64)
+        out = np.zeros(len(seg), np.float32)
+        st = self.struct()
+        lib().oracle_medium_tr_batch(st, medium_id, _p(seg), _p(seeds), len(seg), _p(out))
+        return out
 
     def prepare(self):
         if self._prepared is None:
