@@ -53,7 +53,8 @@ class BuildOpts(C.Structure):
 
 class RenderOpts(C.Structure):
     _fields_ = [("spp", C.c_int32), ("state_count", C.c_int32), ("output_on_device", C.c_int32),
-                ("use_graphs", C.c_int32), ("profile", C.c_int32)]
+                ("use_graphs", C.c_int32), ("profile", C.c_int32), ("post_process", C.c_int32),
+                ("albedo_out", _vp), ("normal_out", _vp)]
 
 
 STAGES = ("control", "generate", "trace", "medium", "shade", "shadow")
@@ -94,6 +95,8 @@ SIGNATURES = {
                                      _vp, _vp]),
     "btrc_bsdf_batch": (C.c_int, [_vp, C.c_int32, _vp, _vp, _vp, C.c_uint64, _vp, _vp]),
     "btrc_medium_tr_batch": (C.c_int, [_vp, _vp, C.c_int32, _vp, _vp, C.c_uint64, _vp, _vp]),
+    "btrc_tonemap_aces": (C.c_int, [_vp, _vp, C.c_int32, C.c_int32, C.c_int32, C.c_float, _vp]),
+    "btrc_image_save": (C.c_int, [_vp, C.c_char_p, _vp, C.c_int32, C.c_int32, C.c_int32, C.c_float]),
 }
 
 _lib = None
@@ -189,14 +192,19 @@ class Context:
         self._lib.btrc_cancel(self.handle)
 
     def render(self, scene: "Scene", spp: int = 0, state_count: int = 0, out=None, use_graphs: bool = True,
-               stats: dict | None = None, profile: int = 0) -> np.ndarray:
+               stats: dict | None = None, profile: int = 0, post_process: bool = False, albedo=None,
+               normal=None) -> np.ndarray:
         """Render the scene's frame. `out` may be a CUDA tensor (rendered in place) or None
-        (a new host float32 array of shape (H, W, 3) is returned)."""
+        (a new host float32 array of shape (H, W, 3) is returned). `albedo` / `normal`
+        receive the first-hit g-buffers (arrays in the same memory space as `out`);
+        post_process runs the scene's post_processors (tonemap, save) on the result."""
         info = scene.info()
         on_dev = out is not None and hasattr(out, "is_cuda") and out.is_cuda
         if out is None:
             out = np.zeros((info.height, info.width, 3), np.float32)
-        opts = RenderOpts(spp, state_count, 1 if on_dev else 0, 1 if use_graphs else 0, profile)
+        opts = RenderOpts(spp, state_count, 1 if on_dev else 0, 1 if use_graphs else 0, profile,
+                          1 if post_process else 0, _ptr(albedo) if albedo is not None else None,
+                          _ptr(normal) if normal is not None else None)
         st = Stats()
         self._check(self._lib.btrc_render(self.handle, scene.handle, C.byref(opts), _ptr(out), C.byref(st)))
         if stats is not None:
@@ -235,6 +243,18 @@ class Context:
     def medium_tr_batch(self, scene: "Scene", medium_id: int, seg, seeds, n: int, out, stream: int | None = None):
         self._check(self._lib.btrc_medium_tr_batch(self.handle, scene.handle, medium_id, _ptr(seg), _ptr(seeds),
                                                    n, _ptr(out), stream))
+
+    def tonemap_aces(self, pixels, width: int, height: int, channels: int = 3, exposure: float = 1.0,
+                     stream: int | None = None):
+        """In-place ACES tone map of a device buffer (tonemap post-processor)."""
+        self._check(self._lib.btrc_tonemap_aces(self.handle, _ptr(pixels), width, height, channels, exposure,
+                                                stream))
+
+    def image_save(self, filename: str, pixels: np.ndarray, gamma: float = 1.0):
+        """Write an (H, W, 3|4) float image to .png / .exr / .hdr (save post-processor)."""
+        px = np.ascontiguousarray(pixels, np.float32)
+        h, w, c = px.shape
+        self._check(self._lib.btrc_image_save(self.handle, str(filename).encode(), _ptr(px), w, h, c, gamma))
 
 
 class Scene:

@@ -15,6 +15,7 @@
 
 #include "btrc.h"
 #include "bvh.h"
+#include "image_io.h"
 #include "kernels.h"
 #include "scene.h"
 
@@ -408,6 +409,34 @@ void ensure_render_buffers(btrc_ctx *ctx, uint32_t capacity, size_t pixels)
     ctx->film_pixels = pixels;
 }
 
+// g-buffer films, allocated the first time a render asks for them
+void ensure_aov_buffers(btrc_ctx *ctx, size_t pixels, bool albedo, bool normal)
+{
+    RenderBuffers &B = ctx->buf;
+    if(albedo && !B.aov_albedo)
+        B.aov_albedo = static_cast<float4 *>(dev_alloc(ctx->buf_allocs, sizeof(float4) * pixels));
+    if(normal && !B.aov_normal)
+        B.aov_normal = static_cast<float4 *>(dev_alloc(ctx->buf_allocs, sizeof(float4) * pixels));
+}
+
+// device scratch: 256 bytes of error flags, then `images` images of pixels * 3 floats
+float *ctx_scratch_images(btrc_ctx *ctx, size_t pixels, int images)
+{
+    const size_t need = 256 + static_cast<size_t>(images) * pixels * 3 * sizeof(float);
+    if(ctx->scratch_bytes < need)
+    {
+        check_cuda(cudaStreamSynchronize(ctx->stream), "stream sync");
+        if(ctx->scratch)
+            cudaFree(ctx->scratch);
+        ctx->scratch = nullptr;
+        ctx->scratch_bytes = 0;
+        check_cuda(cudaMalloc(&ctx->scratch, need), "cudaMalloc");
+        check_cuda(cudaMemset(ctx->scratch, 0, 256), "cudaMemset");
+        ctx->scratch_bytes = need;
+    }
+    return reinterpret_cast<float *>(static_cast<char *>(ctx->scratch) + 256);
+}
+
 DevRender make_render_params(const btrc_scene *sc, int spp, uint32_t capacity)
 {
     const HostScene &H = sc->host;
@@ -653,7 +682,21 @@ btrc_status btrc_render(btrc_ctx *ctx, btrc_scene *scene, const btrc_render_opts
         const size_t pixels = static_cast<size_t>(H.params.width) * H.params.height;
         ensure_render_buffers(ctx, capacity, pixels);
         check_cuda(cudaMemsetAsync(ctx->buf.film, 0, sizeof(float4) * pixels, ctx->stream), "film clear");
+        const bool post_on = opts && opts->post_process;
+        const bool want_albedo = (opts && opts->albedo_out) || (post_on && H.params.albedo);
+        const bool want_normal = (opts && opts->normal_out) || (post_on && H.params.normal);
+        ensure_aov_buffers(ctx, pixels, want_albedo, want_normal);
         DevRender R = make_render_params(scene, spp, capacity);
+        if(want_albedo)
+        {
+            R.aov_albedo = ctx->buf.aov_albedo;
+            check_cuda(cudaMemsetAsync(R.aov_albedo, 0, sizeof(float4) * pixels, ctx->stream), "albedo clear");
+        }
+        if(want_normal)
+        {
+            R.aov_normal = ctx->buf.aov_normal;
+            check_cuda(cudaMemsetAsync(R.aov_normal, 0, sizeof(float4) * pixels, ctx->stream), "normal clear");
+        }
         ctx->buf.capacity = capacity;
         RenderStats rs{};
         const bool graphs = !opts || opts->use_graphs != 0;
@@ -664,25 +707,104 @@ btrc_status btrc_render(btrc_ctx *ctx, btrc_scene *scene, const btrc_render_opts
                                     &cancelled),
                    "wavefront render");
         const bool on_dev = opts && opts->output_on_device;
-        float *rgb_dev = rgb_out;
-        if(!on_dev)
+        const bool post = opts && opts->post_process;
+        float *rgb_dev = rgb_out, *alb_dev = want_albedo ? (opts ? opts->albedo_out : nullptr) : nullptr,
+              *nrm_dev = want_normal ? (opts ? opts->normal_out : nullptr) : nullptr;
+        if(!on_dev || (want_albedo && !alb_dev) || (want_normal && !nrm_dev))
         {
-            if(ctx->scratch_bytes < pixels * 3 * sizeof(float) + 256)
-            {
-                if(ctx->scratch)
-                    cudaFree(ctx->scratch);
-                ctx->scratch = nullptr;
-                check_cuda(cudaMalloc(&ctx->scratch, pixels * 3 * sizeof(float) + 256), "cudaMalloc");
-                check_cuda(cudaMemset(ctx->scratch, 0, 256), "cudaMemset");
-                ctx->scratch_bytes = pixels * 3 * sizeof(float) + 256;
-            }
-            rgb_dev = reinterpret_cast<float *>(static_cast<char *>(ctx->scratch) + 256);
+            float *img = ctx_scratch_images(ctx, pixels, 3);
+            if(!on_dev)
+                rgb_dev = img;
+            if(want_albedo && (!on_dev || !alb_dev))
+                alb_dev = img + pixels * 3;
+            if(want_normal && (!on_dev || !nrm_dev))
+                nrm_dev = img + pixels * 6;
         }
         check_cuda(launch_resolve(ctx->buf.film, rgb_dev, static_cast<uint32_t>(pixels), ctx->stream), "resolve");
+        int extra_launches = 1;
+        if(want_albedo)
+        {
+            check_cuda(launch_resolve_aov(ctx->buf.film, ctx->buf.aov_albedo, alb_dev, static_cast<uint32_t>(pixels),
+                                          false, ctx->stream),
+                       "albedo resolve");
+            ++extra_launches;
+        }
+        if(want_normal)
+        {
+            check_cuda(launch_resolve_aov(ctx->buf.film, ctx->buf.aov_normal, nrm_dev, static_cast<uint32_t>(pixels),
+                                          true, ctx->stream),
+                       "normal resolve");
+            ++extra_launches;
+        }
+        // post_processors in scene order (src/cli/main.cpp:79-80)
+        if(post && !cancelled)
+        {
+            std::vector<float> host_img;
+            auto download = [&](const float *d) {
+                host_img.resize(pixels * 3);
+                check_cuda(cudaMemcpyAsync(host_img.data(), d, pixels * 3 * sizeof(float), cudaMemcpyDeviceToHost,
+                                           ctx->stream),
+                           "post-process download");
+                check_cuda(cudaStreamSynchronize(ctx->stream), "post-process sync");
+            };
+            for(const PostProcess &q : H.post)
+            {
+                if(q.type == POST_DENOISE)
+                    throw StatusError(BTRC_ERR_UNSUPPORTED, "post processor 'denoise' (OptiX denoiser) is not available");
+                if(q.type == POST_TONEMAP)
+                {
+                    check_cuda(launch_tonemap_aces(rgb_dev, static_cast<uint32_t>(pixels), 3, q.exposure, ctx->stream),
+                               "tonemap");
+                    ++extra_launches;
+                    continue;
+                }
+                const int w = H.params.width, h = H.params.height;
+                try
+                {
+                    if(!q.color.empty())
+                    {
+                        download(rgb_dev);
+                        save_image(q.color, host_img.data(), w, h, 3, q.gamma);
+                    }
+                    if(!q.albedo.empty() && want_albedo)
+                    {
+                        download(alb_dev);
+                        save_image(q.albedo, host_img.data(), w, h, 3, 1.0f);
+                    }
+                    if(!q.normal.empty() && want_normal)
+                    {
+                        download(nrm_dev);
+                        save_image(q.normal, host_img.data(), w, h, 3, 1.0f);
+                    }
+                }
+                catch(const UnsupportedFormat &ex)
+                {
+                    throw StatusError(BTRC_ERR_UNSUPPORTED, ex.what());
+                }
+                catch(const std::invalid_argument &ex)
+                {
+                    throw StatusError(BTRC_ERR_INVALID_ARG, ex.what());
+                }
+                catch(const std::runtime_error &ex)
+                {
+                    throw StatusError(BTRC_ERR_IO, ex.what());
+                }
+            }
+        }
         if(!on_dev)
+        {
             check_cuda(cudaMemcpyAsync(rgb_out, rgb_dev, pixels * 3 * sizeof(float), cudaMemcpyDeviceToHost,
                                        ctx->stream),
                        "image download");
+            if(opts && opts->albedo_out)
+                check_cuda(cudaMemcpyAsync(opts->albedo_out, alb_dev, pixels * 3 * sizeof(float),
+                                           cudaMemcpyDeviceToHost, ctx->stream),
+                           "albedo download");
+            if(opts && opts->normal_out)
+                check_cuda(cudaMemcpyAsync(opts->normal_out, nrm_dev, pixels * 3 * sizeof(float),
+                                           cudaMemcpyDeviceToHost, ctx->stream),
+                           "normal download");
+        }
         check_cuda(cudaStreamSynchronize(ctx->stream), "render sync");
         if(stats)
         {
@@ -693,7 +815,7 @@ btrc_status btrc_render(btrc_ctx *ctx, btrc_scene *scene, const btrc_render_opts
             stats->traversal_errors = rs.err;
             stats->device_ms = rs.device_ms;
             stats->wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
-            stats->kernel_launches = rs.kernel_launches + 1;  // + resolve
+            stats->kernel_launches = rs.kernel_launches + extra_launches;  // + resolves, tonemaps
             for(int k = 0; k < 6; ++k)
             {
                 stats->stage_ms[k] = rs.stage_ms[k];
@@ -873,6 +995,48 @@ btrc_status btrc_medium_tr_batch(btrc_ctx *ctx, const btrc_scene *scene, int32_t
         check_cuda(launch_medium_tr_batch(scene->dev, medium_id, d_seg, d_seeds, static_cast<uint32_t>(n), d_out,
                                           pick_stream(ctx, stream)),
                    "medium tr batch");
+    });
+}
+
+btrc_status btrc_tonemap_aces(btrc_ctx *ctx, float *d_pixels, int32_t width, int32_t height, int32_t channels,
+                              float exposure, void *stream)
+{
+    if(!ctx || width < 0 || height < 0 || (channels != 3 && channels != 4) ||
+       static_cast<uint64_t>(width) * static_cast<uint64_t>(height) > 0xffffffffull ||
+       (width > 0 && height > 0 && !d_pixels))
+        return BTRC_ERR_INVALID_ARG;
+    return guarded(ctx, [&] {
+        if(ctx->device < 0)
+            throw StatusError(BTRC_ERR_INVALID_ARG, "host-only context");
+        check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+        check_cuda(launch_tonemap_aces(d_pixels, static_cast<uint32_t>(width) * static_cast<uint32_t>(height), channels,
+                                       exposure, pick_stream(ctx, stream)),
+                   "tonemap");
+    });
+}
+
+btrc_status btrc_image_save(btrc_ctx *ctx, const char *filename, const float *pixels, int32_t width, int32_t height,
+                            int32_t channels, float gamma)
+{
+    if(!filename || !pixels || width <= 0 || height <= 0 || (channels != 3 && channels != 4) || !(gamma > 0))
+        return BTRC_ERR_INVALID_ARG;
+    return guarded(ctx, [&] {
+        try
+        {
+            save_image(filename, pixels, width, height, channels, gamma);
+        }
+        catch(const UnsupportedFormat &ex)
+        {
+            throw StatusError(BTRC_ERR_UNSUPPORTED, ex.what());
+        }
+        catch(const std::invalid_argument &ex)
+        {
+            throw StatusError(BTRC_ERR_INVALID_ARG, ex.what());
+        }
+        catch(const std::runtime_error &ex)
+        {
+            throw StatusError(BTRC_ERR_IO, ex.what());
+        }
     });
 }
 

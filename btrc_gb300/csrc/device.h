@@ -51,6 +51,8 @@ struct DevRender
     HaltonConsts halton;
     const AliasEntry8 *filter_table;
     V3 cam_eye, cam_lbc, cam_fx, cam_fy;
+    float4 *aov_albedo;       // first-hit albedo sums (xyz), or null
+    float4 *aov_normal;       // first-hit normal sums (xyz), or null
 };
 
 // Queue counters, resident in device memory for the whole render.

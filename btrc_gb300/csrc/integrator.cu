@@ -1067,6 +1067,21 @@ __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, DevRender R, PathSo
         sh.mat = make_material_eval(mat);
         sh.shadow_terminator = mat.shadow_terminator != 0;
 
+        // g-buffer at the first hit (shade.cpp:133-139, 195-202): Shader::albedo and
+        // Shader::normal; black / invisible report the geometric normal
+        if(depth == 0 && (R.aov_albedo != nullptr || R.aov_normal != nullptr))
+        {
+            const bool geo_normal = mat.type == MAT_BLACK || mat.type == MAT_INVISIBLE;
+            const V3 alb = mat.type == MAT_BLACK ? V3(0.0f)
+                           : mat.type == MAT_INVISIBLE ? V3(1.0f)
+                                                       : V3(mat.p[0], mat.p[1], mat.p[2]);
+            const V3 nrm = geo_normal ? sp.frame.z : sh.frame.shading.z;
+            if(R.aov_albedo != nullptr)
+                splat(R.aov_albedo, pixel, R.width, alb);
+            if(R.aov_normal != nullptr)
+                splat(R.aov_normal, pixel, R.width, nrm);
+        }
+
         float u0, u1, u2;
         smp.get3d(u0, u1, u2);
         const V3 wo = -d;
@@ -1434,6 +1449,63 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
         }
     }
     return e;
+}
+
+// preview kernels for the g-buffer (wavefront/preview.cpp:27-78): sum / weight, and
+// normals renormalised (zero when shorter than 1e-3)
+__global__ void k_resolve_aov(const float4 *film, const float4 *aov, float *out, uint32_t pixels, int normal)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= pixels)
+        return;
+    const float w = film[i].w;
+    const float4 v = aov[i];
+    V3 o(0.0f);
+    if(w > 0)
+    {
+        o = V3(v.x, v.y, v.z) / w;
+        if(normal)
+            o = length(o) > 1e-3f ? normalize(o) : V3(0.0f);
+    }
+    out[i * 3 + 0] = o.x;
+    out[i * 3 + 1] = o.y;
+    out[i * 3 + 2] = o.z;
+}
+
+// ACESToneMap (builtin/btrc/builtin/postprocess/tonemap.cpp:14-53): the ACES filmic fit
+// x (2.51 x + 0.03) / (x (2.43 x + 0.59) + 0.14), saturated, on exposure-scaled RGB
+__device__ __forceinline__ float aces(float x)
+{
+    const float v = (x * (2.51f * x + 0.03f)) / (x * (2.43f * x + 0.59f) + 0.14f);
+    return fminf(fmaxf(v, 0.0f), 1.0f);
+}
+
+__global__ void k_tonemap_aces(float *px, uint32_t pixels, int channels, float exposure)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= pixels)
+        return;
+    float *p = px + static_cast<size_t>(i) * channels;
+    p[0] = aces(p[0] * exposure);
+    p[1] = aces(p[1] * exposure);
+    p[2] = aces(p[2] * exposure);
+}
+
+cudaError_t launch_resolve_aov(const float4 *film, const float4 *aov, float *out, uint32_t pixels, bool normal,
+                               cudaStream_t st)
+{
+    if(pixels == 0)
+        return cudaSuccess;
+    k_resolve_aov<<<(pixels + 255) / 256, 256, 0, st>>>(film, aov, out, pixels, normal ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tonemap_aces(float *px, uint32_t pixels, int channels, float exposure, cudaStream_t st)
+{
+    if(pixels == 0)
+        return cudaSuccess;
+    k_tonemap_aces<<<(pixels + 255) / 256, 256, 0, st>>>(px, pixels, channels, exposure);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_resolve(const float4 *film, float *rgb, uint32_t pixels, cudaStream_t st)

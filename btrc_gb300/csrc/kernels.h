@@ -28,6 +28,8 @@ struct RenderBuffers
     uint32_t *hit_flag;
     HitDetail *hit_detail;
     float4 *film;          // radiance.rgb, weight per pixel
+    float4 *aov_albedo;    // first-hit albedo sums, allocated on demand
+    float4 *aov_normal;    // first-hit normal sums, allocated on demand
     Counters *counters;
     Counters *host_counters;  // pinned, ring of RING_SLOTS
     uint32_t capacity;
@@ -81,6 +83,11 @@ cudaError_t render_wavefront_noalloc(const DevScene &S, const DevRender &R, void
 
 // radiance / weight -> rgb (3 floats per pixel)
 cudaError_t launch_resolve(const float4 *film, float *rgb, uint32_t pixels, cudaStream_t st);
+// g-buffer resolve (sum / weight; normals renormalised) into 3 floats per pixel
+cudaError_t launch_resolve_aov(const float4 *film, const float4 *aov, float *out, uint32_t pixels, bool normal,
+                               cudaStream_t st);
+// in-place ACES tone map of 3- or 4-channel float pixels
+cudaError_t launch_tonemap_aces(float *px, uint32_t pixels, int channels, float exposure, cudaStream_t st);
 
 // test hooks
 cudaError_t launch_sampler_batch(int type, int width, int height, const HaltonConsts &hc,

@@ -973,6 +973,48 @@ HostScene load_scene(const std::string &path)
                                 static_cast<float>(S.params.width) / S.params.height);
     }
 
+    // post_processors: one group or an array of them
+    if(auto pp = root->find("post_processors"))
+    {
+        std::vector<NodeP> items;
+        if(pp->is_group())
+            items.push_back(pp);
+        else if(pp->is_array())
+            items = pp->elems;
+        else
+            throw std::runtime_error("parse_post_processors: array or group is expected");
+        for(const NodeP &n : items)
+        {
+            PostProcess q;
+            const std::string type = json::as_string(n->child("type"));
+            auto path_or_empty = [&](const char *key) {
+                auto c = n->find(key);
+                if(!c)
+                    return std::string();
+                const std::string v = json::as_string(c);
+                return v.empty() ? v : resolve_path(v, scene_dir);
+            };
+            if(type == "save")
+            {
+                q.type = POST_SAVE;
+                q.gamma = json::float_or(n, "gamma", 1.0f);
+                q.color = path_or_empty("color");
+                q.albedo = path_or_empty("albedo");
+                q.normal = path_or_empty("normal");
+            }
+            else if(type == "tonemap")
+            {
+                q.type = POST_TONEMAP;
+                q.exposure = json::float_or(n, "exposure", 1.0f);
+            }
+            else if(type == "denoise")
+                q.type = POST_DENOISE;
+            else
+                throw std::runtime_error("unsupported post processor type '" + type + "'");
+            S.post.push_back(q);
+        }
+    }
+
     // renderer (builtin/btrc/builtin/renderer/wavefront.cpp:375-397)
     {
         NodeP r = root->child("renderer");

@@ -74,6 +74,22 @@ struct RenderParams
     std::string renderer_type = "wfpt";
 };
 
+// Post-processor of the scene's post_processors list (factory/btrc/factory/post_processor.cpp:5-25)
+enum PostType : int32_t
+{
+    POST_SAVE = 0,      // builtin/btrc/builtin/postprocess/save_to_image.cpp:63-76
+    POST_TONEMAP = 1,   // builtin/btrc/builtin/postprocess/tonemap.cpp:103-108
+    POST_DENOISE = 2,   // optix_denoiser.cpp: the OptiX denoiser, not available here
+};
+
+struct PostProcess
+{
+    PostType type = POST_SAVE;
+    float exposure = 1.0f;    // tonemap
+    float gamma = 1.0f;       // save
+    std::string color, albedo, normal;  // save: output files ("" = not written)
+};
+
 struct HostMedium
 {
     Medium dev{};
@@ -97,6 +113,7 @@ struct HostScene
     std::vector<float> volume_grids; // VolumePrim grid offsets index this pool
     Camera camera{};
     RenderParams params;
+    std::vector<PostProcess> post;
     V3 world_min, world_max;
     uint64_t triangle_count = 0;     // after instance flattening
 };

@@ -101,6 +101,12 @@ typedef struct btrc_render_opts
     int32_t use_graphs;       /* 1: capture bounces in CUDA graphs (default behaviour) */
     int32_t profile;          /* 0 off; 1 CUDA events around every stage launch (no graphs);
                                  2 closest-hit traversal counters (no graphs, slower) */
+    int32_t post_process;     /* 1: run the scene's post_processors on the result, in order:
+                                 tonemap in place, save writes files; a denoise entry
+                                 fails with BTRC_ERR_UNSUPPORTED */
+    float *albedo_out;        /* optional first-hit albedo, width*height*3 floats, same memory
+                                 space as rgb_out (wavefront/shade.cpp:133-139, preview.cpp:27-47) */
+    float *normal_out;        /* optional first-hit normal (world space, renormalised) */
 } btrc_render_opts;
 
 /* stage indices of btrc_stats.stage_ms / stage_launches */
@@ -154,7 +160,9 @@ btrc_status btrc_scene_export_triangles(const btrc_scene *scene, float *xyz, uin
 btrc_status btrc_scene_export_bvh(const btrc_scene *scene, void *nodes, uint64_t node_capacity, void *tris,
                                   uint64_t tri_capacity);
 
-/* Render the whole frame: rgb_out receives width*height*3 floats (radiance / weight). */
+/* Render the whole frame: rgb_out receives width*height*3 floats (radiance / weight).
+   The albedo / normal g-buffers are produced when opts asks for them, or for the save
+   post-processor when the scene's renderer sets "albedo" / "normal" to true. */
 btrc_status btrc_render(btrc_ctx *ctx, btrc_scene *scene, const btrc_render_opts *opts, float *rgb_out,
                         btrc_stats *stats);
 
@@ -173,6 +181,21 @@ btrc_status btrc_render(btrc_ctx *ctx, btrc_scene *scene, const btrc_render_opts
    up the array's device address (cudaGetSymbolAddress); make that first call before any
    stream capture. spp 0 uses the scene's renderer.spp. */
 btrc_status btrc_render_noalloc(btrc_ctx *ctx, btrc_scene *scene, int32_t spp, float *d_rgb_out, btrc_stats *stats);
+
+/* ACESToneMap::process (src/builtin/btrc/builtin/postprocess/tonemap.cpp:86-101): in place
+   on device pixels of 3 (RGB) or 4 (RGBA, alpha untouched) floats:
+   c = saturate(x (2.51 x + 0.03) / (x (2.43 x + 0.59) + 0.14)) with x = c * exposure. */
+btrc_status btrc_tonemap_aces(btrc_ctx *ctx, float *d_pixels, int32_t width, int32_t height, int32_t channels,
+                              float exposure, void *stream);
+
+/* SaveToImage::process (src/builtin/btrc/builtin/postprocess/save_to_image.cpp:30-61) with
+   Image::save (src/common/btrc/utils/image.h:495-550): write host pixels (3 or 4 floats,
+   top row first), raised to 1 / gamma, to the format of the file extension: .png (8-bit
+   RGBA, byte = min(int(v * 256), 255), alpha 255), .exr (float B, G, R, uncompressed),
+   .hdr (RGBE). .jpg / .jpeg: BTRC_ERR_UNSUPPORTED. ctx may be a host-only context; it
+   only receives the error message. */
+btrc_status btrc_image_save(btrc_ctx *ctx, const char *filename, const float *pixels, int32_t width, int32_t height,
+                            int32_t channels, float gamma);
 
 /* Closest hit for n device-resident rays. flags[i] = instance | BTRC_HIT_BIT or 0. */
 btrc_status btrc_trace_closest(btrc_ctx *ctx, const btrc_scene *scene, const btrc_ray *d_rays, uint64_t n,

@@ -61,6 +61,7 @@ def lib() -> C.CDLL:
         L.oracle_medium_tr_batch.argtypes = [C.POINTER(OracleScene), C.c_int, _vp, _vp, C.c_uint64, _vp]
         L.oracle_release.argtypes = [_vp]
         L.oracle_render.argtypes = [_vp, C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, _vp, C.c_int]
+        L.oracle_render_aov.argtypes = [_vp, C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, _vp, _vp, C.c_int]
         _lib = L
     return _lib
 

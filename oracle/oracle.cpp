@@ -1928,7 +1928,7 @@ struct Shadow
     int medium = 0;
 };
 
-void trace_path(const Prepared &P, uint64_t g, double *film)
+void trace_path(const Prepared &P, uint64_t g, double *film, double *aov = nullptr)
 {
     const OracleScene &S = *P.S;
     const uint64_t pixels = static_cast<uint64_t>(S.width) * S.height;
@@ -2141,6 +2141,21 @@ void trace_path(const Prepared &P, uint64_t g, double *film)
                     Mat<float> M;
                     if(mtype <= 2)
                         M.init(mtype, mr + 2);
+                    // g-buffer at the first hit (shade.cpp:133-139, 195-202): black has
+                    // albedo 0, invisible 1, the others their colour; black and invisible
+                    // report the geometric normal, the others the shading normal
+                    if(depth == 0 && aov)
+                    {
+                        const V3f alb = mtype == 3 ? V3f(0.0f) : mtype == 4 ? V3f(1.0f) : V3f(mr[2], mr[3], mr[4]);
+                        const V3f nv = (mtype == 3 || mtype == 4) ? gf.z : fr.s.z;
+                        if(std::isfinite(alb.x) && std::isfinite(alb.y) && std::isfinite(alb.z) &&
+                           std::isfinite(nv.x) && std::isfinite(nv.y) && std::isfinite(nv.z))
+                        {
+                            double *q = aov + (static_cast<size_t>(py) * S.width + px) * 6;
+                            q[0] += alb.x; q[1] += alb.y; q[2] += alb.z;
+                            q[3] += nv.x; q[4] += nv.y; q[5] += nv.z;
+                        }
+                    }
                     float u0, u1, u2;
                     smp.get3d(u0, u1, u2);
                     const V3f wo = -d;
@@ -2517,6 +2532,20 @@ void oracle_render(const void *prepared, uint64_t pixel_begin, uint64_t pixel_en
         const uint64_t pix = pixel_begin + k;
         for(uint32_t s = sample_begin; s < sample_end; ++s)
             trace_path(P, static_cast<uint64_t>(s) * pixels + pix, film);
+    });
+}
+
+// the same with the first-hit g-buffer: aov holds 6 doubles per pixel (albedo sum,
+// normal sum); weights are in film[3]
+void oracle_render_aov(const void *prepared, uint64_t pixel_begin, uint64_t pixel_end, uint32_t sample_begin,
+                       uint32_t sample_end, double *film, double *aov, int threads)
+{
+    const Prepared &P = *static_cast<const Prepared *>(prepared);
+    const uint64_t pixels = static_cast<uint64_t>(P.S->width) * P.S->height;
+    parallel_for(pixel_end - pixel_begin, threads, [&](uint64_t k) {
+        const uint64_t pix = pixel_begin + k;
+        for(uint32_t s = sample_begin; s < sample_end; ++s)
+            trace_path(P, static_cast<uint64_t>(s) * pixels + pix, film, aov);
     });
 }
 

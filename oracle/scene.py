@@ -812,6 +812,16 @@ class Scene:
         lib().oracle_render(h, pixel_begin, pe, sample_begin, sample_begin + spp, _p(film), threads)
         return film
 
+    def render_aov(self, spp: int | None = None, sample_begin: int = 0, threads: int = 0):
+        """Film (H, W, 4) and first-hit g-buffer sums (H, W, 6): albedo.rgb, normal.xyz."""
+        h = self.prepare()
+        spp = self.spp if spp is None else spp
+        film = np.zeros((self.height, self.width, 4), np.float64)
+        aov = np.zeros((self.height, self.width, 6), np.float64)
+        lib().oracle_render_aov(h, 0, self.width * self.height, sample_begin, sample_begin + spp, _p(film), _p(aov),
+                                threads)
+        return film, aov
+
     def __del__(self):
         try:
             if self._prepared is not None:
@@ -833,3 +843,14 @@ def _pinhole(eye, dst, up, fov_deg, w_over_h):
 def resolve(film: np.ndarray) -> np.ndarray:
     w = film[..., 3:4]
     return np.where(w > 0, film[..., :3] / np.maximum(w, 1e-300), 0.0)
+
+
+def resolve_aov(film: np.ndarray, aov: np.ndarray):
+    """The preview resolve of the g-buffer (wavefront/preview.cpp:27-78): albedo = sum /
+    weight; normal = sum / weight renormalised, zero when shorter than 1e-3."""
+    w = film[..., 3:4]
+    alb = np.where(w > 0, aov[..., 0:3] / np.maximum(w, 1e-300), 0.0)
+    n = np.where(w > 0, aov[..., 3:6] / np.maximum(w, 1e-300), 0.0)
+    ln = np.linalg.norm(n, axis=-1, keepdims=True)
+    n = np.where(ln > 1e-3, n / np.maximum(ln, 1e-300), 0.0)
+    return alb, n

@@ -158,3 +158,25 @@ def test_wfpt_defaults_and_pt_renderer(native_lib, tmp_path):
     # WavefrontPathTracer::Params defaults (builtin/btrc/builtin/renderer/wavefront.h:13-27)
     assert (info.spp, info.min_depth, info.max_depth, info.state_count) == (128, 5, 10, 1000000)
     assert info.sampler == 0 and info.filter == 0
+
+
+def test_post_processors_parse(native_lib, tmp_path):
+    # a group or an array of post processors (factory/btrc/factory/post_processor.cpp:5-25);
+    # unknown types fail to load, denoise loads (it is refused only when run)
+    base = json.loads(scenes.cornell(out_dir=tmp_path, width=8, height=8, spp=1).read_text())
+    ctx = B.Context(-1)
+    for post, ok in (({"type": "tonemap"}, True),
+                     ([{"type": "tonemap", "exposure": 2}, {"type": "save", "color": "x.png"}], True),
+                     ([{"type": "denoise"}], True),
+                     ([{"type": "blur"}], False),
+                     ("tonemap", False)):
+        sc = dict(base)
+        sc["post_processors"] = post
+        q = tmp_path / "p.json"
+        q.write_text(json.dumps(sc))
+        if ok:
+            ctx.load_scene(q)
+        else:
+            with pytest.raises(B.BtrcError):
+                ctx.load_scene(q)
+    ctx.close()
