@@ -97,6 +97,8 @@ SIGNATURES = {
     "btrc_medium_tr_batch": (C.c_int, [_vp, _vp, C.c_int32, _vp, _vp, C.c_uint64, _vp, _vp]),
     "btrc_tonemap_aces": (C.c_int, [_vp, _vp, C.c_int32, C.c_int32, C.c_int32, C.c_float, _vp]),
     "btrc_image_save": (C.c_int, [_vp, C.c_char_p, _vp, C.c_int32, C.c_int32, C.c_int32, C.c_float]),
+    "btrc_image_load": (C.c_int, [_vp, C.c_char_p, _vp, C.c_uint64, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                  C.POINTER(C.c_int32)]),
 }
 
 _lib = None
@@ -249,6 +251,16 @@ class Context:
         """In-place ACES tone map of a device buffer (tonemap post-processor)."""
         self._check(self._lib.btrc_tonemap_aces(self.handle, _ptr(pixels), width, height, channels, exposure,
                                                 stream))
+
+    def image_load(self, filename: str) -> tuple[np.ndarray, int]:
+        """Decode a .png / .hdr texture file: ((H, W, 4) float32 texels, file channels)."""
+        w, h, c = C.c_int32(), C.c_int32(), C.c_int32()
+        fn = str(filename).encode()
+        self._check(self._lib.btrc_image_load(self.handle, fn, None, 0, C.byref(w), C.byref(h), C.byref(c)))
+        out = np.zeros((h.value, w.value, 4), np.float32)
+        self._check(self._lib.btrc_image_load(self.handle, fn, _ptr(out), out.size, C.byref(w), C.byref(h),
+                                              C.byref(c)))
+        return out, c.value
 
     def image_save(self, filename: str, pixels: np.ndarray, gamma: float = 1.0):
         """Write an (H, W, 3|4) float image to .png / .exr / .hdr (save post-processor)."""

@@ -99,7 +99,8 @@ struct Frame
             ny = cross(nz, V3(0, 1, 0));
         else
             ny = cross(nz, V3(1, 0, 0));
-        return Frame(cross(ny, nz), ny, nz);
+        // x = z cross y, as CFrame::from_z builds it (common/btrc/utils/cmath/cframe.cpp:52-64)
+        return Frame(cross(nz, ny), ny, nz);
     }
     BT_HD V3 local_to_global(V3 l) const { return x * l.x + y * l.y + z * l.z; }
     BT_HD V3 global_to_local(V3 g) const { return V3(dot(g, x), dot(g, y), dot(g, z)); }

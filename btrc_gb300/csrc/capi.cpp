@@ -344,6 +344,17 @@ void build_scene(btrc_scene *sc, int threads)
                                              : dev_upload(sc->allocs, H.volume_nodes.data(), H.volume_nodes.size());
     D.num_volumes = static_cast<int32_t>(vols.size());
     D.media = dev_upload(sc->allocs, meds.data(), meds.size());
+    // textures and the environment map's importance table
+    {
+        const TexStore &T = H.textures;
+        D.tex_images = T.images.empty() ? nullptr : dev_upload(sc->allocs, T.images.data(), T.images.size());
+        D.tex_texels = T.texels.empty() ? nullptr : dev_upload(sc->allocs, T.texels.data(), T.texels.size());
+        D.tex_instr = T.instr.empty() ? nullptr : dev_upload(sc->allocs, T.instr.data(), T.instr.size());
+        D.material_tex = H.material_tex.empty() ? nullptr
+                                                 : dev_upload(sc->allocs, H.material_tex.data(), H.material_tex.size());
+        D.env_probs = H.env_probs.empty() ? nullptr : dev_upload(sc->allocs, H.env_probs.data(), H.env_probs.size());
+        D.env_alias = H.env_alias.empty() ? nullptr : dev_upload(sc->allocs, H.env_alias.data(), H.env_alias.size());
+    }
     D.grids = grids.empty() ? nullptr : dev_upload(sc->allocs, grids.data(), grids.size());
     D.num_media = static_cast<int32_t>(meds.size());
     D.vacuum_medium = H.vacuum_medium;
@@ -1012,6 +1023,41 @@ btrc_status btrc_tonemap_aces(btrc_ctx *ctx, float *d_pixels, int32_t width, int
         check_cuda(launch_tonemap_aces(d_pixels, static_cast<uint32_t>(width) * static_cast<uint32_t>(height), channels,
                                        exposure, pick_stream(ctx, stream)),
                    "tonemap");
+    });
+}
+
+btrc_status btrc_image_load(btrc_ctx *ctx, const char *filename, float *texels, uint64_t capacity, int32_t *width,
+                            int32_t *height, int32_t *channels)
+{
+    if(!filename || !width || !height || !channels)
+        return BTRC_ERR_INVALID_ARG;
+    return guarded(ctx, [&] {
+        LoadedImage img;
+        try
+        {
+            img = load_image(filename);
+        }
+        catch(const UnsupportedFormat &ex)
+        {
+            throw StatusError(BTRC_ERR_UNSUPPORTED, ex.what());
+        }
+        catch(const std::invalid_argument &ex)
+        {
+            throw StatusError(BTRC_ERR_INVALID_ARG, ex.what());
+        }
+        catch(const std::runtime_error &ex)
+        {
+            throw StatusError(BTRC_ERR_IO, ex.what());
+        }
+        *width = img.width;
+        *height = img.height;
+        *channels = img.channels;
+        if(texels)
+        {
+            if(capacity < img.texels.size())
+                throw StatusError(BTRC_ERR_INVALID_ARG, "texel buffer too small");
+            std::memcpy(texels, img.texels.data(), img.texels.size() * sizeof(float));
+        }
     });
 }
 

@@ -35,6 +35,13 @@ struct DevScene
     const VolumePrim *volumes;
     const VolNode *volume_nodes;
     int32_t num_volumes;
+
+    const TexImage *tex_images;
+    const float *tex_texels;   // 4 floats per texel
+    const TexInstr *tex_instr;
+    const MaterialTex *material_tex;
+    const float *env_probs;    // ibl tile probabilities
+    const AliasEntry8 *env_alias;
 };
 
 struct DevRender

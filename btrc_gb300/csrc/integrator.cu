@@ -16,6 +16,7 @@
 
 #include "bsdf.cuh"
 #include "kernels.h"
+#include "texture.h"
 #include "traverse.cuh"
 
 namespace bt {
@@ -183,6 +184,7 @@ struct SurfacePoint
     V3 position;
     Frame frame;
     V3 interp_z;
+    float tu, tv;    // texture coordinate
 };
 
 // get_hitinfo (core/btrc/core/scene.cpp:9-64)
@@ -200,6 +202,8 @@ __device__ SurfacePoint get_hitinfo(const DevScene &S, V3 o, V3 d, const Instanc
     sp.frame = f;
     const V3 in = v3(sa) + v3(sba) * b1 + v3(sca) * b2;
     sp.interp_z = normalize(aff_normal(inst.w2l, in));
+    sp.tu = gx.w + gy.w * b1 + gz.w * b2;
+    sp.tv = sa.w + sba.w * b1 + sca.w * b2;
     return sp;
 }
 
@@ -214,12 +218,71 @@ __device__ __forceinline__ uint32_t alias_sample(const AliasEntry8 *table, uint3
     return s <= e.accept ? i : e.alias;
 }
 
-__device__ __forceinline__ V3 env_le(const EnvLight &env, V3 to_light)
+__device__ __forceinline__ TexTables tex_tables(const DevScene &S)
 {
+    return TexTables{ S.tex_images, S.tex_texels, S.tex_instr };
+}
+
+// IBL::eval_local (builtin/btrc/builtin/light/ibl.cpp:69-77): (phi / 2 pi, theta / pi)
+__device__ __forceinline__ V3 ibl_eval_local(const DevScene &S, V3 d)
+{
+    float phi = 0.0f;
+    if(d.x != 0.0f || d.y != 0.0f)
+    {
+        phi = atan2f(d.y, d.x);
+        phi = phi < 0 ? phi + 2 * PI : phi;
+    }
+    const float theta = acosf(fminf(fmaxf(d.z, -1.0f), 1.0f));
+    const float u = saturate(1 / (2 * PI) * phi);
+    const float v = saturate(1 / PI * theta);
+    return tex_eval(tex_tables(S), S.env.prog, u, v);
+}
+
+__device__ __forceinline__ V3 ibl_to_local(const EnvLight &env, V3 g)
+{
+    return V3(dot(g, V3(env.frame_x[0], env.frame_x[1], env.frame_x[2])),
+              dot(g, V3(env.frame_y[0], env.frame_y[1], env.frame_y[2])), dot(g, V3(env.up[0], env.up[1], env.up[2])));
+}
+
+// EnvirLightSampler::pdf (builtin/btrc/builtin/light/env_sampler.cpp:165-187)
+__device__ float ibl_pdf_local(const DevScene &S, V3 to_light)
+{
+    const V3 dir = normalize(to_light);
+    const float theta = acosf(fminf(fmaxf(dir.z, -1.0f), 1.0f));
+    float phi = 0.0f;
+    if(dir.x != 0.0f || dir.y != 0.0f)
+    {
+        phi = atan2f(dir.y, dir.x);
+        phi = phi < 0 ? phi + 2 * PI : phi;
+    }
+    const float u = phi / (2 * PI), v = theta / PI;
+    const int w = S.env.lut_w, h = S.env.lut_h;
+    const int tx = min(max(static_cast<int>(floorf(u * w)), 0), w - 1);
+    const int ty = min(max(static_cast<int>(floorf(v * h)), 0), h - 1);
+    const float tile_pdf = S.env_probs[ty * w + tx];
+    const float u0 = static_cast<float>(tx) / w, u1 = static_cast<float>(tx + 1) / w;
+    const float v0 = static_cast<float>(ty) / h, v1 = static_cast<float>(ty + 1) / h;
+    const float c0 = cosf(PI * v0), c1 = cosf(PI * v1);
+    return tile_pdf * (1.0f / fabsf(2 * PI * (u1 - u0) * (c1 - c0)));
+}
+
+__device__ __forceinline__ V3 env_le(const DevScene &S, V3 to_light)
+{
+    const EnvLight &env = S.env;
+    if(env.type == ENV_IBL)
+        return ibl_eval_local(S, normalize(ibl_to_local(env, to_light)));
     const V3 up(env.up[0], env.up[1], env.up[2]);
     const float c = dot(up, normalize(to_light));
     const float s = saturate(0.5f * (c + 1.0f));
     return V3(env.lower[0], env.lower[1], env.lower[2]) * (1.0f - s) + V3(env.upper[0], env.upper[1], env.upper[2]) * s;
+}
+
+// pdf_li of the environment light (solid angle): uniform sphere for gradient_sky
+__device__ __forceinline__ float env_pdf(const DevScene &S, V3 to_light)
+{
+    if(S.env.type == ENV_IBL)
+        return ibl_pdf_local(S, ibl_to_local(S.env, to_light));
+    return 1.0f / (4.0f * PI);
 }
 
 struct LightSample
@@ -273,6 +336,36 @@ __device__ LightSample sample_light(const DevScene &S, V3 ref_pos, V3 ref_nor, b
         r.li = rad;
         r.light_pdf = select_pdf * pdf_sa;
     }
+    else if(S.env.type == ENV_IBL)
+    {
+        // IBL::sample_li_inline (ibl.cpp:31-42) over EnvirLightSampler::sample (env_sampler.cpp:137-163)
+        const int w = S.env.lut_w, h = S.env.lut_h;
+        const uint32_t tile = alias_sample(S.env_alias, static_cast<uint32_t>(w * h), s0);
+        const int ty = static_cast<int>(tile) / w, tx = static_cast<int>(tile) % w;
+        const float tile_pdf = S.env_probs[tile];
+        const float u0 = static_cast<float>(tx) / w, u1 = static_cast<float>(tx + 1) / w;
+        const float v0 = static_cast<float>(ty) / h, v1 = static_cast<float>(ty + 1) / h;
+        float cv0 = cosf(PI * v0), cv1 = cosf(PI * v1);
+        if(cv0 > cv1)
+        {
+            const float t = cv0;
+            cv0 = cv1;
+            cv1 = t;
+        }
+        const float cos_theta = cv0 + s2 * (cv1 - cv0);
+        const float sin_theta = cos2sin(cos_theta);
+        const float phi = 2 * PI * (u0 + (u1 - u0) * s1);
+        const V3 local(sin_theta * cosf(phi), sin_theta * sinf(phi), cos_theta);
+        const float in_tile_pdf = 1.0f / (2 * PI * (u1 - u0) * (cv1 - cv0));
+        const V3 dir = V3(S.env.frame_x[0], S.env.frame_x[1], S.env.frame_x[2]) * local.x +
+                       V3(S.env.frame_y[0], S.env.frame_y[1], S.env.frame_y[2]) * local.y +
+                       V3(S.env.up[0], S.env.up[1], S.env.up[2]) * local.z;
+        r.o = offset_origin ? offset_dir(ref_pos, ref_nor, dir) : ref_pos;
+        r.d = dir;
+        r.t1 = MAX_FLOAT;
+        r.li = ibl_eval_local(S, local);
+        r.light_pdf = select_pdf * (tile_pdf * in_tile_pdf);
+    }
     else
     {
         // GradientSky::sample_li_inline (builtin/btrc/builtin/light/gradient_sky.cpp:28-35)
@@ -280,7 +373,7 @@ __device__ LightSample sample_light(const DevScene &S, V3 ref_pos, V3 ref_nor, b
         r.o = offset_origin ? offset_dir(ref_pos, ref_nor, dir) : ref_pos;
         r.d = dir;
         r.t1 = MAX_FLOAT;
-        r.li = env_le(S.env, dir);
+        r.li = env_le(S, dir);
         r.light_pdf = select_pdf * (1.0f / (4.0f * PI));
     }
     r.success = true;
@@ -292,10 +385,10 @@ __device__ __forceinline__ V3 miss_le(const DevScene &S, V3 d, V3 beta_le, float
 {
     if(S.env.type == ENV_NONE)
         return V3(0);
-    const V3 le = env_le(S.env, d);
+    const V3 le = env_le(S, d);
     if(bsdf_pdf < 0)
         return beta_le * le / -bsdf_pdf;
-    const float light_pdf = (1.0f / static_cast<float>(S.num_lights)) * (1.0f / (4.0f * PI));
+    const float light_pdf = (1.0f / static_cast<float>(S.num_lights)) * env_pdf(S, d);
     return beta_le * le / (bsdf_pdf + light_pdf);
 }
 
@@ -1008,6 +1101,33 @@ __global__ void __launch_bounds__(BLOCK) k_medium(DevScene S, DevRender R, PathS
     }
 }
 
+// Texture2D parameters of a material sampled at the hit's texture coordinate (every
+// material creator's context.create<Texture2D>), then the normal map
+// (builtin/btrc/builtin/material/utils/normal_map.cpp:13-21): n = 2 tex - 1 in the shading
+// frame, which is rotated onto it
+__device__ __noinline__ void apply_material_textures(const DevScene &S, const SurfacePoint &sp, Material &mat,
+                                                     Frame &shading)
+{
+    const MaterialTex &mt = S.material_tex[mat.tex];
+    const TexTables T = tex_tables(S);
+    if(mt.prog[0] >= 0)
+    {
+        const V3 c = tex_eval(T, mt.prog[0], sp.tu, sp.tv);
+        mat.p[0] = c.x;
+        mat.p[1] = c.y;
+        mat.p[2] = c.z;
+    }
+#pragma unroll
+    for(int k = 3; k < 16; ++k)
+        if(mt.prog[k] >= 0)
+            mat.p[k] = tex_eval(T, mt.prog[k], sp.tu, sp.tv).x;
+    if(mt.normal >= 0)
+    {
+        const V3 ln = 2.0f * tex_eval(T, mt.normal, sp.tu, sp.tv) - V3(1.0f);
+        shading = shading.rotate_to_new_z(normalize(shading.local_to_global(ln)));
+    }
+}
+
 // ShadePipeline (builtin/btrc/builtin/renderer/wavefront/shade.cpp:29-235)
 __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, DevRender R, PathSoA P, PathSoA N, ShadowSoA SH,
                                                  const uint32_t *flags, const HitDetail *hits, float4 *film,
@@ -1060,10 +1180,12 @@ __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, DevRender R, PathSo
 
         LightSample ls = sample_light(S, sp.position, sp.frame.z, true, smp);
 
-        const Material mat = S.materials[inst.material];
+        Material mat = S.materials[inst.material];
         SurfaceShader sh;
         sh.frame.geometry = sp.frame;
         sh.frame.shading = sp.frame.rotate_to_new_z(sp.interp_z);
+        if(mat.tex >= 0)
+            apply_material_textures(S, sp, mat, sh.frame.shading);
         sh.mat = make_material_eval(mat);
         sh.shadow_terminator = mat.shadow_terminator != 0;
 

@@ -77,7 +77,61 @@ enum MaterialType : int32_t
     MAT_GLASS = 6,
 };
 
-// Material parameters (constant textures only).
+// ---- 2D textures (core/btrc/core/texture2d.h, builtin/btrc/builtin/texture2d/*)
+// An image texture: RGBA float texels (8-bit files already divided by 255 and, with
+// srgb_to_linear, decoded), sampled in normalised coordinates like a CUDA texture object.
+enum TexAddress : int32_t
+{
+    TEX_WRAP = 0,
+    TEX_CLAMP = 1,
+    TEX_MIRROR = 2,
+    TEX_BORDER = 3,
+};
+
+struct alignas(16) TexImage
+{
+    int32_t offset;          // first texel (float4 index) in the texel pool
+    int32_t width, height;
+    int32_t filter;          // 0 point, 1 linear
+    int32_t address_u, address_v;
+    int32_t pad[2];
+    float border[4];
+};
+
+// One instruction of a texture program (postfix): constants and image samples push an RGB
+// value, the binary operators of texture2d/math.cpp pop two and push one. uv transforms
+// (texture2d/transform.cpp) are folded into the sample instruction's affine map.
+enum TexOp : int32_t
+{
+    TEXOP_END = 0,
+    TEXOP_CONST = 1,
+    TEXOP_SAMPLE = 2,
+    TEXOP_ADD = 3,
+    TEXOP_SUB = 4,
+    TEXOP_MUL = 5,
+    TEXOP_DIV = 6,
+};
+
+struct alignas(16) TexInstr
+{
+    int32_t op;
+    int32_t image;           // TEXOP_SAMPLE: index into the image table
+    float a[6];              // CONST: rgb in a[0..2]; SAMPLE: u' = a0 u + a1 v + a2, v' = a3 u + a4 v + a5
+};
+
+constexpr int TEX_STACK = 8;
+
+// Textured parameters of one material: prog[k] is the first instruction of the program
+// that replaces p[k] (k = 0 covers the colour p[0..2]), -1 where p[k] is a constant;
+// normal is the normal map's program (material/utils/normal_map.cpp), or -1.
+struct alignas(16) MaterialTex
+{
+    int32_t prog[16];
+    int32_t normal;
+    int32_t pad[3];
+};
+
+// Material parameters (constants, or the values of the textures in MaterialTex).
 //   diffuse: p[0..2] albedo
 //   metal  : p[0..2] R0, p[3] roughness, p[4] anisotropic
 //   disney : p[0..2] base color, p[3] metallic, p[4] roughness, p[5] specular,
@@ -91,7 +145,8 @@ struct alignas(16) Material
     int32_t type;
     int32_t shadow_terminator;
     float p[16];
-    int32_t pad[2];
+    int32_t tex;             // row of the MaterialTex table, -1: all parameters constant
+    int32_t pad;
 };
 
 struct alignas(16) Instance
@@ -132,15 +187,24 @@ enum EnvType : int32_t
 {
     ENV_NONE = 0,
     ENV_GRADIENT_SKY = 1,
+    ENV_IBL = 2,
 };
 
+// Environment light: gradient_sky (builtin/btrc/builtin/light/gradient_sky.cpp) or ibl
+// (builtin/btrc/builtin/light/ibl.cpp + env_sampler.cpp): a texture program over the
+// (phi / 2 pi, theta / pi) parameterisation of the local frame (frame_x/y/up = from_z(up))
+// and a lut_w x lut_h table of tile probabilities with its alias table.
 struct alignas(16) EnvLight
 {
     int32_t type;
     float lower[3];
     float upper[3];
     float up[3];
-    float pad[2];
+    float frame_x[3];
+    float frame_y[3];
+    int32_t prog;            // ibl texture program
+    int32_t lut_w, lut_h;
+    int32_t pad;
 };
 
 enum MediumType : int32_t

@@ -522,72 +522,116 @@ std::string resolve_path(const std::string &p, const std::string &scene_dir)
     return fp.lexically_normal().string();
 }
 
-float tex_float(const NodeP &n, float def_if_null)
+// Material parameters from Texture2D nodes: constants go to p[k]; other textures compile
+// to programs recorded in the material's MaterialTex row (k = 0 is the RGB colour).
+struct ParamSink
 {
-    if(!n)
-        return def_if_null;
-    if(n->is_value() || n->is_array())
-        return json::as_spectrum(n).x;  // Constant2D::sample_float returns .r
-    const std::string type = json::as_string(n->child("type"));
-    if(type == "constant")
-        return json::as_spectrum(n->child("value")).x;
-    throw std::runtime_error("unsupported texture2d type '" + type + "' (only constant textures)");
-}
+    TexStore &T;
+    Material &m;
+    MaterialTex &mt;
+    bool textured = false;
 
-V3 tex_spectrum(const NodeP &n)
-{
-    if(n->is_value() || n->is_array())
-        return json::as_spectrum(n);
-    const std::string type = json::as_string(n->child("type"));
-    if(type == "constant")
-        return json::as_spectrum(n->child("value"));
-    throw std::runtime_error("unsupported texture2d type '" + type + "' (only constant textures)");
-}
+    void spectrum(int k, const NodeP &n)
+    {
+        V3 c;
+        const int prog = compile_texture2d(T, n, c);
+        if(prog < 0)
+        {
+            m.p[k] = c.x; m.p[k + 1] = c.y; m.p[k + 2] = c.z;
+        }
+        else
+        {
+            mt.prog[k] = prog;
+            textured = true;
+        }
+    }
+    // a float parameter reads the texture's red channel (Texture2D::sample_float)
+    void scalar(int k, const NodeP &n, float def_if_null)
+    {
+        if(!n)
+        {
+            m.p[k] = def_if_null;
+            return;
+        }
+        V3 c;
+        const int prog = compile_texture2d(T, n, c);
+        if(prog < 0)
+            m.p[k] = c.x;
+        else
+        {
+            mt.prog[k] = prog;
+            textured = true;
+        }
+    }
+};
 
-Material make_material(const NodeP &n)
+Material make_material(const NodeP &n, TexStore &T, std::vector<MaterialTex> &rows)
 {
     Material m{};
+    MaterialTex mt;
+    for(int &k : mt.prog)
+        k = -1;
+    mt.normal = -1;
+    mt.pad[0] = mt.pad[1] = mt.pad[2] = 0;
+    ParamSink P{ T, m, mt };
     const std::string type = json::as_string(n->child("type"));
     m.shadow_terminator = json::bool_or(n, "shadow_terminator_term", true) ? 1 : 0;
-    if(n->find("normal_map") || n->find("normal"))
+    // NormalMap::load (builtin/btrc/builtin/material/utils/normal_map.cpp:5-11): the
+    // "normal" texture of diffuse, metal, disney, glass and mirror
+    if(type == "diffuse" || type == "metal" || type == "disney" || type == "glass" || type == "mirror")
     {
-        // normal maps need image textures, which are not supported yet
-        auto nm = n->find("normal_map") ? n->find("normal_map") : n->find("normal");
-        if(!nm->is_value() || !nm->str.empty())
-            throw std::runtime_error("normal maps are not supported");
+        if(auto nn = n->find("normal"))
+        {
+            V3 c;
+            const int prog = compile_texture2d(T, nn, c);
+            if(prog < 0)
+            {
+                // a constant normal map: one instruction holding the constant
+                TexInstr ins{};
+                ins.op = TEXOP_CONST;
+                ins.a[0] = c.x; ins.a[1] = c.y; ins.a[2] = c.z;
+                TexInstr end{};
+                end.op = TEXOP_END;
+                mt.normal = static_cast<int>(T.instr.size());
+                T.instr.push_back(ins);
+                T.instr.push_back(end);
+            }
+            else
+                mt.normal = prog;
+            P.textured = true;
+        }
     }
     if(type == "diffuse")
     {
         m.type = MAT_DIFFUSE;
-        const V3 c = tex_spectrum(n->child("color"));
-        m.p[0] = c.x; m.p[1] = c.y; m.p[2] = c.z;
+        P.spectrum(0, n->child("color"));
     }
     else if(type == "metal")
     {
+        // builtin/btrc/builtin/material/metal.cpp:50-78
         m.type = MAT_METAL;
-        const V3 c = tex_spectrum(n->child("color"));
-        m.p[0] = c.x; m.p[1] = c.y; m.p[2] = c.z;
-        m.p[3] = tex_float(n->child("roughness"), 0);
-        m.p[4] = tex_float(n->find("anisotropic"), 0);
+        P.spectrum(0, n->child("color"));
+        P.scalar(3, n->child("roughness"), 0);
+        P.scalar(4, n->find("anisotropic"), 0);
     }
     else if(type == "disney")
     {
         // builtin/btrc/builtin/material/disney.cpp:844-894 creator defaults
         m.type = MAT_DISNEY;
-        const V3 c = tex_spectrum(n->child("color"));
-        m.p[0] = c.x; m.p[1] = c.y; m.p[2] = c.z;
-        m.p[3] = tex_float(n->child("metallic"), 0);
-        m.p[4] = tex_float(n->child("roughness"), 0);
-        m.p[5] = tex_float(n->find("specular"), 1);
-        m.p[6] = tex_float(n->find("specular_tint"), 0);
-        m.p[7] = tex_float(n->find("anisotropic"), 0);
-        m.p[8] = tex_float(n->find("sheen"), 0);
-        m.p[9] = tex_float(n->find("sheen_tint"), 0);
-        m.p[10] = tex_float(n->find("clearcoat"), 0);
-        m.p[11] = tex_float(n->find("clearcoat_gloss"), 1);
-        m.p[12] = tex_float(n->find("transmission"), 0);
-        m.p[13] = n->find("transmission_roughness") ? tex_float(n->find("transmission_roughness"), 0) : m.p[4];
-        m.p[14] = tex_float(n->find("ior"), 1.5f);
+        P.spectrum(0, n->child("color"));
+        P.scalar(3, n->child("metallic"), 0);
+        P.scalar(4, n->child("roughness"), 0);
+        P.scalar(5, n->find("specular"), 1);
+        P.scalar(6, n->find("specular_tint"), 0);
+        P.scalar(7, n->find("anisotropic"), 0);
+        P.scalar(8, n->find("sheen"), 0);
+        P.scalar(9, n->find("sheen_tint"), 0);
+        P.scalar(10, n->find("clearcoat"), 0);
+        P.scalar(11, n->find("clearcoat_gloss"), 1);
+        P.scalar(12, n->find("transmission"), 0);
+        // transmission_roughness defaults to the roughness texture
+        P.scalar(13, n->find("transmission_roughness") ? n->find("transmission_roughness") : n->child("roughness"), 0);
+        P.scalar(14, n->find("ior"), 1.5f);
     }
     else if(type == "black")
         m.type = MAT_BLACK;
@@ -596,19 +640,23 @@ Material make_material(const NodeP &n)
     else if(type == "mirror")
     {
         m.type = MAT_MIRROR;
-        const V3 c = tex_spectrum(n->child("color"));
-        m.p[0] = c.x; m.p[1] = c.y; m.p[2] = c.z;
+        P.spectrum(0, n->child("color"));
     }
     else if(type == "glass")
     {
         // builtin/btrc/builtin/material/glass.cpp:117-129
         m.type = MAT_GLASS;
-        const V3 c = tex_spectrum(n->child("color"));
-        m.p[0] = c.x; m.p[1] = c.y; m.p[2] = c.z;
-        m.p[3] = tex_float(n->child("ior"), 1.5f);
+        P.spectrum(0, n->child("color"));
+        P.scalar(3, n->child("ior"), 1.5f);
     }
     else
         throw std::runtime_error("unsupported material type '" + type + "'");
+    m.tex = -1;
+    if(P.textured)
+    {
+        m.tex = static_cast<int32_t>(rows.size());
+        rows.push_back(mt);
+    }
     return m;
 }
 
@@ -1068,6 +1116,7 @@ HostScene load_scene(const std::string &path)
     std::map<const json::Node *, int> geo_pool, mat_pool;
     MediumBuilder mb;
     mb.scene_dir = scene_dir;
+    S.textures.scene_dir = scene_dir;
     struct PendingInstance { int geo, mat, light; int inner, outer; Transform xf; V3 intensity; };
     std::vector<PendingInstance> pend;
     for(auto &e : ents->elems)
@@ -1093,7 +1142,7 @@ HostScene load_scene(const std::string &path)
         auto mit = mat_pool.find(mn.get());
         if(mit == mat_pool.end())
         {
-            S.materials.push_back(make_material(mn));
+            S.materials.push_back(make_material(mn, S.textures, S.material_tex));
             pi.mat = static_cast<int>(S.materials.size()) - 1;
             mat_pool[mn.get()] = pi.mat;
         }
@@ -1127,15 +1176,47 @@ HostScene load_scene(const std::string &path)
     if(auto en = scene->find("envir_light"))
     {
         const std::string et = json::as_string(en->child("type"));
-        if(et != "gradient_sky")
+        if(et == "gradient_sky")
+        {
+            S.env.type = ENV_GRADIENT_SKY;
+            const V3 up = normalize(json::as_vec3(en->child("up")));
+            const V3 lo = json::as_spectrum(en->child("lower"));
+            const V3 hi = json::as_spectrum(en->child("upper"));
+            S.env.lower[0] = lo.x; S.env.lower[1] = lo.y; S.env.lower[2] = lo.z;
+            S.env.upper[0] = hi.x; S.env.upper[1] = hi.y; S.env.upper[2] = hi.z;
+            S.env.up[0] = up.x; S.env.up[1] = up.y; S.env.up[2] = up.z;
+        }
+        else if(et == "ibl")
+        {
+            // IBLCreator (builtin/btrc/builtin/light/ibl.cpp:80-91)
+            S.env.type = ENV_IBL;
+            V3 c;
+            int prog = compile_texture2d(S.textures, en->child("tex"), c);
+            if(prog < 0)
+            {
+                TexInstr ins{};
+                ins.op = TEXOP_CONST;
+                ins.a[0] = c.x; ins.a[1] = c.y; ins.a[2] = c.z;
+                TexInstr end{};
+                end.op = TEXOP_END;
+                prog = static_cast<int>(S.textures.instr.size());
+                S.textures.instr.push_back(ins);
+                S.textures.instr.push_back(end);
+            }
+            S.env.prog = prog;
+            const V3 up = en->find("up") ? json::as_vec3(en->child("up")) : V3(0, 0, 1);
+            const Frame f = Frame::from_z(up);
+            S.env.frame_x[0] = f.x.x; S.env.frame_x[1] = f.x.y; S.env.frame_x[2] = f.x.z;
+            S.env.frame_y[0] = f.y.x; S.env.frame_y[1] = f.y.y; S.env.frame_y[2] = f.y.z;
+            S.env.up[0] = f.z.x; S.env.up[1] = f.z.y; S.env.up[2] = f.z.z;
+            S.env.lut_w = json::int_or(en, "lut_width", 400);
+            S.env.lut_h = json::int_or(en, "lut_height", 200);
+            if(S.env.lut_w <= 0 || S.env.lut_h <= 0 || S.env.lut_w > 8192 || S.env.lut_h > 8192)
+                throw std::runtime_error("ibl lut size out of range");
+            build_env_sampler(S.textures, prog, S.env.lut_w, S.env.lut_h, S.env_probs, S.env_alias);
+        }
+        else
             throw std::runtime_error("unsupported environment light '" + et + "'");
-        S.env.type = ENV_GRADIENT_SKY;
-        const V3 up = normalize(json::as_vec3(en->child("up")));
-        const V3 lo = json::as_spectrum(en->child("lower"));
-        const V3 hi = json::as_spectrum(en->child("upper"));
-        S.env.lower[0] = lo.x; S.env.lower[1] = lo.y; S.env.lower[2] = lo.z;
-        S.env.upper[0] = hi.x; S.env.upper[1] = hi.y; S.env.upper[2] = hi.z;
-        S.env.up[0] = up.x; S.env.up[1] = up.y; S.env.up[2] = up.z;
     }
 
     // medium id table (core/btrc/core/scene.cpp:136-161): media sorted by priority

@@ -9,6 +9,7 @@
 
 #include "json.h"
 #include "layout.h"
+#include "textures.h"
 
 namespace bt {
 
@@ -104,6 +105,10 @@ struct HostScene
     std::vector<Instance> instances;
     std::vector<Transform> instance_xf;
     std::vector<Material> materials;
+    std::vector<MaterialTex> material_tex;  // rows referenced by Material::tex
+    TexStore textures;                       // images, texels and texture programs
+    std::vector<float> env_probs;            // ibl tile probabilities (lut_w * lut_h)
+    std::vector<AliasEntry8> env_alias;
     std::vector<AreaLight> area_lights;
     EnvLight env{};
     std::vector<HostMedium> media;   // index 0 .. n-1; vacuum (volume-primitive medium) included

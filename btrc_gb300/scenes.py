@@ -22,6 +22,7 @@ Every random choice draws from numpy's PCG64 seeded with the scene seed.
 from __future__ import annotations
 
 import json
+import struct
 import os
 from pathlib import Path
 
@@ -67,12 +68,22 @@ def icosphere(level: int) -> tuple[np.ndarray, np.ndarray]:
     return np.array(verts), np.array(faces, np.int64)
 
 
-def write_obj(path: Path, verts: np.ndarray, faces: np.ndarray, normals: np.ndarray | None = None) -> None:
-    """OBJ with 1-based indices; with normals, faces are written as a//a."""
+def write_obj(path: Path, verts: np.ndarray, faces: np.ndarray, normals: np.ndarray | None = None,
+              uvs: np.ndarray | None = None) -> None:
+    """OBJ with 1-based indices; with normals, faces are written as a//a, with normals and
+    per-vertex texture coordinates as a/a/a."""
     verts = np.asarray(verts, np.float64)
     faces = np.asarray(faces, np.int64) + 1
     parts = [("v %.7g %.7g %.7g\n" * len(verts)) % tuple(verts.ravel())]
-    if normals is not None:
+    if uvs is not None:
+        assert normals is not None
+        normals = np.asarray(normals, np.float64)
+        uvs = np.asarray(uvs, np.float64)
+        parts.append(("vt %.7g %.7g\n" * len(uvs)) % tuple(uvs.ravel()))
+        parts.append(("vn %.6g %.6g %.6g\n" * len(normals)) % tuple(normals.ravel()))
+        ff = np.repeat(faces, 3, axis=1)
+        parts.append(("f %d/%d/%d %d/%d/%d %d/%d/%d\n" * len(faces)) % tuple(ff.ravel()))
+    elif normals is not None:
         normals = np.asarray(normals, np.float64)
         parts.append(("vn %.6g %.6g %.6g\n" * len(normals)) % tuple(normals.ravel()))
         ff = np.repeat(faces, 2, axis=1)
@@ -84,6 +95,93 @@ def write_obj(path: Path, verts: np.ndarray, faces: np.ndarray, normals: np.ndar
         for p in parts:
             fobj.write(p)
     os.replace(tmp, path)
+
+
+def write_png(path: Path, img: np.ndarray, depth: int = 8, palette: np.ndarray | None = None,
+              alpha: np.ndarray | None = None) -> None:
+    """PNG writer for test textures: 8/16-bit grey (H, W), RGB (H, W, 3) or RGBA (H, W, 4),
+    low-depth grey (depth 1/2/4), or palette indices (H, W) with `palette` (N, 3) and an
+    optional tRNS `alpha`. Rows cycle through the five filter types; zlib level 6."""
+    import zlib
+    img = np.asarray(img)
+    h, w = img.shape[:2]
+    if palette is not None:
+        ctype, samples = 3, 1
+    else:
+        samples = 1 if img.ndim == 2 else img.shape[2]
+        ctype = {1: 0, 3: 2, 4: 6}[samples]
+    if depth < 8:
+        bits = np.unpackbits(img.astype(np.uint8)[..., None], axis=-1)[..., 8 - depth:]
+        rows = np.packbits(bits.reshape(h, -1), axis=1)
+    elif depth == 16:
+        rows = img.astype(">u2").reshape(h, -1).view(np.uint8).reshape(h, -1)
+    else:
+        rows = img.astype(np.uint8).reshape(h, -1)
+    bpp = max(1, samples * depth // 8)
+    out = bytearray()
+    prev = np.zeros(rows.shape[1], np.int32)
+    for y in range(h):
+        cur = rows[y].astype(np.int32)
+        ft = y % 5
+        left = np.concatenate([np.zeros(bpp, np.int32), cur[:-bpp]])
+        ul = np.concatenate([np.zeros(bpp, np.int32), prev[:-bpp]])
+        if ft == 0:
+            f = cur
+        elif ft == 1:
+            f = cur - left
+        elif ft == 2:
+            f = cur - prev
+        elif ft == 3:
+            f = cur - (left + prev) // 2
+        else:
+            pa, pb, pc = np.abs(prev - ul), np.abs(left - ul), np.abs(left + prev - 2 * ul)
+            pred = np.where((pa <= pb) & (pa <= pc), left, np.where(pb <= pc, prev, ul))
+            f = cur - pred
+        out.append(ft)
+        out += (f & 255).astype(np.uint8).tobytes()
+        prev = cur
+
+    def chunk(t, d):
+        return struct.pack(">I", len(d)) + t + d + struct.pack(">I", zlib.crc32(t + d) & 0xffffffff)
+    data = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, ctype, 0, 0, 0))
+    if palette is not None:
+        data += chunk(b"PLTE", np.asarray(palette, np.uint8).tobytes())
+        if alpha is not None:
+            data += chunk(b"tRNS", np.asarray(alpha, np.uint8).tobytes())
+    data += chunk(b"IDAT", zlib.compress(bytes(out), 6)) + chunk(b"IEND", b"")
+    Path(path).write_bytes(data)
+
+
+def write_hdr(path: Path, rgb: np.ndarray) -> None:
+    """Radiance RGBE file, adaptive run-length encoded scanlines."""
+    rgb = np.maximum(np.asarray(rgb, np.float64), 0)
+    h, w = rgb.shape[:2]
+    m = rgb.max(-1)
+    e = np.where(m > 1e-32, np.floor(np.log2(np.maximum(m, 1e-32))) + 1, 0)
+    scale = np.where(m > 1e-32, 256.0 / np.exp2(e), 0)
+    rgbe = np.zeros((h, w, 4), np.uint8)
+    rgbe[..., :3] = np.clip(rgb * scale[..., None], 0, 255).astype(np.uint8)
+    rgbe[..., 3] = np.where(m > 1e-32, e + 128, 0).astype(np.uint8)
+    out = bytearray(f"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n-Y {h} +X {w}\n".encode())
+    for y in range(h):
+        out += bytes([2, 2, w >> 8, w & 255])
+        for c in range(4):
+            row = rgbe[y, :, c]
+            x = 0
+            while x < w:
+                run = 1
+                while x + run < w and run < 127 and row[x + run] == row[x]:
+                    run += 1
+                if run >= 4:
+                    out += bytes([128 + run, row[x]])
+                    x += run
+                else:
+                    n = 1
+                    while x + n < w and n < 128 and not (x + n + 2 < w and row[x + n] == row[x + n + 1] == row[x + n + 2]):
+                        n += 1
+                    out += bytes([n]) + row[x:x + n].tobytes()
+                    x += n
+    Path(path).write_bytes(bytes(out))
 
 
 def quad(size: float = 1.0) -> tuple[np.ndarray, np.ndarray]:
@@ -497,3 +595,103 @@ def volume(seed: int = 1002, width: int = 1024, height: int = 1024, spp: int = 6
         "scene": {"entities": ents},
     }
     return _write_scene(out / name, scene)
+
+
+def _sphere_uv(level: int):
+    """Icosphere with spherical texture coordinates (u from the azimuth, v from the polar
+    angle); normals are the positions."""
+    v, f = icosphere(level)
+    u = np.arctan2(v[:, 2], v[:, 0]) / (2 * np.pi) + 0.5
+    t = np.arccos(np.clip(v[:, 1], -1, 1)) / np.pi
+    return v, f, np.stack([u, t], 1)
+
+
+def textured(seed: int = 1003, width: int = 256, height: int = 192, spp: int = 64, out_dir: Path | None = None,
+             force: bool = False, lut: tuple[int, int] = (64, 32)) -> Path:
+    """Image textures, texture expressions, normal maps and an HDR environment light:
+    a checker-textured, bump-mapped ground (sRGB PNG, wrap / mirror addressing), a Disney
+    sphere whose colour is a palette PNG times a constant and whose roughness is a rotated,
+    scaled 16-bit PNG, a metal sphere with a 4-bit border-addressed roughness map plus a
+    constant, and a glass sphere with a constant normal map, all lit by an `ibl` light over
+    a run-length-encoded Radiance HDR sky (builtin/btrc/builtin/light/ibl.cpp)."""
+    out = Path(out_dir or cache_dir() / f"textured-{seed}")
+    out.mkdir(parents=True, exist_ok=True)
+    name = f"scene-{width}x{height}-{spp}-{lut[0]}x{lut[1]}.json"
+    if (out / name).exists() and not force:
+        return out / name
+    rng = np.random.default_rng(seed)
+    # textures
+    yy, xx = np.mgrid[0:64, 0:64]
+    chk = ((xx // 8 + yy // 8) % 2).astype(np.float64)
+    c0, c1 = rng.uniform(0.1, 0.4, 3), rng.uniform(0.6, 0.95, 3)
+    rgb = chk[..., None] * c1 + (1 - chk[..., None]) * c0 + rng.uniform(-0.03, 0.03, (64, 64, 3))
+    write_png(out / "checker.png", np.clip(rgb * 255, 0, 255).astype(np.uint8))
+    hy, hx = np.mgrid[0:32, 0:32] / 32.0
+    hgt = 0.5 * np.sin(2 * np.pi * 3 * hx) * np.cos(2 * np.pi * 2 * hy)
+    gx, gy = np.gradient(hgt, 1 / 32.0)
+    nrm = np.stack([-gx * 0.05, -gy * 0.05, np.ones_like(hgt)], -1)
+    nrm /= np.linalg.norm(nrm, axis=-1, keepdims=True)
+    rgba = np.concatenate([(nrm * 0.5 + 0.5) * 255, np.full((32, 32, 1), 255.0)], -1)
+    write_png(out / "bumps.png", np.clip(rgba, 0, 255).astype(np.uint8))
+    pal = rng.integers(30, 255, (8, 3))
+    write_png(out / "palette.png", rng.integers(0, 8, (16, 16)), palette=pal, alpha=[255, 200, 255, 128])
+    write_png(out / "rough16.png", rng.integers(5000, 60000, (32, 32)), depth=16)
+    write_png(out / "rough4.png", rng.integers(0, 16, (16, 16)), depth=4)
+    ey, ex = np.mgrid[0:64, 0:128]
+    theta = (ey + 0.5) / 64 * np.pi
+    phi = (ex + 0.5) / 128 * 2 * np.pi
+    sky = np.stack([0.3 + 0.5 * np.cos(theta).clip(0), 0.45 + 0.5 * np.cos(theta).clip(0), 0.7 + 0.4 * np.cos(theta).clip(0)], -1)
+    sky[theta > np.pi / 2] = [0.12, 0.1, 0.08]
+    sun = np.exp(-((theta - 0.6) ** 2 + (phi - 1.3) ** 2) / 0.01)
+    sky += sun[..., None] * np.array([60.0, 55.0, 45.0])
+    write_hdr(out / "sky.hdr", sky)
+    # geometry
+    qv = np.array([[-2, 0, -2], [2, 0, -2], [2, 0, 2], [-2, 0, 2]], np.float64)
+    qf = np.array([[0, 2, 1], [0, 3, 2]], np.int64)
+    quv = np.array([[0, 0], [3, 0], [3, 3], [0, 3]], np.float64)
+    write_obj(out / "ground.obj", qv, qf, normals=np.tile([[0, 1, 0]], (4, 1)), uvs=quv)
+    sv, sf, suv = _sphere_uv(4)
+    write_obj(out / "sphere_uv.obj", sv, sf, normals=sv, uvs=suv)
+
+    def arr(fn, **kw):
+        d = {"type": "array", "filename": "$env{scene_directory}/" + fn}
+        d.update(kw)
+        return d
+    ents = [
+        _entity({"type": "triangle_mesh", "filename": "$env{scene_directory}/ground.obj"},
+                {"type": "diffuse",
+                 "color": arr("checker.png", srgb_to_linear=True, address_mode_u="wrap", address_mode_v="mirror"),
+                 "normal": arr("bumps.png", address_mode_u="wrap", address_mode_v="wrap")},
+                [{"translate": [0.0, -0.3, 0.0]}]),
+        _entity({"type": "triangle_mesh", "filename": "$env{scene_directory}/sphere_uv.obj"},
+                {"type": "disney",
+                 "color": {"type": "mul", "lhs": arr("palette.png", filter="point", address_mode_u="wrap"),
+                           "rhs": [0.9, 0.85, 0.8]},
+                 "metallic": 0.0,
+                 "roughness": {"type": "transform", "transform": [{"scale": [2, 2]}, {"rotate": {"angle": {"deg": 30}}}],
+                               "tex": arr("rough16.png", address_mode_u="wrap", address_mode_v="wrap")},
+                 "clearcoat": 0.3},
+                [{"scale": [0.3, 0.3, 0.3]}, {"translate": [-0.7, 0.0, 0.0]}]),
+        _entity({"type": "triangle_mesh", "filename": "$env{scene_directory}/sphere_uv.obj"},
+                {"type": "metal", "color": [0.9, 0.7, 0.5],
+                 "roughness": {"type": "add", "lhs": arr("rough4.png", address_mode_u="border", address_mode_v="border",
+                                                          border=0.2),
+                               "rhs": 0.05}},
+                [{"scale": [0.3, 0.3, 0.3]}]),
+        _entity({"type": "triangle_mesh", "filename": "$env{scene_directory}/sphere_uv.obj"},
+                {"type": "glass", "color": [1.0, 1.0, 1.0], "ior": 1.5, "normal": [0.5, 0.5, 1.0]},
+                [{"scale": [0.3, 0.3, 0.3]}, {"translate": [0.7, 0.0, 0.0]}]),
+    ]
+    scene = {
+        "width": width, "height": height,
+        "camera": {"type": "pinhole", "eye": [0.0, 0.45, 2.2], "dst": [0.0, -0.05, 0.0], "up": [0.0, 1.0, 0.0],
+                   "fov_y": {"deg": 40.0}},
+        "renderer": {"type": "wfpt", "spp": spp, "min_depth": 3, "max_depth": 8, "rr_threshold": 0.1,
+                     "rr_cont_prob": 0.5, "state_count": 1000000, "sampler": "halton",
+                     "filter": {"type": "gaussian", "radius": 1.5, "alpha": 1.6}},
+        "scene": {"entities": ents,
+                  "envir_light": {"type": "ibl", "tex": arr("sky.hdr", address_mode_u="wrap"), "up": [0.0, 1.0, 0.0],
+                                  "lut_width": lut[0], "lut_height": lut[1]}},
+    }
+    _write_scene(out / name, scene)
+    return out / name

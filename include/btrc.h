@@ -197,6 +197,15 @@ btrc_status btrc_tonemap_aces(btrc_ctx *ctx, float *d_pixels, int32_t width, int
 btrc_status btrc_image_save(btrc_ctx *ctx, const char *filename, const float *pixels, int32_t width, int32_t height,
                             int32_t channels, float gamma);
 
+/* ImageDynamic::load (src/common/btrc/utils/image.cpp:296-346) as a 2D texture reads the
+   file: .png (1, 3 or 4 channels after palette expansion; 16-bit samples keep their high
+   byte) or .hdr (RGBE), as RGBA floats, top row first: 8-bit samples / 255, a one-channel
+   image as (v, 0, 0, 1), three channels as (r, g, b, 1). Writes width, height and the
+   file's channel count; with texels == NULL only those. capacity is in floats and must
+   be at least width*height*4. .jpg / .exr / interlaced PNG: BTRC_ERR_UNSUPPORTED. */
+btrc_status btrc_image_load(btrc_ctx *ctx, const char *filename, float *texels, uint64_t capacity, int32_t *width,
+                            int32_t *height, int32_t *channels);
+
 /* Closest hit for n device-resident rays. flags[i] = instance | BTRC_HIT_BIT or 0. */
 btrc_status btrc_trace_closest(btrc_ctx *ctx, const btrc_scene *scene, const btrc_ray *d_rays, uint64_t n,
                                uint32_t *d_flags, btrc_hit *d_hits, void *stream);

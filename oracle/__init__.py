@@ -37,6 +37,8 @@ class OracleScene(C.Structure):
         ("max_depth", C.c_int32), ("rr_threshold", C.c_float), ("rr_cont_prob", C.c_float),
         ("sampler", C.c_int32), ("filter", C.c_int32), ("filter_radius", C.c_float), ("filter_alpha", C.c_float),
         ("nvol", C.c_int32), ("vol", _vp), ("vol_off", _vp),
+        ("ntex_img", C.c_int32), ("tex_img", _vp), ("tex_texels", _vp), ("tex_instr", _vp), ("mat_tex", _vp),
+        ("mat_texrow", _vp), ("env_prog", C.c_int32), ("env_lut_w", C.c_int32), ("env_lut_h", C.c_int32),
     ]
 
 

@@ -42,6 +42,7 @@ template<class T> V<T> operator*(V<T> a, V<T> b) { return V<T>(a.x * b.x, a.y * 
 template<class T> V<T> operator*(V<T> a, T s) { return V<T>(a.x * s, a.y * s, a.z * s); }
 template<class T> V<T> operator*(T s, V<T> a) { return V<T>(a.x * s, a.y * s, a.z * s); }
 template<class T> V<T> operator/(V<T> a, T s) { return V<T>(a.x / s, a.y / s, a.z / s); }
+template<class T> V<T> operator/(V<T> a, V<T> b) { return V<T>(a.x / b.x, a.y / b.y, a.z / b.z); }
 template<class T> V<T> operator-(V<T> a) { return V<T>(-a.x, -a.y, -a.z); }
 template<class T> T dot(V<T> a, V<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 template<class T> V<T> cross(V<T> a, V<T> b) { return V<T>(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
@@ -71,7 +72,8 @@ struct Frame
             ny = cross(nz, V<T>(0, 1, 0));
         else
             ny = cross(nz, V<T>(1, 0, 0));
-        return Frame(cross(ny, nz), ny, nz);
+        // x = z cross y (common/btrc/utils/cmath/cframe.cpp:52-64)
+        return Frame(cross(nz, ny), ny, nz);
     }
     V<T> l2g(V<T> l) const { return x * l.x + y * l.y + z * l.z; }
     V<T> g2l(V<T> g) const { return V<T>(dot(g, x), dot(g, y), dot(g, z)); }
@@ -1349,6 +1351,15 @@ struct OracleScene
     int32_t nvol;           // volumes[] in file order
     const float *vol;       // 32 floats per volume (layout at volume() below)
     const uint64_t *vol_off; // 2 per volume: sigma_t grid, albedo grid offsets into grids
+
+    // 2D textures (layouts at OTexImage / OTexInstr / OMatTex below)
+    int32_t ntex_img;
+    const void *tex_img;
+    const float *tex_texels;   // 4 floats per texel
+    const void *tex_instr;
+    const void *mat_tex;
+    const int32_t *mat_texrow; // per material: row of mat_tex or -1
+    int32_t env_prog, env_lut_w, env_lut_h;  // env_type 2 (ibl); env_up holds its "up"
 };
 
 namespace {
@@ -1361,6 +1372,10 @@ struct Prepared
     Alias filter;
     Sampler::HC hc;
     bool has_media = false;
+    // ibl importance table (EnvirLightSampler::preprocess, env_sampler.cpp:83-135)
+    std::vector<float> env_probs;
+    Alias env_alias;
+    Frame<float> env_frame;
 };
 
 V3f pt(const float *m, V3f p)
@@ -1406,6 +1421,208 @@ V3f sky(const OracleScene &S, V3f d)
 }
 
 int nlights_total(const OracleScene &S) { return S.nlight + (S.env_type ? 1 : 0); }
+
+// ---- 2D textures: image textures in normalised coordinates with the address modes and
+// filters of a CUDA texture object (common/btrc/utils/cuda/texture.cpp:62-102, exact
+// bilinear weights), and postfix programs for add / sub / mul / div and uv transforms
+// (builtin/btrc/builtin/texture2d/{array2d,math,transform}.cpp)
+struct OTexImage
+{
+    int32_t offset, width, height, filter, au, av, pad0, pad1;
+    float border[4];
+};
+struct OTexInstr
+{
+    int32_t op, image;   // op: 0 end, 1 const, 2 sample, 3 add, 4 sub, 5 mul, 6 div
+    float a[6];
+};
+struct OMatTex
+{
+    int32_t prog[16];
+    int32_t normal;
+    int32_t pad[3];
+};
+
+bool otex_index(int i, int n, int mode, int &out)
+{
+    if(mode == 0)  // wrap
+    {
+        const int m = i % n;
+        out = m < 0 ? m + n : m;
+        return true;
+    }
+    if(mode == 2)  // mirror
+    {
+        int m = i % (2 * n);
+        m = m < 0 ? m + 2 * n : m;
+        out = m < n ? m : 2 * n - 1 - m;
+        return true;
+    }
+    if(mode == 3)  // border
+    {
+        out = i;
+        return i >= 0 && i < n;
+    }
+    out = std::min(std::max(i, 0), n - 1);  // clamp
+    return true;
+}
+
+V3f otex_fetch(const OracleScene &S, const OTexImage &im, int x, int y)
+{
+    int ix, iy;
+    const bool a = otex_index(x, im.width, im.au, ix), b = otex_index(y, im.height, im.av, iy);
+    if(!a || !b)
+        return V3f(im.border[0], im.border[1], im.border[2]);
+    const float *t = S.tex_texels + (static_cast<int64_t>(im.offset) + static_cast<int64_t>(iy) * im.width + ix) * 4;
+    return V3f(t[0], t[1], t[2]);
+}
+
+float otex_coord(float u, int mode)
+{
+    if(mode == 0)
+        return u - std::floor(u);
+    if(mode == 2)
+    {
+        const float f = std::floor(u), r = u - f;
+        return (static_cast<int>(f) & 1) ? 1.0f - r : r;
+    }
+    return u;
+}
+
+V3f otex_sample(const OracleScene &S, const OTexImage &im, float u, float v)
+{
+    u = otex_coord(u, im.au);
+    v = otex_coord(v, im.av);
+    if(!(u == u) || !(v == v))
+        return V3f(0.0f);
+    auto lim = [](float x) { return std::min(std::max(x, -1.0e9f), 1.0e9f); };
+    if(im.filter == 0)
+        return otex_fetch(S, im, static_cast<int>(std::floor(lim(u * im.width))),
+                          static_cast<int>(std::floor(lim(v * im.height))));
+    const float xb = lim(u * im.width - 0.5f), yb = lim(v * im.height - 0.5f);
+    const float fx = std::floor(xb), fy = std::floor(yb), ax = xb - fx, ay = yb - fy;
+    const int x0 = static_cast<int>(fx), y0 = static_cast<int>(fy);
+    const V3f t00 = otex_fetch(S, im, x0, y0), t10 = otex_fetch(S, im, x0 + 1, y0);
+    const V3f t01 = otex_fetch(S, im, x0, y0 + 1), t11 = otex_fetch(S, im, x0 + 1, y0 + 1);
+    return (t00 * (1.0f - ax) + t10 * ax) * (1.0f - ay) + (t01 * (1.0f - ax) + t11 * ax) * ay;
+}
+
+V3f otex_eval(const OracleScene &S, int prog, float u, float v)
+{
+    const OTexInstr *code = static_cast<const OTexInstr *>(S.tex_instr);
+    const OTexImage *imgs = static_cast<const OTexImage *>(S.tex_img);
+    std::vector<V3f> st;
+    for(int k = prog;; ++k)
+    {
+        const OTexInstr &ins = code[k];
+        if(ins.op == 1)
+            st.push_back(V3f(ins.a[0], ins.a[1], ins.a[2]));
+        else if(ins.op == 2)
+            st.push_back(otex_sample(S, imgs[ins.image], ins.a[0] * u + ins.a[1] * v + ins.a[2],
+                                     ins.a[3] * u + ins.a[4] * v + ins.a[5]));
+        else if(ins.op >= 3 && ins.op <= 6)
+        {
+            const V3f r = st.back();
+            st.pop_back();
+            V3f &l = st.back();
+            l = ins.op == 3 ? l + r : ins.op == 4 ? l - r : ins.op == 5 ? l * r : l / r;
+        }
+        else
+            return st.empty() ? V3f(0.0f) : st.back();
+    }
+}
+
+// ---- ibl (builtin/btrc/builtin/light/ibl.cpp, env_sampler.cpp)
+float local_phi(V3f d)
+{
+    float phi = 0.0f;
+    if(d.x != 0 || d.y != 0)
+    {
+        phi = std::atan2(d.y, d.x);
+        if(phi < 0)
+            phi += 2 * PIf;
+    }
+    return phi;
+}
+
+V3f ibl_eval_local(const OracleScene &S, V3f d)
+{
+    const float theta = std::acos(std::min(std::max(d.z, -1.0f), 1.0f));
+    const float u = std::min(std::max(1 / (2 * PIf) * local_phi(d), 0.0f), 1.0f);
+    const float v = std::min(std::max(1 / PIf * theta, 0.0f), 1.0f);
+    return otex_eval(S, S.env_prog, u, v);
+}
+
+V3f env_le(const Prepared &P, V3f d)
+{
+    if(P.S->env_type == 2)
+        return ibl_eval_local(*P.S, nrm(P.env_frame.g2l(d)));
+    return sky(*P.S, d);
+}
+
+// pdf_li of the environment light; EnvirLightSampler::pdf (env_sampler.cpp:165-187) for ibl
+float env_pdf(const Prepared &P, V3f d)
+{
+    const OracleScene &S = *P.S;
+    if(S.env_type != 2)
+        return 1.0f / (4.0f * PIf);
+    const V3f dir = nrm(P.env_frame.g2l(d));
+    const float theta = std::acos(std::min(std::max(dir.z, -1.0f), 1.0f));
+    const float u = local_phi(dir) / (2 * PIf), v = theta / PIf;
+    const int w = S.env_lut_w, h = S.env_lut_h;
+    const int tx = std::min(std::max(static_cast<int>(std::floor(u * w)), 0), w - 1);
+    const int ty = std::min(std::max(static_cast<int>(std::floor(v * h)), 0), h - 1);
+    const float u0 = static_cast<float>(tx) / w, u1 = static_cast<float>(tx + 1) / w;
+    const float v0 = static_cast<float>(ty) / h, v1 = static_cast<float>(ty + 1) / h;
+    return P.env_probs[ty * w + tx] / std::fabs(2 * PIf * (u1 - u0) * (std::cos(PIf * v1) - std::cos(PIf * v0)));
+}
+
+void build_env_table(Prepared &P)
+{
+    const OracleScene &S = *P.S;
+    const int w = S.env_lut_w, h = S.env_lut_h;
+    std::vector<float> lum(static_cast<size_t>(w) * h), area(lum.size());
+    for(int yi = 0; yi < h; ++yi)
+        for(int xi = 0; xi < w; ++xi)
+        {
+            const float x0 = static_cast<float>(xi) / w, x1 = static_cast<float>(xi + 1) / w;
+            const float y0 = static_cast<float>(yi) / h, y1 = static_cast<float>(yi + 1) / h;
+            float sum = 0;
+            for(uint32_t i = 0; i < 256; ++i)
+            {
+                // Hammersley point (i / 256, radical inverse of i), spread over 1.2x the tile
+                uint32_t b = (i << 16u) | (i >> 16u);
+                b = ((b & 0x55555555u) << 1u) | ((b & 0xAAAAAAAAu) >> 1u);
+                b = ((b & 0x33333333u) << 2u) | ((b & 0xCCCCCCCCu) >> 2u);
+                b = ((b & 0x0F0F0F0Fu) << 4u) | ((b & 0xF0F0F0F0u) >> 4u);
+                b = ((b & 0x00FF00FFu) << 8u) | ((b & 0xFF00FF00u) >> 8u);
+                const float sx = 1.2f * (static_cast<float>(i) / 256) - 0.1f;
+                const float sy = 1.2f * (b * 2.3283064365386963e-10f) - 0.1f;
+                const V3f c = otex_eval(S, S.env_prog, x0 + (x1 - x0) * sx, y0 + (y1 - y0) * sy);
+                sum += 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z;
+            }
+            lum[yi * w + xi] = sum / 256;
+            area[yi * w + xi] = std::fabs(2 * PIf * (x1 - x0) * (std::cos(PIf * y1) - std::cos(PIf * y0)));
+        }
+    float la = 0, as = 0;
+    for(size_t i = 0; i < lum.size(); ++i)
+    {
+        la += lum[i] * area[i];
+        as += area[i];
+    }
+    const float avg = la / as;
+    float total = 0;
+    for(size_t i = 0; i < lum.size(); ++i)
+    {
+        lum[i] = std::max(0.0f, area[i] * (lum[i] - avg));
+        total += lum[i];
+    }
+    if(total > 1e-3f)
+        for(float &v : lum)
+            v *= 1 / total;
+    P.env_probs = lum;
+    P.env_alias.init(lum);
+}
 
 struct ShadeFrame
 {
@@ -1888,6 +2105,28 @@ LightSample sample_light(const Prepared &P, V3f ref, V3f ref_nor, bool offset_or
         r.t1 = 1.0f;
         r.pdf = spdf * pdf_sa;
     }
+    else if(S.env_type == 2)
+    {
+        // IBL::sample_li_inline (ibl.cpp:31-42), EnvirLightSampler::sample (env_sampler.cpp:137-163)
+        const int w = S.env_lut_w, h = S.env_lut_h;
+        const uint32_t tile = P.env_alias.sample(s0);
+        const int ty = static_cast<int>(tile) / w, tx = static_cast<int>(tile) % w;
+        const float u0 = static_cast<float>(tx) / w, u1 = static_cast<float>(tx + 1) / w;
+        const float v0 = static_cast<float>(ty) / h, v1 = static_cast<float>(ty + 1) / h;
+        float cv0 = std::cos(PIf * v0), cv1 = std::cos(PIf * v1);
+        if(cv0 > cv1)
+            std::swap(cv0, cv1);
+        const float ct = cv0 + s2 * (cv1 - cv0);
+        const float st = std::sqrt(std::max(0.0f, 1.0f - ct * ct));
+        const float phi = 2 * PIf * (u0 + (u1 - u0) * s1);
+        const V3f local(st * std::cos(phi), st * std::sin(phi), ct);
+        const V3f dir = P.env_frame.l2g(local);
+        r.o = offset_origin ? ioffset_dir(ref, ref_nor, dir) : ref;
+        r.d = dir;
+        r.t1 = FMAX;
+        r.li = ibl_eval_local(S, local);
+        r.pdf = spdf * (P.env_probs[tile] * (1.0f / (2 * PIf * (u1 - u0) * (cv1 - cv0))));
+    }
     else
     {
         const float z = 1.0f - (s0 + s0);
@@ -2073,11 +2312,11 @@ void trace_path(const Prepared &P, uint64_t g, double *film, double *aov = nullp
             V3f le(0.0f);
             if(S.env_type)
             {
-                const V3f L = sky(S, d);
+                const V3f L = env_le(P, d);
                 if(bsdf_pdf < 0)
                     le = beta_le * L / -bsdf_pdf;
                 else
-                    le = beta_le * L / (bsdf_pdf + (1.0f / NL) * (1.0f / (4.0f * PIf)));
+                    le = beta_le * L / (bsdf_pdf + (1.0f / NL) * env_pdf(P, d));
             }
             splat(film, S.width, px, py, scattered ? le : le + rad);
         }
@@ -2098,6 +2337,10 @@ void trace_path(const Prepared &P, uint64_t g, double *film, double *aov = nullp
             gf.y = nrm(vec(l2w, gf.y));
             gf.z = nrm(nor(w2l, gf.z));
             const V3f interp = nrm(nor(w2l, shd(3) + shd(4) * h.b1 + shd(5) * h.b2));
+            // texture coordinate (core/btrc/core/scene.cpp:48-51)
+            auto shw = [&](int k) { return S.shade[(static_cast<uint64_t>(k) * S.total_geo_tris + ti) * 4 + 3]; };
+            const float tu = shw(0) + shw(1) * h.b1 + shw(2) * h.b2;
+            const float tv = shw(3) + shw(4) * h.b1 + shw(5) * h.b2;
 
             V3f le(0.0f);
             const int light = S.inst_light[inst];
@@ -2132,12 +2375,34 @@ void trace_path(const Prepared &P, uint64_t g, double *film, double *aov = nullp
                 else
                 {
                     LightSample ls = sample_light(P, pos, gf.z, true, smp);
-                    const float *mr = S.mat + S.inst_mat[inst] * 20;
+                    float mr[20];
+                    std::memcpy(mr, S.mat + S.inst_mat[inst] * 20, sizeof(mr));
                     const int mtype = static_cast<int>(mr[0]);
                     const bool term = mr[1] != 0.0f;
                     ShadeFrame fr;
                     fr.g = gf;
                     fr.s = gf.rotate_to_new_z(interp);
+                    // textured parameters and the normal map (material/utils/normal_map.cpp:13-21)
+                    const int trow = S.mat_texrow ? S.mat_texrow[S.inst_mat[inst]] : -1;
+                    if(trow >= 0)
+                    {
+                        const OMatTex &mt = static_cast<const OMatTex *>(S.mat_tex)[trow];
+                        if(mt.prog[0] >= 0)
+                        {
+                            const V3f c = otex_eval(S, mt.prog[0], tu, tv);
+                            mr[2] = c.x;
+                            mr[3] = c.y;
+                            mr[4] = c.z;
+                        }
+                        for(int k = 3; k < 16; ++k)
+                            if(mt.prog[k] >= 0)
+                                mr[2 + k] = otex_eval(S, mt.prog[k], tu, tv).x;
+                        if(mt.normal >= 0)
+                        {
+                            const V3f ln = 2.0f * otex_eval(S, mt.normal, tu, tv) - V3f(1.0f);
+                            fr.s = fr.s.rotate_to_new_z(nrm(fr.s.l2g(ln)));
+                        }
+                    }
                     Mat<float> M;
                     if(mtype <= 2)
                         M.init(mtype, mr + 2);
@@ -2512,6 +2777,11 @@ void *oracle_prepare(const OracleScene *S)
         P->filter.init(v);
     }
     P->hc = Sampler::consts(S->width, S->height);
+    if(S->env_type == 2)
+    {
+        P->env_frame = Frame<float>::from_z(V3f(S->env_up[0], S->env_up[1], S->env_up[2]));
+        build_env_table(*P);
+    }
     P->has_media = S->nvol > 0;
     for(int i = 0; i < S->ninst && S->nmed > 0; ++i)
         if(medium(*S, S->inst_inner[i]).type != 0 || medium(*S, S->inst_outer[i]).type != 0)

@@ -23,6 +23,7 @@ from pathlib import Path
 import numpy as np
 
 from . import OracleScene, _p, lib
+from .textures import MATTEX_DT, TexStore, parse_transform2d
 
 f32 = np.float32
 
@@ -419,49 +420,74 @@ def _obj_records(V, N, T, F, to_unit_cube):
 MAT_TYPES = {"diffuse": 0, "metal": 1, "disney": 2, "black": 3, "invisible": 4, "mirror": 5, "glass": 6}
 
 
-def _tex_rgb(n: Node) -> np.ndarray:
-    if n.kind in ("value", "array"):
-        return vvec3(n)
-    if n.child("type").s == "constant":
-        return vvec3(n.child("value"))
-    raise ValueError("only constant textures")
-
-
-def _tex_float(n: Node | None, default: float) -> np.float32:
-    return f32(default) if n is None else _tex_rgb(n)[0]
-
-
-def _material(n: Node) -> np.ndarray:
+def _material(n: Node, T: TexStore):
+    """Material record (20 floats: type, shadow terminator, p[16], pad) and, when a
+    parameter is a non-constant Texture2D or a normal map is present, its MaterialTex row
+    (programs per p index; k = 0 is the colour)."""
     rec = np.zeros(20, np.float32)
     t = n.child("type").s
     rec[0] = MAT_TYPES[t]
     st = n.find("shadow_terminator_term")
     rec[1] = 1.0 if st is None or st.s == "true" else 0.0
     p = rec[2:18]
+    row = np.zeros((), MATTEX_DT)
+    row["prog"][:] = -1
+    row["normal"] = -1
+    textured = False
+
+    def comp(node):
+        return T.compile(node, vvec3, vfloat, lambda m: parse_transform2d(m, vfloat, vangle_rad))
+
+    def spec(k, node):
+        nonlocal textured
+        c, prog = comp(node)
+        if prog is None:
+            p[k:k + 3] = c
+        else:
+            row["prog"][k] = prog
+            textured = True
+
+    def scal(k, node, default):
+        nonlocal textured
+        if node is None:
+            p[k] = default
+            return
+        c, prog = comp(node)
+        if prog is None:
+            p[k] = c[0]
+        else:
+            row["prog"][k] = prog
+            textured = True
+
+    if t in ("diffuse", "metal", "disney", "glass", "mirror") and n.find("normal") is not None:
+        c, prog = comp(n.child("normal"))
+        row["normal"] = T.constant_program(c) if prog is None else prog
+        textured = True
     if t in ("diffuse", "mirror"):
-        p[0:3] = _tex_rgb(n.child("color"))
+        spec(0, n.child("color"))
     elif t == "glass":
-        p[0:3] = _tex_rgb(n.child("color"))
-        p[3] = _tex_float(n.child("ior"), 1.5)
+        spec(0, n.child("color"))
+        scal(3, n.child("ior"), 1.5)
     elif t == "metal":
-        p[0:3] = _tex_rgb(n.child("color"))
-        p[3] = _tex_float(n.child("roughness"), 0)
-        p[4] = _tex_float(n.find("anisotropic"), 0)
+        spec(0, n.child("color"))
+        scal(3, n.child("roughness"), 0)
+        scal(4, n.find("anisotropic"), 0)
     elif t == "disney":
-        p[0:3] = _tex_rgb(n.child("color"))
-        p[3] = _tex_float(n.child("metallic"), 0)
-        p[4] = _tex_float(n.child("roughness"), 0)
-        p[5] = _tex_float(n.find("specular"), 1)
-        p[6] = _tex_float(n.find("specular_tint"), 0)
-        p[7] = _tex_float(n.find("anisotropic"), 0)
-        p[8] = _tex_float(n.find("sheen"), 0)
-        p[9] = _tex_float(n.find("sheen_tint"), 0)
-        p[10] = _tex_float(n.find("clearcoat"), 0)
-        p[11] = _tex_float(n.find("clearcoat_gloss"), 1)
-        p[12] = _tex_float(n.find("transmission"), 0)
-        p[13] = _tex_float(n.find("transmission_roughness"), float(p[4]))
-        p[14] = _tex_float(n.find("ior"), 1.5)
-    return rec
+        spec(0, n.child("color"))
+        scal(3, n.child("metallic"), 0)
+        scal(4, n.child("roughness"), 0)
+        scal(5, n.find("specular"), 1)
+        scal(6, n.find("specular_tint"), 0)
+        scal(7, n.find("anisotropic"), 0)
+        scal(8, n.find("sheen"), 0)
+        scal(9, n.find("sheen_tint"), 0)
+        scal(10, n.find("clearcoat"), 0)
+        scal(11, n.find("clearcoat_gloss"), 1)
+        scal(12, n.find("transmission"), 0)
+        tr = n.find("transmission_roughness")
+        scal(13, tr if tr is not None else n.child("roughness"), 0)
+        scal(14, n.find("ior"), 1.5)
+    return rec, (row if textured else None)
 
 
 def _grid(n: Node, sdir: str, rgb: bool = False):
@@ -609,6 +635,8 @@ class Scene:
         inst = []
         med_ids: dict[int, int] = {}
         meds = []
+        self.tex = TexStore(sdir)
+        mat_rows, mat_texrow = [], []
         for e in scene.child("entities").elems:
             gn = e.child("geometry")
             if id(gn) not in geo_ids:
@@ -618,7 +646,13 @@ class Scene:
                 geo_ids[id(gn)] = len(geos) - 1
             mn = e.child("material")
             if id(mn) not in mat_ids:
-                mats.append(_material(mn))
+                rec, row = _material(mn, self.tex)
+                mats.append(rec)
+                if row is not None:
+                    mat_texrow.append(len(mat_rows))
+                    mat_rows.append(row)
+                else:
+                    mat_texrow.append(-1)
                 mat_ids[id(mn)] = len(mats) - 1
             xf = parse_transform(e.child("local_to_world")) if e.find("local_to_world") is not None else \
                 (np.eye(4, dtype=np.float32), np.eye(4, dtype=np.float32))
@@ -746,12 +780,28 @@ class Scene:
         self.light_scale = np.array(lscale, np.float32)
         self.light_intensity = np.ascontiguousarray(np.array(lint, np.float32).reshape(-1, 3))
         self.env = None
+        self.env_ibl = None
         en = scene.find("envir_light")
         if en is not None:
-            if en.child("type").s != "gradient_sky":
-                raise ValueError("only gradient_sky")
-            upv = vvec3(en.child("up"))
-            self.env = (vvec3(en.child("lower")), vvec3(en.child("upper")), _nrm(upv[None])[0])
+            et = en.child("type").s
+            if et == "gradient_sky":
+                upv = vvec3(en.child("up"))
+                self.env = (vvec3(en.child("lower")), vvec3(en.child("upper")), _nrm(upv[None])[0])
+            elif et == "ibl":
+                # IBLCreator (builtin/btrc/builtin/light/ibl.cpp:80-91); oracle.cpp builds
+                # the frame from "up" and the tile table itself
+                c, prog = self.tex.compile(en.child("tex"), vvec3, vfloat,
+                                           lambda m: parse_transform2d(m, vfloat, vangle_rad))
+                prog = self.tex.constant_program(c) if prog is None else prog
+                upv = vvec3(en.child("up")) if en.find("up") is not None else np.array([0, 0, 1], np.float32)
+                lw = int(vfloat(en.child("lut_width"))) if en.find("lut_width") is not None else 400
+                lh = int(vfloat(en.child("lut_height"))) if en.find("lut_height") is not None else 200
+                self.env_ibl = (prog, upv, lw, lh)
+            else:
+                raise ValueError("environment light " + et)
+        self.mat_tex = np.ascontiguousarray(np.stack(mat_rows) if mat_rows else np.zeros(1, MATTEX_DT))
+        self.mat_texrow = np.array(mat_texrow, np.int32)
+        self.tex_img, self.tex_texels, self.tex_instr = self.tex.arrays()
         self._prepared = None
 
     def struct(self) -> OracleScene:
@@ -773,6 +823,13 @@ class Scene:
         if self.env is not None:
             s.env_type = 1
             s.env_lower[:], s.env_upper[:], s.env_up[:] = [list(map(float, v)) for v in self.env]
+        if self.env_ibl is not None:
+            s.env_type = 2
+            s.env_prog, up, s.env_lut_w, s.env_lut_h = self.env_ibl
+            s.env_up[:] = list(map(float, up))
+        s.ntex_img = len(self.tex.images)
+        s.tex_img, s.tex_texels, s.tex_instr = _p(self.tex_img), _p(self.tex_texels), _p(self.tex_instr)
+        s.mat_tex, s.mat_texrow = _p(self.mat_tex), _p(self.mat_texrow)
         s.vacuum_medium = self.vacuum
         s.world_diagonal = self.world_diagonal
         s.nmed, s.med, s.med_grid_offset, s.grids = len(self.med), _p(self.med), _p(self.med_grid_offset), _p(self.grids)

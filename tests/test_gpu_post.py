@@ -26,9 +26,13 @@ def aces(x):
     return np.clip(v, 0, 1)
 
 
-@pytest.mark.parametrize("variant", ["diffuse", "glass"])
+@pytest.mark.parametrize("variant", ["diffuse", "glass", "textured"])
 def test_gbuffer_matches_oracle(gpu_ctx, scene_dir, variant):
-    p = scenes.cornell(out_dir=scene_dir / "cornell", width=48, height=48, spp=16, variant=variant)
+    if variant == "textured":
+        # albedo from image textures, normals from normal maps
+        p = scenes.textured(out_dir=scene_dir / "textured", width=48, height=48, spp=16)
+    else:
+        p = scenes.cornell(out_dir=scene_dir / "cornell", width=48, height=48, spp=16, variant=variant)
     sc = gpu_ctx.load_scene(p).build()
     alb = np.zeros((48, 48, 3), np.float32)
     nrm = np.zeros((48, 48, 3), np.float32)

@@ -52,6 +52,20 @@ def test_cornell_glass_and_mirror(gpu_ctx, scene_dir):
     assert z < 2.0, z
 
 
+def test_textured_ibl_scene(gpu_ctx, scene_dir):
+    # PNG image textures (sRGB, wrap / mirror / border addressing, point and linear
+    # filters), texture expressions (mul, add, uv transform), normal maps and an HDR
+    # environment light with its tile importance table
+    p = scenes.textured(out_dir=scene_dir / "textured", width=64, height=48, spp=256)
+    g, o, var, stats = _render_both(gpu_ctx, p, 256)
+    assert stats["traversal_errors"] == 0
+    assert np.isfinite(g).all()
+    err = rel_mse(g, o)
+    assert err < 2e-3, err
+    z = np.mean((g - o) ** 2 / (2 * var + 1e-8))
+    assert z < 2.0, z
+
+
 def test_terrain_disney_sky(gpu_ctx, scene_dir):
     p = scenes.terrain(out_dir=scene_dir / "terrain-small", width=96, height=54, spp=128, grid=96, instances=24)
     g, o, var, stats = _render_both(gpu_ctx, p, 128)

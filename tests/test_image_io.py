@@ -154,3 +154,35 @@ def test_unsupported_and_bad_extension(host_ctx, tmp_path):
     with pytest.raises(B.BtrcError) as e:
         host_ctx.image_save(tmp_path / "no_such_dir" / "e.png", img)
     assert e.value.status == 2  # IO
+
+
+def test_texture_decoders_match_oracle(host_ctx, tmp_path):
+    # PNG: every filter type, 8/16/4-bit grey, RGB, RGBA, palette + tRNS; HDR: RLE scanlines
+    from btrc_gb300 import scenes
+    from oracle import textures as OT
+    rng = np.random.default_rng(11)
+    cases = {
+        "rgb.png": dict(img=rng.integers(0, 256, (13, 17, 3))),
+        "rgba.png": dict(img=rng.integers(0, 256, (9, 21, 4))),
+        "g8.png": dict(img=rng.integers(0, 256, (7, 9))),
+        "g16.png": dict(img=rng.integers(0, 65536, (11, 5)), depth=16),
+        "g4.png": dict(img=rng.integers(0, 16, (6, 13)), depth=4),
+        "g1.png": dict(img=rng.integers(0, 2, (5, 19)), depth=1),
+        "pal.png": dict(img=rng.integers(0, 6, (8, 8)), palette=rng.integers(0, 256, (6, 3)), alpha=[255, 0, 77]),
+    }
+    for name, kw in cases.items():
+        scenes.write_png(tmp_path / name, **kw)
+        got, ch = host_ctx.image_load(tmp_path / name)
+        want, wch, _ = OT.load_png(str(tmp_path / name))
+        assert ch == wch, name
+        assert np.array_equal(got, want), name
+    sky = rng.uniform(0, 5, (9, 40, 3)) * (rng.random((9, 40, 1)) < 0.7)
+    sky[:, 10:30] = 2.5  # long runs
+    scenes.write_hdr(tmp_path / "s.hdr", sky)
+    got, ch = host_ctx.image_load(tmp_path / "s.hdr")
+    want, _, _ = OT.load_hdr(str(tmp_path / "s.hdr"))
+    assert ch == 3 and np.array_equal(got, want)
+    assert np.allclose(got[..., :3], sky, rtol=1 / 64, atol=1e-6 + sky.max(-1, keepdims=True) / 128)
+    with pytest.raises(B.BtrcError) as e:
+        host_ctx.image_load(tmp_path / "x.jpg")
+    assert e.value.status == 8
