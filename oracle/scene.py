@@ -400,7 +400,8 @@ def _obj_records(V, N, T, F, to_unit_cube):
         z = _nrm(geo_z[~nz])
         y = np.where((f32(1) - np.abs(z[:, 0]) < f32(0.1))[:, None],
                      _cross(z, np.array([0, 1, 0], np.float32)), _cross(z, np.array([1, 0, 0], np.float32)))
-        gx[~nz] = _nrm(_cross(y, z))
+        # Frame::from_z(nor).x = z cross y (common/btrc/utils/math/frame.cpp:45-57)
+        gx[~nz] = _nrm(_cross(z, y))
     gy = _nrm(_cross(geo_z, gx))
     shade = np.zeros((6, len(F), 4), np.float32)
     shade[0, :, :3], shade[0, :, 3] = gx, uv[0][:, 0]

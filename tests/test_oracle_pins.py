@@ -90,3 +90,18 @@ def test_oracle_watertight_no_leaks_through_closed_box(oracle_lib, scene_dir):
     rays[:, 7] = 3.0e38
     flags, _ = oracle.OracleBvh(S.tris, S.ids).closest(rays)
     assert (flags != 0).all()
+
+
+def test_uvless_geometry_frame_follows_frame_from_z(tmp_path):
+    # a triangle without texture coordinates: triangle_dpdu falls back to
+    # Frame::from_z(normal).x, and the reference builds x = z cross y
+    # (common/btrc/utils/math/triangle.h, frame.cpp:45-57)
+    from btrc_gb300 import scenes
+    from oracle import scene as OS
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 0, -1]], np.float64)   # normal +y
+    scenes.write_obj(tmp_path / "t.obj", v, np.array([[0, 1, 2]]))
+    pos, shade, _ = OS.load_obj(str(tmp_path / "t.obj"), False)
+    z = shade[2, 0, :3] / np.linalg.norm(shade[2, 0, :3])
+    y = np.cross(z, [1, 0, 0]) if 1 - abs(z[0]) >= 0.1 else np.cross(z, [0, 1, 0])
+    x = np.cross(z, y)
+    assert np.allclose(shade[0, 0, :3], x / np.linalg.norm(x), atol=1e-6)
