@@ -1102,33 +1102,50 @@ __global__ void __launch_bounds__(BLOCK) k_medium(DevScene S, DevRender R, PathS
 }
 
 // Texture2D parameters of a material sampled at the hit's texture coordinate (every
-// material creator's context.create<Texture2D>), then the normal map
-// (builtin/btrc/builtin/material/utils/normal_map.cpp:13-21): n = 2 tex - 1 in the shading
-// frame, which is rotated onto it
-__device__ __noinline__ void apply_material_textures(const DevScene &S, const SurfacePoint &sp, Material &mat,
-                                                     Frame &shading)
+// material creator's context.create<Texture2D>), and the normal map's local normal
+// 2 tex - 1 (builtin/btrc/builtin/material/utils/normal_map.cpp:13-21). Returned by value
+// so that the untextured path keeps the material and frame in registers.
+struct MaterialTexValues
 {
-    const MaterialTex &mt = S.material_tex[mat.tex];
+    float p[16];
+    uint32_t mask;    // bit k: p[k] comes from a texture
+    int has_normal;
+    V3 normal;        // normal-map direction in the shading frame
+};
+
+__device__ __forceinline__ MaterialTexValues eval_material_textures(const DevScene &S, int row, float tu, float tv)
+{
+    MaterialTexValues r;
+    r.mask = 0;
+    r.has_normal = 0;
+    const MaterialTex &mt = S.material_tex[row];
     const TexTables T = tex_tables(S);
     if(mt.prog[0] >= 0)
     {
-        const V3 c = tex_eval(T, mt.prog[0], sp.tu, sp.tv);
-        mat.p[0] = c.x;
-        mat.p[1] = c.y;
-        mat.p[2] = c.z;
+        const V3 c = tex_eval(T, mt.prog[0], tu, tv);
+        r.p[0] = c.x;
+        r.p[1] = c.y;
+        r.p[2] = c.z;
+        r.mask |= 7u;
     }
-#pragma unroll
     for(int k = 3; k < 16; ++k)
         if(mt.prog[k] >= 0)
-            mat.p[k] = tex_eval(T, mt.prog[k], sp.tu, sp.tv).x;
+        {
+            r.p[k] = tex_eval(T, mt.prog[k], tu, tv).x;
+            r.mask |= 1u << k;
+        }
     if(mt.normal >= 0)
     {
-        const V3 ln = 2.0f * tex_eval(T, mt.normal, sp.tu, sp.tv) - V3(1.0f);
-        shading = shading.rotate_to_new_z(normalize(shading.local_to_global(ln)));
+        r.has_normal = 1;
+        r.normal = 2.0f * tex_eval(T, mt.normal, tu, tv) - V3(1.0f);
     }
+    return r;
 }
 
 // ShadePipeline (builtin/btrc/builtin/renderer/wavefront/shade.cpp:29-235)
+// TEX = false compiles the texture evaluation out, so scenes without textured materials
+// keep the shade kernel's registers
+template<bool TEX>
 __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, DevRender R, PathSoA P, PathSoA N, ShadowSoA SH,
                                                  const uint32_t *flags, const HitDetail *hits, float4 *film,
                                                  Counters *cnt)
@@ -1184,8 +1201,17 @@ __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, DevRender R, PathSo
         SurfaceShader sh;
         sh.frame.geometry = sp.frame;
         sh.frame.shading = sp.frame.rotate_to_new_z(sp.interp_z);
-        if(mat.tex >= 0)
-            apply_material_textures(S, sp, mat, sh.frame.shading);
+        if(TEX && mat.tex >= 0)
+        {
+            const MaterialTexValues tv = eval_material_textures(S, mat.tex, sp.tu, sp.tv);
+#pragma unroll
+            for(int k = 0; k < 16; ++k)
+                if(tv.mask & (1u << k))
+                    mat.p[k] = tv.p[k];
+            if(tv.has_normal)
+                sh.frame.shading =
+                    sh.frame.shading.rotate_to_new_z(normalize(sh.frame.shading.local_to_global(tv.normal)));
+        }
         sh.mat = make_material_eval(mat);
         sh.shadow_terminator = mat.shadow_terminator != 0;
 
@@ -1386,7 +1412,12 @@ cudaError_t enqueue_bounce(const DevScene &S, const DevRender &R, RenderBuffers 
             k_medium<<<grids[2], BLOCK, 0, st>>>(S, R, P, N, B.shadow, B.hit_flag, B.hit_detail, B.film, B.counters);
         });
     timed(T, STAGE_SHADE, st, launches, [&] {
-        k_shade<<<grids[3], BLOCK, 0, st>>>(S, R, P, N, B.shadow, B.hit_flag, B.hit_detail, B.film, B.counters);
+        if(S.material_tex != nullptr)
+            k_shade<true><<<grids[3], BLOCK, 0, st>>>(S, R, P, N, B.shadow, B.hit_flag, B.hit_detail, B.film,
+                                                      B.counters);
+        else
+            k_shade<false><<<grids[3], BLOCK, 0, st>>>(S, R, P, N, B.shadow, B.hit_flag, B.hit_detail, B.film,
+                                                       B.counters);
     });
     timed(T, STAGE_SHADOW, st, launches,
           [&] {
@@ -1446,7 +1477,8 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_generate)),
         persistent_grid(128, reinterpret_cast<const void *>(k_trace<false>)),
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_medium)),
-        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_shade)),
+        persistent_grid(BLOCK, S.material_tex != nullptr ? reinterpret_cast<const void *>(k_shade<true>)
+                                                         : reinterpret_cast<const void *>(k_shade<false>)),
         persistent_grid(128, S.has_media ? reinterpret_cast<const void *>(k_shadow<true>)
                                          : reinterpret_cast<const void *>(k_shadow<false>)),
     };
@@ -1739,7 +1771,8 @@ cudaError_t render_wavefront_noalloc(const DevScene &S, const DevRender &R, void
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_generate)),
         persistent_grid(128, reinterpret_cast<const void *>(k_trace<false>)),
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_medium)),
-        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_shade)),
+        persistent_grid(BLOCK, S.material_tex != nullptr ? reinterpret_cast<const void *>(k_shade<true>)
+                                                         : reinterpret_cast<const void *>(k_shade<false>)),
         persistent_grid(128, S.has_media ? reinterpret_cast<const void *>(k_shadow<true>)
                                          : reinterpret_cast<const void *>(k_shadow<false>)),
     };
