@@ -97,6 +97,11 @@ SIGNATURES = {
     "btrc_medium_tr_batch": (C.c_int, [_vp, _vp, C.c_int32, _vp, _vp, C.c_uint64, _vp, _vp]),
     "btrc_tonemap_aces": (C.c_int, [_vp, _vp, C.c_int32, C.c_int32, C.c_int32, C.c_float, _vp]),
     "btrc_image_save": (C.c_int, [_vp, C.c_char_p, _vp, C.c_int32, C.c_int32, C.c_int32, C.c_float]),
+    "btrc_nrc_create": (C.c_int, [_vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint64, C.POINTER(_vp)]),
+    "btrc_nrc_destroy": (None, [_vp]),
+    "btrc_nrc_infer": (C.c_int, [_vp, _vp, _vp, C.c_uint64, _vp, _vp]),
+    "btrc_nrc_train": (C.c_int, [_vp, _vp, _vp, C.c_uint64, C.c_int32, C.POINTER(C.c_float)]),
+    "btrc_nrc_params": (C.c_int, [_vp, _vp, C.c_int32, _vp, C.c_uint64, C.c_int32]),
     "btrc_image_load": (C.c_int, [_vp, C.c_char_p, _vp, C.c_uint64, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                   C.POINTER(C.c_int32)]),
 }
@@ -267,6 +272,55 @@ class Context:
         px = np.ascontiguousarray(pixels, np.float32)
         h, w, c = px.shape
         self._check(self._lib.btrc_image_save(self.handle, str(filename).encode(), _ptr(px), w, h, c, gamma))
+
+
+NRC_QUERY_FLOATS = 13
+NRC_SAMPLE_FLOATS = 16
+NRC_WEIGHTS = 22528
+NRC_HASH_FLOATS = 16 * (1 << 19) * 2
+
+
+class RadianceCache:
+    """btrc_nrc: hash-grid + SH encoded 5x64 BF16 MLP radiance cache trained with Adam."""
+
+    def __init__(self, ctx: "Context", bbox_min, bbox_max, seed: int = 1):
+        self.ctx = ctx
+        lo = (C.c_float * 3)(*map(float, bbox_min))
+        hi = (C.c_float * 3)(*map(float, bbox_max))
+        h = _vp()
+        ctx._check(ctx._lib.btrc_nrc_create(ctx.handle, lo, hi, seed, C.byref(h)))
+        self.handle = h
+
+    def infer(self, queries, n: int, out, stream: int | None = None):
+        self.ctx._check(self.ctx._lib.btrc_nrc_infer(self.ctx.handle, self.handle, _ptr(queries), n, _ptr(out),
+                                                     stream))
+
+    def train(self, samples, n: int, apply_adam: bool = True) -> float:
+        loss = C.c_float()
+        self.ctx._check(self.ctx._lib.btrc_nrc_train(self.ctx.handle, self.handle, _ptr(samples), n,
+                                                     1 if apply_adam else 0, C.byref(loss)))
+        return loss.value
+
+    def params(self, which: int) -> np.ndarray:
+        n = NRC_WEIGHTS if which in (0, 2) else NRC_HASH_FLOATS
+        out = np.zeros(n, np.float32)
+        self.ctx._check(self.ctx._lib.btrc_nrc_params(self.ctx.handle, self.handle, which, _ptr(out), n, 0))
+        return out
+
+    def set_params(self, which: int, values: np.ndarray):
+        v = np.ascontiguousarray(values, np.float32)
+        self.ctx._check(self.ctx._lib.btrc_nrc_params(self.ctx.handle, self.handle, which, _ptr(v), v.size, 1))
+
+    def close(self):
+        if self.handle:
+            self.ctx._lib.btrc_nrc_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Scene:

@@ -16,6 +16,7 @@
 #include "btrc.h"
 #include "bvh.h"
 #include "image_io.h"
+#include "nrc.h"
 #include "kernels.h"
 #include "scene.h"
 
@@ -1083,6 +1084,87 @@ btrc_status btrc_image_save(btrc_ctx *ctx, const char *filename, const float *pi
         {
             throw StatusError(BTRC_ERR_IO, ex.what());
         }
+    });
+}
+
+struct btrc_nrc
+{
+    btrc_ctx *ctx;
+    std::unique_ptr<bt::Nrc> impl;
+};
+
+btrc_status btrc_nrc_create(btrc_ctx *ctx, const float bbox_min[3], const float bbox_max[3], uint64_t seed,
+                            btrc_nrc **out)
+{
+    if(!ctx || !bbox_min || !bbox_max || !out)
+        return BTRC_ERR_INVALID_ARG;
+    *out = nullptr;
+    return guarded(ctx, [&] {
+        if(ctx->device < 0)
+            throw StatusError(BTRC_ERR_INVALID_ARG, "host-only context");
+        for(int a = 0; a < 3; ++a)
+            if(!(bbox_max[a] >= bbox_min[a]))
+                throw StatusError(BTRC_ERR_INVALID_ARG, "empty bounding box");
+        check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+        auto n = std::make_unique<btrc_nrc>();
+        n->ctx = ctx;
+        try
+        {
+            n->impl = std::make_unique<bt::Nrc>(bbox_min, bbox_max, seed);
+        }
+        catch(const std::runtime_error &e)
+        {
+            throw StatusError(BTRC_ERR_CUDA, e.what());
+        }
+        *out = n.release();
+    });
+}
+
+void btrc_nrc_destroy(btrc_nrc *nrc)
+{
+    if(!nrc)
+        return;
+    if(nrc->ctx && nrc->ctx->device >= 0)
+        cudaSetDevice(nrc->ctx->device);
+    delete nrc;
+}
+
+btrc_status btrc_nrc_infer(btrc_ctx *ctx, btrc_nrc *nrc, const float *d_queries, uint64_t n, float *d_out,
+                           void *stream)
+{
+    if(!ctx || !nrc || n > 0xffffffffull || (n > 0 && (!d_queries || !d_out)))
+        return BTRC_ERR_INVALID_ARG;
+    return guarded(ctx, [&] {
+        check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+        check_cuda(nrc->impl->infer(d_queries, static_cast<uint32_t>(n), d_out, pick_stream(ctx, stream)),
+                   "radiance cache inference");
+    });
+}
+
+btrc_status btrc_nrc_train(btrc_ctx *ctx, btrc_nrc *nrc, const float *d_samples, uint64_t n, int32_t apply_adam,
+                           float *loss_out)
+{
+    if(!ctx || !nrc || n > 0xffffffffull || (n > 0 && !d_samples))
+        return BTRC_ERR_INVALID_ARG;
+    return guarded(ctx, [&] {
+        check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+        check_cuda(nrc->impl->train(d_samples, static_cast<uint32_t>(n), loss_out, apply_adam != 0, ctx->stream),
+                   "radiance cache training");
+        if(!loss_out)
+            check_cuda(cudaStreamSynchronize(ctx->stream), "radiance cache training");
+    });
+}
+
+btrc_status btrc_nrc_params(btrc_ctx *ctx, btrc_nrc *nrc, int32_t which, float *host, uint64_t count, int32_t set)
+{
+    if(!ctx || !nrc || !host || which < 0 || which > 3 || (set && which > 1))
+        return BTRC_ERR_INVALID_ARG;
+    return guarded(ctx, [&] {
+        check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+        const cudaError_t e = nrc->impl->copy_params(which, host, count, set != 0, ctx->stream);
+        if(e == cudaErrorInvalidValue)
+            throw StatusError(BTRC_ERR_INVALID_ARG, "parameter count mismatch");
+        check_cuda(e, "radiance cache parameters");
     });
 }
 

@@ -238,6 +238,33 @@ btrc_status btrc_bsdf_batch(btrc_ctx *ctx, int32_t op, const float *d_material, 
 btrc_status btrc_medium_tr_batch(btrc_ctx *ctx, const btrc_scene *scene, int32_t medium_id, const float *d_seg,
                                  const uint64_t *d_seeds, uint64_t n, float *d_out, void *stream);
 
+/* ---- Neural radiance cache (no counterpart in the reference) ----------------------
+   A multiresolution hash-grid (16 levels x 2 features, 2^19 FP16 entries per level) and
+   degree-4 spherical-harmonics encoding of a path vertex feeding a 5 x 64 ReLU MLP with
+   BF16 weights and activations and FP32 accumulation, trained online with FP32 Adam
+   (lr 1e-2, beta 0.9 / 0.99) on a relative L2 loss. All data pointers are device memory. */
+typedef struct btrc_nrc btrc_nrc;
+
+#define BTRC_NRC_QUERY_FLOATS 13   /* position(3), direction to the viewer(3), normal(3), roughness, albedo(3) */
+#define BTRC_NRC_SAMPLE_FLOATS 16  /* a query followed by the target radiance (3) */
+#define BTRC_NRC_WEIGHTS 22528     /* 80x64 + 4 x 64x64 + 64x16, row-major K x N per layer */
+#define BTRC_NRC_HASH_FLOATS 16777216 /* 16 levels x 2^19 entries x 2 features */
+
+/* positions are normalised to [bbox_min, bbox_max]; seed drives the initialisation */
+btrc_status btrc_nrc_create(btrc_ctx *ctx, const float bbox_min[3], const float bbox_max[3], uint64_t seed,
+                            btrc_nrc **out);
+void btrc_nrc_destroy(btrc_nrc *nrc);
+/* predicted radiance for n queries: 4 floats per query (rgb, unused) */
+btrc_status btrc_nrc_infer(btrc_ctx *ctx, btrc_nrc *nrc, const float *d_queries, uint64_t n, float *d_out,
+                           void *stream);
+/* one optimisation step over n training samples (apply_adam 0: gradients only, kept until
+   the next step); loss_out (host, may be NULL) receives the batch's mean loss */
+btrc_status btrc_nrc_train(btrc_ctx *ctx, btrc_nrc *nrc, const float *d_samples, uint64_t n, int32_t apply_adam,
+                           float *loss_out);
+/* test hook: FP32 host copies of parameters (which 0: MLP weights, 1: hash features) or
+   gradients (2: MLP, 3: hash); set != 0 writes parameters 0 / 1 instead */
+btrc_status btrc_nrc_params(btrc_ctx *ctx, btrc_nrc *nrc, int32_t which, float *host, uint64_t count, int32_t set);
+
 #ifdef __cplusplus
 }
 #endif
