@@ -57,6 +57,19 @@ class RenderOpts(C.Structure):
                 ("albedo_out", _vp), ("normal_out", _vp)]
 
 
+class NrcRenderOpts(C.Structure):
+    _fields_ = [("frame", C.c_uint32), ("terminate_vertex", C.c_int32), ("train_stride", C.c_int32),
+                ("train_steps", C.c_int32), ("train_batch", C.c_int32), ("output_on_device", C.c_int32)]
+
+
+class NrcFrameStats(C.Structure):
+    _fields_ = [("paths", C.c_uint64), ("queries", C.c_uint64), ("train_samples", C.c_uint64),
+                ("train_steps", C.c_int32), ("loss", C.c_float), ("render_ms", C.c_double), ("wall_ms", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 STAGES = ("control", "generate", "trace", "medium", "shade", "shadow")
 
 
@@ -102,6 +115,7 @@ SIGNATURES = {
     "btrc_nrc_infer": (C.c_int, [_vp, _vp, _vp, C.c_uint64, _vp, _vp]),
     "btrc_nrc_train": (C.c_int, [_vp, _vp, _vp, C.c_uint64, C.c_int32, C.POINTER(C.c_float)]),
     "btrc_nrc_params": (C.c_int, [_vp, _vp, C.c_int32, _vp, C.c_uint64, C.c_int32]),
+    "btrc_render_nrc_frame": (C.c_int, [_vp, _vp, _vp, C.POINTER(NrcRenderOpts), _vp, C.POINTER(NrcFrameStats)]),
     "btrc_image_load": (C.c_int, [_vp, C.c_char_p, _vp, C.c_uint64, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                   C.POINTER(C.c_int32)]),
 }
@@ -305,6 +319,22 @@ class RadianceCache:
         n = NRC_WEIGHTS if which in (0, 2) else NRC_HASH_FLOATS
         out = np.zeros(n, np.float32)
         self.ctx._check(self.ctx._lib.btrc_nrc_params(self.ctx.handle, self.handle, which, _ptr(out), n, 0))
+        return out
+
+    def render_frame(self, scene: "Scene", frame: int, out=None, terminate_vertex: int = 1, train_stride: int = 16,
+                     train_steps: int = 4, train_batch: int = 16384, stats: dict | None = None):
+        """One frame (one path per pixel) with cache termination, training and inference
+        (btrc_render_nrc_frame). Returns the frame image (H, W, 3)."""
+        info = scene.info()
+        on_dev = out is not None and hasattr(out, "is_cuda") and out.is_cuda
+        if out is None:
+            out = np.zeros((info.height, info.width, 3), np.float32)
+        opts = NrcRenderOpts(frame, terminate_vertex, train_stride, train_steps, train_batch, 1 if on_dev else 0)
+        st = NrcFrameStats()
+        self.ctx._check(self.ctx._lib.btrc_render_nrc_frame(self.ctx.handle, scene.handle, self.handle, C.byref(opts),
+                                                            _ptr(out), C.byref(st)))
+        if stats is not None:
+            stats.update(st.as_dict())
         return out
 
     def set_params(self, which: int, values: np.ndarray):

@@ -37,6 +37,12 @@ struct btrc_ctx
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
     std::set<btrc_scene *> scenes;  // live scenes, destroyed with the context
+    // radiance-cache frame buffers (queries, weights, predictions, training samples)
+    std::vector<void *> nrc_allocs;
+    size_t nrc_pixels = 0, nrc_sample_cap = 0;
+    float *nrc_query = nullptr, *nrc_samples = nullptr;
+    float4 *nrc_weight = nullptr, *nrc_pred = nullptr;
+    uint32_t *nrc_counts = nullptr;
 };
 
 struct btrc_scene
@@ -472,6 +478,8 @@ DevRender make_render_params(const btrc_scene *sc, int spp, uint32_t capacity)
     R.cam_lbc = H.camera.lbc;
     R.cam_fx = H.camera.film_x;
     R.cam_fy = H.camera.film_y;
+    R.sample_offset = 0;
+    R.nrc_terminate = -1;
     return R;
 }
 
@@ -551,6 +559,8 @@ void btrc_ctx_destroy(btrc_ctx *ctx)
     if(ctx->stream)
         cudaStreamSynchronize(ctx->stream);
     for(void *p : ctx->buf_allocs)
+        cudaFree(p);
+    for(void *p : ctx->nrc_allocs)
         cudaFree(p);
     if(ctx->buf.host_counters)
         cudaFreeHost(ctx->buf.host_counters);
@@ -1092,6 +1102,131 @@ struct btrc_nrc
     btrc_ctx *ctx;
     std::unique_ptr<bt::Nrc> impl;
 };
+
+namespace {
+
+void ensure_nrc_buffers(btrc_ctx *ctx, size_t pixels, size_t sample_cap)
+{
+    if(ctx->nrc_pixels >= pixels && ctx->nrc_sample_cap >= sample_cap && ctx->nrc_counts)
+        return;
+    check_cuda(cudaStreamSynchronize(ctx->stream), "stream sync");
+    for(void *p : ctx->nrc_allocs)
+        cudaFree(p);
+    ctx->nrc_allocs.clear();
+    ctx->nrc_pixels = ctx->nrc_sample_cap = 0;
+    auto A = [&](size_t bytes) { return dev_alloc(ctx->nrc_allocs, bytes); };
+    ctx->nrc_query = static_cast<float *>(A(sizeof(float) * NRC_QUERY_FLOATS * pixels));
+    ctx->nrc_weight = static_cast<float4 *>(A(sizeof(float4) * pixels));
+    ctx->nrc_pred = static_cast<float4 *>(A(sizeof(float4) * pixels));
+    ctx->nrc_samples = static_cast<float *>(A(sizeof(float) * NRC_SAMPLE_FLOATS * std::max<size_t>(sample_cap, 1)));
+    ctx->nrc_counts = static_cast<uint32_t *>(A(sizeof(uint32_t) * 4));
+    ctx->nrc_pixels = pixels;
+    ctx->nrc_sample_cap = sample_cap;
+}
+
+} // namespace
+
+btrc_status btrc_render_nrc_frame(btrc_ctx *ctx, btrc_scene *scene, btrc_nrc *nrc, const btrc_nrc_render_opts *opts,
+                                  float *rgb_out, btrc_nrc_frame_stats *fstats)
+{
+    if(!ctx || !scene || !nrc || !opts || !rgb_out)
+        return BTRC_ERR_INVALID_ARG;
+    bool cancelled = false;
+    const btrc_status st = guarded(ctx, [&] {
+        require_built(scene);
+        const auto w0 = std::chrono::steady_clock::now();
+        check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+        if(scene->dev.has_media)
+            throw StatusError(BTRC_ERR_UNSUPPORTED, "radiance-cache rendering of scenes with participating media");
+        if(opts->train_stride < 0 || opts->train_steps < 0 || opts->train_batch < 0)
+            throw StatusError(BTRC_ERR_INVALID_ARG, "negative training option");
+        ctx->cancel.store(false);
+        const HostScene &H = scene->host;
+        const size_t pixels = static_cast<size_t>(H.params.width) * H.params.height;
+        const uint32_t capacity = static_cast<uint32_t>(
+            std::min<uint64_t>(static_cast<uint64_t>(H.params.state_count), std::max<size_t>(pixels, 1)));
+        const size_t sample_cap = static_cast<size_t>(opts->train_steps) * static_cast<size_t>(opts->train_batch);
+        ensure_render_buffers(ctx, capacity, pixels);
+        ensure_nrc_buffers(ctx, pixels, sample_cap);
+        cudaStream_t s = ctx->stream;
+        check_cuda(cudaMemsetAsync(ctx->buf.film, 0, sizeof(float4) * pixels, s), "film clear");
+        check_cuda(cudaMemsetAsync(ctx->nrc_counts, 0, sizeof(uint32_t) * 4, s), "counter clear");
+        DevRender R = make_render_params(scene, 1, capacity);
+        R.sample_offset = opts->frame;
+        R.nrc_terminate = opts->terminate_vertex;
+        R.nrc_query = ctx->nrc_query;
+        R.nrc_weight = ctx->nrc_weight;
+        R.nrc_count = ctx->nrc_counts;
+        R.nrc_cap = static_cast<uint32_t>(pixels);
+        ctx->buf.capacity = capacity;
+        RenderStats rs{};
+        check_cuda(render_wavefront(scene->dev, R, ctx->buf, s, &ctx->cancel, true, 0, &rs, &cancelled),
+                   "wavefront render");
+        const bool on_dev = opts->output_on_device != 0;
+        float *rgb_dev = on_dev ? rgb_out : ctx_scratch_images(ctx, pixels, 1);
+        uint32_t *err = ctx_scratch_err(ctx);
+        if(opts->train_stride > 0 && sample_cap > 0)
+        {
+            const uint32_t stride = static_cast<uint32_t>(opts->train_stride);
+            const uint32_t phase = (opts->frame * 7u + 3u) % stride;
+            check_cuda(launch_nrc_train_paths(scene->dev, R, stride, phase, opts->frame + (1u << 20), ctx->nrc_samples,
+                                              ctx->nrc_counts + 1, static_cast<uint32_t>(sample_cap), err, s),
+                       "training paths");
+        }
+        uint32_t counts[4] = {};
+        check_cuda(cudaMemcpyAsync(counts, ctx->nrc_counts, sizeof(counts), cudaMemcpyDeviceToHost, s), "counters");
+        check_cuda(cudaStreamSynchronize(s), "counters");
+        const uint32_t nq = std::min<uint32_t>(counts[0], static_cast<uint32_t>(pixels));
+        if(nq > 0 && opts->terminate_vertex >= 0)
+        {
+            check_cuda(nrc->impl->infer(ctx->nrc_query, nq, reinterpret_cast<float *>(ctx->nrc_pred), s),
+                       "cache inference");
+            check_cuda(launch_nrc_splat(ctx->nrc_pred, ctx->nrc_weight, ctx->nrc_counts, static_cast<uint32_t>(pixels),
+                                        ctx->buf.film, H.params.width, s),
+                       "cache splat");
+        }
+        check_cuda(launch_resolve(ctx->buf.film, rgb_dev, static_cast<uint32_t>(pixels), s), "resolve");
+        // train on this frame's samples
+        const uint32_t ns = std::min<uint32_t>(counts[1], static_cast<uint32_t>(sample_cap));
+        float loss = 0.0f;
+        int steps = 0;
+        for(int k = 0; k < opts->train_steps; ++k)
+        {
+            const uint32_t b0 = static_cast<uint32_t>(k) * static_cast<uint32_t>(opts->train_batch);
+            if(b0 >= ns)
+                break;
+            const uint32_t nb = std::min<uint32_t>(static_cast<uint32_t>(opts->train_batch), ns - b0);
+            float l = 0.0f;
+            check_cuda(nrc->impl->train(ctx->nrc_samples + static_cast<size_t>(b0) * NRC_SAMPLE_FLOATS, nb,
+                                        fstats ? &l : nullptr, true, s),
+                       "cache training");
+            loss += l;
+            ++steps;
+        }
+        if(!on_dev)
+            check_cuda(cudaMemcpyAsync(rgb_out, rgb_dev, pixels * 3 * sizeof(float), cudaMemcpyDeviceToHost, s),
+                       "image download");
+        check_cuda(cudaStreamSynchronize(s), "frame sync");
+        if(fstats)
+        {
+            fstats->paths = rs.paths;
+            fstats->queries = nq;
+            fstats->train_samples = ns;
+            fstats->train_steps = steps;
+            fstats->loss = steps ? loss / steps : 0.0f;
+            fstats->render_ms = rs.device_ms;
+            fstats->wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
+        }
+        if(rs.err)
+            throw StatusError(BTRC_ERR_INTERNAL, "traversal stack overflow reported by the device");
+    });
+    if(st == BTRC_OK && cancelled)
+    {
+        ctx->last_error = "render cancelled";
+        return BTRC_ERR_CANCELLED;
+    }
+    return st;
+}
 
 btrc_status btrc_nrc_create(btrc_ctx *ctx, const float bbox_min[3], const float bbox_max[3], uint64_t seed,
                             btrc_nrc **out)

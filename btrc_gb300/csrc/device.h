@@ -60,6 +60,14 @@ struct DevRender
     V3 cam_eye, cam_lbc, cam_fx, cam_fy;
     float4 *aov_albedo;       // first-hit albedo sums (xyz), or null
     float4 *aov_normal;       // first-hit normal sums (xyz), or null
+    uint32_t sample_offset;   // added to every path's sample index (frame-by-frame rendering)
+    // radiance-cache termination: at the first non-delta surface vertex with depth >=
+    // nrc_terminate a path writes a cache query and ends (-1: off)
+    int32_t nrc_terminate;
+    float *nrc_query;         // NRC_QUERY_FLOATS per query
+    float4 *nrc_weight;       // path throughput (xyz) and pixel bits (w) per query
+    uint32_t *nrc_count;
+    uint32_t nrc_cap;
 };
 
 // Queue counters, resident in device memory for the whole render.

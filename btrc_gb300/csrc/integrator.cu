@@ -16,6 +16,7 @@
 
 #include "bsdf.cuh"
 #include "kernels.h"
+#include "nrc.h"
 #include "texture.h"
 #include "traverse.cuh"
 
@@ -908,7 +909,7 @@ __global__ void __launch_bounds__(BLOCK) k_generate(DevRender R, PathSoA P, floa
         const uint32_t py = static_cast<uint32_t>(pixel / R.width);
         DSampler smp;
         smp.type = R.sampler;
-        smp.s = sampler_init(R.sampler, R.halton, px, py, static_cast<uint32_t>(sample));
+        smp.s = sampler_init(R.sampler, R.halton, px, py, static_cast<uint32_t>(sample) + R.sample_offset);
         float fx, fy;
         if(R.filter == FILTER_GAUSSIAN)
         {
@@ -1143,9 +1144,47 @@ __device__ __forceinline__ MaterialTexValues eval_material_textures(const DevSce
 }
 
 // ShadePipeline (builtin/btrc/builtin/renderer/wavefront/shade.cpp:29-235)
+// Radiance-cache query of a surface vertex: position, direction towards the previous
+// vertex, shading normal (normal-mapped), roughness and diffuse albedo. Delta surfaces
+// (mirror, glass, invisible) get no query: the path continues through them.
+template<bool TEX>
+__device__ __forceinline__ bool nrc_query_at(const DevScene &S, const SurfacePoint &sp, const Instance &inst, V3 wo,
+                                             float *q)
+{
+    Material mat = S.materials[inst.material];
+    if(mat.type == MAT_MIRROR || mat.type == MAT_GLASS || mat.type == MAT_INVISIBLE)
+        return false;
+    Frame shading = sp.frame.rotate_to_new_z(sp.interp_z);
+    if(TEX && mat.tex >= 0)
+    {
+        const MaterialTexValues tv = eval_material_textures(S, mat.tex, sp.tu, sp.tv);
+#pragma unroll
+        for(int k = 0; k < 16; ++k)
+            if(tv.mask & (1u << k))
+                mat.p[k] = tv.p[k];
+        if(tv.has_normal)
+            shading = shading.rotate_to_new_z(normalize(shading.local_to_global(tv.normal)));
+    }
+    const V3 n = shading.z;
+    float rough = 1.0f;
+    V3 alb(mat.p[0], mat.p[1], mat.p[2]);
+    if(mat.type == MAT_METAL)
+        rough = mat.p[3];
+    else if(mat.type == MAT_DISNEY)
+        rough = mat.p[4];
+    else if(mat.type == MAT_BLACK)
+        alb = V3(0.0f);
+    q[0] = sp.position.x; q[1] = sp.position.y; q[2] = sp.position.z;
+    q[3] = wo.x; q[4] = wo.y; q[5] = wo.z;
+    q[6] = n.x; q[7] = n.y; q[8] = n.z;
+    q[9] = rough;
+    q[10] = alb.x; q[11] = alb.y; q[12] = alb.z;
+    return true;
+}
+
 // TEX = false compiles the texture evaluation out, so scenes without textured materials
 // keep the shade kernel's registers
-template<bool TEX>
+template<bool TEX, bool NRC = false>
 __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, DevRender R, PathSoA P, PathSoA N, ShadowSoA SH,
                                                  const uint32_t *flags, const HitDetail *hits, float4 *film,
                                                  Counters *cnt)
@@ -1186,6 +1225,24 @@ __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, DevRender R, PathSo
 
         V3 beta = v3(bd);
         const int depth = __float_as_int(bd.w);
+        if(NRC && depth >= R.nrc_terminate)
+        {
+            // terminate into the radiance cache at a non-delta vertex: the cache's
+            // prediction replaces light sampling and everything after this vertex
+            float q[NRC_QUERY_FLOATS];
+            if(nrc_query_at<TEX>(S, sp, inst, -d, q))
+            {
+                const uint32_t k = atomicAdd(R.nrc_count, 1u);
+                if(k < R.nrc_cap)
+                {
+                    for(int j = 0; j < NRC_QUERY_FLOATS; ++j)
+                        R.nrc_query[static_cast<size_t>(k) * NRC_QUERY_FLOATS + j] = q[j];
+                    R.nrc_weight[k] = make_float4(beta.x, beta.y, beta.z, __uint_as_float(pixel));
+                }
+                splat(film, pixel, R.width, path_rad);
+                continue;
+            }
+        }
         DSampler smp;
         smp.type = R.sampler;
         smp.s = P.sampler[i];
@@ -1286,6 +1343,18 @@ __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, DevRender R, PathSo
         else
             splat(film, pixel, R.width, path_rad);
     }
+}
+
+using ShadeKernel = void (*)(DevScene, DevRender, PathSoA, PathSoA, ShadowSoA, const uint32_t *, const HitDetail *,
+                             float4 *, Counters *);
+
+// the shade kernel variant for a scene and render: textured materials, cache termination
+ShadeKernel shade_kernel(const DevScene &S, const DevRender &R)
+{
+    const bool tex = S.material_tex != nullptr, nrc = R.nrc_terminate >= 0;
+    if(tex)
+        return nrc ? k_shade<true, true> : k_shade<true, false>;
+    return nrc ? k_shade<false, true> : k_shade<false, false>;
 }
 
 // ShadowPipeline (builtin/btrc/builtin/renderer/wavefront/shadow.cpp:24-76): occlusion by
@@ -1412,11 +1481,7 @@ cudaError_t enqueue_bounce(const DevScene &S, const DevRender &R, RenderBuffers 
             k_medium<<<grids[2], BLOCK, 0, st>>>(S, R, P, N, B.shadow, B.hit_flag, B.hit_detail, B.film, B.counters);
         });
     timed(T, STAGE_SHADE, st, launches, [&] {
-        if(S.material_tex != nullptr)
-            k_shade<true><<<grids[3], BLOCK, 0, st>>>(S, R, P, N, B.shadow, B.hit_flag, B.hit_detail, B.film,
-                                                      B.counters);
-        else
-            k_shade<false><<<grids[3], BLOCK, 0, st>>>(S, R, P, N, B.shadow, B.hit_flag, B.hit_detail, B.film,
+        shade_kernel(S, R)<<<grids[3], BLOCK, 0, st>>>(S, R, P, N, B.shadow, B.hit_flag, B.hit_detail, B.film,
                                                        B.counters);
     });
     timed(T, STAGE_SHADOW, st, launches,
@@ -1477,8 +1542,7 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_generate)),
         persistent_grid(128, reinterpret_cast<const void *>(k_trace<false>)),
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_medium)),
-        persistent_grid(BLOCK, S.material_tex != nullptr ? reinterpret_cast<const void *>(k_shade<true>)
-                                                         : reinterpret_cast<const void *>(k_shade<false>)),
+        persistent_grid(BLOCK, reinterpret_cast<const void *>(shade_kernel(S, R))),
         persistent_grid(128, S.has_media ? reinterpret_cast<const void *>(k_shadow<true>)
                                          : reinterpret_cast<const void *>(k_shadow<false>)),
     };
@@ -1662,6 +1726,182 @@ cudaError_t launch_tonemap_aces(float *px, uint32_t pixels, int channels, float 
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- radiance-cache training paths
+
+constexpr int NRC_TRAIN_VERTS = 6;   // recorded vertices per training path
+
+// Training paths for the radiance cache: one thread traces one whole path of a training
+// pixel with the wavefront's per-path semantics (same light sampling, MIS, Russian
+// roulette and BSDF sampling; the shadow ray is traced at once), records its first
+// non-delta vertices (cache query, throughput, radiance gathered so far) and, when the
+// path ends, emits one sample per vertex whose target is the radiance the path gathered
+// after that vertex divided by the throughput at it: an unbiased estimate of the
+// vertex's outgoing radiance. Scenes with participating media are not supported here.
+template<bool TEX>
+__global__ void __launch_bounds__(128) k_nrc_train_paths(DevScene S, DevRender R, uint32_t stride, uint32_t phase,
+                                                         uint32_t sample_index, float *samples, uint32_t *count,
+                                                         uint32_t cap, uint32_t *err)
+{
+    const uint32_t pixels = static_cast<uint32_t>(R.width) * R.height;
+    const uint32_t n = phase < pixels ? (pixels - phase + stride - 1) / stride : 0;
+    const float4 *nodes = reinterpret_cast<const float4 *>(S.nodes);
+    const float4 *tris = reinterpret_cast<const float4 *>(S.tris);
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const uint32_t pixel = i * stride + phase;
+        const uint32_t px = pixel % R.width, py = pixel / R.width;
+        DSampler smp;
+        smp.type = R.sampler;
+        smp.s = sampler_init(R.sampler, R.halton, px, py, sample_index);
+        float fx, fy;
+        if(R.filter == FILTER_GAUSSIAN)
+        {
+            const uint32_t cell = alias_sample(R.filter_table, FILTER_GRID * FILTER_GRID, smp.get1d());
+            const uint32_t gy = cell / FILTER_GRID, gx = cell % FILTER_GRID;
+            const float r = R.filter_radius, w = 2 * r / FILTER_GRID;
+            fx = lerpf(-r + w * static_cast<float>(gx), -r + w * static_cast<float>(gx + 1), smp.get1d());
+            fy = lerpf(-r + w * static_cast<float>(gy), -r + w * static_cast<float>(gy + 1), smp.get1d());
+        }
+        else
+        {
+            fx = smp.get1d() - 0.5f;
+            fy = smp.get1d() - 0.5f;
+        }
+        (void)smp.get1d();
+        const float film_x = (static_cast<float>(px) + 0.5f + fx) / static_cast<float>(R.width);
+        const float film_y = (static_cast<float>(py) + 0.5f + fy) / static_cast<float>(R.height);
+        V3 o = R.cam_eye;
+        V3 d = normalize(R.cam_lbc + film_x * R.cam_fx + film_y * R.cam_fy - R.cam_eye);
+        V3 beta(1.0f), beta_le(1.0f), rad(0.0f);
+        float bsdf_pdf = -1.0f;
+        float vq[NRC_TRAIN_VERTS][NRC_QUERY_FLOATS];
+        V3 vbeta[NRC_TRAIN_VERTS], vrad[NRC_TRAIN_VERTS];
+        int nv = 0;
+        for(int depth = 0; depth < 256; ++depth)
+        {
+            const ClosestResult c = trace_closest(make_trav_ray(o.x, o.y, o.z, d.x, d.y, d.z), MAX_FLOAT, nodes, tris,
+                                                  S.node_count, err);
+            if(!c.hit)
+            {
+                rad = rad + miss_le(S, d, beta_le, bsdf_pdf);
+                break;
+            }
+            const Instance &inst = S.instances[c.inst];
+            const Geometry geo = S.geometries[inst.geometry];
+            const SurfacePoint sp = get_hitinfo(S, o, d, inst, geo.tri_offset + c.prim, c.t, c.b1, c.b2);
+            rad = rad + hit_light_le(S, o, d, sp, beta_le, bsdf_pdf, inst.light);
+            if(nv < NRC_TRAIN_VERTS && nrc_query_at<TEX>(S, sp, inst, -d, vq[nv]))
+            {
+                vbeta[nv] = beta;
+                vrad[nv] = rad;
+                ++nv;
+            }
+            if(russian_roulette(beta, depth, smp, R))
+                break;
+            LightSample ls = sample_light(S, sp.position, sp.frame.z, true, smp);
+            Material mat = S.materials[inst.material];
+            SurfaceShader sh;
+            sh.frame.geometry = sp.frame;
+            sh.frame.shading = sp.frame.rotate_to_new_z(sp.interp_z);
+            if(TEX && mat.tex >= 0)
+            {
+                const MaterialTexValues tv = eval_material_textures(S, mat.tex, sp.tu, sp.tv);
+#pragma unroll
+                for(int k = 0; k < 16; ++k)
+                    if(tv.mask & (1u << k))
+                        mat.p[k] = tv.p[k];
+                if(tv.has_normal)
+                    sh.frame.shading =
+                        sh.frame.shading.rotate_to_new_z(normalize(sh.frame.shading.local_to_global(tv.normal)));
+            }
+            sh.mat = make_material_eval(mat);
+            sh.shadow_terminator = mat.shadow_terminator != 0;
+            float u0, u1, u2;
+            smp.get3d(u0, u1, u2);
+            const V3 wo = -d;
+            const CompSample bs = sh.sample(wo, u0, u1, u2);
+            if(ls.success)
+            {
+                const V3 f = sh.eval(ls.d, wo);
+                if(!is_zero(f))
+                {
+                    const float spdf = sh.pdf(ls.d, wo);
+                    const float cs = fabsf(dot(normalize(ls.d), sp.frame.z));
+                    const V3 li = ls.li * beta * f * cs / (spdf + ls.light_pdf);
+                    if(!trace_any(make_trav_ray(ls.o.x, ls.o.y, ls.o.z, ls.d.x, ls.d.y, ls.d.z), ls.t1, nodes, tris,
+                                  S.node_count, err) &&
+                       all_finite(li))
+                        rad = rad + li;
+                }
+            }
+            if(is_zero(bs.f))
+                break;
+            const V3 ndir = normalize(bs.dir);
+            const float cn = fabsf(dot(ndir, sp.frame.z));
+            beta_le = beta * cn * bs.f;
+            beta = beta_le / bs.pdf;
+            bsdf_pdf = bs.is_delta ? -bs.pdf : bs.pdf;
+            o = offset_dir(sp.position, sp.frame.z, ndir);
+            d = ndir;
+        }
+        for(int k = 0; k < nv; ++k)
+        {
+            const V3 b = vbeta[k];
+            if(!(b.x > 1e-6f && b.y > 1e-6f && b.z > 1e-6f))
+                continue;
+            const V3 t = (rad - vrad[k]) / b;
+            if(!all_finite(t))
+                continue;
+            const uint32_t slot = atomicAdd(count, 1u);
+            if(slot >= cap)
+                break;
+            float *dst = samples + static_cast<size_t>(slot) * NRC_SAMPLE_FLOATS;
+            for(int j = 0; j < NRC_QUERY_FLOATS; ++j)
+                dst[j] = vq[k][j];
+            dst[13] = fmaxf(t.x, 0.0f);
+            dst[14] = fmaxf(t.y, 0.0f);
+            dst[15] = fmaxf(t.z, 0.0f);
+        }
+    }
+}
+
+// cache predictions times path throughput, splatted to the paths' pixels
+__global__ void k_nrc_splat(const float4 *__restrict__ pred, const float4 *__restrict__ weight, const uint32_t *count,
+                            uint32_t cap, float4 *film, int width)
+{
+    const uint32_t n = min(*count, cap);
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const float4 p = pred[i], w = weight[i];
+        splat(film, __float_as_uint(w.w), width, V3(fmaxf(p.x, 0.0f) * w.x, fmaxf(p.y, 0.0f) * w.y, fmaxf(p.z, 0.0f) * w.z));
+    }
+}
+
+cudaError_t launch_nrc_train_paths(const DevScene &S, const DevRender &R, uint32_t stride, uint32_t phase,
+                                   uint32_t sample_index, float *samples, uint32_t *count, uint32_t cap, uint32_t *err,
+                                   cudaStream_t st)
+{
+    const uint32_t pixels = static_cast<uint32_t>(R.width) * R.height;
+    const uint32_t n = phase < pixels ? (pixels - phase + stride - 1) / stride : 0;
+    if(n == 0)
+        return cudaSuccess;
+    const uint32_t blocks = (n + 127) / 128;
+    if(S.material_tex != nullptr)
+        k_nrc_train_paths<true><<<blocks, 128, 0, st>>>(S, R, stride, phase, sample_index, samples, count, cap, err);
+    else
+        k_nrc_train_paths<false><<<blocks, 128, 0, st>>>(S, R, stride, phase, sample_index, samples, count, cap, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nrc_splat(const float4 *pred, const float4 *weight, const uint32_t *count, uint32_t cap,
+                             float4 *film, int width, cudaStream_t st)
+{
+    if(cap == 0)
+        return cudaSuccess;
+    k_nrc_splat<<<std::min<uint32_t>((cap + 255) / 256, 152 * 16), 256, 0, st>>>(pred, weight, count, cap, film, width);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_resolve(const float4 *film, float *rgb, uint32_t pixels, cudaStream_t st)
 {
     if(pixels == 0)
@@ -1771,8 +2011,7 @@ cudaError_t render_wavefront_noalloc(const DevScene &S, const DevRender &R, void
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_generate)),
         persistent_grid(128, reinterpret_cast<const void *>(k_trace<false>)),
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_medium)),
-        persistent_grid(BLOCK, S.material_tex != nullptr ? reinterpret_cast<const void *>(k_shade<true>)
-                                                         : reinterpret_cast<const void *>(k_shade<false>)),
+        persistent_grid(BLOCK, reinterpret_cast<const void *>(shade_kernel(S, R))),
         persistent_grid(128, S.has_media ? reinterpret_cast<const void *>(k_shadow<true>)
                                          : reinterpret_cast<const void *>(k_shadow<false>)),
     };

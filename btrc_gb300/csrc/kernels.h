@@ -86,6 +86,14 @@ cudaError_t launch_resolve(const float4 *film, float *rgb, uint32_t pixels, cuda
 // g-buffer resolve (sum / weight; normals renormalised) into 3 floats per pixel
 cudaError_t launch_resolve_aov(const float4 *film, const float4 *aov, float *out, uint32_t pixels, bool normal,
                                cudaStream_t st);
+// radiance-cache training paths over the pixels p with p % stride == phase (sample index
+// sample_index): emits up to cap training samples (NRC_SAMPLE_FLOATS each)
+cudaError_t launch_nrc_train_paths(const DevScene &S, const DevRender &R, uint32_t stride, uint32_t phase,
+                                   uint32_t sample_index, float *samples, uint32_t *count, uint32_t cap, uint32_t *err,
+                                   cudaStream_t st);
+// film += max(pred, 0) * weight.xyz at pixel weight.w, for min(*count, cap) queries
+cudaError_t launch_nrc_splat(const float4 *pred, const float4 *weight, const uint32_t *count, uint32_t cap,
+                             float4 *film, int width, cudaStream_t st);
 // in-place ACES tone map of 3- or 4-channel float pixels
 cudaError_t launch_tonemap_aces(float *px, uint32_t pixels, int channels, float exposure, cudaStream_t st);
 

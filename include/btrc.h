@@ -265,6 +265,36 @@ btrc_status btrc_nrc_train(btrc_ctx *ctx, btrc_nrc *nrc, const float *d_samples,
    gradients (2: MLP, 3: hash); set != 0 writes parameters 0 / 1 instead */
 btrc_status btrc_nrc_params(btrc_ctx *ctx, btrc_nrc *nrc, int32_t which, float *host, uint64_t count, int32_t set);
 
+typedef struct btrc_nrc_render_opts
+{
+    uint32_t frame;            /* sample index of the frame's single path per pixel */
+    int32_t terminate_vertex;  /* paths end in a cache query at the first non-delta surface
+                                  vertex of depth >= this (1: after one bounce); -1: no cache */
+    int32_t train_stride;      /* one pixel in train_stride traces a training path; 0: none */
+    int32_t train_steps;       /* Adam steps per frame */
+    int32_t train_batch;       /* training samples per step */
+    int32_t output_on_device;  /* 1: rgb_out is a device pointer */
+} btrc_nrc_render_opts;
+
+typedef struct btrc_nrc_frame_stats
+{
+    uint64_t paths;            /* camera paths of the frame */
+    uint64_t queries;          /* paths that ended in a cache query */
+    uint64_t train_samples;    /* training samples produced */
+    int32_t train_steps;
+    float loss;                /* mean training loss of the frame's steps */
+    double render_ms;          /* GPU time of the wavefront loop */
+    double wall_ms;            /* host wall time of the call */
+} btrc_nrc_frame_stats;
+
+/* One frame of one path per pixel through the wavefront renderer with paths terminated
+   into the radiance cache, training paths for 1 / train_stride of the pixels, cache
+   inference and splatting, then the frame's Adam steps. rgb_out receives the frame's
+   width*height*3 image (radiance / weight). Scenes with participating media:
+   BTRC_ERR_UNSUPPORTED. */
+btrc_status btrc_render_nrc_frame(btrc_ctx *ctx, btrc_scene *scene, btrc_nrc *nrc, const btrc_nrc_render_opts *opts,
+                                  float *rgb_out, btrc_nrc_frame_stats *stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -95,3 +95,38 @@ def test_training_reduces_loss(gpu_ctx):
     assert np.isfinite(losses).all()
     assert last < first / 10, (first, last)
     c.close()
+
+
+def _relmse(a, r):
+    return float(np.mean((a - r) ** 2 / (r ** 2 + 1e-2)))
+
+
+def test_cache_render_off_matches_plain_and_training_helps(gpu_ctx, scene_dir):
+    # with the cache off a frame is exactly the plain renderer's single sample; with it on,
+    # the trained cache must beat terminating paths into the untrained network (the
+    # method without learning) by a wide margin on the same frames
+    from btrc_gb300 import scenes
+    p = scenes.cornell(out_dir=scene_dir / "cornell", width=64, height=64, spp=1)
+    sc = gpu_ctx.load_scene(p).build()
+    info = sc.info()
+    ref = gpu_ctx.render(sc, spp=2048).astype(np.float64)
+    cache = B.RadianceCache(gpu_ctx, info.world_min, info.world_max, seed=1)
+    f0 = cache.render_frame(sc, 0, terminate_vertex=-1, train_stride=0, train_steps=0)
+    assert np.array_equal(f0, gpu_ctx.render(sc, spp=1))
+    frames = 96
+    res = {}
+    for mode, steps in (("trained", 4), ("untrained", 0)):
+        c = B.RadianceCache(gpu_ctx, info.world_min, info.world_max, seed=2)
+        acc = np.zeros_like(ref)
+        st, losses = {}, []
+        for f in range(frames):
+            acc += c.render_frame(sc, f, terminate_vertex=1, train_stride=4, train_steps=steps, train_batch=4096,
+                                  stats=st)
+            losses.append(st["loss"])
+        assert st["queries"] > 0.5 * 64 * 64
+        res[mode] = _relmse(acc / frames, ref)
+        if steps:
+            assert st["train_samples"] > 0 and np.isfinite(losses).all()
+            assert np.mean(losses[-8:]) < np.mean(losses[:4])
+        c.close()
+    assert res["trained"] < 0.5 * res["untrained"], res
