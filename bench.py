@@ -45,6 +45,9 @@ def parse():
     ap.add_argument("--state-count", type=int, default=2 * 1024 * 1024)
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-nrc", action="store_true", help="skip the radiance-cache equal-time study")
+    ap.add_argument("--nrc-frames", type=int, default=256, help="frames of the radiance-cache study")
+    ap.add_argument("--ref-spp", type=int, default=4096, help="spp of the converged reference image")
     return ap.parse_args()
 
 
@@ -192,6 +195,90 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def _time_to(curve, target):
+    """First time at which a (time_ms, relMSE) curve reaches target, interpolated in
+    log-log between the bracketing points; None if it never does."""
+    prev = None
+    for t, e in curve:
+        if e <= target:
+            if prev is None:
+                return t
+            (t0, e0), (t1, e1) = prev, (t, e)
+            if e0 <= 0 or e1 <= 0 or e0 == e1:
+                return t1
+            a = (np.log(target) - np.log(e0)) / (np.log(e1) - np.log(e0))
+            return float(np.exp(np.log(t0) + a * (np.log(t1) - np.log(t0))))
+        prev = (t, e)
+    return None
+
+
+def nrc_study(B, ctx, sc, info, args):
+    """Equal-time comparison of the radiance cache against the plain tracer on the
+    benchmark scene: relMSE against a converged plain render (args.ref_spp spp) as a
+    function of wall time, for plain renders of 1..128 spp and for the cache (one path per
+    pixel per frame, paths ending in the cache after one bounce, 1/16 of the pixels
+    tracing training paths, 4 Adam steps of 16384 samples per frame, trained from scratch
+    inside the timed region)."""
+    import torch
+    W, H = info.width, info.height
+    img = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
+    t = time.perf_counter()
+    ctx.render(sc, spp=args.ref_spp, out=img)
+    torch.cuda.synchronize()
+    ref_s = time.perf_counter() - t
+    ref = img.clone().double()
+    den = ref * ref + 1e-2
+
+    def relmse(x):
+        return float(((x.double() - ref) ** 2 / den).mean())
+    target = 1e-2
+    plain = []
+    for spp in (1, 2, 4, 8, 16, 32, 64, 128):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        ctx.render(sc, spp=spp, out=img)
+        torch.cuda.synchronize()
+        plain.append(((time.perf_counter() - t) * 1000, relmse(img)))
+    cache = B.RadianceCache(ctx, info.world_min, info.world_max, seed=1)
+    acc = torch.zeros((H, W, 3), dtype=torch.float64, device="cuda")
+    curve, elapsed, st = [], 0.0, {}
+    checkpoints = {1, 2, 4, 8, 16, 24, 32, 48, 64, 96, 128, 192, 256, 384, 512}
+    losses, queries, samples = [], 0, 0
+    for f in range(args.nrc_frames):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        cache.render_frame(sc, f, out=img, terminate_vertex=1, train_stride=16, train_steps=4, train_batch=16384,
+                           stats=st)
+        acc += img
+        torch.cuda.synchronize()
+        elapsed += (time.perf_counter() - t) * 1000
+        losses.append(st["loss"])
+        queries, samples = st["queries"], st["train_samples"]
+        if f + 1 in checkpoints or f + 1 == args.nrc_frames:
+            curve.append((elapsed, relmse(acc / (f + 1))))
+    cache.close()
+    tp, tn = _time_to(plain, target), _time_to(curve, target)
+    # the cache's relMSE at the plain tracer's time to reach the target, and vice versa
+    at_plain = None
+    if tp is not None:
+        below = [e for t, e in curve if t <= tp]
+        at_plain = below[-1] if below else None
+    return {
+        "target_relmse": target, "reference_spp": args.ref_spp, "reference_s": ref_s,
+        "plain_curve_ms_relmse": [[round(t, 3), e] for t, e in plain],
+        "nrc_curve_ms_relmse": [[round(t, 3), e] for t, e in curve],
+        "plain_ms_to_target": tp, "nrc_ms_to_target": tn,
+        "time_ratio_nrc_over_plain": (tn / tp) if (tp and tn) else None,
+        "nrc_relmse_at_plain_time": at_plain,
+        "nrc_frames": args.nrc_frames, "nrc_ms_per_frame": elapsed / args.nrc_frames,
+        "nrc_queries_per_frame": queries, "nrc_train_samples_per_frame": samples,
+        "nrc_loss_first_last": [float(np.mean(losses[:4])), float(np.mean(losses[-4:]))],
+        "setup": "paths end in the cache at the first non-delta vertex after one bounce; 1/16 of the pixels "
+                 "trace training paths each frame; 4 Adam steps x 16384 samples per frame; cache trained "
+                 "from scratch inside the timed frames",
+    }
+
+
 def run_ours(args, world, rank, local):
     import torch
 
@@ -272,6 +359,13 @@ def run_ours(args, world, rank, local):
         except ValueError:
             traffic = None
 
+    nrc = None
+    if rank == 0 and not args.no_nrc:
+        try:
+            nrc = nrc_study(B, ctx, sc, info, args)
+        except Exception as ex:  # the study must not sink the throughput number
+            nrc = {"error": str(ex)}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
@@ -309,6 +403,7 @@ def run_ours(args, world, rank, local):
                          "dominant_stage": dom},
             "cpu_baseline": cpu,
             "clocks": clk,
+            "radiance_cache": nrc,
             "mrays_per_s": world * (st["extension_rays"] + st["shadow_rays"]) / (step_ms / 1000) / 1e6,
             "scene_load_s": load_s, "bvh_build_ms": info.build_ms,
         }

@@ -1190,19 +1190,19 @@ btrc_status btrc_render_nrc_frame(btrc_ctx *ctx, btrc_scene *scene, btrc_nrc *nr
         const uint32_t ns = std::min<uint32_t>(counts[1], static_cast<uint32_t>(sample_cap));
         float loss = 0.0f;
         int steps = 0;
+        check_cuda(nrc->impl->reset_loss(s), "cache training");
         for(int k = 0; k < opts->train_steps; ++k)
         {
             const uint32_t b0 = static_cast<uint32_t>(k) * static_cast<uint32_t>(opts->train_batch);
             if(b0 >= ns)
                 break;
             const uint32_t nb = std::min<uint32_t>(static_cast<uint32_t>(opts->train_batch), ns - b0);
-            float l = 0.0f;
-            check_cuda(nrc->impl->train(ctx->nrc_samples + static_cast<size_t>(b0) * NRC_SAMPLE_FLOATS, nb,
-                                        fstats ? &l : nullptr, true, s),
+            check_cuda(nrc->impl->train(ctx->nrc_samples + static_cast<size_t>(b0) * NRC_SAMPLE_FLOATS, nb, true, s),
                        "cache training");
-            loss += l;
             ++steps;
         }
+        if(fstats && steps)
+            check_cuda(nrc->impl->read_loss(&loss, s), "cache training");
         if(!on_dev)
             check_cuda(cudaMemcpyAsync(rgb_out, rgb_dev, pixels * 3 * sizeof(float), cudaMemcpyDeviceToHost, s),
                        "image download");
@@ -1283,10 +1283,13 @@ btrc_status btrc_nrc_train(btrc_ctx *ctx, btrc_nrc *nrc, const float *d_samples,
         return BTRC_ERR_INVALID_ARG;
     return guarded(ctx, [&] {
         check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
-        check_cuda(nrc->impl->train(d_samples, static_cast<uint32_t>(n), loss_out, apply_adam != 0, ctx->stream),
+        check_cuda(nrc->impl->reset_loss(ctx->stream), "radiance cache training");
+        check_cuda(nrc->impl->train(d_samples, static_cast<uint32_t>(n), apply_adam != 0, ctx->stream),
                    "radiance cache training");
-        if(!loss_out)
-            check_cuda(cudaStreamSynchronize(ctx->stream), "radiance cache training");
+        float l = 0.0f;
+        check_cuda(nrc->impl->read_loss(&l, ctx->stream), "radiance cache training");
+        if(loss_out)
+            *loss_out = l;
     });
 }
 

@@ -569,69 +569,73 @@ __global__ void __launch_bounds__(NRC_BLOCK) k_nrc_train(NrcDev D, const float *
 
 // ------------------------------------------------------------------ weight gradients
 
-// dW_l[K][N] += X_l^T dY_l over a chunk of rows, on the tensor cores: A = X^T (K x rows),
-// B = dY (rows x N). Rows are staged transposed in shared memory so that fragments load
-// as 32-bit pairs; every warp owns a set of 16 x 8 output tiles.
-constexpr int WG_ROWS = 128;             // rows per stage
+// dW_l[K][N] += X_l^T dY_l over 128 rows per block, for all layers at once (blockIdx.y =
+// layer), on the tensor cores: A = X^T (K x rows), B = dY (rows x N). Rows are staged
+// transposed in shared memory (an odd word stride keeps the transposing stores free of
+// bank conflicts) so that fragments load as 32-bit pairs; every warp owns up to five
+// 16 x 8 output tiles and adds them to the FP32 gradient with atomics.
+constexpr int WG_ROWS = 128;
 constexpr int WG_BLOCK = 256;
+constexpr int WG_STRIDE = WG_ROWS + 2;    // 65 words per staged row
 
 __global__ void __launch_bounds__(WG_BLOCK) k_nrc_wgrad(const __nv_bfloat16 *__restrict__ act,
-                                                        const __nv_bfloat16 *__restrict__ dact, uint32_t n, int l,
-                                                        uint32_t rows_per_block, float *__restrict__ dw)
+                                                        const __nv_bfloat16 *__restrict__ dact, uint32_t n,
+                                                        float *__restrict__ dw_all)
 {
-    __shared__ __nv_bfloat16 sxt[NRC_IN][WG_ROWS + 8];
-    __shared__ __nv_bfloat16 sdt[NRC_WIDTH][WG_ROWS + 8];
+    __shared__ __nv_bfloat16 sxt[NRC_IN][WG_STRIDE];
+    __shared__ __nv_bfloat16 sdt[NRC_WIDTH][WG_STRIDE];
+    const int l = blockIdx.y;
     const int K = layer_k(l), N = layer_n(l);
-    const int mtiles = K / 16, ntiles = N / 8, tiles = mtiles * ntiles;
+    const int ntiles = N / 8, tiles = (K / 16) * ntiles;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = WG_BLOCK / 32;
     const int g = lane >> 2, t = lane & 3;
     constexpr int MAXT = 5;                    // at most 40 tiles over 8 warps
     float acc[MAXT][4];
+#pragma unroll
     for(int i = 0; i < MAXT; ++i)
         acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = 0.0f;
-    const uint32_t r_begin = blockIdx.x * rows_per_block;
-    const uint32_t r_end = min(n, r_begin + rows_per_block);
+    const uint32_t r0 = blockIdx.x * WG_ROWS;
     const int acol = act_cols_before(l), dcol = dact_cols_before(l);
-    for(uint32_t r0 = r_begin; r0 < r_end; r0 += WG_ROWS)
+    // stage: consecutive threads read consecutive columns of a row (coalesced) and store
+    // them down a column of the transposed tile
+    for(int i = threadIdx.x; i < WG_ROWS * K; i += WG_BLOCK)
     {
-        __syncthreads();
-        for(int i = threadIdx.x; i < WG_ROWS * K; i += WG_BLOCK)
-        {
-            const int r = i / K, k = i % K;
-            const uint32_t row = r0 + r;
-            sxt[k][r] = row < r_end ? act[static_cast<size_t>(row) * ACT_COLS + acol + k] : __float2bfloat16_rn(0.0f);
-        }
-        for(int i = threadIdx.x; i < WG_ROWS * N; i += WG_BLOCK)
-        {
-            const int r = i / N, c = i % N;
-            const uint32_t row = r0 + r;
-            sdt[c][r] = row < r_end ? dact[static_cast<size_t>(row) * DACT_COLS + dcol + c] : __float2bfloat16_rn(0.0f);
-        }
-        __syncthreads();
+        const int r = i / K, k = i % K;
+        const uint32_t row = r0 + r;
+        sxt[k][r] = row < n ? act[static_cast<size_t>(row) * ACT_COLS + acol + k] : __float2bfloat16_rn(0.0f);
+    }
+    for(int i = threadIdx.x; i < WG_ROWS * N; i += WG_BLOCK)
+    {
+        const int r = i / N, c = i % N;
+        const uint32_t row = r0 + r;
+        sdt[c][r] = row < n ? dact[static_cast<size_t>(row) * DACT_COLS + dcol + c] : __float2bfloat16_rn(0.0f);
+    }
+    __syncthreads();
+#pragma unroll
+    for(int slot = 0; slot < MAXT; ++slot)
+    {
+        const int tile = warp + slot * nwarps;
+        if(tile >= tiles)
+            break;
+        const int mt = tile / ntiles, nt = tile % ntiles;
+#pragma unroll 4
         for(int kk = 0; kk < WG_ROWS / 16; ++kk)
         {
-#pragma unroll
-            for(int slot = 0; slot < MAXT; ++slot)
-            {
-                const int tile = warp + slot * nwarps;
-                if(tile >= tiles)
-                    break;
-                const int mt = tile / ntiles, nt = tile % ntiles;
-                uint32_t a[4];
-                const __nv_bfloat16 *ar0 = &sxt[mt * 16 + g][kk * 16 + 2 * t];
-                const __nv_bfloat16 *ar1 = &sxt[mt * 16 + g + 8][kk * 16 + 2 * t];
-                a[0] = *reinterpret_cast<const uint32_t *>(ar0);
-                a[1] = *reinterpret_cast<const uint32_t *>(ar1);
-                a[2] = *reinterpret_cast<const uint32_t *>(ar0 + 8);
-                a[3] = *reinterpret_cast<const uint32_t *>(ar1 + 8);
-                const __nv_bfloat16 *br = &sdt[nt * 8 + g][kk * 16 + 2 * t];
-                uint2 b;
-                b.x = *reinterpret_cast<const uint32_t *>(br);
-                b.y = *reinterpret_cast<const uint32_t *>(br + 8);
-                mma(acc[slot], a, b);
-            }
+            uint32_t a[4];
+            const __nv_bfloat16 *ar0 = &sxt[mt * 16 + g][kk * 16 + 2 * t];
+            const __nv_bfloat16 *ar1 = &sxt[mt * 16 + g + 8][kk * 16 + 2 * t];
+            a[0] = *reinterpret_cast<const uint32_t *>(ar0);
+            a[1] = *reinterpret_cast<const uint32_t *>(ar1);
+            a[2] = *reinterpret_cast<const uint32_t *>(ar0 + 8);
+            a[3] = *reinterpret_cast<const uint32_t *>(ar1 + 8);
+            const __nv_bfloat16 *br = &sdt[nt * 8 + g][kk * 16 + 2 * t];
+            uint2 b;
+            b.x = *reinterpret_cast<const uint32_t *>(br);
+            b.y = *reinterpret_cast<const uint32_t *>(br + 8);
+            mma(acc[slot], a, b);
         }
     }
+    float *dw = dw_all + w_offset(l);
 #pragma unroll
     for(int slot = 0; slot < MAXT; ++slot)
     {
@@ -858,23 +862,25 @@ cudaError_t Nrc::infer(const float *d_queries, uint32_t n, float *d_out, cudaStr
     return cudaGetLastError();
 }
 
-cudaError_t Nrc::train(const float *d_samples, uint32_t n, float *loss_out, bool apply_adam, cudaStream_t st)
+cudaError_t Nrc::reset_loss(cudaStream_t st) { return cudaMemsetAsync(loss_, 0, sizeof(float), st); }
+
+cudaError_t Nrc::read_loss(float *out, cudaStream_t st)
+{
+    NRC_CHECK(cudaMemcpyAsync(out, loss_, sizeof(float), cudaMemcpyDeviceToHost, st));
+    return cudaStreamSynchronize(st);
+}
+
+cudaError_t Nrc::train(const float *d_samples, uint32_t n, bool apply_adam, cudaStream_t st)
 {
     if(n == 0)
         return cudaSuccess;
     NRC_CHECK(ensure_batch(n));
-    NRC_CHECK(cudaMemsetAsync(loss_, 0, sizeof(float), st));
     const uint32_t tiles = (n + 15) / 16;
     const uint32_t blocks = std::min<uint32_t>((tiles + NRC_WARPS - 1) / NRC_WARPS, static_cast<uint32_t>(sm_count()) * 4);
     k_nrc_train<<<blocks, NRC_BLOCK, train_smem(), st>>>(d_, d_samples, n, hyper_.rel_eps);
     NRC_CHECK(cudaGetLastError());
-    const uint32_t rows_per_block = 1024;
-    const uint32_t wblocks = (n + rows_per_block - 1) / rows_per_block;
-    for(int l = 0; l < NRC_LAYERS; ++l)
-    {
-        k_nrc_wgrad<<<wblocks, WG_BLOCK, 0, st>>>(act_, dact_, n, l, rows_per_block, w_grad_ + w_offset(l));
-        NRC_CHECK(cudaGetLastError());
-    }
+    k_nrc_wgrad<<<dim3((n + WG_ROWS - 1) / WG_ROWS, NRC_LAYERS), WG_BLOCK, 0, st>>>(act_, dact_, n, w_grad_);
+    NRC_CHECK(cudaGetLastError());
     if(apply_adam)
     {
         ++step_;
@@ -891,11 +897,6 @@ cudaError_t Nrc::train(const float *d_samples, uint32_t n, float *loss_out, bool
                                                    hcount, lr_t, hyper_.beta1, hyper_.beta2, hyper_.eps);
         NRC_CHECK(cudaGetLastError());
         NRC_CHECK(repack(st));
-    }
-    if(loss_out)
-    {
-        NRC_CHECK(cudaMemcpyAsync(loss_out, loss_, sizeof(float), cudaMemcpyDeviceToHost, st));
-        NRC_CHECK(cudaStreamSynchronize(st));
     }
     return cudaSuccess;
 }

@@ -66,9 +66,12 @@ public:
 
     // predictions (3 floats per query, 4-float stride) for n queries
     cudaError_t infer(const float *d_queries, uint32_t n, float *d_out, cudaStream_t st);
-    // one optimisation step over n training samples; *loss_out receives the mean loss when
-    // non-null (synchronises). apply_adam = false computes gradients only.
-    cudaError_t train(const float *d_samples, uint32_t n, float *loss_out, bool apply_adam, cudaStream_t st);
+    // one optimisation step over n training samples; its mean loss is added to a device
+    // accumulator (reset_loss / read_loss). apply_adam = false computes gradients only.
+    cudaError_t train(const float *d_samples, uint32_t n, bool apply_adam, cudaStream_t st);
+    cudaError_t reset_loss(cudaStream_t st);
+    // synchronises st and returns the accumulated loss
+    cudaError_t read_loss(float *out, cudaStream_t st);
 
     // parameters / gradients as FP32 host copies (test hooks). which: 0 MLP weights
     // (NRC_WEIGHTS, layer-major, row-major K x N), 1 hash features (LEVELS * TABLE * 2),
