@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-nrc", action="store_true", help="skip the radiance-cache equal-time study")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched uneven-scenes measurement")
     ap.add_argument("--nrc-frames", type=int, default=256, help="frames of the radiance-cache study")
     ap.add_argument("--ref-spp", type=int, default=4096, help="spp of the converged reference image")
     return ap.parse_args()
@@ -279,6 +280,53 @@ def nrc_study(B, ctx, sc, info, args):
     }
 
 
+def batch_study(B, ctx):
+    """Batched uneven scenes (64 seeded terrain scenes, 1e4..5e5 triangles, 128^2..512^2,
+    16..64 spp, depth 12): aggregate Mpaths/s rendering them one after another with the
+    default settings, and through 4 concurrent lanes with the autotuner's queue capacity
+    and grid size (autotuning probes run before the timed batch)."""
+    import torch
+    from btrc_gb300 import scenes
+    paths = scenes.batch(count=64, seed=1004)
+    t = time.perf_counter()
+    scs = [ctx.load_scene(p).build() for p in paths]
+    build_s = time.perf_counter() - t
+    infos = [s.info() for s in scs]
+    outs = [torch.empty((i.height, i.width, 3), dtype=torch.float32, device="cuda") for i in infos]
+    total_paths = sum(i.width * i.height * i.spp for i in infos)
+    for s, o in zip(scs, outs):  # warm
+        ctx.render(s, out=o)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    per = []
+    for s, o in zip(scs, outs):
+        t1 = time.perf_counter()
+        ctx.render(s, out=o)
+        per.append((time.perf_counter() - t1) * 1000)
+    torch.cuda.synchronize()
+    seq_ms = (time.perf_counter() - t) * 1000
+    ctx.render_batch(scs, outs, lanes=4, autotune=True)  # tunes and warms
+    runs = []
+    for _ in range(3):
+        stats, total_ms = ctx.render_batch(scs, outs, lanes=4, autotune=True)
+        runs.append(total_ms)
+    batch_ms = float(np.median(runs))
+    caps = sorted({(st["capacity"], st["grid_pct"]) for st in stats})
+    for s in scs:
+        s.close()
+    return {
+        "scenes": len(scs), "total_paths": total_paths, "triangles_range": [min(i.triangles for i in infos),
+                                                                             max(i.triangles for i in infos)],
+        "sequential_mpaths_s": total_paths / (seq_ms / 1000) / 1e6, "sequential_ms": seq_ms,
+        "batched_mpaths_s": total_paths / (batch_ms / 1000) / 1e6, "batched_ms": batch_ms, "lanes": 4,
+        "per_scene_ms_sequential": {"min": min(per), "median": float(np.median(per)), "max": max(per)},
+        "per_scene_ms_batched": {"min": min(st["ms"] for st in stats),
+                                 "median": float(np.median([st["ms"] for st in stats])),
+                                 "max": max(st["ms"] for st in stats)},
+        "autotuned_capacity_grid_pct": caps, "scene_build_s": build_s,
+    }
+
+
 def run_ours(args, world, rank, local):
     import torch
 
@@ -359,6 +407,13 @@ def run_ours(args, world, rank, local):
         except ValueError:
             traffic = None
 
+    batch = None
+    if rank == 0 and not args.no_batch:
+        try:
+            batch = batch_study(B, ctx)
+        except Exception as ex:  # the study must not sink the throughput number
+            batch = {"error": str(ex)}
+
     nrc = None
     if rank == 0 and not args.no_nrc:
         try:
@@ -404,6 +459,7 @@ def run_ours(args, world, rank, local):
             "cpu_baseline": cpu,
             "clocks": clk,
             "radiance_cache": nrc,
+            "batch": batch,
             "mrays_per_s": world * (st["extension_rays"] + st["shadow_rays"]) / (step_ms / 1000) / 1e6,
             "scene_load_s": load_s, "bvh_build_ms": info.build_ms,
         }

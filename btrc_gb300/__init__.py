@@ -70,6 +70,15 @@ class NrcFrameStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class BatchOpts(C.Structure):
+    _fields_ = [("lanes", C.c_int32), ("autotune", C.c_int32), ("output_on_device", C.c_int32)]
+
+
+class BatchSceneStats(C.Structure):
+    _fields_ = [("paths", C.c_uint64), ("ms", C.c_double), ("lane", C.c_int32), ("capacity", C.c_uint32),
+                ("grid_pct", C.c_int32), ("pad", C.c_int32)]
+
+
 STAGES = ("control", "generate", "trace", "medium", "shade", "shadow")
 
 
@@ -115,6 +124,8 @@ SIGNATURES = {
     "btrc_nrc_infer": (C.c_int, [_vp, _vp, _vp, C.c_uint64, _vp, _vp]),
     "btrc_nrc_train": (C.c_int, [_vp, _vp, _vp, C.c_uint64, C.c_int32, C.POINTER(C.c_float)]),
     "btrc_nrc_params": (C.c_int, [_vp, _vp, C.c_int32, _vp, C.c_uint64, C.c_int32]),
+    "btrc_render_batch": (C.c_int, [_vp, C.POINTER(_vp), C.c_uint32, C.POINTER(BatchOpts), C.POINTER(_vp),
+                                    C.POINTER(BatchSceneStats), C.POINTER(C.c_double)]),
     "btrc_render_nrc_frame": (C.c_int, [_vp, _vp, _vp, C.POINTER(NrcRenderOpts), _vp, C.POINTER(NrcFrameStats)]),
     "btrc_image_load": (C.c_int, [_vp, C.c_char_p, _vp, C.c_uint64, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                   C.POINTER(C.c_int32)]),
@@ -231,6 +242,20 @@ class Context:
         if stats is not None:
             stats.update(st.as_dict())
         return out
+
+    def render_batch(self, scenes: list, outs: list, lanes: int = 4, autotune: bool = True) -> tuple[list, float]:
+        """Render many built scenes through concurrent lanes (btrc_render_batch). outs are
+        CUDA tensors or host arrays of each scene's (H, W, 3). Returns (per-scene stats,
+        total wall ms)."""
+        n = len(scenes)
+        on_dev = n > 0 and hasattr(outs[0], "is_cuda") and outs[0].is_cuda
+        arr_s = (_vp * n)(*[s.handle for s in scenes])
+        arr_o = (_vp * n)(*[_ptr(o) for o in outs])
+        st = (BatchSceneStats * n)()
+        total = C.c_double()
+        opts = BatchOpts(lanes, 1 if autotune else 0, 1 if on_dev else 0)
+        self._check(self._lib.btrc_render_batch(self.handle, arr_s, n, C.byref(opts), arr_o, st, C.byref(total)))
+        return [{k: getattr(x, k) for k, _ in BatchSceneStats._fields_ if k != "pad"} for x in st], total.value
 
     def render_noalloc(self, scene: "Scene", out, spp: int = 0, stats: dict | None = None):
         """Allocation-free render into a caller-owned CUDA tensor of shape (H, W, 3)

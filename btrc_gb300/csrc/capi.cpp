@@ -1,12 +1,16 @@
 // C-ABI implementation: host runtime around the CUDA kernels. No C++ exception
 // crosses this boundary; every failure becomes a btrc_status plus a message.
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <cstring>
 #include <memory>
 #include <mutex>
 #include <new>
+#include <numeric>
+#include <map>
 #include <set>
+#include <thread>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -21,6 +25,20 @@
 #include "scene.h"
 
 using namespace bt;
+
+// One render lane of the batch renderer: its own stream, queues, film and scratch.
+struct BatchLane
+{
+    cudaStream_t stream = nullptr;
+    RenderBuffers buf{};
+    std::vector<void *> allocs;
+    uint32_t capacity = 0;
+    size_t pixels = 0;
+    float *rgb = nullptr;      // device image for host outputs
+    size_t rgb_pixels = 0;
+    uint32_t *err = nullptr;
+    ~BatchLane();
+};
 
 struct btrc_ctx
 {
@@ -37,6 +55,9 @@ struct btrc_ctx
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
     std::set<btrc_scene *> scenes;  // live scenes, destroyed with the context
+    // batched rendering: concurrent lanes and the autotuner's choices per scene class
+    std::vector<std::unique_ptr<struct BatchLane>> lanes;
+    std::map<std::pair<int, int>, std::pair<uint32_t, int>> tuned;  // (pixel class, triangle class) -> (capacity, grid %)
     // radiance-cache frame buffers (queries, weights, predictions, training samples)
     std::vector<void *> nrc_allocs;
     size_t nrc_pixels = 0, nrc_sample_cap = 0;
@@ -388,20 +409,16 @@ void build_scene(btrc_scene *sc, int threads)
     sc->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
-void ensure_render_buffers(btrc_ctx *ctx, uint32_t capacity, size_t pixels)
+// path queues, shadow queue, hit records, film and counters for `capacity` states
+void alloc_render_buffers(RenderBuffers &B, std::vector<void *> &allocs, uint32_t capacity, size_t pixels)
 {
-    if(ctx->buf_capacity >= capacity && ctx->film_pixels == pixels)
-        return;
-    check_cuda(cudaStreamSynchronize(ctx->stream), "stream sync");
-    for(void *p : ctx->buf_allocs)
+    for(void *p : allocs)
         cudaFree(p);
-    ctx->buf_allocs.clear();
-    if(ctx->buf.host_counters)
-        cudaFreeHost(ctx->buf.host_counters);
-    ctx->buf = RenderBuffers{};
-    ctx->buf_capacity = 0;
-    RenderBuffers &B = ctx->buf;
-    auto A = [&](size_t bytes) { return dev_alloc(ctx->buf_allocs, bytes); };
+    allocs.clear();
+    if(B.host_counters)
+        cudaFreeHost(B.host_counters);
+    B = RenderBuffers{};
+    auto A = [&](size_t bytes) { return dev_alloc(allocs, bytes); };
     for(int k = 0; k < 2; ++k)
     {
         B.path[k].beta_depth = static_cast<F4 *>(A(sizeof(F4) * capacity));
@@ -423,6 +440,15 @@ void ensure_render_buffers(btrc_ctx *ctx, uint32_t capacity, size_t pixels)
     check_cuda(cudaMallocHost(&hc, sizeof(Counters) * RING_SLOTS), "cudaMallocHost");
     B.host_counters = static_cast<Counters *>(hc);
     B.capacity = capacity;
+}
+
+void ensure_render_buffers(btrc_ctx *ctx, uint32_t capacity, size_t pixels)
+{
+    if(ctx->buf_capacity >= capacity && ctx->film_pixels == pixels)
+        return;
+    check_cuda(cudaStreamSynchronize(ctx->stream), "stream sync");
+    ctx->buf_capacity = 0;
+    alloc_render_buffers(ctx->buf, ctx->buf_allocs, capacity, pixels);
     ctx->buf_capacity = capacity;
     ctx->film_pixels = pixels;
 }
@@ -479,6 +505,7 @@ DevRender make_render_params(const btrc_scene *sc, int spp, uint32_t capacity)
     R.cam_fx = H.camera.film_x;
     R.cam_fy = H.camera.film_y;
     R.sample_offset = 0;
+    R.grid_pct = 100;
     R.nrc_terminate = -1;
     return R;
 }
@@ -1303,6 +1330,241 @@ btrc_status btrc_nrc_params(btrc_ctx *ctx, btrc_nrc *nrc, int32_t which, float *
         if(e == cudaErrorInvalidValue)
             throw StatusError(BTRC_ERR_INVALID_ARG, "parameter count mismatch");
         check_cuda(e, "radiance cache parameters");
+    });
+}
+
+BatchLane::~BatchLane()
+{
+    if(stream)
+        cudaStreamSynchronize(stream);
+    for(void *p : allocs)
+        cudaFree(p);
+    if(buf.host_counters)
+        cudaFreeHost(buf.host_counters);
+    if(rgb)
+        cudaFree(rgb);
+    if(err)
+        cudaFree(err);
+    if(stream)
+        cudaStreamDestroy(stream);
+}
+
+namespace {
+
+int ilog2(uint64_t v)
+{
+    int r = 0;
+    while(v > 1)
+    {
+        v >>= 1;
+        ++r;
+    }
+    return r;
+}
+
+std::pair<int, int> scene_class(const btrc_scene *sc)
+{
+    const uint64_t pixels = static_cast<uint64_t>(sc->host.params.width) * sc->host.params.height;
+    return { ilog2(pixels), ilog2(std::max<uint64_t>(sc->host.triangle_count, 1)) / 2 };
+}
+
+void lane_prepare(BatchLane &L, uint32_t capacity, size_t pixels, bool host_out)
+{
+    if(!L.stream)
+        check_cuda(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    if(!L.err)
+    {
+        check_cuda(cudaMalloc(&L.err, 256), "cudaMalloc");
+        check_cuda(cudaMemset(L.err, 0, 256), "cudaMemset");
+    }
+    if(L.capacity < capacity || L.pixels < pixels)
+    {
+        check_cuda(cudaStreamSynchronize(L.stream), "stream sync");
+        const uint32_t cap = std::max(L.capacity, capacity);
+        const size_t px = std::max(L.pixels, pixels);
+        L.capacity = 0;
+        alloc_render_buffers(L.buf, L.allocs, cap, px);
+        L.capacity = cap;
+        L.pixels = px;
+    }
+    if(host_out && L.rgb_pixels < pixels)
+    {
+        check_cuda(cudaStreamSynchronize(L.stream), "stream sync");
+        if(L.rgb)
+            cudaFree(L.rgb);
+        L.rgb = nullptr;
+        L.rgb_pixels = 0;
+        check_cuda(cudaMalloc(&L.rgb, pixels * 3 * sizeof(float)), "cudaMalloc");
+        L.rgb_pixels = pixels;
+    }
+}
+
+// one scene through one lane; returns the wall milliseconds
+double lane_render(btrc_ctx *ctx, BatchLane &L, btrc_scene *sc, uint32_t capacity, int grid_pct, float *out,
+                   bool on_dev, int spp_override, RenderStats &rs)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    const HostScene &H = sc->host;
+    const size_t pixels = static_cast<size_t>(H.params.width) * H.params.height;
+    const int spp = spp_override > 0 ? spp_override : H.params.spp;
+    const uint64_t total = static_cast<uint64_t>(spp) * pixels;
+    capacity = static_cast<uint32_t>(std::min<uint64_t>(capacity, std::max<uint64_t>(total, 1)));
+    lane_prepare(L, capacity, pixels, !on_dev);
+    check_cuda(cudaMemsetAsync(L.buf.film, 0, sizeof(float4) * pixels, L.stream), "film clear");
+    DevRender R = make_render_params(sc, spp, capacity);
+    R.grid_pct = grid_pct;
+    L.buf.capacity = capacity;
+    bool cancelled = false;
+    check_cuda(render_wavefront(sc->dev, R, L.buf, L.stream, &ctx->cancel, true, 0, &rs, &cancelled), "batch render");
+    if(out)
+    {
+        float *dst = on_dev ? out : L.rgb;
+        check_cuda(launch_resolve(L.buf.film, dst, static_cast<uint32_t>(pixels), L.stream), "resolve");
+        if(!on_dev)
+            check_cuda(cudaMemcpyAsync(out, L.rgb, pixels * 3 * sizeof(float), cudaMemcpyDeviceToHost, L.stream),
+                       "image download");
+    }
+    check_cuda(cudaStreamSynchronize(L.stream), "lane sync");
+    if(rs.err)
+        throw StatusError(BTRC_ERR_INTERNAL, "traversal stack overflow reported by the device");
+    if(cancelled)
+        throw StatusError(BTRC_ERR_CANCELLED, "render cancelled");
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+// Autotuner: per scene class, probe queue capacities and grid sizes on one lane with a
+// short render (about 2^20 paths) and keep the fastest per path.
+void autotune(btrc_ctx *ctx, btrc_scene *const *scenes, uint32_t n)
+{
+    if(ctx->lanes.empty())
+        ctx->lanes.push_back(std::make_unique<BatchLane>());
+    BatchLane &L = *ctx->lanes[0];
+    for(uint32_t i = 0; i < n; ++i)
+    {
+        const auto key = scene_class(scenes[i]);
+        if(ctx->tuned.count(key))
+            continue;
+        const HostScene &H = scenes[i]->host;
+        const uint64_t pixels = static_cast<uint64_t>(H.params.width) * H.params.height;
+        const int probe_spp = static_cast<int>(std::max<uint64_t>(1, std::min<uint64_t>(H.params.spp, (1u << 20) / pixels)));
+        double best = 1e300;
+        std::pair<uint32_t, int> choice{ 1u << 20, 100 };
+        for(uint32_t cap : { 1u << 18, 1u << 19, 1u << 20, 1u << 21 })
+        {
+            if(cap > 4 * pixels * probe_spp && cap != (1u << 18))
+                continue;
+            for(int pct : { 100, 50 })
+            {
+                RenderStats rs{};
+                lane_render(ctx, L, scenes[i], cap, pct, nullptr, true, probe_spp, rs);  // warm
+                const double ms = lane_render(ctx, L, scenes[i], cap, pct, nullptr, true, probe_spp, rs);
+                const double per_path = ms / static_cast<double>(std::max<uint64_t>(rs.paths, 1));
+                if(per_path < best)
+                {
+                    best = per_path;
+                    choice = { cap, pct };
+                }
+            }
+        }
+        ctx->tuned[key] = choice;
+    }
+}
+
+} // namespace
+
+btrc_status btrc_render_batch(btrc_ctx *ctx, btrc_scene *const *scenes, uint32_t n, const btrc_batch_opts *opts,
+                              float *const *rgb_out, btrc_batch_scene_stats *stats, double *total_ms)
+{
+    if(!ctx || (n > 0 && (!scenes || !rgb_out)))
+        return BTRC_ERR_INVALID_ARG;
+    return guarded(ctx, [&] {
+        if(ctx->device < 0)
+            throw StatusError(BTRC_ERR_INVALID_ARG, "host-only context");
+        for(uint32_t i = 0; i < n; ++i)
+        {
+            if(!scenes[i] || !rgb_out[i] || scenes[i]->ctx != ctx)
+                throw StatusError(BTRC_ERR_INVALID_ARG, "null scene or output, or scene of another context");
+            require_built(scenes[i]);
+        }
+        check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+        ctx->cancel.store(false);
+        const int lanes = opts && opts->lanes > 0 ? opts->lanes : 4;
+        const bool on_dev = opts && opts->output_on_device;
+        const bool tune = opts && opts->autotune;
+        if(tune)
+            autotune(ctx, scenes, n);
+        while(static_cast<int>(ctx->lanes.size()) < lanes)
+            ctx->lanes.push_back(std::make_unique<BatchLane>());
+        // longest processing time first onto the least loaded lane
+        std::vector<uint32_t> order(n);
+        std::iota(order.begin(), order.end(), 0u);
+        auto work = [&](uint32_t i) {
+            const HostScene &H = scenes[i]->host;
+            return static_cast<double>(H.params.width) * H.params.height * H.params.spp;
+        };
+        std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return work(a) > work(b); });
+        std::vector<std::vector<uint32_t>> assign(lanes);
+        std::vector<double> load(lanes, 0.0);
+        for(uint32_t i : order)
+        {
+            const int l = static_cast<int>(std::min_element(load.begin(), load.end()) - load.begin());
+            assign[l].push_back(i);
+            load[l] += work(i);
+        }
+        std::vector<std::string> errors(lanes);
+        std::vector<btrc_status> codes(lanes, BTRC_OK);
+        const auto t0 = std::chrono::steady_clock::now();
+        std::vector<std::thread> threads;
+        for(int l = 0; l < lanes; ++l)
+            threads.emplace_back([&, l] {
+                try
+                {
+                    cudaSetDevice(ctx->device);
+                    for(uint32_t i : assign[l])
+                    {
+                        uint32_t cap = static_cast<uint32_t>(scenes[i]->host.params.state_count);
+                        int pct = 100;
+                        if(tune)
+                        {
+                            const auto it = ctx->tuned.find(scene_class(scenes[i]));
+                            if(it != ctx->tuned.end())
+                            {
+                                cap = it->second.first;
+                                pct = it->second.second;
+                            }
+                        }
+                        RenderStats rs{};
+                        const double ms = lane_render(ctx, *ctx->lanes[l], scenes[i], cap, pct, rgb_out[i], on_dev, 0, rs);
+                        if(stats)
+                        {
+                            stats[i].paths = rs.paths;
+                            stats[i].ms = ms;
+                            stats[i].lane = l;
+                            stats[i].capacity = std::min<uint32_t>(
+                                cap, static_cast<uint32_t>(std::max<uint64_t>(rs.paths, 1)));
+                            stats[i].grid_pct = pct;
+                            stats[i].pad = 0;
+                        }
+                    }
+                }
+                catch(const StatusError &e)
+                {
+                    codes[l] = e.status;
+                    errors[l] = e.what();
+                }
+                catch(const std::exception &e)
+                {
+                    codes[l] = BTRC_ERR_INTERNAL;
+                    errors[l] = e.what();
+                }
+            });
+        for(auto &t : threads)
+            t.join();
+        if(total_ms)
+            *total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        for(int l = 0; l < lanes; ++l)
+            if(codes[l] != BTRC_OK)
+                throw StatusError(codes[l], errors[l]);
     });
 }
 

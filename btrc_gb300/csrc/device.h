@@ -61,6 +61,7 @@ struct DevRender
     float4 *aov_albedo;       // first-hit albedo sums (xyz), or null
     float4 *aov_normal;       // first-hit normal sums (xyz), or null
     uint32_t sample_offset;   // added to every path's sample index (frame-by-frame rendering)
+    int32_t grid_pct;         // persistent grids at this percentage of full occupancy (batched lanes)
     // radiance-cache termination: at the first non-delta surface vertex with depth >=
     // nrc_terminate a path writes a cache query and ends (-1: off)
     int32_t nrc_terminate;

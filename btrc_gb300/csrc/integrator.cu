@@ -1414,13 +1414,15 @@ __global__ void k_resolve(const float4 *film, float *rgb, uint32_t pixels)
 
 uint64_t *launches_by_stage_ptr(uint64_t *p) { return p; }
 
-int persistent_grid(int block, const void *kernel)
+int persistent_grid(int block, const void *kernel, int pct = 100)
 {
     int dev = 0, sms = 152, per_sm = 4;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
-    return sms * (per_sm > 0 ? per_sm : 1);
+    const int full = sms * (per_sm > 0 ? per_sm : 1);
+    const int scaled = pct > 0 && pct < 100 ? full * pct / 100 : full;
+    return scaled > 0 ? scaled : 1;
 }
 
 // Per-stage event timing for profile mode 1: a pair of events around every launch.
@@ -1539,12 +1541,12 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
     if(e != cudaSuccess)
         return e;
     const int grids[5] = {
-        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_generate)),
-        persistent_grid(128, reinterpret_cast<const void *>(k_trace<false>)),
-        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_medium)),
-        persistent_grid(BLOCK, reinterpret_cast<const void *>(shade_kernel(S, R))),
+        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_generate), R.grid_pct),
+        persistent_grid(128, reinterpret_cast<const void *>(k_trace<false>), R.grid_pct),
+        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_medium), R.grid_pct),
+        persistent_grid(BLOCK, reinterpret_cast<const void *>(shade_kernel(S, R)), R.grid_pct),
         persistent_grid(128, S.has_media ? reinterpret_cast<const void *>(k_shadow<true>)
-                                         : reinterpret_cast<const void *>(k_shadow<false>)),
+                                         : reinterpret_cast<const void *>(k_shadow<false>), R.grid_pct),
     };
 
     cudaGraphExec_t exec = nullptr;
@@ -2008,12 +2010,12 @@ cudaError_t render_wavefront_noalloc(const DevScene &S, const DevRender &R, void
     if(e != cudaSuccess)
         return e;
     const int grids[5] = {
-        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_generate)),
-        persistent_grid(128, reinterpret_cast<const void *>(k_trace<false>)),
-        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_medium)),
-        persistent_grid(BLOCK, reinterpret_cast<const void *>(shade_kernel(S, R))),
+        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_generate), R.grid_pct),
+        persistent_grid(128, reinterpret_cast<const void *>(k_trace<false>), R.grid_pct),
+        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_medium), R.grid_pct),
+        persistent_grid(BLOCK, reinterpret_cast<const void *>(shade_kernel(S, R)), R.grid_pct),
         persistent_grid(128, S.has_media ? reinterpret_cast<const void *>(k_shadow<true>)
-                                         : reinterpret_cast<const void *>(k_shadow<false>)),
+                                         : reinterpret_cast<const void *>(k_shadow<false>), R.grid_pct),
     };
     const uint64_t depth_bound = static_cast<uint64_t>(std::max(R.max_depth, R.min_depth)) + 2;
     const uint64_t max_launches = ((R.total_paths + cap - 1) / cap + 2) * depth_bound + 64;

@@ -695,3 +695,84 @@ def textured(seed: int = 1003, width: int = 256, height: int = 192, spp: int = 6
     }
     _write_scene(out / name, scene)
     return out / name
+
+
+def _write_terrain_mesh(path: Path, perlin: Perlin, grid: int) -> None:
+    xs = np.linspace(-1.0, 1.0, grid)
+    X, Z = np.meshgrid(xs, xs, indexing="xy")
+    H = 0.2 * perlin.fbm3(X * 2.0 + 0.5, Z * 2.0 + 0.5, np.full_like(X, 0.37), octaves=8, lacunarity=2.0)
+    V = np.stack([X, H, Z], axis=-1).reshape(-1, 3)
+    dhdx = np.gradient(H, xs, axis=1)
+    dhdz = np.gradient(H, xs, axis=0)
+    N = np.stack([-dhdx, np.ones_like(H), -dhdz], axis=-1)
+    N /= np.linalg.norm(N, axis=-1, keepdims=True)
+    idx = np.arange(grid * grid).reshape(grid, grid)
+    a, b, c, d = idx[:-1, :-1], idx[:-1, 1:], idx[1:, :-1], idx[1:, 1:]
+    F = np.concatenate([np.stack([a, c, b], -1).reshape(-1, 3), np.stack([b, c, d], -1).reshape(-1, 3)])
+    write_obj(path, V, F, normals=N.reshape(-1, 3))
+
+
+def batch(count: int = 64, seed: int = 1004, out_dir: Path | None = None, force: bool = False) -> list[Path]:
+    """Batched uneven scenes: `count` seeded terrain scenes in the style of the large-mesh
+    scene (fBm heightfield, instanced spheres, Disney materials, 8 quad lights and a sky),
+    triangle counts log-uniform in [1e4, 5e5] (eight shared meshes, one per octave step),
+    films of 128^2, 256^2, 384^2 or 512^2, 16, 32 or 64 spp, depth 12."""
+    out = Path(out_dir or cache_dir() / f"batch-{seed}-{count}")
+    out.mkdir(parents=True, exist_ok=True)
+    rng = np.random.default_rng(seed)
+    perlin = Perlin(rng)
+    levels = [1e4 * 50 ** (k / 7) for k in range(8)]
+    grids = [int(round(np.sqrt(t / 2))) for t in levels]
+    for k, g in enumerate(grids):
+        if force or not (out / f"terrain{k}.obj").exists():
+            _write_terrain_mesh(out / f"terrain{k}.obj", perlin, g + 1)
+    if force or not (out / "sphere2.obj").exists():
+        sv, sf = icosphere(2)
+        write_obj(out / "sphere2.obj", sv, sf, normals=sv)
+        qv, qf = quad(1.0)
+        write_obj(out / "quad.obj", qv, flip(qf))
+    paths = []
+    for i in range(count):
+        r = np.random.default_rng(seed * 1000 + i)
+        k = int(r.integers(0, 8))
+        res = int(r.choice([128, 256, 384, 512]))
+        spp = int(r.choice([16, 32, 64]))
+        name = out / f"scene{i:03d}.json"
+        paths.append(name)
+        if name.exists() and not force:
+            continue
+
+        def disney():
+            return {"type": "disney", "color": [float(v) for v in r.uniform(0, 1, 3)],
+                    "roughness": float(r.uniform(0.05, 1.0)), "metallic": float(r.random() < 0.3),
+                    "specular": 0.5, "clearcoat": float(r.uniform(0, 1))}
+        ents = [_entity({"type": "triangle_mesh", "filename": f"$env{{scene_directory}}/terrain{k}.obj"}, disney())]
+        for j in range(8):
+            x, z = r.uniform(-0.9, 0.9, 2)
+            s = float(r.uniform(0.02, 0.06))
+            geo = {"type": "triangle_mesh", "filename": "$env{scene_directory}/sphere2.obj"} if j == 0 else \
+                "$reference{$root/scene/entities/1/geometry}"
+            ents.append(_entity(geo, disney(), [{"scale": [s, s, s]}, {"translate": [float(x), 0.25, float(z)]}]))
+        for j in range(8):
+            x, z = r.uniform(-0.8, 0.8, 2)
+            s = float(r.uniform(0.05, 0.15))
+            inten = [float(v) for v in r.uniform(2.0, 10.0) * r.uniform(0.6, 1.0, 3)]
+            geo = {"type": "triangle_mesh", "filename": "$env{scene_directory}/quad.obj"} if j == 0 else \
+                "$reference{$root/scene/entities/9/geometry}"
+            ents.append(_entity(geo, _diffuse([0.0, 0.0, 0.0]), [{"scale": [s, 1.0, s]},
+                                                                  {"translate": [float(x), 0.5, float(z)]}],
+                                light={"type": "mesh_light", "intensity": inten}))
+        ang = float(r.uniform(0, 2 * np.pi))
+        scene = {
+            "width": res, "height": res,
+            "camera": {"type": "pinhole", "eye": [1.6 * np.sin(ang), 0.8, 1.6 * np.cos(ang)], "dst": [0.0, 0.0, 0.0],
+                       "up": [0.0, 1.0, 0.0], "fov_y": {"deg": 45.0}},
+            "renderer": {"type": "wfpt", "spp": spp, "min_depth": 5, "max_depth": 12, "rr_threshold": 0.1,
+                         "rr_cont_prob": 0.5, "state_count": 1 << 20, "sampler": "independent",
+                         "filter": {"type": "gaussian", "radius": 1.5, "alpha": 1.6}},
+            "scene": {"entities": ents,
+                      "envir_light": {"type": "gradient_sky", "lower": [0.1, 0.1, 0.12], "upper": [0.6, 0.75, 1.0],
+                                      "up": [0.0, 1.0, 0.0]}},
+        }
+        _write_scene(name, scene)
+    return paths

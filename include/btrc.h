@@ -238,6 +238,36 @@ btrc_status btrc_bsdf_batch(btrc_ctx *ctx, int32_t op, const float *d_material, 
 btrc_status btrc_medium_tr_batch(btrc_ctx *ctx, const btrc_scene *scene, int32_t medium_id, const float *d_seg,
                                  const uint64_t *d_seeds, uint64_t n, float *d_out, void *stream);
 
+/* ---- Batched rendering of many scenes (no counterpart in the reference) ------------
+   Renders n built scenes (each with its own renderer settings) through concurrent render
+   lanes: every lane owns a CUDA stream, its path queues and a host thread, and renders
+   its share of the scenes with captured per-bounce graphs. Scenes are assigned
+   longest-first to the least loaded lane. With autotune, each scene class (film size and
+   triangle count, in powers of two) gets the queue capacity and persistent-grid size
+   that rendered a probe fastest; choices are cached in the context, and probing happens
+   before the timed batch. */
+typedef struct btrc_batch_opts
+{
+    int32_t lanes;             /* concurrent render lanes (<= 0: 4) */
+    int32_t autotune;          /* 1: choose queue capacity and grid size per scene class */
+    int32_t output_on_device;  /* 1: rgb_out[i] are device pointers, 0: host pointers */
+} btrc_batch_opts;
+
+typedef struct btrc_batch_scene_stats
+{
+    uint64_t paths;
+    double ms;                 /* wall time of the scene's render in its lane */
+    int32_t lane;
+    uint32_t capacity;         /* queue capacity used */
+    int32_t grid_pct;          /* persistent grid size used, percent of full occupancy */
+    int32_t pad;
+} btrc_batch_scene_stats;
+
+/* rgb_out[i]: width_i * height_i * 3 floats for scene i. stats (n entries) and total_ms
+   (wall time of the batch, probes excluded) may be NULL. */
+btrc_status btrc_render_batch(btrc_ctx *ctx, btrc_scene *const *scenes, uint32_t n, const btrc_batch_opts *opts,
+                              float *const *rgb_out, btrc_batch_scene_stats *stats, double *total_ms);
+
 /* ---- Neural radiance cache (no counterpart in the reference) ----------------------
    A multiresolution hash-grid (16 levels x 2 features, 2^19 FP16 entries per level) and
    degree-4 spherical-harmonics encoding of a path vertex feeding a 5 x 64 ReLU MLP with
