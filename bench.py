@@ -257,6 +257,50 @@ def nrc_study(B, ctx, sc, info, args):
         queries, samples = st["queries"], st["train_samples"]
         if f + 1 in checkpoints or f + 1 == args.nrc_frames:
             curve.append((elapsed, relmse(acc / (f + 1))))
+    # MLP throughput on the tensor cores: inference of 2^21 queries and training steps of
+    # 2^14 samples, CUDA events on the context stream around the calls
+    mlp = None
+    try:
+        nq = 1 << 21
+        g = torch.Generator(device="cuda").manual_seed(0)
+        q = torch.rand((nq, 13), device="cuda", generator=g)
+        lo = torch.tensor(info.world_min, device="cuda")
+        hi = torch.tensor(info.world_max, device="cuda")
+        q[:, 0:3] = lo + (hi - lo) * q[:, 0:3]
+        q[:, 3:9] = q[:, 3:9] * 2 - 1
+        pred = torch.empty((nq, 4), device="cuda")
+        sid = torch.cuda.current_stream().cuda_stream  # the events' stream
+        for _ in range(3):
+            cache.infer(q, nq, pred, stream=sid)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        reps = 10
+        for _ in range(reps):
+            cache.infer(q, nq, pred, stream=sid)
+        e1.record()
+        torch.cuda.synchronize()
+        infer_ms = e0.elapsed_time(e1) / reps
+        flops_fwd = 2 * (80 * 64 + 4 * 64 * 64 + 64 * 16)
+        samples = torch.cat([q[:16384], torch.rand((16384, 3), device="cuda", generator=g)], 1).contiguous()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(reps):
+            cache.train(samples, 16384)
+        train_ms = (time.perf_counter() - t) * 1000 / reps
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+        bf16_peak = peaks.get("bf16_tflops", 1900.0)
+        infer_tflops = nq * flops_fwd / (infer_ms / 1000) / 1e12
+        mlp = {"infer_queries": nq, "infer_ms": infer_ms, "infer_mqueries_s": nq / infer_ms / 1e3,
+               "flops_per_query_fwd": flops_fwd, "infer_tflops": infer_tflops, "bf16_peak_tflops": bf16_peak,
+               "infer_frac_of_bf16_peak": infer_tflops / bf16_peak,
+               "hash_bytes_per_query": 16 * 8 * 2 * 2,
+               "train_step_ms_16384": train_ms,
+               "note": "mma.sync m16n8k16 BF16 (FP32 accumulate); inference includes the hash-grid and SH "
+                       "encoding in the same kernel; training step = fused forward/backward + weight-gradient "
+                       "GEMMs + Adam over all 16.8M hash and 22.5K MLP parameters (wall time, synchronised)"}
+    except Exception as ex:
+        mlp = {"error": str(ex)}
     cache.close()
     tp, tn = _time_to(plain, target), _time_to(curve, target)
     # the cache's relMSE at the plain tracer's time to reach the target, and vice versa
@@ -274,6 +318,7 @@ def nrc_study(B, ctx, sc, info, args):
         "nrc_frames": args.nrc_frames, "nrc_ms_per_frame": elapsed / args.nrc_frames,
         "nrc_queries_per_frame": queries, "nrc_train_samples_per_frame": samples,
         "nrc_loss_first_last": [float(np.mean(losses[:4])), float(np.mean(losses[-4:]))],
+        "mlp": mlp,
         "setup": "paths end in the cache at the first non-delta vertex after one bounce; 1/16 of the pixels "
                  "trace training paths each frame; 4 Adam steps x 16384 samples per frame; cache trained "
                  "from scratch inside the timed frames",
