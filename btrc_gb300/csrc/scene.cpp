@@ -1,6 +1,7 @@
 #include "scene.h"
 
 #include <algorithm>
+#include <array>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -339,6 +340,10 @@ V3 triangle_dpdu(V3 B_A, V3 C_A, float bax, float bay, float cax, float cay, V3 
 
 } // namespace
 
+HostGeometry geometry_from_arrays(const std::string &name, std::vector<V3> positions, const std::vector<V3> &normals,
+                                  const std::vector<float> &uvs, const std::vector<ObjIndex> &corners,
+                                  bool to_unit_cube);
+
 HostGeometry load_obj(const std::string &filename, bool to_unit_cube)
 {
     std::ifstream fin(filename, std::ios::binary);
@@ -424,6 +429,14 @@ HostGeometry load_obj(const std::string &filename, bool to_unit_cube)
             throw std::runtime_error("invalid obj tex coord index: out of range");
     }
 
+    return geometry_from_arrays(filename, std::move(positions), normals, uvs, corners, to_unit_cube);
+}
+
+HostGeometry geometry_from_arrays(const std::string &name, std::vector<V3> positions, const std::vector<V3> &normals,
+                                  const std::vector<float> &uvs, const std::vector<ObjIndex> &corners,
+                                  bool to_unit_cube)
+{
+    const std::string &filename = name;
     if(to_unit_cube && !positions.empty())
     {
         // common/btrc/utils/triangle_mesh_loader.cpp:195-213
@@ -502,6 +515,97 @@ HostGeometry load_obj(const std::string &filename, bool to_unit_cube)
     }
     g.total_area = static_cast<float>(total);
     return g;
+}
+
+// ---------------------------------------------------------------- procedural geometry
+
+// Inline geometry creators (an extension; the reference reads triangle meshes from OBJ
+// files only): "sphere" (icosphere of radius 1, `subdivisions` 0..8, smooth normals,
+// spherical texture coordinates), "quad" (unit square in the xz plane facing +y, texture
+// coordinates over [0,1]^2) and "box" (the cube [-0.5, 0.5]^3 facing outwards, flat).
+// Built in double precision and rounded once.
+HostGeometry procedural_geometry(const std::string &type, int subdivisions)
+{
+    std::vector<V3> pos, nor;
+    std::vector<float> uvs;
+    std::vector<ObjIndex> corners;
+    if(type == "sphere")
+    {
+        if(subdivisions < 0 || subdivisions > 8)
+            throw std::runtime_error("sphere subdivisions must be within 0..8");
+        const double t = (1.0 + std::sqrt(5.0)) / 2.0;
+        std::vector<std::array<double, 3>> v = { { -1, t, 0 }, { 1, t, 0 }, { -1, -t, 0 }, { 1, -t, 0 },
+                                                 { 0, -1, t }, { 0, 1, t }, { 0, -1, -t }, { 0, 1, -t },
+                                                 { t, 0, -1 }, { t, 0, 1 }, { -t, 0, -1 }, { -t, 0, 1 } };
+        auto unit = [](std::array<double, 3> p) {
+            const double l = std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+            return std::array<double, 3>{ p[0] / l, p[1] / l, p[2] / l };
+        };
+        for(auto &p : v)
+            p = unit(p);
+        std::vector<std::array<int, 3>> f = { { 0, 11, 5 }, { 0, 5, 1 },  { 0, 1, 7 },   { 0, 7, 10 }, { 0, 10, 11 },
+                                              { 1, 5, 9 },  { 5, 11, 4 }, { 11, 10, 2 }, { 10, 7, 6 }, { 7, 1, 8 },
+                                              { 3, 9, 4 },  { 3, 4, 2 },  { 3, 2, 6 },   { 3, 6, 8 },  { 3, 8, 9 },
+                                              { 4, 9, 5 },  { 2, 4, 11 }, { 6, 2, 10 },  { 8, 6, 7 },  { 9, 8, 1 } };
+        for(int level = 0; level < subdivisions; ++level)
+        {
+            std::map<std::pair<int, int>, int> cache;
+            auto mid = [&](int a, int b) {
+                const auto key = a < b ? std::make_pair(a, b) : std::make_pair(b, a);
+                auto it = cache.find(key);
+                if(it != cache.end())
+                    return it->second;
+                v.push_back(unit({ v[a][0] + v[b][0], v[a][1] + v[b][1], v[a][2] + v[b][2] }));
+                const int id = static_cast<int>(v.size()) - 1;
+                cache[key] = id;
+                return id;
+            };
+            std::vector<std::array<int, 3>> nf;
+            nf.reserve(f.size() * 4);
+            for(auto &tri : f)
+            {
+                const int a = tri[0], b = tri[1], c = tri[2];
+                const int ab = mid(a, b), bc = mid(b, c), ca = mid(c, a);
+                nf.push_back({ a, ab, ca });
+                nf.push_back({ b, bc, ab });
+                nf.push_back({ c, ca, bc });
+                nf.push_back({ ab, bc, ca });
+            }
+            f.swap(nf);
+        }
+        const double PI_D = 3.14159265358979323846;
+        for(auto &p : v)
+        {
+            pos.emplace_back(static_cast<float>(p[0]), static_cast<float>(p[1]), static_cast<float>(p[2]));
+            nor.push_back(pos.back());
+            uvs.push_back(static_cast<float>(std::atan2(p[2], p[0]) / (2 * PI_D) + 0.5));
+            uvs.push_back(static_cast<float>(std::acos(std::max(-1.0, std::min(1.0, p[1]))) / PI_D));
+        }
+        for(auto &tri : f)
+            for(int k = 0; k < 3; ++k)
+                corners.push_back({ tri[k], tri[k], tri[k] });
+    }
+    else if(type == "quad")
+    {
+        pos = { V3(-0.5f, 0, -0.5f), V3(0.5f, 0, -0.5f), V3(0.5f, 0, 0.5f), V3(-0.5f, 0, 0.5f) };
+        uvs = { 0, 0, 1, 0, 1, 1, 0, 1 };
+        for(int k : { 0, 2, 1, 0, 3, 2 })
+            corners.push_back({ k, k, -1 });
+    }
+    else if(type == "box")
+    {
+        for(int c = 0; c < 8; ++c)
+            pos.emplace_back((c & 4) ? 0.5f : -0.5f, (c & 2) ? 0.5f : -0.5f, (c & 1) ? 0.5f : -0.5f);
+        // two outward-facing triangles per face (vertex index = 4 x + 2 y + z)
+        const int faces[12][3] = { { 0, 1, 3 }, { 0, 3, 2 }, { 4, 6, 7 }, { 4, 7, 5 }, { 0, 4, 5 }, { 0, 5, 1 },
+                                   { 2, 3, 7 }, { 2, 7, 6 }, { 0, 2, 6 }, { 0, 6, 4 }, { 1, 5, 7 }, { 1, 7, 3 } };
+        for(auto &tri : faces)
+            for(int k = 0; k < 3; ++k)
+                corners.push_back({ tri[k], -1, -1 });
+    }
+    else
+        throw std::runtime_error("unsupported geometry type '" + type + "'");
+    return geometry_from_arrays("<" + type + ">", std::move(pos), nor, uvs, corners, false);
 }
 
 // ---------------------------------------------------------------- scene file
@@ -1129,10 +1233,13 @@ HostScene load_scene(const std::string &path)
         if(git == geo_pool.end())
         {
             const std::string gt = json::as_string(gn->child("type"));
-            if(gt != "triangle_mesh")
-                throw std::runtime_error("unsupported geometry type '" + gt + "'");
-            const std::string fn = resolve_path(json::as_string(gn->child("filename")), scene_dir);
-            S.geometries.push_back(load_obj(fn, json::bool_or(gn, "transform_to_unit_cube", false)));
+            if(gt == "triangle_mesh")
+            {
+                const std::string fn = resolve_path(json::as_string(gn->child("filename")), scene_dir);
+                S.geometries.push_back(load_obj(fn, json::bool_or(gn, "transform_to_unit_cube", false)));
+            }
+            else
+                S.geometries.push_back(procedural_geometry(gt, json::int_or(gn, "subdivisions", 3)));
             pi.geo = static_cast<int>(S.geometries.size()) - 1;
             geo_pool[gn.get()] = pi.geo;
         }

@@ -362,6 +362,57 @@ def load_obj(path: str, to_unit_cube: bool):
     return _obj_records(V, N, T, F, to_unit_cube)
 
 
+def procedural(kind: str, subdivisions: int = 3):
+    """Inline geometry creators of the scene format extension: "sphere" (icosphere of
+    radius 1 with `subdivisions` levels, smooth normals, spherical texture coordinates),
+    "quad" (unit square in xz facing +y, uv over [0,1]^2), "box" ([-0.5, 0.5]^3 facing
+    outwards, flat); built in float64 and rounded once, like the loader."""
+    if kind == "sphere":
+        t = (1.0 + math.sqrt(5.0)) / 2.0
+        v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+             (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+        verts = [np.array(q, np.float64) / math.sqrt(sum(x * x for x in q)) for q in v]
+        faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+                 (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5),
+                 (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+        for _ in range(subdivisions):
+            cache = {}
+
+            def mid(a, b):
+                key = (min(a, b), max(a, b))
+                if key not in cache:
+                    m = verts[a] + verts[b]
+                    verts.append(m / math.sqrt(float(m @ m)))
+                    cache[key] = len(verts) - 1
+                return cache[key]
+            nf = []
+            for a, b, c in faces:
+                ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+                nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+            faces = nf
+        P = np.array(verts, np.float64)
+        V = P.astype(np.float32)
+        T = np.stack([np.arctan2(P[:, 2], P[:, 0]) / (2 * math.pi) + 0.5,
+                      np.arccos(np.clip(P[:, 1], -1, 1)) / math.pi], 1).astype(np.float32)
+        f = np.array(faces, np.int64)
+        F = np.stack([f, f, f], -1)
+        return _obj_records(V, V.copy(), T, F, False)
+    if kind == "quad":
+        V = np.array([[-0.5, 0, -0.5], [0.5, 0, -0.5], [0.5, 0, 0.5], [-0.5, 0, 0.5]], np.float32)
+        T = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)
+        f = np.array([[0, 2, 1], [0, 3, 2]], np.int64)
+        F = np.stack([f, f, np.full_like(f, -1)], -1)
+        return _obj_records(V, np.zeros((0, 3), np.float32), T, F, False)
+    if kind == "box":
+        V = np.array([[0.5 if c & 4 else -0.5, 0.5 if c & 2 else -0.5, 0.5 if c & 1 else -0.5] for c in range(8)],
+                     np.float32)
+        f = np.array([[0, 1, 3], [0, 3, 2], [4, 6, 7], [4, 7, 5], [0, 4, 5], [0, 5, 1], [2, 3, 7], [2, 7, 6],
+                      [0, 2, 6], [0, 6, 4], [1, 5, 7], [1, 7, 3]], np.int64)
+        F = np.stack([f, np.full_like(f, -1), np.full_like(f, -1)], -1)
+        return _obj_records(V, np.zeros((0, 3), np.float32), np.zeros((0, 2), np.float32), F, False)
+    raise ValueError("geometry type " + kind)
+
+
 def _obj_records(V, N, T, F, to_unit_cube):
     if to_unit_cube and len(V):
         lo, hi = V.min(0), V.max(0)
@@ -641,9 +692,14 @@ class Scene:
         for e in scene.child("entities").elems:
             gn = e.child("geometry")
             if id(gn) not in geo_ids:
-                fn = gn.child("filename").s.replace("$env{scene_directory}", sdir)
-                unit = gn.find("transform_to_unit_cube")
-                geos.append(load_obj(fn, unit is not None and unit.s == "true"))
+                gtype = gn.child("type").s
+                if gtype == "triangle_mesh":
+                    fn = gn.child("filename").s.replace("$env{scene_directory}", sdir)
+                    unit = gn.find("transform_to_unit_cube")
+                    geos.append(load_obj(fn, unit is not None and unit.s == "true"))
+                else:
+                    sub = gn.find("subdivisions")
+                    geos.append(procedural(gtype, int(vfloat(sub)) if sub is not None else 3))
                 geo_ids[id(gn)] = len(geos) - 1
             mn = e.child("material")
             if id(mn) not in mat_ids:

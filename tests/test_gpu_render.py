@@ -83,3 +83,13 @@ def test_render_reuses_context_and_cancel_flag_resets(gpu_ctx, scene_dir):
     b = gpu_ctx.render(sc)
     # deterministic: same sampler streams, same queue order -> same image up to atomic order
     assert np.allclose(a, b, rtol=1e-4, atol=1e-5)
+
+
+def test_procedural_geometry_scene(gpu_ctx, tmp_path):
+    # inline sphere / quad / box creators (smooth normals, texture coordinates, flat boxes)
+    from tests.test_abi_loader import _procedural_scene
+    p = _procedural_scene(tmp_path)
+    g, o, var, stats = _render_both(gpu_ctx, p, 256)
+    assert stats["traversal_errors"] == 0
+    err = rel_mse(g, o)
+    assert err < 1e-3, err
