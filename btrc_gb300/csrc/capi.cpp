@@ -434,6 +434,7 @@ void alloc_render_buffers(RenderBuffers &B, std::vector<void *> &allocs, uint32_
     B.shadow.sampler = static_cast<SamplerState *>(A(sizeof(SamplerState) * capacity));
     B.hit_flag = static_cast<uint32_t *>(A(sizeof(uint32_t) * capacity));
     B.hit_detail = static_cast<HitDetail *>(A(sizeof(HitDetail) * capacity));
+    B.order = static_cast<uint32_t *>(A(sizeof(uint32_t) * capacity));
     B.film = static_cast<float4 *>(A(sizeof(float4) * pixels));
     B.counters = static_cast<Counters *>(A(sizeof(Counters)));
     void *hc = nullptr;

@@ -90,6 +90,8 @@ struct Counters
     uint64_t tri_tests;    // closest-hit triangle tests (counting mode only)
     uint32_t trace_cursor;   // next ray for the warp-refill traversal (reset every bounce)
     uint32_t shadow_cursor;
+    uint32_t hit_count;      // closest-hit results partitioned into the shade order
+    uint32_t miss_count;     // (hits from the front, misses from the back)
 };
 
 // Structure-of-arrays path state. Two copies (current / next) per render.

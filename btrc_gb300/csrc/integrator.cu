@@ -878,6 +878,8 @@ __global__ void k_control(Counters *c, uint32_t capacity, uint64_t total)
     k.shadow = 0;
     k.trace_cursor = 0;
     k.shadow_cursor = 0;
+    k.hit_count = 0;
+    k.miss_count = 0;
     if(k.active > 0)
         ++k.iterations;
     *c = k;
@@ -977,6 +979,83 @@ __global__ void __launch_bounds__(128) k_trace(DevScene S, PathSoA P, uint32_t *
             atomicAdd(reinterpret_cast<unsigned long long *>(&cnt->node_visits), static_cast<unsigned long long>(nv));
             atomicAdd(reinterpret_cast<unsigned long long *>(&cnt->tri_tests), static_cast<unsigned long long>(tv));
         }
+    }
+}
+
+// Shade order: a permutation of the queue slots with the paths that hit a surface first
+// (in slot order) and the misses after them, so that the shade kernel's warps run the
+// surface code with full lanes and the short miss code apart from it. Each block takes
+// ORDER_ITEMS consecutive slots per thread, scans the counts in shared memory and claims
+// its ranges with one atomic per kind. The shade kernel checks every path's flags itself,
+// so the order only groups work; it never changes a result.
+constexpr uint32_t ORDER_ITEMS = 8;
+
+__global__ void __launch_bounds__(BLOCK) k_order(const uint32_t *__restrict__ flags, uint32_t *__restrict__ order,
+                                                 Counters *cnt)
+{
+    __shared__ uint32_t s_warp[BLOCK / 32];
+    __shared__ uint32_t s_base[2];
+    const uint32_t n = cnt->active;
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    const uint32_t chunk = BLOCK * ORDER_ITEMS;
+    for(uint32_t c0 = blockIdx.x * chunk; c0 < n; c0 += gridDim.x * chunk)
+    {
+        const uint32_t first = c0 + threadIdx.x * ORDER_ITEMS;
+        uint32_t hitbits = 0, valid = 0;
+#pragma unroll
+        for(uint32_t k = 0; k < ORDER_ITEMS; ++k)
+            if(first + k < n)
+            {
+                ++valid;
+                if(flags[first + k] & HIT_BIT)
+                    hitbits |= 1u << k;
+            }
+        // hits in the low half, misses in the high half (at most BLOCK * ORDER_ITEMS each)
+        const uint32_t v = static_cast<uint32_t>(__popc(hitbits)) | ((valid - __popc(hitbits)) << 16);
+        uint32_t x = v;
+#pragma unroll
+        for(int off = 1; off < 32; off <<= 1)
+        {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+            if(lane >= static_cast<uint32_t>(off))
+                x += y;
+        }
+        if(lane == 31)
+            s_warp[warp] = x;
+        __syncthreads();
+        if(warp == 0)
+        {
+            const uint32_t w = lane < BLOCK / 32 ? s_warp[lane] : 0u;
+            uint32_t t = w;
+#pragma unroll
+            for(int off = 1; off < 32; off <<= 1)
+            {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, t, off);
+                if(lane >= static_cast<uint32_t>(off))
+                    t += y;
+            }
+            if(lane < BLOCK / 32)
+                s_warp[lane] = t - w;
+            if(lane == 31)
+            {
+                s_base[0] = (t & 0xffffu) ? atomicAdd(&cnt->hit_count, t & 0xffffu) : 0u;
+                s_base[1] = (t >> 16) ? atomicAdd(&cnt->miss_count, t >> 16) : 0u;
+            }
+        }
+        __syncthreads();
+        const uint32_t excl = s_warp[warp] + x - v;
+        uint32_t hpos = s_base[0] + (excl & 0xffffu);
+        uint32_t mpos = s_base[1] + (excl >> 16);
+#pragma unroll
+        for(uint32_t k = 0; k < ORDER_ITEMS; ++k)
+            if(first + k < n)
+            {
+                if(hitbits & (1u << k))
+                    order[hpos++] = first + k;
+                else
+                    order[n - 1u - mpos++] = first + k;
+            }
+        __syncthreads();
     }
 }
 
@@ -1186,13 +1265,14 @@ __device__ __forceinline__ bool nrc_query_at(const DevScene &S, const SurfacePoi
 // keep the shade kernel's registers
 template<bool TEX, bool NRC = false>
 __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, DevRender R, PathSoA P, PathSoA N, ShadowSoA SH,
-                                                 const uint32_t *flags, const HitDetail *hits, float4 *film,
-                                                 Counters *cnt)
+                                                 const uint32_t *flags, const HitDetail *hits,
+                                                 const uint32_t *order, float4 *film, Counters *cnt)
 {
     const uint32_t n = cnt->active;
     const uint32_t stride = gridDim.x * blockDim.x;
-    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    for(uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride)
     {
+        const uint32_t i = order[j];
         const uint32_t flag = flags[i];
         const F4 bd = P.beta_depth[i], rp = P.rad_pixel[i];
         const F4 ro = P.ray_o[i], rd = P.ray_d[i], ble = P.bsdf_le[i];
@@ -1346,7 +1426,7 @@ __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, DevRender R, PathSo
 }
 
 using ShadeKernel = void (*)(DevScene, DevRender, PathSoA, PathSoA, ShadowSoA, const uint32_t *, const HitDetail *,
-                             float4 *, Counters *);
+                             const uint32_t *, float4 *, Counters *);
 
 // the shade kernel variant for a scene and render: textured materials, cache termination
 ShadeKernel shade_kernel(const DevScene &S, const DevRender &R)
@@ -1465,7 +1545,7 @@ void timed(StageTimer *T, int stage, cudaStream_t st, uint64_t *launches, Launch
 }
 
 cudaError_t enqueue_bounce(const DevScene &S, const DevRender &R, RenderBuffers &B, int parity, cudaStream_t st,
-                           const int grids[5], int profile, StageTimer *T, uint64_t *launches)
+                           const int grids[6], int profile, StageTimer *T, uint64_t *launches)
 {
     PathSoA &P = B.path[parity];
     PathSoA &N = B.path[1 - parity];
@@ -1482,9 +1562,11 @@ cudaError_t enqueue_bounce(const DevScene &S, const DevRender &R, RenderBuffers 
         timed(T, STAGE_MEDIUM, st, launches, [&] {
             k_medium<<<grids[2], BLOCK, 0, st>>>(S, R, P, N, B.shadow, B.hit_flag, B.hit_detail, B.film, B.counters);
         });
+    timed(T, STAGE_SHADE, st, launches,
+          [&] { k_order<<<grids[5], BLOCK, 0, st>>>(B.hit_flag, B.order, B.counters); });
     timed(T, STAGE_SHADE, st, launches, [&] {
-        shade_kernel(S, R)<<<grids[3], BLOCK, 0, st>>>(S, R, P, N, B.shadow, B.hit_flag, B.hit_detail, B.film,
-                                                       B.counters);
+        shade_kernel(S, R)<<<grids[3], BLOCK, 0, st>>>(S, R, P, N, B.shadow, B.hit_flag, B.hit_detail, B.order,
+                                                       B.film, B.counters);
     });
     timed(T, STAGE_SHADOW, st, launches,
           [&] {
@@ -1540,13 +1622,14 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
     cudaError_t e = cudaMemsetAsync(B.counters, 0, sizeof(Counters), st);
     if(e != cudaSuccess)
         return e;
-    const int grids[5] = {
+    const int grids[6] = {
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_generate), R.grid_pct),
         persistent_grid(128, reinterpret_cast<const void *>(k_trace<false>), R.grid_pct),
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_medium), R.grid_pct),
         persistent_grid(BLOCK, reinterpret_cast<const void *>(shade_kernel(S, R)), R.grid_pct),
         persistent_grid(128, S.has_media ? reinterpret_cast<const void *>(k_shadow<true>)
                                          : reinterpret_cast<const void *>(k_shadow<false>), R.grid_pct),
+        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_order), R.grid_pct),
     };
 
     cudaGraphExec_t exec = nullptr;
@@ -1929,7 +2012,7 @@ constexpr size_t NOALLOC_PATH_BYTES = 6 * 16;    // one PathSoA slot
 constexpr size_t NOALLOC_BYTES =
     2 * NOALLOC_PATH_BYTES * NOALLOC_MAX_STATES      // current + next queues
     + 4 * 16 * NOALLOC_MAX_STATES                     // shadow queue (o, d, beta, sampler)
-    + (4 + 16) * NOALLOC_MAX_STATES                   // hit flags + details
+    + (4 + 16 + 4) * NOALLOC_MAX_STATES               // hit flags + details + shade order
     + 16 * static_cast<size_t>(NOALLOC_MAX_PIXELS)    // film
     + 256                                             // counters
     + 32 * 256;                                       // 256-byte alignment of each buffer
@@ -1996,6 +2079,7 @@ cudaError_t render_wavefront_noalloc(const DevScene &S, const DevRender &R, void
     B.shadow.sampler = reinterpret_cast<SamplerState *>(take(16ull * cap));
     B.hit_flag = reinterpret_cast<uint32_t *>(take(4ull * cap));
     B.hit_detail = reinterpret_cast<HitDetail *>(take(16ull * cap));
+    B.order = reinterpret_cast<uint32_t *>(take(4ull * cap));
     B.film = reinterpret_cast<float4 *>(take(16ull * pixels));
     B.counters = reinterpret_cast<Counters *>(take(sizeof(Counters)));
     B.host_counters = nullptr;
@@ -2009,13 +2093,14 @@ cudaError_t render_wavefront_noalloc(const DevScene &S, const DevRender &R, void
         e = cudaMemsetAsync(B.counters, 0, sizeof(Counters), st);
     if(e != cudaSuccess)
         return e;
-    const int grids[5] = {
+    const int grids[6] = {
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_generate), R.grid_pct),
         persistent_grid(128, reinterpret_cast<const void *>(k_trace<false>), R.grid_pct),
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_medium), R.grid_pct),
         persistent_grid(BLOCK, reinterpret_cast<const void *>(shade_kernel(S, R)), R.grid_pct),
         persistent_grid(128, S.has_media ? reinterpret_cast<const void *>(k_shadow<true>)
                                          : reinterpret_cast<const void *>(k_shadow<false>), R.grid_pct),
+        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_order), R.grid_pct),
     };
     const uint64_t depth_bound = static_cast<uint64_t>(std::max(R.max_depth, R.min_depth)) + 2;
     const uint64_t max_launches = ((R.total_paths + cap - 1) / cap + 2) * depth_bound + 64;

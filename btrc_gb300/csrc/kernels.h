@@ -27,6 +27,7 @@ struct RenderBuffers
     ShadowSoA shadow;
     uint32_t *hit_flag;
     HitDetail *hit_detail;
+    uint32_t *order;       // this bounce's queue slots, paths that hit first (trace -> shade)
     float4 *film;          // radiance.rgb, weight per pixel
     float4 *aov_albedo;    // first-hit albedo sums, allocated on demand
     float4 *aov_normal;    // first-hit normal sums, allocated on demand

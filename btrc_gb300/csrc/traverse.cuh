@@ -174,12 +174,19 @@ __device__ __forceinline__ uint32_t intersect_children(const TravRay &r, const f
     const float forgx = orgx * BOX_EPS, forgy = orgy * BOX_EPS, forgz = orgz * BOX_EPS;
     const float tcur_e = tcur * BOX_EPS;
     const bool nx = r.idx < 0.0f, ny = r.idy < 0.0f, nz = r.idz < 0.0f;
+    const uint32_t oct4 = r.oct_inv * 0x01010101u;
 
     uint32_t hitmask = 0;
 #pragma unroll
     for(int half = 0; half < 2; ++half)
     {
+        // four meta bytes decoded at once: inner children (bits 3 and 4 set) get their
+        // slot XOR the ray octant as bit index, leaves their triangle offset; an empty
+        // slot (meta 0) contributes no bits, so it needs no test of its own
         const uint32_t meta4 = half ? n1.w : n1.z;
+        const uint32_t inner4 = (meta4 & (meta4 << 1)) & 0x10101010u;
+        const uint32_t bitidx4 = (meta4 ^ (oct4 & ((inner4 >> 4) * 7u))) & 0x1f1f1f1fu;
+        const uint32_t cbits4 = (meta4 >> 5) & 0x07070707u;
         const uint32_t qlox = half ? n2.y : n2.x, qloy = half ? n2.w : n2.z, qloz = half ? n3.y : n3.x;
         const uint32_t qhix = half ? n3.w : n3.z, qhiy = half ? n4.y : n4.x, qhiz = half ? n4.w : n4.z;
         const uint32_t xn = nx ? qhix : qlox, xf = nx ? qlox : qhix;
@@ -188,7 +195,6 @@ __device__ __forceinline__ uint32_t intersect_children(const TravRay &r, const f
 #pragma unroll
         for(int j = 0; j < 4; ++j)
         {
-            const uint32_t m = (meta4 >> (8 * j)) & 0xffu;
             const float tnx = fmaf(byte_f(xn, j), adjx, orgx);
             const float tny = fmaf(byte_f(yn, j), adjy, orgy);
             const float tnz = fmaf(byte_f(zn, j), adjz, orgz);
@@ -197,12 +203,8 @@ __device__ __forceinline__ uint32_t intersect_children(const TravRay &r, const f
             const float tfz = fmaf(byte_f(zf, j), fadjz, forgz);
             const float tmin = fmaxf(max3f(tnx, tny, tnz), 0.0f);
             const float tmax = fminf(min3f(tfx, tfy, tfz), tcur_e);
-            if(m != 0u && tmin <= tmax)
-            {
-                const bool inner = (m & 0x18u) == 0x18u;
-                const uint32_t bit = inner ? ((m & 0x1fu) ^ r.oct_inv) : (m & 0x1fu);
-                hitmask |= (m >> 5) << bit;
-            }
+            if(tmin <= tmax)
+                hitmask |= __byte_perm(cbits4, 0u, 0x4440u + j) << __byte_perm(bitidx4, 0u, 0x4440u + j);
         }
     }
     return hitmask;
