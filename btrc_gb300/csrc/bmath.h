@@ -53,6 +53,28 @@ BT_HD V3 vmax(V3 a, V3 b) { return V3(fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.
 BT_HD float max_comp(V3 a) { return fmaxf(a.x, fmaxf(a.y, a.z)); }
 BT_HD bool is_zero(V3 a) { return a.x == 0.0f && a.y == 0.0f && a.z == 0.0f; }
 BT_HD float saturate(float v) { return fminf(1.0f, fmaxf(0.0f, v)); }
+
+// sin(pi x) and cos(pi x). Every angle the tracer samples is a fraction of pi, and on
+// the device sincospif reduces such arguments exactly, so it needs none of the large-
+// argument code that sinf / cosf carry at each call site.
+BT_HD void sincos_pi(float x, float &s, float &c)
+{
+#if defined(__CUDA_ARCH__)
+    sincospif(x, &s, &c);
+#else
+    s = std::sin(PI * x);
+    c = std::cos(PI * x);
+#endif
+}
+
+BT_HD float cos_pi(float x)
+{
+#if defined(__CUDA_ARCH__)
+    return cospif(x);
+#else
+    return std::cos(PI * x);
+#endif
+}
 BT_HD float clampf(float v, float lo, float hi) { return fminf(hi, fmaxf(lo, v)); }
 BT_HD float lerpf(float a, float b, float t) { return a * (1.0f - t) + b * t; }
 BT_HD V3 lerp3(V3 a, V3 b, float t) { return a * (1.0f - t) + b * t; }

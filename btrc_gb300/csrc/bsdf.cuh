@@ -44,19 +44,22 @@ BT_HD V3 sample_hemisphere_zweighted(float u1, float u2)
     u2 = 2.0f * u2 - 1.0f;
     if(u1 != 0.0f || u2 != 0.0f)
     {
+        // theta in units of pi
         float theta, r;
         if(fabsf(u1) > fabsf(u2))
         {
             r = u1;
-            theta = 0.25f * PI * (u2 / u1);
+            theta = 0.25f * (u2 / u1);
         }
         else
         {
             r = u2;
-            theta = 0.5f * PI - 0.25f * PI * (u1 / u2);
+            theta = 0.5f - 0.25f * (u1 / u2);
         }
-        sx = r * cosf(theta);
-        sy = r * sinf(theta);
+        float st, ct;
+        sincos_pi(theta, st, ct);
+        sx = r * ct;
+        sy = r * st;
     }
     const float z = sqrtf(fmaxf(0.0f, 1.0f - (sx * sx + sy * sy)));
     return V3(sx, sy, z);
@@ -67,9 +70,10 @@ BT_HD float pdf_hemisphere_zweighted(V3 v) { return v.z >= 0 ? v.z / PI : 0.0f; 
 BT_HD V3 sample_sphere_uniform(float u1, float u2)
 {
     const float z = 1.0f - (u1 + u1);
-    const float phi = 2.0f * PI * u2;
     const float r = sqrtf(fmaxf(0.0f, 1.0f - z * z));
-    return V3(r * cosf(phi), r * sinf(phi), z);
+    float sp, cp;
+    sincos_pi(2.0f * u2, sp, cp);
+    return V3(r * cp, r * sp, z);
 }
 
 // Numerics. The reference evaluates these quantities as sqrt(1 - c*c), sin/cos of
@@ -178,8 +182,10 @@ BT_HD float mf_smith_aniso_gtr2(float cos_phi, float sin_phi, float ax, float ay
 
 BT_HD V3 mf_sample_aniso_gtr2(float ax, float ay, float s0, float s1)
 {
-    float sin_phi_h = ay * sinf(2 * PI * s0);
-    float cos_phi_h = ax * cosf(2 * PI * s0);
+    float sp, cp;
+    sincos_pi(2.0f * s0, sp, cp);
+    float sin_phi_h = ay * sp;
+    float cos_phi_h = ax * cp;
     const float nor = 1.0f / sqrtf(sqrf(sin_phi_h) + sqrf(cos_phi_h));
     sin_phi_h *= nor;
     cos_phi_h *= nor;
@@ -199,10 +205,11 @@ BT_HD float mf_gtr1(float sin_theta_h, float cos_theta_h, float alpha)
 
 BT_HD V3 mf_sample_gtr1(float alpha, float s0, float s1)
 {
-    const float phi = 2 * PI * s0;
     const float cos_theta = sqrtf((powf(alpha, 2.0f - 2.0f * s1) - 1.0f) / (sqrf(alpha) - 1.0f));
     const float sin_theta = cos2sin(cos_theta);
-    return normalize(V3(sin_theta * cosf(phi), sin_theta * sinf(phi), cos_theta));
+    float sp, cp;
+    sincos_pi(2.0f * s0, sp, cp);
+    return normalize(V3(sin_theta * cp, sin_theta * sp, cos_theta));
 }
 
 BT_HD V3 mf_sample_vndf(V3 ve, float ax, float ay, float s0, float s1)
@@ -214,9 +221,10 @@ BT_HD V3 mf_sample_vndf(V3 ve, float ax, float ay, float s0, float s1)
         t1 = V3(-vh.y, vh.x, 0) / sqrtf(lensq);
     const V3 t2 = cross(vh, t1);
     const float r = sqrtf(s0);
-    const float phi = 2 * PI * s1;
-    const float tt1 = r * cosf(phi);
-    const float tt2_ = r * sinf(phi);
+    float sp, cp;
+    sincos_pi(2.0f * s1, sp, cp);
+    const float tt1 = r * cp;
+    const float tt2_ = r * sp;
     const float s = 0.5f * (1.0f + vh.z);
     const float tt2 = (1.0f - s) * sqrtf(1.0f - tt1 * tt1) + s * tt2_;
     const V3 nh = tt1 * t1 + tt2 * t2 + sqrtf(fmaxf(0.0f, 1.0f - tt1 * tt1 - tt2 * tt2)) * vh;
@@ -224,18 +232,6 @@ BT_HD V3 mf_sample_vndf(V3 ve, float ax, float ay, float s0, float s1)
 }
 
 // ---------------------------------------------------------------- diffuse component
-
-BT_HD CompSample diffuse_sample(V3 albedo, V3 lwo, float s1, float s2)
-{
-    if(lwo.z <= 0)
-        return comp_clear();
-    CompSample r;
-    r.dir = sample_hemisphere_zweighted(s1, s2);
-    r.f = albedo / PI;
-    r.pdf = pdf_hemisphere_zweighted(r.dir);
-    r.is_delta = false;
-    return r;
-}
 
 BT_HD V3 diffuse_eval(V3 albedo, V3 lwi, V3 lwo)
 {
@@ -288,25 +284,6 @@ BT_HD void metal_eval_pdf(const MetalParams &m, V3 lwi, V3 lwo, V3 &f, float &pd
     const V3 F = schlick3(m.R0, ctd);
     f = F * (D * Gi * Go / fabsf(4.0f * cti * cto));
     pdf = Go * D / (4.0f * lwo.z);
-}
-
-BT_HD CompSample metal_sample(const MetalParams &m, V3 lwo, float s1, float s2)
-{
-    CompSample r = comp_clear();
-    if(lwo.z > 0)
-    {
-        const V3 lwh = normalize(mf_sample_vndf(lwo, m.ax, m.ay, s1, s2));
-        if(lwh.z > 0)
-        {
-            const V3 lwi = normalize(2.0f * dot(lwo, lwh) * lwh - lwo);
-            if(lwi.z > 0)
-            {
-                r.dir = lwi;
-                metal_eval_pdf(m, lwi, lwo, r.f, r.pdf);
-            }
-        }
-    }
-    return r;
 }
 
 // ---------------------------------------------------------------- Disney component
@@ -521,6 +498,66 @@ BT_HD float disney_pdf(const DisneyParams &d, V3 lwi, V3 lwo)
     return d.w_diffuse * diffuse + d.w_specular * pdf_spec + d.w_clearcoat * pdf_cc;
 }
 
+// disney_eval and disney_pdf in one pass: in the reflection case (both directions above
+// the surface) the half vector, the specular D, the outgoing Smith G, both tangents and
+// the clearcoat D are shared, each computed by the same expression as in the separate
+// functions; the other cases call them.
+BT_HD void disney_eval_pdf_split(const DisneyParams &d, V3 lwi, V3 lwo, V3 &f, float &pdf)
+{
+    f = disney_eval(d, lwi, lwo);
+    pdf = disney_pdf(d, lwi, lwo);
+}
+
+BT_HD void disney_eval_pdf(const DisneyParams &d, V3 lwi, V3 lwo, V3 &f, float &pdf)
+{
+    if(!(lwi.z >= 1e-4f && lwo.z >= 1e-4f))
+    {
+        disney_eval_pdf_split(d, lwi, lwo, f, pdf);
+        return;
+    }
+    const float cti = lwi.z, cto = lwo.z;
+    const V3 lwh = normalize(lwi + lwo);
+    const float ctd = dot(lwi, lwh);
+    const float cth = lwh.z, sth = sin_theta_n(lwh);
+    const float tti = tan_theta(lwi), tto = tan_theta(lwo);
+    V3 diffuse(0), sheen(0);
+    if(d.metallic < 1.0f)
+    {
+        const V3 lambert = d.C / PI;
+        const float fl = one_minus_5(cti), fv = one_minus_5(cto);
+        const float rr = 2.0f * d.roughness * ctd * ctd;
+        const V3 retro = d.C / PI * (rr * (fl + fv + fl * fv * (rr - 1)));
+        diffuse = lambert * ((1.0f - 0.5f * fl) * (1.0f - 0.5f * fv)) + retro;
+        if(d.sheen > 0.0f)
+            sheen = 4.0f * d.sheen * lerp3(V3(1.0f), d.C_tint, d.sheen_tint) * one_minus_5(ctd);
+    }
+    // specular (disney_eval_specular)
+    const V3 Cspec = lerp3(lerp3(V3(1.0f), d.C_tint, d.specular_tint), d.C, d.metallic);
+    const V3 dielectric = Cspec * dielectric_fresnel(d.ior, 1.0f, ctd);
+    const V3 conductor = schlick3(Cspec, ctd);
+    const V3 Fs = lerp3(d.specular * dielectric, conductor, d.metallic);
+    const float Ds = gtr2_of(lwh, d.ax, d.ay);
+    float cpi, spi, cpo, spo;
+    phi_cs(lwi, cpi, spi);
+    phi_cs(lwo, cpo, spo);
+    // G is even in sin(phi): the pdf's |sin(phi_o)| gives the same Go
+    const float Go = mf_smith_aniso_gtr2(cpo, spo, d.ax, d.ay, tto);
+    const float G = mf_smith_aniso_gtr2(cpi, spi, d.ax, d.ay, tti) * Go;
+    const V3 specular = Fs * (Ds * G / fabsf(4.0f * cti * cto));
+    const float cc_D = mf_gtr1(sth, cth, d.clearcoat_roughness);
+    V3 clearcoat(0);
+    if(d.clearcoat > 0.0f)
+    {
+        const float Fc = schlick(0.04f, ctd);
+        const float Gc = mf_smith_gtr2(tti, 0.25f) * mf_smith_gtr2(tto, 0.25f);
+        clearcoat = V3(d.clearcoat * cc_D * Fc * Gc / fabsf(4.0f * cti * cto));
+    }
+    f = (diffuse + sheen) * ((1.0f - d.metallic) * (1.0f - d.transmission)) + specular + clearcoat;
+    const float pdf_spec = Go * Ds / (4.0f * lwo.z);
+    const float pdf_cc = cth * cc_D / (4.0f * ctd);
+    pdf = d.w_diffuse * pdf_hemisphere_zweighted(lwi) + d.w_specular * pdf_spec + d.w_clearcoat * pdf_cc;
+}
+
 BT_HD V3 disney_sample_transmission(const DisneyParams &d, V3 lwo, float s0, float s1)
 {
     const V3 lwh = mf_sample_aniso_gtr2(d.trans_ax, d.trans_ay, s0, s1);
@@ -571,16 +608,16 @@ BT_HD V3 disney_sample_clearcoat(const DisneyParams &d, V3 lwo, float s0, float 
     return normalize(lwi);
 }
 
-BT_HD CompSample disney_sample(const DisneyParams &d, V3 lwo, float s0, float s1, float s2)
+// Disney::sample direction (disney.cpp): lobe selection by s0, the lobe's sampler on
+// (s1, s2); false when no direction results
+BT_HD bool disney_sample_dir(const DisneyParams &d, V3 lwo, float s0, float s1, float s2, V3 &lwi)
 {
-    CompSample r = comp_clear();
     if(fabsf(lwo.z) < 1e-4f)
-        return r;
-    V3 lwi;
+        return false;
     if(lwo.z < 0)
     {
         if(d.transmission == 0.0f)
-            return r;
+            return false;
         const float macro_F = clampf(dielectric_fresnel(d.ior, 1, lwo.z), 0.1f, 0.9f);
         lwi = s0 >= macro_F ? disney_sample_transmission(d, lwo, s1, s2) : disney_sample_inner_refl(d, lwo, s1, s2);
     }
@@ -604,16 +641,14 @@ BT_HD CompSample disney_sample(const DisneyParams &d, V3 lwo, float s0, float s1
             }
         }
     }
-    if(lwi.x == 0 && lwi.y == 0 && lwi.z == 0)
-        return r;
-    r.dir = lwi;
-    r.f = disney_eval(d, lwi, lwo);
-    r.pdf = disney_pdf(d, lwi, lwo);
-    // handle_bad_sample (disney.cpp:566-573)
-    const V3 v = r.f * (fabsf(r.dir.z) / r.pdf);
-    if(fmaxf(fmaxf(v.x, v.y), v.z) > 10)
-        return comp_clear();
-    return r;
+    return !(lwi.x == 0 && lwi.y == 0 && lwi.z == 0);
+}
+
+// handle_bad_sample (disney.cpp:566-573): a sample whose f |cos| / pdf exceeds 10 is dropped
+BT_HD bool disney_bad_sample(V3 f, V3 lwi, float pdf)
+{
+    const V3 v = f * (fabsf(lwi.z) / pdf);
+    return fmaxf(fmaxf(v.x, v.y), v.z) > 10;
 }
 
 // ---------------------------------------------------------------- shading frame + aggregate
@@ -674,41 +709,65 @@ BT_HD MaterialEval make_material_eval(const Material &m)
     return e;
 }
 
+// Direction of the component's sample (diffuse: cosine hemisphere; metal: visible-normal
+// GGX; disney: lobe selection); false when there is none.
+BT_HD bool comp_sample_dir(const MaterialEval &e, V3 lwo, float s0, float s1, float s2, V3 &lwi)
+{
+    if(e.type == MAT_DIFFUSE)
+    {
+        if(lwo.z <= 0)
+            return false;
+        lwi = sample_hemisphere_zweighted(s1, s2);
+        return true;
+    }
+    if(e.type == MAT_METAL)
+    {
+        if(lwo.z <= 0)
+            return false;
+        const V3 lwh = normalize(mf_sample_vndf(lwo, e.metal.ax, e.metal.ay, s1, s2));
+        if(lwh.z <= 0)
+            return false;
+        lwi = normalize(2.0f * dot(lwo, lwh) * lwh - lwo);
+        return lwi.z > 0;
+    }
+    return disney_sample_dir(e.disney, lwo, s0, s1, s2, lwi);
+}
+
+BT_HD void comp_eval_pdf(const MaterialEval &e, V3 lwi, V3 lwo, V3 &f, float &pdf)
+{
+    if(e.type == MAT_DIFFUSE)
+    {
+        f = diffuse_eval(e.albedo, lwi, lwo);
+        pdf = diffuse_pdf(lwi, lwo);
+    }
+    else if(e.type == MAT_METAL)
+        metal_eval_pdf(e.metal, lwi, lwo, f, pdf);
+    else
+        disney_eval_pdf(e.disney, lwi, lwo, f, pdf);
+}
+
+// a sampled direction with its f and pdf; Disney drops bad samples
+BT_HD CompSample comp_finish(const MaterialEval &e, V3 lwi, V3 f, float pdf)
+{
+    if(e.type == MAT_DISNEY && disney_bad_sample(f, lwi, pdf))
+        return comp_clear();
+    CompSample r;
+    r.dir = lwi;
+    r.f = f;
+    r.pdf = pdf;
+    r.is_delta = false;
+    return r;
+}
+
 BT_HD CompSample comp_sample(const MaterialEval &e, V3 lwo, float s0, float s1, float s2)
 {
-    if(e.type == MAT_DIFFUSE)
-        return diffuse_sample(e.albedo, lwo, s1, s2);
-    if(e.type == MAT_METAL)
-        return metal_sample(e.metal, lwo, s1, s2);
-    return disney_sample(e.disney, lwo, s0, s1, s2);
-}
-
-BT_HD V3 comp_eval(const MaterialEval &e, V3 lwi, V3 lwo)
-{
-    if(e.type == MAT_DIFFUSE)
-        return diffuse_eval(e.albedo, lwi, lwo);
-    if(e.type == MAT_METAL)
-    {
-        V3 f;
-        float pdf;
-        metal_eval_pdf(e.metal, lwi, lwo, f, pdf);
-        return f;
-    }
-    return disney_eval(e.disney, lwi, lwo);
-}
-
-BT_HD float comp_pdf(const MaterialEval &e, V3 lwi, V3 lwo)
-{
-    if(e.type == MAT_DIFFUSE)
-        return diffuse_pdf(lwi, lwo);
-    if(e.type == MAT_METAL)
-    {
-        V3 f;
-        float pdf;
-        metal_eval_pdf(e.metal, lwi, lwo, f, pdf);
-        return pdf;
-    }
-    return disney_pdf(e.disney, lwi, lwo);
+    V3 lwi;
+    if(!comp_sample_dir(e, lwo, s0, s1, s2, lwi))
+        return comp_clear();
+    V3 f;
+    float pdf;
+    comp_eval_pdf(e, lwi, lwo, f, pdf);
+    return comp_finish(e, lwi, f, pdf);
 }
 
 // Full surface shader: aggregate materials go through the shading-frame logic with a
@@ -721,6 +780,19 @@ struct SurfaceShader
 
     BT_HD CompSample sample(V3 wo, float s0, float s1, float s2) const
     {
+        V3 f;
+        float pdf;
+        return sample_eval(wo, s0, s1, s2, false, V3(0, 0, 1), f, pdf);
+    }
+
+    // BSDF sample for the path's next direction and, when want_li, f and pdf of the light
+    // sample's direction wi_li (zero for delta shaders); the values are those of sample
+    // and eval_pdf, each evaluation computing f and pdf in one pass.
+    BT_HD CompSample sample_eval(V3 wo, float s0, float s1, float s2, bool want_li, V3 wi_li, V3 &f_li,
+                                 float &pdf_li) const
+    {
+        f_li = V3(0);
+        pdf_li = 0.0f;
         CompSample r = comp_clear();
         if(mat.type == MAT_BLACK)
             return r;
@@ -753,7 +825,24 @@ struct SurfaceShader
             return r;
         }
         const V3 lwo = normalize(fr.shading.global_to_local(wo));
-        const CompSample c = comp_sample(mat, lwo, s0, s1, s2);
+        V3 lwi_bs(0, 0, 1);
+        const bool has_bs = comp_sample_dir(mat, lwo, s0, s1, s2, lwi_bs);
+        const V3 lwi_li = want_li ? normalize(fr.shading.global_to_local(wi_li)) : V3(0, 0, 1);
+        V3 f_bs(0);
+        float pdf_bs = 0.0f;
+        if(has_bs)
+            comp_eval_pdf(mat, lwi_bs, lwo, f_bs, pdf_bs);
+        if(want_li)
+        {
+            comp_eval_pdf(mat, lwi_li, lwo, f_li, pdf_li);
+            float kk = fr.correct_shading_energy(wi_li);
+            if(shadow_terminator)
+                kk *= frame.shadow_terminator(wi_li);
+            f_li = f_li * kk;
+        }
+        if(!has_bs)
+            return r;
+        const CompSample c = comp_finish(mat, lwi_bs, f_bs, pdf_bs);
         if(c.pdf <= 0)
             return r;
         r.dir = fr.shading.local_to_global(c.dir);
@@ -810,27 +899,20 @@ struct SurfaceShader
         return r;
     }
 
-    BT_HD V3 eval(V3 wi, V3 wo) const
+    BT_HD void eval_pdf(V3 wi, V3 wo, V3 &f, float &pdf) const
     {
+        f = V3(0);
+        pdf = 0.0f;
         if(mat.type == MAT_BLACK || mat.type == MAT_INVISIBLE || mat.type == MAT_MIRROR || mat.type == MAT_GLASS)
-            return V3(0);
+            return;
         const ShaderFrame fr = frame.flip_for_black_fringes(wo);
         const V3 lwi = normalize(fr.shading.global_to_local(wi));
         const V3 lwo = normalize(fr.shading.global_to_local(wo));
         float k = fr.correct_shading_energy(wi);
         if(shadow_terminator)
             k *= frame.shadow_terminator(wi);
-        return comp_eval(mat, lwi, lwo) * k;
-    }
-
-    BT_HD float pdf(V3 wi, V3 wo) const
-    {
-        if(mat.type == MAT_BLACK || mat.type == MAT_INVISIBLE || mat.type == MAT_MIRROR || mat.type == MAT_GLASS)
-            return 0.0f;
-        const ShaderFrame fr = frame.flip_for_black_fringes(wo);
-        const V3 lwi = normalize(fr.shading.global_to_local(wi));
-        const V3 lwo = normalize(fr.shading.global_to_local(wo));
-        return comp_pdf(mat, lwi, lwo);
+        comp_eval_pdf(mat, lwi, lwo, f, pdf);
+        f = f * k;
     }
 };
 

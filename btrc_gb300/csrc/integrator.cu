@@ -263,7 +263,7 @@ __device__ float ibl_pdf_local(const DevScene &S, V3 to_light)
     const float tile_pdf = S.env_probs[ty * w + tx];
     const float u0 = static_cast<float>(tx) / w, u1 = static_cast<float>(tx + 1) / w;
     const float v0 = static_cast<float>(ty) / h, v1 = static_cast<float>(ty + 1) / h;
-    const float c0 = cosf(PI * v0), c1 = cosf(PI * v1);
+    const float c0 = cos_pi(v0), c1 = cos_pi(v1);
     return tile_pdf * (1.0f / fabsf(2 * PI * (u1 - u0) * (c1 - c0)));
 }
 
@@ -293,6 +293,39 @@ struct LightSample
     float t1, light_pdf;
     V3 li;
 };
+
+// IBL::sample_li_inline (ibl.cpp:31-42) over EnvirLightSampler::sample (env_sampler.cpp:137-163)
+__device__ __forceinline__ void sample_ibl(const DevScene &S, V3 ref_pos, V3 ref_nor, bool offset_origin, float s0,
+                                        float s1, float s2, float select_pdf, LightSample &r)
+{
+    const int w = S.env.lut_w, h = S.env.lut_h;
+    const uint32_t tile = alias_sample(S.env_alias, static_cast<uint32_t>(w * h), s0);
+    const int ty = static_cast<int>(tile) / w, tx = static_cast<int>(tile) % w;
+    const float tile_pdf = S.env_probs[tile];
+    const float u0 = static_cast<float>(tx) / w, u1 = static_cast<float>(tx + 1) / w;
+    const float v0 = static_cast<float>(ty) / h, v1 = static_cast<float>(ty + 1) / h;
+    float cv0 = cos_pi(v0), cv1 = cos_pi(v1);
+    if(cv0 > cv1)
+    {
+        const float t = cv0;
+        cv0 = cv1;
+        cv1 = t;
+    }
+    const float cos_theta = cv0 + s2 * (cv1 - cv0);
+    const float sin_theta = cos2sin(cos_theta);
+    float sp, cp;
+    sincos_pi(2.0f * (u0 + (u1 - u0) * s1), sp, cp);
+    const V3 local(sin_theta * cp, sin_theta * sp, cos_theta);
+    const float in_tile_pdf = 1.0f / (2 * PI * (u1 - u0) * (cv1 - cv0));
+    const V3 dir = V3(S.env.frame_x[0], S.env.frame_x[1], S.env.frame_x[2]) * local.x +
+                   V3(S.env.frame_y[0], S.env.frame_y[1], S.env.frame_y[2]) * local.y +
+                   V3(S.env.up[0], S.env.up[1], S.env.up[2]) * local.z;
+    r.o = offset_origin ? offset_dir(ref_pos, ref_nor, dir) : ref_pos;
+    r.d = dir;
+    r.t1 = MAX_FLOAT;
+    r.li = ibl_eval_local(S, local);
+    r.light_pdf = select_pdf * (tile_pdf * in_tile_pdf);
+}
 
 // sample_light_li_impl (builtin/.../wavefront/helper.cpp:9-61); offset_origin selects the
 // surface form (origin offset along the normal) or the medium form (origin = ref_pos)
@@ -338,35 +371,7 @@ __device__ LightSample sample_light(const DevScene &S, V3 ref_pos, V3 ref_nor, b
         r.light_pdf = select_pdf * pdf_sa;
     }
     else if(S.env.type == ENV_IBL)
-    {
-        // IBL::sample_li_inline (ibl.cpp:31-42) over EnvirLightSampler::sample (env_sampler.cpp:137-163)
-        const int w = S.env.lut_w, h = S.env.lut_h;
-        const uint32_t tile = alias_sample(S.env_alias, static_cast<uint32_t>(w * h), s0);
-        const int ty = static_cast<int>(tile) / w, tx = static_cast<int>(tile) % w;
-        const float tile_pdf = S.env_probs[tile];
-        const float u0 = static_cast<float>(tx) / w, u1 = static_cast<float>(tx + 1) / w;
-        const float v0 = static_cast<float>(ty) / h, v1 = static_cast<float>(ty + 1) / h;
-        float cv0 = cosf(PI * v0), cv1 = cosf(PI * v1);
-        if(cv0 > cv1)
-        {
-            const float t = cv0;
-            cv0 = cv1;
-            cv1 = t;
-        }
-        const float cos_theta = cv0 + s2 * (cv1 - cv0);
-        const float sin_theta = cos2sin(cos_theta);
-        const float phi = 2 * PI * (u0 + (u1 - u0) * s1);
-        const V3 local(sin_theta * cosf(phi), sin_theta * sinf(phi), cos_theta);
-        const float in_tile_pdf = 1.0f / (2 * PI * (u1 - u0) * (cv1 - cv0));
-        const V3 dir = V3(S.env.frame_x[0], S.env.frame_x[1], S.env.frame_x[2]) * local.x +
-                       V3(S.env.frame_y[0], S.env.frame_y[1], S.env.frame_y[2]) * local.y +
-                       V3(S.env.up[0], S.env.up[1], S.env.up[2]) * local.z;
-        r.o = offset_origin ? offset_dir(ref_pos, ref_nor, dir) : ref_pos;
-        r.d = dir;
-        r.t1 = MAX_FLOAT;
-        r.li = ibl_eval_local(S, local);
-        r.light_pdf = select_pdf * (tile_pdf * in_tile_pdf);
-    }
+        sample_ibl(S, ref_pos, ref_nor, offset_origin, s0, s1, s2, select_pdf, r);
     else
     {
         // GradientSky::sample_li_inline (builtin/btrc/builtin/light/gradient_sky.cpp:28-35)
@@ -1146,8 +1151,9 @@ __global__ void __launch_bounds__(BLOCK) k_medium(DevScene S, DevRender R, PathS
         }
         const float cos_theta = -u;
         const float sin_theta = cos2sin(cos_theta);
-        const float phi = 2 * PI * s1;
-        const V3 lwi(sin_theta * sinf(phi), sin_theta * cosf(phi), cos_theta);
+        float sp, cp;
+        sincos_pi(2.0f * s1, sp, cp);
+        const V3 lwi(sin_theta * sp, sin_theta * cp, cos_theta);
         const float phase_val = henyey_greenstein(g, u);
         const V3 phase = albedo * phase_val;
         V3 ndir = Frame::from_z(-d).local_to_global(lwi);
@@ -1262,9 +1268,10 @@ __device__ __forceinline__ bool nrc_query_at(const DevScene &S, const SurfacePoi
 }
 
 // TEX = false compiles the texture evaluation out, so scenes without textured materials
-// keep the shade kernel's registers
+// keep the shade kernel's registers. Two blocks per SM (at most 128 registers a thread):
+// the kernel waits on scattered loads, and the occupancy pays for the few spills.
 template<bool TEX, bool NRC = false>
-__global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, DevRender R, PathSoA P, PathSoA N, ShadowSoA SH,
+__global__ void __launch_bounds__(BLOCK, 2) k_shade(DevScene S, DevRender R, PathSoA P, PathSoA N, ShadowSoA SH,
                                                  const uint32_t *flags, const HitDetail *hits,
                                                  const uint32_t *order, float4 *film, Counters *cnt)
 {
@@ -1370,16 +1377,11 @@ __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, DevRender R, PathSo
         float u0, u1, u2;
         smp.get3d(u0, u1, u2);
         const V3 wo = -d;
-        CompSample bs = sh.sample(wo, u0, u1, u2);
-        V3 shadow_f(0);
-        float shadow_pdf = 0;
+        V3 shadow_f;
+        float shadow_pdf;
+        CompSample bs = sh.sample_eval(wo, u0, u1, u2, ls.success, ls.d, shadow_f, shadow_pdf);
         if(ls.success)
-        {
-            shadow_f = sh.eval(ls.d, wo);
             ls.success = !is_zero(shadow_f);
-            if(ls.success)
-                shadow_pdf = sh.pdf(ls.d, wo);
-        }
 
         if(ls.success)
         {
@@ -1728,13 +1730,16 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
         stats->device_ms = ms;
         stats->node_visits = fin.node_visits;
         stats->tri_tests = fin.tri_tests;
-        const uint64_t per_bounce = S.has_media ? 6 : 5;
+        // per bounce: control, generate, trace, [medium], order + shade, shadow
+        const uint64_t per_bounce = S.has_media ? 7 : 6;
         for(int k = 0; k < STAGE_COUNT; ++k)
             stats->stage_launches[k] = launches[k];
         if(use_graphs)
         {
             for(int k = 0; k < STAGE_COUNT; ++k)
-                stats->stage_launches[k] = (k == STAGE_MEDIUM && !S.has_media) ? 0 : graph_launches * 2;
+                stats->stage_launches[k] = (k == STAGE_MEDIUM && !S.has_media) ? 0
+                                           : k == STAGE_SHADE                    ? graph_launches * 4
+                                                                                 : graph_launches * 2;
             stats->kernel_launches = graph_launches * 2 * per_bounce;
         }
         else
@@ -1904,13 +1909,13 @@ __global__ void __launch_bounds__(128) k_nrc_train_paths(DevScene S, DevRender R
             float u0, u1, u2;
             smp.get3d(u0, u1, u2);
             const V3 wo = -d;
-            const CompSample bs = sh.sample(wo, u0, u1, u2);
+            V3 f;
+            float spdf;
+            const CompSample bs = sh.sample_eval(wo, u0, u1, u2, ls.success, ls.d, f, spdf);
             if(ls.success)
             {
-                const V3 f = sh.eval(ls.d, wo);
                 if(!is_zero(f))
                 {
-                    const float spdf = sh.pdf(ls.d, wo);
                     const float cs = fabsf(dot(normalize(ls.d), sp.frame.z));
                     const V3 li = ls.li * beta * f * cs / (spdf + ls.light_pdf);
                     if(!trace_any(make_trav_ray(ls.o.x, ls.o.y, ls.o.z, ls.d.x, ls.d.y, ls.d.z), ls.t1, nodes, tris,
@@ -2187,8 +2192,9 @@ __global__ void k_bsdf_batch(int op, const Material *mats, const float *wo, cons
     if(op == 0)
     {
         const V3 lwi(wu[i * 3 + 0], wu[i * 3 + 1], wu[i * 3 + 2]);
-        const V3 f = comp_eval(e, lwi, lwo);
-        const float pdf = comp_pdf(e, lwi, lwo);
+        V3 f;
+        float pdf;
+        comp_eval_pdf(e, lwi, lwo, f, pdf);
         out[i * 4 + 0] = f.x;
         out[i * 4 + 1] = f.y;
         out[i * 4 + 2] = f.z;

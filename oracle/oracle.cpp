@@ -805,6 +805,16 @@ template<class T> struct CS
 
 template<class T> T PI_T() { return T(3.14159265358979323846); }
 
+// sin(pi x) and cos(pi x), as the kernels evaluate sampled angles (sincospif): computed
+// in double and rounded once
+template<class T> void sincos_pi(T x, T &s, T &c)
+{
+    const double a = 3.14159265358979323846 * static_cast<double>(x);
+    s = static_cast<T>(std::sin(a));
+    c = static_cast<T>(std::cos(a));
+}
+template<class T> T cos_pi(T x) { return static_cast<T>(std::cos(3.14159265358979323846 * static_cast<double>(x))); }
+
 template<class T> V<T> hemi_zw(T u1, T u2)
 {
     T sx = 0, sy = 0;
@@ -812,19 +822,21 @@ template<class T> V<T> hemi_zw(T u1, T u2)
     u2 = T(2) * u2 - T(1);
     if(u1 != 0 || u2 != 0)
     {
-        T theta, r;
+        T theta, r;  // in units of pi
         if(std::abs(u1) > std::abs(u2))
         {
             r = u1;
-            theta = T(0.25) * PI_T<T>() * (u2 / u1);
+            theta = T(0.25) * (u2 / u1);
         }
         else
         {
             r = u2;
-            theta = T(0.5) * PI_T<T>() - T(0.25) * PI_T<T>() * (u1 / u2);
+            theta = T(0.5) - T(0.25) * (u1 / u2);
         }
-        sx = r * std::cos(theta);
-        sy = r * std::sin(theta);
+        T st, ct;
+        sincos_pi(theta, st, ct);
+        sx = r * ct;
+        sy = r * st;
     }
     return V<T>(sx, sy, std::sqrt(std::max(T(0), T(1) - (sx * sx + sy * sy))));
 }
@@ -893,8 +905,10 @@ template<class T> T smith_aniso(T cp, T sp, T ax, T ay, T tt)
 }
 template<class T> V<T> sample_aniso_gtr2(T ax, T ay, T s0, T s1)
 {
-    T sph = ay * std::sin(2 * PI_T<T>() * s0);
-    T cph = ax * std::cos(2 * PI_T<T>() * s0);
+    T sp, cp;
+    sincos_pi(T(2) * s0, sp, cp);
+    T sph = ay * sp;
+    T cph = ax * cp;
     T nor = T(1) / std::sqrt(sq(sph) + sq(cph));
     sph *= nor;
     cph *= nor;
@@ -909,10 +923,11 @@ template<class T> T gtr1(T sth, T cth, T a)
 }
 template<class T> V<T> sample_gtr1(T a, T s0, T s1)
 {
-    T phi = 2 * PI_T<T>() * s0;
     T cth = std::sqrt((std::pow(a, T(2) - T(2) * s1) - T(1)) / (sq(a) - T(1)));
     T sth = cos2sin(cth);
-    return nrm(V<T>(sth * std::cos(phi), sth * std::sin(phi), cth));
+    T sp, cp;
+    sincos_pi(T(2) * s0, sp, cp);
+    return nrm(V<T>(sth * cp, sth * sp, cth));
 }
 template<class T> V<T> sample_vndf(V<T> ve, T ax, T ay, T s0, T s1)
 {
@@ -922,8 +937,9 @@ template<class T> V<T> sample_vndf(V<T> ve, T ax, T ay, T s0, T s1)
     if(lensq > T(3e-4))
         t1 = V<T>(-vh.y, vh.x, 0) / std::sqrt(lensq);
     V<T> t2 = cross(vh, t1);
-    T r = std::sqrt(s0), phi = 2 * PI_T<T>() * s1;
-    T a1 = r * std::cos(phi), a2_ = r * std::sin(phi);
+    T r = std::sqrt(s0), sp, cp;
+    sincos_pi(T(2) * s1, sp, cp);
+    T a1 = r * cp, a2_ = r * sp;
     T s = T(0.5) * (T(1) + vh.z);
     T a2 = (T(1) - s) * std::sqrt(T(1) - a1 * a1) + s * a2_;
     V<T> nh = a1 * t1 + a2 * t2 + std::sqrt(std::max(T(0), T(1) - a1 * a1 - a2 * a2)) * vh;
@@ -1574,7 +1590,7 @@ float env_pdf(const Prepared &P, V3f d)
     const int ty = std::min(std::max(static_cast<int>(std::floor(v * h)), 0), h - 1);
     const float u0 = static_cast<float>(tx) / w, u1 = static_cast<float>(tx + 1) / w;
     const float v0 = static_cast<float>(ty) / h, v1 = static_cast<float>(ty + 1) / h;
-    return P.env_probs[ty * w + tx] / std::fabs(2 * PIf * (u1 - u0) * (std::cos(PIf * v1) - std::cos(PIf * v0)));
+    return P.env_probs[ty * w + tx] * (1.0f / std::fabs(2 * PIf * (u1 - u0) * (cos_pi(v1) - cos_pi(v0))));
 }
 
 void build_env_table(Prepared &P)
@@ -2113,13 +2129,14 @@ LightSample sample_light(const Prepared &P, V3f ref, V3f ref_nor, bool offset_or
         const int ty = static_cast<int>(tile) / w, tx = static_cast<int>(tile) % w;
         const float u0 = static_cast<float>(tx) / w, u1 = static_cast<float>(tx + 1) / w;
         const float v0 = static_cast<float>(ty) / h, v1 = static_cast<float>(ty + 1) / h;
-        float cv0 = std::cos(PIf * v0), cv1 = std::cos(PIf * v1);
+        float cv0 = cos_pi(v0), cv1 = cos_pi(v1);
         if(cv0 > cv1)
             std::swap(cv0, cv1);
         const float ct = cv0 + s2 * (cv1 - cv0);
         const float st = std::sqrt(std::max(0.0f, 1.0f - ct * ct));
-        const float phi = 2 * PIf * (u0 + (u1 - u0) * s1);
-        const V3f local(st * std::cos(phi), st * std::sin(phi), ct);
+        float sp, cp;
+        sincos_pi(2.0f * (u0 + (u1 - u0) * s1), sp, cp);
+        const V3f local(st * cp, st * sp, ct);
         const V3f dir = P.env_frame.l2g(local);
         r.o = offset_origin ? ioffset_dir(ref, ref_nor, dir) : ref;
         r.d = dir;
@@ -2130,9 +2147,10 @@ LightSample sample_light(const Prepared &P, V3f ref, V3f ref_nor, bool offset_or
     else
     {
         const float z = 1.0f - (s0 + s0);
-        const float phi = 2.0f * PIf * s1;
         const float rr = std::sqrt(std::max(0.0f, 1.0f - z * z));
-        const V3f dir(rr * std::cos(phi), rr * std::sin(phi), z);
+        float sp, cp;
+        sincos_pi(2.0f * s1, sp, cp);
+        const V3f dir(rr * cp, rr * sp, z);
         r.o = offset_origin ? ioffset_dir(ref, ref_nor, dir) : ref;
         r.d = dir;
         r.t1 = FMAX;
@@ -2275,8 +2293,10 @@ void trace_path(const Prepared &P, uint64_t g, double *film, double *aov = nullp
                             const float g2 = pg * pg;
                             u = (1.0f + g2 - sq((1.0f - g2) / (1.0f + pg * ss))) / (pg + pg);
                         }
-                        const float ct = -u, st = cos2sin(ct), phi = 2 * PIf * a1;
-                        const V3f lwi(st * std::sin(phi), st * std::cos(phi), ct);
+                        const float ct = -u, st = cos2sin(ct);
+                        float sp, cp;
+                        sincos_pi(2.0f * a1, sp, cp);
+                        const V3f lwi(st * sp, st * cp, ct);
                         const float pv = hg(pg, u);
                         const V3f phase = pcolor * pv;
                         const V3f nd = Frame<float>::from_z(-d).l2g(lwi);
