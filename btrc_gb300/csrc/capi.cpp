@@ -279,6 +279,9 @@ void build_scene(btrc_scene *sc, int threads)
         return;
     }
 
+    // the traversal's pooled triangle tests address triangle records with 27 bits
+    if(bvh.tris.size() >= (1ull << 27))
+        throw StatusError(BTRC_ERR_INVALID_ARG, "scene exceeds 2^27 triangle records");
     DevScene &D = sc->dev;
     D = DevScene{};
     D.nodes = reinterpret_cast<const F4 *>(dev_upload(sc->allocs, bvh.nodes.data(), bvh.nodes.size()));

@@ -953,7 +953,7 @@ __global__ void __launch_bounds__(BLOCK) k_generate(DevRender R, PathSoA P, floa
 }
 
 template<bool COUNT>
-__global__ void __launch_bounds__(128) k_trace(DevScene S, PathSoA P, uint32_t *flags, HitDetail *hits,
+__global__ void __launch_bounds__(TRAVERSE_BLOCK) k_trace(DevScene S, PathSoA P, uint32_t *flags, HitDetail *hits,
                                                Counters *cnt)
 {
     const uint32_t n = cnt->active;
@@ -1444,7 +1444,7 @@ ShadeKernel shade_kernel(const DevScene &S, const DevRender &R)
 // MEDIA = false compiles the transmittance code out, so the traversal of scenes without
 // media keeps its registers
 template<bool MEDIA>
-__global__ void __launch_bounds__(128) k_shadow(DevScene S, DevRender R, ShadowSoA SH, float4 *film, Counters *cnt)
+__global__ void __launch_bounds__(TRAVERSE_BLOCK) k_shadow(DevScene S, DevRender R, ShadowSoA SH, float4 *film, Counters *cnt)
 {
     const uint32_t n = cnt->shadow;
     traverse_refill<true>(
@@ -1556,9 +1556,9 @@ cudaError_t enqueue_bounce(const DevScene &S, const DevRender &R, RenderBuffers 
           [&] { k_generate<<<grids[0], BLOCK, 0, st>>>(R, P, B.film, B.counters, S.vacuum_medium); });
     timed(T, STAGE_TRACE, st, launches, [&] {
         if(profile == 2)
-            k_trace<true><<<grids[1], 128, 0, st>>>(S, P, B.hit_flag, B.hit_detail, B.counters);
+            k_trace<true><<<grids[1], TRAVERSE_BLOCK, 0, st>>>(S, P, B.hit_flag, B.hit_detail, B.counters);
         else
-            k_trace<false><<<grids[1], 128, 0, st>>>(S, P, B.hit_flag, B.hit_detail, B.counters);
+            k_trace<false><<<grids[1], TRAVERSE_BLOCK, 0, st>>>(S, P, B.hit_flag, B.hit_detail, B.counters);
     });
     if(S.has_media)
         timed(T, STAGE_MEDIUM, st, launches, [&] {
@@ -1573,9 +1573,9 @@ cudaError_t enqueue_bounce(const DevScene &S, const DevRender &R, RenderBuffers 
     timed(T, STAGE_SHADOW, st, launches,
           [&] {
               if(S.has_media)
-                  k_shadow<true><<<grids[4], 128, 0, st>>>(S, R, B.shadow, B.film, B.counters);
+                  k_shadow<true><<<grids[4], TRAVERSE_BLOCK, 0, st>>>(S, R, B.shadow, B.film, B.counters);
               else
-                  k_shadow<false><<<grids[4], 128, 0, st>>>(S, R, B.shadow, B.film, B.counters);
+                  k_shadow<false><<<grids[4], TRAVERSE_BLOCK, 0, st>>>(S, R, B.shadow, B.film, B.counters);
           });
     return cudaGetLastError();
 }
@@ -1626,10 +1626,10 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
         return e;
     const int grids[6] = {
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_generate), R.grid_pct),
-        persistent_grid(128, reinterpret_cast<const void *>(k_trace<false>), R.grid_pct),
+        persistent_grid(TRAVERSE_BLOCK, reinterpret_cast<const void *>(k_trace<false>), R.grid_pct),
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_medium), R.grid_pct),
         persistent_grid(BLOCK, reinterpret_cast<const void *>(shade_kernel(S, R)), R.grid_pct),
-        persistent_grid(128, S.has_media ? reinterpret_cast<const void *>(k_shadow<true>)
+        persistent_grid(TRAVERSE_BLOCK, S.has_media ? reinterpret_cast<const void *>(k_shadow<true>)
                                          : reinterpret_cast<const void *>(k_shadow<false>), R.grid_pct),
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_order), R.grid_pct),
     };
@@ -2100,10 +2100,10 @@ cudaError_t render_wavefront_noalloc(const DevScene &S, const DevRender &R, void
         return e;
     const int grids[6] = {
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_generate), R.grid_pct),
-        persistent_grid(128, reinterpret_cast<const void *>(k_trace<false>), R.grid_pct),
+        persistent_grid(TRAVERSE_BLOCK, reinterpret_cast<const void *>(k_trace<false>), R.grid_pct),
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_medium), R.grid_pct),
         persistent_grid(BLOCK, reinterpret_cast<const void *>(shade_kernel(S, R)), R.grid_pct),
-        persistent_grid(128, S.has_media ? reinterpret_cast<const void *>(k_shadow<true>)
+        persistent_grid(TRAVERSE_BLOCK, S.has_media ? reinterpret_cast<const void *>(k_shadow<true>)
                                          : reinterpret_cast<const void *>(k_shadow<false>), R.grid_pct),
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_order), R.grid_pct),
     };

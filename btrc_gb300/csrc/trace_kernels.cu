@@ -8,7 +8,7 @@ namespace bt {
 
 namespace {
 
-constexpr int TRACE_BLOCK = 128;
+constexpr int TRACE_BLOCK = TRAVERSE_BLOCK;  // traverse_refill's shared-memory slices
 
 __global__ void __launch_bounds__(TRACE_BLOCK) k_trace_stats(DevScene S, const Ray *__restrict__ rays, uint32_t n,
                                                              uint32_t *__restrict__ nv, uint32_t *__restrict__ tv,

@@ -372,11 +372,28 @@ namespace bt {
 // Persistent traversal with warp-level ray refill. Every lane runs the same loop; a lane
 // whose ray has finished becomes idle, and once at least `refill` lanes of the warp are
 // idle (or no lane is busy) the idle lanes take the next rays from a global cursor with
-// one atomic per warp. Each loop iteration advances every busy lane by one node (plus
-// that node's triangles), so lanes never wait for the slowest ray of their warp.
-// All 32 lanes must enter (the warp-wide votes use the full mask).
+// one atomic per warp. Each loop iteration advances every busy lane by one node, so
+// lanes never wait for the slowest ray of their warp.
+//
+// Triangle tests are pooled across the warp: after the node step every lane's pending
+// triangles (the leaf bits of its node) are queued in shared memory, up to 32 per
+// iteration, and each lane of the warp then tests one queued (ray, triangle) pair with
+// the owning lane's ray, read from shared memory. The owners merge their results by
+// shuffles. A lane whose triangles did not all fit keeps the rest for the next
+// iteration and takes no node step meanwhile. Testing a leaf's triangles one after the
+// other, lane by lane, ran with ~3 of 32 lanes active; pooled, a round runs with as
+// many lanes as the warp has tests. Results are those of sequential testing: the
+// closest hit is a strict total order on (t, instance, primitive).
+//
+// The kernel launches 128-thread blocks (TRAVERSE_WARPS warps, one shared-memory slice
+// each), and all 32 lanes of a warp enter (the warp-wide votes use the full mask).
 //   fetch(i, o, d, t1): load ray i;  emit(i, hit): store its result
 constexpr int REFILL_LANES = 8;  // idle lanes that trigger a warp refill (measured best of 8/16/24)
+constexpr int TRAVERSE_BLOCK = 128;
+constexpr int TRAVERSE_WARPS = TRAVERSE_BLOCK / 32;
+// queue entry: owner lane in bits 27..31, triangle record index in bits 0..26
+constexpr uint32_t TRI_INDEX_BITS = 27;
+constexpr uint32_t MAX_POOLED_TRIANGLES = 1u << TRI_INDEX_BITS;
 
 template<bool ANY, bool COUNT = false, typename Fetch, typename Emit>
 __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes4, const float4 *__restrict__ tris4,
@@ -384,10 +401,16 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
                                                 uint32_t *err, Fetch fetch, Emit emit,
                                                 uint64_t *node_visits = nullptr, uint64_t *tri_tests = nullptr)
 {
+    // per lane: (ox, oy, oz, Sx), (Sy, Sz, kx | ky << 2 | kz << 4, tmax); per warp: the queue
+    __shared__ float4 s_ray0[TRAVERSE_WARPS][32];
+    __shared__ float4 s_ray1[TRAVERSE_WARPS][32];
+    __shared__ uint32_t s_queue[TRAVERSE_WARPS][32];
     uint64_t visits = 0, tests = 0;
     const uint32_t FULL = 0xffffffffu;
     const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warp = threadIdx.x >> 5;
     const uint32_t lt_mask = (1u << lane) - 1u;
+    const float NO_HIT = __int_as_float(0x7f800000);
     int state = 0;  // 0 idle, 1 busy, 2 exhausted
     uint32_t ray = 0;
     TravRay r;
@@ -424,6 +447,9 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
                     ngroup = make_uint2(0u, node_count ? 0x80000000u : 0u);
                     tgroup = make_uint2(0u, 0u);
                     state = 1;
+                    s_ray0[warp][lane] = make_float4(r.ox, r.oy, r.oz, r.Sx);
+                    s_ray1[warp][lane] =
+                        make_float4(r.Sy, r.Sz, __int_as_float(r.kx | (r.ky << 2) | (r.kz << 4)), t1);
                 }
                 else
                     state = 2;
@@ -431,13 +457,12 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
         }
         if(__all_sync(FULL, state == 2))
             break;
-        if(state != 1)
-            continue;
-        if(COUNT && ngroup.y > 0x00ffffffu)
-            ++visits;
 
-        if(ngroup.y > 0x00ffffffu)
+        // node step: busy lanes without pending triangles
+        if(state == 1 && tgroup.y == 0u && ngroup.y > 0x00ffffffu)
         {
+            if(COUNT)
+                ++visits;
             const int bit = 31 - __clz(ngroup.y);
             const uint32_t slot = (static_cast<uint32_t>(bit) - 24u) ^ r.oct_inv;
             const uint32_t rel = __popc(ngroup.y & ~(0xffffffffu << slot));
@@ -468,44 +493,104 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
                 tgroup = make_uint2(tbase, hm & 0x00ffffffu);
             }
         }
-        bool done_any = false;
-        while(tgroup.y != 0u)
+
+        // triangle round (all lanes): queue positions by a warp prefix sum of the counts
+        const uint32_t cnt = static_cast<uint32_t>(__popc(tgroup.y));
+        uint32_t incl = cnt;
+#pragma unroll
+        for(int off = 1; off < 32; off <<= 1)
         {
-            const int tb = 31 - __clz(tgroup.y);
-            tgroup.y &= ~(1u << tb);
-            const uint32_t ti = tgroup.x + static_cast<uint32_t>(tb);
-            const float4 a = __ldg(tris4 + ti * 3 + 0);
-            const float4 b = __ldg(tris4 + ti * 3 + 1);
-            const float4 c = __ldg(tris4 + ti * 3 + 2);
-            if(COUNT)
-                ++tests;
-            TriHit h;
-            if(watertight(r, a, b, c, best.t, h))
+            const uint32_t v = __shfl_up_sync(FULL, incl, off);
+            if(lane >= static_cast<uint32_t>(off))
+                incl += v;
+        }
+        const uint32_t total = __shfl_sync(FULL, incl, 31);
+        bool found_any = false;
+        if(total != 0u)
+        {
+            const uint32_t excl = incl - cnt;
+            const uint32_t take = excl >= 32u ? 0u : min(cnt, 32u - excl);
+            if(take != 0u)
             {
-                const uint32_t inst = __float_as_uint(a.w), prim = __float_as_uint(b.w);
-                if(!best.hit || closer(h.t, inst, prim, best.t, best.inst, best.prim))
+                uint32_t bits = tgroup.y;
+                for(uint32_t k = 0; k < take; ++k)
                 {
-                    best.hit = true;
-                    best.t = h.t;
-                    best.b1 = h.b1;
-                    best.b2 = h.b2;
-                    best.inst = inst;
-                    best.prim = prim;
+                    const int tb = 31 - __clz(bits);
+                    bits &= ~(1u << tb);
+                    s_queue[warp][excl + k] = (lane << TRI_INDEX_BITS) | (tgroup.x + static_cast<uint32_t>(tb));
                 }
+                tgroup.y = bits;
+                s_ray1[warp][lane].w = best.t;
+                if(COUNT)
+                    tests += take;
+            }
+            __syncwarp();
+            // tester: queue entry `lane`
+            float ht = NO_HIT, hb1 = 0.0f, hb2 = 0.0f;
+            uint32_t hinst = 0u, hprim = 0u;
+            if(lane < min(total, 32u))
+            {
+                const uint32_t e = s_queue[warp][lane];
+                const uint32_t owner = e >> TRI_INDEX_BITS, ti = e & (MAX_POOLED_TRIANGLES - 1u);
+                const float4 q0 = s_ray0[warp][owner], q1 = s_ray1[warp][owner];
+                TravRay tr;
+                tr.ox = q0.x; tr.oy = q0.y; tr.oz = q0.z;
+                tr.Sx = q0.w; tr.Sy = q1.x; tr.Sz = q1.y;
+                const int kk = __float_as_int(q1.z);
+                tr.kx = kk & 3; tr.ky = (kk >> 2) & 3; tr.kz = (kk >> 4) & 3;
+                const float4 a = __ldg(tris4 + ti * 3 + 0);
+                const float4 b = __ldg(tris4 + ti * 3 + 1);
+                const float4 c = __ldg(tris4 + ti * 3 + 2);
+                TriHit h;
+                if(watertight(tr, a, b, c, q1.w, h))
+                {
+                    ht = h.t;
+                    hb1 = h.b1;
+                    hb2 = h.b2;
+                    hinst = __float_as_uint(a.w);
+                    hprim = __float_as_uint(b.w);
+                }
+            }
+            // owners merge their entries [excl, excl + take)
+            const uint32_t rounds = __reduce_max_sync(FULL, take);
+            for(uint32_t k = 0; k < rounds; ++k)
+            {
+                const int src = static_cast<int>(min(excl + k, 31u));
+                const float ct = __shfl_sync(FULL, ht, src);
                 if(ANY)
                 {
-                    done_any = true;
-                    tgroup.y = 0u;
+                    if(k < take && ct != NO_HIT)
+                        found_any = true;
+                }
+                else
+                {
+                    const float cb1 = __shfl_sync(FULL, hb1, src);
+                    const float cb2 = __shfl_sync(FULL, hb2, src);
+                    const uint32_t ci = __shfl_sync(FULL, hinst, src);
+                    const uint32_t cp = __shfl_sync(FULL, hprim, src);
+                    if(k < take && ct != NO_HIT && (!best.hit || closer(ct, ci, cp, best.t, best.inst, best.prim)))
+                    {
+                        best.hit = true;
+                        best.t = ct;
+                        best.b1 = cb1;
+                        best.b2 = cb2;
+                        best.inst = ci;
+                        best.prim = cp;
+                    }
                 }
             }
         }
-        if(done_any)
+        if(state != 1)
+            continue;
+        if(ANY && found_any)
         {
+            best.hit = true;
             emit(ray, best);
+            tgroup.y = 0u;
             state = 0;
             continue;
         }
-        if(ngroup.y <= 0x00ffffffu)
+        if(tgroup.y == 0u && ngroup.y <= 0x00ffffffu)
         {
             if(sp == 0)
             {
