@@ -400,6 +400,7 @@ void build_scene(btrc_scene *sc, int threads)
         D.has_media = 1;
     const V3 ext = H.world_max - H.world_min;
     D.world_diagonal = length(ext);
+    D.tri_round = TRI_ROUND_TESTS;
 
     // film filter table
     if(H.params.filter == FILTER_GAUSSIAN)

@@ -42,7 +42,12 @@ struct DevScene
     const MaterialTex *material_tex;
     const float *env_probs;    // ibl tile probabilities
     const AliasEntry8 *env_alias;
+    int32_t tri_round;         // pending triangle tests that start a pooled round
 };
+
+// default of DevScene::tri_round: on the 1080p terrain (3.1 M triangles) rounds of >= 16
+// pending tests traced 5 % faster than rounds started for any test (1, 8, 16, 24 measured)
+constexpr int32_t TRI_ROUND_TESTS = 16;
 
 struct DevRender
 {

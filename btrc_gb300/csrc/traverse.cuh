@@ -399,7 +399,8 @@ template<bool ANY, bool COUNT = false, typename Fetch, typename Emit>
 __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes4, const float4 *__restrict__ tris4,
                                                 uint32_t node_count, uint32_t *cursor, uint32_t n, int refill,
                                                 uint32_t *err, Fetch fetch, Emit emit,
-                                                uint64_t *node_visits = nullptr, uint64_t *tri_tests = nullptr)
+                                                uint64_t *node_visits = nullptr, uint64_t *tri_tests = nullptr,
+                                                int min_round = 1)
 {
     // per lane: (ox, oy, oz, Sx), (Sy, Sz, kx | ky << 2 | kz << 4, tmax); per warp: the queue
     __shared__ float4 s_ray0[TRAVERSE_WARPS][32];
@@ -506,7 +507,11 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
         }
         const uint32_t total = __shfl_sync(FULL, incl, 31);
         bool found_any = false;
-        if(total != 0u)
+        // a round runs once min_round tests are pending, or when no busy lane could
+        // make progress without one (every busy lane waits on its triangles)
+        const uint32_t steppers = __ballot_sync(FULL, state == 1 && tgroup.y == 0u);
+        const bool round = total != 0u && (total >= static_cast<uint32_t>(min_round) || steppers == 0u);
+        if(round)
         {
             const uint32_t excl = incl - cnt;
             const uint32_t take = excl >= 32u ? 0u : min(cnt, 32u - excl);
