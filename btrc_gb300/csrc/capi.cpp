@@ -309,13 +309,15 @@ void build_scene(btrc_scene *sc, int threads)
         std::memcpy(&geos[g].pad, &lo, sizeof(lo));
         total += H.geometries[g].area.size();
     }
-    for(int k = 0; k < 6; ++k)
     {
-        std::vector<F4> cat;
-        cat.reserve(total);
+        // interleave the per-geometry component arrays into one record per triangle
+        std::vector<F4> rec;
+        rec.reserve(total * SHADE_F4);
         for(auto &g : H.geometries)
-            cat.insert(cat.end(), g.shade[k].begin(), g.shade[k].end());
-        D.shade[k] = dev_upload(sc->allocs, cat.data(), cat.size());
+            for(size_t i = 0; i < g.shade[0].size(); ++i)
+                for(int k = 0; k < SHADE_F4; ++k)
+                    rec.push_back(g.shade[k][i]);
+        D.shade = dev_upload(sc->allocs, rec.data(), rec.size());
     }
     std::vector<F4> lpos;
     std::vector<AliasEntry8> lalias;
@@ -328,10 +330,13 @@ void build_scene(btrc_scene *sc, int threads)
         const HostGeometry &G = H.geometries[g];
         for(size_t t = 0; t < G.area.size(); ++t)
         {
+            // the w components carry the triangle's geometric normal (shading record 2), so
+            // that a light sample reads one 48-byte record
             const V3 a = G.pos[t * 3], ba = G.pos[t * 3 + 1] - a, ca = G.pos[t * 3 + 2] - a;
-            lpos.push_back({ a.x, a.y, a.z, 0 });
-            lpos.push_back({ ba.x, ba.y, ba.z, 0 });
-            lpos.push_back({ ca.x, ca.y, ca.z, 0 });
+            const F4 gz = G.shade[2][t];
+            lpos.push_back({ a.x, a.y, a.z, gz.x });
+            lpos.push_back({ ba.x, ba.y, ba.z, gz.y });
+            lpos.push_back({ ca.x, ca.y, ca.z, gz.z });
         }
         auto tab = build_alias_table(G.area);
         lalias.insert(lalias.end(), tab.begin(), tab.end());

@@ -8,6 +8,8 @@
 
 namespace bt {
 
+constexpr int SHADE_F4 = 6;
+
 struct DevScene
 {
     const F4 *nodes;          // CWNode array viewed as float4 (5 per node)
@@ -15,12 +17,15 @@ struct DevScene
     uint32_t node_count;
     uint32_t tri_count;
 
-    const F4 *shade[6];       // per-geometry shading SoA, concatenated over geometries
+    // shading records, SHADE_F4 float4 per triangle (AoS: one hit reads 96 contiguous
+    // bytes, three 32-byte sectors), concatenated over geometries:
+    // (gx, u0) (gy, u1 - u0) (gz, u2 - u0) (n0, v0) (n1 - n0, v1 - v0) (n2 - n0, v2 - v0)
+    const F4 *shade;
     const Geometry *geometries;
     const Instance *instances;
     const Material *materials;
     const AreaLight *area_lights;
-    const F4 *light_pos;      // a, b-a, c-a per triangle of light geometries (local space)
+    const F4 *light_pos;      // a, b-a, c-a per triangle of light geometries (local space); w: geometric normal
     const AliasEntry8 *light_alias;
     int32_t num_area_lights;
     int32_t num_lights;       // area lights + environment (if any)

@@ -194,8 +194,9 @@ __device__ SurfacePoint get_hitinfo(const DevScene &S, V3 o, V3 d, const Instanc
 {
     SurfacePoint sp;
     sp.position = o + t * d;
-    const F4 gx = ldf4(S.shade[0] + idx), gy = ldf4(S.shade[1] + idx), gz = ldf4(S.shade[2] + idx);
-    const F4 sa = ldf4(S.shade[3] + idx), sba = ldf4(S.shade[4] + idx), sca = ldf4(S.shade[5] + idx);
+    const F4 *rec = S.shade + static_cast<size_t>(idx) * SHADE_F4;
+    const F4 gx = ldf4(rec + 0), gy = ldf4(rec + 1), gz = ldf4(rec + 2);
+    const F4 sa = ldf4(rec + 3), sba = ldf4(rec + 4), sca = ldf4(rec + 5);
     Frame f(v3(gx), v3(gy), v3(gz));
     f.x = normalize(aff_vector(inst.l2w, f.x));
     f.y = normalize(aff_vector(inst.l2w, f.y));
@@ -350,11 +351,12 @@ __device__ LightSample sample_light(const DevScene &S, V3 ref_pos, V3 ref_nor, b
         const uint32_t prim = alias_sample(S.light_alias + base, g.tri_count, s0);
         const float tq = sqrtf(s1);
         const float u = 1.0f - tq, v = tq * s2;
-        const V3 a = v3(S.light_pos[(base + prim) * 3 + 0]);
-        const V3 ba = v3(S.light_pos[(base + prim) * 3 + 1]);
-        const V3 ca = v3(S.light_pos[(base + prim) * 3 + 2]);
+        const F4 pa = ldf4(S.light_pos + (base + prim) * 3 + 0);
+        const F4 pb = ldf4(S.light_pos + (base + prim) * 3 + 1);
+        const F4 pc = ldf4(S.light_pos + (base + prim) * 3 + 2);
+        const V3 a = v3(pa), ba = v3(pb), ca = v3(pc);
         const V3 pos = a + ba * u + ca * v;
-        const V3 ez = normalize(v3(ldf4(S.shade[2] + g.tri_offset + prim)));
+        const V3 ez = normalize(V3(pa.w, pb.w, pc.w));
         const V3 spos = aff_point(inst.l2w, pos);
         const V3 snor = normalize(aff_normal(inst.w2l, ez));
         const V3 pos_to_ref = ref_pos - spos;
@@ -1083,7 +1085,7 @@ __global__ void __launch_bounds__(BLOCK) k_medium(DevScene S, DevRender R, PathS
             const HitDetail h = hits[i];
             const Instance &inst = S.instances[flag & INST_MASK];
             const Geometry g = S.geometries[inst.geometry];
-            const V3 ln = v3(ldf4(S.shade[2] + g.tri_offset + h.prim));
+            const V3 ln = v3(ldf4(S.shade + static_cast<size_t>(g.tri_offset + h.prim) * SHADE_F4 + 2));
             const V3 nor = aff_normal(inst.w2l, ln);
             const int inner = static_cast<int>(inst.media & 0xffffu), outer = static_cast<int>(inst.media >> 16);
             const int inct_medium = dot(d, nor) < 0 ? outer : inner;

@@ -139,12 +139,11 @@ __device__ __forceinline__ float min3f(float a, float b, float c)
     return d;
 }
 
-// Byte j of w as an exact float without the (quarter-rate) integer-to-float unit: one
-// byte permute builds 0x4B0000bb, i.e. the float 2^23 + b, and one full-rate add removes
-// 2^23. The result equals (float)b bit for bit.
-__device__ __forceinline__ float byte_f(uint32_t w, int j)
+// 1 + b 2^-15 for byte j of w: the byte in mantissa bits 8..15 of 1.0f (0x3F80bb00), one
+// byte permute and no arithmetic
+__device__ __forceinline__ float byte_mant(uint32_t w, int j)
 {
-    return __uint_as_float(__byte_perm(w, 0x4Bu, 0x4550u + static_cast<uint32_t>(j))) - 8388608.0f;
+    return __uint_as_float(__byte_perm(w, 0x3F800000u, 0x7604u + (static_cast<uint32_t>(j) << 4)));
 }
 
 // Intersects the 8 children of a node. Returns the hit mask: bits 24..31 child nodes
@@ -162,16 +161,30 @@ __device__ __forceinline__ uint32_t intersect_children(const TravRay &r, const f
     imask = ew >> 24;
     child_base = n1.x;
     tri_base = n1.y;
+    // Child plane k of an axis lies at n0 + k 2^e (k a byte, 2^e the node's grid step).
+    // With F_k = 1 + k 2^-15 (the byte placed in mantissa bits 8..15 of 1.0f: one byte
+    // permute), its distance along the ray is fma(F_k, A, C), A = 2^15 2^e / d exact and
+    // C = (n0 - o) / d - A, since F_k A = A + k 2^e / d exactly inside the fma. C carries
+    // rounding errors of up to 2^-23 (|org| + |A|); near planes use C lowered and far
+    // planes C raised by pad = 2^-20 (|org| + |A|), and far distances are widened by
+    // BOX_EPS as before, so every child box stays conservative.
     const float adjx = __uint_as_float((ew & 0xffu) << 23) * r.idx;
     const float adjy = __uint_as_float(((ew >> 8) & 0xffu) << 23) * r.idy;
     const float adjz = __uint_as_float(((ew >> 16) & 0xffu) << 23) * r.idz;
     const float orgx = (n0.x - r.ox) * r.idx;
     const float orgy = (n0.y - r.oy) * r.idy;
     const float orgz = (n0.z - r.oz) * r.idz;
+    const float Ax = adjx * 32768.0f, Ay = adjy * 32768.0f, Az = adjz * 32768.0f;
+    const float Cx = orgx - Ax, Cy = orgy - Ay, Cz = orgz - Az;
+    const float PAD = 1.0f / 1048576.0f;
+    const float padx = (fabsf(orgx) + fabsf(Ax)) * PAD;
+    const float pady = (fabsf(orgy) + fabsf(Ay)) * PAD;
+    const float padz = (fabsf(orgz) + fabsf(Az)) * PAD;
+    const float ncx = Cx - padx, ncy = Cy - pady, ncz = Cz - padz;
     // far planes use coefficients pre-scaled by BOX_EPS, so every far distance comes out
     // widened by 2^-20 relative without a multiply per child
-    const float fadjx = adjx * BOX_EPS, fadjy = adjy * BOX_EPS, fadjz = adjz * BOX_EPS;
-    const float forgx = orgx * BOX_EPS, forgy = orgy * BOX_EPS, forgz = orgz * BOX_EPS;
+    const float fAx = Ax * BOX_EPS, fAy = Ay * BOX_EPS, fAz = Az * BOX_EPS;
+    const float fcx = fmaf(Cx, BOX_EPS, padx), fcy = fmaf(Cy, BOX_EPS, pady), fcz = fmaf(Cz, BOX_EPS, padz);
     const float tcur_e = tcur * BOX_EPS;
     const bool nx = r.idx < 0.0f, ny = r.idy < 0.0f, nz = r.idz < 0.0f;
     const uint32_t oct4 = r.oct_inv * 0x01010101u;
@@ -195,12 +208,12 @@ __device__ __forceinline__ uint32_t intersect_children(const TravRay &r, const f
 #pragma unroll
         for(int j = 0; j < 4; ++j)
         {
-            const float tnx = fmaf(byte_f(xn, j), adjx, orgx);
-            const float tny = fmaf(byte_f(yn, j), adjy, orgy);
-            const float tnz = fmaf(byte_f(zn, j), adjz, orgz);
-            const float tfx = fmaf(byte_f(xf, j), fadjx, forgx);
-            const float tfy = fmaf(byte_f(yf, j), fadjy, forgy);
-            const float tfz = fmaf(byte_f(zf, j), fadjz, forgz);
+            const float tnx = fmaf(byte_mant(xn, j), Ax, ncx);
+            const float tny = fmaf(byte_mant(yn, j), Ay, ncy);
+            const float tnz = fmaf(byte_mant(zn, j), Az, ncz);
+            const float tfx = fmaf(byte_mant(xf, j), fAx, fcx);
+            const float tfy = fmaf(byte_mant(yf, j), fAy, fcy);
+            const float tfz = fmaf(byte_mant(zf, j), fAz, fcz);
             const float tmin = fmaxf(max3f(tnx, tny, tnz), 0.0f);
             const float tmax = fminf(min3f(tfx, tfy, tfz), tcur_e);
             if(tmin <= tmax)
