@@ -26,6 +26,13 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread", "-Wall", "-Wno-unused-function"]
 NVCCFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
                     "-Xptxas", "-warn-spills"]
+# The wavefront stage kernels use approximate FP32 division and square root (max 2 ulp),
+# as the reference's own kernels do (they are built with fast math); denormals and the
+# transcendental functions stay accurate. Without the IEEE slow paths at every division
+# the shade kernel's code shrinks by a third and it runs ~30 % faster. The traversal and
+# the samplers, which match the oracle bit for bit, use explicitly rounded operations.
+SHADING_SOURCES = {"integrator.cu"}
+SHADING_FLAGS = ["-prec-div=false", "-prec-sqrt=false"]
 
 
 def _run(cmd: list[str]) -> str:
@@ -67,7 +74,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     for src in cu:
         obj = OUT / (src.stem + ".cu.o")
         objs.append(obj)
-        jobs.append([NVCC] + NVCCFLAGS + inc + ["-c", str(src), "-o", str(obj)])
+        extra = SHADING_FLAGS if src.name in SHADING_SOURCES else []
+        jobs.append([NVCC] + NVCCFLAGS + extra + inc + ["-c", str(src), "-o", str(obj)])
     workers = max(1, min(len(jobs), os.cpu_count() or 4))
     with cf.ThreadPoolExecutor(workers) as ex:
         outs = list(ex.map(_run, jobs))

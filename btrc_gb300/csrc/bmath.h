@@ -54,6 +54,18 @@ BT_HD float max_comp(V3 a) { return fmaxf(a.x, fmaxf(a.y, a.z)); }
 BT_HD bool is_zero(V3 a) { return a.x == 0.0f && a.y == 0.0f && a.z == 0.0f; }
 BT_HD float saturate(float v) { return fminf(1.0f, fmaxf(0.0f, v)); }
 
+// IEEE-rounded reciprocal. The shading translation unit is compiled with approximate
+// division; code that must match the oracle bit for bit (sampler, traversal setup) uses
+// this instead of 1.0f / x.
+BT_HD float rcp_rn(float x)
+{
+#if defined(__CUDA_ARCH__)
+    return __frcp_rn(x);
+#else
+    return 1.0f / x;
+#endif
+}
+
 // sin(pi x) and cos(pi x). Every angle the tracer samples is a fraction of pi, and on
 // the device sincospif reduces such arguments exactly, so it needs none of the large-
 // argument code that sinf / cosf carry at each call site.

@@ -135,7 +135,7 @@ BT_HD uint32_t permutation_element(uint32_t i, uint32_t l, uint32_t p)
 
 BT_HD float owen_scrambled_radical_inverse(uint32_t base, uint64_t a, uint64_t hash)
 {
-    const float inv_base = 1.0f / static_cast<float>(base);
+    const float inv_base = rcp_rn(static_cast<float>(base));
     float inv_base_m = 1.0f;
     uint64_t reversed = 0;
     // digits: loop while 1 - inv_base^m is still distinguishable from 1 in FP32

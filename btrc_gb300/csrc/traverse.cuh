@@ -49,9 +49,9 @@ __device__ __forceinline__ TravRay make_trav_ray(float ox, float oy, float oz, f
     const float sx = fabsf(dx) < tiny ? copysignf(tiny, dx) : dx;
     const float sy = fabsf(dy) < tiny ? copysignf(tiny, dy) : dy;
     const float sz = fabsf(dz) < tiny ? copysignf(tiny, dz) : dz;
-    r.idx = 1.0f / sx;
-    r.idy = 1.0f / sy;
-    r.idz = 1.0f / sz;
+    r.idx = __frcp_rn(sx);
+    r.idy = __frcp_rn(sy);
+    r.idz = __frcp_rn(sz);
     const uint32_t octant = (dx < 0.0f ? 1u : 0u) | (dy < 0.0f ? 2u : 0u) | (dz < 0.0f ? 4u : 0u);
     r.oct_inv = 7u - octant;
 
