@@ -282,11 +282,11 @@ def nrc_study(B, ctx, sc, info, args):
         torch.cuda.synchronize()
         infer_ms = e0.elapsed_time(e1) / reps
         flops_fwd = 2 * (80 * 64 + 4 * 64 * 64 + 64 * 16)
-        samples = torch.cat([q[:16384], torch.rand((16384, 3), device="cuda", generator=g)], 1).contiguous()
+        train_batch = torch.cat([q[:16384], torch.rand((16384, 3), device="cuda", generator=g)], 1).contiguous()
         torch.cuda.synchronize()
         t = time.perf_counter()
         for _ in range(reps):
-            cache.train(samples, 16384)
+            cache.train(train_batch, 16384)
         train_ms = (time.perf_counter() - t) * 1000 / reps
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
         bf16_peak = peaks.get("bf16_tflops", 1900.0)
