@@ -269,16 +269,20 @@ def nrc_study(B, ctx, sc, info, args):
         q[:, 0:3] = lo + (hi - lo) * q[:, 0:3]
         q[:, 3:9] = q[:, 3:9] * 2 - 1
         pred = torch.empty((nq, 4), device="cuda")
-        sid = torch.cuda.current_stream().cuda_stream  # the events' stream
+        # a stream of our own: handle 0 would select the library context's stream, which
+        # events recorded on torch's default stream do not order against
+        ts = torch.cuda.Stream()
+        sid = ts.cuda_stream
+        torch.cuda.synchronize()
         for _ in range(3):
             cache.infer(q, nq, pred, stream=sid)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
+        e0.record(ts)
         reps = 10
         for _ in range(reps):
             cache.infer(q, nq, pred, stream=sid)
-        e1.record()
+        e1.record(ts)
         torch.cuda.synchronize()
         infer_ms = e0.elapsed_time(e1) / reps
         flops_fwd = 2 * (80 * 64 + 4 * 64 * 64 + 64 * 16)
