@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstring>
 #include <deque>
+#include <limits>
 #include <stdexcept>
 #include <thread>
 
@@ -17,6 +18,10 @@ constexpr uint32_t MAX_LEAF = 3;      // a wide-node leaf child holds up to 3 tr
 constexpr int MAX_BINARY_DEPTH = 64;  // deeper nodes fall back to median splits
 constexpr double COST_TRAVERSE = 1.0;
 constexpr double COST_INTERSECT = 1.0;
+// SAH weights of the wide collapse: a wide-node test (8 child boxes) against one triangle
+// test, in the traversal kernel's instruction counts
+constexpr float WIDE_COST_NODE = 1.0f;
+constexpr float WIDE_COST_TRI = 0.4f;
 
 struct Box
 {
@@ -260,6 +265,98 @@ CWBVH build_cwbvh(const std::vector<TriRec> &tris, int threads)
     const std::vector<BNode> &bn = bb.nodes_;
     out.binary_nodes = static_cast<int>(bn.size());
 
+    // Wide collapse by dynamic programming over the binary tree (Ylitie, Karras and
+    // Laine, "Efficient incoherent ray traversal on GPUs through compressed wide BVHs",
+    // HPG 2017, section 3): C(n, i) is the least SAH cost of the subtree of n spread over
+    // at most i child slots of a wide node; one slot holds either a leaf of <= 3
+    // triangles or a wide node whose 8 slots hold the subtree. Children have larger
+    // indices than their parents, so one reverse sweep visits the tree bottom-up.
+    const size_t N = bn.size();
+    std::vector<uint32_t> ntri(N);
+    std::vector<float> cost(N * 8);
+    std::vector<uint8_t> split(N * 8, 0);    // [n][i-1], i >= 2: left share k, 0: same as i - 1
+    std::vector<uint8_t> split8(N, 0);       // left share of the 8-slot distribution
+    std::vector<uint8_t> as_leaf(N, 0);
+    const float INF = std::numeric_limits<float>::infinity();
+    for(size_t q = N; q-- > 0;)
+    {
+        const BNode &nd = bn[q];
+        const float A = static_cast<float>(nd.box.area());
+        float *c = &cost[q * 8];
+        if(nd.left < 0)
+        {
+            ntri[q] = nd.count;
+            as_leaf[q] = 1;
+            for(int i = 0; i < 8; ++i)
+                c[i] = A * WIDE_COST_TRI * static_cast<float>(nd.count);
+            continue;
+        }
+        ntri[q] = ntri[nd.left] + ntri[nd.right];
+        const float *cl = &cost[static_cast<size_t>(nd.left) * 8], *cr = &cost[static_cast<size_t>(nd.right) * 8];
+        float dist[9];
+        uint8_t arg[9] = {};
+        for(int j = 2; j <= 8; ++j)
+        {
+            dist[j] = INF;
+            for(int k = 1; k < j; ++k)
+            {
+                const float v = cl[k - 1] + cr[j - k - 1];
+                if(v < dist[j])
+                {
+                    dist[j] = v;
+                    arg[j] = static_cast<uint8_t>(k);
+                }
+            }
+        }
+        split8[q] = arg[8];
+        const float c_internal = A * WIDE_COST_NODE + dist[8];
+        const float c_leaf = ntri[q] <= MAX_LEAF ? A * WIDE_COST_TRI * static_cast<float>(ntri[q]) : INF;
+        as_leaf[q] = c_leaf <= c_internal ? 1 : 0;
+        c[0] = std::min(c_leaf, c_internal);
+        for(int i = 2; i <= 8; ++i)
+        {
+            if(dist[i] < c[i - 2])
+            {
+                c[i - 1] = dist[i];
+                split[q * 8 + i - 1] = arg[i];
+            }
+            else
+                c[i - 1] = c[i - 2];
+        }
+    }
+    // the slots a subtree takes when it may use up to i of them
+    auto expand = [&](auto &&self, int m, int i, std::vector<int> &out) -> void {
+        while(i >= 2 && split[static_cast<size_t>(m) * 8 + i - 1] == 0)
+            --i;
+        if(i == 1)
+        {
+            out.push_back(m);
+            return;
+        }
+        const int k = split[static_cast<size_t>(m) * 8 + i - 1];
+        self(self, bn[m].left, k, out);
+        self(self, bn[m].right, i - k, out);
+    };
+    // triangles (binary-leaf ranges) of a subtree kept as one leaf slot
+    auto leaf_tris = [&](int m, std::vector<uint32_t> &out) {
+        std::vector<int> st{ m };
+        while(!st.empty())
+        {
+            const int x = st.back();
+            st.pop_back();
+            if(bn[x].left < 0)
+            {
+                for(uint32_t t = 0; t < bn[x].count; ++t)
+                    out.push_back(bb.idx_[bn[x].first + t]);
+            }
+            else
+            {
+                st.push_back(bn[x].right);
+                st.push_back(bn[x].left);
+            }
+        }
+    };
+
     struct Job { int bnode; int wnode; int depth; };
     std::deque<Job> queue;
     out.nodes.reserve(bn.size() / 4 + 1);
@@ -267,42 +364,29 @@ CWBVH build_cwbvh(const std::vector<TriRec> &tris, int threads)
     out.nodes.push_back(CWNode{});
     queue.push_back({ 0, 0, 1 });
 
+    std::vector<int> kidv;
+    std::vector<uint32_t> ltris;
     while(!queue.empty())
     {
         const Job job = queue.front();
         queue.pop_front();
         out.depth = std::max(out.depth, job.depth);
 
-        // gather up to 8 children by repeatedly opening the largest internal child
-        int kids[8];
-        int nk = 0;
+        // the wide node's children: the 8-slot distribution of the binary node's subtree
+        kidv.clear();
         const BNode &root = bn[job.bnode];
         if(root.left < 0)
-            kids[nk++] = job.bnode;
+            kidv.push_back(job.bnode);
         else
         {
-            kids[nk++] = root.left;
-            kids[nk++] = root.right;
-            while(nk < 8)
-            {
-                int best = -1;
-                double best_area = -1;
-                for(int k = 0; k < nk; ++k)
-                {
-                    const BNode &c = bn[kids[k]];
-                    if(c.left >= 0 && c.box.area() > best_area)
-                    {
-                        best_area = c.box.area();
-                        best = k;
-                    }
-                }
-                if(best < 0)
-                    break;
-                const BNode &c = bn[kids[best]];
-                kids[best] = c.left;
-                kids[nk++] = c.right;
-            }
+            const int k = split8[job.bnode];
+            expand(expand, root.left, k, kidv);
+            expand(expand, root.right, 8 - k, kidv);
         }
+        int kids[8];
+        const int nk = static_cast<int>(kidv.size());
+        for(int k = 0; k < nk; ++k)
+            kids[k] = kidv[k];
 
         // node origin and quantisation grid
         Box nbox;
@@ -366,7 +450,7 @@ CWBVH build_cwbvh(const std::vector<TriRec> &tris, int threads)
         // triangles are appended contiguously
         int n_internal = 0;
         for(int s = 0; s < 8; ++s)
-            if(kid_in_slot[s] >= 0 && bn[kids[kid_in_slot[s]]].left >= 0)
+            if(kid_in_slot[s] >= 0 && !as_leaf[kids[kid_in_slot[s]]])
                 ++n_internal;
         node.child_base = static_cast<uint32_t>(out.nodes.size());
         node.tri_base = static_cast<uint32_t>(out.tris.size());
@@ -399,7 +483,7 @@ CWBVH build_cwbvh(const std::vector<TriRec> &tris, int threads)
             }
             node.qlo_x[s] = ql[0]; node.qlo_y[s] = ql[1]; node.qlo_z[s] = ql[2];
             node.qhi_x[s] = qh[0]; node.qhi_y[s] = qh[1]; node.qhi_z[s] = qh[2];
-            if(c.left >= 0)
+            if(!as_leaf[kids[k]])
             {
                 node.imask |= static_cast<uint8_t>(1u << s);
                 node.meta[s] = static_cast<uint8_t>((1u << 5) | (24u + s));
@@ -409,10 +493,13 @@ CWBVH build_cwbvh(const std::vector<TriRec> &tris, int threads)
             else
             {
                 static const uint8_t unary[4] = { 0, 1, 3, 7 };
-                node.meta[s] = static_cast<uint8_t>((unary[c.count] << 5) | tri_off);
-                for(uint32_t t = 0; t < c.count; ++t)
-                    out.tris.push_back(tris[bb.idx_[c.first + t]]);
-                tri_off += c.count;
+                ltris.clear();
+                leaf_tris(kids[k], ltris);
+                const uint32_t cnt = static_cast<uint32_t>(ltris.size());
+                node.meta[s] = static_cast<uint8_t>((unary[cnt] << 5) | tri_off);
+                for(uint32_t t : ltris)
+                    out.tris.push_back(tris[t]);
+                tri_off += cnt;
             }
         }
         (void)slot_of;
