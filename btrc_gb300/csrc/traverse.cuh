@@ -508,24 +508,24 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
             }
         }
 
-        // triangle round (all lanes): queue positions by a warp prefix sum of the counts
+        // triangle round (all lanes). A round runs once min_round tests are pending, or
+        // when no busy lane could make progress without one (every busy lane waits on
+        // its triangles); queue positions come from a warp prefix sum of the counts.
         const uint32_t cnt = static_cast<uint32_t>(__popc(tgroup.y));
-        uint32_t incl = cnt;
-#pragma unroll
-        for(int off = 1; off < 32; off <<= 1)
-        {
-            const uint32_t v = __shfl_up_sync(FULL, incl, off);
-            if(lane >= static_cast<uint32_t>(off))
-                incl += v;
-        }
-        const uint32_t total = __shfl_sync(FULL, incl, 31);
+        const uint32_t total = __reduce_add_sync(FULL, cnt);
         bool found_any = false;
-        // a round runs once min_round tests are pending, or when no busy lane could
-        // make progress without one (every busy lane waits on its triangles)
         const uint32_t steppers = __ballot_sync(FULL, state == 1 && tgroup.y == 0u);
         const bool round = total != 0u && (total >= static_cast<uint32_t>(min_round) || steppers == 0u);
         if(round)
         {
+            uint32_t incl = cnt;
+#pragma unroll
+            for(int off = 1; off < 32; off <<= 1)
+            {
+                const uint32_t v = __shfl_up_sync(FULL, incl, off);
+                if(lane >= static_cast<uint32_t>(off))
+                    incl += v;
+            }
             const uint32_t excl = incl - cnt;
             const uint32_t take = excl >= 32u ? 0u : min(cnt, 32u - excl);
             if(take != 0u)
@@ -569,31 +569,76 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
                     hprim = __float_as_uint(b.w);
                 }
             }
-            // owners merge their entries [excl, excl + take)
+            // owners merge their entries [excl, excl + take): the smallest t by shuffling
+            // t alone, then the winner's record; equal t within one owner's entries (a ray
+            // through a shared edge) takes the exact (t, instance, primitive) order
             const uint32_t rounds = __reduce_max_sync(FULL, take);
-            for(uint32_t k = 0; k < rounds; ++k)
+            if(ANY)
             {
-                const int src = static_cast<int>(min(excl + k, 31u));
-                const float ct = __shfl_sync(FULL, ht, src);
-                if(ANY)
+                for(uint32_t k = 0; k < rounds; ++k)
                 {
+                    const float ct = __shfl_sync(FULL, ht, static_cast<int>(min(excl + k, 31u)));
                     if(k < take && ct != NO_HIT)
                         found_any = true;
                 }
-                else
+            }
+            else
+            {
+                float mt = NO_HIT;
+                uint32_t msrc = lane;
+                bool tie = false;
+                for(uint32_t k = 0; k < rounds; ++k)
                 {
-                    const float cb1 = __shfl_sync(FULL, hb1, src);
-                    const float cb2 = __shfl_sync(FULL, hb2, src);
-                    const uint32_t ci = __shfl_sync(FULL, hinst, src);
-                    const uint32_t cp = __shfl_sync(FULL, hprim, src);
-                    if(k < take && ct != NO_HIT && (!best.hit || closer(ct, ci, cp, best.t, best.inst, best.prim)))
+                    const uint32_t src = min(excl + k, 31u);
+                    const float ct = __shfl_sync(FULL, ht, static_cast<int>(src));
+                    if(k < take && ct != NO_HIT)
+                    {
+                        if(ct < mt)
+                        {
+                            mt = ct;
+                            msrc = src;
+                            tie = false;
+                        }
+                        else if(ct == mt)
+                            tie = true;
+                    }
+                }
+                if(__ballot_sync(FULL, tie) == 0u)
+                {
+                    const float cb1 = __shfl_sync(FULL, hb1, static_cast<int>(msrc));
+                    const float cb2 = __shfl_sync(FULL, hb2, static_cast<int>(msrc));
+                    const uint32_t ci = __shfl_sync(FULL, hinst, static_cast<int>(msrc));
+                    const uint32_t cp = __shfl_sync(FULL, hprim, static_cast<int>(msrc));
+                    if(mt != NO_HIT && (!best.hit || closer(mt, ci, cp, best.t, best.inst, best.prim)))
                     {
                         best.hit = true;
-                        best.t = ct;
+                        best.t = mt;
                         best.b1 = cb1;
                         best.b2 = cb2;
                         best.inst = ci;
                         best.prim = cp;
+                    }
+                }
+                else
+                {
+                    for(uint32_t k = 0; k < rounds; ++k)
+                    {
+                        const int src = static_cast<int>(min(excl + k, 31u));
+                        const float ct = __shfl_sync(FULL, ht, src);
+                        const float cb1 = __shfl_sync(FULL, hb1, src);
+                        const float cb2 = __shfl_sync(FULL, hb2, src);
+                        const uint32_t ci = __shfl_sync(FULL, hinst, src);
+                        const uint32_t cp = __shfl_sync(FULL, hprim, src);
+                        if(k < take && ct != NO_HIT &&
+                           (!best.hit || closer(ct, ci, cp, best.t, best.inst, best.prim)))
+                        {
+                            best.hit = true;
+                            best.t = ct;
+                            best.b1 = cb1;
+                            best.b2 = cb2;
+                            best.inst = ci;
+                            best.prim = cp;
+                        }
                     }
                 }
             }
