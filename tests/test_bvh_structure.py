@@ -171,3 +171,24 @@ def test_emulated_traversal_visits_the_oracle_hit(native_lib, scene_dir):
             got = {(int(tu[c, 3]), int(tu[c, 7])) for c in cand}
             assert (int(want[0]), int(want[1])) in got
         assert visited <= len(nodes)
+
+
+def test_wide_collapse_fills_nodes(native_lib, scene_dir):
+    """The dynamic-programming collapse keeps the 8-wide nodes full: on a small terrain
+    (128^2 vertices + 8 instanced spheres) most slots hold a child, few nodes hold only two,
+    and the tree stays within the traversal stack."""
+    path = scenes.terrain(seed=7, width=64, height=64, spp=1, grid=128, instances=8, out_dir=scene_dir / "terrain")
+    ctx, sc = _host_scene(path)
+    nodes, tris = sc.export_bvh()
+    meta = nodes[:, 24:32]
+    occupied = (meta != 0).sum(1)
+    assert occupied.mean() > 5.5, occupied.mean()
+    assert (occupied == 2).mean() < 0.15, np.bincount(occupied, minlength=9)
+    assert sc.info().bvh_depth <= STACK
+    # leaf slots hold 1..3 triangles and every triangle sits in exactly one of them
+    leaf = (meta != 0) & ((meta & 0x18) != 0x18)
+    count = np.zeros(meta.shape, np.int64)
+    for b in range(3):
+        count += ((meta >> (5 + b)) & 1).astype(np.int64) * leaf
+    assert count[leaf].min() >= 1 and count[leaf].max() <= 3
+    assert count.sum() == len(tris)
