@@ -23,6 +23,10 @@
 namespace bt {
 
 __constant__ uint32_t c_primes[PRIME_COUNT];
+// per Halton dimension: ceil(2^64 / prime) for exact division by a multiply, and the
+// dimension's scrambling seed mix_bits(1 + (dim << 4))
+__constant__ uint64_t c_prime_magic[PRIME_COUNT];
+__constant__ uint64_t c_dim_hash[PRIME_COUNT];
 
 namespace {
 
@@ -104,7 +108,7 @@ struct DSampler
 
     __device__ __forceinline__ float halton(uint32_t dim) const
     {
-        return owen_scrambled_radical_inverse(c_primes[dim], s.a, mix_bits(static_cast<uint64_t>(1u + (dim << 4))));
+        return owen_scrambled_radical_inverse(c_primes[dim], s.a, c_dim_hash[dim], c_prime_magic[dim]);
     }
     __device__ __forceinline__ float get1d()
     {
@@ -1604,7 +1608,18 @@ cudaError_t upload_primes()
         if(is_prime)
             primes.push_back(v);
     }
-    return cudaMemcpyToSymbol(c_primes, primes.data(), sizeof(uint32_t) * PRIME_COUNT);
+    std::vector<uint64_t> magic(PRIME_COUNT), hash(PRIME_COUNT);
+    for(uint32_t d = 0; d < PRIME_COUNT; ++d)
+    {
+        magic[d] = UINT64_MAX / primes[d] + 1ull;
+        hash[d] = mix_bits(static_cast<uint64_t>(1u + (d << 4)));
+    }
+    cudaError_t e = cudaMemcpyToSymbol(c_primes, primes.data(), sizeof(uint32_t) * PRIME_COUNT);
+    if(e == cudaSuccess)
+        e = cudaMemcpyToSymbol(c_prime_magic, magic.data(), sizeof(uint64_t) * PRIME_COUNT);
+    if(e == cudaSuccess)
+        e = cudaMemcpyToSymbol(c_dim_hash, hash.data(), sizeof(uint64_t) * PRIME_COUNT);
+    return e;
 }
 
 cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffers &B, cudaStream_t st,

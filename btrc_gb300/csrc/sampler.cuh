@@ -101,7 +101,21 @@ BT_HD uint64_t mix_bits(uint64_t v)
     return v;
 }
 
-BT_HD uint32_t permutation_element(uint32_t i, uint32_t l, uint32_t p)
+// n / d for n < 2^32 and 2 <= d < 2^32 by one 64x64 high multiply with
+// magic = (2^64 - 1) / d + 1 = ceil(2^64 / d): n * magic / 2^64 exceeds n / d by less than
+// n / 2^64 < 1 / d, so the floor is exact. magic == 0 divides directly.
+BT_HD uint32_t udiv_magic(uint32_t n, uint32_t d, uint64_t magic)
+{
+#if defined(__CUDA_ARCH__)
+    if(magic != 0ull)
+        return static_cast<uint32_t>(__umul64hi(static_cast<uint64_t>(n), magic));
+#else
+    (void)magic;
+#endif
+    return n / d;
+}
+
+BT_HD uint32_t permutation_element(uint32_t i, uint32_t l, uint32_t p, uint64_t magic = 0ull)
 {
     uint32_t w = l - 1;
     w |= w >> 1;
@@ -130,10 +144,11 @@ BT_HD uint32_t permutation_element(uint32_t i, uint32_t l, uint32_t p)
         i &= w;
         i ^= i >> 5;
     } while(i >= l);
-    return (i + p) % l;
+    const uint32_t x = i + p;
+    return x - udiv_magic(x, l, magic) * l;
 }
 
-BT_HD float owen_scrambled_radical_inverse(uint32_t base, uint64_t a, uint64_t hash)
+BT_HD float owen_scrambled_radical_inverse(uint32_t base, uint64_t a, uint64_t hash, uint64_t magic = 0ull)
 {
     const float inv_base = rcp_rn(static_cast<float>(base));
     float inv_base_m = 1.0f;
@@ -145,7 +160,7 @@ BT_HD float owen_scrambled_radical_inverse(uint32_t base, uint64_t a, uint64_t h
         if(a < 0x100000000ull)
         {
             const uint32_t a32 = static_cast<uint32_t>(a);
-            next = a32 / base;
+            next = udiv_magic(a32, base, magic);
             digit = a32 - static_cast<uint32_t>(next) * base;
         }
         else
@@ -154,7 +169,7 @@ BT_HD float owen_scrambled_radical_inverse(uint32_t base, uint64_t a, uint64_t h
             digit = a - next * base;
         }
         const uint64_t digit_hash = mix_bits(hash ^ reversed);
-        digit = permutation_element(static_cast<uint32_t>(digit), base, static_cast<uint32_t>(digit_hash));
+        digit = permutation_element(static_cast<uint32_t>(digit), base, static_cast<uint32_t>(digit_hash), magic);
         reversed = reversed * base + digit;
         inv_base_m = inv_base_m * inv_base;
         a = next;
