@@ -93,3 +93,29 @@ def test_procedural_geometry_scene(gpu_ctx, tmp_path):
     assert stats["traversal_errors"] == 0
     err = rel_mse(g, o)
     assert err < 1e-3, err
+
+
+def test_tile_generation_matches_uniform(gpu_ctx, scene_dir):
+    # renderer.tile (W/generate.cpp:56-60) orders the (pixel, sample) pairs pixel-major
+    # instead of sample-major; every pair keeps its own sampler stream, so the two modes
+    # trace the same paths and the images differ only by the order of the film atomics.
+    # The state queue is smaller than the frame so that both orders need several refills.
+    import json
+    p = scenes.cornell(out_dir=scene_dir / "cornell", width=40, height=40, spp=64)
+    scene = json.loads(p.read_text())
+    scene["renderer"]["state_count"] = 8192
+    uni = p.parent / "tile-off.json"
+    uni.write_text(json.dumps(scene))
+    scene["renderer"]["tile"] = True
+    til = p.parent / "tile-on.json"
+    til.write_text(json.dumps(scene))
+    imgs = []
+    for q in (uni, til):
+        sc = gpu_ctx.load_scene(q).build()
+        stats = {}
+        imgs.append(gpu_ctx.render(sc, stats=stats).astype(np.float64))
+        assert stats["paths"] == 40 * 40 * 64 and stats["traversal_errors"] == 0
+        sc.close()
+    a, b = imgs
+    assert np.isfinite(a).all() and np.isfinite(b).all()
+    assert np.allclose(a, b, rtol=1e-4, atol=1e-6), np.abs(a - b).max()

@@ -95,3 +95,22 @@ def test_invalid_arguments(gpu_ctx, scene_dir):
     with pytest.raises(B.BtrcError) as e:
         gpu_ctx.trace_closest(sc, 1, 1, 1, 1)  # not built
     assert e.value.status == 1
+
+
+def test_closest_bitexact_small_terrain(gpu_ctx, scene_dir):
+    # a 128^2 heightfield with 8 instanced spheres (~73 K triangles): the 8-wide nodes of
+    # the dynamic-programming collapse are mostly full, leaves hold 1-3 triangles, and rays
+    # from above graze the surface at every angle
+    p = scenes.terrain(seed=7, width=64, height=64, spp=1, grid=128, instances=8, out_dir=scene_dir / "terrain")
+    rng = np.random.default_rng(14)
+    S = OS.Scene(p)
+    n = 100000
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0:3] = rng.uniform([-1.2, 0.3, -1.2], [1.2, 1.5, 1.2], (n, 3))
+    d = rng.normal(size=(n, 3))
+    d[:, 1] = -np.abs(d[:, 1]) * rng.uniform(0.05, 1.0, n)
+    rays[:, 4:7] = d
+    rays[:, 7] = 3.0e38
+    rays = np.concatenate([rays, edge_rays(rng, S.tris, 50000)])
+    _, hit_rate = _compare(gpu_ctx, p, rays)
+    assert hit_rate > 0.5
