@@ -437,10 +437,13 @@ void alloc_render_buffers(RenderBuffers &B, std::vector<void *> &allocs, uint32_
         B.path[k].ray_d = static_cast<F4 *>(A(sizeof(F4) * capacity));
         B.path[k].bsdf_le = static_cast<F4 *>(A(sizeof(F4) * capacity));
     }
-    B.shadow.o = static_cast<F4 *>(A(sizeof(F4) * capacity));
-    B.shadow.d = static_cast<F4 *>(A(sizeof(F4) * capacity));
-    B.shadow.beta = static_cast<F4 *>(A(sizeof(F4) * capacity));
-    B.shadow.sampler = static_cast<SamplerState *>(A(sizeof(SamplerState) * capacity));
+    for(int k = 0; k < 2; ++k)
+    {
+        B.shadow[k].o = static_cast<F4 *>(A(sizeof(F4) * capacity));
+        B.shadow[k].d = static_cast<F4 *>(A(sizeof(F4) * capacity));
+        B.shadow[k].beta = static_cast<F4 *>(A(sizeof(F4) * capacity));
+        B.shadow[k].sampler = static_cast<SamplerState *>(A(sizeof(SamplerState) * capacity));
+    }
     B.hit_flag = static_cast<uint32_t *>(A(sizeof(uint32_t) * capacity));
     B.hit_detail = static_cast<HitDetail *>(A(sizeof(HitDetail) * capacity));
     B.order = static_cast<uint32_t *>(A(sizeof(uint32_t) * capacity));

@@ -81,25 +81,26 @@ struct DevRender
     uint32_t nrc_cap;
 };
 
-// Queue counters, resident in device memory for the whole render.
+// Queue counters, resident in device memory for the whole render. Shadow records are
+// double-buffered by bounce parity (bounce b appends to queue b & 1), so that the shadow
+// kernel of one bounce may run beside the next bounce's kernels.
 struct Counters
 {
     uint32_t active;       // states in the current queue (survivors + new)
     uint32_t slot_base;    // first slot written by generate this iteration
     uint32_t n_new;        // paths generated this iteration
     uint32_t next_active;  // survivors appended by shade/medium
-    uint32_t shadow;       // shadow records appended this iteration
+    uint32_t shadow_n[2];  // shadow records of the last bounce of each parity
     uint32_t err;          // traversal stack overflow flag
     uint32_t iterations;
-    uint32_t pad;
     uint64_t generated;    // total camera paths generated
     uint64_t gen_base;     // global path index of slot_base
     uint64_t ext_rays;     // extension rays traced
-    uint64_t shadow_rays;  // shadow rays traced
+    uint64_t shadow_rays;  // shadow records of bounces whose queue was reused since
     uint64_t node_visits;  // closest-hit node visits (counting mode only)
     uint64_t tri_tests;    // closest-hit triangle tests (counting mode only)
-    uint32_t trace_cursor;   // next ray for the warp-refill traversal (reset every bounce)
-    uint32_t shadow_cursor;
+    uint32_t trace_cursor;      // next ray for the warp-refill traversal (reset every bounce)
+    uint32_t shadow_cursor[2];  // per shadow queue
     uint32_t hit_count;      // closest-hit results partitioned into the shade order
     uint32_t miss_count;     // (hits from the front, misses from the back)
 };

@@ -871,29 +871,31 @@ __device__ __forceinline__ float henyey_greenstein(float g, float u)
 
 // ---------------------------------------------------------------- kernels
 
-__global__ void k_control(Counters *c, uint32_t capacity, uint64_t total)
+// Starts a bounce of the given parity. Writes its fields one by one: the shadow kernel of
+// the previous bounce (other parity) may still be running and updating its own cursor.
+__global__ void k_control(Counters *c, uint32_t capacity, uint64_t total, int parity)
 {
-    Counters k = *c;
-    k.shadow_rays += k.shadow;
-    const uint32_t survivors = k.next_active;
-    const uint64_t remaining = total - k.generated;
+    const uint32_t survivors = c->next_active;
+    const uint64_t generated = c->generated;
+    const uint64_t remaining = total - generated;
     const uint64_t room = capacity - survivors;
     const uint32_t n_new = static_cast<uint32_t>(remaining < room ? remaining : room);
-    k.slot_base = survivors;
-    k.n_new = n_new;
-    k.gen_base = k.generated;
-    k.generated += n_new;
-    k.active = survivors + n_new;
-    k.ext_rays += k.active;
-    k.next_active = 0;
-    k.shadow = 0;
-    k.trace_cursor = 0;
-    k.shadow_cursor = 0;
-    k.hit_count = 0;
-    k.miss_count = 0;
-    if(k.active > 0)
-        ++k.iterations;
-    *c = k;
+    const uint32_t active = survivors + n_new;
+    c->shadow_rays += c->shadow_n[parity];
+    c->shadow_n[parity] = 0;
+    c->shadow_cursor[parity] = 0;
+    c->slot_base = survivors;
+    c->n_new = n_new;
+    c->gen_base = generated;
+    c->generated = generated + n_new;
+    c->active = active;
+    c->ext_rays += active;
+    c->next_active = 0;
+    c->trace_cursor = 0;
+    c->hit_count = 0;
+    c->miss_count = 0;
+    if(active > 0)
+        ++c->iterations;
 }
 
 __global__ void __launch_bounds__(BLOCK) k_generate(DevRender R, PathSoA P, float4 *film, const Counters *cnt,
@@ -1071,7 +1073,7 @@ __global__ void __launch_bounds__(BLOCK) k_order(const uint32_t *__restrict__ fl
 }
 
 // MediumPipeline (builtin/btrc/builtin/renderer/wavefront/medium.cpp:28-249)
-__global__ void __launch_bounds__(BLOCK) k_medium(DevScene S, DevRender R, PathSoA P, PathSoA N, ShadowSoA SH,
+__global__ void __launch_bounds__(BLOCK) k_medium(DevScene S, DevRender R, PathSoA P, PathSoA N, ShadowSoA SH, int shq,
                                                   uint32_t *flags, const HitDetail *hits, float4 *film, Counters *cnt)
 {
     const uint32_t n = cnt->active;
@@ -1166,7 +1168,7 @@ __global__ void __launch_bounds__(BLOCK) k_medium(DevScene S, DevRender R, PathS
         (void)s2;
         if(ls.success)
         {
-            const uint32_t k = queue_append(&cnt->shadow);
+            const uint32_t k = queue_append(&cnt->shadow_n[shq]);
             const int smed = ls.t1 > 1 ? S.vacuum_medium : medium_id;
             SH.o[k] = f4(ls.o, __uint_as_float(pixel));
             SH.d[k] = f4(ls.d, ls.t1);
@@ -1278,7 +1280,7 @@ __device__ __forceinline__ bool nrc_query_at(const DevScene &S, const SurfacePoi
 // the kernel waits on scattered loads, and the occupancy pays for the few spills.
 template<bool TEX, bool NRC = false>
 __global__ void __launch_bounds__(BLOCK, 2) k_shade(DevScene S, DevRender R, PathSoA P, PathSoA N, ShadowSoA SH,
-                                                 const uint32_t *flags, const HitDetail *hits,
+                                                    int shq, const uint32_t *flags, const HitDetail *hits,
                                                  const uint32_t *order, float4 *film, Counters *cnt)
 {
     const uint32_t n = cnt->active;
@@ -1397,7 +1399,7 @@ __global__ void __launch_bounds__(BLOCK, 2) k_shade(DevScene S, DevRender R, Pat
             const int smed = shadow_out == last_out ? __float_as_int(ro.w) : (shadow_out ? outer : inner);
             const float c = fabsf(dot(normalize(ls.d), sp.frame.z));
             const V3 beta_li = ls.li * beta * shadow_f * c / (shadow_pdf + ls.light_pdf);
-            const uint32_t k = queue_append(&cnt->shadow);
+            const uint32_t k = queue_append(&cnt->shadow_n[shq]);
             SH.o[k] = f4(ls.o, __uint_as_float(pixel));
             SH.d[k] = f4(ls.d, ls.t1);
             SH.beta[k] = f4(beta_li, __int_as_float(smed));
@@ -1433,8 +1435,8 @@ __global__ void __launch_bounds__(BLOCK, 2) k_shade(DevScene S, DevRender R, Pat
     }
 }
 
-using ShadeKernel = void (*)(DevScene, DevRender, PathSoA, PathSoA, ShadowSoA, const uint32_t *, const HitDetail *,
-                             const uint32_t *, float4 *, Counters *);
+using ShadeKernel = void (*)(DevScene, DevRender, PathSoA, PathSoA, ShadowSoA, int, const uint32_t *,
+                             const HitDetail *, const uint32_t *, float4 *, Counters *);
 
 // the shade kernel variant for a scene and render: textured materials, cache termination
 ShadeKernel shade_kernel(const DevScene &S, const DevRender &R)
@@ -1450,12 +1452,13 @@ ShadeKernel shade_kernel(const DevScene &S, const DevRender &R)
 // MEDIA = false compiles the transmittance code out, so the traversal of scenes without
 // media keeps its registers
 template<bool MEDIA>
-__global__ void __launch_bounds__(TRAVERSE_BLOCK) k_shadow(DevScene S, DevRender R, ShadowSoA SH, float4 *film, Counters *cnt)
+__global__ void __launch_bounds__(TRAVERSE_BLOCK) k_shadow(DevScene S, DevRender R, ShadowSoA SH, float4 *film,
+                                                           Counters *cnt, int shq)
 {
-    const uint32_t n = cnt->shadow;
+    const uint32_t n = cnt->shadow_n[shq];
     traverse_refill<true>(
         reinterpret_cast<const float4 *>(S.nodes), reinterpret_cast<const float4 *>(S.tris), S.node_count,
-        &cnt->shadow_cursor, n, REFILL_LANES, &cnt->err,
+        &cnt->shadow_cursor[shq], n, REFILL_LANES, &cnt->err,
         [&](uint32_t i, float *o, float *d, float &t1) {
             const F4 so = SH.o[i], sd = SH.d[i];
             o[0] = so.x; o[1] = so.y; o[2] = so.z;
@@ -1553,12 +1556,25 @@ void timed(StageTimer *T, int stage, cudaStream_t st, uint64_t *launches, Launch
     T->marks.push_back({ stage, { a, b } });
 }
 
+void launch_shadow(const DevScene &S, const DevRender &R, RenderBuffers &B, int parity, cudaStream_t st, int grid)
+{
+    if(S.has_media)
+        k_shadow<true><<<grid, TRAVERSE_BLOCK, 0, st>>>(S, R, B.shadow[parity], B.film, B.counters, parity);
+    else
+        k_shadow<false><<<grid, TRAVERSE_BLOCK, 0, st>>>(S, R, B.shadow[parity], B.film, B.counters, parity);
+}
+
+// One bounce of the given parity. With defer_shadow the caller launches its shadow kernel
+// (on another stream, beside the next bounce).
 cudaError_t enqueue_bounce(const DevScene &S, const DevRender &R, RenderBuffers &B, int parity, cudaStream_t st,
-                           const int grids[6], int profile, StageTimer *T, uint64_t *launches)
+                           const int grids[6], int profile, StageTimer *T, uint64_t *launches,
+                           bool defer_shadow = false)
 {
     PathSoA &P = B.path[parity];
     PathSoA &N = B.path[1 - parity];
-    timed(T, STAGE_CONTROL, st, launches, [&] { k_control<<<1, 1, 0, st>>>(B.counters, B.capacity, R.total_paths); });
+    ShadowSoA &SH = B.shadow[parity];
+    timed(T, STAGE_CONTROL, st, launches,
+          [&] { k_control<<<1, 1, 0, st>>>(B.counters, B.capacity, R.total_paths, parity); });
     timed(T, STAGE_GENERATE, st, launches,
           [&] { k_generate<<<grids[0], BLOCK, 0, st>>>(R, P, B.film, B.counters, S.vacuum_medium); });
     timed(T, STAGE_TRACE, st, launches, [&] {
@@ -1569,21 +1585,17 @@ cudaError_t enqueue_bounce(const DevScene &S, const DevRender &R, RenderBuffers 
     });
     if(S.has_media)
         timed(T, STAGE_MEDIUM, st, launches, [&] {
-            k_medium<<<grids[2], BLOCK, 0, st>>>(S, R, P, N, B.shadow, B.hit_flag, B.hit_detail, B.film, B.counters);
+            k_medium<<<grids[2], BLOCK, 0, st>>>(S, R, P, N, SH, parity, B.hit_flag, B.hit_detail, B.film,
+                                                 B.counters);
         });
     timed(T, STAGE_SHADE, st, launches,
           [&] { k_order<<<grids[5], BLOCK, 0, st>>>(B.hit_flag, B.order, B.counters); });
     timed(T, STAGE_SHADE, st, launches, [&] {
-        shade_kernel(S, R)<<<grids[3], BLOCK, 0, st>>>(S, R, P, N, B.shadow, B.hit_flag, B.hit_detail, B.order,
+        shade_kernel(S, R)<<<grids[3], BLOCK, 0, st>>>(S, R, P, N, SH, parity, B.hit_flag, B.hit_detail, B.order,
                                                        B.film, B.counters);
     });
-    timed(T, STAGE_SHADOW, st, launches,
-          [&] {
-              if(S.has_media)
-                  k_shadow<true><<<grids[4], TRAVERSE_BLOCK, 0, st>>>(S, R, B.shadow, B.film, B.counters);
-              else
-                  k_shadow<false><<<grids[4], TRAVERSE_BLOCK, 0, st>>>(S, R, B.shadow, B.film, B.counters);
-          });
+    if(!defer_shadow)
+        timed(T, STAGE_SHADOW, st, launches, [&] { launch_shadow(S, R, B, parity, st, grids[4]); });
     return cudaGetLastError();
 }
 
@@ -1652,23 +1664,61 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
         persistent_grid(BLOCK, reinterpret_cast<const void *>(k_order), R.grid_pct),
     };
 
+    // Graph of two bounces. Each bounce's shadow kernel runs on a second stream beside the
+    // next bounce: the odd bounce's shadow rays are traced at the start of the following
+    // launch, beside its even bounce, and once more after the last launch. A bounce that
+    // reuses a shadow queue (its control kernel resets the queue's counters) waits for the
+    // shadow kernel that reads it.
     cudaGraphExec_t exec = nullptr;
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, odd_done = nullptr, even_shaded = nullptr, even_done = nullptr;
+    auto release = [&] {
+        if(exec)
+            cudaGraphExecDestroy(exec);
+        for(cudaEvent_t ev : { fork, odd_done, even_shaded, even_done })
+            if(ev)
+                cudaEventDestroy(ev);
+        if(side)
+            cudaStreamDestroy(side);
+    };
     if(use_graphs)
     {
-        cudaGraph_t graph = nullptr;
-        e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+        e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
+        for(cudaEvent_t *ev : { &fork, &odd_done, &even_shaded, &even_done })
+            if(e == cudaSuccess)
+                e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+        if(e == cudaSuccess)
+            e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
         if(e != cudaSuccess)
+        {
+            release();
             return e;
+        }
         uint64_t dummy[STAGE_COUNT] = {};
-        enqueue_bounce(S, R, B, 0, st, grids, 0, nullptr, dummy);
-        enqueue_bounce(S, R, B, 1, st, grids, 0, nullptr, dummy);
+        cudaEventRecord(fork, st);
+        cudaStreamWaitEvent(side, fork, 0);
+        launch_shadow(S, R, B, 1, side, grids[4]);
+        cudaEventRecord(odd_done, side);
+        enqueue_bounce(S, R, B, 0, st, grids, 0, nullptr, dummy, true);
+        cudaEventRecord(even_shaded, st);
+        cudaStreamWaitEvent(side, even_shaded, 0);
+        launch_shadow(S, R, B, 0, side, grids[4]);
+        cudaEventRecord(even_done, side);
+        cudaStreamWaitEvent(st, odd_done, 0);
+        enqueue_bounce(S, R, B, 1, st, grids, 0, nullptr, dummy, true);
+        cudaStreamWaitEvent(st, even_done, 0);
+        cudaGraph_t graph = nullptr;
         e = cudaStreamEndCapture(st, &graph);
+        if(e == cudaSuccess)
+        {
+            e = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+        }
         if(e != cudaSuccess)
+        {
+            release();
             return e;
-        e = cudaGraphInstantiate(&exec, graph, 0);
-        cudaGraphDestroy(graph);
-        if(e != cudaSuccess)
-            return e;
+        }
     }
 
     cudaEvent_t ev[RING_SLOTS];
@@ -1723,6 +1773,12 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
         cudaEventRecord(ev[slot], st);
         ++launches_total;
     }
+    // the last launch's odd-bounce shadow rays
+    if(use_graphs && e == cudaSuccess)
+    {
+        launch_shadow(S, R, B, 1, st, grids[4]);
+        e = cudaGetLastError();
+    }
     cudaEventRecord(t1, st);
     cudaError_t se = cudaEventSynchronize(t1);
     if(e == cudaSuccess)
@@ -1735,14 +1791,13 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
         cudaEventDestroy(ev[k]);
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
-    if(exec)
-        cudaGraphExecDestroy(exec);
+    release();
     if(stats)
     {
         *stats = RenderStats{};
         stats->paths = fin.generated;
         stats->ext_rays = fin.ext_rays;
-        stats->shadow_rays = fin.shadow_rays + fin.shadow;
+        stats->shadow_rays = fin.shadow_rays + fin.shadow_n[0] + fin.shadow_n[1];
         stats->iterations = fin.iterations;
         stats->err = fin.err;
         stats->device_ms = ms;
@@ -1757,8 +1812,9 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
             for(int k = 0; k < STAGE_COUNT; ++k)
                 stats->stage_launches[k] = (k == STAGE_MEDIUM && !S.has_media) ? 0
                                            : k == STAGE_SHADE                    ? graph_launches * 4
+                                           : k == STAGE_SHADOW                   ? graph_launches * 2 + 1
                                                                                  : graph_launches * 2;
-            stats->kernel_launches = graph_launches * 2 * per_bounce;
+            stats->kernel_launches = graph_launches * 2 * per_bounce + 1;
         }
         else
         {
@@ -2034,11 +2090,11 @@ constexpr uint32_t NOALLOC_MAX_PIXELS = 512 * 512;
 constexpr size_t NOALLOC_PATH_BYTES = 6 * 16;    // one PathSoA slot
 constexpr size_t NOALLOC_BYTES =
     2 * NOALLOC_PATH_BYTES * NOALLOC_MAX_STATES      // current + next queues
-    + 4 * 16 * NOALLOC_MAX_STATES                     // shadow queue (o, d, beta, sampler)
+    + 2 * 4 * 16 * NOALLOC_MAX_STATES                 // two shadow queues (o, d, beta, sampler)
     + (4 + 16 + 4) * NOALLOC_MAX_STATES               // hit flags + details + shade order
     + 16 * static_cast<size_t>(NOALLOC_MAX_PIXELS)    // film
     + 256                                             // counters
-    + 32 * 256;                                       // 256-byte alignment of each buffer
+    + 40 * 256;                                       // 256-byte alignment of each buffer
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 
@@ -2096,10 +2152,13 @@ cudaError_t render_wavefront_noalloc(const DevScene &S, const DevRender &R, void
         B.path[k].ray_d = reinterpret_cast<F4 *>(take(16ull * cap));
         B.path[k].bsdf_le = reinterpret_cast<F4 *>(take(16ull * cap));
     }
-    B.shadow.o = reinterpret_cast<F4 *>(take(16ull * cap));
-    B.shadow.d = reinterpret_cast<F4 *>(take(16ull * cap));
-    B.shadow.beta = reinterpret_cast<F4 *>(take(16ull * cap));
-    B.shadow.sampler = reinterpret_cast<SamplerState *>(take(16ull * cap));
+    for(int k = 0; k < 2; ++k)
+    {
+        B.shadow[k].o = reinterpret_cast<F4 *>(take(16ull * cap));
+        B.shadow[k].d = reinterpret_cast<F4 *>(take(16ull * cap));
+        B.shadow[k].beta = reinterpret_cast<F4 *>(take(16ull * cap));
+        B.shadow[k].sampler = reinterpret_cast<SamplerState *>(take(16ull * cap));
+    }
     B.hit_flag = reinterpret_cast<uint32_t *>(take(4ull * cap));
     B.hit_detail = reinterpret_cast<HitDetail *>(take(16ull * cap));
     B.order = reinterpret_cast<uint32_t *>(take(4ull * cap));
@@ -2165,7 +2224,7 @@ cudaError_t render_wavefront_noalloc(const DevScene &S, const DevRender &R, void
         *stats = RenderStats{};
         stats->paths = c.generated;
         stats->ext_rays = c.ext_rays;
-        stats->shadow_rays = c.shadow_rays + c.shadow;
+        stats->shadow_rays = c.shadow_rays + c.shadow_n[0] + c.shadow_n[1];
         stats->iterations = c.iterations;
         stats->err = c.err;
         uint64_t total = 0;

@@ -24,7 +24,7 @@ cudaError_t launch_trace_stats(const DevScene &S, const Ray *rays, uint32_t n, u
 struct RenderBuffers
 {
     PathSoA path[2];
-    ShadowSoA shadow;
+    ShadowSoA shadow[2];   // by bounce parity
     uint32_t *hit_flag;
     HitDetail *hit_detail;
     uint32_t *order;       // this bounce's queue slots, paths that hit first (trace -> shade)

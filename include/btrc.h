@@ -173,7 +173,7 @@ btrc_status btrc_render(btrc_ctx *ctx, btrc_scene *scene, const btrc_render_opts
    (which synchronise the device) are not allowed. The scene must already be built;
    d_rgb_out is a caller-owned device buffer of width*height*3 floats.
    All scratch (path queues of 32768 states, film, counters) lives in one fixed
-   ~13 MB __device__ array that every GPU loading this library reserves until the
+   ~15 MB __device__ array that every GPU loading this library reserves until the
    process exits. Limits: width*height <= 262144 (e.g. 512x512), otherwise
    BTRC_ERR_INVALID_ARG. Each call clears the film and counters it needs; calls share the
    array, so calls that overlap on the GPU (other threads, other contexts on the same
