@@ -732,10 +732,13 @@ class Scene:
         self.geo_offset = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.uint64)
         self.geo_count = counts
         self.geo_area_total = np.array([float(np.sum(g[2], dtype=np.float64)) for g in geos], np.float32)
-        self.shade = np.ascontiguousarray(np.concatenate([g[1] for g in geos], axis=1), np.float32)
-        self.tri_area = np.ascontiguousarray(np.concatenate([g[2] for g in geos]), np.float32)
-        self.local_pos = np.ascontiguousarray(np.concatenate([g[0].reshape(-1, 9) for g in geos]), np.float32)
-        self.mat = np.ascontiguousarray(np.stack(mats), np.float32)
+        # a scene without entities has no geometry: empty tables of the same layouts
+        self.shade = np.ascontiguousarray(np.concatenate([g[1] for g in geos], axis=1) if geos
+                                          else np.zeros((6, 0, 4)), np.float32)
+        self.tri_area = np.ascontiguousarray(np.concatenate([g[2] for g in geos]) if geos else np.zeros(0), np.float32)
+        self.local_pos = np.ascontiguousarray(np.concatenate([g[0].reshape(-1, 9) for g in geos]) if geos
+                                              else np.zeros((0, 9)), np.float32)
+        self.mat = np.ascontiguousarray(np.stack(mats) if mats else np.zeros((1, 20)), np.float32)
 
         tris, ids = [], []
         l2w, w2l, igeo, imat, ilight = [], [], [], [], []
@@ -804,10 +807,10 @@ class Scene:
                 lint.append(inten)
             else:
                 ilight.append(-1)
-        self.tris = np.ascontiguousarray(np.concatenate(tris), np.float32)
-        self.ids = np.ascontiguousarray(np.concatenate(ids), np.uint32)
-        self.inst_l2w = np.ascontiguousarray(np.stack(l2w), np.float32)
-        self.inst_w2l = np.ascontiguousarray(np.stack(w2l), np.float32)
+        self.tris = np.ascontiguousarray(np.concatenate(tris) if tris else np.zeros((0, 9)), np.float32)
+        self.ids = np.ascontiguousarray(np.concatenate(ids) if ids else np.zeros((0, 2)), np.uint32)
+        self.inst_l2w = np.ascontiguousarray(np.stack(l2w) if l2w else np.zeros((1, 12)), np.float32)
+        self.inst_w2l = np.ascontiguousarray(np.stack(w2l) if w2l else np.zeros((1, 12)), np.float32)
         self.inst_geo = np.array(igeo, np.int32)
         self.inst_mat = np.array(imat, np.int32)
         self.inst_light = np.array(ilight, np.int32)

@@ -119,3 +119,26 @@ def test_tile_generation_matches_uniform(gpu_ctx, scene_dir):
     a, b = imgs
     assert np.isfinite(a).all() and np.isfinite(b).all()
     assert np.allclose(a, b, rtol=1e-4, atol=1e-6), np.abs(a - b).max()
+
+
+def test_scene_without_geometry_sees_the_sky(gpu_ctx, tmp_path):
+    # no entities: an empty BVH, every camera ray misses and collects the gradient sky
+    # (B/light/gradient_sky.cpp:20-40) at its direction, so the image is the oracle's
+    # exactly up to the filter's weights
+    import json
+    scene = {"width": 32, "height": 24,
+             "camera": {"type": "pinhole", "eye": [0, 0, 0], "dst": [0, 0.3, -1], "up": [0, 1, 0],
+                        "fov_y": {"deg": 60}},
+             "renderer": {"type": "wfpt", "spp": 16, "sampler": "independent"},
+             "scene": {"entities": [],
+                       "envir_light": {"type": "gradient_sky", "lower": [0.1, 0.2, 0.3], "upper": [0.9, 0.8, 0.5],
+                                       "up": [0, 1, 0]}}}
+    p = tmp_path / "sky.json"
+    p.write_text(json.dumps(scene))
+    g, o, var, stats = _render_both(gpu_ctx, p, 16)
+    assert stats["traversal_errors"] == 0 and stats["paths"] == 32 * 24 * 16
+    assert stats["extension_rays"] == 32 * 24 * 16  # one per path, all misses
+    assert np.isfinite(g).all()
+    assert np.allclose(g, o, rtol=1e-4, atol=1e-5), np.abs(g - o).max()
+    # the sky brightens upwards: top rows brighter than bottom rows in red
+    assert g[0, :, 0].mean() > g[-1, :, 0].mean()
