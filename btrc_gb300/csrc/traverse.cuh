@@ -388,12 +388,12 @@ namespace bt {
 // one atomic per warp. Each loop iteration advances every busy lane by one node, so
 // lanes never wait for the slowest ray of their warp.
 //
-// Triangle tests are pooled across the warp: after the node step every lane's pending
-// triangles (the leaf bits of its node) are queued in shared memory, up to 32 per
-// iteration, and each lane of the warp then tests one queued (ray, triangle) pair with
-// the owning lane's ray, read from shared memory. The owners merge their results by
-// shuffles. A lane whose triangles did not all fit keeps the rest for the next
-// iteration and takes no node step meanwhile. Testing a leaf's triangles one after the
+// Triangle tests are pooled across the warp: a lane's pending triangles (the leaf bits of
+// its last node) wait until the warp has min_round of them, or until no busy lane could
+// go on without its results; then up to 32 are queued in shared memory and each lane of
+// the warp tests one queued (ray, triangle) pair with the owning lane's ray, read from
+// shared memory. The owners merge their results by shuffles. A lane with pending
+// triangles takes no node step. Testing a leaf's triangles one after the
 // other, lane by lane, ran with ~3 of 32 lanes active; pooled, a round runs with as
 // many lanes as the warp has tests. Results are those of sequential testing: the
 // closest hit is a strict total order on (t, instance, primitive).
@@ -401,7 +401,7 @@ namespace bt {
 // The kernel launches 128-thread blocks (TRAVERSE_WARPS warps, one shared-memory slice
 // each), and all 32 lanes of a warp enter (the warp-wide votes use the full mask).
 //   fetch(i, o, d, t1): load ray i;  emit(i, hit): store its result
-constexpr int REFILL_LANES = 8;  // idle lanes that trigger a warp refill (measured best of 8/16/24)
+constexpr int REFILL_LANES = 8;  // idle lanes that trigger a warp refill (measured best of 4/8/12/16/24)
 constexpr int TRAVERSE_BLOCK = 128;
 constexpr int TRAVERSE_WARPS = TRAVERSE_BLOCK / 32;
 // queue entry: owner lane in bits 27..31, triangle record index in bits 0..26
