@@ -214,8 +214,8 @@ def _time_to(curve, target):
 
 
 def nrc_study(B, ctx, sc, info, args):
-    """Equal-time comparison of the radiance cache against the plain tracer on the
-    benchmark scene: relMSE against a converged plain render (args.ref_spp spp) as a
+    """Equal-time comparison of the radiance cache against the plain tracer on a built
+    scene: relMSE against a converged plain render (args.ref_spp spp) as a
     function of wall time, for plain renders of 1..128 spp and for the cache (one path per
     pixel per frame, paths ending in the cache after one bounce, 1/16 of the pixels
     tracing training paths, 4 Adam steps of 16384 samples per frame, trained from scratch
@@ -464,11 +464,26 @@ def run_ours(args, world, rank, local):
             batch = {"error": str(ex)}
 
     nrc = None
+    nrc_interior = None
     if rank == 0 and not args.no_nrc:
         try:
             nrc = nrc_study(B, ctx, sc, info, args)
         except Exception as ex:  # the study must not sink the throughput number
             nrc = {"error": str(ex)}
+        # the same study in a closed interior, where most light arrives after several bounces
+        try:
+            from btrc_gb300 import scenes
+            csc = ctx.load_scene(scenes.cornell(width=512, height=512, spp=16)).build()
+            nrc_interior = nrc_study(B, ctx, csc, csc.info(), args)
+            nrc_interior = {"scene": "config 0's Cornell box (two icospheres, quad light) at 512x512",
+                            **{k: nrc_interior[k] for k in ("target_relmse", "reference_spp", "plain_ms_to_target",
+                                                            "nrc_ms_to_target", "time_ratio_nrc_over_plain",
+                                                            "nrc_relmse_at_plain_time", "nrc_ms_per_frame",
+                                                            "nrc_queries_per_frame", "plain_curve_ms_relmse",
+                                                            "nrc_curve_ms_relmse")}}
+            csc.close()
+        except Exception as ex:
+            nrc_interior = {"error": str(ex)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -508,6 +523,7 @@ def run_ours(args, world, rank, local):
             "cpu_baseline": cpu,
             "clocks": clk,
             "radiance_cache": nrc,
+            "radiance_cache_interior": nrc_interior,
             "batch": batch,
             "mrays_per_s": world * (st["extension_rays"] + st["shadow_rays"]) / (step_ms / 1000) / 1e6,
             "scene_load_s": load_s, "bvh_build_ms": info.build_ms,
