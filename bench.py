@@ -42,7 +42,9 @@ def parse():
     ap.add_argument("--instances", type=int, default=200)
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
-    ap.add_argument("--state-count", type=int, default=2 * 1024 * 1024)
+    # path-queue length (the renderer's state_count): 32 M states, 11.5 GB of queues, so
+    # each bounce launch keeps every SM busy for milliseconds and launch tails are few
+    ap.add_argument("--state-count", type=int, default=32 * 1024 * 1024)
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-nrc", action="store_true", help="skip the radiance-cache equal-time study")

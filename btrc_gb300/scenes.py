@@ -401,7 +401,7 @@ def terrain(seed: int = 1001, width: int = 1920, height: int = 1080, spp: int = 
     """Config 1: fBm terrain + instanced icospheres + Disney + sky + 8 quad lights."""
     out = Path(out_dir or cache_dir() / f"terrain-{seed}-{grid}-{instances}")
     out.mkdir(parents=True, exist_ok=True)
-    name = f"scene-{width}x{height}-{spp}.json"
+    name = f"scene-{width}x{height}-{spp}-q{state_count}.json"
     if (out / name).exists() and not force:
         return out / name
     rng = np.random.default_rng(seed)
@@ -548,7 +548,7 @@ def volume(seed: int = 1002, width: int = 1024, height: int = 1024, spp: int = 6
     GGX conductor of roughness 0.2; depth 32."""
     out = Path(out_dir or cache_dir() / f"volume-{seed}-{grid_res}-{sphere_level}")
     out.mkdir(parents=True, exist_ok=True)
-    name = f"scene-{width}x{height}-{spp}.json"
+    name = f"scene-{width}x{height}-{spp}-q{state_count}.json"
     if (out / name).exists() and not force:
         return out / name
     rng = np.random.default_rng(seed)
