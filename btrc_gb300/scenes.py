@@ -397,7 +397,7 @@ def cornell(seed: int = 1000, width: int = 256, height: int = 256, spp: int = 16
 
 def terrain(seed: int = 1001, width: int = 1920, height: int = 1080, spp: int = 64, grid: int = 1024,
             instances: int = 200, out_dir: Path | None = None, force: bool = False,
-            state_count: int = 2 * 1024 * 1024) -> Path:
+            state_count: int = 32 * 1024 * 1024) -> Path:
     """Config 1: fBm terrain + instanced icospheres + Disney + sky + 8 quad lights."""
     out = Path(out_dir or cache_dir() / f"terrain-{seed}-{grid}-{instances}")
     out.mkdir(parents=True, exist_ok=True)
@@ -542,7 +542,7 @@ def displaced_sphere(perlin: Perlin, level: int, radius: float, amp: float):
 
 def volume(seed: int = 1002, width: int = 1024, height: int = 1024, spp: int = 64, grid_res: int = 256,
            sphere_level: int = 7, text_grid: bool = False, out_dir: Path | None = None, force: bool = False,
-           state_count: int = 2 * 1024 * 1024) -> Path:
+           state_count: int = 32 * 1024 * 1024) -> Path:
     """Config 2: the cornell box with a heterogeneous fBm medium (sigma_t max 20, albedo 0.9,
     HG g 0.6) behind a transform inside an invisible cube, plus a displaced icosphere with a
     GGX conductor of roughness 0.2; depth 32."""
