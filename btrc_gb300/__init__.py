@@ -118,6 +118,7 @@ SIGNATURES = {
     "btrc_bsdf_batch": (C.c_int, [_vp, C.c_int32, _vp, _vp, _vp, C.c_uint64, _vp, _vp]),
     "btrc_medium_tr_batch": (C.c_int, [_vp, _vp, C.c_int32, _vp, _vp, C.c_uint64, _vp, _vp]),
     "btrc_tonemap_aces": (C.c_int, [_vp, _vp, C.c_int32, C.c_int32, C.c_int32, C.c_float, _vp]),
+    "btrc_denoise_atrous": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32, _vp]),
     "btrc_image_save": (C.c_int, [_vp, C.c_char_p, _vp, C.c_int32, C.c_int32, C.c_int32, C.c_float]),
     "btrc_nrc_create": (C.c_int, [_vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint64, C.POINTER(_vp)]),
     "btrc_nrc_destroy": (None, [_vp]),
@@ -229,7 +230,7 @@ class Context:
         """Render the scene's frame. `out` may be a CUDA tensor (rendered in place) or None
         (a new host float32 array of shape (H, W, 3) is returned). `albedo` / `normal`
         receive the first-hit g-buffers (arrays in the same memory space as `out`);
-        post_process runs the scene's post_processors (tonemap, save) on the result."""
+        post_process runs the scene's post_processors (tonemap, denoise, save) on the result."""
         info = scene.info()
         on_dev = out is not None and hasattr(out, "is_cuda") and out.is_cuda
         if out is None:
@@ -295,6 +296,12 @@ class Context:
         """In-place ACES tone map of a device buffer (tonemap post-processor)."""
         self._check(self._lib.btrc_tonemap_aces(self.handle, _ptr(pixels), width, height, channels, exposure,
                                                 stream))
+
+    def denoise_atrous(self, pixels, width: int, height: int, albedo=None, normal=None, stream: int | None = None):
+        """In-place edge-avoiding a-trous denoise of a device RGB buffer, optionally guided by
+        device albedo / normal images (denoise post-processor)."""
+        self._check(self._lib.btrc_denoise_atrous(self.handle, _ptr(pixels), _ptr(albedo), _ptr(normal), width,
+                                                  height, stream))
 
     def image_load(self, filename: str) -> tuple[np.ndarray, int]:
         """Decode a .png / .hdr texture file: ((H, W, 4) float32 texels, file channels)."""

@@ -54,6 +54,8 @@ struct btrc_ctx
     bool has_media_buffers = false;
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
+    float *denoise_tmp = nullptr;  // ping-pong image of the denoise post-processor
+    size_t denoise_bytes = 0;
     std::set<btrc_scene *> scenes;  // live scenes, destroyed with the context
     // batched rendering: concurrent lanes and the autotuner's choices per scene class
     std::vector<std::unique_ptr<struct BatchLane>> lanes;
@@ -494,6 +496,22 @@ float *ctx_scratch_images(btrc_ctx *ctx, size_t pixels, int images)
     return reinterpret_cast<float *>(static_cast<char *>(ctx->scratch) + 256);
 }
 
+float *ctx_denoise_tmp(btrc_ctx *ctx, size_t pixels)
+{
+    const size_t need = pixels * 3 * sizeof(float);
+    if(ctx->denoise_bytes < need)
+    {
+        check_cuda(cudaStreamSynchronize(ctx->stream), "stream sync");
+        if(ctx->denoise_tmp)
+            cudaFree(ctx->denoise_tmp);
+        ctx->denoise_tmp = nullptr;
+        ctx->denoise_bytes = 0;
+        check_cuda(cudaMalloc(&ctx->denoise_tmp, need), "cudaMalloc");
+        ctx->denoise_bytes = need;
+    }
+    return ctx->denoise_tmp;
+}
+
 DevRender make_render_params(const btrc_scene *sc, int spp, uint32_t capacity)
 {
     const HostScene &H = sc->host;
@@ -606,6 +624,8 @@ void btrc_ctx_destroy(btrc_ctx *ctx)
         cudaFreeHost(ctx->buf.host_counters);
     if(ctx->scratch)
         cudaFree(ctx->scratch);
+    if(ctx->denoise_tmp)
+        cudaFree(ctx->denoise_tmp);
     if(ctx->stream)
         cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -812,7 +832,15 @@ btrc_status btrc_render(btrc_ctx *ctx, btrc_scene *scene, const btrc_render_opts
             for(const PostProcess &q : H.post)
             {
                 if(q.type == POST_DENOISE)
-                    throw StatusError(BTRC_ERR_UNSUPPORTED, "post processor 'denoise' (OptiX denoiser) is not available");
+                {
+                    // guided by the albedo / normal AOVs when the renderer produces them, as the
+                    // OptiX denoiser is (postprocess/optix_denoiser.cpp:51-98)
+                    check_cuda(launch_denoise_atrous(rgb_dev, ctx_denoise_tmp(ctx, pixels), alb_dev, nrm_dev,
+                                                     H.params.width, H.params.height, ctx->stream),
+                               "denoise");
+                    extra_launches += DENOISE_PASSES;
+                    continue;
+                }
                 if(q.type == POST_TONEMAP)
                 {
                     check_cuda(launch_tonemap_aces(rgb_dev, static_cast<uint32_t>(pixels), 3, q.exposure, ctx->stream),
@@ -1074,6 +1102,24 @@ btrc_status btrc_tonemap_aces(btrc_ctx *ctx, float *d_pixels, int32_t width, int
         check_cuda(launch_tonemap_aces(d_pixels, static_cast<uint32_t>(width) * static_cast<uint32_t>(height), channels,
                                        exposure, pick_stream(ctx, stream)),
                    "tonemap");
+    });
+}
+
+btrc_status btrc_denoise_atrous(btrc_ctx *ctx, float *d_rgb, const float *d_albedo, const float *d_normal,
+                                int32_t width, int32_t height, void *stream)
+{
+    if(!ctx || width < 0 || height < 0 || static_cast<uint64_t>(width) * static_cast<uint64_t>(height) > 0xffffffffull ||
+       (width > 0 && height > 0 && !d_rgb))
+        return BTRC_ERR_INVALID_ARG;
+    return guarded(ctx, [&] {
+        if(ctx->device < 0)
+            throw StatusError(BTRC_ERR_INVALID_ARG, "host-only context");
+        if(width == 0 || height == 0)
+            return;
+        check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+        cudaStream_t st = pick_stream(ctx, stream);
+        float *tmp = ctx_denoise_tmp(ctx, static_cast<size_t>(width) * height);
+        check_cuda(launch_denoise_atrous(d_rgb, tmp, d_albedo, d_normal, width, height, st), "denoise");
     });
 }
 

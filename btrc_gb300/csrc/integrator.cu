@@ -1890,6 +1890,107 @@ cudaError_t launch_tonemap_aces(float *px, uint32_t pixels, int channels, float 
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- denoise post-processor
+
+// Edge-avoiding a-trous wavelet filter (Dammertz, Sewtz, Hanika and Lensch, "Edge-Avoiding
+// A-Trous Wavelet Transform for fast Global Illumination Filtering", HPG 2010), the stand-in
+// for the reference's `denoise` post-processor, whose OptiX AI denoiser is a closed library
+// (builtin/btrc/builtin/postprocess/optix_denoiser.cpp:51-126: in place on the colour, with
+// optional albedo and normal guides). Pass k convolves with the 5x5 B3-spline kernel
+// (1/16, 1/4, 3/8, 1/4, 1/16) dilated to a tap spacing of 2^k pixels; each tap is weighted
+// by exp(-(e_c + e_a + e_n)) with e_c = |T(c_p) - T(c_q)|^2 / sigma_c^2, T(c) = c / (1 + c)
+// per channel (HDR colours compared in a bounded space) and sigma_c halved every pass,
+// e_a = |a_p - a_q|^2 / sigma_a^2 and e_n = |n_p - n_q|^2 / (4^k sigma_n^2) when the guides
+// are present. Taps outside the image are skipped and the weights renormalised.
+namespace
+{
+__device__ __forceinline__ float3 ld3(const float *__restrict__ a, size_t i)
+{
+    return make_float3(a[i * 3 + 0], a[i * 3 + 1], a[i * 3 + 2]);
+}
+
+__device__ __forceinline__ float3 tone01(float3 c)
+{
+    c.x = fmaxf(c.x, 0.0f);
+    c.y = fmaxf(c.y, 0.0f);
+    c.z = fmaxf(c.z, 0.0f);
+    return make_float3(c.x / (1.0f + c.x), c.y / (1.0f + c.y), c.z / (1.0f + c.z));
+}
+
+__device__ __forceinline__ float dist2(float3 a, float3 b)
+{
+    const float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+    return dx * dx + dy * dy + dz * dz;
+}
+} // namespace
+
+__global__ void __launch_bounds__(256) k_denoise_atrous(const float *__restrict__ in, float *__restrict__ out,
+                                                        const float *__restrict__ alb, const float *__restrict__ nrm,
+                                                        int w, int h, int step, float inv_sc2, float inv_sa2,
+                                                        float inv_sn2)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if(x >= w || y >= h)
+        return;
+    const size_t p = static_cast<size_t>(y) * w + x;
+    const float3 tp = tone01(ld3(in, p));
+    const float3 ap = alb ? ld3(alb, p) : make_float3(0.0f, 0.0f, 0.0f);
+    const float3 np = nrm ? ld3(nrm, p) : make_float3(0.0f, 0.0f, 0.0f);
+    const float hk[3] = { 0.375f, 0.25f, 0.0625f };
+    float sx = 0.0f, sy = 0.0f, sz = 0.0f, sw = 0.0f;
+    for(int dy = -2; dy <= 2; ++dy)
+    {
+        const int qy = y + dy * step;
+        if(qy < 0 || qy >= h)
+            continue;
+        for(int dx = -2; dx <= 2; ++dx)
+        {
+            const int qx = x + dx * step;
+            if(qx < 0 || qx >= w)
+                continue;
+            const size_t q = static_cast<size_t>(qy) * w + qx;
+            const float3 cq = ld3(in, q);
+            float e = dist2(tp, tone01(cq)) * inv_sc2;
+            if(alb)
+                e += dist2(ap, ld3(alb, q)) * inv_sa2;
+            if(nrm)
+                e += dist2(np, ld3(nrm, q)) * inv_sn2;
+            const float wt = hk[dx < 0 ? -dx : dx] * hk[dy < 0 ? -dy : dy] * expf(-e);
+            sx += wt * cq.x;
+            sy += wt * cq.y;
+            sz += wt * cq.z;
+            sw += wt;
+        }
+    }
+    // the centre tap (weight 9/64) is always present, so sw > 0
+    out[p * 3 + 0] = sx / sw;
+    out[p * 3 + 1] = sy / sw;
+    out[p * 3 + 2] = sz / sw;
+}
+
+cudaError_t launch_denoise_atrous(float *rgb, float *tmp, const float *albedo, const float *normal, int width,
+                                  int height, cudaStream_t st)
+{
+    if(width <= 0 || height <= 0)
+        return cudaSuccess;
+    const dim3 block(16, 16), grid((width + 15) / 16, (height + 15) / 16);
+    float *src = rgb, *dst = tmp;
+    for(int k = 0; k < DENOISE_PASSES; ++k)
+    {
+        const float step = static_cast<float>(1 << k);
+        const float sc = DENOISE_SIGMA_COLOR / step;  // halved every pass
+        k_denoise_atrous<<<grid, block, 0, st>>>(src, dst, albedo, normal, width, height, 1 << k, 1.0f / (sc * sc),
+                                                 1.0f / (DENOISE_SIGMA_ALBEDO * DENOISE_SIGMA_ALBEDO),
+                                                 1.0f / (DENOISE_SIGMA_NORMAL * DENOISE_SIGMA_NORMAL * step * step));
+        std::swap(src, dst);
+    }
+    if(src != rgb)
+        return cudaMemcpyAsync(rgb, src, sizeof(float) * 3 * static_cast<size_t>(width) * height,
+                               cudaMemcpyDeviceToDevice, st);
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------- radiance-cache training paths
 
 constexpr int NRC_TRAIN_VERTS = 6;   // recorded vertices per training path

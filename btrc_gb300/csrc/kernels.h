@@ -97,6 +97,15 @@ cudaError_t launch_nrc_splat(const float4 *pred, const float4 *weight, const uin
                              float4 *film, int width, cudaStream_t st);
 // in-place ACES tone map of 3- or 4-channel float pixels
 cudaError_t launch_tonemap_aces(float *px, uint32_t pixels, int channels, float exposure, cudaStream_t st);
+// denoise post-processor: edge-avoiding a-trous filter, DENOISE_PASSES passes (tap spacing
+// 1, 2, 4, 8, 16), in place on 3-float pixels; tmp holds width x height x 3 floats;
+// albedo / normal (3 floats per pixel) may be null
+constexpr int DENOISE_PASSES = 5;
+constexpr float DENOISE_SIGMA_COLOR = 0.5f;   // in c / (1 + c) space, first pass
+constexpr float DENOISE_SIGMA_ALBEDO = 0.05f;
+constexpr float DENOISE_SIGMA_NORMAL = 0.3f;  // first pass; scaled by the tap spacing
+cudaError_t launch_denoise_atrous(float *rgb, float *tmp, const float *albedo, const float *normal, int width,
+                                  int height, cudaStream_t st);
 
 // test hooks
 cudaError_t launch_sampler_batch(int type, int width, int height, const HaltonConsts &hc,

@@ -80,7 +80,7 @@ enum PostType : int32_t
 {
     POST_SAVE = 0,      // builtin/btrc/builtin/postprocess/save_to_image.cpp:63-76
     POST_TONEMAP = 1,   // builtin/btrc/builtin/postprocess/tonemap.cpp:103-108
-    POST_DENOISE = 2,   // optix_denoiser.cpp: the OptiX denoiser, not available here
+    POST_DENOISE = 2,   // optix_denoiser.cpp: run as the a-trous filter (the OptiX denoiser is closed)
 };
 
 struct PostProcess

@@ -102,8 +102,9 @@ typedef struct btrc_render_opts
     int32_t profile;          /* 0 off; 1 CUDA events around every stage launch (no graphs);
                                  2 closest-hit traversal counters (no graphs, slower) */
     int32_t post_process;     /* 1: run the scene's post_processors on the result, in order:
-                                 tonemap in place, save writes files; a denoise entry
-                                 fails with BTRC_ERR_UNSUPPORTED */
+                                 tonemap in place, save writes files, denoise runs
+                                 btrc_denoise_atrous (guided by the albedo / normal
+                                 images when the renderer produces them) */
     float *albedo_out;        /* optional first-hit albedo, width*height*3 floats, same memory
                                  space as rgb_out (wavefront/shade.cpp:133-139, preview.cpp:27-47) */
     float *normal_out;        /* optional first-hit normal (world space, renormalised) */
@@ -187,6 +188,15 @@ btrc_status btrc_render_noalloc(btrc_ctx *ctx, btrc_scene *scene, int32_t spp, f
    c = saturate(x (2.51 x + 0.03) / (x (2.43 x + 0.59) + 0.14)) with x = c * exposure. */
 btrc_status btrc_tonemap_aces(btrc_ctx *ctx, float *d_pixels, int32_t width, int32_t height, int32_t channels,
                               float exposure, void *stream);
+
+/* Stand-in for OptixAIDenoiser::process (src/builtin/btrc/builtin/postprocess/optix_denoiser.cpp:51-126),
+   whose OptiX AI denoiser is a closed library: an edge-avoiding a-trous wavelet filter
+   (Dammertz et al., HPG 2010; 5 passes, tap spacing 1..16) in place on device pixels of 3
+   floats, guided by the optional first-hit albedo and normal images (3 floats per pixel,
+   NULL = unused). Runs on `stream` (NULL = the context's stream). The `denoise` entry of a
+   scene's post_processors runs the same filter. */
+btrc_status btrc_denoise_atrous(btrc_ctx *ctx, float *d_rgb, const float *d_albedo, const float *d_normal,
+                                int32_t width, int32_t height, void *stream);
 
 /* SaveToImage::process (src/builtin/btrc/builtin/postprocess/save_to_image.cpp:30-61) with
    Image::save (src/common/btrc/utils/image.h:495-550): write host pixels (3 or 4 floats,

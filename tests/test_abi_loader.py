@@ -162,7 +162,7 @@ def test_wfpt_defaults_and_pt_renderer(native_lib, tmp_path):
 
 def test_post_processors_parse(native_lib, tmp_path):
     # a group or an array of post processors (factory/btrc/factory/post_processor.cpp:5-25);
-    # unknown types fail to load, denoise loads (it is refused only when run)
+    # unknown types fail to load, denoise loads
     base = json.loads(scenes.cornell(out_dir=tmp_path, width=8, height=8, spp=1).read_text())
     ctx = B.Context(-1)
     for post, ok in (({"type": "tonemap"}, True),

@@ -5,7 +5,8 @@
     sampler streams;
   * the ACES tone map kernel (postprocess/tonemap.cpp:14-53) against its formula;
   * a scene's post_processors list run by btrc_render (tonemap, then save of colour,
-    albedo and normal), and a denoise entry reported as unsupported."""
+    albedo and normal), and the denoise entry (edge-avoiding a-trous filter standing in
+    for the closed OptiX denoiser) against its NumPy restatement."""
 import json
 
 import numpy as np
@@ -95,10 +96,53 @@ def test_post_processors_tonemap_then_save(gpu_ctx, tmp_path):
     assert np.allclose(np.linalg.norm(n, axis=-1), 1, atol=1e-5)
 
 
-def test_post_processors_denoise_unsupported(gpu_ctx, tmp_path):
-    p = _post_scene(tmp_path, {"type": "denoise"})
-    sc = gpu_ctx.load_scene(p).build()
-    gpu_ctx.render(sc)  # without post-processing the scene renders
-    with pytest.raises(B.BtrcError) as e:
-        gpu_ctx.render(sc, post_process=True)
-    assert e.value.status == 8
+@pytest.mark.parametrize("guides", [False, True])
+def test_denoise_kernel_matches_oracle(gpu_ctx, guides):
+    # HDR noise over piecewise-constant albedo / normal regions; the CUDA a-trous filter
+    # against its NumPy restatement (FMA contraction and expf rounding: 1e-4 relative)
+    import torch
+    from oracle import denoise as OD
+    rng = np.random.default_rng(31)
+    h, w = 48, 64
+    reg = (np.arange(w)[None, :] // 16 + 2 * (np.arange(h)[:, None] // 24)) % 4
+    alb = rng.uniform(0.1, 0.9, (4, 3)).astype(np.float32)[reg]
+    n = rng.normal(size=(4, 3))
+    nrm = (n / np.linalg.norm(n, axis=1, keepdims=True)).astype(np.float32)[reg]
+    img = (3.0 * alb * rng.exponential(1.0, (h, w, 3))).astype(np.float32)
+    d_img = torch.from_numpy(img).cuda()
+    d_alb = torch.from_numpy(np.ascontiguousarray(alb)).cuda() if guides else None
+    d_nrm = torch.from_numpy(np.ascontiguousarray(nrm)).cuda() if guides else None
+    gpu_ctx.denoise_atrous(d_img, w, h, d_alb, d_nrm)
+    torch.cuda.synchronize()
+    got = d_img.cpu().numpy()
+    want = OD.atrous(img, alb if guides else None, nrm if guides else None)
+    assert np.allclose(got, want, rtol=1e-4, atol=1e-6), np.abs(got - want).max()
+    # noise within each region falls; with the guides the regions keep their own colours
+    within = lambda a: np.mean([a[reg == r].std(0).mean() for r in range(4)])
+    assert within(got) < 0.5 * within(img)
+    # an empty image is a no-op
+    gpu_ctx.denoise_atrous(None, 0, 0)
+
+
+def test_post_processors_denoise(gpu_ctx, tmp_path):
+    # the scene's denoise entry runs the a-trous filter on the render, guided by the
+    # renderer's albedo / normal g-buffers, and brings a 4-spp render closer to the
+    # converged image
+    from oracle import denoise as OD
+    from tests.util import rel_mse
+    p = scenes.cornell(out_dir=tmp_path, width=96, height=72, spp=4)
+    scene = json.loads(p.read_text())
+    scene["renderer"]["albedo"] = True
+    scene["renderer"]["normal"] = True
+    scene["post_processors"] = {"type": "denoise"}
+    q = tmp_path / "denoise.json"
+    q.write_text(json.dumps(scene))
+    sc = gpu_ctx.load_scene(q).build()
+    raw = gpu_ctx.render(sc)
+    alb = np.zeros_like(raw)
+    nrm = np.zeros_like(raw)
+    out = gpu_ctx.render(sc, post_process=True, albedo=alb, normal=nrm)
+    # raw comes from a second render of the same paths (film sums differ in atomic order)
+    assert np.allclose(out, OD.atrous(raw, alb, nrm), rtol=1e-3, atol=1e-4)
+    ref = gpu_ctx.render(sc, spp=1024)
+    assert rel_mse(out, ref) < 0.5 * rel_mse(raw, ref)
