@@ -337,14 +337,15 @@ def _fog_volumes(out: Path, rng: np.random.Generator) -> list[dict]:
 
 
 def cornell(seed: int = 1000, width: int = 256, height: int = 256, spp: int = 16, sampler: str = "halton",
-            out_dir: Path | None = None, force: bool = False, variant: str = "diffuse") -> Path:
+            out_dir: Path | None = None, force: bool = False, variant: str = "diffuse",
+            state_count: int = 32 * 1024 * 1024) -> Path:
     """Config 0: closed unit box, two icospheres, one quad light (see module docstring).
     `variant` picks the spheres' materials from SPHERE_VARIANTS."""
     mats = SPHERE_VARIANTS[variant]
     out = Path(out_dir or cache_dir() / f"cornell-{seed}")
     out.mkdir(parents=True, exist_ok=True)
     tag = "" if variant == "diffuse" else f"-{variant}"
-    name = f"scene-{width}x{height}-{spp}-{sampler}{tag}.json"
+    name = f"scene-{width}x{height}-{spp}-{sampler}{tag}-q{state_count}.json"
     if (out / name).exists() and not force:
         return out / name
     rng = np.random.default_rng(seed)
@@ -381,7 +382,7 @@ def cornell(seed: int = 1000, width: int = 256, height: int = 256, spp: int = 16
         "camera": {"type": "pinhole", "eye": eye.tolist(), "dst": [0.0, 0.0, -half], "up": [0.0, 1.0, 0.0],
                    "fov_y": {"deg": 40.0}},
         "renderer": {"type": "wfpt", "spp": spp, "min_depth": 3, "max_depth": 8, "rr_threshold": 0.1,
-                     "rr_cont_prob": 0.5, "state_count": 1000000, "sampler": sampler,
+                     "rr_cont_prob": 0.5, "state_count": state_count, "sampler": sampler,
                      "filter": {"type": "gaussian", "radius": 1.5, "alpha": 1.6}},
         "scene": {"entities": ents},
     }
