@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched uneven-scenes measurement")
     ap.add_argument("--nrc-frames", type=int, default=256, help="frames of the radiance-cache study")
     ap.add_argument("--ref-spp", type=int, default=4096, help="spp of the converged reference image")
+    ap.add_argument("--trace-probe", action="store_true",
+                    help="trace the workload's camera rays, then one diffuse bounce ray per camera hit, "
+                         "through btrc_trace_closest (two launches, for DRAM-traffic captures) and exit")
     return ap.parse_args()
 
 
@@ -448,14 +451,18 @@ def run_ours(args, world, rank, local):
     node_b, tri_b = 80, 48
     trace_bytes = ext_rays * (32 + 20) + cnt["node_visits"] * node_b + cnt["tri_tests"] * tri_b
     achieved = trace_bytes / (trace_ms / 1000) / 1e9 if trace_ms > 0 else None
-    # DRAM bytes per ray from the committed ncu capture, scaled to this run's average launch
+    # DRAM bytes per camera / secondary ray from the committed ncu capture, scaled to this
+    # run's average launch
     traffic_path = ROOT / "profiles" / "trace_traffic.json"
     traffic = None
     if traffic_path.exists():
         try:
-            per_ray = json.loads(traffic_path.read_text()).get("dram_bytes_per_ray")
-            traffic = per_ray * ext_rays / max(trace_launches, 1) if per_ray else None
-        except ValueError:
+            tj = json.loads(traffic_path.read_text())
+            # camera rays (one per path) and secondary rays measured separately
+            cam_rays = min(cnt["paths"], ext_rays)
+            traffic = (tj["camera_dram_bytes_per_ray"] * cam_rays +
+                       tj["secondary_dram_bytes_per_ray"] * (ext_rays - cam_rays)) / max(trace_launches, 1)
+        except (ValueError, KeyError):
             traffic = None
 
     batch = None
@@ -535,8 +542,60 @@ def run_ours(args, world, rank, local):
     ctx.close()
 
 
+def trace_probe(args):
+    """Two closest-hit launches over the benchmark scene: the 1-spp pinhole camera rays
+    through pixel centres, then one ray per camera hit in a uniform direction of the upper
+    hemisphere (the terrain's surfaces face up), so that an ncu capture can measure DRAM
+    bytes per camera ray and per secondary ray separately."""
+    import math
+    import torch
+    import btrc_gb300 as B
+    from btrc_gb300 import scenes
+    p = scenes.terrain(seed=1001, width=args.width, height=args.height, spp=1, grid=args.grid,
+                       instances=args.instances)
+    js = json.loads(Path(p).read_text())
+    W, H, cam = js["width"], js["height"], js["camera"]
+    eye, dst, up = (np.array(cam[k], np.float64) for k in ("eye", "dst", "up"))
+    fwd = (dst - eye) / np.linalg.norm(dst - eye)
+    right = np.cross(fwd, up)
+    right /= np.linalg.norm(right)
+    upv = np.cross(right, fwd)
+    th = math.tan(math.radians(cam["fov_y"]["deg"]) / 2)
+    X, Y = np.meshgrid((2 * (np.arange(W) + 0.5) / W - 1) * th * W / H, (1 - 2 * (np.arange(H) + 0.5) / H) * th)
+    d = (fwd[None, None] + X[..., None] * right + Y[..., None] * upv).reshape(-1, 3)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    ctx = B.Context(0)
+    sc = ctx.load_scene(p).build()
+
+    def trace(o, dirs):
+        m = len(o)
+        r = np.zeros((m, 8), np.float32)
+        r[:, 0:3], r[:, 4:7], r[:, 7] = o, dirs, 3.0e38
+        dr = torch.from_numpy(r).cuda()
+        f = torch.zeros(m, dtype=torch.int32, device="cuda")
+        h = torch.zeros((m, 4), dtype=torch.float32, device="cuda")
+        ctx.trace_closest(sc, dr, m, f, h)
+        torch.cuda.synchronize()
+        return f.cpu().numpy().view(np.uint32), h.cpu().numpy()
+
+    f, h = trace(np.broadcast_to(eye, d.shape), d)
+    hit = f != 0
+    org = eye + d[hit] * (h[hit, 0:1].astype(np.float64) - 1e-4)
+    nd = np.random.default_rng(3).normal(size=org.shape)
+    nd /= np.linalg.norm(nd, axis=1, keepdims=True)
+    nd[:, 1] = np.abs(nd[:, 1])
+    f2, _ = trace(org, nd)
+    print(json.dumps({"camera_rays": len(d), "camera_hit_rate": float(hit.mean()), "secondary_rays": int(hit.sum()),
+                      "secondary_hit_rate": float((f2 != 0).mean())}), flush=True)
+    sc.close()
+    ctx.close()
+
+
 def main():
     args = parse()
+    if args.trace_probe:
+        trace_probe(args)
+        return
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank)
