@@ -527,6 +527,8 @@ def run_ours(args, world, rank, local):
                          "tris_per_ray": cnt["tri_tests"] / max(ext_rays, 1),
                          "launches": trace_launches, "avg_launch_ms": trace_ms / max(trace_launches, 1),
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6800",
+                         "traffic_source": "ncu dram__bytes per camera ray and per secondary ray "
+                                           "(profiles/trace_traffic.json) x this frame's rays / launches",
                          "stage_share": {k: v / total_stage for k, v in stage_ms.items() if total_stage > 0},
                          "dominant_stage": dom},
             "cpu_baseline": cpu,
