@@ -83,6 +83,15 @@ def all_max(world, v: float) -> float:
     return float(t.item())
 
 
+def bench_config(args, triangles: int) -> dict:
+    """The workload description both arms print (same keys and values)."""
+    return {"workload": WORKLOAD, "width": args.width, "height": args.height, "spp": args.spp, "max_depth": 16,
+            "triangles": int(triangles), "state_count": args.state_count, "sampler": "independent",
+            "filter": "gaussian r1.5",
+            "l2": "inputs larger than L2: BVH + shading records of the 3.1 M-triangle scene > 129 MB",
+            "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU"}
+
+
 def scene_path(args):
     from btrc_gb300 import scenes
     return scenes.terrain(seed=1001, width=args.width, height=args.height, spp=args.spp, grid=args.grid,
@@ -190,8 +199,7 @@ def run_reference(args, world, rank):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Mpaths/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "width": args.width, "height": args.height, "spp": args.spp,
-                   "max_depth": 16, "triangles": int(len(S.tris))},
+        "config": bench_config(args, len(S.tris)),
         "cpu_baseline": {"value": value, "unit": "Mpaths/s", "cores": threads, "kind": "port",
                          "sample": f"each step: {k_spp} spp over the full 1920x1080 film ({n_step} paths)"},
         "e2e": {"value": value, "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -507,12 +515,8 @@ def run_ours(args, world, rank, local):
             "metric": METRIC, "value": value, "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-            "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": spp, "max_depth": info.max_depth,
-                       "triangles": int(info.triangles), "bvh_bytes": int(info.bvh_bytes),
-                       "state_count": args.state_count, "sampler": "independent", "filter": "gaussian r1.5",
-                       "l2": f"inputs larger than L2: BVH {info.bvh_bytes / 1e6:.0f} MB + shading records "
-                             f"{info.triangles * 96 / 1e6:.0f} MB > 129 MB",
-                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "config": bench_config(args, info.triangles),
+            "bvh_bytes": int(info.bvh_bytes), "shading_record_bytes": int(info.triangles) * 96,
             "e2e": {"value": e2e_value, "unit": "Mpaths/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": W * H * 3 * 4,
                     "note": "btrc_render through the C ABI into a pinned host buffer (image download "

@@ -260,7 +260,24 @@ class Context:
 
     def render_noalloc(self, scene: "Scene", out, spp: int = 0, stats: dict | None = None):
         """Allocation-free render into a caller-owned CUDA tensor of shape (H, W, 3)
-        (btrc_render_noalloc: fixed scratch, film up to 512x512 pixels)."""
+        (btrc_render_noalloc: fixed scratch, film up to 512x512 pixels).
+
+        `out` must be a contiguous float32 CUDA tensor on this context's device with at
+        least H*W*3 elements; anything else raises BtrcError(INVALID_ARG) before the
+        library is called. Work already queued on torch's current stream (a fill of
+        `out`, say) is finished first, since the render runs on the context's own stream."""
+        info = scene.info()
+        need = info.width * info.height * 3
+        if not (hasattr(out, "is_cuda") and out.is_cuda):
+            raise BtrcError(1, "render_noalloc: out must be a CUDA tensor (device memory)")
+        import torch
+        if out.dtype != torch.float32 or not out.is_contiguous():
+            raise BtrcError(1, "render_noalloc: out must be a contiguous float32 tensor")
+        if out.device.index != self.device:
+            raise BtrcError(1, f"render_noalloc: out is on cuda:{out.device.index}, the context on cuda:{self.device}")
+        if out.numel() < need:
+            raise BtrcError(1, f"render_noalloc: out holds {out.numel()} floats, the film needs {need}")
+        torch.cuda.current_stream(out.device).synchronize()
         st = Stats()
         self._check(self._lib.btrc_render_noalloc(self.handle, scene.handle, spp, _ptr(out), C.byref(st)))
         if stats is not None:

@@ -597,7 +597,11 @@ btrc_status btrc_ctx_create(int device, btrc_ctx **out)
         check_cuda(upload_primes(), "prime table upload");
     });
     if(s == BTRC_OK)
+    {
+        if(device >= 0)
+            noalloc_context_opened(device);
         *out = ctx.release();
+    }
     return s;
 }
 
@@ -628,6 +632,7 @@ void btrc_ctx_destroy(btrc_ctx *ctx)
         cudaFree(ctx->denoise_tmp);
     if(ctx->stream)
         cudaStreamDestroy(ctx->stream);
+    noalloc_context_closed(ctx->device);
     delete ctx;
 }
 
@@ -939,6 +944,19 @@ btrc_status btrc_render_noalloc(btrc_ctx *ctx, btrc_scene *scene, int32_t spp, f
                               "btrc_render_noalloc: film of " + std::to_string(pixels) + " pixels exceeds the " +
                                   std::to_string(noalloc_max_pixels()) + "-pixel limit of its fixed scratch");
         check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+        // k_resolve writes width*height*3 floats through d_rgb_out: it must be device (or
+        // managed) memory of this context's device, never a host address
+        cudaPointerAttributes attr{};
+        if(cudaPointerGetAttributes(&attr, d_rgb_out) != cudaSuccess)
+        {
+            cudaGetLastError();
+            throw StatusError(BTRC_ERR_INVALID_ARG, "btrc_render_noalloc: d_rgb_out is not a CUDA pointer");
+        }
+        if((attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged) ||
+           (attr.type == cudaMemoryTypeDevice && attr.device != ctx->device))
+            throw StatusError(BTRC_ERR_INVALID_ARG,
+                              "btrc_render_noalloc: d_rgb_out must be device memory of device " +
+                                  std::to_string(ctx->device));
         void *scratch = nullptr;
         check_cuda(noalloc_scratch_address(ctx->device, &scratch), "cudaGetSymbolAddress(scratch)");
         ctx->cancel.store(false);
@@ -1036,7 +1054,7 @@ btrc_status btrc_sampler_batch(btrc_ctx *ctx, int32_t type, int32_t width, int32
 btrc_status btrc_bsdf_batch(btrc_ctx *ctx, int32_t op, const float *d_material, const float *d_wo,
                             const float *d_wi_or_u, uint64_t n, float *d_out, void *stream)
 {
-    if(!ctx || (op != 0 && op != 1) || n > 0xffffffffull || (n > 0 && (!d_material || !d_wo || !d_wi_or_u || !d_out)))
+    if(!ctx || op < 0 || op > 2 || n > 0xffffffffull || (n > 0 && (!d_material || !d_wo || !d_wi_or_u || !d_out)))
         return BTRC_ERR_INVALID_ARG;
     return guarded(ctx, [&] {
         require_device(ctx);

@@ -444,6 +444,18 @@ __device__ __forceinline__ bool russian_roulette(V3 &beta, int depth, DSampler &
     return false;
 }
 
+// Seed of the PCG stream that a shadow ray's medium transmittance draws from: a hash of
+// the path's sampler state at the start of the stage that emits the ray (the medium
+// stage for a scattering event, the shade stage for a surface vertex) and of that stage.
+// The stream is then a function of the path alone, not of its queue slot, so a CPU
+// restatement that follows the same sampler streams draws the same transmittance.
+constexpr uint64_t SHADOW_FROM_MEDIUM = 1, SHADOW_FROM_SURFACE = 2;
+
+__device__ __forceinline__ uint64_t shadow_stream_seed(const SamplerState &s, uint64_t stage)
+{
+    return mix_bits(s.a ^ mix_bits(s.b + stage));
+}
+
 // ---------------------------------------------------------------- media
 
 // software trilinear lookup of channel c of an nch-channel grid (x fastest), normalised
@@ -1174,7 +1186,7 @@ __global__ void __launch_bounds__(BLOCK) k_medium(DevScene S, DevRender R, PathS
             SH.d[k] = f4(ls.d, ls.t1);
             SH.beta[k] = f4(ls.li, __int_as_float(smed));
             SamplerState ss;
-            pcg32_seed(ss.a, ss.b, mix_bits((static_cast<uint64_t>(cnt->iterations) << 32) ^ i) ^ pixel, PCG_STREAM);
+            pcg32_seed(ss.a, ss.b, shadow_stream_seed(P.sampler[i], SHADOW_FROM_MEDIUM), PCG_STREAM);
             SH.sampler[k] = ss;
         }
         if(!is_zero(phase))
@@ -1406,8 +1418,7 @@ __global__ void __launch_bounds__(BLOCK, 2) k_shade(DevScene S, DevRender R, Pat
             if(S.has_media)
             {
                 SamplerState ss;
-                pcg32_seed(ss.a, ss.b, mix_bits((static_cast<uint64_t>(cnt->iterations) << 32) ^ i) ^ pixel,
-                           PCG_STREAM);
+                pcg32_seed(ss.a, ss.b, shadow_stream_seed(P.sampler[i], SHADOW_FROM_SURFACE), PCG_STREAM);
                 SH.sampler[k] = ss;
             }
         }
@@ -2202,6 +2213,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 constexpr int NOALLOC_MAX_DEVICES = 64;
 std::mutex g_noalloc_mutex;
 void *g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
+int g_noalloc_contexts[NOALLOC_MAX_DEVICES] = {};   // live btrc contexts per device
 
 } // namespace
 
@@ -2211,7 +2223,26 @@ uint32_t noalloc_max_pixels() { return NOALLOC_MAX_PIXELS; }
 
 // Device address of the scratch array for the current device. The host-side name of a
 // __device__ variable is only a stand-in, so the address is looked up once per device
-// (with that device current) and cached.
+// (with that device current) and cached while a context of this library is alive on that
+// device; when the last one is destroyed the entry is dropped, so a device reset between
+// contexts (which reloads the module and moves the array) cannot leave a stale address.
+void noalloc_context_opened(int device)
+{
+    if(device < 0 || device >= NOALLOC_MAX_DEVICES)
+        return;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    ++g_noalloc_contexts[device];
+}
+
+void noalloc_context_closed(int device)
+{
+    if(device < 0 || device >= NOALLOC_MAX_DEVICES)
+        return;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if(g_noalloc_contexts[device] > 0 && --g_noalloc_contexts[device] == 0)
+        g_noalloc_addr[device] = nullptr;
+}
+
 cudaError_t noalloc_scratch_address(int device, void **out)
 {
     if(device < 0 || device >= NOALLOC_MAX_DEVICES)
@@ -2377,6 +2408,19 @@ __global__ void k_bsdf_batch(int op, const Material *mats, const float *wo, cons
         out[i * 4 + 1] = f.y;
         out[i * 4 + 2] = f.z;
         out[i * 4 + 3] = pdf;
+    }
+    else if(op == 2)
+    {
+        // the sampled direction alone, before Disney's bad-sample rejection
+        V3 lwi(0.0f);
+        const bool ok = comp_sample_dir(e, lwo, wu[i * 3 + 0], wu[i * 3 + 1], wu[i * 3 + 2], lwi);
+        out[i * 7 + 0] = ok ? 1.0f : 0.0f;
+        out[i * 7 + 1] = 0.0f;
+        out[i * 7 + 2] = 0.0f;
+        out[i * 7 + 3] = 0.0f;
+        out[i * 7 + 4] = ok ? lwi.x : 0.0f;
+        out[i * 7 + 5] = ok ? lwi.y : 0.0f;
+        out[i * 7 + 6] = ok ? lwi.z : 0.0f;
     }
     else
     {

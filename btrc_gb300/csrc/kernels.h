@@ -78,6 +78,8 @@ size_t noalloc_scratch_bytes();
 uint32_t noalloc_max_states();
 uint32_t noalloc_max_pixels();
 cudaError_t noalloc_scratch_address(int device, void **out);
+void noalloc_context_opened(int device);
+void noalloc_context_closed(int device);
 cudaError_t render_wavefront_noalloc(const DevScene &S, const DevRender &R, void *scratch, float *rgb_out,
                                      cudaStream_t st, const std::atomic<bool> *cancel, RenderStats *stats,
                                      bool *cancelled);

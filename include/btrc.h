@@ -180,7 +180,15 @@ btrc_status btrc_render(btrc_ctx *ctx, btrc_scene *scene, const btrc_render_opts
    array, so calls that overlap on the GPU (other threads, other contexts on the same
    device) race and must be serialised by the caller. The first call on a device looks
    up the array's device address (cudaGetSymbolAddress); make that first call before any
-   stream capture. spp 0 uses the scene's renderer.spp. */
+   stream capture. The address is kept while a context is alive on the device and
+   dropped with the last one, so do not reset the device (cudaDeviceReset) while a
+   context is alive. spp 0 uses the scene's renderer.spp.
+   The render runs on the context's own stream, unordered with the caller's streams:
+   finish pending work that writes d_rgb_out before the call. d_rgb_out must be device
+   (or managed) memory of the context's device, else BTRC_ERR_INVALID_ARG.
+   Differences from btrc_render: the scene's post_processors are not run, no albedo /
+   normal g-buffers are produced, and at most 32768 paths are in flight whatever the
+   scene's renderer.state_count (the image is the same, rendered in more waves). */
 btrc_status btrc_render_noalloc(btrc_ctx *ctx, btrc_scene *scene, int32_t spp, float *d_rgb_out, btrc_stats *stats);
 
 /* ACESToneMap::process (src/builtin/btrc/builtin/postprocess/tonemap.cpp:86-101): in place
@@ -239,7 +247,10 @@ btrc_status btrc_sampler_batch(btrc_ctx *ctx, int32_t type, int32_t width, int32
    material: 16 floats per record, layout of the scene's material parameters with the
    material type in record[15] (0 diffuse, 1 metal, 2 disney).
    op 0 (eval/pdf): wo, wi: 3 floats each; out: 4 floats (f.rgb, pdf)
-   op 1 (sample)  : wo: 3 floats, u: 3 floats; out: 7 floats (f.rgb, pdf, wi.xyz) */
+   op 1 (sample)  : wo: 3 floats, u: 3 floats; out: 7 floats (f.rgb, pdf, wi.xyz)
+   op 2 (direction): as op 1, but only the sampled direction, before Disney's bad-sample
+                    rejection; out: 7 floats (1 if a direction was drawn else 0, 0, 0, 0,
+                    wi.xyz), for statistical tests of the sampling density against pdf */
 btrc_status btrc_bsdf_batch(btrc_ctx *ctx, int32_t op, const float *d_material, const float *d_wo,
                             const float *d_wi_or_u, uint64_t n, float *d_out, void *stream);
 

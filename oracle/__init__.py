@@ -139,7 +139,8 @@ def murmur64a(data: bytes, seed: int = 0) -> int:
 
 def bsdf_batch(op: int, material: np.ndarray, wo: np.ndarray, wi_or_u: np.ndarray, fp32: bool = False) -> np.ndarray:
     """Local-space BSDF in FP64 (or the same code in FP32). material: (n, 16) float32,
-    type in column 15. op 0: (f.rgb, pdf); op 1: (f.rgb, pdf, wi.xyz)."""
+    type in column 15. op 0: (f.rgb, pdf); op 1: (f.rgb, pdf, wi.xyz); op 2 (FP64 only):
+    (drawn, 0, 0, 0, wi.xyz), the sampled direction before Disney's bad-sample rejection."""
     material = np.ascontiguousarray(material, np.float32)
     wo = np.ascontiguousarray(wo, np.float64)
     wu = np.ascontiguousarray(wi_or_u, np.float64)

@@ -17,7 +17,11 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 ORACLE_LIB = HERE / "_build" / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libref_bvh.so"
-REFERENCE_BVH_INCLUDE = Path(os.environ.get("BTRC_REFERENCE_ROOT", "/root/reference")) / "lib" / "bvh" / "include"
+# The reference tree: $BTRC_REFERENCE_ROOT, else a checkout named "reference" beside this
+# repository. Absent (as on a machine without the reference), lib/bvh is simply not built.
+REFERENCE_ROOT = Path(os.environ["BTRC_REFERENCE_ROOT"]) if os.environ.get("BTRC_REFERENCE_ROOT") \
+    else HERE.parent.parent / "reference"
+REFERENCE_BVH_INCLUDE = REFERENCE_ROOT / "lib" / "bvh" / "include"
 
 FLAGS = ["-O2", "-std=c++17", "-fPIC", "-shared", "-pthread", "-ffp-contract=off"]
 

@@ -711,6 +711,9 @@ struct Sampler
         index = index + static_cast<uint64_t>(sample) * static_cast<uint64_t>(hc.stride);
         dim = 2;
     }
+    // the 16-byte state as the GPU stores it: independent (PCG state, inc), halton (index, dim)
+    uint64_t word_a() const { return type == 0 ? pcg.state : index; }
+    uint64_t word_b() const { return type == 0 ? pcg.inc : static_cast<uint64_t>(dim); }
     float halton(uint32_t d) const
     {
         return owen_radical_inverse(static_cast<int>(d), index, mix_bits(static_cast<uint64_t>(1u + (d << 4))));
@@ -1252,10 +1255,11 @@ struct Mat
         r.f = disney_eval(wi, wo);
         r.pdf = disney_pdf(wi, wo);
         V<T> v = r.f * (std::abs(wi.z) / r.pdf);
-        if(std::max(std::max(v.x, v.y), v.z) > T(10))
+        if(!keep_bad && std::max(std::max(v.x, v.y), v.z) > T(10))
             return CS<T>();
         return r;
     }
+    bool keep_bad = false;  // test hook: skip handle_bad_sample to expose the raw sampling density
 
     // ---- component dispatch (diffuse.cpp:10-60, metal, disney)
     CS<T> sample(V<T> wo, T s0, T s1, T s2) const
@@ -2183,7 +2187,16 @@ struct Shadow
     V3f o, d, beta;
     float t1 = 0;
     int medium = 0;
+    uint64_t seed = 0;  // seed of the PCG stream its medium transmittance draws from
 };
+
+// Shadow-ray transmittance stream (the GPU kernels' rule, not the reference's one stream
+// per shadow slot of W/soa_buffer.cpp:86-96): PCG seeded by a hash of the path's sampler
+// state at the start of the emitting stage (1 medium scattering, 2 surface vertex).
+inline uint64_t shadow_stream_seed(uint64_t a, uint64_t b, uint64_t stage)
+{
+    return mix_bits(a ^ mix_bits(b + stage));
+}
 
 void trace_path(const Prepared &P, uint64_t g, double *film, double *aov = nullptr)
 {
@@ -2224,8 +2237,6 @@ void trace_path(const Prepared &P, uint64_t g, double *film, double *aov = nullp
     float bsdf_pdf = -1.0f;
     int depth = 0;
     const int NL = nlights_total(S);
-    PcgSmp shadow_rng;
-    shadow_rng.p.seed(mix_bits(g), PCG_STREAM);
 
     for(;;)
     {
@@ -2262,6 +2273,7 @@ void trace_path(const Prepared &P, uint64_t g, double *film, double *aov = nullp
             const Med m = medium(S, medium_id);
             if(m.type != 0)
             {
+                const uint64_t stage_a = smp.word_a(), stage_b = smp.word_b();
                 V3f spos, pcolor;
                 float pg = 0.0f;
                 const bool sc = medium_sample(S, m, o, end, smp, spos, pcolor, pg);
@@ -2308,6 +2320,7 @@ void trace_path(const Prepared &P, uint64_t g, double *film, double *aov = nullp
                             sh.t1 = ls.t1;
                             sh.beta = ls.li;
                             sh.medium = ls.t1 > 1 ? S.vacuum_medium : medium_id;
+                            sh.seed = shadow_stream_seed(stage_a, stage_b, 1);
                         }
                         if(!zero3(phase))
                         {
@@ -2327,6 +2340,7 @@ void trace_path(const Prepared &P, uint64_t g, double *film, double *aov = nullp
         }
 
         // ---------------- shade stage (shade.cpp:29-235)
+        const uint64_t shade_a = smp.word_a(), shade_b = smp.word_b();
         if(!h.hit)
         {
             V3f le(0.0f);
@@ -2569,6 +2583,7 @@ void trace_path(const Prepared &P, uint64_t g, double *film, double *aov = nullp
                         sh.medium = sout == lout ? ray_medium : (sout ? S.inst_outer[inst] : S.inst_inner[inst]);
                         const float c = std::fabs(dot(nrm(ls.d), gf.z));
                         sh.beta = ls.li * beta * sf * c / (spdf + ls.pdf);
+                        sh.seed = shadow_stream_seed(shade_a, shade_b, 2);
                     }
                     if(zero3(bs.f))
                         splat(film, S.width, px, py, rad);
@@ -2597,6 +2612,8 @@ void trace_path(const Prepared &P, uint64_t g, double *film, double *aov = nullp
                 V3f b = sh.beta;
                 if(P.has_media)
                 {
+                    PcgSmp shadow_rng;
+                    shadow_rng.p.seed(sh.seed, PCG_STREAM);
                     if(sh.t1 > 1)
                         b = b * medium_tr(S, medium(S, S.vacuum_medium), sh.o, sh.o + nrm(sh.d) * S.world_diagonal,
                                           shadow_rng);
@@ -2716,6 +2733,18 @@ void oracle_bsdf_batch(int op, const float *mat, const double *wo, const double 
             out[i * 4 + 1] = f.y;
             out[i * 4 + 2] = f.z;
             out[i * 4 + 3] = M.pdf(lwi, lwo);
+        }
+        else if(op == 2)
+        {
+            // the sampled direction alone, before Disney's bad-sample rejection
+            M.keep_bad = true;
+            const CS<double> s = M.sample(lwo, wu[i * 3], wu[i * 3 + 1], wu[i * 3 + 2]);
+            const bool ok = !(s.dir.x == 0 && s.dir.y == 0 && s.dir.z == 0);
+            out[i * 7 + 0] = ok ? 1.0 : 0.0;
+            out[i * 7 + 1] = out[i * 7 + 2] = out[i * 7 + 3] = 0.0;
+            out[i * 7 + 4] = s.dir.x;
+            out[i * 7 + 5] = s.dir.y;
+            out[i * 7 + 6] = s.dir.z;
         }
         else
         {

@@ -215,3 +215,19 @@ def test_procedural_geometry_matches_oracle(native_lib, tmp_path):
     assert np.array_equal(ids[order_p], S.ids[order_o])
     assert np.array_equal(xyz[order_p].view(np.uint32), S.tris[order_o].view(np.uint32))
     ctx.close()
+
+
+def test_render_noalloc_rejects_host_or_short_outputs(native_lib, tmp_path):
+    """k_resolve writes H*W*3 floats through the allocation-free entry point's output
+    pointer, so the Python mirror refuses anything but a large enough float32 CUDA tensor
+    before the library is called (no launch happens; a host-only context suffices)."""
+    torch = pytest.importorskip("torch")
+    p = _write(tmp_path, "s.json", _minimal(tmp_path))
+    ctx = B.Context(-1)
+    sc = ctx.load_scene(p).build()
+    for bad in (np.zeros((6, 8, 3), np.float32), torch.zeros((6, 8, 3), dtype=torch.float32)):
+        with pytest.raises(B.BtrcError) as e:
+            ctx.render_noalloc(sc, bad)
+        assert e.value.status == 1 and "CUDA tensor" in str(e.value)
+    sc.close()
+    ctx.close()

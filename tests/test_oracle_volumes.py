@@ -63,3 +63,17 @@ def test_byte_text_grid_reads_characters(tmp_path):
     from oracle.scene import _grid, _to_node
     _c, g = _grid(_to_node({"type": "array", "text": str(tmp_path / "g.txt")}), str(tmp_path))
     assert np.allclose(g.ravel(), [1.0, 64 / 127.0])
+
+
+def test_oracle_ratio_tracking_linear_grid(tmp_path):
+    """The oracle's heterogeneous-medium ratio tracking (builtin/btrc/builtin/medium/
+    hetergeneous.cpp:75-106) behind a transform medium: along a density linear in x, y
+    and z its mean estimate is exp(-length * sigma(midpoint))."""
+    from tests.util import ramp_medium_scene, ramp_segments, ramp_tr_exact
+    S = OS.Scene(ramp_medium_scene(tmp_path))
+    n = 60000
+    for s in ramp_segments():
+        seg = np.tile(s.astype(np.float32), (n, 1))
+        tr = S.medium_tr(0, seg, np.arange(n, dtype=np.uint64) * 7919 + 3).astype(np.float64)
+        want = float(ramp_tr_exact(s.astype(np.float32).astype(np.float64)))
+        assert abs(tr.mean() - want) < 4.5 * tr.std() / np.sqrt(n), (s, tr.mean(), want)
