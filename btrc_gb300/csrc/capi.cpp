@@ -233,37 +233,40 @@ void build_scene(btrc_scene *sc, int threads)
         free_all(sc->allocs);
     }
 
-    // flatten instances into world-space triangles (single-level BVH)
-    std::vector<TriRec> world;
-    world.reserve(H.triangle_count);
-    sc->export_xyz.clear();
-    sc->export_ids.clear();
+    if(threads <= 0)
+        threads = static_cast<int>(std::max(1u, std::thread::hardware_concurrency()));
+    TaskPool pool(threads);
+
+    // flatten instances into world-space triangles (single-level BVH), in parallel over
+    // triangle ranges of each instance
+    std::vector<size_t> inst_first(H.instances.size() + 1, 0);
+    for(size_t i = 0; i < H.instances.size(); ++i)
+        inst_first[i + 1] = inst_first[i] + H.geometries[H.instances[i].geometry].area.size();
+    std::vector<TriRec> world(inst_first.back());
+    sc->export_xyz.assign(world.size() * 9, 0.0f);
+    sc->export_ids.assign(world.size() * 2, 0u);
     for(size_t i = 0; i < H.instances.size(); ++i)
     {
         const HostGeometry &g = H.geometries[H.instances[i].geometry];
         const Transform &xf = H.instance_xf[i];
-        const size_t nt = g.area.size();
-        for(size_t t = 0; t < nt; ++t)
-        {
-            const V3 a = xf.point(g.pos[t * 3 + 0]);
-            const V3 b = xf.point(g.pos[t * 3 + 1]);
-            const V3 c = xf.point(g.pos[t * 3 + 2]);
-            TriRec r{ a.x, a.y, a.z, static_cast<uint32_t>(i), b.x, b.y, b.z, static_cast<uint32_t>(t),
-                      c.x, c.y, c.z, 0u };
-            world.push_back(r);
-        }
+        const size_t base = inst_first[i];
+        pool.parallel_for(g.area.size(), 1u << 14, [&, i, base](size_t tb, size_t te) {
+            for(size_t t = tb; t < te; ++t)
+            {
+                const V3 a = xf.point(g.pos[t * 3 + 0]);
+                const V3 b = xf.point(g.pos[t * 3 + 1]);
+                const V3 c = xf.point(g.pos[t * 3 + 2]);
+                const size_t k = base + t;
+                world[k] = TriRec{ a.x, a.y, a.z, static_cast<uint32_t>(i), b.x, b.y, b.z, static_cast<uint32_t>(t),
+                                   c.x, c.y, c.z, 0u };
+                const float v[9] = { a.x, a.y, a.z, b.x, b.y, b.z, c.x, c.y, c.z };
+                std::memcpy(&sc->export_xyz[k * 9], v, sizeof(v));
+                sc->export_ids[k * 2] = static_cast<uint32_t>(i);
+                sc->export_ids[k * 2 + 1] = static_cast<uint32_t>(t);
+            }
+        });
     }
-    CWBVH bvh = build_cwbvh(world, threads);
-    sc->export_xyz.resize(world.size() * 9);
-    sc->export_ids.resize(world.size() * 2);
-    for(size_t k = 0; k < world.size(); ++k)
-    {
-        const TriRec &r = world[k];
-        const float v[9] = { r.v0x, r.v0y, r.v0z, r.v1x, r.v1y, r.v1z, r.v2x, r.v2y, r.v2z };
-        std::memcpy(&sc->export_xyz[k * 9], v, sizeof(v));
-        sc->export_ids[k * 2] = r.inst;
-        sc->export_ids[k * 2 + 1] = r.prim;
-    }
+    CWBVH bvh = build_cwbvh(world, pool);
     world.clear();
     world.shrink_to_fit();
     sc->bvh_nodes = static_cast<int>(bvh.nodes.size());
@@ -313,12 +316,18 @@ void build_scene(btrc_scene *sc, int threads)
     }
     {
         // interleave the per-geometry component arrays into one record per triangle
-        std::vector<F4> rec;
-        rec.reserve(total * SHADE_F4);
+        std::vector<F4> rec(total * SHADE_F4);
+        size_t first = 0;
         for(auto &g : H.geometries)
-            for(size_t i = 0; i < g.shade[0].size(); ++i)
-                for(int k = 0; k < SHADE_F4; ++k)
-                    rec.push_back(g.shade[k][i]);
+        {
+            F4 *dst = rec.data() + first * SHADE_F4;
+            pool.parallel_for(g.shade[0].size(), 1u << 14, [&g, dst](size_t b, size_t e) {
+                for(size_t i = b; i < e; ++i)
+                    for(int k = 0; k < SHADE_F4; ++k)
+                        dst[i * SHADE_F4 + k] = g.shade[k][i];
+            });
+            first += g.shade[0].size();
+        }
         D.shade = dev_upload(sc->allocs, rec.data(), rec.size());
     }
     std::vector<F4> lpos;

@@ -1,4 +1,5 @@
 #include "scene.h"
+#include "taskpool.h"
 
 #include <algorithm>
 #include <array>
@@ -10,6 +11,7 @@
 #include <map>
 #include <numeric>
 #include <stdexcept>
+#include <thread>
 
 namespace bt {
 
@@ -344,80 +346,194 @@ HostGeometry geometry_from_arrays(const std::string &name, std::vector<V3> posit
                                   const std::vector<float> &uvs, const std::vector<ObjIndex> &corners,
                                   bool to_unit_cube);
 
-HostGeometry load_obj(const std::string &filename, bool to_unit_cube)
+namespace {
+
+// One line-aligned piece of an OBJ file: what it holds (first pass) and where its
+// records go in the whole file's arrays (second pass).
+struct ObjChunk
 {
-    std::ifstream fin(filename, std::ios::binary);
-    if(!fin)
-        throw std::runtime_error("cannot open obj file '" + filename + "'");
-    std::string text((std::istreambuf_iterator<char>(fin)), std::istreambuf_iterator<char>());
+    const char *begin, *end;
+    size_t nv = 0, nvn = 0, nvt = 0, ncorner = 0;    // counts in this chunk
+    size_t v0 = 0, vn0 = 0, vt0 = 0, corner0 = 0;    // records before this chunk
+    std::string error;
+};
 
-    std::vector<V3> positions, normals;
-    std::vector<float> uvs;
-    std::vector<ObjIndex> corners;  // 3 per triangle, already resolved to 0-based (-1 absent)
-    positions.reserve(text.size() / 64);
-    corners.reserve(text.size() / 16);
+inline bool is_v(const char *l) { return l[0] == 'v' && (l[1] == ' ' || l[1] == '\t'); }
+inline bool is_f(const char *l) { return l[0] == 'f' && (l[1] == ' ' || l[1] == '\t'); }
 
-    const char *p = text.c_str();
-    const char *end = p + text.size();
-    std::vector<ObjIndex> face;
-    while(p < end)
+// vertices of a face line (without parsing the numbers)
+size_t face_vertex_count(const char *q, const char *eol)
+{
+    size_t n = 0;
+    for(;;)
+    {
+        q = skip_spaces(q);
+        if(q >= eol || *q == '\r' || *q == '\n')
+            return n;
+        ++n;
+        while(q < eol && *q != ' ' && *q != '\t' && *q != '\r' && *q != '\n')
+            ++q;
+    }
+}
+
+void obj_count(ObjChunk &c)
+{
+    for(const char *p = c.begin; p < c.end;)
     {
         const char *line = skip_spaces(p);
-        const char *eol = static_cast<const char *>(std::memchr(line, '\n', end - line));
+        const char *eol = static_cast<const char *>(std::memchr(line, '\n', c.end - line));
         if(!eol)
-            eol = end;
-        if(line[0] == 'v' && (line[1] == ' ' || line[1] == '\t'))
+            eol = c.end;
+        if(is_v(line))
+            ++c.nv;
+        else if(line[0] == 'v' && line[1] == 'n')
+            ++c.nvn;
+        else if(line[0] == 'v' && line[1] == 't')
+            ++c.nvt;
+        else if(is_f(line))
+        {
+            const size_t k = face_vertex_count(line + 2, eol);
+            if(k >= 3)
+                c.ncorner += 3 * (k - 2);
+        }
+        p = eol + 1;
+    }
+}
+
+void obj_parse(ObjChunk &c, V3 *positions, V3 *normals, float *uvs, ObjIndex *corners)
+{
+    size_t nv = c.v0, nvn = c.vn0, nvt = c.vt0, nc = c.corner0;
+    ObjIndex face[64];
+    std::vector<ObjIndex> big;
+    for(const char *p = c.begin; p < c.end;)
+    {
+        const char *line = skip_spaces(p);
+        const char *eol = static_cast<const char *>(std::memchr(line, '\n', c.end - line));
+        if(!eol)
+            eol = c.end;
+        if(is_v(line))
         {
             char *e;
-            float x = std::strtof(line + 2, &e);
-            float y = std::strtof(e, &e);
-            float z = std::strtof(e, &e);
-            positions.emplace_back(x, y, z);
+            const float x = std::strtof(line + 2, &e);
+            const float y = std::strtof(e, &e);
+            const float z = std::strtof(e, &e);
+            positions[nv++] = V3(x, y, z);
         }
         else if(line[0] == 'v' && line[1] == 'n')
         {
             char *e;
-            float x = std::strtof(line + 3, &e);
-            float y = std::strtof(e, &e);
-            float z = std::strtof(e, &e);
-            normals.emplace_back(x, y, z);
+            const float x = std::strtof(line + 3, &e);
+            const float y = std::strtof(e, &e);
+            const float z = std::strtof(e, &e);
+            normals[nvn++] = V3(x, y, z);
         }
         else if(line[0] == 'v' && line[1] == 't')
         {
             char *e;
-            float u = std::strtof(line + 3, &e);
-            float v = std::strtof(e, &e);
-            uvs.push_back(u);
-            uvs.push_back(v);
+            const float u = std::strtof(line + 3, &e);
+            const float v = std::strtof(e, &e);
+            uvs[2 * nvt] = u;
+            uvs[2 * nvt + 1] = v;
+            ++nvt;
         }
-        else if(line[0] == 'f' && (line[1] == ' ' || line[1] == '\t'))
+        else if(is_f(line))
         {
-            face.clear();
+            const size_t k = face_vertex_count(line + 2, eol);
+            ObjIndex *f = face;
+            if(k > 64)
+            {
+                big.resize(k);
+                f = big.data();
+            }
             const char *q = line + 2;
-            for(;;)
+            for(size_t j = 0; j < k; ++j)
             {
                 q = skip_spaces(q);
-                if(q >= eol || *q == '\r' || *q == '\n')
-                    break;
-                ObjIndex oi;
-                if(!parse_obj_index(q, oi))
-                    throw std::runtime_error("bad face in obj file '" + filename + "'");
-                oi.v = resolve_obj(oi.v, positions.size());
-                oi.vt = resolve_obj(oi.vt, uvs.size() / 2);
-                oi.vn = resolve_obj(oi.vn, normals.size());
-                face.push_back(oi);
+                if(!parse_obj_index(q, f[j]))
+                {
+                    c.error = "bad face";
+                    return;
+                }
+                // negative indices count back from the records read so far
+                f[j].v = resolve_obj(f[j].v, nv);
+                f[j].vt = resolve_obj(f[j].vt, nvt);
+                f[j].vn = resolve_obj(f[j].vn, nvn);
             }
-            if(face.size() < 3)
-                throw std::runtime_error("invalid obj face vertex count in '" + filename + "'");
-            for(size_t k = 1; k + 1 < face.size(); ++k)
+            if(k < 3)
             {
-                corners.push_back(face[0]);
-                corners.push_back(face[k]);
-                corners.push_back(face[k + 1]);
+                c.error = "invalid obj face vertex count";
+                return;
+            }
+            for(size_t j = 1; j + 1 < k; ++j)
+            {
+                corners[nc++] = f[0];
+                corners[nc++] = f[j];
+                corners[nc++] = f[j + 1];
             }
         }
         p = eol + 1;
     }
+}
+
+} // namespace
+
+// OBJ meshes are parsed in two passes over line-aligned pieces of the file, in
+// parallel: the first counts the records of each piece, the second parses every piece
+// into its place (negative indices resolve against the records before the face, as in
+// a sequential read), so the result does not depend on the number of threads.
+HostGeometry load_obj(const std::string &filename, bool to_unit_cube)
+{
+    std::ifstream fin(filename, std::ios::binary | std::ios::ate);
+    if(!fin)
+        throw std::runtime_error("cannot open obj file '" + filename + "'");
+    std::string text(static_cast<size_t>(fin.tellg()), '\0');
+    fin.seekg(0);
+    fin.read(&text[0], static_cast<std::streamsize>(text.size()));
+
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t pieces = std::max<size_t>(1, std::min<size_t>(hw * 4, text.size() / (1u << 18)));
+    std::vector<ObjChunk> chunks;
+    const char *base = text.data(), *tend = base + text.size();
+    const char *p = base;
+    for(size_t k = 0; k < pieces && p < tend; ++k)
+    {
+        const char *e = k + 1 == pieces ? tend : std::min(tend, base + text.size() * (k + 1) / pieces);
+        if(e < tend)
+        {
+            const char *nl = static_cast<const char *>(std::memchr(e, '\n', tend - e));
+            e = nl ? nl + 1 : tend;
+        }
+        if(e > p)
+            chunks.push_back(ObjChunk{ p, e });
+        p = e;
+    }
+    TaskPool pool(static_cast<int>(std::min<size_t>(hw, chunks.size())));
+    pool.parallel_for(chunks.size(), 1, [&](size_t b, size_t e) {
+        for(size_t k = b; k < e; ++k)
+            obj_count(chunks[k]);
+    });
+    size_t nv = 0, nvn = 0, nvt = 0, nc = 0;
+    for(auto &c : chunks)
+    {
+        c.v0 = nv;
+        c.vn0 = nvn;
+        c.vt0 = nvt;
+        c.corner0 = nc;
+        nv += c.nv;
+        nvn += c.nvn;
+        nvt += c.nvt;
+        nc += c.ncorner;
+    }
+    std::vector<V3> positions(nv), normals(nvn);
+    std::vector<float> uvs(2 * nvt);
+    std::vector<ObjIndex> corners(nc);  // 3 per triangle, already resolved to 0-based (-1 absent)
+    pool.parallel_for(chunks.size(), 1, [&](size_t b, size_t e) {
+        for(size_t k = b; k < e; ++k)
+            obj_parse(chunks[k], positions.data(), normals.data(), uvs.data(), corners.data());
+    });
+    for(auto &c : chunks)
+        if(!c.error.empty())
+            throw std::runtime_error(c.error + " in obj file '" + filename + "'");
 
     for(auto &c : corners)
     {
@@ -467,8 +583,10 @@ HostGeometry geometry_from_arrays(const std::string &name, std::vector<V3> posit
         g.bmin = vmin(g.bmin, q);
         g.bmax = vmax(g.bmax, q);
     }
-    double total = 0;
-    for(size_t i = 0; i < ntri; ++i)
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    TaskPool pool(ntri >= (1u << 16) ? static_cast<int>(hw) : 1);
+    pool.parallel_for(ntri, 1u << 13, [&](size_t tb, size_t te) {
+    for(size_t i = tb; i < te; ++i)
     {
         const ObjIndex *c = &corners[i * 3];
         const V3 a = positions[c[0].v], b = positions[c[1].v], cc = positions[c[2].v];
@@ -511,8 +629,11 @@ HostGeometry geometry_from_arrays(const std::string &name, std::vector<V3> posit
         g.shade[4][i] = { sba.x, sba.y, sba.z, tv[1] - tv[0] };
         g.shade[5][i] = { sca.x, sca.y, sca.z, tv[2] - tv[0] };
         g.area[i] = 0.5f * length(cross(b - a, cc - a));
-        total += g.area[i];
     }
+    });
+    double total = 0;
+    for(size_t i = 0; i < ntri; ++i)
+        total += g.area[i];
     g.total_area = static_cast<float>(total);
     return g;
 }
