@@ -51,6 +51,10 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched uneven-scenes measurement")
     ap.add_argument("--nrc-frames", type=int, default=256, help="frames of the radiance-cache study")
     ap.add_argument("--ref-spp", type=int, default=4096, help="spp of the converged reference image")
+    ap.add_argument("--probe", choices=["nrc", "medium", "generate", "trace"],
+                    help="run one small profiling case and exit: nrc (cache inference on 2^20 queries and "
+                         "training steps of 16,384 samples), medium (volume workload at 256x256, 4 spp), "
+                         "generate / trace (terrain at 1920x1080, 1 spp, 2 M-state queue)")
     ap.add_argument("--trace-probe", action="store_true",
                     help="trace the workload's camera rays, then one diffuse bounce ray per camera hit, "
                          "through btrc_trace_closest (two launches, for DRAM-traffic captures) and exit")
@@ -597,8 +601,50 @@ def trace_probe(args):
     ctx.close()
 
 
+def probe(args):
+    """Small cases for ncu captures (a few GB on the device at most, few launches)."""
+    import torch
+    import btrc_gb300 as B
+    from btrc_gb300 import scenes
+    ctx = B.Context(0)
+    if args.probe == "nrc":
+        p = scenes.terrain(width=480, height=270, spp=1, grid=256, instances=20)
+        sc = ctx.load_scene(p).build()
+        info = sc.info()
+        cache = B.RadianceCache(ctx, info.world_min, info.world_max, seed=1)
+        nq = 1 << 20
+        g = torch.Generator(device="cuda").manual_seed(0)
+        q = torch.rand((nq, 13), device="cuda", generator=g)
+        lo, hi = torch.tensor(info.world_min, device="cuda"), torch.tensor(info.world_max, device="cuda")
+        q[:, 0:3] = lo + (hi - lo) * q[:, 0:3]
+        q[:, 3:9] = q[:, 3:9] * 2 - 1
+        pred = torch.empty((nq, 4), device="cuda")
+        tb = torch.cat([q[:16384], torch.rand((16384, 3), device="cuda", generator=g)], 1).contiguous()
+        for _ in range(3):
+            cache.infer(q, nq, pred)
+            cache.train(tb, 16384)
+        torch.cuda.synchronize()
+        cache.close()
+    else:
+        if args.probe == "medium":
+            p = scenes.volume(width=256, height=256, spp=4, state_count=1 << 20)
+        else:
+            p = scenes.terrain(width=1920, height=1080, spp=1, state_count=1 << 21)
+        sc = ctx.load_scene(p).build()
+        info = sc.info()
+        img = torch.empty((info.height, info.width, 3), device="cuda")
+        st = {}
+        ctx.render(sc, out=img, stats=st)
+        torch.cuda.synchronize()
+        print(json.dumps({k: v for k, v in st.items() if k not in ("stage_ms", "stage_launches")}), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
+    if args.probe:
+        probe(args)
+        return
     if args.trace_probe:
         trace_probe(args)
         return
