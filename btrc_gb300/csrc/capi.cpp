@@ -1320,6 +1320,7 @@ btrc_status btrc_render_nrc_frame(btrc_ctx *ctx, btrc_scene *scene, btrc_nrc *nr
             check_cuda(cudaMemcpyAsync(rgb_out, rgb_dev, pixels * 3 * sizeof(float), cudaMemcpyDeviceToHost, s),
                        "image download");
         check_cuda(cudaStreamSynchronize(s), "frame sync");
+        check_cuda(nrc->impl->check_error(s), "radiance cache tensor-core kernel");
         if(fstats)
         {
             fstats->paths = rs.paths;

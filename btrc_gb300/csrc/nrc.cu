@@ -12,7 +12,9 @@
 // table with float2 atomics, and finishes with FP32 Adam over all parameters.
 #include "nrc.h"
 
+#include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <stdexcept>
 #include <vector>
@@ -336,6 +338,308 @@ __global__ void __launch_bounds__(NRC_BLOCK) k_nrc_infer(NrcDev D, const float *
         }
         __syncwarp();
     }
+}
+
+// ------------------------------------------------------------------ inference on tcgen05
+//
+// The same network on the 5th-generation tensor cores. A block of 1024 threads holds the
+// weights (45 KB) in shared memory once and runs eight independent groups of 128
+// threads; each group takes 128 queries at a time: every thread encodes one query
+// (16 hash levels, the two SH bands, the material inputs) straight into shared memory in
+// the UMMA canonical K-major layout (8-row x 16-byte core matrices), one thread issues
+// each layer as tcgen05.mma (M = 128, N = 64 or 16, K = 16 per instruction, BF16 x BF16
+// -> FP32) into the group's 64 tensor-memory columns, and the group's four warps read the
+// accumulator back with tcgen05.ld (warp w: lanes 32 (w % 4)..), apply ReLU, round to
+// BF16 and write the next layer's operand over the previous one. The groups run out of
+// step, so one group's hash gathers overlap another's MMAs; 32 warps per SM keep the
+// gathers in flight. Every wait on an MMA completion barrier is bounded; on a timeout the
+// group records an error and leaves, and the block releases its tensor memory.
+
+constexpr int TC_GROUPS = 8;
+constexpr int TC_ROWS = 128;                              // rows per group tile (MMA M)
+constexpr int TC_BLOCK = TC_ROWS * TC_GROUPS;             // 1024 threads, one block per SM
+constexpr uint32_t TC_GROUP_COLS = 64;                    // FP32 accumulator columns per group
+constexpr uint32_t TC_TMEM_COLS = TC_GROUP_COLS * TC_GROUPS;  // all 512 columns of the SM
+constexpr uint32_t TC_W_BYTES = NRC_WEIGHTS * 2;          // all layers, canonical layout
+constexpr uint32_t TC_A_BYTES = TC_ROWS * NRC_IN * 2;     // one group's operand (80 columns at most)
+
+// byte offset of layer l in the canonical weight image: W_l^T as N x K, K-major
+__host__ __device__ constexpr uint32_t tc_w_offset(int l) { return static_cast<uint32_t>(w_offset(l)) * 2u; }
+// byte offset of element (row r, column k) of an R x K K-major operand in core matrices:
+// 16 bytes of 8 consecutive k per row, 8 rows per 128-byte core matrix, core matrices
+// along K adjacent (128 bytes apart), 8-row groups K * 16 bytes apart
+__host__ __device__ constexpr uint32_t tc_offset(int r, int k, int K)
+{
+    return static_cast<uint32_t>((r >> 3) * (K * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// shared-memory matrix descriptor, no swizzle: start, leading (K-direction core matrix
+// stride) and stride (8-row group stride) byte offsets, descriptor version 1
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    return static_cast<uint64_t>((saddr >> 4) & 0x3fffu) | (static_cast<uint64_t>((lbo >> 4) & 0x3fffu) << 16) |
+           (static_cast<uint64_t>((sbo >> 4) & 0x3fffu) << 32) | (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major
+__host__ __device__ constexpr uint32_t tc_idesc(int M, int N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(N >> 3) << 17) |
+           (static_cast<uint32_t>(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate)
+{
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+                 :
+                 : "r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t mbar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+__device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// wait for phase `parity` of the barrier, at most ~1 s; false on timeout
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity)
+{
+    const uint64_t t0 = global_ns();
+    for(uint32_t it = 0;; ++it)
+    {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}\n"
+                     : "=r"(done)
+                     : "r"(mbar), "r"(parity)
+                     : "memory");
+        if(done)
+            return true;
+        if((it & 1023u) == 1023u && global_ns() - t0 > 1000000000ull)
+            return false;
+        if(it > 64)
+            __nanosleep(32);
+    }
+}
+
+// 16 consecutive FP32 columns of this warp's 32 TMEM lanes (one row per thread)
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                 "[%16];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                   "=r"(r[15])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+    for(int k = 0; k < 16; ++k)
+        v[k] = __uint_as_float(r[k]);
+}
+
+__device__ __forceinline__ void tc_ld4(uint32_t taddr, float (&v)[4])
+{
+    uint32_t r[4];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+    for(int k = 0; k < 4; ++k)
+        v[k] = __uint_as_float(r[k]);
+}
+
+// a query's 80 inputs (the columns of encode_half) written as the ten 16-byte chunks of
+// row m of a canonical 128 x 80 operand
+__device__ __forceinline__ void encode_row_tc(const NrcDev &D, const float *q, unsigned char *a, int m)
+{
+    const V3 p = nrc_unit_pos(D, q);
+    unsigned char *row = a + tc_offset(m, 0, NRC_IN);
+#pragma unroll 1
+    for(int chunk = 0; chunk < 4; ++chunk)
+    {
+        // levels 4 chunk .. 4 chunk + 3: columns 8 chunk .. 8 chunk + 7
+        uint32_t w4[4];
+#pragma unroll
+        for(int j = 0; j < 4; ++j)
+        {
+            uint32_t idx[8];
+            float w[8];
+            level_corners(p, chunk * 4 + j, idx, w);
+            float f0 = 0.0f, f1 = 0.0f;
+#pragma unroll
+            for(int c = 0; c < 8; ++c)
+            {
+                const float2 f = __half22float2(D.hash[idx[c]]);
+                f0 += w[c] * f.x;
+                f1 += w[c] * f.y;
+            }
+            w4[j] = pack_bf16(f0, f1);
+        }
+        *reinterpret_cast<uint4 *>(row + chunk * 128) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+    }
+#pragma unroll 1
+    for(int half = 0; half < 2; ++half)
+    {
+        // columns 32..47: SH of the direction to the viewer; 48..63: SH of the normal
+        float sh[16];
+        sh16(normalize(half == 0 ? V3(q[3], q[4], q[5]) : V3(q[6], q[7], q[8])), sh);
+        unsigned char *c = row + (4 + 2 * half) * 128;
+        *reinterpret_cast<uint4 *>(c) = make_uint4(pack_bf16(sh[0], sh[1]), pack_bf16(sh[2], sh[3]),
+                                                   pack_bf16(sh[4], sh[5]), pack_bf16(sh[6], sh[7]));
+        *reinterpret_cast<uint4 *>(c + 128) = make_uint4(pack_bf16(sh[8], sh[9]), pack_bf16(sh[10], sh[11]),
+                                                         pack_bf16(sh[12], sh[13]), pack_bf16(sh[14], sh[15]));
+    }
+    // columns 64..79: roughness, albedo, the constant 1, zero padding
+    *reinterpret_cast<uint4 *>(row + 8 * 128) =
+        make_uint4(pack_bf16(q[9], q[10]), pack_bf16(q[11], q[12]), pack_bf16(1.0f, 0.0f), 0u);
+    *reinterpret_cast<uint4 *>(row + 9 * 128) = make_uint4(0u, 0u, 0u, 0u);
+}
+
+// barrier over the 128 threads of group g (named barrier 1 + g), returning whether every
+// thread passed `pred`
+__device__ __forceinline__ bool group_sync_and(int g, bool pred)
+{
+    uint32_t r;
+    asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\t"
+                 "bar.red.and.pred q, %2, 128, p;\n\tselp.u32 %0, 1, 0, q;\n\t}\n"
+                 : "=r"(r)
+                 : "r"(pred ? 1u : 0u), "r"(1 + g)
+                 : "memory");
+    return r != 0;
+}
+
+__device__ __forceinline__ void group_sync(int g) { asm volatile("bar.sync %0, 128;\n" ::"r"(1 + g) : "memory"); }
+
+__global__ void __launch_bounds__(TC_BLOCK, 1)
+    k_nrc_infer_tc(NrcDev D, const float *__restrict__ queries, uint32_t n, float *__restrict__ out)
+{
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    unsigned char *sw = tc_smem;                                   // weights, canonical layout per layer
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(tc_smem + TC_W_BYTES + TC_GROUPS * TC_A_BYTES);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + TC_GROUPS);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int g = tid / TC_ROWS, m = tid % TC_ROWS;               // group, row of the group's tile
+    unsigned char *sa = tc_smem + TC_W_BYTES + g * TC_A_BYTES;     // the group's operand
+
+    // weights into shared memory (16-byte copies), barrier init, tensor-memory allocation
+    for(uint32_t i = tid; i < TC_W_BYTES / 16; i += TC_BLOCK)
+        reinterpret_cast<uint4 *>(sw)[i] = reinterpret_cast<const uint4 *>(D.w_tc)[i];
+    if(tid < TC_GROUPS)
+    {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(mbar + tid)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if(warp == 0)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_addr(tmem_slot)),
+                     "r"(TC_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot + static_cast<uint32_t>(g) * TC_GROUP_COLS;
+    const uint32_t mb = smem_addr(mbar + g);
+    const uint32_t a_addr = smem_addr(sa), w_addr = smem_addr(sw);
+    // this warp's TMEM lane quarter; the row it reads back
+    const uint32_t lane_base = static_cast<uint32_t>(32 * (warp & 3)) << 16;
+    const int erow = 32 * (warp & 3) + lane;
+    uint32_t phase = 0;
+    bool ok = true;
+
+    const uint32_t tiles = (n + TC_ROWS - 1) / TC_ROWS;
+    for(uint32_t tile = blockIdx.x * TC_GROUPS + g; tile < tiles && ok; tile += gridDim.x * TC_GROUPS)
+    {
+        const uint32_t row = tile * TC_ROWS + m;
+        float q[NRC_QUERY_FLOATS];
+        if(row < n)
+            for(int k = 0; k < NRC_QUERY_FLOATS; ++k)
+                q[k] = queries[static_cast<size_t>(row) * NRC_QUERY_FLOATS + k];
+        else
+            for(int k = 0; k < NRC_QUERY_FLOATS; ++k)
+                q[k] = k == 5 || k == 8 ? 1.0f : 0.0f;
+        encode_row_tc(D, q, sa, m);
+        fence_async_smem();
+        group_sync(g);
+
+        for(int l = 0; l < NRC_LAYERS && ok; ++l)
+        {
+            const int K = layer_k(l), N = layer_n(l);
+            if(m == 0)
+            {
+                tc_fence_after();
+                const uint32_t sbo = static_cast<uint32_t>(K * 16);
+                for(int ks = 0; ks < K / 16; ++ks)
+                    tc_mma(tmem, tc_desc(a_addr + ks * 256, 128, sbo),
+                           tc_desc(w_addr + tc_w_offset(l) + ks * 256, 128, sbo), tc_idesc(TC_ROWS, N),
+                           ks > 0 ? 1u : 0u);
+                tc_commit(mb);
+            }
+            const bool done = mbar_wait(mb, phase);
+            phase ^= 1u;
+            tc_fence_after();
+            if(!done)
+                ;  // leave the accumulator unread; the group agrees on the timeout below
+            else if(l + 1 < NRC_LAYERS)
+            {
+                unsigned char *dst = sa + tc_offset(erow, 0, NRC_WIDTH);
+#pragma unroll 1
+                for(int c = 0; c < NRC_WIDTH / 16; ++c)
+                {
+                    float v[16];
+                    tc_ld16(tmem + lane_base + static_cast<uint32_t>(16 * c), v);
+#pragma unroll
+                    for(int h = 0; h < 2; ++h)
+                        *reinterpret_cast<uint4 *>(dst + (2 * c + h) * 128) =
+                            make_uint4(pack_bf16(fmaxf(v[8 * h + 0], 0.0f), fmaxf(v[8 * h + 1], 0.0f)),
+                                       pack_bf16(fmaxf(v[8 * h + 2], 0.0f), fmaxf(v[8 * h + 3], 0.0f)),
+                                       pack_bf16(fmaxf(v[8 * h + 4], 0.0f), fmaxf(v[8 * h + 5], 0.0f)),
+                                       pack_bf16(fmaxf(v[8 * h + 6], 0.0f), fmaxf(v[8 * h + 7], 0.0f)));
+                }
+                fence_async_smem();
+            }
+            else
+            {
+                float v[4];
+                tc_ld4(tmem + lane_base, v);
+                const uint32_t r = tile * TC_ROWS + erow;
+                if(r < n)
+                    *reinterpret_cast<float4 *>(out + static_cast<size_t>(r) * 4) = make_float4(v[0], v[1], v[2], v[3]);
+            }
+            tc_fence_before();
+            ok = group_sync_and(g, done);
+        }
+    }
+    if(!ok && m == 0)
+        atomicOr(D.err, 1u);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if(warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(*tmem_slot), "r"(TC_TMEM_COLS)
+                     : "memory");
 }
 
 // ------------------------------------------------------------------ training: fused fwd + bwd
@@ -676,9 +980,20 @@ __global__ void k_nrc_hash_to_f16(const float2 *__restrict__ src, __half2 *__res
         dst[i] = __floats2half2_rn(src[i].x, src[i].y);
 }
 
-__global__ void k_nrc_pack(const float *__restrict__ w, uint2 *__restrict__ fwd, uint2 *__restrict__ bwd)
+__global__ void k_nrc_pack(const float *__restrict__ w, uint2 *__restrict__ fwd, uint2 *__restrict__ bwd,
+                           __nv_bfloat16 *__restrict__ wtc)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i < NRC_WEIGHTS)
+    {
+        // W_l (row-major K x N) -> W_l^T as an N x K K-major operand in core matrices
+        int l = 0;
+        while(l + 1 < NRC_LAYERS && i >= w_offset(l + 1))
+            ++l;
+        const int local = i - w_offset(l), N = layer_n(l), K = layer_k(l);
+        const int k = local / N, c = local % N;
+        wtc[(tc_w_offset(l) + tc_offset(c, k, K)) / 2] = __float2bfloat16_rn(w[i]);
+    }
     if(i < FWD_PACKED)
     {
         int l = 0;
@@ -708,6 +1023,7 @@ __global__ void k_nrc_pack(const float *__restrict__ w, uint2 *__restrict__ fwd,
 }
 
 size_t infer_smem() { return FWD_PACKED * sizeof(uint2) + NRC_WARPS * 16 * X0_STRIDE * sizeof(__nv_bfloat16); }
+size_t infer_tc_smem() { return TC_W_BYTES + TC_GROUPS * TC_A_BYTES + 8 * TC_GROUPS + 16; }
 size_t train_smem()
 {
     return (FWD_PACKED + BWD_PACKED) * sizeof(uint2) +
@@ -777,6 +1093,9 @@ Nrc::Nrc(const float bbox_min[3], const float bbox_max[3], uint64_t seed)
     fail(cudaMalloc(&h_f16_, sizeof(__half2) * hcount));
     fail(cudaMalloc(&w_fwd_, sizeof(uint2) * FWD_PACKED));
     fail(cudaMalloc(&w_bwd_, sizeof(uint2) * BWD_PACKED));
+    fail(cudaMalloc(&w_tc_, TC_W_BYTES));
+    fail(cudaMalloc(&err_, sizeof(uint32_t)));
+    fail(cudaMemset(err_, 0, sizeof(uint32_t)));
     fail(cudaMalloc(&loss_, sizeof(float)));
     fail(cudaMemset(w_grad_, 0, sizeof(float) * NRC_WEIGHTS));
     fail(cudaMemset(w_m_, 0, sizeof(float) * NRC_WEIGHTS));
@@ -805,9 +1124,16 @@ Nrc::Nrc(const float bbox_min[3], const float bbox_max[3], uint64_t seed)
     d_.hash = h_f16_;
     d_.w_fwd = w_fwd_;
     d_.w_bwd = w_bwd_;
+    d_.w_tc = w_tc_;
+    d_.err = err_;
     d_.loss = loss_;
     fail(cudaFuncSetAttribute(k_nrc_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(infer_smem())));
+    fail(cudaFuncSetAttribute(k_nrc_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              static_cast<int>(infer_tc_smem())));
     fail(cudaFuncSetAttribute(k_nrc_train, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(train_smem())));
+    // inference kernel: tcgen05 (default) or the mma.sync kernel (BTRC_NRC_INFER=mma)
+    if(const char *k = std::getenv("BTRC_NRC_INFER"))
+        use_tc_ = std::strcmp(k, "mma") != 0;
     fail(repack(nullptr));
     fail(cudaStreamSynchronize(nullptr));
 }
@@ -818,6 +1144,7 @@ Nrc::~Nrc()
                     static_cast<void *>(w_v_), static_cast<void *>(h_master_), static_cast<void *>(h_m_),
                     static_cast<void *>(h_v_), static_cast<void *>(d_.hash_grad), static_cast<void *>(h_f16_),
                     static_cast<void *>(w_fwd_), static_cast<void *>(w_bwd_), static_cast<void *>(loss_),
+                    static_cast<void *>(w_tc_), static_cast<void *>(err_),
                     static_cast<void *>(act_), static_cast<void *>(dact_) })
         if(p)
             cudaFree(p);
@@ -825,8 +1152,8 @@ Nrc::~Nrc()
 
 cudaError_t Nrc::repack(cudaStream_t st)
 {
-    const int n = FWD_PACKED > BWD_PACKED ? FWD_PACKED : BWD_PACKED;
-    k_nrc_pack<<<(n + 255) / 256, 256, 0, st>>>(w_master_, w_fwd_, w_bwd_);
+    const int n = std::max(NRC_WEIGHTS, std::max(FWD_PACKED, BWD_PACKED));
+    k_nrc_pack<<<(n + 255) / 256, 256, 0, st>>>(w_master_, w_fwd_, w_bwd_, w_tc_);
     NRC_CHECK(cudaGetLastError());
     const uint64_t hcount = static_cast<uint64_t>(NRC_LEVELS) * NRC_TABLE;
     k_nrc_hash_to_f16<<<sm_count() * 8, 256, 0, st>>>(h_master_, h_f16_, hcount);
@@ -856,6 +1183,13 @@ cudaError_t Nrc::infer(const float *d_queries, uint32_t n, float *d_out, cudaStr
 {
     if(n == 0)
         return cudaSuccess;
+    if(use_tc_)
+    {
+        const uint32_t tiles = (n + TC_ROWS - 1) / TC_ROWS;
+        const uint32_t blocks = std::min<uint32_t>((tiles + TC_GROUPS - 1) / TC_GROUPS, static_cast<uint32_t>(sm_count()));
+        k_nrc_infer_tc<<<blocks, TC_BLOCK, infer_tc_smem(), st>>>(d_, d_queries, n, d_out);
+        return cudaGetLastError();
+    }
     const uint32_t tiles = (n + 15) / 16;
     const uint32_t blocks = std::min<uint32_t>((tiles + NRC_WARPS - 1) / NRC_WARPS, static_cast<uint32_t>(sm_count()) * 8);
     k_nrc_infer<<<blocks, NRC_BLOCK, infer_smem(), st>>>(d_, d_queries, n, d_out);
@@ -867,7 +1201,16 @@ cudaError_t Nrc::reset_loss(cudaStream_t st) { return cudaMemsetAsync(loss_, 0, 
 cudaError_t Nrc::read_loss(float *out, cudaStream_t st)
 {
     NRC_CHECK(cudaMemcpyAsync(out, loss_, sizeof(float), cudaMemcpyDeviceToHost, st));
-    return cudaStreamSynchronize(st);
+    NRC_CHECK(cudaStreamSynchronize(st));
+    return check_error(st);
+}
+
+cudaError_t Nrc::check_error(cudaStream_t st)
+{
+    uint32_t e = 0;
+    NRC_CHECK(cudaMemcpyAsync(&e, err_, sizeof(e), cudaMemcpyDeviceToHost, st));
+    NRC_CHECK(cudaStreamSynchronize(st));
+    return e ? cudaErrorLaunchTimeout : cudaSuccess;
 }
 
 cudaError_t Nrc::train(const float *d_samples, uint32_t n, bool apply_adam, cudaStream_t st)
@@ -924,7 +1267,8 @@ cudaError_t Nrc::copy_params(int which, float *host, uint64_t count, bool set, c
     }
     else
         NRC_CHECK(cudaMemcpyAsync(host, src, sizeof(float) * n, cudaMemcpyDeviceToHost, st));
-    return cudaStreamSynchronize(st);
+    NRC_CHECK(cudaStreamSynchronize(st));
+    return check_error(st);
 }
 
 } // namespace bt

@@ -54,6 +54,8 @@ struct NrcDev
     __nv_bfloat16 *act;         // training: layer inputs X_l, row-major per layer (see nrc.cu)
     __nv_bfloat16 *dact;        // training: pre-activation gradients dY_l
     float *loss;                // training: summed loss
+    const __nv_bfloat16 *w_tc;  // weights as tcgen05 B operands (W_l^T, K-major core matrices)
+    uint32_t *err;              // set when a tensor-core wait timed out
 };
 
 class Nrc
@@ -72,6 +74,8 @@ public:
     cudaError_t reset_loss(cudaStream_t st);
     // synchronises st and returns the accumulated loss
     cudaError_t read_loss(float *out, cudaStream_t st);
+    // synchronises st; cudaErrorLaunchTimeout when a tensor-core kernel gave up waiting
+    cudaError_t check_error(cudaStream_t st);
 
     // parameters / gradients as FP32 host copies (test hooks). which: 0 MLP weights
     // (NRC_WEIGHTS, layer-major, row-major K x N), 1 hash features (LEVELS * TABLE * 2),
@@ -91,6 +95,9 @@ private:
     float2 *h_master_ = nullptr, *h_m_ = nullptr, *h_v_ = nullptr;
     __half2 *h_f16_ = nullptr;
     uint2 *w_fwd_ = nullptr, *w_bwd_ = nullptr;
+    __nv_bfloat16 *w_tc_ = nullptr;
+    uint32_t *err_ = nullptr;
+    bool use_tc_ = true;        // inference on tcgen05 (false: the mma.sync kernel)
     __nv_bfloat16 *act_ = nullptr, *dact_ = nullptr;
     float *loss_ = nullptr;
     uint32_t batch_cap_ = 0;
