@@ -378,6 +378,25 @@ def batch_study(B, ctx):
         runs.append(total_ms)
     batch_ms = float(np.median(runs))
     caps = sorted({(st["capacity"], st["grid_pct"]) for st in stats})
+    # one merged pass: every scene's paths in one queue through one set of stage kernels
+    merged = None
+    try:
+        ctx.render_batch(scs, outs, autotune=True, merged=True)  # concatenates, tunes and warms
+        mruns, mstats = [], None
+        for _ in range(3):
+            mstats, mtotal = ctx.render_batch(scs, outs, autotune=True, merged=True)
+            mruns.append(mtotal)
+        mms = float(np.median(mruns))
+        done = [st["ms"] for st in mstats]
+        merged = {"merged_mpaths_s": total_paths / (mms / 1000) / 1e6, "merged_ms": mms,
+                  "autotuned_capacity_block_grid_pct": [mstats[0]["capacity"], mstats[0]["block"],
+                                                        mstats[0]["grid_pct"]],
+                  "per_scene_done_ms": {"min": min(done), "median": float(np.median(done)), "max": max(done)},
+                  "note": "all scenes in one path queue through one set of persistent stage kernels under one "
+                          "captured two-bounce graph; per-scene time is the device time until every path of "
+                          "the scene had been generated and could have ended (scenes are queued in list order)"}
+    except Exception as ex:  # the merged pass must not sink the lanes figures
+        merged = {"error": str(ex)}
     for s in scs:
         s.close()
     return {
@@ -390,6 +409,7 @@ def batch_study(B, ctx):
                                  "median": float(np.median([st["ms"] for st in stats])),
                                  "max": max(st["ms"] for st in stats)},
         "autotuned_capacity_grid_pct": caps, "scene_build_s": build_s,
+        "merged": merged,
     }
 
 

@@ -71,12 +71,13 @@ class NrcFrameStats(C.Structure):
 
 
 class BatchOpts(C.Structure):
-    _fields_ = [("lanes", C.c_int32), ("autotune", C.c_int32), ("output_on_device", C.c_int32)]
+    _fields_ = [("lanes", C.c_int32), ("autotune", C.c_int32), ("output_on_device", C.c_int32),
+                ("merged", C.c_int32)]
 
 
 class BatchSceneStats(C.Structure):
     _fields_ = [("paths", C.c_uint64), ("ms", C.c_double), ("lane", C.c_int32), ("capacity", C.c_uint32),
-                ("grid_pct", C.c_int32), ("pad", C.c_int32)]
+                ("grid_pct", C.c_int32), ("block", C.c_int32)]
 
 
 STAGES = ("control", "generate", "trace", "medium", "shade", "shadow")
@@ -244,8 +245,10 @@ class Context:
             stats.update(st.as_dict())
         return out
 
-    def render_batch(self, scenes: list, outs: list, lanes: int = 4, autotune: bool = True) -> tuple[list, float]:
-        """Render many built scenes through concurrent lanes (btrc_render_batch). outs are
+    def render_batch(self, scenes: list, outs: list, lanes: int = 4, autotune: bool = True,
+                     merged: bool = False) -> tuple[list, float]:
+        """Render many built scenes (btrc_render_batch): through concurrent lanes, or with
+        merged=True in one pass of one path queue through one set of stage kernels. outs are
         CUDA tensors or host arrays of each scene's (H, W, 3). Returns (per-scene stats,
         total wall ms)."""
         n = len(scenes)
@@ -254,9 +257,9 @@ class Context:
         arr_o = (_vp * n)(*[_ptr(o) for o in outs])
         st = (BatchSceneStats * n)()
         total = C.c_double()
-        opts = BatchOpts(lanes, 1 if autotune else 0, 1 if on_dev else 0)
+        opts = BatchOpts(lanes, 1 if autotune else 0, 1 if on_dev else 0, 1 if merged else 0)
         self._check(self._lib.btrc_render_batch(self.handle, arr_s, n, C.byref(opts), arr_o, st, C.byref(total)))
-        return [{k: getattr(x, k) for k, _ in BatchSceneStats._fields_ if k != "pad"} for x in st], total.value
+        return [{k: getattr(x, k) for k, _ in BatchSceneStats._fields_} for x in st], total.value
 
     def render_noalloc(self, scene: "Scene", out, spp: int = 0, stats: dict | None = None):
         """Allocation-free render into a caller-owned CUDA tensor of shape (H, W, 3)

@@ -40,6 +40,32 @@ struct BatchLane
     ~BatchLane();
 };
 
+// A merged batch: several built scenes concatenated into one device scene (see
+// merge_scenes), their per-scene table and the combined film's shape.
+struct MergedBatch
+{
+    std::vector<const btrc_scene *> scenes;
+    std::vector<uint64_t> serials;
+    std::vector<void *> allocs;
+    DevScene S{};
+    std::vector<BatchScene> table;
+    BatchScene *d_table = nullptr;
+    uint8_t *d_row_scene = nullptr;
+    BatchOut *d_outs = nullptr;
+    uint32_t film_width = 0, film_rows = 0;
+    uint64_t total_paths = 0;
+    int min_depth = 0, max_depth = 0;
+    // autotuner's choice for this batch
+    bool tuned = false;
+    uint32_t capacity = 0;
+    int block = 0, grid_pct = 100;
+    ~MergedBatch()
+    {
+        for(void *p : allocs)
+            cudaFree(p);
+    }
+};
+
 struct btrc_ctx
 {
     int device = 0;
@@ -60,6 +86,7 @@ struct btrc_ctx
     // batched rendering: concurrent lanes and the autotuner's choices per scene class
     std::vector<std::unique_ptr<struct BatchLane>> lanes;
     std::map<std::pair<int, int>, std::pair<uint32_t, int>> tuned;  // (pixel class, triangle class) -> (capacity, grid %)
+    std::unique_ptr<MergedBatch> merged;                              // the last merged batch of scenes
     // radiance-cache frame buffers (queries, weights, predictions, training samples)
     std::vector<void *> nrc_allocs;
     size_t nrc_pixels = 0, nrc_sample_cap = 0;
@@ -84,6 +111,9 @@ struct btrc_scene
     std::vector<uint32_t> export_ids;
     std::vector<CWNode> host_nodes;  // kept for host-only contexts and small scenes
     std::vector<TriRec> host_tris;
+    uint64_t n_shade_tris = 0;       // shading records (triangles over all geometries)
+    uint64_t n_light_tris = 0;       // triangles of light geometries (light sampling arrays)
+    uint64_t serial = 0;             // build number, for caches built from this scene
 };
 
 namespace {
@@ -352,6 +382,8 @@ void build_scene(btrc_scene *sc, int threads)
         auto tab = build_alias_table(G.area);
         lalias.insert(lalias.end(), tab.begin(), tab.end());
     }
+    sc->n_shade_tris = total;
+    sc->n_light_tris = light_total;
     D.geometries = dev_upload(sc->allocs, geos.data(), geos.size());
     D.instances = dev_upload(sc->allocs, H.instances.data(), H.instances.size());
     D.materials = dev_upload(sc->allocs, H.materials.data(), H.materials.size());
@@ -425,6 +457,8 @@ void build_scene(btrc_scene *sc, int threads)
         sc->filter_table = dev_upload(sc->allocs, sc->filter_table_host.data(), sc->filter_table_host.size());
     }
     check_cuda(cudaDeviceSynchronize(), "scene upload");
+    static std::atomic<uint64_t> build_serial{ 0 };
+    sc->serial = ++build_serial;
     sc->built = true;
     sc->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
@@ -1559,6 +1593,275 @@ void autotune(btrc_ctx *ctx, btrc_scene *const *scenes, uint32_t n)
 
 } // namespace
 
+namespace {
+
+// The scenes of a merged batch, concatenated on the device: each scene's arrays are copied
+// behind the previous scenes' and the indices its records hold are shifted by the offsets
+// of its slices. Scenes without media, textures, image-based lights or volume primitives
+// (what the merged stage kernels read per scene: BVH root, lights, sky, camera, film).
+std::unique_ptr<MergedBatch> merge_scenes(btrc_ctx *ctx, btrc_scene *const *scenes, uint32_t n)
+{
+    if(n == 0 || n > 255)
+        throw StatusError(BTRC_ERR_INVALID_ARG, "a merged batch holds 1 to 255 scenes");
+    auto mb = std::make_unique<MergedBatch>();
+    uint64_t nodes = 0, tris = 0, inst = 0, geos = 0, mats = 0, lights = 0, meds = 0, shade = 0, ltris = 0, rows = 0;
+    uint32_t width = 0;
+    for(uint32_t i = 0; i < n; ++i)
+    {
+        const btrc_scene *sc = scenes[i];
+        const DevScene &D = sc->dev;
+        const HostScene &H = sc->host;
+        if(D.has_media || D.material_tex || D.num_volumes || D.env.type == ENV_IBL)
+            throw StatusError(BTRC_ERR_UNSUPPORTED,
+                              "merged batches take scenes without media, textures, image lights or volumes");
+        if(D.node_count == 0)
+            throw StatusError(BTRC_ERR_UNSUPPORTED, "merged batches take scenes with at least one triangle");
+        if(H.params.width > 65535)
+            throw StatusError(BTRC_ERR_UNSUPPORTED, "film too wide for a merged batch");
+        nodes += D.node_count;
+        tris += D.tri_count;
+        inst += H.instances.size();
+        geos += H.geometries.size();
+        mats += H.materials.size();
+        lights += static_cast<uint64_t>(D.num_area_lights);
+        meds += static_cast<uint64_t>(D.num_media);
+        shade += sc->n_shade_tris;
+        ltris += sc->n_light_tris;
+        rows += static_cast<uint64_t>(H.params.height);
+        width = std::max<uint32_t>(width, static_cast<uint32_t>(H.params.width));
+        mb->scenes.push_back(sc);
+        mb->serials.push_back(sc->serial);
+    }
+    if(rows > 65535)
+        throw StatusError(BTRC_ERR_UNSUPPORTED, "merged films taller than 65535 rows");
+    if(tris >= (1ull << 27) || nodes >= 0xffffffffull)
+        throw StatusError(BTRC_ERR_UNSUPPORTED, "merged batch exceeds 2^27 triangle records");
+    auto alloc = [&](size_t bytes) { return dev_alloc(mb->allocs, std::max<size_t>(bytes, 16)); };
+    CWNode *d_nodes = static_cast<CWNode *>(alloc(nodes * sizeof(CWNode)));
+    TriRec *d_tris = static_cast<TriRec *>(alloc(tris * sizeof(TriRec)));
+    Instance *d_inst = static_cast<Instance *>(alloc(inst * sizeof(Instance)));
+    Geometry *d_geo = static_cast<Geometry *>(alloc(geos * sizeof(Geometry)));
+    Material *d_mat = static_cast<Material *>(alloc(mats * sizeof(Material)));
+    AreaLight *d_light = static_cast<AreaLight *>(alloc(lights * sizeof(AreaLight)));
+    Medium *d_med = static_cast<Medium *>(alloc(meds * sizeof(Medium)));
+    F4 *d_shade = static_cast<F4 *>(alloc(shade * SHADE_F4 * sizeof(F4)));
+    F4 *d_lpos = static_cast<F4 *>(alloc(ltris * 3 * sizeof(F4)));
+    AliasEntry8 *d_lalias = static_cast<AliasEntry8 *>(alloc(ltris * sizeof(AliasEntry8)));
+    cudaStream_t st = ctx->stream;
+    RebaseOffsets o{};
+    uint64_t path_begin = 0;
+    uint32_t row_base = 0;
+    auto copy = [&](void *dst, const void *src, size_t bytes) {
+        if(bytes)
+            check_cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st), "merged batch copy");
+    };
+    for(uint32_t i = 0; i < n; ++i)
+    {
+        const btrc_scene *sc = scenes[i];
+        const DevScene &D = sc->dev;
+        const HostScene &H = sc->host;
+        const uint32_t n_inst = static_cast<uint32_t>(H.instances.size());
+        const uint32_t n_geo = static_cast<uint32_t>(H.geometries.size());
+        const uint32_t n_mat = static_cast<uint32_t>(H.materials.size());
+        copy(d_nodes + o.node, D.nodes, D.node_count * sizeof(CWNode));
+        copy(d_tris + o.tri, D.tris, D.tri_count * sizeof(TriRec));
+        copy(d_inst + o.inst, D.instances, n_inst * sizeof(Instance));
+        copy(d_geo + o.geo, D.geometries, n_geo * sizeof(Geometry));
+        copy(d_mat + o.mat, D.materials, n_mat * sizeof(Material));
+        copy(d_light + o.light, D.area_lights, static_cast<size_t>(D.num_area_lights) * sizeof(AreaLight));
+        copy(d_med + o.med, D.media, static_cast<size_t>(D.num_media) * sizeof(Medium));
+        copy(d_shade + static_cast<size_t>(o.shade_tri) * SHADE_F4, D.shade, sc->n_shade_tris * SHADE_F4 * sizeof(F4));
+        copy(d_lpos + static_cast<size_t>(o.light_tri) * 3, D.light_pos, sc->n_light_tris * 3 * sizeof(F4));
+        copy(d_lalias + o.light_tri, D.light_alias, sc->n_light_tris * sizeof(AliasEntry8));
+        check_cuda(launch_rebase_scene(d_nodes + o.node, D.node_count, d_tris + o.tri, D.tri_count, d_inst + o.inst,
+                                       n_inst, d_geo + o.geo, n_geo, d_light + o.light,
+                                       static_cast<uint32_t>(D.num_area_lights), o, st),
+                   "merged batch rebase");
+        BatchScene b{};
+        b.R = make_render_params(sc, H.params.spp, 0);
+        b.path_begin = path_begin;
+        b.row_base = row_base;
+        b.root = o.node;
+        b.light_begin = static_cast<int32_t>(o.light);
+        b.num_area_lights = D.num_area_lights;
+        b.num_lights = D.num_lights;
+        b.vacuum_medium = D.vacuum_medium + static_cast<int32_t>(o.med);
+        b.world_diagonal = D.world_diagonal;
+        b.env = D.env;
+        mb->table.push_back(b);
+        mb->min_depth = std::max(mb->min_depth, H.params.min_depth);
+        mb->max_depth = std::max(mb->max_depth, H.params.max_depth);
+        path_begin += b.R.total_paths;
+        row_base += static_cast<uint32_t>(H.params.height);
+        o.node += D.node_count;
+        o.tri += D.tri_count;
+        o.inst += n_inst;
+        o.geo += n_geo;
+        o.mat += n_mat;
+        o.light += static_cast<uint32_t>(D.num_area_lights);
+        o.med += static_cast<uint32_t>(D.num_media);
+        o.shade_tri += static_cast<uint32_t>(sc->n_shade_tris);
+        o.light_tri += static_cast<uint32_t>(sc->n_light_tris);
+    }
+    std::vector<uint8_t> row_scene(rows);
+    for(uint32_t i = 0; i < n; ++i)
+        std::fill(row_scene.begin() + mb->table[i].row_base,
+                  row_scene.begin() + mb->table[i].row_base + mb->table[i].R.height, static_cast<uint8_t>(i));
+    mb->d_table = dev_upload(mb->allocs, mb->table.data(), mb->table.size());
+    mb->d_row_scene = dev_upload(mb->allocs, row_scene.data(), row_scene.size());
+    mb->d_outs = static_cast<BatchOut *>(alloc(n * sizeof(BatchOut)));
+    mb->film_width = width;
+    mb->film_rows = static_cast<uint32_t>(rows);
+    mb->total_paths = path_begin;
+    DevScene &S = mb->S;
+    S = scenes[0]->dev;
+    S.nodes = reinterpret_cast<const F4 *>(d_nodes);
+    S.tris = reinterpret_cast<const F4 *>(d_tris);
+    S.node_count = static_cast<uint32_t>(nodes);
+    S.tri_count = static_cast<uint32_t>(tris);
+    S.shade = d_shade;
+    S.geometries = d_geo;
+    S.instances = d_inst;
+    S.materials = d_mat;
+    S.area_lights = d_light;
+    S.light_pos = d_lpos;
+    S.light_alias = d_lalias;
+    S.media = d_med;
+    S.num_media = static_cast<int32_t>(meds);
+    S.has_media = 0;
+    check_cuda(cudaStreamSynchronize(st), "merged batch build");
+    return mb;
+}
+
+bool merged_matches(const MergedBatch *mb, btrc_scene *const *scenes, uint32_t n)
+{
+    if(!mb || mb->scenes.size() != n)
+        return false;
+    for(uint32_t i = 0; i < n; ++i)
+        if(mb->scenes[i] != scenes[i] || mb->serials[i] != scenes[i]->serial)
+            return false;
+    return true;
+}
+
+// one pass over the whole merged batch: every scene's paths in one queue of `capacity`
+// states, through the stage kernels' merged variants under the captured bounce graph
+double merged_render(btrc_ctx *ctx, MergedBatch &mb, uint32_t capacity, int block, int grid_pct, float *const *outs,
+                     bool on_dev, RenderStats &rs, std::vector<double> *scene_done_ms)
+{
+    const size_t pixels = static_cast<size_t>(mb.film_width) * mb.film_rows;
+    capacity = static_cast<uint32_t>(std::min<uint64_t>(capacity, std::max<uint64_t>(mb.total_paths, 1)));
+    ensure_render_buffers(ctx, capacity, pixels);
+    cudaStream_t st = ctx->stream;
+    const auto t0 = std::chrono::steady_clock::now();
+    check_cuda(cudaMemsetAsync(ctx->buf.film, 0, sizeof(float4) * pixels, st), "film clear");
+    DevRender R{};
+    R.width = static_cast<int32_t>(mb.film_width);
+    R.height = static_cast<int32_t>(mb.film_rows);
+    R.spp = 1;
+    R.min_depth = mb.min_depth;
+    R.max_depth = mb.max_depth;
+    R.sampler = mb.table[0].R.sampler;
+    R.capacity = capacity;
+    R.total_paths = mb.total_paths;
+    R.grid_pct = grid_pct;
+    R.nrc_terminate = -1;
+    R.batch = mb.d_table;
+    R.row_scene = mb.d_row_scene;
+    R.batch_count = static_cast<uint32_t>(mb.table.size());
+    R.stage_block = block;
+    ctx->buf.capacity = capacity;
+    bool cancelled = false;
+    std::vector<std::pair<double, uint64_t>> progress;
+    check_cuda(render_wavefront(mb.S, R, ctx->buf, st, &ctx->cancel, true, 0, &rs, &cancelled,
+                                scene_done_ms ? &progress : nullptr),
+               "merged batch render");
+    if(outs)
+    {
+        // device images: the callers' own, or scratch images copied out afterwards
+        const uint32_t n = static_cast<uint32_t>(mb.table.size());
+        std::vector<BatchOut> o(n);
+        size_t scratch_px = 0;
+        uint32_t max_px = 0;
+        for(uint32_t i = 0; i < n; ++i)
+        {
+            const DevRender &r = mb.table[i].R;
+            max_px = std::max<uint32_t>(max_px, static_cast<uint32_t>(r.width * r.height));
+            scratch_px += static_cast<size_t>(r.width) * r.height;
+        }
+        float *scratch = on_dev ? nullptr : ctx_scratch_images(ctx, scratch_px, 1);
+        size_t at = 0;
+        for(uint32_t i = 0; i < n; ++i)
+        {
+            const DevRender &r = mb.table[i].R;
+            o[i].rgb = on_dev ? outs[i] : scratch + at * 3;
+            o[i].row_base = mb.table[i].row_base;
+            o[i].width = static_cast<uint32_t>(r.width);
+            o[i].height = static_cast<uint32_t>(r.height);
+            at += static_cast<size_t>(r.width) * r.height;
+        }
+        check_cuda(cudaMemcpyAsync(mb.d_outs, o.data(), n * sizeof(BatchOut), cudaMemcpyHostToDevice, st),
+                   "batch outputs");
+        check_cuda(launch_resolve_batch(ctx->buf.film, mb.film_width, mb.d_outs, n, max_px, st), "batch resolve");
+        if(!on_dev)
+            for(uint32_t i = 0; i < n; ++i)
+                check_cuda(cudaMemcpyAsync(outs[i], o[i].rgb,
+                                           static_cast<size_t>(o[i].width) * o[i].height * 3 * sizeof(float),
+                                           cudaMemcpyDeviceToHost, st),
+                           "image download");
+    }
+    check_cuda(cudaStreamSynchronize(st), "merged batch sync");
+    if(rs.err)
+        throw StatusError(BTRC_ERR_INTERNAL, "traversal stack overflow reported by the device");
+    if(cancelled)
+        throw StatusError(BTRC_ERR_CANCELLED, "render cancelled");
+    if(scene_done_ms)
+    {
+        // a scene's paths have all ended once every one of them was generated and as many
+        // two-bounce launches followed as its longest path can take
+        const size_t tail = static_cast<size_t>((std::max(mb.max_depth, mb.min_depth) + 3) / 2);
+        scene_done_ms->assign(mb.table.size(), static_cast<double>(rs.device_ms));
+        for(size_t i = 0; i < mb.table.size(); ++i)
+        {
+            const uint64_t end = mb.table[i].path_begin + mb.table[i].R.total_paths;
+            for(size_t k = 0; k < progress.size(); ++k)
+                if(progress[k].second >= end)
+                {
+                    const size_t done = std::min(progress.size() - 1, k + tail);
+                    (*scene_done_ms)[i] = progress[done].first;
+                    break;
+                }
+        }
+    }
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+// queue capacity x threads per block of the stage kernels x persistent-grid size: the
+// fastest full pass over the batch (each setting timed after a warm-up pass)
+void autotune_merged(btrc_ctx *ctx, MergedBatch &mb)
+{
+    double best = 1e300;
+    for(uint32_t cap : { 1u << 21, 1u << 22, 1u << 23, 1u << 24 })
+        for(int block : { 128, 256 })
+            for(int pct : { 100, 50 })
+            {
+                if(pct == 50 && block == 128)
+                    continue;
+                RenderStats rs{};
+                merged_render(ctx, mb, cap, block, pct, nullptr, true, rs, nullptr);
+                const double ms = merged_render(ctx, mb, cap, block, pct, nullptr, true, rs, nullptr);
+                if(ms < best)
+                {
+                    best = ms;
+                    mb.capacity = cap;
+                    mb.block = block;
+                    mb.grid_pct = pct;
+                }
+            }
+    mb.tuned = true;
+}
+
+} // namespace
+
 btrc_status btrc_render_batch(btrc_ctx *ctx, btrc_scene *const *scenes, uint32_t n, const btrc_batch_opts *opts,
                               float *const *rgb_out, btrc_batch_scene_stats *stats, double *total_ms)
 {
@@ -1578,6 +1881,36 @@ btrc_status btrc_render_batch(btrc_ctx *ctx, btrc_scene *const *scenes, uint32_t
         const int lanes = opts && opts->lanes > 0 ? opts->lanes : 4;
         const bool on_dev = opts && opts->output_on_device;
         const bool tune = opts && opts->autotune;
+        if(opts && opts->merged)
+        {
+            if(!merged_matches(ctx->merged.get(), scenes, n))
+            {
+                check_cuda(cudaStreamSynchronize(ctx->stream), "stream sync");
+                ctx->merged.reset();
+                ctx->merged = merge_scenes(ctx, scenes, n);
+            }
+            MergedBatch &mb = *ctx->merged;
+            if(tune && !mb.tuned)
+                autotune_merged(ctx, mb);
+            const uint32_t cap = mb.tuned ? mb.capacity : static_cast<uint32_t>(scenes[0]->host.params.state_count);
+            const int block = mb.tuned ? mb.block : 0, pct = mb.tuned ? mb.grid_pct : 100;
+            RenderStats rs{};
+            std::vector<double> done;
+            const double ms = merged_render(ctx, mb, cap, block, pct, rgb_out, on_dev, rs, stats ? &done : nullptr);
+            if(total_ms)
+                *total_ms = ms;
+            if(stats)
+                for(uint32_t i = 0; i < n; ++i)
+                {
+                    stats[i].paths = mb.table[i].R.total_paths;
+                    stats[i].ms = done[i];
+                    stats[i].lane = 0;
+                    stats[i].capacity = static_cast<uint32_t>(std::min<uint64_t>(cap, mb.total_paths));
+                    stats[i].grid_pct = pct;
+                    stats[i].block = block > 0 ? block : 256;
+                }
+            return;
+        }
         if(tune)
             autotune(ctx, scenes, n);
         while(static_cast<int>(ctx->lanes.size()) < lanes)
@@ -1630,7 +1963,7 @@ btrc_status btrc_render_batch(btrc_ctx *ctx, btrc_scene *const *scenes, uint32_t
                             stats[i].capacity = std::min<uint32_t>(
                                 cap, static_cast<uint32_t>(std::max<uint64_t>(rs.paths, 1)));
                             stats[i].grid_pct = pct;
-                            stats[i].pad = 0;
+                            stats[i].block = 256;
                         }
                     }
                 }

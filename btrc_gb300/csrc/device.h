@@ -54,6 +54,8 @@ struct DevScene
 // pending tests traced 5 % faster than rounds started for any test (1, 8, 16, 24 measured)
 constexpr int32_t TRI_ROUND_TESTS = 16;
 
+struct BatchScene;
+
 struct DevRender
 {
     int32_t width, height, spp;
@@ -79,6 +81,32 @@ struct DevRender
     float4 *nrc_weight;       // path throughput (xyz) and pixel bits (w) per query
     uint32_t *nrc_count;
     uint32_t nrc_cap;
+    // merged batch of scenes (null for one scene): the stage kernels read each path's
+    // scene from the film row of its pixel word, row_scene[y]
+    const BatchScene *batch;
+    const uint8_t *row_scene;
+    uint32_t batch_count;
+    int32_t stage_block;      // threads per block of the grid-stride stage kernels (0: BLOCK)
+};
+
+// One scene of a merged batch: its own render parameters and the parts of the combined
+// scene that are its own. Its geometry, instances, materials and light triangles live in
+// the combined arrays (indices rebased); its BVH is a subtree of the combined node array
+// reachable only from `root`, and its film is rows [row_base, row_base + height) of the
+// combined film.
+struct BatchScene
+{
+    DevRender R;              // camera, film size, spp, depths, sampler, filter; R.total_paths its paths
+    uint64_t path_begin;      // global index of its first camera path
+    uint32_t row_base;
+    uint32_t root;            // root node of its BVH in the combined node array
+    int32_t light_begin;      // its first area light in the combined table
+    int32_t num_area_lights;
+    int32_t num_lights;       // area lights + its environment light
+    int32_t vacuum_medium;
+    float world_diagonal;
+    int32_t pad[3];
+    EnvLight env;
 };
 
 // Queue counters, resident in device memory for the whole render. Shadow records are

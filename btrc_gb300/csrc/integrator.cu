@@ -910,17 +910,47 @@ __global__ void k_control(Counters *c, uint32_t capacity, uint64_t total, int pa
         ++c->iterations;
 }
 
-__global__ void __launch_bounds__(BLOCK) k_generate(DevRender R, PathSoA P, float4 *film, const Counters *cnt,
-                                                    int vacuum_medium)
+// the scene of global camera path g in a merged batch: the last with path_begin <= g
+__device__ __forceinline__ int batch_scene_of_path(const DevRender &R, uint64_t g)
+{
+    int lo = 0, hi = static_cast<int>(R.batch_count) - 1;
+    while(lo < hi)
+    {
+        const int mid = (lo + hi + 1) >> 1;
+        if(R.batch[mid].path_begin <= g)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+template<bool MULTI>
+__global__ void __launch_bounds__(BLOCK) k_generate(DevRender R_in, PathSoA P, float4 *film, const Counters *cnt,
+                                                    int vacuum_in)
 {
     const uint32_t n = cnt->n_new;
     const uint32_t slot_base = cnt->slot_base;
     const uint64_t gen_base = cnt->gen_base;
     const uint32_t stride = gridDim.x * blockDim.x;
-    const uint64_t pixel_count = static_cast<uint64_t>(R.width) * R.height;
     for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
     {
-        const uint64_t g = gen_base + i;
+        // a merged batch: the path's scene supplies camera, film and sampler; its film is
+        // a band of rows of the combined film
+        uint64_t g = gen_base + i;
+        uint32_t row_base = 0;
+        int vacuum_medium = vacuum_in;
+        DevRender Rb;
+        if(MULTI)
+        {
+            const BatchScene &b = R_in.batch[batch_scene_of_path(R_in, g)];
+            Rb = b.R;
+            g -= b.path_begin;
+            row_base = b.row_base;
+            vacuum_medium = b.vacuum_medium;
+        }
+        const DevRender &R = MULTI ? Rb : R_in;
+        const uint64_t pixel_count = static_cast<uint64_t>(R.width) * R.height;
         uint64_t pixel, sample;
         if(!R.tile)
         {
@@ -960,8 +990,9 @@ __global__ void __launch_bounds__(BLOCK) k_generate(DevRender R, PathSoA P, floa
         // PinholeCamera::generate_ray_inline (builtin/btrc/builtin/camera/pinhole.cpp:84-99)
         const V3 dst = R.cam_lbc + film_x * R.cam_fx + film_y * R.cam_fy;
         const V3 dir = normalize(dst - R.cam_eye);
-        const uint32_t pix = px | (py << 16);
-        atomicAdd(&film[static_cast<size_t>(py) * R.width + px].w, 1.0f);
+        const uint32_t row = py + row_base;
+        const uint32_t pix = px | (row << 16);
+        atomicAdd(&film[static_cast<size_t>(row) * R_in.width + px].w, 1.0f);
         const uint32_t s = slot_base + i;
         P.beta_depth[s] = F4{ 1.0f, 1.0f, 1.0f, __int_as_float(0) };
         P.rad_pixel[s] = F4{ 0.0f, 0.0f, 0.0f, __uint_as_float(pix) };
@@ -972,20 +1003,22 @@ __global__ void __launch_bounds__(BLOCK) k_generate(DevRender R, PathSoA P, floa
     }
 }
 
-template<bool COUNT>
+template<bool COUNT, bool MULTI = false>
 __global__ void __launch_bounds__(TRAVERSE_BLOCK) k_trace(DevScene S, PathSoA P, uint32_t *flags, HitDetail *hits,
-                                               Counters *cnt)
+                                               Counters *cnt, DevRender R)
 {
     const uint32_t n = cnt->active;
     uint64_t nv = 0, tv = 0;
     traverse_refill<false, COUNT>(
         reinterpret_cast<const float4 *>(S.nodes), reinterpret_cast<const float4 *>(S.tris), S.node_count,
         &cnt->trace_cursor, n, REFILL_LANES, &cnt->err,
-        [&](uint32_t i, float *o, float *d, float &t1) {
+        [&](uint32_t i, float *o, float *d, float &t1, uint32_t &root) {
             const F4 ro = P.ray_o[i], rd = P.ray_d[i];
             o[0] = ro.x; o[1] = ro.y; o[2] = ro.z;
             d[0] = rd.x; d[1] = rd.y; d[2] = rd.z;
             t1 = rd.w;
+            if(MULTI)
+                root = R.batch[R.row_scene[__float_as_uint(P.rad_pixel[i].w) >> 16]].root;
         },
         [&](uint32_t i, const ClosestResult &c) {
             flags[i] = c.hit ? (c.inst | HIT_BIT) : 0u;
@@ -1290,8 +1323,8 @@ __device__ __forceinline__ bool nrc_query_at(const DevScene &S, const SurfacePoi
 // TEX = false compiles the texture evaluation out, so scenes without textured materials
 // keep the shade kernel's registers. Two blocks per SM (at most 128 registers a thread):
 // the kernel waits on scattered loads, and the occupancy pays for the few spills.
-template<bool TEX, bool NRC = false>
-__global__ void __launch_bounds__(BLOCK, 2) k_shade(DevScene S, DevRender R, PathSoA P, PathSoA N, ShadowSoA SH,
+template<bool TEX, bool NRC = false, bool MULTI = false>
+__global__ void __launch_bounds__(BLOCK, 2) k_shade(DevScene S_in, DevRender R_in, PathSoA P, PathSoA N, ShadowSoA SH,
                                                     int shq, const uint32_t *flags, const HitDetail *hits,
                                                  const uint32_t *order, float4 *film, Counters *cnt)
 {
@@ -1304,6 +1337,29 @@ __global__ void __launch_bounds__(BLOCK, 2) k_shade(DevScene S, DevRender R, Pat
         const F4 bd = P.beta_depth[i], rp = P.rad_pixel[i];
         const F4 ro = P.ray_o[i], rd = P.ray_d[i], ble = P.bsdf_le[i];
         const uint32_t pixel = __float_as_uint(rp.w);
+        // a merged batch: the path's scene supplies its lights, environment and path-length
+        // rules; film splats stay in combined-film coordinates
+        DevScene Sb;
+        DevRender Rb;
+        if(MULTI)
+        {
+            const BatchScene &b = R_in.batch[R_in.row_scene[pixel >> 16]];
+            Sb = S_in;
+            Sb.area_lights = S_in.area_lights + b.light_begin;
+            Sb.num_area_lights = b.num_area_lights;
+            Sb.num_lights = b.num_lights;
+            Sb.env = b.env;
+            Sb.world_diagonal = b.world_diagonal;
+            Sb.vacuum_medium = b.vacuum_medium;
+            Rb = R_in;
+            Rb.min_depth = b.R.min_depth;
+            Rb.max_depth = b.R.max_depth;
+            Rb.rr_threshold = b.R.rr_threshold;
+            Rb.rr_cont_prob = b.R.rr_cont_prob;
+            Rb.sampler = b.R.sampler;
+        }
+        const DevScene &S = MULTI ? Sb : S_in;
+        const DevRender &R = MULTI ? Rb : R_in;
         const V3 o = v3(ro), d = v3(rd), beta_le = v3(ble);
         const float bsdf_pdf = ble.w;
         V3 path_rad = v3(rp);
@@ -1449,9 +1505,12 @@ __global__ void __launch_bounds__(BLOCK, 2) k_shade(DevScene S, DevRender R, Pat
 using ShadeKernel = void (*)(DevScene, DevRender, PathSoA, PathSoA, ShadowSoA, int, const uint32_t *,
                              const HitDetail *, const uint32_t *, float4 *, Counters *);
 
-// the shade kernel variant for a scene and render: textured materials, cache termination
+// the shade kernel variant for a scene and render: textured materials, cache termination,
+// a merged batch (untextured, no cache)
 ShadeKernel shade_kernel(const DevScene &S, const DevRender &R)
 {
+    if(R.batch)
+        return k_shade<false, false, true>;
     const bool tex = S.material_tex != nullptr, nrc = R.nrc_terminate >= 0;
     if(tex)
         return nrc ? k_shade<true, true> : k_shade<true, false>;
@@ -1462,7 +1521,7 @@ ShadeKernel shade_kernel(const DevScene &S, const DevRender &R)
 // the warp-refill traversal; unoccluded records splat (times the medium transmittance)
 // MEDIA = false compiles the transmittance code out, so the traversal of scenes without
 // media keeps its registers
-template<bool MEDIA>
+template<bool MEDIA, bool MULTI = false>
 __global__ void __launch_bounds__(TRAVERSE_BLOCK) k_shadow(DevScene S, DevRender R, ShadowSoA SH, float4 *film,
                                                            Counters *cnt, int shq)
 {
@@ -1470,11 +1529,13 @@ __global__ void __launch_bounds__(TRAVERSE_BLOCK) k_shadow(DevScene S, DevRender
     traverse_refill<true>(
         reinterpret_cast<const float4 *>(S.nodes), reinterpret_cast<const float4 *>(S.tris), S.node_count,
         &cnt->shadow_cursor[shq], n, REFILL_LANES, &cnt->err,
-        [&](uint32_t i, float *o, float *d, float &t1) {
+        [&](uint32_t i, float *o, float *d, float &t1, uint32_t &root) {
             const F4 so = SH.o[i], sd = SH.d[i];
             o[0] = so.x; o[1] = so.y; o[2] = so.z;
             d[0] = sd.x; d[1] = sd.y; d[2] = sd.z;
             t1 = sd.w;
+            if(MULTI)
+                root = R.batch[R.row_scene[__float_as_uint(so.w) >> 16]].root;
         },
         [&](uint32_t i, const ClosestResult &c) {
             if(c.hit)
@@ -1569,10 +1630,34 @@ void timed(StageTimer *T, int stage, cudaStream_t st, uint64_t *launches, Launch
 
 void launch_shadow(const DevScene &S, const DevRender &R, RenderBuffers &B, int parity, cudaStream_t st, int grid)
 {
-    if(S.has_media)
+    if(R.batch)
+        k_shadow<false, true><<<grid, TRAVERSE_BLOCK, 0, st>>>(S, R, B.shadow[parity], B.film, B.counters, parity);
+    else if(S.has_media)
         k_shadow<true><<<grid, TRAVERSE_BLOCK, 0, st>>>(S, R, B.shadow[parity], B.film, B.counters, parity);
     else
         k_shadow<false><<<grid, TRAVERSE_BLOCK, 0, st>>>(S, R, B.shadow[parity], B.film, B.counters, parity);
+}
+
+// threads per block of the grid-stride stage kernels (generate, medium, shade); k_order
+// is written for BLOCK threads
+int stage_block(const DevRender &R) { return R.stage_block > 0 ? R.stage_block : BLOCK; }
+
+// persistent grid of every stage kernel for this scene and render (variants as launched)
+void stage_grids(const DevScene &S, const DevRender &R, int grids[6])
+{
+    const int sb = stage_block(R);
+    const bool multi = R.batch != nullptr;
+    grids[0] = persistent_grid(sb, multi ? reinterpret_cast<const void *>(k_generate<true>)
+                                         : reinterpret_cast<const void *>(k_generate<false>), R.grid_pct);
+    grids[1] = persistent_grid(TRAVERSE_BLOCK, multi ? reinterpret_cast<const void *>(k_trace<false, true>)
+                                                     : reinterpret_cast<const void *>(k_trace<false>), R.grid_pct);
+    grids[2] = persistent_grid(sb, reinterpret_cast<const void *>(k_medium), R.grid_pct);
+    grids[3] = persistent_grid(sb, reinterpret_cast<const void *>(shade_kernel(S, R)), R.grid_pct);
+    grids[4] = persistent_grid(TRAVERSE_BLOCK, multi ? reinterpret_cast<const void *>(k_shadow<false, true>)
+                                               : S.has_media ? reinterpret_cast<const void *>(k_shadow<true>)
+                                                             : reinterpret_cast<const void *>(k_shadow<false>),
+                               R.grid_pct);
+    grids[5] = persistent_grid(BLOCK, reinterpret_cast<const void *>(k_order), R.grid_pct);  // sized for BLOCK
 }
 
 // One bounce of the given parity. With defer_shadow the caller launches its shadow kernel
@@ -1587,22 +1672,29 @@ cudaError_t enqueue_bounce(const DevScene &S, const DevRender &R, RenderBuffers 
     timed(T, STAGE_CONTROL, st, launches,
           [&] { k_control<<<1, 1, 0, st>>>(B.counters, B.capacity, R.total_paths, parity); });
     timed(T, STAGE_GENERATE, st, launches,
-          [&] { k_generate<<<grids[0], BLOCK, 0, st>>>(R, P, B.film, B.counters, S.vacuum_medium); });
+          [&] {
+              if(R.batch)
+                  k_generate<true><<<grids[0], stage_block(R), 0, st>>>(R, P, B.film, B.counters, S.vacuum_medium);
+              else
+                  k_generate<false><<<grids[0], stage_block(R), 0, st>>>(R, P, B.film, B.counters, S.vacuum_medium);
+          });
     timed(T, STAGE_TRACE, st, launches, [&] {
-        if(profile == 2)
-            k_trace<true><<<grids[1], TRAVERSE_BLOCK, 0, st>>>(S, P, B.hit_flag, B.hit_detail, B.counters);
+        if(R.batch)
+            k_trace<false, true><<<grids[1], TRAVERSE_BLOCK, 0, st>>>(S, P, B.hit_flag, B.hit_detail, B.counters, R);
+        else if(profile == 2)
+            k_trace<true><<<grids[1], TRAVERSE_BLOCK, 0, st>>>(S, P, B.hit_flag, B.hit_detail, B.counters, R);
         else
-            k_trace<false><<<grids[1], TRAVERSE_BLOCK, 0, st>>>(S, P, B.hit_flag, B.hit_detail, B.counters);
+            k_trace<false><<<grids[1], TRAVERSE_BLOCK, 0, st>>>(S, P, B.hit_flag, B.hit_detail, B.counters, R);
     });
     if(S.has_media)
         timed(T, STAGE_MEDIUM, st, launches, [&] {
-            k_medium<<<grids[2], BLOCK, 0, st>>>(S, R, P, N, SH, parity, B.hit_flag, B.hit_detail, B.film,
+            k_medium<<<grids[2], stage_block(R), 0, st>>>(S, R, P, N, SH, parity, B.hit_flag, B.hit_detail, B.film,
                                                  B.counters);
         });
     timed(T, STAGE_SHADE, st, launches,
           [&] { k_order<<<grids[5], BLOCK, 0, st>>>(B.hit_flag, B.order, B.counters); });
     timed(T, STAGE_SHADE, st, launches, [&] {
-        shade_kernel(S, R)<<<grids[3], BLOCK, 0, st>>>(S, R, P, N, SH, parity, B.hit_flag, B.hit_detail, B.order,
+        shade_kernel(S, R)<<<grids[3], stage_block(R), 0, st>>>(S, R, P, N, SH, parity, B.hit_flag, B.hit_detail, B.order,
                                                        B.film, B.counters);
     });
     if(!defer_shadow)
@@ -1647,7 +1739,7 @@ cudaError_t upload_primes()
 
 cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffers &B, cudaStream_t st,
                              const std::atomic<bool> *cancel, bool use_graphs, int profile, RenderStats *stats,
-                             bool *cancelled)
+                             bool *cancelled, std::vector<std::pair<double, uint64_t>> *progress)
 {
     *cancelled = false;
     if(profile != 0)
@@ -1665,15 +1757,8 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
     cudaError_t e = cudaMemsetAsync(B.counters, 0, sizeof(Counters), st);
     if(e != cudaSuccess)
         return e;
-    const int grids[6] = {
-        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_generate), R.grid_pct),
-        persistent_grid(TRAVERSE_BLOCK, reinterpret_cast<const void *>(k_trace<false>), R.grid_pct),
-        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_medium), R.grid_pct),
-        persistent_grid(BLOCK, reinterpret_cast<const void *>(shade_kernel(S, R)), R.grid_pct),
-        persistent_grid(TRAVERSE_BLOCK, S.has_media ? reinterpret_cast<const void *>(k_shadow<true>)
-                                         : reinterpret_cast<const void *>(k_shadow<false>), R.grid_pct),
-        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_order), R.grid_pct),
-    };
+    int grids[6];
+    stage_grids(S, R, grids);
 
     // Graph of two bounces. Each bounce's shadow kernel runs on a second stream beside the
     // next bounce: the odd bounce's shadow rays are traced at the start of the following
@@ -1738,6 +1823,18 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
     cudaEvent_t t0, t1;
     cudaEventCreate(&t0);
     cudaEventCreate(&t1);
+    // progress log: one timing event and one copy of the generated-path counter per launch
+    std::vector<cudaEvent_t> prog_ev;
+    uint64_t *prog_gen = nullptr;
+    if(progress && use_graphs)
+    {
+        progress->clear();
+        if(cudaMalloc(&prog_gen, sizeof(uint64_t) * (max_launches + 1)) != cudaSuccess)
+        {
+            prog_gen = nullptr;
+            cudaGetLastError();
+        }
+    }
     cudaEventRecord(t0, st);
 
     // Launch pairs of bounces; read the counters back asynchronously and test completion
@@ -1780,6 +1877,15 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
         }
         if(e != cudaSuccess)
             break;
+        if(prog_gen)
+        {
+            cudaEvent_t pe;
+            cudaEventCreate(&pe);
+            cudaEventRecord(pe, st);
+            prog_ev.push_back(pe);
+            cudaMemcpyAsync(prog_gen + launches_now, &B.counters->generated, sizeof(uint64_t), cudaMemcpyDeviceToDevice,
+                            st);
+        }
         cudaMemcpyAsync(&B.host_counters[slot], B.counters, sizeof(Counters), cudaMemcpyDeviceToHost, st);
         cudaEventRecord(ev[slot], st);
         ++launches_total;
@@ -1796,6 +1902,20 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
         e = se;
     float ms = 0;
     cudaEventElapsedTime(&ms, t0, t1);
+    if(prog_gen)
+    {
+        std::vector<uint64_t> gen(prog_ev.size());
+        if(!gen.empty())
+            cudaMemcpy(gen.data(), prog_gen, sizeof(uint64_t) * gen.size(), cudaMemcpyDeviceToHost);
+        for(size_t k = 0; k < prog_ev.size(); ++k)
+        {
+            float t = 0;
+            cudaEventElapsedTime(&t, t0, prog_ev[k]);
+            progress->emplace_back(t, gen[k]);
+            cudaEventDestroy(prog_ev[k]);
+        }
+        cudaFree(prog_gen);
+    }
     Counters fin{};
     cudaMemcpy(&fin, B.counters, sizeof(Counters), cudaMemcpyDeviceToHost);
     for(int k = 0; k < RING_SLOTS; ++k)
@@ -2186,6 +2306,96 @@ cudaError_t launch_resolve(const float4 *film, float *rgb, uint32_t pixels, cuda
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- merged batches
+//
+// Several built scenes concatenated into one device scene: node, triangle, instance,
+// geometry, material, light and medium arrays placed one scene after another, with every
+// index a record holds shifted by its scene's offsets (applied by the kernels below to
+// each scene's slice after the copy).
+
+namespace {
+
+__global__ void k_rebase_scene(CWNode *nodes, uint32_t n_nodes, TriRec *tris, uint32_t n_tris, Instance *inst,
+                               uint32_t n_inst, Geometry *geo, uint32_t n_geo, AreaLight *lights, uint32_t n_lights,
+                               RebaseOffsets o)
+{
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_nodes; i += stride)
+    {
+        nodes[i].child_base += o.node;
+        nodes[i].tri_base += o.tri;
+    }
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_tris; i += stride)
+        tris[i].inst += o.inst;
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_inst; i += stride)
+    {
+        Instance &x = inst[i];
+        x.geometry += static_cast<int32_t>(o.geo);
+        x.material += static_cast<int32_t>(o.mat);
+        // x.light stays an index into its own scene's lights: the merged kernels read the
+        // scene's light table through a view that starts at the scene's first light
+        const uint32_t inner = (x.media & 0xffffu) + o.med, outer = (x.media >> 16) + o.med;
+        x.media = (inner & 0xffffu) | (outer << 16);
+    }
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_geo; i += stride)
+    {
+        Geometry &g = geo[i];
+        g.tri_offset += o.shade_tri;
+        uint32_t lo;
+        memcpy(&lo, &g.pad, sizeof(lo));
+        if(lo != 0xffffffffu)
+        {
+            lo += o.light_tri;
+            memcpy(&g.pad, &lo, sizeof(lo));
+        }
+    }
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_lights; i += stride)
+    {
+        lights[i].instance += static_cast<int32_t>(o.inst);
+        lights[i].geometry += static_cast<int32_t>(o.geo);
+    }
+}
+
+// radiance / weight of each scene's band of the combined film into its own image
+__global__ void k_resolve_batch(const float4 *film, uint32_t film_width, const BatchOut *outs)
+{
+    const BatchOut o = outs[blockIdx.y];
+    const uint32_t pixels = o.width * o.height;
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < pixels; i += gridDim.x * blockDim.x)
+    {
+        const uint32_t x = i % o.width, y = i / o.width;
+        const float4 f = film[static_cast<size_t>(o.row_base + y) * film_width + x];
+        const float inv = f.w > 0 ? 1.0f / f.w : 0.0f;
+        o.rgb[static_cast<size_t>(i) * 3 + 0] = f.x * inv;
+        o.rgb[static_cast<size_t>(i) * 3 + 1] = f.y * inv;
+        o.rgb[static_cast<size_t>(i) * 3 + 2] = f.z * inv;
+    }
+}
+
+} // namespace
+
+cudaError_t launch_rebase_scene(CWNode *nodes, uint32_t n_nodes, TriRec *tris, uint32_t n_tris, Instance *inst,
+                                uint32_t n_inst, Geometry *geo, uint32_t n_geo, AreaLight *lights, uint32_t n_lights,
+                                const RebaseOffsets &o, cudaStream_t st)
+{
+    const uint32_t n = std::max(std::max(n_nodes, n_tris), std::max(n_inst, std::max(n_geo, n_lights)));
+    if(n == 0)
+        return cudaSuccess;
+    const uint32_t blocks = std::min<uint32_t>((n + 255) / 256, 4096);
+    k_rebase_scene<<<blocks, 256, 0, st>>>(nodes, n_nodes, tris, n_tris, inst, n_inst, geo, n_geo, lights, n_lights, o);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_resolve_batch(const float4 *film, uint32_t film_width, const BatchOut *outs, uint32_t count,
+                                 uint32_t max_pixels, cudaStream_t st)
+{
+    if(count == 0)
+        return cudaSuccess;
+    const uint32_t bx = std::min<uint32_t>((max_pixels + 255) / 256, 1024);
+    k_resolve_batch<<<dim3(bx, count), 256, 0, st>>>(film, film_width, outs);
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------- allocation-free render
 //
 // For callers that cannot allocate GPU memory while they render: engines that reserve
@@ -2307,15 +2517,8 @@ cudaError_t render_wavefront_noalloc(const DevScene &S, const DevRender &R, void
         e = cudaMemsetAsync(B.counters, 0, sizeof(Counters), st);
     if(e != cudaSuccess)
         return e;
-    const int grids[6] = {
-        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_generate), R.grid_pct),
-        persistent_grid(TRAVERSE_BLOCK, reinterpret_cast<const void *>(k_trace<false>), R.grid_pct),
-        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_medium), R.grid_pct),
-        persistent_grid(BLOCK, reinterpret_cast<const void *>(shade_kernel(S, R)), R.grid_pct),
-        persistent_grid(TRAVERSE_BLOCK, S.has_media ? reinterpret_cast<const void *>(k_shadow<true>)
-                                         : reinterpret_cast<const void *>(k_shadow<false>), R.grid_pct),
-        persistent_grid(BLOCK, reinterpret_cast<const void *>(k_order), R.grid_pct),
-    };
+    int grids[6];
+    stage_grids(S, R, grids);
     const uint64_t depth_bound = static_cast<uint64_t>(std::max(R.max_depth, R.min_depth)) + 2;
     const uint64_t max_launches = ((R.total_paths + cap - 1) / cap + 2) * depth_bound + 64;
     uint64_t launches[STAGE_COUNT] = {};

@@ -3,6 +3,8 @@
 
 #include <atomic>
 #include <cstdint>
+#include <utility>
+#include <vector>
 
 #include <cuda_runtime.h>
 
@@ -68,9 +70,11 @@ struct RenderStats
 // flag stopped the loop early.
 // profile: 0 none (graphs allowed), 1 per-stage CUDA events (no graphs),
 //          2 traversal counters in the closest-hit stage (no graphs, slower)
+// progress (optional, graphs only): per launch of the two-bounce graph, the milliseconds
+// since the loop started at the end of that launch and the camera paths generated by then
 cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffers &B, cudaStream_t st,
                              const std::atomic<bool> *cancel, bool use_graphs, int profile, RenderStats *stats,
-                             bool *cancelled);
+                             bool *cancelled, std::vector<std::pair<double, uint64_t>> *progress = nullptr);
 
 // Allocation-free variant of render_wavefront: all scratch (queues, film, counters) lives
 // in a fixed device array; see the block comment above render_wavefront_noalloc.
@@ -86,6 +90,24 @@ cudaError_t render_wavefront_noalloc(const DevScene &S, const DevRender &R, void
 
 // radiance / weight -> rgb (3 floats per pixel)
 cudaError_t launch_resolve(const float4 *film, float *rgb, uint32_t pixels, cudaStream_t st);
+
+// merged batches of scenes: index shifts applied to one scene's slice of the combined
+// arrays (instance light indices stay scene-local), and the per-scene resolve of the
+// combined film
+struct RebaseOffsets
+{
+    uint32_t node, tri, inst, geo, mat, light, med, shade_tri, light_tri;
+};
+cudaError_t launch_rebase_scene(CWNode *nodes, uint32_t n_nodes, TriRec *tris, uint32_t n_tris, Instance *inst,
+                                uint32_t n_inst, Geometry *geo, uint32_t n_geo, AreaLight *lights, uint32_t n_lights,
+                                const RebaseOffsets &o, cudaStream_t st);
+struct BatchOut
+{
+    float *rgb;               // device image of width * height * 3 floats
+    uint32_t row_base, width, height, pad;
+};
+cudaError_t launch_resolve_batch(const float4 *film, uint32_t film_width, const BatchOut *outs, uint32_t count,
+                                 uint32_t max_pixels, cudaStream_t st);
 // g-buffer resolve (sum / weight; normals renormalised) into 3 floats per pixel
 cudaError_t launch_resolve_aov(const float4 *film, const float4 *aov, float *out, uint32_t pixels, bool normal,
                                cudaStream_t st);

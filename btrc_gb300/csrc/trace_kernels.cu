@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(TRACE_BLOCK) k_trace_closest_dyn(DevScene S, c
     traverse_refill<false>(
         reinterpret_cast<const float4 *>(S.nodes), reinterpret_cast<const float4 *>(S.tris), S.node_count, cursor, n,
         REFILL_LANES, err,
-        [&](uint32_t i, float *o, float *d, float &t1) {
+        [&](uint32_t i, float *o, float *d, float &t1, uint32_t &) {
             const float4 ro = __ldg(reinterpret_cast<const float4 *>(rays) + i * 2);
             const float4 rd = __ldg(reinterpret_cast<const float4 *>(rays) + i * 2 + 1);
             o[0] = ro.x; o[1] = ro.y; o[2] = ro.z;
@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(TRACE_BLOCK) k_trace_any_dyn(DevScene S, const
     traverse_refill<true>(
         reinterpret_cast<const float4 *>(S.nodes), reinterpret_cast<const float4 *>(S.tris), S.node_count, cursor, n,
         REFILL_LANES, err,
-        [&](uint32_t i, float *o, float *d, float &t1) {
+        [&](uint32_t i, float *o, float *d, float &t1, uint32_t &) {
             const float4 ro = __ldg(reinterpret_cast<const float4 *>(rays) + i * 2);
             const float4 rd = __ldg(reinterpret_cast<const float4 *>(rays) + i * 2 + 1);
             o[0] = ro.x; o[1] = ro.y; o[2] = ro.z;

@@ -400,7 +400,7 @@ namespace bt {
 //
 // The kernel launches 128-thread blocks (TRAVERSE_WARPS warps, one shared-memory slice
 // each), and all 32 lanes of a warp enter (the warp-wide votes use the full mask).
-//   fetch(i, o, d, t1): load ray i;  emit(i, hit): store its result
+//   fetch(i, o, d, t1, root): load ray i;  emit(i, hit): store its result
 constexpr int REFILL_LANES = 8;  // idle lanes that trigger a warp refill (measured best of 4/8/12/16/24)
 constexpr int TRAVERSE_BLOCK = 128;
 constexpr int TRAVERSE_WARPS = TRAVERSE_BLOCK / 32;
@@ -408,6 +408,8 @@ constexpr int TRAVERSE_WARPS = TRAVERSE_BLOCK / 32;
 constexpr uint32_t TRI_INDEX_BITS = 27;
 constexpr uint32_t MAX_POOLED_TRIANGLES = 1u << TRI_INDEX_BITS;
 
+// fetch(i, o, d, t1, root) loads ray i; root (0 unless fetch sets it) is the node the
+// ray starts from, so that one node array can hold several BVHs
 template<bool ANY, bool COUNT = false, typename Fetch, typename Emit>
 __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes4, const float4 *__restrict__ tris4,
                                                 uint32_t node_count, uint32_t *cursor, uint32_t n, int refill,
@@ -450,7 +452,8 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
                 if(mine < n)
                 {
                     float o[3], d[3], t1;
-                    fetch(mine, o, d, t1);
+                    uint32_t root = 0;
+                    fetch(mine, o, d, t1, root);
                     r = make_trav_ray(o[0], o[1], o[2], d[0], d[1], d[2]);
                     ray = mine;
                     best.hit = false;
@@ -458,7 +461,7 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
                     best.b1 = best.b2 = 0.0f;
                     best.inst = best.prim = 0xffffffffu;
                     sp = 0;
-                    ngroup = make_uint2(0u, node_count ? 0x80000000u : 0u);
+                    ngroup = make_uint2(root, node_count ? 0x80000000u : 0u);
                     tgroup = make_uint2(0u, 0u);
                     state = 1;
                     s_ray0[warp][lane] = make_float4(r.ox, r.oy, r.oz, r.Sx);

@@ -260,28 +260,40 @@ btrc_status btrc_medium_tr_batch(btrc_ctx *ctx, const btrc_scene *scene, int32_t
                                  const uint64_t *d_seeds, uint64_t n, float *d_out, void *stream);
 
 /* ---- Batched rendering of many scenes (no counterpart in the reference) ------------
-   Renders n built scenes (each with its own renderer settings) through concurrent render
-   lanes: every lane owns a CUDA stream, its path queues and a host thread, and renders
-   its share of the scenes with captured per-bounce graphs. Scenes are assigned
+   Renders n built scenes (each with its own renderer settings) in one of two ways.
+   Lanes: concurrent render lanes, each with its own CUDA stream, path queues and host
+   thread, render their share of the scenes with captured per-bounce graphs; scenes go
    longest-first to the least loaded lane. With autotune, each scene class (film size and
    triangle count, in powers of two) gets the queue capacity and persistent-grid size
-   that rendered a probe fastest; choices are cached in the context, and probing happens
-   before the timed batch. */
+   that rendered a probe fastest. Merged (opts->merged): the scenes are concatenated into
+   one device scene (each scene's BVH, instances, materials and lights become slices of
+   combined arrays, its film a band of rows of one film) and every path carries its scene
+   in its film row, so one queue and one set of persistent stage kernels render them all;
+   autotune picks queue capacity, stage-kernel block size and grid size for the batch.
+   Choices are cached in the context; probing happens before the timed batch. */
 typedef struct btrc_batch_opts
 {
     int32_t lanes;             /* concurrent render lanes (<= 0: 4) */
-    int32_t autotune;          /* 1: choose queue capacity and grid size per scene class */
+    int32_t autotune;          /* 1: choose queue capacity and grid size per scene class (lanes), or
+                                  queue capacity, stage-kernel block size and grid size (merged) */
     int32_t output_on_device;  /* 1: rgb_out[i] are device pointers, 0: host pointers */
+    int32_t merged;            /* 1: one merged pass: every scene's paths in one path queue through
+                                  one set of persistent stage kernels under one captured bounce graph
+                                  (scenes without media, textures, image lights or volumes; at most
+                                  255 scenes, 65535 film rows in total). The concatenated scene is
+                                  kept for the next call with the same built scenes. */
 } btrc_batch_opts;
 
 typedef struct btrc_batch_scene_stats
 {
     uint64_t paths;
-    double ms;                 /* wall time of the scene's render in its lane */
+    double ms;                 /* lanes: wall time of the scene's render in its lane; merged: device
+                                  time from the start of the pass until every path of the scene had
+                                  been generated and could have ended (an upper bound) */
     int32_t lane;
     uint32_t capacity;         /* queue capacity used */
     int32_t grid_pct;          /* persistent grid size used, percent of full occupancy */
-    int32_t pad;
+    int32_t block;             /* threads per block of the stage kernels */
 } btrc_batch_scene_stats;
 
 /* rgb_out[i]: width_i * height_i * 3 floats for scene i. stats (n entries) and total_ms

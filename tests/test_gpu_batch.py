@@ -31,3 +31,42 @@ def test_batch_matches_single_renders(gpu_ctx, scene_dir):
         assert np.allclose(o.cpu().numpy(), h, rtol=1e-4, atol=1e-5)
     for s in scs:
         s.close()
+
+
+def test_merged_batch_matches_single_renders(gpu_ctx, scene_dir):
+    """One merged pass (every scene's paths in one queue, one set of stage kernels, each
+    path's scene read from its film row) gives every scene the image of its own render:
+    same sampler streams, rebased BVH / instance / light indices, per-scene cameras,
+    lights, sky and path-length rules."""
+    import torch
+    paths = scenes.batch(count=6, seed=78, out_dir=scene_dir / "batch-merged")
+    scs = [gpu_ctx.load_scene(p).build() for p in paths]
+    infos = [s.info() for s in scs]
+    refs = [gpu_ctx.render(s) for s in scs]
+    outs = [np.zeros((i.height, i.width, 3), np.float32) for i in infos]
+    stats, total = gpu_ctx.render_batch(scs, outs, autotune=False, merged=True)
+    assert total > 0
+    for o, r, st, i in zip(outs, refs, stats, infos):
+        assert st["paths"] == i.width * i.height * i.spp
+        assert 0 < st["ms"] <= total
+        assert np.allclose(o, r, rtol=1e-4, atol=1e-5), np.abs(o - r).max()
+    # autotuned, device outputs; the concatenated scene is reused
+    outs_d = [torch.zeros((i.height, i.width, 3), dtype=torch.float32, device="cuda") for i in infos]
+    stats, _ = gpu_ctx.render_batch(scs, outs_d, autotune=True, merged=True)
+    torch.cuda.synchronize()
+    for o, r, st in zip(outs_d, refs, stats):
+        assert st["block"] in (128, 256) and st["grid_pct"] in (50, 100) and st["capacity"] > 0
+        assert np.allclose(o.cpu().numpy(), r, rtol=1e-4, atol=1e-5)
+    for s in scs:
+        s.close()
+
+
+def test_merged_batch_refuses_media(gpu_ctx, scene_dir):
+    import btrc_gb300 as B
+    p = scenes.cornell(out_dir=scene_dir / "cornell", width=48, height=48, spp=4, variant="fog")
+    sc = gpu_ctx.load_scene(p).build()
+    out = np.zeros((48, 48, 3), np.float32)
+    with pytest.raises(B.BtrcError) as e:
+        gpu_ctx.render_batch([sc], [out], merged=True)
+    assert e.value.status == 8
+    sc.close()
