@@ -48,7 +48,8 @@ struct MergedBatch
     std::vector<uint64_t> serials;
     std::vector<void *> allocs;
     DevScene S{};
-    std::vector<BatchScene> table;
+    std::vector<BatchScene> table;   // in queue order: fewest camera paths first
+    std::vector<uint32_t> input;     // table entry -> position in the caller's scene list
     BatchScene *d_table = nullptr;
     uint8_t *d_row_scene = nullptr;
     BatchOut *d_outs = nullptr;
@@ -1655,7 +1656,16 @@ std::unique_ptr<MergedBatch> merge_scenes(btrc_ctx *ctx, btrc_scene *const *scen
         if(bytes)
             check_cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st), "merged batch copy");
     };
-    for(uint32_t i = 0; i < n; ++i)
+    // queue order: scenes with fewer camera paths first, so that small scenes finish early
+    std::vector<uint32_t> order(n);
+    std::iota(order.begin(), order.end(), 0u);
+    auto paths_of = [&](uint32_t i) {
+        const HostScene &H = scenes[i]->host;
+        return static_cast<uint64_t>(H.params.width) * H.params.height * H.params.spp;
+    };
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return paths_of(a) < paths_of(b); });
+    mb->input = order;
+    for(uint32_t i : order)
     {
         const btrc_scene *sc = scenes[i];
         const DevScene &D = sc->dev;
@@ -1714,7 +1724,7 @@ std::unique_ptr<MergedBatch> merge_scenes(btrc_ctx *ctx, btrc_scene *const *scen
     mb->film_rows = static_cast<uint32_t>(rows);
     mb->total_paths = path_begin;
     DevScene &S = mb->S;
-    S = scenes[0]->dev;
+    S = scenes[order[0]]->dev;
     S.nodes = reinterpret_cast<const F4 *>(d_nodes);
     S.tris = reinterpret_cast<const F4 *>(d_tris);
     S.node_count = static_cast<uint32_t>(nodes);
@@ -1793,7 +1803,7 @@ double merged_render(btrc_ctx *ctx, MergedBatch &mb, uint32_t capacity, int bloc
         for(uint32_t i = 0; i < n; ++i)
         {
             const DevRender &r = mb.table[i].R;
-            o[i].rgb = on_dev ? outs[i] : scratch + at * 3;
+            o[i].rgb = on_dev ? outs[mb.input[i]] : scratch + at * 3;
             o[i].row_base = mb.table[i].row_base;
             o[i].width = static_cast<uint32_t>(r.width);
             o[i].height = static_cast<uint32_t>(r.height);
@@ -1804,7 +1814,7 @@ double merged_render(btrc_ctx *ctx, MergedBatch &mb, uint32_t capacity, int bloc
         check_cuda(launch_resolve_batch(ctx->buf.film, mb.film_width, mb.d_outs, n, max_px, st), "batch resolve");
         if(!on_dev)
             for(uint32_t i = 0; i < n; ++i)
-                check_cuda(cudaMemcpyAsync(outs[i], o[i].rgb,
+                check_cuda(cudaMemcpyAsync(outs[mb.input[i]], o[i].rgb,
                                            static_cast<size_t>(o[i].width) * o[i].height * 3 * sizeof(float),
                                            cudaMemcpyDeviceToHost, st),
                            "image download");
@@ -1840,7 +1850,7 @@ double merged_render(btrc_ctx *ctx, MergedBatch &mb, uint32_t capacity, int bloc
 void autotune_merged(btrc_ctx *ctx, MergedBatch &mb)
 {
     double best = 1e300;
-    for(uint32_t cap : { 1u << 21, 1u << 22, 1u << 23, 1u << 24 })
+    for(uint32_t cap : { 1u << 21, 1u << 22, 1u << 23, 1u << 24, 1u << 25 })
         for(int block : { 128, 256 })
             for(int pct : { 100, 50 })
             {
@@ -1900,14 +1910,15 @@ btrc_status btrc_render_batch(btrc_ctx *ctx, btrc_scene *const *scenes, uint32_t
             if(total_ms)
                 *total_ms = ms;
             if(stats)
-                for(uint32_t i = 0; i < n; ++i)
+                for(uint32_t k = 0; k < n; ++k)
                 {
-                    stats[i].paths = mb.table[i].R.total_paths;
-                    stats[i].ms = done[i];
-                    stats[i].lane = 0;
-                    stats[i].capacity = static_cast<uint32_t>(std::min<uint64_t>(cap, mb.total_paths));
-                    stats[i].grid_pct = pct;
-                    stats[i].block = block > 0 ? block : 256;
+                    btrc_batch_scene_stats &sst = stats[mb.input[k]];
+                    sst.paths = mb.table[k].R.total_paths;
+                    sst.ms = done[k];
+                    sst.lane = 0;
+                    sst.capacity = static_cast<uint32_t>(std::min<uint64_t>(cap, mb.total_paths));
+                    sst.grid_pct = pct;
+                    sst.block = block > 0 ? block : 256;
                 }
             return;
         }

@@ -289,7 +289,8 @@ typedef struct btrc_batch_scene_stats
     uint64_t paths;
     double ms;                 /* lanes: wall time of the scene's render in its lane; merged: device
                                   time from the start of the pass until every path of the scene had
-                                  been generated and could have ended (an upper bound) */
+                                  been generated and could have ended (an upper bound; the pass
+                                  queues scenes with fewer camera paths first) */
     int32_t lane;
     uint32_t capacity;         /* queue capacity used */
     int32_t grid_pct;          /* persistent grid size used, percent of full occupancy */
