@@ -213,6 +213,20 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def l2_figures():
+    """L2 traffic of k_trace from the committed ncu capture of two launches of the 1080p
+    terrain (lts__t_bytes and ncu's L2 throughput as a fraction of its peak)."""
+    path = ROOT / "profiles" / "trace_traffic.json"
+    try:
+        tj = json.loads(path.read_text())
+        return {k: tj[k] for k in ("lts_bytes_camera_launch", "lts_bytes_first_bounce_launch",
+                                   "lts_frac_of_peak_camera", "lts_frac_of_peak_first_bounce",
+                                   "l2_gbs_camera", "l2_gbs_first_bounce") if k in tj} | {
+            "source": "profiles/k_trace_l2_terrain-1080p.md (ncu, one pass, two launches)"}
+    except (OSError, ValueError):
+        return None
+
+
 def _time_to(curve, target):
     """First time at which a (time_ms, relMSE) curve reaches target, interpolated in
     log-log between the bracketing points; None if it never does."""
@@ -481,7 +495,24 @@ def run_ours(args, world, rank, local):
     trace_launches = prof["stage_launches"]["trace"]
     ext_rays = cnt["extension_rays"]
     node_b, tri_b = 80, 48
-    trace_bytes = ext_rays * (32 + 20) + cnt["node_visits"] * node_b + cnt["tri_tests"] * tri_b
+    # algorithmic bytes: node visits and triangle tests per ray from the oracle's traversal
+    # of the same BVH on camera and bounce rays of this workload, weighted by this frame's
+    # camera rays (one per path) and secondary rays; the kernel's own counters beside them
+    cam_rays = min(cnt["paths"], ext_rays)
+    sec_rays = ext_rays - cam_rays
+    try:
+        tc = traversal_counts(args, ctx, sc)
+        c, b = tc["camera"], tc["bounce"]
+        oracle_nodes = cam_rays * c["oracle_nodes"] + sec_rays * b["oracle_nodes"]
+        oracle_tris = cam_rays * c["oracle_tris"] + sec_rays * b["oracle_tris"]
+        counts_source = ("oracle: sequential exact-box traversal of the exported BVH on 1/8 of the camera rays "
+                         "and one diffuse bounce ray per camera hit, weighted by this frame's camera and "
+                         "secondary rays")
+    except Exception as ex:  # fall back to the kernel's counters, and say so
+        tc = {"error": str(ex)}
+        oracle_nodes, oracle_tris = cnt["node_visits"], cnt["tri_tests"]
+        counts_source = "kernel counters (profile 2): the oracle count failed"
+    trace_bytes = ext_rays * (32 + 20) + oracle_nodes * node_b + oracle_tris * tri_b
     achieved = trace_bytes / (trace_ms / 1000) / 1e9 if trace_ms > 0 else None
     # DRAM bytes per camera / secondary ray from the committed ncu capture, scaled to this
     # run's average launch
@@ -551,8 +582,13 @@ def run_ours(args, world, rank, local):
                          "peak": hbm_peak, "unit": "GB/s",
                          "frac": (achieved / hbm_peak) if achieved else None, "traffic": traffic,
                          "bytes_per_ray": trace_bytes / max(ext_rays, 1),
-                         "nodes_per_ray": cnt["node_visits"] / max(ext_rays, 1),
-                         "tris_per_ray": cnt["tri_tests"] / max(ext_rays, 1),
+                         "nodes_per_ray": oracle_nodes / max(ext_rays, 1),
+                         "tris_per_ray": oracle_tris / max(ext_rays, 1),
+                         "counts_source": counts_source,
+                         "kernel_nodes_per_ray": cnt["node_visits"] / max(ext_rays, 1),
+                         "kernel_tris_per_ray": cnt["tri_tests"] / max(ext_rays, 1),
+                         "probe_counts": tc,
+                         "l2": l2_figures(),
                          "launches": trace_launches, "avg_launch_ms": trace_ms / max(trace_launches, 1),
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6800",
                          "traffic_source": "ncu dram__bytes per camera ray and per secondary ray "
@@ -570,6 +606,75 @@ def run_ours(args, world, rank, local):
         print(json.dumps(line), flush=True)
     sc.close()
     ctx.close()
+
+
+def probe_rays(args, ctx, sc, stride: int = 1):
+    """Camera rays through pixel centres of the workload's camera (every stride-th pixel)
+    and one ray per camera hit in a uniform direction of the upper hemisphere (the
+    terrain's surfaces face up), traced through btrc_trace_closest."""
+    import math
+    import torch
+    p = scene_path(args)
+    js = json.loads(Path(p).read_text())
+    W, H, cam = js["width"], js["height"], js["camera"]
+    eye, dst, up = (np.array(cam[k], np.float64) for k in ("eye", "dst", "up"))
+    fwd = (dst - eye) / np.linalg.norm(dst - eye)
+    right = np.cross(fwd, up)
+    right /= np.linalg.norm(right)
+    upv = np.cross(right, fwd)
+    th = math.tan(math.radians(cam["fov_y"]["deg"]) / 2)
+    X, Y = np.meshgrid((2 * (np.arange(W) + 0.5) / W - 1) * th * W / H, (1 - 2 * (np.arange(H) + 0.5) / H) * th)
+    d = (fwd[None, None] + X[..., None] * right + Y[..., None] * upv).reshape(-1, 3)[::stride]
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+
+    def pack(o, dirs):
+        r = np.zeros((len(o), 8), np.float32)
+        r[:, 0:3], r[:, 4:7], r[:, 7] = o, dirs, 3.0e38
+        return r
+
+    def trace(rays):
+        m = len(rays)
+        dr = torch.from_numpy(rays).cuda()
+        f = torch.zeros(m, dtype=torch.int32, device="cuda")
+        h = torch.zeros((m, 4), dtype=torch.float32, device="cuda")
+        ctx.trace_closest(sc, dr, m, f, h)
+        torch.cuda.synchronize()
+        return f.cpu().numpy().view(np.uint32), h.cpu().numpy()
+
+    cam_rays = pack(np.broadcast_to(eye, d.shape), d)
+    f, h = trace(cam_rays)
+    hit = f != 0
+    org = eye + d[hit] * (h[hit, 0:1].astype(np.float64) - 1e-4)
+    nd = np.random.default_rng(3).normal(size=org.shape)
+    nd /= np.linalg.norm(nd, axis=1, keepdims=True)
+    nd[:, 1] = np.abs(nd[:, 1])
+    return cam_rays, pack(org, nd), trace
+
+
+def traversal_counts(args, ctx, sc):
+    """Node visits and triangle tests per camera ray and per bounce ray: the oracle's
+    sequential exact-box traversal of the same exported BVH on the same rays, and the
+    kernel's own per-ray counters (btrc_trace_stats) beside it."""
+    import torch
+    import btrc_gb300 as B
+    import oracle
+    hctx = B.Context(-1)
+    hsc = hctx.load_scene(scene_path(args)).build()
+    nodes, tris = hsc.export_bvh()
+    hsc.close()
+    hctx.close()
+    cam, sec, _ = probe_rays(args, ctx, sc, stride=8)
+    out = {}
+    for name, rays in (("camera", cam), ("bounce", sec)):
+        nv, tt = oracle.wide_bvh_counts(nodes, tris, rays)
+        dr = torch.from_numpy(rays).cuda()
+        gn = torch.zeros(len(rays), dtype=torch.int32, device="cuda")
+        gt = torch.zeros(len(rays), dtype=torch.int32, device="cuda")
+        ctx.trace_stats(sc, dr, len(rays), gn, gt)
+        torch.cuda.synchronize()
+        out[name] = {"rays": len(rays), "oracle_nodes": float(nv.mean()), "oracle_tris": float(tt.mean()),
+                     "kernel_nodes": float(gn.cpu().numpy().mean()), "kernel_tris": float(gt.cpu().numpy().mean())}
+    return out
 
 
 def trace_probe(args):

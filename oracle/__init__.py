@@ -62,6 +62,7 @@ def lib() -> C.CDLL:
         L.oracle_prepare.argtypes = [C.POINTER(OracleScene)]
         L.oracle_medium_tr_batch.argtypes = [C.POINTER(OracleScene), C.c_int, _vp, _vp, C.c_uint64, _vp]
         L.oracle_release.argtypes = [_vp]
+        L.oracle_wide_bvh_counts.argtypes = [_vp, _vp, _vp, C.c_uint64, _vp, _vp, C.c_int]
         L.oracle_render.argtypes = [_vp, C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, _vp, C.c_int]
         L.oracle_render_aov.argtypes = [_vp, C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, _vp, _vp, C.c_int]
         _lib = L
@@ -135,6 +136,19 @@ def pcg32_stream(initstate: int, initseq: int, n: int) -> np.ndarray:
 def murmur64a(data: bytes, seed: int = 0) -> int:
     buf = np.frombuffer(data, np.uint8).copy() if data else np.zeros(1, np.uint8)
     return int(lib().oracle_murmur64a(_p(buf), len(data), seed))
+
+
+def wide_bvh_counts(nodes: np.ndarray, tris: np.ndarray, rays: np.ndarray, threads: int = 0):
+    """Node visits and triangle tests per ray of a sequential, exact-box closest-hit
+    traversal of the library's exported 8-wide BVH (nodes: (n, 80) uint8, tris: (m, 48)
+    uint8 as btrc_scene_export_bvh writes them; rays: (k, 8) float32)."""
+    nodes = np.ascontiguousarray(nodes, np.uint8)
+    tris = np.ascontiguousarray(tris).view(np.uint8)
+    rays = np.ascontiguousarray(rays, np.float32)
+    nv = np.zeros(len(rays), np.uint32)
+    tt = np.zeros(len(rays), np.uint32)
+    lib().oracle_wide_bvh_counts(_p(nodes), _p(tris), _p(rays), len(rays), _p(nv), _p(tt), threads)
+    return nv, tt
 
 
 def bsdf_batch(op: int, material: np.ndarray, wo: np.ndarray, wi_or_u: np.ndarray, fp32: bool = False) -> np.ndarray:

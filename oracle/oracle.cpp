@@ -2638,6 +2638,117 @@ void trace_path(const Prepared &P, uint64_t g, double *film, double *aov = nullp
 
 } // namespace
 
+// ------------------------------------------------------------------ wide-BVH work counts
+// The closest-hit traversal of the library's exported 8-wide BVH (80-byte nodes,
+// 48-byte triangle records; layout in btrc_gb300/csrc/layout.h), restated sequentially:
+// node groups visited in the kernel's child order (slot XOR ray octant), child boxes
+// dequantised and slab-tested exactly in FP64 against the current closest t, every
+// triangle of a hit leaf tested with the watertight test. The counts are the traversal's
+// algorithmic work on these rays: node visits and triangle tests with exact box tests and
+// no deferred triangle rounds (the kernel pads its FP32 box tests and tests triangles in
+// pooled rounds, so it can only do more).
+namespace {
+
+struct WideCount
+{
+    uint32_t nodes = 0, tris = 0;
+};
+
+WideCount wide_count(const uint8_t *nodes, const float *tris, const float *o, const float *d, float t1)
+{
+    WideCount c;
+    const WRay wr = make_wray(o, d);
+    const int octant = (d[0] < 0) | ((d[1] < 0) << 1) | ((d[2] < 0) << 2);
+    const uint32_t oct_inv = static_cast<uint32_t>(7 - octant);
+    double inv[3];
+    for(int a = 0; a < 3; ++a)
+    {
+        const double dd = std::fabs(d[a]) < 1e-20 ? std::copysign(1e-20, static_cast<double>(d[a])) : d[a];
+        inv[a] = 1.0 / dd;
+    }
+    float best = t1;
+    uint32_t stack_x[64], stack_y[64];
+    int sp = 0;
+    uint32_t ngx = 0, ngy = 0x80000000u;
+    for(;;)
+    {
+        uint32_t tgx = 0, tgy = 0;
+        if(ngy > 0x00ffffffu)
+        {
+            int bit = 31;
+            while(!((ngy >> bit) & 1u))
+                --bit;
+            const uint32_t slot = (static_cast<uint32_t>(bit) - 24u) ^ oct_inv;
+            const uint32_t below = slot ? (ngy & ((1u << slot) - 1u) & 0xffu) : 0u;
+            const uint32_t ni = ngx + static_cast<uint32_t>(__builtin_popcount(below));
+            ngy &= ~(1u << bit);
+            if(ngy > 0x00ffffffu && sp < 64)
+            {
+                stack_x[sp] = ngx;
+                stack_y[sp] = ngy;
+                ++sp;
+            }
+            ++c.nodes;
+            const uint8_t *nd = nodes + static_cast<size_t>(ni) * 80;
+            float px[3];
+            std::memcpy(px, nd, 12);
+            uint32_t child_base, tri_base;
+            std::memcpy(&child_base, nd + 16, 4);
+            std::memcpy(&tri_base, nd + 20, 4);
+            const uint8_t imask = nd[15];
+            uint32_t hm = 0;
+            for(int sl = 0; sl < 8; ++sl)
+            {
+                const uint32_t m = nd[24 + sl];
+                if(!m)
+                    continue;
+                double tmin = 0.0, tmax = best;
+                for(int a = 0; a < 3; ++a)
+                {
+                    const double scale = std::ldexp(1.0, static_cast<int>(nd[12 + a]) - 127);
+                    const double lo = px[a] + nd[32 + a * 8 + sl] * scale, hi = px[a] + nd[56 + a * 8 + sl] * scale;
+                    const double ta = (lo - o[a]) * inv[a], tb = (hi - o[a]) * inv[a];
+                    tmin = std::max(tmin, std::min(ta, tb));
+                    tmax = std::min(tmax, std::max(ta, tb));
+                }
+                if(tmin <= tmax)
+                {
+                    const bool inner = (m & 0x18u) == 0x18u;
+                    const uint32_t b = inner ? ((m & 0x1fu) ^ oct_inv) : (m & 0x1fu);
+                    hm |= (m >> 5) << b;
+                }
+            }
+            ngx = child_base;
+            ngy = (hm & 0xff000000u) | imask;
+            tgx = tri_base;
+            tgy = hm & 0x00ffffffu;
+        }
+        while(tgy)
+        {
+            int tb = 31;
+            while(!((tgy >> tb) & 1u))
+                --tb;
+            tgy &= ~(1u << tb);
+            const float *r = tris + static_cast<size_t>(tgx + static_cast<uint32_t>(tb)) * 12;
+            ++c.tris;
+            float t, b1, b2;
+            if(watertight(wr, r, r + 4, r + 8, best, t, b1, b2))
+                best = std::min(best, t);
+        }
+        if(ngy <= 0x00ffffffu)
+        {
+            if(!sp)
+                break;
+            --sp;
+            ngx = stack_x[sp];
+            ngy = stack_y[sp];
+        }
+    }
+    return c;
+}
+
+} // namespace
+
 extern "C" {
 
 // transmittance of segments (a, b: 6 floats each) through one medium of the scene, each
@@ -2655,6 +2766,18 @@ void oracle_medium_tr_batch(const OracleScene *S, int medium_id, const float *se
         const V3f b(seg[i * 6 + 3], seg[i * 6 + 4], seg[i * 6 + 5]);
         out[i] = medium_tr(*S, m, a, b, smp).x;
     }
+}
+
+// node visits and triangle tests of the exported wide BVH per ray (see wide_count)
+void oracle_wide_bvh_counts(const uint8_t *nodes, const float *tris, const float *rays, uint64_t n,
+                            uint32_t *node_visits, uint32_t *tri_tests, int threads)
+{
+    parallel_for(n, threads, [&](uint64_t i) {
+        const float *r = rays + i * 8;
+        const WideCount c = wide_count(nodes, tris, r, r + 4, r[7]);
+        node_visits[i] = c.nodes;
+        tri_tests[i] = c.tris;
+    });
 }
 
 void *oracle_bvh_build(const float *tris, const uint32_t *ids, uint64_t n)

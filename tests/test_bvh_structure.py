@@ -192,3 +192,36 @@ def test_wide_collapse_fills_nodes(native_lib, scene_dir):
         count += ((meta >> (5 + b)) & 1).astype(np.int64) * leaf
     assert count[leaf].min() >= 1 and count[leaf].max() <= 3
     assert count.sum() == len(tris)
+
+
+def test_oracle_wide_traversal_counts(native_lib, scene_dir):
+    """The oracle's sequential traversal of the exported 8-wide BVH (the algorithmic node
+    and triangle counts the benchmark's roofline uses): a ray that leaves the scene's box
+    visits the root only, every hit tests at least one triangle, and a shorter segment
+    never does more work than the full ray."""
+    path = scenes.random_soup(scene_dir / "soup", seed=5, n_tris=20000, n_instances=4)
+    ctx, sc = _host_scene(path)
+    nodes, tris = sc.export_bvh()
+    S = OS.Scene(path)
+    rng = np.random.default_rng(9)
+    n = 4000
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0:3] = rng.uniform(-2, 2, (n, 3))
+    rays[:, 4:7] = rng.normal(size=(n, 3))
+    rays[:, 7] = 3.0e38
+    nv, tt = oracle.wide_bvh_counts(nodes, tris, rays)
+    flags, _ = oracle.OracleBvh(S.tris, S.ids).closest(rays)
+    assert np.all(nv >= 1)
+    assert np.all(tt[flags != 0] >= 1)
+    short = rays.copy()
+    short[:, 7] = 1e-3
+    nv2, tt2 = oracle.wide_bvh_counts(nodes, tris, short)
+    assert np.all(nv2 <= nv) and np.all(tt2 <= tt)
+    away = np.zeros((8, 8), np.float32)
+    away[:, 0:3] = 100.0
+    away[:, 4:7] = 1.0
+    away[:, 7] = 3.0e38
+    nv3, tt3 = oracle.wide_bvh_counts(nodes, tris, away)
+    assert np.all(nv3 == 1) and np.all(tt3 == 0)
+    sc.close()
+    ctx.close()

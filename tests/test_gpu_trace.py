@@ -114,3 +114,34 @@ def test_closest_bitexact_small_terrain(gpu_ctx, scene_dir):
     rays = np.concatenate([rays, edge_rays(rng, S.tris, 50000)])
     _, hit_rate = _compare(gpu_ctx, p, rays)
     assert hit_rate > 0.25
+
+
+def test_kernel_counts_match_oracle_traversal(gpu_ctx, scene_dir):
+    """The closest-hit kernel's per-ray work counters (btrc_trace_stats) against the
+    oracle's sequential exact-box traversal of the same BVH: the kernel's padded FP32 box
+    tests can only add visits, and only a few percent of them."""
+    import torch
+    import btrc_gb300 as B
+    path = scenes.random_soup(scene_dir / "soup", seed=5, n_tris=20000, n_instances=4)
+    hctx = B.Context(-1)
+    hsc = hctx.load_scene(path).build()
+    nodes, tris = hsc.export_bvh()
+    sc = gpu_ctx.load_scene(path).build()
+    rng = np.random.default_rng(10)
+    n = 20000
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0:3] = rng.uniform(-2, 2, (n, 3))
+    rays[:, 4:7] = rng.normal(size=(n, 3))
+    rays[:, 7] = 3.0e38
+    nv, tt = oracle.wide_bvh_counts(nodes, tris, rays)
+    dr = torch.from_numpy(rays).cuda()
+    gn = torch.zeros(n, dtype=torch.int32, device="cuda")
+    gt = torch.zeros(n, dtype=torch.int32, device="cuda")
+    gpu_ctx.trace_stats(sc, dr, n, gn, gt)
+    torch.cuda.synchronize()
+    gn, gt = gn.cpu().numpy(), gt.cpu().numpy()
+    assert gn.mean() >= nv.mean() * 0.999 and gn.mean() <= nv.mean() * 1.05, (gn.mean(), nv.mean())
+    assert gt.mean() >= tt.mean() * 0.999 and gt.mean() <= tt.mean() * 1.05, (gt.mean(), tt.mean())
+    sc.close()
+    hsc.close()
+    hctx.close()
