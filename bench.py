@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-nrc", action="store_true", help="skip the radiance-cache equal-time study")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched uneven-scenes measurement")
-    ap.add_argument("--nrc-frames", type=int, default=256, help="frames of the radiance-cache study")
+    ap.add_argument("--nrc-frames", type=int, default=1000, help="frames of the radiance-cache study")
     ap.add_argument("--ref-spp", type=int, default=4096, help="spp of the converged reference image")
     ap.add_argument("--probe", choices=["nrc", "medium", "generate", "trace"],
                     help="run one small profiling case and exit: nrc (cache inference on 2^20 queries and "
@@ -244,7 +244,7 @@ def _time_to(curve, target):
     return None
 
 
-def nrc_study(B, ctx, sc, info, args):
+def nrc_study(B, ctx, sc, info, args, spread: float = 0.0):
     """Equal-time comparison of the radiance cache against the plain tracer on a built
     scene: relMSE against a converged plain render (args.ref_spp spp) as a
     function of wall time, for plain renders of 1..128 spp and for the cache (one path per
@@ -274,13 +274,13 @@ def nrc_study(B, ctx, sc, info, args):
     cache = B.RadianceCache(ctx, info.world_min, info.world_max, seed=1)
     acc = torch.zeros((H, W, 3), dtype=torch.float64, device="cuda")
     curve, elapsed, st = [], 0.0, {}
-    checkpoints = {1, 2, 4, 8, 16, 24, 32, 48, 64, 96, 128, 192, 256, 384, 512}
+    checkpoints = {1, 2, 4, 8, 16, 24, 32, 48, 64, 96, 128, 192, 256, 384, 512, 768, 1000}
     losses, queries, samples = [], 0, 0
     for f in range(args.nrc_frames):
         torch.cuda.synchronize()
         t = time.perf_counter()
         cache.render_frame(sc, f, out=img, terminate_vertex=1, train_stride=16, train_steps=4, train_batch=16384,
-                           stats=st)
+                           stats=st, spread_threshold=spread)
         acc += img
         torch.cuda.synchronize()
         elapsed += (time.perf_counter() - t) * 1000
@@ -337,6 +337,29 @@ def nrc_study(B, ctx, sc, info, args):
     except Exception as ex:
         mlp = {"error": str(ex)}
     cache.close()
+    # the same study with the path-spread termination rule (c = 0.01)
+    spread_rule = None
+    if spread > 0:
+        cache = B.RadianceCache(ctx, info.world_min, info.world_max, seed=1)
+        acc.zero_()
+        scurve, selapsed, sst = [], 0.0, {}
+        for f in range(args.nrc_frames):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            cache.render_frame(sc, f, out=img, terminate_vertex=1, train_stride=16, train_steps=4,
+                               train_batch=16384, stats=sst, spread_threshold=spread)
+            acc += img
+            torch.cuda.synchronize()
+            selapsed += (time.perf_counter() - t) * 1000
+            if f + 1 in checkpoints or f + 1 == args.nrc_frames:
+                scurve.append((selapsed, relmse(acc / (f + 1))))
+        cache.close()
+        tsp = _time_to(scurve, target)
+        tpp = _time_to(plain, target)
+        spread_rule = {"spread_c": spread, "nrc_ms_to_target": tsp,
+                       "time_ratio_nrc_over_plain": (tsp / tpp) if (tsp and tpp) else None,
+                       "nrc_ms_per_frame": selapsed / args.nrc_frames, "nrc_queries_per_frame": sst.get("queries"),
+                       "nrc_curve_ms_relmse": [[round(t, 3), e] for t, e in scurve]}
     tp, tn = _time_to(plain, target), _time_to(curve, target)
     # the cache's relMSE at the plain tracer's time to reach the target, and vice versa
     at_plain = None
@@ -354,6 +377,7 @@ def nrc_study(B, ctx, sc, info, args):
         "nrc_queries_per_frame": queries, "nrc_train_samples_per_frame": samples,
         "nrc_loss_first_last": [float(np.mean(losses[:4])), float(np.mean(losses[-4:]))],
         "mlp": mlp,
+        "spread_rule": spread_rule,
         "setup": "paths end in the cache at the first non-delta vertex after one bounce; 1/16 of the pixels "
                  "trace training paths each frame; 4 Adam steps x 16384 samples per frame; cache trained "
                  "from scratch inside the timed frames",
@@ -539,20 +563,20 @@ def run_ours(args, world, rank, local):
     nrc_interior = None
     if rank == 0 and not args.no_nrc:
         try:
-            nrc = nrc_study(B, ctx, sc, info, args)
+            nrc = nrc_study(B, ctx, sc, info, args, spread=0.01)
         except Exception as ex:  # the study must not sink the throughput number
             nrc = {"error": str(ex)}
         # the same study in a closed interior, where most light arrives after several bounces
         try:
             from btrc_gb300 import scenes
             csc = ctx.load_scene(scenes.cornell(width=512, height=512, spp=16)).build()
-            nrc_interior = nrc_study(B, ctx, csc, csc.info(), args)
+            nrc_interior = nrc_study(B, ctx, csc, csc.info(), args, spread=0.01)
             nrc_interior = {"scene": "config 0's Cornell box (two icospheres, quad light) at 512x512",
                             **{k: nrc_interior[k] for k in ("target_relmse", "reference_spp", "plain_ms_to_target",
                                                             "nrc_ms_to_target", "time_ratio_nrc_over_plain",
                                                             "nrc_relmse_at_plain_time", "nrc_ms_per_frame",
                                                             "nrc_queries_per_frame", "plain_curve_ms_relmse",
-                                                            "nrc_curve_ms_relmse")}}
+                                                            "nrc_curve_ms_relmse", "spread_rule")}}
             csc.close()
         except Exception as ex:
             nrc_interior = {"error": str(ex)}

@@ -59,7 +59,8 @@ class RenderOpts(C.Structure):
 
 class NrcRenderOpts(C.Structure):
     _fields_ = [("frame", C.c_uint32), ("terminate_vertex", C.c_int32), ("train_stride", C.c_int32),
-                ("train_steps", C.c_int32), ("train_batch", C.c_int32), ("output_on_device", C.c_int32)]
+                ("train_steps", C.c_int32), ("train_batch", C.c_int32), ("output_on_device", C.c_int32),
+                ("spread_threshold", C.c_float)]
 
 
 class NrcFrameStats(C.Structure):
@@ -374,14 +375,17 @@ class RadianceCache:
         return out
 
     def render_frame(self, scene: "Scene", frame: int, out=None, terminate_vertex: int = 1, train_stride: int = 16,
-                     train_steps: int = 4, train_batch: int = 16384, stats: dict | None = None):
+                     train_steps: int = 4, train_batch: int = 16384, stats: dict | None = None,
+                     spread_threshold: float = 0.0):
         """One frame (one path per pixel) with cache termination, training and inference
-        (btrc_render_nrc_frame). Returns the frame image (H, W, 3)."""
+        (btrc_render_nrc_frame). spread_threshold > 0 ends paths by the path-spread rule
+        instead of at terminate_vertex. Returns the frame image (H, W, 3)."""
         info = scene.info()
         on_dev = out is not None and hasattr(out, "is_cuda") and out.is_cuda
         if out is None:
             out = np.zeros((info.height, info.width, 3), np.float32)
-        opts = NrcRenderOpts(frame, terminate_vertex, train_stride, train_steps, train_batch, 1 if on_dev else 0)
+        opts = NrcRenderOpts(frame, terminate_vertex, train_stride, train_steps, train_batch, 1 if on_dev else 0,
+                             spread_threshold)
         st = NrcFrameStats()
         self.ctx._check(self.ctx._lib.btrc_render_nrc_frame(self.ctx.handle, scene.handle, self.handle, C.byref(opts),
                                                             _ptr(out), C.byref(st)))

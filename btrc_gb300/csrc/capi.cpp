@@ -94,6 +94,7 @@ struct btrc_ctx
     float *nrc_query = nullptr, *nrc_samples = nullptr;
     float4 *nrc_weight = nullptr, *nrc_pred = nullptr;
     uint32_t *nrc_counts = nullptr;
+    float2 *nrc_spread[2] = {};      // path-spread state per queue slot, by bounce parity
 };
 
 struct btrc_scene
@@ -1268,6 +1269,8 @@ void ensure_nrc_buffers(btrc_ctx *ctx, size_t pixels, size_t sample_cap)
     ctx->nrc_pred = static_cast<float4 *>(A(sizeof(float4) * pixels));
     ctx->nrc_samples = static_cast<float *>(A(sizeof(float) * NRC_SAMPLE_FLOATS * std::max<size_t>(sample_cap, 1)));
     ctx->nrc_counts = static_cast<uint32_t *>(A(sizeof(uint32_t) * 4));
+    for(auto &sp : ctx->nrc_spread)
+        sp = static_cast<float2 *>(A(sizeof(float2) * pixels));
     ctx->nrc_pixels = pixels;
     ctx->nrc_sample_cap = sample_cap;
 }
@@ -1302,6 +1305,9 @@ btrc_status btrc_render_nrc_frame(btrc_ctx *ctx, btrc_scene *scene, btrc_nrc *nr
         DevRender R = make_render_params(scene, 1, capacity);
         R.sample_offset = opts->frame;
         R.nrc_terminate = opts->terminate_vertex;
+        R.nrc_spread_c = opts->terminate_vertex >= 0 ? opts->spread_threshold : 0.0f;
+        R.nrc_spread[0] = ctx->nrc_spread[0];
+        R.nrc_spread[1] = ctx->nrc_spread[1];
         R.nrc_query = ctx->nrc_query;
         R.nrc_weight = ctx->nrc_weight;
         R.nrc_count = ctx->nrc_counts;

@@ -81,6 +81,11 @@ struct DevRender
     float4 *nrc_weight;       // path throughput (xyz) and pixel bits (w) per query
     uint32_t *nrc_count;
     uint32_t nrc_cap;
+    // path-spread termination (> 0: end a path at its first non-delta vertex whose spread
+    // exceeds nrc_spread_c times the primary spread); per queue slot (spread sum / sqrt(a0),
+    // sqrt(a0)) in two arrays indexed by bounce parity
+    float nrc_spread_c;
+    float2 *nrc_spread[2];
     // merged batch of scenes (null for one scene): the stage kernels read each path's
     // scene from the film row of its pixel word, row_scene[y]
     const BatchScene *batch;

@@ -1388,7 +1388,26 @@ __global__ void __launch_bounds__(BLOCK, 2) k_shade(DevScene S_in, DevRender R_i
 
         V3 beta = v3(bd);
         const int depth = __float_as_int(bd.w);
-        if(NRC && depth >= R.nrc_terminate)
+        // path spread (Mueller, Rousselle, Novak, Keller, "Real-time Neural Radiance Caching
+        // for Path Tracing", 2021, section 4): a(x1..xn) = (sum_{i>=2} sqrt(|x_{i-1} - x_i|^2 /
+        // (p(w_i) |cos theta_i|)))^2 against a0 = |x0 - x1|^2 / (4 pi cos theta_1); kept
+        // normalised by sqrt(a0), so the path ends once the sum passes sqrt(c)
+        float2 spread = make_float2(0.0f, 0.0f);
+        bool spread_end = false;
+        if(NRC && R.nrc_spread_c > 0.0f)
+        {
+            const float cosv = fmaxf(fabsf(dot(sp.frame.z, d)), 1e-6f);
+            if(depth == 0)
+                spread = make_float2(0.0f, h.t / sqrtf(4.0f * PI * cosv));
+            else
+            {
+                spread = R.nrc_spread[shq][i];
+                if(bsdf_pdf > 0.0f && spread.y > 0.0f)
+                    spread.x += sqrtf(h.t * h.t / (bsdf_pdf * cosv)) / spread.y;
+                spread_end = spread.x * spread.x > R.nrc_spread_c;
+            }
+        }
+        if(NRC && (R.nrc_spread_c > 0.0f ? spread_end : depth >= R.nrc_terminate))
         {
             // terminate into the radiance cache at a non-delta vertex: the cache's
             // prediction replaces light sampling and everything after this vertex
@@ -1496,6 +1515,8 @@ __global__ void __launch_bounds__(BLOCK, 2) k_shade(DevScene S_in, DevRender R_i
             N.ray_o[k] = f4(no, __int_as_float(nmed));
             N.ray_d[k] = f4(ndir, MAX_FLOAT);
             N.bsdf_le[k] = f4(new_beta_le, stored_pdf);
+            if(NRC && R.nrc_spread_c > 0.0f)
+                R.nrc_spread[1 - shq][k] = spread;
         }
         else
             splat(film, pixel, R.width, path_rad);

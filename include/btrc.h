@@ -338,6 +338,9 @@ typedef struct btrc_nrc_render_opts
     int32_t train_steps;       /* Adam steps per frame */
     int32_t train_batch;       /* training samples per step */
     int32_t output_on_device;  /* 1: rgb_out is a device pointer */
+    float spread_threshold;    /* > 0: end paths instead at the first non-delta vertex of depth
+                                  >= 1 whose path spread exceeds this times the primary spread
+                                  (Mueller et al. 2021, c = 0.01 there); 0: the depth rule */
 } btrc_nrc_render_opts;
 
 typedef struct btrc_nrc_frame_stats

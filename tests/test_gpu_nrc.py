@@ -130,3 +130,26 @@ def test_cache_render_off_matches_plain_and_training_helps(gpu_ctx, scene_dir):
             assert np.mean(losses[-8:]) < np.mean(losses[:4])
         c.close()
     assert res["trained"] < 0.5 * res["untrained"], res
+
+
+def test_path_spread_termination(gpu_ctx, scene_dir):
+    """The path-spread rule (Mueller et al. 2021, section 4): with a vanishing threshold a
+    path ends at its first non-delta vertex after one bounce, as with the depth rule; with
+    a huge one no path ever reaches the cache; in between fewer paths end there."""
+    from btrc_gb300 import scenes
+    p = scenes.cornell(out_dir=scene_dir / "cornell", width=64, height=64, spp=1)
+    sc = gpu_ctx.load_scene(p).build()
+    info = sc.info()
+    c = B.RadianceCache(gpu_ctx, info.world_min, info.world_max, seed=2)
+    counts = {}
+    for name, kw in (("depth", {}), ("tiny", {"spread_threshold": 1e-12}), ("mid", {"spread_threshold": 1.0}),
+                     ("huge", {"spread_threshold": 1e12})):
+        st = {}
+        img = c.render_frame(sc, 0, train_stride=0, train_steps=0, stats=st, **kw)
+        assert np.isfinite(img).all()
+        counts[name] = st["queries"]
+    assert counts["huge"] == 0
+    assert counts["depth"] > 0 and counts["tiny"] >= 0.95 * counts["depth"], counts
+    assert counts["mid"] <= counts["tiny"], counts
+    c.close()
+    sc.close()
