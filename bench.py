@@ -393,7 +393,7 @@ def batch_study(B, ctx):
     from btrc_gb300 import scenes
     paths = scenes.batch(count=64, seed=1004)
     t = time.perf_counter()
-    scs = [ctx.load_scene(p).build() for p in paths]
+    scs = ctx.load_build_scenes(paths)  # all 64 loads and builds on one pool of host threads
     build_s = time.perf_counter() - t
     infos = [s.info() for s in scs]
     outs = [torch.empty((i.height, i.width, 3), dtype=torch.float32, device="cuda") for i in infos]

@@ -106,6 +106,8 @@ SIGNATURES = {
     "btrc_cancel": (None, [_vp]),
     "btrc_scene_load_json": (C.c_int, [_vp, C.c_char_p, C.POINTER(_vp)]),
     "btrc_scene_build": (C.c_int, [_vp, C.POINTER(BuildOpts)]),
+    "btrc_scenes_load_build": (C.c_int, [_vp, C.POINTER(C.c_char_p), C.c_uint32, C.POINTER(BuildOpts),
+                                         C.POINTER(_vp)]),
     "btrc_scene_info_get": (C.c_int, [_vp, C.POINTER(SceneInfo)]),
     "btrc_scene_destroy": (None, [_vp]),
     "btrc_scene_export_triangles": (C.c_int, [_vp, _vp, _vp, C.c_uint64]),
@@ -222,6 +224,21 @@ class Context:
         sc = Scene(self, h)
         self._scenes.add(sc)
         return sc
+
+    def load_build_scenes(self, paths: list, threads: int = 0) -> list:
+        """Load and build many scenes at once on one pool of host threads
+        (btrc_scenes_load_build). Returns the built scenes in order."""
+        n = len(paths)
+        arr_p = (C.c_char_p * n)(*[str(p).encode() for p in paths])
+        arr_s = (_vp * n)()
+        opts = BuildOpts(threads)
+        self._check(self._lib.btrc_scenes_load_build(self.handle, arr_p, n, C.byref(opts), arr_s))
+        out = []
+        for h in arr_s:
+            sc = Scene(self, _vp(h))
+            self._scenes.add(sc)
+            out.append(sc)
+        return out
 
     def cancel(self):
         self._lib.btrc_cancel(self.handle)

@@ -5,6 +5,7 @@
 #include <chrono>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <memory>
 #include <mutex>
 #include <new>
@@ -268,7 +269,14 @@ void build_scene(btrc_scene *sc, int threads)
 
     if(threads <= 0)
         threads = static_cast<int>(std::max(1u, std::thread::hardware_concurrency()));
-    TaskPool pool(threads);
+    std::unique_ptr<TaskPool> own;
+    TaskPool *pp = current_pool();  // a batch build's pool, else threads of our own
+    if(!pp)
+    {
+        own = std::make_unique<TaskPool>(threads);
+        pp = own.get();
+    }
+    TaskPool &pool = *pp;
 
     // flatten instances into world-space triangles (single-level BVH), in parallel over
     // triangle ranges of each instance
@@ -717,6 +725,61 @@ btrc_status btrc_scene_build(btrc_scene *scene, const btrc_build_opts *opts)
     if(!scene)
         return BTRC_ERR_INVALID_ARG;
     return guarded(scene->ctx, [&] { build_scene(scene, opts ? opts->threads : 0); });
+}
+
+btrc_status btrc_scenes_load_build(btrc_ctx *ctx, const char *const *paths, uint32_t n, const btrc_build_opts *opts,
+                                   btrc_scene **out)
+{
+    if(!ctx || (n > 0 && (!paths || !out)))
+        return BTRC_ERR_INVALID_ARG;
+    for(uint32_t i = 0; i < n; ++i)
+    {
+        out[i] = nullptr;
+        if(!paths[i])
+            return BTRC_ERR_INVALID_ARG;
+    }
+    std::vector<std::unique_ptr<btrc_scene>> scs(n);
+    std::vector<std::exception_ptr> errors(n);
+    const btrc_status s = guarded(ctx, [&] {
+        int threads = opts ? opts->threads : 0;
+        if(threads <= 0)
+            threads = static_cast<int>(std::max(1u, std::thread::hardware_concurrency()));
+        // one pool for everything: scene tasks, and inside them the OBJ pieces, the
+        // geometry records and the BVH builds, so small and large scenes share the cores
+        TaskPool pool(threads);
+        PoolScope scope(pool);
+        TaskPool::Group g;
+        for(uint32_t i = 0; i < n; ++i)
+            pool.run(g, [&, i] {
+                try
+                {
+                    auto sc = std::make_unique<btrc_scene>();
+                    sc->ctx = ctx;
+                    sc->host = load_scene(paths[i]);
+                    if(ctx->device >= 0)
+                        check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+                    build_scene(sc.get(), threads);
+                    scs[i] = std::move(sc);
+                }
+                catch(...)
+                {
+                    errors[i] = std::current_exception();
+                }
+            });
+        pool.wait(g);
+        // the first scene that failed reports, classified like a single load / build
+        for(uint32_t i = 0; i < n; ++i)
+            if(errors[i])
+                std::rethrow_exception(errors[i]);
+    });
+    if(s != BTRC_OK)
+        return s;  // the scenes built so far are freed with scs
+    for(uint32_t i = 0; i < n; ++i)
+    {
+        out[i] = scs[i].release();
+        ctx->scenes.insert(out[i]);
+    }
+    return BTRC_OK;
 }
 
 btrc_status btrc_scene_info_get(const btrc_scene *sc, btrc_scene_info *out)

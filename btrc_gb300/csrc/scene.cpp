@@ -9,6 +9,7 @@
 #include <filesystem>
 #include <fstream>
 #include <map>
+#include <memory>
 #include <numeric>
 #include <stdexcept>
 #include <thread>
@@ -507,7 +508,15 @@ HostGeometry load_obj(const std::string &filename, bool to_unit_cube)
             chunks.push_back(ObjChunk{ p, e });
         p = e;
     }
-    TaskPool pool(static_cast<int>(std::min<size_t>(hw, chunks.size())));
+    // the pool of a batch load when there is one, else threads of our own
+    std::unique_ptr<TaskPool> own;
+    TaskPool *pp = current_pool();
+    if(!pp)
+    {
+        own = std::make_unique<TaskPool>(static_cast<int>(std::min<size_t>(hw, chunks.size())));
+        pp = own.get();
+    }
+    TaskPool &pool = *pp;
     pool.parallel_for(chunks.size(), 1, [&](size_t b, size_t e) {
         for(size_t k = b; k < e; ++k)
             obj_count(chunks[k]);
@@ -584,7 +593,14 @@ HostGeometry geometry_from_arrays(const std::string &name, std::vector<V3> posit
         g.bmax = vmax(g.bmax, q);
     }
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    TaskPool pool(ntri >= (1u << 16) ? static_cast<int>(hw) : 1);
+    std::unique_ptr<TaskPool> own;
+    TaskPool *pp = current_pool();
+    if(!pp)
+    {
+        own = std::make_unique<TaskPool>(ntri >= (1u << 16) ? static_cast<int>(hw) : 1);
+        pp = own.get();
+    }
+    TaskPool &pool = *pp;
     pool.parallel_for(ntri, 1u << 13, [&](size_t tb, size_t te) {
     for(size_t i = tb; i < te; ++i)
     {

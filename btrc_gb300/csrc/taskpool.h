@@ -16,6 +16,17 @@
 
 namespace bt {
 
+class TaskPool;
+
+// The pool the calling thread works for: set on the pool's workers and, through
+// PoolScope, on a thread that waits on it, so that code running inside a task (a scene
+// load or build in a batch) reuses that pool instead of starting threads of its own.
+inline TaskPool *&current_pool()
+{
+    thread_local TaskPool *p = nullptr;
+    return p;
+}
+
 class TaskPool
 {
 public:
@@ -118,6 +129,7 @@ private:
 
     void work()
     {
+        current_pool() = this;
         for(;;)
         {
             Task t;
@@ -140,5 +152,32 @@ private:
     std::vector<std::thread> workers_;
     bool stop_ = false;
 };
+
+// marks the calling thread as working for `pool` while the scope lives
+class PoolScope
+{
+public:
+    explicit PoolScope(TaskPool &pool) : prev_(current_pool()) { current_pool() = &pool; }
+    ~PoolScope() { current_pool() = prev_; }
+    PoolScope(const PoolScope &) = delete;
+    PoolScope &operator=(const PoolScope &) = delete;
+
+private:
+    TaskPool *prev_;
+};
+
+// f(pool) on the pool the thread already works for, or on a new pool of `threads`
+template<class F>
+void with_pool(int threads, F &&f)
+{
+    if(TaskPool *p = current_pool())
+    {
+        f(*p);
+        return;
+    }
+    TaskPool pool(threads);
+    PoolScope scope(pool);
+    f(pool);
+}
 
 } // namespace bt

@@ -148,6 +148,14 @@ void btrc_cancel(btrc_ctx *ctx);
 
 btrc_status btrc_scene_load_json(btrc_ctx *ctx, const char *path, btrc_scene **out);
 btrc_status btrc_scene_build(btrc_scene *scene, const btrc_build_opts *opts);
+/* Load and build n scenes at once (no counterpart in the reference, which loads one scene
+   per process): JSON parsing, OBJ loading, shading records and BVH builds of all scenes
+   run as tasks of one pool of opts->threads host threads (<= 0: all cores), so small and
+   large scenes share the cores; each scene is uploaded when built. out[i] receives scene
+   i. On any failure every scene of the call is released, out[] stays NULL and the first
+   failing scene's status and message are returned. */
+btrc_status btrc_scenes_load_build(btrc_ctx *ctx, const char *const *paths, uint32_t n, const btrc_build_opts *opts,
+                                   btrc_scene **out);
 btrc_status btrc_scene_info_get(const btrc_scene *scene, btrc_scene_info *out);
 void btrc_scene_destroy(btrc_scene *scene);
 

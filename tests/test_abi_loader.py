@@ -231,3 +231,26 @@ def test_render_noalloc_rejects_host_or_short_outputs(native_lib, tmp_path):
         assert e.value.status == 1 and "CUDA tensor" in str(e.value)
     sc.close()
     ctx.close()
+
+
+def test_scenes_load_build_matches_one_by_one(native_lib, scene_dir):
+    """btrc_scenes_load_build loads and builds several scenes on one shared pool of host
+    threads; each scene's BVH is the one a single load and build gives (the build does not
+    depend on the threads it gets), and a missing file fails the whole call with IO."""
+    paths = scenes.batch(count=5, seed=79, out_dir=scene_dir / "batch-load")
+    ctx = B.Context(-1)
+    many = ctx.load_build_scenes(paths)
+    for p, sc in zip(paths, many):
+        one = ctx.load_scene(p).build()
+        a, b = sc.info(), one.info()
+        assert (a.triangles, a.bvh_nodes, a.bvh_bytes, a.width, a.height) == \
+            (b.triangles, b.bvh_nodes, b.bvh_bytes, b.width, b.height)
+        na, ta = sc.export_bvh()
+        nb, tb = one.export_bvh()
+        assert np.array_equal(na, nb)
+        one.close()
+        sc.close()
+    with pytest.raises(B.BtrcError) as e:
+        ctx.load_build_scenes([paths[0], str(Path(paths[0]).parent / "missing.json")])
+    assert e.value.status == 2
+    ctx.close()
