@@ -221,8 +221,10 @@ def l2_figures():
         tj = json.loads(path.read_text())
         return {k: tj[k] for k in ("lts_bytes_camera_launch", "lts_bytes_first_bounce_launch",
                                    "lts_frac_of_peak_camera", "lts_frac_of_peak_first_bounce",
-                                   "l2_gbs_camera", "l2_gbs_first_bounce") if k in tj} | {
-            "source": "profiles/k_trace_l2_terrain-1080p.md (ncu, one pass, two launches)"}
+                                   "l2_gbs_camera", "l2_gbs_first_bounce", "issue_frac_camera",
+                                   "issue_frac_first_bounce") if k in tj} | {
+            "source": "profiles/k_trace_l2_terrain-1080p.md (ncu, one pass, two launches); issue_frac = warp "
+                      "instructions / (152 SMs x 4 per cycle x 2070 MHz x duration)"}
     except (OSError, ValueError):
         return None
 
