@@ -460,9 +460,6 @@ void build_scene(btrc_scene *sc, int threads)
     const V3 ext = H.world_max - H.world_min;
     D.world_diagonal = length(ext);
     D.tri_round = TRI_ROUND_TESTS;
-    D.top_nodes = 0;
-    if(const char *t = std::getenv("BTRC_TOP_NODES"))
-        D.top_nodes = static_cast<uint32_t>(std::max(0, std::atoi(t)));
 
     // film filter table
     if(H.params.filter == FILTER_GAUSSIAN)

@@ -48,7 +48,6 @@ struct DevScene
     const float *env_probs;    // ibl tile probabilities
     const AliasEntry8 *env_alias;
     int32_t tri_round;         // pending triangle tests that start a pooled round
-    uint32_t top_nodes;        // topmost BVH nodes the warp-refill traversal stages in shared memory
 };
 
 // default of DevScene::tri_round: on the 1080p terrain (3.1 M triangles) rounds of >= 16

@@ -1024,7 +1024,7 @@ __global__ void __launch_bounds__(TRAVERSE_BLOCK) k_trace(DevScene S, PathSoA P,
             flags[i] = c.hit ? (c.inst | HIT_BIT) : 0u;
             hits[i] = HitDetail{ c.t, c.prim, c.b1, c.b2 };
         },
-        &nv, &tv, S.tri_round, S.top_nodes);
+        &nv, &tv, S.tri_round);
     if(COUNT)
     {
         for(int off = 16; off > 0; off >>= 1)
@@ -1582,7 +1582,7 @@ __global__ void __launch_bounds__(TRAVERSE_BLOCK) k_shadow(DevScene S, DevRender
             }
             splat(film, __float_as_uint(o.w), R.width, beta);
         },
-        nullptr, nullptr, S.tri_round, S.top_nodes);
+        nullptr, nullptr, S.tri_round);
 }
 
 __global__ void k_resolve(const float4 *film, float *rgb, uint32_t pixels)

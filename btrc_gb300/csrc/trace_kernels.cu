@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(TRACE_BLOCK) k_trace_closest_dyn(DevScene S, c
             flags[i] = c.hit ? (c.inst | HIT_BIT) : 0u;
             hits[i] = c.hit ? HitDetail{ c.t, c.prim, c.b1, c.b2 } : HitDetail{ 0.0f, 0u, 0.0f, 0.0f };
         },
-        nullptr, nullptr, S.tri_round, S.top_nodes);
+        nullptr, nullptr, S.tri_round);
 }
 
 __global__ void __launch_bounds__(TRACE_BLOCK) k_trace_any_dyn(DevScene S, const Ray *__restrict__ rays, uint32_t n,
@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(TRACE_BLOCK) k_trace_any_dyn(DevScene S, const
             d[0] = rd.x; d[1] = rd.y; d[2] = rd.z;
             t1 = rd.w;
         },
-        [&](uint32_t i, const ClosestResult &c) { occluded[i] = c.hit ? 1u : 0u; }, nullptr, nullptr, S.tri_round, S.top_nodes);
+        [&](uint32_t i, const ClosestResult &c) { occluded[i] = c.hit ? 1u : 0u; }, nullptr, nullptr, S.tri_round);
 }
 
 uint32_t persistent_blocks(const void *kernel)

@@ -148,32 +148,15 @@ __device__ __forceinline__ float byte_mant(uint32_t w, int j)
 
 // Intersects the 8 children of a node. Returns the hit mask: bits 24..31 child nodes
 // (slot ^ oct_inv), bits 0..23 triangles relative to tri_base.
-// nodes below top_n are read from top, a shared-memory copy of the first (breadth-first:
-// the topmost) nodes of the tree
 __device__ __forceinline__ uint32_t intersect_children(const TravRay &r, const float4 *__restrict__ nodes4,
                                                       uint32_t ni, float tcur, uint32_t &child_base,
-                                                      uint32_t &tri_base, uint32_t &imask,
-                                                      const float4 *top = nullptr, uint32_t top_n = 0)
+                                                      uint32_t &tri_base, uint32_t &imask)
 {
-    float4 n0;
-    uint4 n1, n2, n3, n4;
-    if(ni < top_n)
-    {
-        const float4 *t = top + ni * 5;
-        n0 = t[0];
-        n1 = *reinterpret_cast<const uint4 *>(t + 1);
-        n2 = *reinterpret_cast<const uint4 *>(t + 2);
-        n3 = *reinterpret_cast<const uint4 *>(t + 3);
-        n4 = *reinterpret_cast<const uint4 *>(t + 4);
-    }
-    else
-    {
-        n0 = __ldg(nodes4 + ni * 5 + 0);
-        n1 = __ldg(reinterpret_cast<const uint4 *>(nodes4) + ni * 5 + 1);
-        n2 = __ldg(reinterpret_cast<const uint4 *>(nodes4) + ni * 5 + 2);
-        n3 = __ldg(reinterpret_cast<const uint4 *>(nodes4) + ni * 5 + 3);
-        n4 = __ldg(reinterpret_cast<const uint4 *>(nodes4) + ni * 5 + 4);
-    }
+    const float4 n0 = __ldg(nodes4 + ni * 5 + 0);
+    const uint4 n1 = __ldg(reinterpret_cast<const uint4 *>(nodes4) + ni * 5 + 1);
+    const uint4 n2 = __ldg(reinterpret_cast<const uint4 *>(nodes4) + ni * 5 + 2);
+    const uint4 n3 = __ldg(reinterpret_cast<const uint4 *>(nodes4) + ni * 5 + 3);
+    const uint4 n4 = __ldg(reinterpret_cast<const uint4 *>(nodes4) + ni * 5 + 4);
     const uint32_t ew = __float_as_uint(n0.w);
     imask = ew >> 24;
     child_base = n1.x;
@@ -418,8 +401,7 @@ namespace bt {
 // The kernel launches 128-thread blocks (TRAVERSE_WARPS warps, one shared-memory slice
 // each), and all 32 lanes of a warp enter (the warp-wide votes use the full mask).
 //   fetch(i, o, d, t1, root): load ray i;  emit(i, hit): store its result
-constexpr int REFILL_LANES = 8;
-constexpr uint32_t TOP_NODES_MAX = 64;  // nodes the warp-refill traversal can stage in shared memory  // idle lanes that trigger a warp refill (measured best of 4/8/12/16/24)
+constexpr int REFILL_LANES = 8;  // idle lanes that trigger a warp refill (measured best of 4/8/12/16/24)
 constexpr int TRAVERSE_BLOCK = 128;
 constexpr int TRAVERSE_WARPS = TRAVERSE_BLOCK / 32;
 // queue entry: owner lane in bits 27..31, triangle record index in bits 0..26
@@ -433,19 +415,12 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
                                                 uint32_t node_count, uint32_t *cursor, uint32_t n, int refill,
                                                 uint32_t *err, Fetch fetch, Emit emit,
                                                 uint64_t *node_visits = nullptr, uint64_t *tri_tests = nullptr,
-                                                int min_round = 1, uint32_t top_n = 0)
+                                                int min_round = 1)
 {
     // per lane: (ox, oy, oz, Sx), (Sy, Sz, kx | ky << 2 | kz << 4, tmax); per warp: the queue
     __shared__ float4 s_ray0[TRAVERSE_WARPS][32];
     __shared__ float4 s_ray1[TRAVERSE_WARPS][32];
     __shared__ uint32_t s_queue[TRAVERSE_WARPS][32];
-    // the tree's top levels (its first nodes in breadth-first order), staged once per block
-    __shared__ float4 s_top[TOP_NODES_MAX * 5];
-    top_n = min(min(top_n, TOP_NODES_MAX), node_count);
-    for(uint32_t k = threadIdx.x; k < top_n * 5; k += blockDim.x)
-        s_top[k] = __ldg(nodes4 + k);
-    if(top_n)
-        __syncthreads();
     uint64_t visits = 0, tests = 0;
     const uint32_t FULL = 0xffffffffu;
     const uint32_t lane = threadIdx.x & 31u;
@@ -530,7 +505,7 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
             else
             {
                 uint32_t cbase, tbase, imask;
-                const uint32_t hm = intersect_children(r, nodes4, ni, best.t, cbase, tbase, imask, s_top, top_n);
+                const uint32_t hm = intersect_children(r, nodes4, ni, best.t, cbase, tbase, imask);
                 ngroup = make_uint2(cbase, (hm & 0xff000000u) | imask);
                 tgroup = make_uint2(tbase, hm & 0x00ffffffu);
             }
