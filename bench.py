@@ -433,8 +433,9 @@ def batch_study(B, ctx):
                                                         mstats[0]["grid_pct"]],
                   "per_scene_done_ms": {"min": min(done), "median": float(np.median(done)), "max": max(done)},
                   "note": "all scenes in one path queue through one set of persistent stage kernels under one "
-                          "captured two-bounce graph; per-scene time is the device time until every path of "
-                          "the scene had been generated and could have ended (scenes with fewer paths are queued first)"}
+                          "captured two-bounce graph; per-scene time is the device time to the end of the launch "
+                          "after the first one that left none of the scene's paths in the queue (a census of the "
+                          "queue after every launch; scenes with fewer paths are queued first)"}
     except Exception as ex:  # the merged pass must not sink the lanes figures
         merged = {"error": str(ex)}
     for s in scs:

@@ -21,6 +21,7 @@
 
 #include "btrc.h"
 #include "bvh.h"
+#include "gpu_bvh.h"
 #include "image_io.h"
 #include "nrc.h"
 #include "kernels.h"
@@ -109,6 +110,8 @@ struct btrc_scene
     int bvh_nodes = 0, bvh_depth = 0;
     uint64_t bvh_bytes = 0;
     double build_ms = 0;
+    double bvh_ms = 0;
+    int bvh_builder = 0;             // 0 host, 1 device
     std::vector<AliasEntry8> filter_table_host;
     AliasEntry8 *filter_table = nullptr;
     std::vector<float> export_xyz;
@@ -256,7 +259,7 @@ HaltonConsts halton_consts(int width, int height)
     return hc;
 }
 
-void build_scene(btrc_scene *sc, int threads)
+void build_scene(btrc_scene *sc, int threads, int builder)
 {
     HostScene &H = sc->host;
     const auto t0 = std::chrono::steady_clock::now();
@@ -307,33 +310,98 @@ void build_scene(btrc_scene *sc, int threads)
             }
         });
     }
-    CWBVH bvh = build_cwbvh(world, pool);
+    // the traversal's pooled triangle tests address triangle records with 27 bits
+    if(!host_only && world.size() >= (1ull << 27))
+        throw StatusError(BTRC_ERR_INVALID_ARG, "scene exceeds 2^27 triangle records");
+    const bool keep_host = host_only || H.triangle_count <= (1u << 20);
+    const auto tb = std::chrono::steady_clock::now();
+    DevScene &D = sc->dev;
+    D = DevScene{};
+    sc->bvh_builder = 0;
+    if(builder == 1 && !host_only && !world.empty())
+    {
+        // device build on a stream of its own, so that concurrent scene builds overlap
+        cudaStream_t bst = nullptr;
+        check_cuda(cudaStreamCreateWithFlags(&bst, cudaStreamNonBlocking), "build stream");
+        TriRec *d_world = nullptr;
+        cudaError_t e = cudaMallocAsync(&d_world, sizeof(TriRec) * world.size(), bst);
+        if(e == cudaSuccess)
+            e = cudaMemcpyAsync(d_world, world.data(), sizeof(TriRec) * world.size(), cudaMemcpyHostToDevice, bst);
+        GpuBvh gb;
+        std::string msg;
+        GpuBvhStatus gs = GpuBvhStatus::cuda;
+        if(e == cudaSuccess)
+            gs = gpu_build_cwbvh(d_world, static_cast<uint32_t>(world.size()), bst, gb, msg);
+        else
+            msg = std::string("device BVH input: ") + cudaGetErrorString(e);
+        cudaFreeAsync(d_world, bst);
+        const cudaError_t se = cudaStreamSynchronize(bst);
+        cudaStreamDestroy(bst);
+        if(gs == GpuBvhStatus::ok && se == cudaSuccess)
+        {
+            sc->allocs.push_back(gb.nodes);
+            sc->allocs.push_back(gb.tris);
+            D.nodes = reinterpret_cast<const F4 *>(gb.nodes);
+            D.tris = reinterpret_cast<const F4 *>(gb.tris);
+            D.node_count = gb.node_count;
+            D.tri_count = gb.tri_count;
+            sc->bvh_nodes = static_cast<int>(gb.node_count);
+            sc->bvh_depth = gb.depth;
+            sc->bvh_bytes = static_cast<uint64_t>(gb.node_count) * sizeof(CWNode) + uint64_t(gb.tri_count) * sizeof(TriRec);
+            sc->bvh_builder = 1;
+            if(keep_host)
+            {
+                sc->host_nodes.resize(gb.node_count);
+                sc->host_tris.resize(gb.tri_count);
+                check_cuda(cudaMemcpy(sc->host_nodes.data(), gb.nodes, sizeof(CWNode) * gb.node_count,
+                                      cudaMemcpyDeviceToHost),
+                           "BVH download");
+                check_cuda(cudaMemcpy(sc->host_tris.data(), gb.tris, sizeof(TriRec) * gb.tri_count,
+                                      cudaMemcpyDeviceToHost),
+                           "BVH download");
+            }
+        }
+        else
+        {
+            cudaFree(gb.nodes);
+            cudaFree(gb.tris);
+            if(se != cudaSuccess)
+                throw StatusError(BTRC_ERR_CUDA, std::string("device BVH build: ") + cudaGetErrorString(se));
+            if(gs == GpuBvhStatus::cuda)
+                throw StatusError(BTRC_ERR_CUDA, msg);
+            if(gs == GpuBvhStatus::internal)
+                throw StatusError(BTRC_ERR_INTERNAL, msg);
+            // no_progress / too_deep: the host builder takes the scene
+        }
+    }
+    if(sc->bvh_builder == 0)
+    {
+        CWBVH bvh = build_cwbvh(world, pool);
+        sc->bvh_nodes = static_cast<int>(bvh.nodes.size());
+        sc->bvh_depth = bvh.depth;
+        sc->bvh_bytes = bvh.nodes.size() * sizeof(CWNode) + bvh.tris.size() * sizeof(TriRec);
+        if(!host_only)
+        {
+            D.nodes = reinterpret_cast<const F4 *>(dev_upload(sc->allocs, bvh.nodes.data(), bvh.nodes.size()));
+            D.tris = reinterpret_cast<const F4 *>(dev_upload(sc->allocs, bvh.tris.data(), bvh.tris.size()));
+            D.node_count = static_cast<uint32_t>(bvh.nodes.size());
+            D.tri_count = static_cast<uint32_t>(bvh.tris.size());
+        }
+        if(keep_host)
+        {
+            sc->host_nodes = std::move(bvh.nodes);
+            sc->host_tris = std::move(bvh.tris);
+        }
+    }
     world.clear();
     world.shrink_to_fit();
-    sc->bvh_nodes = static_cast<int>(bvh.nodes.size());
-    sc->bvh_depth = bvh.depth;
-    sc->bvh_bytes = bvh.nodes.size() * sizeof(CWNode) + bvh.tris.size() * sizeof(TriRec);
-    if(host_only || H.triangle_count <= (1u << 20))
-    {
-        sc->host_nodes = bvh.nodes;
-        sc->host_tris = bvh.tris;
-    }
+    sc->bvh_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb).count();
     if(host_only)
     {
         sc->built = true;
         sc->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         return;
     }
-
-    // the traversal's pooled triangle tests address triangle records with 27 bits
-    if(bvh.tris.size() >= (1ull << 27))
-        throw StatusError(BTRC_ERR_INVALID_ARG, "scene exceeds 2^27 triangle records");
-    DevScene &D = sc->dev;
-    D = DevScene{};
-    D.nodes = reinterpret_cast<const F4 *>(dev_upload(sc->allocs, bvh.nodes.data(), bvh.nodes.size()));
-    D.tris = reinterpret_cast<const F4 *>(dev_upload(sc->allocs, bvh.tris.data(), bvh.tris.size()));
-    D.node_count = static_cast<uint32_t>(bvh.nodes.size());
-    D.tri_count = static_cast<uint32_t>(bvh.tris.size());
 
     // shading SoA + geometry table + light sampling data
     std::vector<Geometry> geos(H.geometries.size());
@@ -721,7 +789,7 @@ btrc_status btrc_scene_build(btrc_scene *scene, const btrc_build_opts *opts)
 {
     if(!scene)
         return BTRC_ERR_INVALID_ARG;
-    return guarded(scene->ctx, [&] { build_scene(scene, opts ? opts->threads : 0); });
+    return guarded(scene->ctx, [&] { build_scene(scene, opts ? opts->threads : 0, opts ? opts->builder : 0); });
 }
 
 btrc_status btrc_scenes_load_build(btrc_ctx *ctx, const char *const *paths, uint32_t n, const btrc_build_opts *opts,
@@ -755,7 +823,7 @@ btrc_status btrc_scenes_load_build(btrc_ctx *ctx, const char *const *paths, uint
                     sc->host = load_scene(paths[i]);
                     if(ctx->device >= 0)
                         check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
-                    build_scene(sc.get(), threads);
+                    build_scene(sc.get(), threads, opts ? opts->builder : 0);
                     scs[i] = std::move(sc);
                 }
                 catch(...)
@@ -806,6 +874,8 @@ btrc_status btrc_scene_info_get(const btrc_scene *sc, btrc_scene_info *out)
     i.world_min[0] = H.world_min.x; i.world_min[1] = H.world_min.y; i.world_min[2] = H.world_min.z;
     i.world_max[0] = H.world_max.x; i.world_max[1] = H.world_max.y; i.world_max[2] = H.world_max.z;
     i.build_ms = sc->build_ms;
+    i.bvh_ms = sc->bvh_ms;
+    i.bvh_builder = sc->bvh_builder;
     *out = i;
     return BTRC_OK;
 }
@@ -1852,8 +1922,9 @@ double merged_render(btrc_ctx *ctx, MergedBatch &mb, uint32_t capacity, int bloc
     ctx->buf.capacity = capacity;
     bool cancelled = false;
     std::vector<std::pair<double, uint64_t>> progress;
+    std::vector<uint8_t> live;
     check_cuda(render_wavefront(mb.S, R, ctx->buf, st, &ctx->cancel, true, 0, &rs, &cancelled,
-                                scene_done_ms ? &progress : nullptr),
+                                scene_done_ms ? &progress : nullptr, scene_done_ms ? &live : nullptr),
                "merged batch render");
     if(outs)
     {
@@ -1896,20 +1967,26 @@ double merged_render(btrc_ctx *ctx, MergedBatch &mb, uint32_t capacity, int bloc
         throw StatusError(BTRC_ERR_CANCELLED, "render cancelled");
     if(scene_done_ms)
     {
-        // a scene's paths have all ended once every one of them was generated and as many
-        // two-bounce launches followed as its longest path can take
+        // a scene is done after the first launch by which all of its paths were generated
+        // and none was left in the queue, plus one launch for the shadow rays of its last
+        // vertices (they run beside the next launch)
+        const size_t nb = mb.table.size();
+        const bool have_live = live.size() == progress.size() * nb;
         const size_t tail = static_cast<size_t>((std::max(mb.max_depth, mb.min_depth) + 3) / 2);
-        scene_done_ms->assign(mb.table.size(), static_cast<double>(rs.device_ms));
-        for(size_t i = 0; i < mb.table.size(); ++i)
+        scene_done_ms->assign(nb, static_cast<double>(rs.device_ms));
+        for(size_t i = 0; i < nb; ++i)
         {
             const uint64_t end = mb.table[i].path_begin + mb.table[i].R.total_paths;
             for(size_t k = 0; k < progress.size(); ++k)
-                if(progress[k].second >= end)
-                {
-                    const size_t done = std::min(progress.size() - 1, k + tail);
+            {
+                if(progress[k].second < end || (have_live && live[k * nb + i]))
+                    continue;
+                // without the queue census: as many launches as the longest path can take
+                const size_t done = have_live ? k + 1 : k + tail;
+                if(done < progress.size())
                     (*scene_done_ms)[i] = progress[done].first;
-                    break;
-                }
+                break;
+            }
         }
     }
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();

@@ -910,6 +910,23 @@ __global__ void k_control(Counters *c, uint32_t capacity, uint64_t total, int pa
         ++c->iterations;
 }
 
+// which scenes of a merged batch still have paths in the queue: live[s] = 1 (warp lanes of
+// one scene store once)
+__global__ void k_batch_live(DevRender R, const F4 *__restrict__ rad_pixel, const Counters *__restrict__ c,
+                             uint8_t *__restrict__ live)
+{
+    const uint32_t n = c->next_active;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t end = (n + 31u) & ~31u;
+    for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < end; i += stride)
+    {
+        const int s = i < n ? R.row_scene[__float_as_uint(rad_pixel[i].w) >> 16] : -1;
+        const uint32_t same = __match_any_sync(0xffffffffu, s);
+        if(s >= 0 && static_cast<uint32_t>(s) < R.batch_count && (threadIdx.x & 31u) == __ffs(same) - 1u)
+            live[s] = 1;
+    }
+}
+
 // the scene of global camera path g in a merged batch: the last with path_begin <= g
 __device__ __forceinline__ int batch_scene_of_path(const DevRender &R, uint64_t g)
 {
@@ -1760,7 +1777,8 @@ cudaError_t upload_primes()
 
 cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffers &B, cudaStream_t st,
                              const std::atomic<bool> *cancel, bool use_graphs, int profile, RenderStats *stats,
-                             bool *cancelled, std::vector<std::pair<double, uint64_t>> *progress)
+                             bool *cancelled, std::vector<std::pair<double, uint64_t>> *progress,
+                             std::vector<uint8_t> *live)
 {
     *cancelled = false;
     if(profile != 0)
@@ -1847,6 +1865,8 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
     // progress log: one timing event and one copy of the generated-path counter per launch
     std::vector<cudaEvent_t> prog_ev;
     uint64_t *prog_gen = nullptr;
+    uint8_t *prog_live = nullptr;
+    const size_t live_stride = R.batch ? R.batch_count : 0;
     if(progress && use_graphs)
     {
         progress->clear();
@@ -1854,6 +1874,16 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
         {
             prog_gen = nullptr;
             cudaGetLastError();
+        }
+        if(prog_gen && live && live_stride)
+        {
+            if(cudaMalloc(&prog_live, live_stride * (max_launches + 1)) != cudaSuccess ||
+               cudaMemsetAsync(prog_live, 0, live_stride * (max_launches + 1), st) != cudaSuccess)
+            {
+                cudaFree(prog_live);
+                prog_live = nullptr;
+                cudaGetLastError();
+            }
         }
     }
     cudaEventRecord(t0, st);
@@ -1906,6 +1936,10 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
             prog_ev.push_back(pe);
             cudaMemcpyAsync(prog_gen + launches_now, &B.counters->generated, sizeof(uint64_t), cudaMemcpyDeviceToDevice,
                             st);
+            // survivors of the launch's second (odd) bounce sit in queue 0
+            if(prog_live)
+                k_batch_live<<<persistent_grid(BLOCK, reinterpret_cast<const void *>(k_batch_live), 100), BLOCK, 0,
+                               st>>>(R, B.path[0].rad_pixel, B.counters, prog_live + launches_now * live_stride);
         }
         cudaMemcpyAsync(&B.host_counters[slot], B.counters, sizeof(Counters), cudaMemcpyDeviceToHost, st);
         cudaEventRecord(ev[slot], st);
@@ -1936,6 +1970,13 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
             cudaEventDestroy(prog_ev[k]);
         }
         cudaFree(prog_gen);
+        if(prog_live)
+        {
+            live->assign(live_stride * prog_ev.size(), 1);
+            if(!prog_ev.empty())
+                cudaMemcpy(live->data(), prog_live, live_stride * prog_ev.size(), cudaMemcpyDeviceToHost);
+            cudaFree(prog_live);
+        }
     }
     Counters fin{};
     cudaMemcpy(&fin, B.counters, sizeof(Counters), cudaMemcpyDeviceToHost);

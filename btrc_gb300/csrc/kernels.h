@@ -71,10 +71,13 @@ struct RenderStats
 // profile: 0 none (graphs allowed), 1 per-stage CUDA events (no graphs),
 //          2 traversal counters in the closest-hit stage (no graphs, slower)
 // progress (optional, graphs only): per launch of the two-bounce graph, the milliseconds
-// since the loop started at the end of that launch and the camera paths generated by then
+// since the loop started at the end of that launch and the camera paths generated by then.
+// live (optional, merged batches with progress): per launch, R.batch_count bytes, 1 where
+// a path of that scene was still in the queue after the launch
 cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffers &B, cudaStream_t st,
                              const std::atomic<bool> *cancel, bool use_graphs, int profile, RenderStats *stats,
-                             bool *cancelled, std::vector<std::pair<double, uint64_t>> *progress = nullptr);
+                             bool *cancelled, std::vector<std::pair<double, uint64_t>> *progress = nullptr,
+                             std::vector<uint8_t> *live = nullptr);
 
 // Allocation-free variant of render_wavefront: all scratch (queues, film, counters) lives
 // in a fixed device array; see the block comment above render_wavefront_noalloc.

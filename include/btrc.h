@@ -86,11 +86,18 @@ typedef struct btrc_scene_info
     uint64_t bvh_bytes;       /* nodes + triangle records */
     float world_min[3], world_max[3];
     double build_ms;
+    double bvh_ms;            /* the BVH part of build_ms */
+    int32_t bvh_builder;      /* the builder that made the BVH: 0 host, 1 device */
 } btrc_scene_info;
 
 typedef struct btrc_build_opts
 {
     int32_t threads;          /* host threads for the BVH build; <= 0: all */
+    int32_t builder;          /* 0: host binned SAH (default); 1: on the device (PLOC
+                                 clustering, then the same 8-wide collapse and layout),
+                                 for batches and cold starts; a scene the device build
+                                 refuses (non-finite boxes, a tree deeper than the
+                                 traversal stack) is built on the host */
 } btrc_build_opts;
 
 typedef struct btrc_render_opts

@@ -41,6 +41,13 @@ def test_structure(native_lib, scene_dir, which):
     path = scenes.cornell(out_dir=scene_dir / "cornell") if which == "cornell" else \
         scenes.random_soup(scene_dir / "soup", seed=5, n_tris=20000, n_instances=4)
     ctx, sc = _host_scene(path)
+    check_structure(sc)
+
+
+def check_structure(sc):
+    """Every index in range, every node and triangle reached exactly once, every
+    triangle inside every quantised box on its path, the records equal to the scene's
+    exported world triangles (any builder's output)."""
     info = sc.info()
     nodes, tris = sc.export_bvh()
     assert info.bvh_depth <= STACK
