@@ -427,7 +427,7 @@ def batch_study(B, ctx):
             mstats, mtotal = ctx.render_batch(scs, outs, autotune=True, merged=True)
             mruns.append(mtotal)
         mms = float(np.median(mruns))
-        done = [st["ms"] for st in mstats]
+        done = [st["done_ms"] for st in mstats]
         merged = {"merged_mpaths_s": total_paths / (mms / 1000) / 1e6, "merged_ms": mms,
                   "autotuned_capacity_block_grid_pct": [mstats[0]["capacity"], mstats[0]["block"],
                                                         mstats[0]["grid_pct"]],
@@ -438,6 +438,28 @@ def batch_study(B, ctx):
                           "queue after every launch; scenes with fewer paths are queued first)"}
     except Exception as ex:  # the merged pass must not sink the lanes figures
         merged = {"error": str(ex)}
+    # the same batch with BVHs built on the device: load + build time, and the merged pass
+    # through those trees (PLOC trees trace a little slower than the host's binned SAH)
+    device = None
+    try:
+        t = time.perf_counter()
+        dscs = ctx.load_build_scenes(paths, builder="device")
+        torch.cuda.synchronize()
+        dbuild_s = time.perf_counter() - t
+        ctx.render_batch(dscs, outs, autotune=True, merged=True)
+        druns = []
+        for _ in range(3):
+            _, dtotal = ctx.render_batch(dscs, outs, autotune=True, merged=True)
+            druns.append(dtotal)
+        dms = float(np.median(druns))
+        device = {"scene_build_s": dbuild_s, "bvh_ms_max": max(x.info().bvh_ms for x in dscs),
+                  "merged_mpaths_s": total_paths / (dms / 1000) / 1e6, "merged_ms": dms,
+                  "build_plus_merged_s": dbuild_s + dms / 1000,
+                  "host_build_plus_merged_s": build_s + (merged or {}).get("merged_ms", float("nan")) / 1000}
+        for x in dscs:
+            x.close()
+    except Exception as ex:
+        device = {"error": str(ex)}
     for s in scs:
         s.close()
     return {
@@ -449,8 +471,15 @@ def batch_study(B, ctx):
         "per_scene_ms_batched": {"min": min(st["ms"] for st in stats),
                                  "median": float(np.median([st["ms"] for st in stats])),
                                  "max": max(st["ms"] for st in stats)},
+        "per_scene_done_ms_batched": {"min": min(st["done_ms"] for st in stats),
+                                      "median": float(np.median([st["done_ms"] for st in stats])),
+                                      "max": max(st["done_ms"] for st in stats),
+                                      "note": "time from the start of the batch until the scene's image was complete"},
+        "per_scene_done_ms_sequential": {"min": float(np.cumsum(per).min()),
+                                         "median": float(np.median(np.cumsum(per))),
+                                         "max": float(np.cumsum(per).max())},
         "autotuned_capacity_grid_pct": caps, "scene_build_s": build_s,
-        "merged": merged,
+        "merged": merged, "device_bvh": device,
     }
 
 
@@ -466,6 +495,16 @@ def run_ours(args, world, rank, local):
     load_s = time.perf_counter() - t0
     sc.build()
     info = sc.info()
+    # the same scene with its BVH built on the device (PLOC + the same 8-wide collapse)
+    build_cmp = {"host": {"build_ms": info.build_ms, "bvh_ms": info.bvh_ms, "bvh_nodes": info.bvh_nodes}}
+    try:
+        dsc = ctx.load_scene(path).build(builder="device")
+        di = dsc.info()
+        build_cmp["device"] = {"build_ms": di.build_ms, "bvh_ms": di.bvh_ms, "bvh_nodes": di.bvh_nodes,
+                               "builder": di.bvh_builder}
+        dsc.close()
+    except Exception as ex:
+        build_cmp["device"] = {"error": str(ex)}
     W, H, spp = info.width, info.height, args.spp
     paths = W * H * spp
     out_dev = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
@@ -629,6 +668,7 @@ def run_ours(args, world, rank, local):
             "batch": batch,
             "mrays_per_s": world * (st["extension_rays"] + st["shadow_rays"]) / (step_ms / 1000) / 1e6,
             "scene_load_s": load_s, "bvh_build_ms": info.build_ms,
+            "scene_build": build_cmp,
         }
         print(json.dumps(line), flush=True)
     sc.close()

@@ -81,7 +81,7 @@ class BatchOpts(C.Structure):
 
 class BatchSceneStats(C.Structure):
     _fields_ = [("paths", C.c_uint64), ("ms", C.c_double), ("lane", C.c_int32), ("capacity", C.c_uint32),
-                ("grid_pct", C.c_int32), ("block", C.c_int32)]
+                ("grid_pct", C.c_int32), ("block", C.c_int32), ("done_ms", C.c_double)]
 
 
 STAGES = ("control", "generate", "trace", "medium", "shade", "shadow")

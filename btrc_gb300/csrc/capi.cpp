@@ -2062,6 +2062,7 @@ btrc_status btrc_render_batch(btrc_ctx *ctx, btrc_scene *const *scenes, uint32_t
                     btrc_batch_scene_stats &sst = stats[mb.input[k]];
                     sst.paths = mb.table[k].R.total_paths;
                     sst.ms = done[k];
+                    sst.done_ms = done[k];
                     sst.lane = 0;
                     sst.capacity = static_cast<uint32_t>(std::min<uint64_t>(cap, mb.total_paths));
                     sst.grid_pct = pct;
@@ -2122,6 +2123,9 @@ btrc_status btrc_render_batch(btrc_ctx *ctx, btrc_scene *const *scenes, uint32_t
                                 cap, static_cast<uint32_t>(std::max<uint64_t>(rs.paths, 1)));
                             stats[i].grid_pct = pct;
                             stats[i].block = 256;
+                            stats[i].done_ms =
+                                std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0)
+                                    .count();
                         }
                     }
                 }

@@ -302,14 +302,17 @@ typedef struct btrc_batch_opts
 typedef struct btrc_batch_scene_stats
 {
     uint64_t paths;
-    double ms;                 /* lanes: wall time of the scene's render in its lane; merged: device
-                                  time from the start of the pass until every path of the scene had
-                                  been generated and could have ended (an upper bound; the pass
-                                  queues scenes with fewer camera paths first) */
+    double ms;                 /* lanes: wall time of the scene's render in its lane; merged: as
+                                  done_ms */
     int32_t lane;
     uint32_t capacity;         /* queue capacity used */
     int32_t grid_pct;          /* persistent grid size used, percent of full occupancy */
     int32_t block;             /* threads per block of the stage kernels */
+    double done_ms;            /* time from the start of the batch's render until the scene's
+                                  image was complete. Lanes: wall clock at the end of its render.
+                                  Merged: device time to the end of the bounce launch after the
+                                  first one that left none of the scene's paths in the queue
+                                  (the pass queues scenes with fewer camera paths first) */
 } btrc_batch_scene_stats;
 
 /* rgb_out[i]: width_i * height_i * 3 floats for scene i. stats (n entries) and total_ms
