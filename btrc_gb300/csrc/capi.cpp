@@ -114,8 +114,7 @@ struct btrc_scene
     int bvh_builder = 0;             // 0 host, 1 device
     std::vector<AliasEntry8> filter_table_host;
     AliasEntry8 *filter_table = nullptr;
-    std::vector<float> export_xyz;
-    std::vector<uint32_t> export_ids;
+    uint64_t export_count = 0;       // flattened triangles (btrc_scene_export_triangles)
     std::vector<CWNode> host_nodes;  // kept for host-only contexts and small scenes
     std::vector<TriRec> host_tris;
     uint64_t n_shade_tris = 0;       // shading records (triangles over all geometries)
@@ -259,6 +258,18 @@ HaltonConsts halton_consts(int width, int height)
     return hc;
 }
 
+// triangle t of instance i in world space: the one transform the BVH, the oracle exports
+// and the shading agree on
+TriRec world_triangle(const HostScene &H, size_t i, size_t t)
+{
+    const HostGeometry &g = H.geometries[H.instances[i].geometry];
+    const Transform &xf = H.instance_xf[i];
+    const V3 a = xf.point(g.pos[t * 3 + 0]);
+    const V3 b = xf.point(g.pos[t * 3 + 1]);
+    const V3 c = xf.point(g.pos[t * 3 + 2]);
+    return TriRec{ a.x, a.y, a.z, static_cast<uint32_t>(i), b.x, b.y, b.z, static_cast<uint32_t>(t), c.x, c.y, c.z, 0u };
+}
+
 void build_scene(btrc_scene *sc, int threads, int builder)
 {
     HostScene &H = sc->host;
@@ -287,29 +298,16 @@ void build_scene(btrc_scene *sc, int threads, int builder)
     for(size_t i = 0; i < H.instances.size(); ++i)
         inst_first[i + 1] = inst_first[i] + H.geometries[H.instances[i].geometry].area.size();
     std::vector<TriRec> world(inst_first.back());
-    sc->export_xyz.assign(world.size() * 9, 0.0f);
-    sc->export_ids.assign(world.size() * 2, 0u);
     for(size_t i = 0; i < H.instances.size(); ++i)
     {
-        const HostGeometry &g = H.geometries[H.instances[i].geometry];
-        const Transform &xf = H.instance_xf[i];
         const size_t base = inst_first[i];
-        pool.parallel_for(g.area.size(), 1u << 14, [&, i, base](size_t tb, size_t te) {
-            for(size_t t = tb; t < te; ++t)
-            {
-                const V3 a = xf.point(g.pos[t * 3 + 0]);
-                const V3 b = xf.point(g.pos[t * 3 + 1]);
-                const V3 c = xf.point(g.pos[t * 3 + 2]);
-                const size_t k = base + t;
-                world[k] = TriRec{ a.x, a.y, a.z, static_cast<uint32_t>(i), b.x, b.y, b.z, static_cast<uint32_t>(t),
-                                   c.x, c.y, c.z, 0u };
-                const float v[9] = { a.x, a.y, a.z, b.x, b.y, b.z, c.x, c.y, c.z };
-                std::memcpy(&sc->export_xyz[k * 9], v, sizeof(v));
-                sc->export_ids[k * 2] = static_cast<uint32_t>(i);
-                sc->export_ids[k * 2 + 1] = static_cast<uint32_t>(t);
-            }
-        });
+        pool.parallel_for(H.geometries[H.instances[i].geometry].area.size(), 1u << 14,
+                          [&, i, base](size_t tb, size_t te) {
+                              for(size_t t = tb; t < te; ++t)
+                                  world[base + t] = world_triangle(H, i, t);
+                          });
     }
+    sc->export_count = world.size();
     // the traversal's pooled triangle tests address triangle records with 27 bits
     if(!host_only && world.size() >= (1ull << 27))
         throw StatusError(BTRC_ERR_INVALID_ARG, "scene exceeds 2^27 triangle records");
@@ -902,13 +900,30 @@ btrc_status btrc_scene_export_triangles(const btrc_scene *sc, float *xyz, uint32
         return BTRC_ERR_INVALID_ARG;
     if(!sc->built)
         return BTRC_ERR_INVALID_ARG;
-    const uint64_t n = sc->export_ids.size() / 2;
+    const uint64_t n = sc->export_count;
     if(capacity < n)
         return BTRC_ERR_INVALID_ARG;
-    if(xyz)
-        std::memcpy(xyz, sc->export_xyz.data(), sizeof(float) * n * 9);
-    if(ids)
-        std::memcpy(ids, sc->export_ids.data(), sizeof(uint32_t) * n * 2);
+    // recomputed on request (tests and tools), so that builds do not keep a second copy
+    const HostScene &H = sc->host;
+    uint64_t k = 0;
+    for(size_t i = 0; i < H.instances.size(); ++i)
+    {
+        const size_t m = H.geometries[H.instances[i].geometry].area.size();
+        for(size_t t = 0; t < m && k < n; ++t, ++k)
+        {
+            const TriRec r = world_triangle(H, i, t);
+            if(xyz)
+            {
+                const float v[9] = { r.v0x, r.v0y, r.v0z, r.v1x, r.v1y, r.v1z, r.v2x, r.v2y, r.v2z };
+                std::memcpy(xyz + k * 9, v, sizeof(v));
+            }
+            if(ids)
+            {
+                ids[k * 2] = r.inst;
+                ids[k * 2 + 1] = r.prim;
+            }
+        }
+    }
     return BTRC_OK;
 }
 

@@ -21,7 +21,12 @@ def test_batch_matches_single_renders(gpu_ctx, scene_dir):
         ref = gpu_ctx.render(s)
         assert st["paths"] == i.width * i.height * i.spp
         assert 0 <= st["lane"] < 3 and st["capacity"] > 0 and st["grid_pct"] in (50, 100)
+        assert 0 < st["ms"] <= st["done_ms"] <= total * 1.001
         assert np.allclose(o, ref, rtol=1e-4, atol=1e-5)
+    # within a lane, scenes complete in the order they were rendered
+    for lane in range(3):
+        done = [st["done_ms"] for st in stats if st["lane"] == lane]
+        assert len(done) <= 1 or np.all(np.diff(sorted(done)) > 0)
     # device outputs, no autotune, one lane
     import torch
     outs_d = [torch.zeros((i.height, i.width, 3), dtype=torch.float32, device="cuda") for i in infos]
@@ -48,8 +53,13 @@ def test_merged_batch_matches_single_renders(gpu_ctx, scene_dir):
     assert total > 0
     for o, r, st, i in zip(outs, refs, stats, infos):
         assert st["paths"] == i.width * i.height * i.spp
-        assert 0 < st["ms"] <= total
+        assert 0 < st["ms"] <= total and st["done_ms"] == st["ms"]
         assert np.allclose(o, r, rtol=1e-4, atol=1e-5), np.abs(o - r).max()
+    # the queue census: a scene is complete no later than the pass, and the scene with the
+    # fewest paths (queued first) no later than the one with the most
+    few = min(range(len(stats)), key=lambda k: stats[k]["paths"])
+    most = max(range(len(stats)), key=lambda k: stats[k]["paths"])
+    assert stats[few]["done_ms"] <= stats[most]["done_ms"]
     # autotuned, device outputs; the concatenated scene is reused
     outs_d = [torch.zeros((i.height, i.width, 3), dtype=torch.float32, device="cuda") for i in infos]
     stats, _ = gpu_ctx.render_batch(scs, outs_d, autotune=True, merged=True)
