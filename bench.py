@@ -282,7 +282,7 @@ def nrc_study(B, ctx, sc, info, args, spread: float = 0.0):
         torch.cuda.synchronize()
         t = time.perf_counter()
         cache.render_frame(sc, f, out=img, terminate_vertex=1, train_stride=16, train_steps=4, train_batch=16384,
-                           stats=st, spread_threshold=spread)
+                           stats=st)
         acc += img
         torch.cuda.synchronize()
         elapsed += (time.perf_counter() - t) * 1000
@@ -333,9 +333,10 @@ def nrc_study(B, ctx, sc, info, args, spread: float = 0.0):
                "infer_frac_of_bf16_peak": infer_tflops / bf16_peak,
                "hash_bytes_per_query": 16 * 8 * 2 * 2,
                "train_step_ms_16384": train_ms,
-               "note": "mma.sync m16n8k16 BF16 (FP32 accumulate); inference includes the hash-grid and SH "
-                       "encoding in the same kernel; training step = fused forward/backward + weight-gradient "
-                       "GEMMs + Adam over all 16.8M hash and 22.5K MLP parameters (wall time, synchronised)"}
+               "note": "inference: tcgen05.mma kind::f16 (BF16, FP32 accumulators in TMEM), hash-grid and SH "
+                       "encoding in the same kernel, uniformly random queries; training step (mma.sync m16n8k16) "
+                       "= fused forward/backward + weight-gradient GEMMs + Adam over all 16.8M hash and 22.5K MLP "
+                       "parameters (wall time, synchronised)"}
     except Exception as ex:
         mlp = {"error": str(ex)}
     cache.close()
@@ -375,6 +376,10 @@ def nrc_study(B, ctx, sc, info, args, spread: float = 0.0):
         "plain_ms_to_target": tp, "nrc_ms_to_target": tn,
         "time_ratio_nrc_over_plain": (tn / tp) if (tp and tn) else None,
         "nrc_relmse_at_plain_time": at_plain,
+        # the bound: one cache frame against one plain path per pixel. A cache that removed no
+        # per-sample error could not reach the target sooner than the plain tracer at any
+        # frame cost; a 2x shorter time needs the cache frame's error (cost x relMSE) halved
+        "per_sample_relmse_ratio_nrc_over_plain": (curve[0][1] / plain[0][1]) if (curve and plain) else None,
         "nrc_frames": args.nrc_frames, "nrc_ms_per_frame": elapsed / args.nrc_frames,
         "nrc_queries_per_frame": queries, "nrc_train_samples_per_frame": samples,
         "nrc_loss_first_last": [float(np.mean(losses[:4])), float(np.mean(losses[-4:]))],
