@@ -129,3 +129,14 @@ def test_device_bvh_batch_build(gpu_ctx, scene_dir):
     for p, sc in zip(paths, built):
         assert sc.info().bvh_builder == 1
         check_structure(sc)
+
+
+def test_device_bvh_is_deterministic(gpu_ctx, scene_dir):
+    """Merges claim node slots with atomics, so binary node numbers vary from run to run;
+    the emitted wide tree depends only on the tree's shape and must not."""
+    path = _path("soup", scene_dir)
+    a = gpu_ctx.load_scene(path).build(builder="device")
+    b = gpu_ctx.load_scene(path).build(builder="device")
+    na, ta = a.export_bvh()
+    nb, tb = b.export_bvh()
+    assert np.array_equal(na, nb) and np.array_equal(ta, tb)
