@@ -551,6 +551,25 @@ def run_ours(args, world, rank, local):
     e2e_step = all_max(world, float(np.mean(e2e_ms)))
     e2e_value = world * paths / (e2e_step / 1000) / 1e6
 
+    # the same frame through the two-level form (one tree per geometry under a top level
+    # over the instances): throughput and acceleration-structure bytes beside the
+    # flattened form's
+    try:
+        tsc = ctx.load_scene(path).build(two_level=True)
+        ti = tsc.info()
+        ctx.render(tsc, spp=spp, out=out_dev)
+        tms = []
+        for _ in range(2):
+            tst = {}
+            ctx.render(tsc, spp=spp, out=out_dev, stats=tst)
+            tms.append(tst["device_ms"])
+        build_cmp["two_level"] = {"mpaths_s": paths / (float(np.mean(tms)) / 1000) / 1e6,
+                                  "bvh_bytes": ti.bvh_bytes, "flattened_bvh_bytes": info.bvh_bytes,
+                                  "build_ms": ti.build_ms}
+        tsc.close()
+    except Exception as ex:
+        build_cmp["two_level"] = {"error": str(ex)}
+
     # roofline of the dominant stage: stage times by CUDA events (profile 1), traversal
     # work from counters (profile 2), both on the same frame
     prof = {}

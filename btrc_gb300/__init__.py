@@ -43,12 +43,12 @@ class SceneInfo(C.Structure):
         ("area_lights", C.c_int32), ("media", C.c_int32), ("has_envir_light", C.c_int32),
         ("triangles", C.c_uint64), ("bvh_nodes", C.c_int32), ("bvh_depth", C.c_int32),
         ("bvh_bytes", C.c_uint64), ("world_min", C.c_float * 3), ("world_max", C.c_float * 3),
-        ("build_ms", C.c_double), ("bvh_ms", C.c_double), ("bvh_builder", C.c_int32),
+        ("build_ms", C.c_double), ("bvh_ms", C.c_double), ("bvh_builder", C.c_int32), ("two_level", C.c_int32),
     ]
 
 
 class BuildOpts(C.Structure):
-    _fields_ = [("threads", C.c_int32), ("builder", C.c_int32)]
+    _fields_ = [("threads", C.c_int32), ("builder", C.c_int32), ("two_level", C.c_int32)]
 
 
 BUILDERS = {"host": 0, "device": 1}
@@ -228,14 +228,15 @@ class Context:
         self._scenes.add(sc)
         return sc
 
-    def load_build_scenes(self, paths: list, threads: int = 0, builder: str = "host") -> list:
+    def load_build_scenes(self, paths: list, threads: int = 0, builder: str = "host",
+                          two_level: bool = False) -> list:
         """Load and build many scenes at once on one pool of host threads
         (btrc_scenes_load_build); builder "device" builds the BVHs on the GPU.
         Returns the built scenes in order."""
         n = len(paths)
         arr_p = (C.c_char_p * n)(*[str(p).encode() for p in paths])
         arr_s = (_vp * n)()
-        opts = BuildOpts(threads, BUILDERS[builder])
+        opts = BuildOpts(threads, BUILDERS[builder], 1 if two_level else 0)
         self._check(self._lib.btrc_scenes_load_build(self.handle, arr_p, n, C.byref(opts), arr_s))
         out = []
         for h in arr_s:
@@ -437,10 +438,11 @@ class Scene:
         self.ctx = ctx
         self.handle = handle
 
-    def build(self, threads: int = 0, builder: str = "host") -> "Scene":
+    def build(self, threads: int = 0, builder: str = "host", two_level: bool = False) -> "Scene":
         """btrc_scene_build; builder "host" (binned SAH on the host threads) or "device"
-        (PLOC on the GPU, then the same 8-wide collapse and node layout)."""
-        opts = BuildOpts(threads, BUILDERS[builder])
+        (PLOC on the GPU, then the same 8-wide collapse and node layout); two_level builds
+        one tree per geometry under a top level over the instances."""
+        opts = BuildOpts(threads, BUILDERS[builder], 1 if two_level else 0)
         self.ctx._check(self.ctx._lib.btrc_scene_build(self.handle, C.byref(opts)))
         return self
 

@@ -1,8 +1,10 @@
 // C-ABI implementation: host runtime around the CUDA kernels. No C++ exception
 // crosses this boundary; every failure becomes a btrc_status plus a message.
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <chrono>
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <exception>
@@ -112,6 +114,7 @@ struct btrc_scene
     double build_ms = 0;
     double bvh_ms = 0;
     int bvh_builder = 0;             // 0 host, 1 device
+    bool two_level = false;          // per-geometry trees under a top level over instances
     std::vector<AliasEntry8> filter_table_host;
     AliasEntry8 *filter_table = nullptr;
     uint64_t export_count = 0;       // flattened triangles (btrc_scene_export_triangles)
@@ -270,7 +273,110 @@ TriRec world_triangle(const HostScene &H, size_t i, size_t t)
     return TriRec{ a.x, a.y, a.z, static_cast<uint32_t>(i), b.x, b.y, b.z, static_cast<uint32_t>(t), c.x, c.y, c.z, 0u };
 }
 
-void build_scene(btrc_scene *sc, int threads, int builder)
+// Two-level form: one object-space tree per geometry (host builder), a top-level tree
+// over the instances' world boxes whose leaf records are the boxes themselves (v0 = low
+// corner with the instance index in v0.w, v1 = high corner), so that memory grows with
+// geometries, not with instances x triangles.
+void build_two_level(btrc_scene *sc, TaskPool &pool, DevScene &D)
+{
+    const HostScene &H = sc->host;
+    const size_t ng = H.geometries.size();
+    std::vector<char> used(ng, 0);
+    for(const auto &in : H.instances)
+        used[static_cast<size_t>(in.geometry)] = 1;
+    std::vector<CWNode> nodes;
+    std::vector<TriRec> tris;
+    std::vector<uint32_t> root(std::max<size_t>(ng, 1), 0xffffffffu);
+    std::vector<std::array<float, 6>> obox(ng);
+    int depth = 0;
+    for(size_t g = 0; g < ng; ++g)
+    {
+        const HostGeometry &geo = H.geometries[g];
+        const size_t nt = geo.area.size();
+        if(!used[g] || nt == 0)
+            continue;
+        std::vector<TriRec> obj(nt);
+        pool.parallel_for(nt, 1u << 14, [&](size_t b, size_t e) {
+            for(size_t t = b; t < e; ++t)
+            {
+                const V3 a = geo.pos[t * 3 + 0], bb = geo.pos[t * 3 + 1], c = geo.pos[t * 3 + 2];
+                obj[t] = TriRec{ a.x, a.y, a.z, 0u, bb.x, bb.y, bb.z, static_cast<uint32_t>(t), c.x, c.y, c.z, 0u };
+            }
+        });
+        std::array<float, 6> bx = { MAX_FLOAT, MAX_FLOAT, MAX_FLOAT, -MAX_FLOAT, -MAX_FLOAT, -MAX_FLOAT };
+        for(size_t k = 0; k < nt * 3; ++k)
+        {
+            const V3 &v = geo.pos[k];
+            bx[0] = std::min(bx[0], v.x); bx[1] = std::min(bx[1], v.y); bx[2] = std::min(bx[2], v.z);
+            bx[3] = std::max(bx[3], v.x); bx[4] = std::max(bx[4], v.y); bx[5] = std::max(bx[5], v.z);
+        }
+        obox[g] = bx;
+        CWBVH b = build_cwbvh(obj, pool);
+        const uint32_t noff = static_cast<uint32_t>(nodes.size()), toff = static_cast<uint32_t>(tris.size());
+        for(CWNode &nd : b.nodes)
+        {
+            nd.child_base += noff;
+            nd.tri_base += toff;
+        }
+        root[g] = noff;
+        nodes.insert(nodes.end(), b.nodes.begin(), b.nodes.end());
+        tris.insert(tris.end(), b.tris.begin(), b.tris.end());
+        depth = std::max(depth, b.depth);
+    }
+    // instance boxes: the geometry box's corners through the instance transform, widened
+    // by 1e-5 of the box's size and magnitude, which covers the rounding of the
+    // transforms in both directions many times over
+    std::vector<TriRec> boxes;
+    boxes.reserve(H.instances.size());
+    for(size_t i = 0; i < H.instances.size(); ++i)
+    {
+        const size_t g = static_cast<size_t>(H.instances[i].geometry);
+        if(root[g] == 0xffffffffu)
+            continue;
+        const auto &bx = obox[g];
+        float lo[3] = { MAX_FLOAT, MAX_FLOAT, MAX_FLOAT }, hi[3] = { -MAX_FLOAT, -MAX_FLOAT, -MAX_FLOAT };
+        for(int c = 0; c < 8; ++c)
+        {
+            const V3 w = H.instance_xf[i].point(V3(bx[(c & 1) ? 3 : 0], bx[(c & 2) ? 4 : 1], bx[(c & 4) ? 5 : 2]));
+            const float v[3] = { w.x, w.y, w.z };
+            for(int a = 0; a < 3; ++a)
+            {
+                lo[a] = std::min(lo[a], v[a]);
+                hi[a] = std::max(hi[a], v[a]);
+            }
+        }
+        float size = 0.0f;
+        for(int a = 0; a < 3; ++a)
+            size = std::max(size, std::max(hi[a] - lo[a], std::max(std::fabs(lo[a]), std::fabs(hi[a]))));
+        const float pad = size * 1e-5f + 1e-30f;
+        for(int a = 0; a < 3; ++a)
+        {
+            lo[a] -= pad;
+            hi[a] += pad;
+        }
+        boxes.push_back(TriRec{ lo[0], lo[1], lo[2], static_cast<uint32_t>(i), hi[0], hi[1], hi[2], 0u, lo[0], lo[1],
+                                lo[2], 0u });
+    }
+    CWBVH top = build_cwbvh(boxes, pool);
+    D.nodes = reinterpret_cast<const F4 *>(dev_upload(sc->allocs, top.nodes.data(), top.nodes.size()));
+    D.tris = reinterpret_cast<const F4 *>(dev_upload(sc->allocs, top.tris.data(), top.tris.size()));
+    D.node_count = static_cast<uint32_t>(top.nodes.size());
+    D.tri_count = static_cast<uint32_t>(top.tris.size());
+    D.blas_nodes = reinterpret_cast<const F4 *>(dev_upload(sc->allocs, nodes.data(), nodes.size()));
+    D.blas_tris = reinterpret_cast<const F4 *>(dev_upload(sc->allocs, tris.data(), tris.size()));
+    D.blas_root = dev_upload(sc->allocs, root.data(), root.size());
+    D.blas_node_count = static_cast<uint32_t>(nodes.size());
+    D.blas_tri_count = static_cast<uint32_t>(tris.size());
+    D.instance_count = static_cast<uint32_t>(H.instances.size());
+    D.two_level = 1;
+    sc->bvh_nodes = static_cast<int>(top.nodes.size() + nodes.size());
+    sc->bvh_depth = top.depth + depth;
+    sc->bvh_bytes = (top.nodes.size() + nodes.size()) * sizeof(CWNode) + (top.tris.size() + tris.size()) * sizeof(TriRec) +
+                    root.size() * sizeof(uint32_t);
+    sc->two_level = true;
+}
+
+void build_scene(btrc_scene *sc, int threads, int builder, int two_level)
 {
     HostScene &H = sc->host;
     const auto t0 = std::chrono::steady_clock::now();
@@ -297,8 +403,9 @@ void build_scene(btrc_scene *sc, int threads, int builder)
     std::vector<size_t> inst_first(H.instances.size() + 1, 0);
     for(size_t i = 0; i < H.instances.size(); ++i)
         inst_first[i + 1] = inst_first[i] + H.geometries[H.instances[i].geometry].area.size();
-    std::vector<TriRec> world(inst_first.back());
-    for(size_t i = 0; i < H.instances.size(); ++i)
+    const bool two = two_level != 0 && !host_only;
+    std::vector<TriRec> world(two ? 0 : inst_first.back());
+    for(size_t i = 0; i < H.instances.size() && !two; ++i)
     {
         const size_t base = inst_first[i];
         pool.parallel_for(H.geometries[H.instances[i].geometry].area.size(), 1u << 14,
@@ -307,16 +414,19 @@ void build_scene(btrc_scene *sc, int threads, int builder)
                                   world[base + t] = world_triangle(H, i, t);
                           });
     }
-    sc->export_count = world.size();
+    sc->export_count = inst_first.back();
     // the traversal's pooled triangle tests address triangle records with 27 bits
-    if(!host_only && world.size() >= (1ull << 27))
+    if(!host_only && !two && world.size() >= (1ull << 27))
         throw StatusError(BTRC_ERR_INVALID_ARG, "scene exceeds 2^27 triangle records");
     const bool keep_host = host_only || H.triangle_count <= (1u << 20);
     const auto tb = std::chrono::steady_clock::now();
     DevScene &D = sc->dev;
     D = DevScene{};
     sc->bvh_builder = 0;
-    if(builder == 1 && !host_only && !world.empty())
+    sc->two_level = false;
+    if(two)
+        build_two_level(sc, pool, D);
+    else if(builder == 1 && !host_only && !world.empty())
     {
         // device build on a stream of its own, so that concurrent scene builds overlap
         cudaStream_t bst = nullptr;
@@ -372,7 +482,7 @@ void build_scene(btrc_scene *sc, int threads, int builder)
             // no_progress / too_deep: the host builder takes the scene
         }
     }
-    if(sc->bvh_builder == 0)
+    if(sc->bvh_builder == 0 && !two)
     {
         CWBVH bvh = build_cwbvh(world, pool);
         sc->bvh_nodes = static_cast<int>(bvh.nodes.size());
@@ -787,7 +897,9 @@ btrc_status btrc_scene_build(btrc_scene *scene, const btrc_build_opts *opts)
 {
     if(!scene)
         return BTRC_ERR_INVALID_ARG;
-    return guarded(scene->ctx, [&] { build_scene(scene, opts ? opts->threads : 0, opts ? opts->builder : 0); });
+    return guarded(scene->ctx, [&] {
+        build_scene(scene, opts ? opts->threads : 0, opts ? opts->builder : 0, opts ? opts->two_level : 0);
+    });
 }
 
 btrc_status btrc_scenes_load_build(btrc_ctx *ctx, const char *const *paths, uint32_t n, const btrc_build_opts *opts,
@@ -821,7 +933,7 @@ btrc_status btrc_scenes_load_build(btrc_ctx *ctx, const char *const *paths, uint
                     sc->host = load_scene(paths[i]);
                     if(ctx->device >= 0)
                         check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
-                    build_scene(sc.get(), threads, opts ? opts->builder : 0);
+                    build_scene(sc.get(), threads, opts ? opts->builder : 0, opts ? opts->two_level : 0);
                     scs[i] = std::move(sc);
                 }
                 catch(...)
@@ -874,6 +986,7 @@ btrc_status btrc_scene_info_get(const btrc_scene *sc, btrc_scene_info *out)
     i.build_ms = sc->build_ms;
     i.bvh_ms = sc->bvh_ms;
     i.bvh_builder = sc->bvh_builder;
+    i.two_level = sc->two_level ? 1 : 0;
     *out = i;
     return BTRC_OK;
 }
@@ -1772,6 +1885,8 @@ std::unique_ptr<MergedBatch> merge_scenes(btrc_ctx *ctx, btrc_scene *const *scen
                               "merged batches take scenes without media, textures, image lights or volumes");
         if(D.node_count == 0)
             throw StatusError(BTRC_ERR_UNSUPPORTED, "merged batches take scenes with at least one triangle");
+        if(D.two_level)
+            throw StatusError(BTRC_ERR_UNSUPPORTED, "merged batches take single-level scenes");
         if(H.params.width > 65535)
             throw StatusError(BTRC_ERR_UNSUPPORTED, "film too wide for a merged batch");
         nodes += D.node_count;

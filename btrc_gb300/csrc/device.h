@@ -48,6 +48,18 @@ struct DevScene
     const float *env_probs;    // ibl tile probabilities
     const AliasEntry8 *env_alias;
     int32_t tri_round;         // pending triangle tests that start a pooled round
+
+    // two-level form (two_level != 0): nodes / tris above are the top level over instance
+    // boxes (a leaf record holds the instance index in v0.w); every geometry has its own
+    // object-space tree in blas_nodes / blas_tris, rooted at blas_root[geometry]
+    // (0xffffffff: no triangles)
+    const F4 *blas_nodes;
+    const F4 *blas_tris;
+    const uint32_t *blas_root;
+    uint32_t blas_node_count;
+    uint32_t blas_tri_count;
+    uint32_t instance_count;
+    int32_t two_level;
 };
 
 // default of DevScene::tri_round: on the 1080p terrain (3.1 M triangles) rounds of >= 16

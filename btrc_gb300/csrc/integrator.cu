@@ -19,6 +19,7 @@
 #include "nrc.h"
 #include "texture.h"
 #include "traverse.cuh"
+#include "two_level.cuh"
 
 namespace bt {
 
@@ -1020,29 +1021,35 @@ __global__ void __launch_bounds__(BLOCK) k_generate(DevRender R_in, PathSoA P, f
     }
 }
 
-template<bool COUNT, bool MULTI = false>
+// TWO: the scene's two-level form (no counting, no merged batch)
+template<bool COUNT, bool MULTI = false, bool TWO = false>
 __global__ void __launch_bounds__(TRAVERSE_BLOCK) k_trace(DevScene S, PathSoA P, uint32_t *flags, HitDetail *hits,
                                                Counters *cnt, DevRender R)
 {
     const uint32_t n = cnt->active;
     uint64_t nv = 0, tv = 0;
-    traverse_refill<false, COUNT>(
-        reinterpret_cast<const float4 *>(S.nodes), reinterpret_cast<const float4 *>(S.tris), S.node_count,
-        &cnt->trace_cursor, n, REFILL_LANES, &cnt->err,
-        [&](uint32_t i, float *o, float *d, float &t1, uint32_t &root) {
-            const F4 ro = P.ray_o[i], rd = P.ray_d[i];
-            o[0] = ro.x; o[1] = ro.y; o[2] = ro.z;
-            d[0] = rd.x; d[1] = rd.y; d[2] = rd.z;
-            t1 = rd.w;
-            if(MULTI)
-                root = R.batch[R.row_scene[__float_as_uint(P.rad_pixel[i].w) >> 16]].root;
-        },
-        [&](uint32_t i, const ClosestResult &c) {
-            flags[i] = c.hit ? (c.inst | HIT_BIT) : 0u;
-            hits[i] = HitDetail{ c.t, c.prim, c.b1, c.b2 };
-        },
-        &nv, &tv, S.tri_round);
-    if(COUNT)
+    auto fetch = [&](uint32_t i, float *o, float *d, float &t1, uint32_t &root) {
+        const F4 ro = P.ray_o[i], rd = P.ray_d[i];
+        o[0] = ro.x; o[1] = ro.y; o[2] = ro.z;
+        d[0] = rd.x; d[1] = rd.y; d[2] = rd.z;
+        t1 = rd.w;
+        if(MULTI)
+            root = R.batch[R.row_scene[__float_as_uint(P.rad_pixel[i].w) >> 16]].root;
+    };
+    auto emit = [&](uint32_t i, const ClosestResult &c) {
+        flags[i] = c.hit ? (c.inst | HIT_BIT) : 0u;
+        hits[i] = HitDetail{ c.t, c.prim, c.b1, c.b2 };
+    };
+    if constexpr(TWO)
+        traverse_refill<false, false, true>(reinterpret_cast<const float4 *>(S.nodes),
+                                            reinterpret_cast<const float4 *>(S.tris), S.node_count, &cnt->trace_cursor,
+                                            n, REFILL_LANES, &cnt->err, fetch, emit, nullptr, nullptr, S.tri_round,
+                                            two_level_view(S));
+    else
+        traverse_refill<false, COUNT>(reinterpret_cast<const float4 *>(S.nodes),
+                                      reinterpret_cast<const float4 *>(S.tris), S.node_count, &cnt->trace_cursor, n,
+                                      REFILL_LANES, &cnt->err, fetch, emit, &nv, &tv, S.tri_round);
+    if(COUNT && !TWO)
     {
         for(int off = 16; off > 0; off >>= 1)
         {
@@ -1559,47 +1566,52 @@ ShadeKernel shade_kernel(const DevScene &S, const DevRender &R)
 // the warp-refill traversal; unoccluded records splat (times the medium transmittance)
 // MEDIA = false compiles the transmittance code out, so the traversal of scenes without
 // media keeps its registers
-template<bool MEDIA, bool MULTI = false>
+template<bool MEDIA, bool MULTI = false, bool TWO = false>
 __global__ void __launch_bounds__(TRAVERSE_BLOCK) k_shadow(DevScene S, DevRender R, ShadowSoA SH, float4 *film,
                                                            Counters *cnt, int shq)
 {
     const uint32_t n = cnt->shadow_n[shq];
-    traverse_refill<true>(
-        reinterpret_cast<const float4 *>(S.nodes), reinterpret_cast<const float4 *>(S.tris), S.node_count,
-        &cnt->shadow_cursor[shq], n, REFILL_LANES, &cnt->err,
-        [&](uint32_t i, float *o, float *d, float &t1, uint32_t &root) {
-            const F4 so = SH.o[i], sd = SH.d[i];
-            o[0] = so.x; o[1] = so.y; o[2] = so.z;
-            d[0] = sd.x; d[1] = sd.y; d[2] = sd.z;
-            t1 = sd.w;
-            if(MULTI)
-                root = R.batch[R.row_scene[__float_as_uint(so.w) >> 16]].root;
-        },
-        [&](uint32_t i, const ClosestResult &c) {
-            if(c.hit)
-                return;
-            const F4 o = SH.o[i], d = SH.d[i], b = SH.beta[i];
-            V3 beta = v3(b);
-            if(MEDIA)
+    auto fetch = [&](uint32_t i, float *o, float *d, float &t1, uint32_t &root) {
+        const F4 so = SH.o[i], sd = SH.d[i];
+        o[0] = so.x; o[1] = so.y; o[2] = so.z;
+        d[0] = sd.x; d[1] = sd.y; d[2] = sd.z;
+        t1 = sd.w;
+        if(MULTI)
+            root = R.batch[R.row_scene[__float_as_uint(so.w) >> 16]].root;
+    };
+    auto emit = [&](uint32_t i, const ClosestResult &c) {
+        if(c.hit)
+            return;
+        const F4 o = SH.o[i], d = SH.d[i], b = SH.beta[i];
+        V3 beta = v3(b);
+        if(MEDIA)
+        {
+            DSampler smp;
+            smp.type = SAMPLER_INDEPENDENT;
+            smp.s = SH.sampler[i];
+            const V3 ro = v3(o), rdv = v3(d);
+            if(d.w > 1)
             {
-                DSampler smp;
-                smp.type = SAMPLER_INDEPENDENT;
-                smp.s = SH.sampler[i];
-                const V3 ro = v3(o), rdv = v3(d);
-                if(d.w > 1)
-                {
-                    const Medium &m = S.media[S.vacuum_medium];
-                    beta = beta * medium_tr(S, m, ro, ro + normalize(rdv) * S.world_diagonal, smp);
-                }
-                else
-                {
-                    const Medium &m = S.media[__float_as_int(b.w)];
-                    beta = beta * medium_tr(S, m, ro, ro + rdv * d.w, smp);
-                }
+                const Medium &m = S.media[S.vacuum_medium];
+                beta = beta * medium_tr(S, m, ro, ro + normalize(rdv) * S.world_diagonal, smp);
             }
-            splat(film, __float_as_uint(o.w), R.width, beta);
-        },
-        nullptr, nullptr, S.tri_round);
+            else
+            {
+                const Medium &m = S.media[__float_as_int(b.w)];
+                beta = beta * medium_tr(S, m, ro, ro + rdv * d.w, smp);
+            }
+        }
+        splat(film, __float_as_uint(o.w), R.width, beta);
+    };
+    if constexpr(TWO)
+        traverse_refill<true, false, true>(reinterpret_cast<const float4 *>(S.nodes),
+                                           reinterpret_cast<const float4 *>(S.tris), S.node_count,
+                                           &cnt->shadow_cursor[shq], n, REFILL_LANES, &cnt->err, fetch, emit, nullptr,
+                                           nullptr, S.tri_round, two_level_view(S));
+    else
+        traverse_refill<true>(reinterpret_cast<const float4 *>(S.nodes), reinterpret_cast<const float4 *>(S.tris),
+                              S.node_count, &cnt->shadow_cursor[shq], n, REFILL_LANES, &cnt->err, fetch, emit, nullptr,
+                              nullptr, S.tri_round);
 }
 
 __global__ void k_resolve(const float4 *film, float *rgb, uint32_t pixels)
@@ -1670,6 +1682,15 @@ void launch_shadow(const DevScene &S, const DevRender &R, RenderBuffers &B, int 
 {
     if(R.batch)
         k_shadow<false, true><<<grid, TRAVERSE_BLOCK, 0, st>>>(S, R, B.shadow[parity], B.film, B.counters, parity);
+    else if(S.two_level)
+    {
+        if(S.has_media)
+            k_shadow<true, false, true><<<grid, TRAVERSE_BLOCK, 0, st>>>(S, R, B.shadow[parity], B.film, B.counters,
+                                                                        parity);
+        else
+            k_shadow<false, false, true><<<grid, TRAVERSE_BLOCK, 0, st>>>(S, R, B.shadow[parity], B.film, B.counters,
+                                                                         parity);
+    }
     else if(S.has_media)
         k_shadow<true><<<grid, TRAVERSE_BLOCK, 0, st>>>(S, R, B.shadow[parity], B.film, B.counters, parity);
     else
@@ -1687,14 +1708,18 @@ void stage_grids(const DevScene &S, const DevRender &R, int grids[6])
     const bool multi = R.batch != nullptr;
     grids[0] = persistent_grid(sb, multi ? reinterpret_cast<const void *>(k_generate<true>)
                                          : reinterpret_cast<const void *>(k_generate<false>), R.grid_pct);
-    grids[1] = persistent_grid(TRAVERSE_BLOCK, multi ? reinterpret_cast<const void *>(k_trace<false, true>)
-                                                     : reinterpret_cast<const void *>(k_trace<false>), R.grid_pct);
+    grids[1] = persistent_grid(TRAVERSE_BLOCK, multi        ? reinterpret_cast<const void *>(k_trace<false, true>)
+                                               : S.two_level ? reinterpret_cast<const void *>(k_trace<false, false, true>)
+                                                             : reinterpret_cast<const void *>(k_trace<false>),
+                               R.grid_pct);
     grids[2] = persistent_grid(sb, reinterpret_cast<const void *>(k_medium), R.grid_pct);
     grids[3] = persistent_grid(sb, reinterpret_cast<const void *>(shade_kernel(S, R)), R.grid_pct);
-    grids[4] = persistent_grid(TRAVERSE_BLOCK, multi ? reinterpret_cast<const void *>(k_shadow<false, true>)
-                                               : S.has_media ? reinterpret_cast<const void *>(k_shadow<true>)
-                                                             : reinterpret_cast<const void *>(k_shadow<false>),
-                               R.grid_pct);
+    const void *shadow_fn = multi ? reinterpret_cast<const void *>(k_shadow<false, true>)
+                            : S.two_level ? (S.has_media ? reinterpret_cast<const void *>(k_shadow<true, false, true>)
+                                                         : reinterpret_cast<const void *>(k_shadow<false, false, true>))
+                            : S.has_media ? reinterpret_cast<const void *>(k_shadow<true>)
+                                          : reinterpret_cast<const void *>(k_shadow<false>);
+    grids[4] = persistent_grid(TRAVERSE_BLOCK, shadow_fn, R.grid_pct);
     grids[5] = persistent_grid(BLOCK, reinterpret_cast<const void *>(k_order), R.grid_pct);  // sized for BLOCK
 }
 
@@ -1719,6 +1744,9 @@ cudaError_t enqueue_bounce(const DevScene &S, const DevRender &R, RenderBuffers 
     timed(T, STAGE_TRACE, st, launches, [&] {
         if(R.batch)
             k_trace<false, true><<<grids[1], TRAVERSE_BLOCK, 0, st>>>(S, P, B.hit_flag, B.hit_detail, B.counters, R);
+        else if(S.two_level)
+            k_trace<false, false, true><<<grids[1], TRAVERSE_BLOCK, 0, st>>>(S, P, B.hit_flag, B.hit_detail,
+                                                                             B.counters, R);
         else if(profile == 2)
             k_trace<true><<<grids[1], TRAVERSE_BLOCK, 0, st>>>(S, P, B.hit_flag, B.hit_detail, B.counters, R);
         else
@@ -2202,8 +2230,6 @@ __global__ void __launch_bounds__(128) k_nrc_train_paths(DevScene S, DevRender R
 {
     const uint32_t pixels = static_cast<uint32_t>(R.width) * R.height;
     const uint32_t n = phase < pixels ? (pixels - phase + stride - 1) / stride : 0;
-    const float4 *nodes = reinterpret_cast<const float4 *>(S.nodes);
-    const float4 *tris = reinterpret_cast<const float4 *>(S.tris);
     for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     {
         const uint32_t pixel = i * stride + phase;
@@ -2237,8 +2263,8 @@ __global__ void __launch_bounds__(128) k_nrc_train_paths(DevScene S, DevRender R
         int nv = 0;
         for(int depth = 0; depth < 256; ++depth)
         {
-            const ClosestResult c = trace_closest(make_trav_ray(o.x, o.y, o.z, d.x, d.y, d.z), MAX_FLOAT, nodes, tris,
-                                                  S.node_count, err);
+            const float ro3[3] = { o.x, o.y, o.z }, rd3[3] = { d.x, d.y, d.z };
+            const ClosestResult c = scene_closest(S, ro3, rd3, MAX_FLOAT, err);
             if(!c.hit)
             {
                 rad = rad + miss_le(S, d, beta_le, bsdf_pdf);
@@ -2286,9 +2312,8 @@ __global__ void __launch_bounds__(128) k_nrc_train_paths(DevScene S, DevRender R
                 {
                     const float cs = fabsf(dot(normalize(ls.d), sp.frame.z));
                     const V3 li = ls.li * beta * f * cs / (spdf + ls.light_pdf);
-                    if(!trace_any(make_trav_ray(ls.o.x, ls.o.y, ls.o.z, ls.d.x, ls.d.y, ls.d.z), ls.t1, nodes, tris,
-                                  S.node_count, err) &&
-                       all_finite(li))
+                    const float so3[3] = { ls.o.x, ls.o.y, ls.o.z }, sd3[3] = { ls.d.x, ls.d.y, ls.d.z };
+                    if(!scene_any(S, so3, sd3, ls.t1, err) && all_finite(li))
                         rad = rad + li;
                 }
             }

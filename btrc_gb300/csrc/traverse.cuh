@@ -408,14 +408,34 @@ constexpr int TRAVERSE_WARPS = TRAVERSE_BLOCK / 32;
 constexpr uint32_t TRI_INDEX_BITS = 27;
 constexpr uint32_t MAX_POOLED_TRIANGLES = 1u << TRI_INDEX_BITS;
 
+// The two-level form (TWO): nodes4 / tris4 are the top level, whose leaf records are
+// instance boxes (instance index in v0.w). A lane with pending instance leaves enters one
+// at a time: it pushes its top-level node group and a marker entry (base | 2^31: node
+// indices never set that bit) holding the remaining instances, takes its ray into the
+// instance's object space (multiplies and adds rounded in the host transform's order),
+// and walks the geometry's tree from its root; pooled triangle tests then use the
+// object-space ray from shared memory like any other, and the owner stamps its
+// instance on the results. Popping the marker restores the world ray.
+struct TwoLevelView
+{
+    const float4 *blas_nodes4;
+    const float4 *blas_tris4;
+    const uint32_t *blas_root;
+    const float *inst_rec;     // Instance records viewed as floats (w2l at offset 12)
+    uint32_t inst_stride;      // floats per Instance record
+    uint32_t inst_geometry;    // float offset of Instance::geometry
+    uint32_t inst_count;
+};
+constexpr uint32_t MARKER_BIT = 0x80000000u;
+
 // fetch(i, o, d, t1, root) loads ray i; root (0 unless fetch sets it) is the node the
 // ray starts from, so that one node array can hold several BVHs
-template<bool ANY, bool COUNT = false, typename Fetch, typename Emit>
+template<bool ANY, bool COUNT = false, bool TWO = false, typename Fetch, typename Emit>
 __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes4, const float4 *__restrict__ tris4,
                                                 uint32_t node_count, uint32_t *cursor, uint32_t n, int refill,
                                                 uint32_t *err, Fetch fetch, Emit emit,
                                                 uint64_t *node_visits = nullptr, uint64_t *tri_tests = nullptr,
-                                                int min_round = 1)
+                                                int min_round = 1, const TwoLevelView tl = TwoLevelView{})
 {
     // per lane: (ox, oy, oz, Sx), (Sy, Sz, kx | ky << 2 | kz << 4, tmax); per warp: the queue
     __shared__ float4 s_ray0[TRAVERSE_WARPS][32];
@@ -431,10 +451,16 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
     uint32_t ray = 0;
     TravRay r;
     ClosestResult best;
-    uint2 stack[STACK_SIZE];
+    constexpr int STACK = TWO ? 2 * STACK_SIZE : STACK_SIZE;
+    uint2 stack[STACK];
     int sp = 0;
     uint2 ngroup = make_uint2(0u, 0u);
     uint2 tgroup = make_uint2(0u, 0u);
+    // two-level state: world ray, whether the lane is inside an instance, which one
+    float wo[3] = { 0.0f, 0.0f, 0.0f }, wd[3] = { 0.0f, 0.0f, 0.0f };
+    bool inside = false;
+    uint32_t cur_inst = 0;
+    const float4 *const leaf_tris4 = TWO ? tl.blas_tris4 : tris4;
     for(;;)
     {
         const uint32_t idle = __ballot_sync(FULL, state == 0);
@@ -455,6 +481,16 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
                     uint32_t root = 0;
                     fetch(mine, o, d, t1, root);
                     r = make_trav_ray(o[0], o[1], o[2], d[0], d[1], d[2]);
+                    if(TWO)
+                    {
+#pragma unroll
+                        for(int k = 0; k < 3; ++k)
+                        {
+                            wo[k] = o[k];
+                            wd[k] = d[k];
+                        }
+                        inside = false;
+                    }
                     ray = mine;
                     best.hit = false;
                     best.t = t1;
@@ -475,8 +511,57 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
         if(__all_sync(FULL, state == 2))
             break;
 
+        // two-level: a lane at the top level with pending instance leaves enters one
+        if(TWO && state == 1 && !inside && tgroup.y != 0u)
+        {
+            const int tb = 31 - __clz(tgroup.y);
+            tgroup.y &= ~(1u << tb);
+            const uint32_t ti = tgroup.x + static_cast<uint32_t>(tb);
+            const uint32_t inst = __float_as_uint(__ldg(tris4 + ti * 3).w);
+            const float *rec = tl.inst_rec + static_cast<size_t>(min(inst, tl.inst_count - 1u)) * tl.inst_stride;
+            const uint32_t root = inst < tl.inst_count ? tl.blas_root[__float_as_int(rec[tl.inst_geometry])] : 0xffffffffu;
+            if(inst >= tl.inst_count)
+                atomicOr(err, 2u);
+            if(root != 0xffffffffu)
+            {
+                if(sp + 2 > STACK)
+                {
+                    atomicOr(err, 1u);
+                    ngroup = make_uint2(0u, 0u);
+                    tgroup = make_uint2(0u, 0u);
+                    sp = 0;
+                }
+                else
+                {
+                    if(ngroup.y > 0x00ffffffu)
+                        stack[sp++] = ngroup;
+                    stack[sp++] = make_uint2(tgroup.x | MARKER_BIT, tgroup.y);
+                    float oo[3], od[3];
+#pragma unroll
+                    for(int rr = 0; rr < 3; ++rr)
+                    {
+                        const float *row = rec + 12 + rr * 4;
+                        float v = __fmul_rn(row[0], wo[0]);
+                        v = __fadd_rn(v, __fmul_rn(row[1], wo[1]));
+                        v = __fadd_rn(v, __fmul_rn(row[2], wo[2]));
+                        oo[rr] = __fadd_rn(v, row[3]);
+                        float w = __fmul_rn(row[0], wd[0]);
+                        w = __fadd_rn(w, __fmul_rn(row[1], wd[1]));
+                        od[rr] = __fadd_rn(w, __fmul_rn(row[2], wd[2]));
+                    }
+                    r = make_trav_ray(oo[0], oo[1], oo[2], od[0], od[1], od[2]);
+                    s_ray0[warp][lane] = make_float4(r.ox, r.oy, r.oz, r.Sx);
+                    s_ray1[warp][lane] =
+                        make_float4(r.Sy, r.Sz, __int_as_float(r.kx | (r.ky << 2) | (r.kz << 4)), best.t);
+                    inside = true;
+                    cur_inst = inst;
+                    ngroup = make_uint2(root, 0x80000000u);
+                    tgroup = make_uint2(0u, 0u);
+                }
+            }
+        }
         // node step: busy lanes without pending triangles
-        if(state == 1 && tgroup.y == 0u && ngroup.y > 0x00ffffffu)
+        else if(state == 1 && tgroup.y == 0u && ngroup.y > 0x00ffffffu)
         {
             if(COUNT)
                 ++visits;
@@ -488,7 +573,7 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
             bool overflow = false;
             if(ngroup.y > 0x00ffffffu)
             {
-                if(sp >= STACK_SIZE)
+                if(sp >= STACK)
                 {
                     atomicOr(err, 1u);
                     overflow = true;
@@ -505,7 +590,8 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
             else
             {
                 uint32_t cbase, tbase, imask;
-                const uint32_t hm = intersect_children(r, nodes4, ni, best.t, cbase, tbase, imask);
+                const uint32_t hm =
+                    intersect_children(r, TWO && inside ? tl.blas_nodes4 : nodes4, ni, best.t, cbase, tbase, imask);
                 ngroup = make_uint2(cbase, (hm & 0xff000000u) | imask);
                 tgroup = make_uint2(tbase, hm & 0x00ffffffu);
             }
@@ -514,10 +600,13 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
         // triangle round (all lanes). A round runs once min_round tests are pending, or
         // when no busy lane could make progress without one (every busy lane waits on
         // its triangles); queue positions come from a warp prefix sum of the counts.
-        const uint32_t cnt = static_cast<uint32_t>(__popc(tgroup.y));
+        // (two-level: only lanes inside an instance hold triangles; instance leaves are
+        // entered, not tested)
+        const bool pooling = !TWO || inside;
+        const uint32_t cnt = pooling ? static_cast<uint32_t>(__popc(tgroup.y)) : 0u;
         const uint32_t total = __reduce_add_sync(FULL, cnt);
         bool found_any = false;
-        const uint32_t steppers = __ballot_sync(FULL, state == 1 && tgroup.y == 0u);
+        const uint32_t steppers = __ballot_sync(FULL, state == 1 && (tgroup.y == 0u || !pooling));
         const bool round = total != 0u && (total >= static_cast<uint32_t>(min_round) || steppers == 0u);
         if(round)
         {
@@ -559,9 +648,9 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
                 tr.Sx = q0.w; tr.Sy = q1.x; tr.Sz = q1.y;
                 const int kk = __float_as_int(q1.z);
                 tr.kx = kk & 3; tr.ky = (kk >> 2) & 3; tr.kz = (kk >> 4) & 3;
-                const float4 a = __ldg(tris4 + ti * 3 + 0);
-                const float4 b = __ldg(tris4 + ti * 3 + 1);
-                const float4 c = __ldg(tris4 + ti * 3 + 2);
+                const float4 a = __ldg(leaf_tris4 + ti * 3 + 0);
+                const float4 b = __ldg(leaf_tris4 + ti * 3 + 1);
+                const float4 c = __ldg(leaf_tris4 + ti * 3 + 2);
                 TriHit h;
                 if(watertight(tr, a, b, c, q1.w, h))
                 {
@@ -572,6 +661,8 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
                     hprim = __float_as_uint(b.w);
                 }
             }
+            // two-level: object-space records carry no instance; the owner's is the one
+            const uint32_t my_inst = cur_inst;
             // owners merge their entries [excl, excl + take): the smallest t by shuffling
             // t alone, then the winner's record; equal t within one owner's entries (a ray
             // through a shared edge) takes the exact (t, instance, primitive) order
@@ -610,7 +701,7 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
                 {
                     const float cb1 = __shfl_sync(FULL, hb1, static_cast<int>(msrc));
                     const float cb2 = __shfl_sync(FULL, hb2, static_cast<int>(msrc));
-                    const uint32_t ci = __shfl_sync(FULL, hinst, static_cast<int>(msrc));
+                    const uint32_t ci = TWO ? my_inst : __shfl_sync(FULL, hinst, static_cast<int>(msrc));
                     const uint32_t cp = __shfl_sync(FULL, hprim, static_cast<int>(msrc));
                     if(mt != NO_HIT && (!best.hit || closer(mt, ci, cp, best.t, best.inst, best.prim)))
                     {
@@ -630,7 +721,7 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
                         const float ct = __shfl_sync(FULL, ht, src);
                         const float cb1 = __shfl_sync(FULL, hb1, src);
                         const float cb2 = __shfl_sync(FULL, hb2, src);
-                        const uint32_t ci = __shfl_sync(FULL, hinst, src);
+                        const uint32_t ci = TWO ? my_inst : __shfl_sync(FULL, hinst, src);
                         const uint32_t cp = __shfl_sync(FULL, hprim, src);
                         if(k < take && ct != NO_HIT &&
                            (!best.hit || closer(ct, ci, cp, best.t, best.inst, best.prim)))
@@ -664,7 +755,22 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
                 state = 0;
             }
             else
-                ngroup = stack[--sp];
+            {
+                const uint2 e = stack[--sp];
+                if(TWO && (e.x & MARKER_BIT))
+                {
+                    // back at the top level: the world ray and the remaining instances
+                    r = make_trav_ray(wo[0], wo[1], wo[2], wd[0], wd[1], wd[2]);
+                    s_ray0[warp][lane] = make_float4(r.ox, r.oy, r.oz, r.Sx);
+                    s_ray1[warp][lane] =
+                        make_float4(r.Sy, r.Sz, __int_as_float(r.kx | (r.ky << 2) | (r.kz << 4)), best.t);
+                    inside = false;
+                    ngroup = make_uint2(0u, 0u);
+                    tgroup = make_uint2(e.x & ~MARKER_BIT, e.y);
+                }
+                else
+                    ngroup = e;
+            }
         }
     }
     if(COUNT)

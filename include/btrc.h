@@ -88,6 +88,7 @@ typedef struct btrc_scene_info
     double build_ms;
     double bvh_ms;            /* the BVH part of build_ms */
     int32_t bvh_builder;      /* the builder that made the BVH: 0 host, 1 device */
+    int32_t two_level;        /* 1: two-level form (bvh_* then cover both levels) */
 } btrc_scene_info;
 
 typedef struct btrc_build_opts
@@ -98,6 +99,12 @@ typedef struct btrc_build_opts
                                  for batches and cold starts; a scene the device build
                                  refuses (non-finite boxes, a tree deeper than the
                                  traversal stack) is built on the host */
+    int32_t two_level;        /* 1: one object-space BVH per geometry under a top-level BVH
+                                 over the instances (the form of the reference's IAS over
+                                 GASes; memory grows with geometries, not instances x
+                                 triangles; rays are walked one per thread, so it traces
+                                 slower than the flattened form); every level is built
+                                 on the host. Not taken by merged batches. */
 } btrc_build_opts;
 
 typedef struct btrc_render_opts

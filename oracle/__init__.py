@@ -118,6 +118,63 @@ class OracleBvh:
             pass
 
 
+def _xf_rows(m: np.ndarray, v: np.ndarray, translate: bool) -> np.ndarray:
+    """Rows of (N, 3) float32 vectors through a 3x4 matrix, ((m0 x + m1 y) + m2 z) (+ m3)
+    with every product and sum rounded to FP32: the host's Transform::point order."""
+    x, y, z = v[:, 0], v[:, 1], v[:, 2]
+    cols = []
+    for r in range(3):
+        a = (m[r, 0] * x).astype(np.float32)
+        a = (a + (m[r, 1] * y).astype(np.float32)).astype(np.float32)
+        a = (a + (m[r, 2] * z).astype(np.float32)).astype(np.float32)
+        if translate:
+            a = (a + m[r, 3]).astype(np.float32)
+        cols.append(a)
+    return np.stack(cols, axis=1).astype(np.float32)
+
+
+def two_level_trace(S, rays: np.ndarray, threads: int = 0):
+    """Closest and any hit through per-instance object-space rays (the two-level form of
+    the acceleration structure): every instance's world-to-local matrix takes the rays
+    into object space, the geometry's own triangles are intersected there with the
+    oracle's watertight test, and hits combine in (t, instance, primitive) order, as
+    OptiX's IAS over GASes does (core/btrc/core/scene.cpp:196-209). S is an
+    oracle.scene.Scene. Returns (flags, hits, occluded) in btrc_trace_* layout."""
+    rays = np.ascontiguousarray(rays, np.float32)
+    n = len(rays)
+    best_t = np.full(n, np.inf, np.float32)
+    best_inst = np.full(n, 0xFFFFFFFF, np.uint64)
+    best_prim = np.full(n, 0xFFFFFFFF, np.uint64)
+    hits = np.zeros((n, 4), np.float32)
+    occ = np.zeros(n, np.uint32)
+    trees = {}
+    for i, g in enumerate(S.inst_geo):
+        g = int(g)
+        cnt, off = int(S.geo_count[g]), int(S.geo_offset[g])
+        if cnt == 0:
+            continue
+        if g not in trees:
+            ids = np.stack([np.zeros(cnt, np.uint32), np.arange(cnt, dtype=np.uint32)], 1)
+            trees[g] = OracleBvh(S.local_pos[off:off + cnt], ids)
+        w = S.inst_w2l[i].reshape(3, 4).astype(np.float32)
+        r = rays.copy()
+        r[:, 0:3] = _xf_rows(w, rays[:, 0:3], True)
+        r[:, 4:7] = _xf_rows(w, rays[:, 4:7], False)
+        f, h = trees[g].closest(r, threads)
+        t = h[:, 0]
+        prim = h[:, 1].view(np.uint32).astype(np.uint64)
+        better = (f != 0) & ((t < best_t) | ((t == best_t) & ((i < best_inst) | ((i == best_inst) & (prim < best_prim)))))
+        best_t[better] = t[better]
+        best_inst[better] = i
+        best_prim[better] = prim[better]
+        hits[better] = h[better]
+        occ |= trees[g].any(r, threads)
+    hit = best_inst != 0xFFFFFFFF
+    flags = np.where(hit, best_inst.astype(np.uint32) | np.uint32(1 << 30), np.uint32(0)).astype(np.uint32)
+    hits[~hit] = 0.0
+    return flags, hits, occ
+
+
 def sampler_batch(kind: int, width: int, height: int, pixel_xy: np.ndarray, sample_index: np.ndarray,
                   dims: int) -> np.ndarray:
     pixel_xy = np.ascontiguousarray(pixel_xy, np.uint32)
