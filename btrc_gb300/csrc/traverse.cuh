@@ -223,6 +223,19 @@ __device__ __forceinline__ uint32_t intersect_children(const TravRay &r, const f
     return hitmask;
 }
 
+// Ray against an axis-aligned box [lo, hi] over (0, tmax], the interval widened by 2^-20
+// relative on both ends (the distances carry rounding errors of ~2^-23 relative), so the
+// test stays conservative at any distance from the ray origin, like the node test
+__device__ __forceinline__ bool box_hit(const TravRay &r, const float4 &lo, const float4 &hi, float tmax)
+{
+    const float x0 = (lo.x - r.ox) * r.idx, x1 = (hi.x - r.ox) * r.idx;
+    const float y0 = (lo.y - r.oy) * r.idy, y1 = (hi.y - r.oy) * r.idy;
+    const float z0 = (lo.z - r.oz) * r.idz, z1 = (hi.z - r.oz) * r.idz;
+    const float tn = fmaxf(max3f(fminf(x0, x1), fminf(y0, y1), fminf(z0, z1)) * (2.0f - BOX_EPS), 0.0f);
+    const float tf = fminf(min3f(fmaxf(x0, x1), fmaxf(y0, y1), fmaxf(z0, z1)), tmax) * BOX_EPS;
+    return tn <= tf;
+}
+
 // Lexicographic (t, inst, prim) comparison used for closest-hit ties.
 __device__ __forceinline__ bool closer(float t, uint32_t inst, uint32_t prim, float bt, uint32_t binst, uint32_t bprim)
 {
@@ -517,11 +530,16 @@ __device__ __forceinline__ void traverse_refill(const float4 *__restrict__ nodes
             const int tb = 31 - __clz(tgroup.y);
             tgroup.y &= ~(1u << tb);
             const uint32_t ti = tgroup.x + static_cast<uint32_t>(tb);
-            const uint32_t inst = __float_as_uint(__ldg(tris4 + ti * 3).w);
+            const float4 blo = __ldg(tris4 + ti * 3), bhi = __ldg(tris4 + ti * 3 + 1);
+            const uint32_t inst = __float_as_uint(blo.w);
             const float *rec = tl.inst_rec + static_cast<size_t>(min(inst, tl.inst_count - 1u)) * tl.inst_stride;
-            const uint32_t root = inst < tl.inst_count ? tl.blas_root[__float_as_int(rec[tl.inst_geometry])] : 0xffffffffu;
+            uint32_t root = inst < tl.inst_count ? tl.blas_root[__float_as_int(rec[tl.inst_geometry])] : 0xffffffffu;
             if(inst >= tl.inst_count)
                 atomicOr(err, 2u);
+            // the instance's own box (a leaf slot's box covers up to three): the box is
+            // widened at build time far beyond the rounding of this test
+            if(root != 0xffffffffu && !box_hit(r, blo, bhi, best.t))
+                root = 0xffffffffu;
             if(root != 0xffffffffu)
             {
                 if(sp + 2 > STACK)

@@ -179,12 +179,15 @@ __device__ __forceinline__ ClosestResult trace_two_level(const DevScene &S, cons
                 tgroup.y = 0u;
                 break;
             }
-            const uint32_t inst = __float_as_uint(__ldg(tris4 + ti * 3).w);
+            const float4 blo = __ldg(tris4 + ti * 3), bhi = __ldg(tris4 + ti * 3 + 1);
+            const uint32_t inst = __float_as_uint(blo.w);
             if(inst >= S.instance_count)
             {
                 atomicOr(err, 2u);
                 continue;
             }
+            if(!box_hit(rw, blo, bhi, best.t))
+                continue;
             const Instance &I = S.instances[inst];
             const uint32_t root = S.blas_root[I.geometry];
             if(root == 0xffffffffu)

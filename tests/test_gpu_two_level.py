@@ -5,7 +5,8 @@ over GASes (core/btrc/core/scene.cpp:196-209).
 - traversal: closest hit (flags, t, barycentrics) and any hit bit-exact against the
   oracle's two-level restatement (oracle.two_level_trace: the same rounded object-space
   rays, the oracle's own watertight test, hits combined in (t, instance, primitive)
-  order), on random rays, segments and rays aimed at triangle vertices and edges;
+  order), on random rays, segments, rays from hundreds of scene sizes away and rays
+  aimed at triangle vertices and edges;
 - memory: the two-level scene holds each instanced geometry once;
 - rendering: a frame through the two-level form equals the flattened form's frame up to
   the rounding of object-space hit distances."""
@@ -30,7 +31,17 @@ def _rays(rng, S, n, n_edge):
     seg = rng.random(n) < 0.3
     rays[seg, 4:7] *= rng.uniform(0.05, 2.0, (int(seg.sum()), 1)).astype(np.float32)
     rays[seg, 7] = 1.0
-    return np.concatenate([rays, edge_rays(rng, S.tris, n_edge)])
+    # far origins (hundreds of scene sizes away) aimed at triangle centroids: box tests
+    # must stay conservative when distances dwarf the instance boxes' padding
+    m = n // 10
+    tgt = S.tris[rng.integers(0, len(S.tris), m)].reshape(m, 3, 3).mean(1)
+    d = rng.normal(size=(m, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    far = np.zeros((m, 8), np.float32)
+    far[:, 0:3] = tgt - d * rng.uniform(100.0, 1000.0, (m, 1)) * float(np.max(hi - lo))
+    far[:, 4:7] = d
+    far[:, 7] = 3.0e38
+    return np.concatenate([rays, far, edge_rays(rng, S.tris, n_edge)])
 
 
 def _compare(ctx, path, n=20000, n_edge=10000, seed=3):
