@@ -51,10 +51,12 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched uneven-scenes measurement")
     ap.add_argument("--nrc-frames", type=int, default=1000, help="frames of the radiance-cache study")
     ap.add_argument("--ref-spp", type=int, default=4096, help="spp of the converged reference image")
-    ap.add_argument("--probe", choices=["nrc", "medium", "generate", "trace"],
+    ap.add_argument("--probe", choices=["nrc", "medium", "generate", "trace", "trace-two-level", "build-device"],
                     help="run one small profiling case and exit: nrc (cache inference on 2^20 queries and "
                          "training steps of 16,384 samples), medium (volume workload at 256x256, 4 spp), "
-                         "generate / trace (terrain at 1920x1080, 1 spp, 2 M-state queue)")
+                         "generate / trace (terrain at 1920x1080, 1 spp, 2 M-state queue), trace-two-level "
+                         "(the same through the two-level acceleration structure), build-device (the "
+                         "terrain's BVH built on the device)")
     ap.add_argument("--trace-probe", action="store_true",
                     help="trace the workload's camera rays, then one diffuse bounce ray per camera hit, "
                          "through btrc_trace_closest (two launches, for DRAM-traffic captures) and exit")
@@ -823,6 +825,14 @@ def probe(args):
     import btrc_gb300 as B
     from btrc_gb300 import scenes
     ctx = B.Context(0)
+    if args.probe == "build-device":
+        p = scenes.terrain(width=1920, height=1080, spp=1, state_count=1 << 21)
+        sc = ctx.load_scene(p).build(builder="device")
+        info = sc.info()
+        print(json.dumps({"bvh_ms": info.bvh_ms, "build_ms": info.build_ms, "bvh_nodes": info.bvh_nodes,
+                          "builder": info.bvh_builder}), flush=True)
+        ctx.close()
+        return
     if args.probe == "nrc":
         p = scenes.terrain(width=480, height=270, spp=1, grid=256, instances=20)
         sc = ctx.load_scene(p).build()
@@ -846,7 +856,7 @@ def probe(args):
             p = scenes.volume(width=256, height=256, spp=4, state_count=1 << 20)
         else:
             p = scenes.terrain(width=1920, height=1080, spp=1, state_count=1 << 21)
-        sc = ctx.load_scene(p).build()
+        sc = ctx.load_scene(p).build(two_level=args.probe == "trace-two-level")
         info = sc.info()
         img = torch.empty((info.height, info.width, 3), device="cuda")
         st = {}
