@@ -717,9 +717,10 @@ GpuBvhStatus gpu_build_cwbvh(const TriRec *d_tris, uint32_t n, cudaStream_t st, 
         // clustering: nearest neighbours, merges of mutual pairs, compaction
         uint32_t m = n;
         int cur = 0, iterations = 0;
-        uint32_t *h_m = nullptr;
-        if((e = cudaMallocHost(&h_m, sizeof(uint32_t))) != cudaSuccess)
-            return fail(e, "pinned counter");
+        // small readbacks into host variables (no pinned allocation per build: concurrent
+        // builds of a batch would wait on each other's page-locking)
+        uint32_t h_m_value = 0;
+        uint32_t *h_m = &h_m_value;
         while(m > 1)
         {
             if(++iterations > MAX_ITERATIONS)
@@ -747,7 +748,6 @@ GpuBvhStatus gpu_build_cwbvh(const TriRec *d_tris, uint32_t n, cudaStream_t st, 
             }
             m = next;
         }
-        cudaFreeHost(h_m);
         if(e != cudaSuccess)
             return fail(e, "device BVH clustering");
         if(status != GpuBvhStatus::ok)
@@ -795,12 +795,12 @@ GpuBvhStatus gpu_build_cwbvh(const TriRec *d_tris, uint32_t n, cudaStream_t st, 
         uint32_t *ni = tmp.get<uint32_t>(static_cast<size_t>(n) + 1), *nt = tmp.get<uint32_t>(static_cast<size_t>(n) + 1);
         uint32_t *cbase = tmp.get<uint32_t>(static_cast<size_t>(n) + 1);
         uint32_t *tbase = tmp.get<uint32_t>(static_cast<size_t>(n) + 1);
-        uint32_t *totals = nullptr;
-        if(tmp.e != cudaSuccess || cudaMallocHost(&totals, 4 * sizeof(uint32_t)) != cudaSuccess)
+        uint32_t totals[4] = {};
+        if(tmp.e != cudaSuccess)
         {
             cudaFree(leaf_tris);
             leaf_tris = nullptr;
-            return fail(tmp.e != cudaSuccess ? tmp.e : cudaErrorMemoryAllocation, "device BVH emission buffers");
+            return fail(tmp.e, "device BVH emission buffers");
         }
         e = cudaMemcpyAsync(level[0], &root, sizeof(uint32_t), cudaMemcpyHostToDevice, st);
         uint32_t count = 1, level_base = 0, tri_cursor = 0;
@@ -851,7 +851,6 @@ GpuBvhStatus gpu_build_cwbvh(const TriRec *d_tris, uint32_t n, cudaStream_t st, 
                (e = cudaStreamSynchronize(st)) == cudaSuccess && (totals[2] != 0 || tri_cursor != n))
                 status = GpuBvhStatus::internal;
         }
-        cudaFreeHost(totals);
         if(e == cudaSuccess && status == GpuBvhStatus::ok)
         {
             if(cudaMalloc(&wide, sizeof(CWNode) * level_base) != cudaSuccess)

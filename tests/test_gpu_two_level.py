@@ -104,3 +104,25 @@ def test_two_level_refused_by_merged_batch(gpu_ctx, scene_dir):
     with pytest.raises(B.BtrcError) as e:
         gpu_ctx.render_batch([sc], [out], merged=True)
     assert e.value.status == 8
+
+
+def test_two_level_noalloc_and_cache_frames(gpu_ctx, scene_dir):
+    """The allocation-free entry point and the radiance-cache frames (whose training paths
+    walk the two-level form one thread per path) take two-level scenes too."""
+    import torch
+    import btrc_gb300 as B
+    path = scenes.terrain(seed=7, width=64, height=64, spp=4, grid=128, instances=8, out_dir=scene_dir / "terrain-n")
+    sc = gpu_ctx.load_scene(path).build(two_level=True)
+    ref = gpu_ctx.render(sc)
+    out = torch.zeros((64, 64, 3), dtype=torch.float32, device="cuda")
+    gpu_ctx.render_noalloc(sc, out)
+    torch.cuda.synchronize()
+    assert np.allclose(out.cpu().numpy(), ref, rtol=1e-5, atol=1e-6)
+    info = sc.info()
+    cache = B.RadianceCache(gpu_ctx, info.world_min, info.world_max, seed=1)
+    st = {}
+    img = cache.render_frame(sc, 0, stats=st)
+    cache.render_frame(sc, 1, stats=st)
+    assert np.all(np.isfinite(img)) and st["train_samples"] > 0 and st["queries"] > 0
+    cache.close()
+
