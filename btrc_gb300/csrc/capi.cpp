@@ -636,6 +636,7 @@ void build_scene(btrc_scene *sc, int threads, int builder, int two_level)
     const V3 ext = H.world_max - H.world_min;
     D.world_diagonal = length(ext);
     D.tri_round = TRI_ROUND_TESTS;
+    D.shadow_round = TRI_ROUND_SHADOW;
 
     // film filter table
     if(H.params.filter == FILTER_GAUSSIAN)

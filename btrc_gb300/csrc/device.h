@@ -47,7 +47,8 @@ struct DevScene
     const MaterialTex *material_tex;
     const float *env_probs;    // ibl tile probabilities
     const AliasEntry8 *env_alias;
-    int32_t tri_round;         // pending triangle tests that start a pooled round
+    int32_t tri_round;         // pending triangle tests that start a pooled round (closest hit)
+    int32_t shadow_round;      // the same for any-hit (shadow) traversal
 
     // two-level form (two_level != 0): nodes / tris above are the top level over instance
     // boxes (a leaf record holds the instance index in v0.w); every geometry has its own
@@ -65,6 +66,10 @@ struct DevScene
 // default of DevScene::tri_round: on the 1080p terrain (3.1 M triangles) rounds of >= 16
 // pending tests traced 5 % faster than rounds started for any test (1, 8, 16, 24 measured)
 constexpr int32_t TRI_ROUND_TESTS = 16;
+// default of DevScene::shadow_round: the shadow kernel on the same frame gave 997.8,
+// 999.4, 1005.2, 1011.4, 1017.6, 1020.3, 1021.2, 1018.7 and 1011.6 Mpaths/s for rounds of
+// 1, 4, 8, 12, 16, 20, 24, 28 and 32 pending tests
+constexpr int32_t TRI_ROUND_SHADOW = 24;
 
 struct BatchScene;
 

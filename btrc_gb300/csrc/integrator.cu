@@ -1607,11 +1607,11 @@ __global__ void __launch_bounds__(TRAVERSE_BLOCK) k_shadow(DevScene S, DevRender
         traverse_refill<true, false, true>(reinterpret_cast<const float4 *>(S.nodes),
                                            reinterpret_cast<const float4 *>(S.tris), S.node_count,
                                            &cnt->shadow_cursor[shq], n, REFILL_LANES, &cnt->err, fetch, emit, nullptr,
-                                           nullptr, S.tri_round, two_level_view(S));
+                                           nullptr, S.shadow_round, two_level_view(S));
     else
         traverse_refill<true>(reinterpret_cast<const float4 *>(S.nodes), reinterpret_cast<const float4 *>(S.tris),
                               S.node_count, &cnt->shadow_cursor[shq], n, REFILL_LANES, &cnt->err, fetch, emit, nullptr,
-                              nullptr, S.tri_round);
+                              nullptr, S.shadow_round);
 }
 
 __global__ void k_resolve(const float4 *film, float *rgb, uint32_t pixels)

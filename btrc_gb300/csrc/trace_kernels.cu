@@ -67,7 +67,8 @@ __global__ void __launch_bounds__(TRACE_BLOCK) k_trace_any_dyn(DevScene S, const
             d[0] = rd.x; d[1] = rd.y; d[2] = rd.z;
             t1 = rd.w;
         },
-        [&](uint32_t i, const ClosestResult &c) { occluded[i] = c.hit ? 1u : 0u; }, nullptr, nullptr, S.tri_round);
+        [&](uint32_t i, const ClosestResult &c) { occluded[i] = c.hit ? 1u : 0u; }, nullptr, nullptr,
+        S.shadow_round);
 }
 
 // the two-level form (the cursor must be zero at launch)
@@ -97,7 +98,7 @@ __global__ void __launch_bounds__(TRACE_BLOCK) k_trace_two_level(DevScene S, con
                 hits[i] = c.hit ? HitDetail{ c.t, c.prim, c.b1, c.b2 } : HitDetail{ 0.0f, 0u, 0.0f, 0.0f };
             }
         },
-        nullptr, nullptr, S.tri_round, two_level_view(S));
+        nullptr, nullptr, ANY ? S.shadow_round : S.tri_round, two_level_view(S));
 }
 
 uint32_t persistent_blocks(const void *kernel)
