@@ -63,9 +63,11 @@ struct DevScene
     int32_t two_level;
 };
 
-// default of DevScene::tri_round: on the 1080p terrain (3.1 M triangles) rounds of >= 16
-// pending tests traced 5 % faster than rounds started for any test (1, 8, 16, 24 measured)
-constexpr int32_t TRI_ROUND_TESTS = 16;
+// default of DevScene::tri_round: on the 1080p terrain (3.1 M triangles, 32 M-state queue,
+// shadow rounds at 24) closest-hit rounds of 16, 20 and 24 pending tests gave 1020.6-1020.9,
+// 1027.0 and 1025.7-1025.8 Mpaths/s (two runs each); rounds started for any single test
+// traced 5 % slower than 16
+constexpr int32_t TRI_ROUND_TESTS = 20;
 // default of DevScene::shadow_round: the shadow kernel on the same frame gave 997.8,
 // 999.4, 1005.2, 1011.4, 1017.6, 1020.3, 1021.2, 1018.7 and 1011.6 Mpaths/s for rounds of
 // 1, 4, 8, 12, 16, 20, 24, 28 and 32 pending tests
