@@ -642,7 +642,9 @@ def run_ours(args, world, rank, local):
             nrc_interior = {"scene": "config 0's Cornell box (two icospheres, quad light) at 512x512",
                             **{k: nrc_interior[k] for k in ("target_relmse", "reference_spp", "plain_ms_to_target",
                                                             "nrc_ms_to_target", "time_ratio_nrc_over_plain",
-                                                            "nrc_relmse_at_plain_time", "nrc_ms_per_frame",
+                                                            "nrc_relmse_at_plain_time",
+                                                            "per_sample_relmse_ratio_nrc_over_plain",
+                                                            "nrc_ms_per_frame",
                                                             "nrc_queries_per_frame", "plain_curve_ms_relmse",
                                                             "nrc_curve_ms_relmse", "spread_rule")}}
             csc.close()
