@@ -104,7 +104,8 @@ typedef struct btrc_build_opts
                                  GASes; memory grows with geometries, not instances x
                                  triangles; rays are walked one per thread, so it traces
                                  slower than the flattened form); every level is built
-                                 on the host. Not taken by merged batches. */
+                                 on the host. Not taken by merged batches; host-only
+                                 contexts (device < 0) build the flattened form. */
 } btrc_build_opts;
 
 typedef struct btrc_render_opts

@@ -63,6 +63,9 @@ def test_host_only_context_loads_and_builds(native_lib, tmp_path):
     with pytest.raises(B.BtrcError) as e:
         ctx.render(sc)
     assert e.value.status == 1 and "host-only" in str(e.value)
+    # host-only contexts build the flattened form whatever the options ask for
+    sc2 = ctx.load_scene(p).build(two_level=True)
+    assert sc2.info().two_level == 0 and sc2.info().bvh_nodes == info.bvh_nodes
 
 
 @pytest.mark.parametrize("content,status", [
