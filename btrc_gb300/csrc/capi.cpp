@@ -96,7 +96,8 @@ struct btrc_ctx
     // radiance-cache frame buffers (queries, weights, predictions, training samples)
     std::vector<void *> nrc_allocs;
     size_t nrc_pixels = 0, nrc_sample_cap = 0;
-    float *nrc_query = nullptr, *nrc_samples = nullptr;
+    float *nrc_query = nullptr, *nrc_samples = nullptr, *nrc_samples2 = nullptr;  // samples by frame parity
+    int nrc_parity = 0;
     float4 *nrc_weight = nullptr, *nrc_pred = nullptr;
     uint32_t *nrc_counts = nullptr;
     float2 *nrc_spread[2] = {};      // path-spread state per queue slot, by bounce parity
@@ -851,6 +852,8 @@ void btrc_ctx_destroy(btrc_ctx *ctx)
     cudaSetDevice(ctx->device);
     if(ctx->stream)
         cudaStreamSynchronize(ctx->stream);
+    if(!ctx->nrc_allocs.empty())
+        cudaDeviceSynchronize();  // a cache's training may still read the sample buffers
     for(void *p : ctx->buf_allocs)
         cudaFree(p);
     for(void *p : ctx->nrc_allocs)
@@ -1509,10 +1512,38 @@ btrc_status btrc_image_save(btrc_ctx *ctx, const char *filename, const float *pi
     });
 }
 
+// A cache's frame training runs on a stream of its own, beside the next frame's path
+// tracing (which does not read the weights); whatever reads or writes the weights waits
+// for it first (wait_training).
 struct btrc_nrc
 {
     btrc_ctx *ctx;
     std::unique_ptr<bt::Nrc> impl;
+    cudaStream_t train_stream = nullptr;
+    cudaEvent_t ready = nullptr;     // this frame's samples written and inference done
+    cudaEvent_t trained = nullptr;   // the last frame's Adam steps done
+    bool pending = false;
+    float *loss_host = nullptr;      // pinned, one slot per frame parity (sum over the frame's steps)
+    int loss_steps[2] = {};          // Adam steps behind each slot
+    int parity = 0;
+    void wait_training()
+    {
+        if(pending && train_stream)
+            cudaStreamSynchronize(train_stream);
+        pending = false;
+    }
+    ~btrc_nrc()
+    {
+        wait_training();
+        if(ready)
+            cudaEventDestroy(ready);
+        if(trained)
+            cudaEventDestroy(trained);
+        if(train_stream)
+            cudaStreamDestroy(train_stream);
+        if(loss_host)
+            cudaFreeHost(loss_host);
+    }
 };
 
 namespace {
@@ -1521,7 +1552,8 @@ void ensure_nrc_buffers(btrc_ctx *ctx, size_t pixels, size_t sample_cap)
 {
     if(ctx->nrc_pixels >= pixels && ctx->nrc_sample_cap >= sample_cap && ctx->nrc_counts)
         return;
-    check_cuda(cudaStreamSynchronize(ctx->stream), "stream sync");
+    // a cache's training may still read the old sample buffers on its own stream
+    check_cuda(cudaDeviceSynchronize(), "device sync");
     for(void *p : ctx->nrc_allocs)
         cudaFree(p);
     ctx->nrc_allocs.clear();
@@ -1531,6 +1563,7 @@ void ensure_nrc_buffers(btrc_ctx *ctx, size_t pixels, size_t sample_cap)
     ctx->nrc_weight = static_cast<float4 *>(A(sizeof(float4) * pixels));
     ctx->nrc_pred = static_cast<float4 *>(A(sizeof(float4) * pixels));
     ctx->nrc_samples = static_cast<float *>(A(sizeof(float) * NRC_SAMPLE_FLOATS * std::max<size_t>(sample_cap, 1)));
+    ctx->nrc_samples2 = static_cast<float *>(A(sizeof(float) * NRC_SAMPLE_FLOATS * std::max<size_t>(sample_cap, 1)));
     ctx->nrc_counts = static_cast<uint32_t *>(A(sizeof(uint32_t) * 4));
     for(auto &sp : ctx->nrc_spread)
         sp = static_cast<float2 *>(A(sizeof(float2) * pixels));
@@ -1576,6 +1609,17 @@ btrc_status btrc_render_nrc_frame(btrc_ctx *ctx, btrc_scene *scene, btrc_nrc *nr
         R.nrc_count = ctx->nrc_counts;
         R.nrc_cap = static_cast<uint32_t>(pixels);
         ctx->buf.capacity = capacity;
+        if(!nrc->train_stream)
+        {
+            check_cuda(cudaStreamCreateWithFlags(&nrc->train_stream, cudaStreamNonBlocking), "training stream");
+            check_cuda(cudaEventCreateWithFlags(&nrc->ready, cudaEventDisableTiming), "training event");
+            check_cuda(cudaEventCreateWithFlags(&nrc->trained, cudaEventDisableTiming), "training event");
+            check_cuda(cudaMallocHost(&nrc->loss_host, 2 * sizeof(float)), "loss buffer");
+            nrc->loss_host[0] = nrc->loss_host[1] = 0.0f;
+        }
+        // this frame's samples: the buffer the last frame's training (maybe still running)
+        // does not read
+        float *samples = ctx->nrc_parity ? ctx->nrc_samples2 : ctx->nrc_samples;
         RenderStats rs{};
         check_cuda(render_wavefront(scene->dev, R, ctx->buf, s, &ctx->cancel, true, 0, &rs, &cancelled),
                    "wavefront render");
@@ -1586,7 +1630,7 @@ btrc_status btrc_render_nrc_frame(btrc_ctx *ctx, btrc_scene *scene, btrc_nrc *nr
         {
             const uint32_t stride = static_cast<uint32_t>(opts->train_stride);
             const uint32_t phase = (opts->frame * 7u + 3u) % stride;
-            check_cuda(launch_nrc_train_paths(scene->dev, R, stride, phase, opts->frame + (1u << 20), ctx->nrc_samples,
+            check_cuda(launch_nrc_train_paths(scene->dev, R, stride, phase, opts->frame + (1u << 20), samples,
                                               ctx->nrc_counts + 1, static_cast<uint32_t>(sample_cap), err, s),
                        "training paths");
         }
@@ -1594,6 +1638,9 @@ btrc_status btrc_render_nrc_frame(btrc_ctx *ctx, btrc_scene *scene, btrc_nrc *nr
         check_cuda(cudaMemcpyAsync(counts, ctx->nrc_counts, sizeof(counts), cudaMemcpyDeviceToHost, s), "counters");
         check_cuda(cudaStreamSynchronize(s), "counters");
         const uint32_t nq = std::min<uint32_t>(counts[0], static_cast<uint32_t>(pixels));
+        // inference reads the weights the last frame's training writes
+        if(nrc->pending)
+            check_cuda(cudaStreamWaitEvent(s, nrc->trained, 0), "training wait");
         if(nq > 0 && opts->terminate_vertex >= 0)
         {
             check_cuda(nrc->impl->infer(ctx->nrc_query, nq, reinterpret_cast<float *>(ctx->nrc_pred), s),
@@ -1603,23 +1650,39 @@ btrc_status btrc_render_nrc_frame(btrc_ctx *ctx, btrc_scene *scene, btrc_nrc *nr
                        "cache splat");
         }
         check_cuda(launch_resolve(ctx->buf.film, rgb_dev, static_cast<uint32_t>(pixels), s), "resolve");
-        // train on this frame's samples
+        // train on this frame's samples, on the cache's own stream after this frame's
+        // inference: the call returns without waiting for it, and the next frame's path
+        // tracing runs beside it
         const uint32_t ns = std::min<uint32_t>(counts[1], static_cast<uint32_t>(sample_cap));
-        float loss = 0.0f;
+        // the last frame's loss slot: final once this frame's stream work (which waited for
+        // that training) has completed, read after the frame sync below
+        const int prev_slot = nrc->parity ^ 1;
         int steps = 0;
-        check_cuda(nrc->impl->reset_loss(s), "cache training");
         for(int k = 0; k < opts->train_steps; ++k)
+            if(static_cast<uint32_t>(k) * static_cast<uint32_t>(opts->train_batch) < ns)
+                ++steps;
+        if(steps > 0)
         {
-            const uint32_t b0 = static_cast<uint32_t>(k) * static_cast<uint32_t>(opts->train_batch);
-            if(b0 >= ns)
-                break;
-            const uint32_t nb = std::min<uint32_t>(static_cast<uint32_t>(opts->train_batch), ns - b0);
-            check_cuda(nrc->impl->train(ctx->nrc_samples + static_cast<size_t>(b0) * NRC_SAMPLE_FLOATS, nb, true, s),
-                       "cache training");
-            ++steps;
+            cudaStream_t ts = nrc->train_stream;
+            check_cuda(cudaEventRecord(nrc->ready, s), "training event");
+            check_cuda(cudaStreamWaitEvent(ts, nrc->ready, 0), "training wait");
+            check_cuda(nrc->impl->reset_loss(ts), "cache training");
+            for(int k = 0; k < steps; ++k)
+            {
+                const uint32_t b0 = static_cast<uint32_t>(k) * static_cast<uint32_t>(opts->train_batch);
+                const uint32_t nb = std::min<uint32_t>(static_cast<uint32_t>(opts->train_batch), ns - b0);
+                check_cuda(nrc->impl->train(samples + static_cast<size_t>(b0) * NRC_SAMPLE_FLOATS, nb, true, ts),
+                           "cache training");
+            }
+            check_cuda(nrc->impl->copy_loss_async(nrc->loss_host + nrc->parity, ts), "cache training");
+            check_cuda(cudaEventRecord(nrc->trained, ts), "training event");
+            nrc->pending = true;
         }
-        if(fstats && steps)
-            check_cuda(nrc->impl->read_loss(&loss, s), "cache training");
+        else
+            nrc->loss_host[nrc->parity] = 0.0f;
+        nrc->loss_steps[nrc->parity] = steps;
+        nrc->parity ^= 1;
+        ctx->nrc_parity ^= 1;
         if(!on_dev)
             check_cuda(cudaMemcpyAsync(rgb_out, rgb_dev, pixels * 3 * sizeof(float), cudaMemcpyDeviceToHost, s),
                        "image download");
@@ -1631,7 +1694,9 @@ btrc_status btrc_render_nrc_frame(btrc_ctx *ctx, btrc_scene *scene, btrc_nrc *nr
             fstats->queries = nq;
             fstats->train_samples = ns;
             fstats->train_steps = steps;
-            fstats->loss = steps ? loss / steps : 0.0f;
+            // the last frame's training has finished by now (this frame's stream waited for
+            // it before inference); this frame's finishes after the call returns
+            fstats->loss = nrc->loss_steps[prev_slot] ? nrc->loss_host[prev_slot] / nrc->loss_steps[prev_slot] : 0.0f;
             fstats->render_ms = rs.device_ms;
             fstats->wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
         }
@@ -1689,6 +1754,7 @@ btrc_status btrc_nrc_infer(btrc_ctx *ctx, btrc_nrc *nrc, const float *d_queries,
         return BTRC_ERR_INVALID_ARG;
     return guarded(ctx, [&] {
         check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+        nrc->wait_training();
         check_cuda(nrc->impl->infer(d_queries, static_cast<uint32_t>(n), d_out, pick_stream(ctx, stream)),
                    "radiance cache inference");
     });
@@ -1701,6 +1767,7 @@ btrc_status btrc_nrc_train(btrc_ctx *ctx, btrc_nrc *nrc, const float *d_samples,
         return BTRC_ERR_INVALID_ARG;
     return guarded(ctx, [&] {
         check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+        nrc->wait_training();
         check_cuda(nrc->impl->reset_loss(ctx->stream), "radiance cache training");
         check_cuda(nrc->impl->train(d_samples, static_cast<uint32_t>(n), apply_adam != 0, ctx->stream),
                    "radiance cache training");
@@ -1717,6 +1784,7 @@ btrc_status btrc_nrc_params(btrc_ctx *ctx, btrc_nrc *nrc, int32_t which, float *
         return BTRC_ERR_INVALID_ARG;
     return guarded(ctx, [&] {
         check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+        nrc->wait_training();
         const cudaError_t e = nrc->impl->copy_params(which, host, count, set != 0, ctx->stream);
         if(e == cudaErrorInvalidValue)
             throw StatusError(BTRC_ERR_INVALID_ARG, "parameter count mismatch");

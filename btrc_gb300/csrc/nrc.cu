@@ -1205,6 +1205,11 @@ cudaError_t Nrc::read_loss(float *out, cudaStream_t st)
     return check_error(st);
 }
 
+cudaError_t Nrc::copy_loss_async(float *out, cudaStream_t st)
+{
+    return cudaMemcpyAsync(out, loss_, sizeof(float), cudaMemcpyDeviceToHost, st);
+}
+
 cudaError_t Nrc::check_error(cudaStream_t st)
 {
     uint32_t e = 0;

@@ -74,6 +74,8 @@ public:
     cudaError_t reset_loss(cudaStream_t st);
     // synchronises st and returns the accumulated loss
     cudaError_t read_loss(float *out, cudaStream_t st);
+    // the loss accumulator copied to host memory on st without waiting (pinned `out`)
+    cudaError_t copy_loss_async(float *out, cudaStream_t st);
     // synchronises st; cudaErrorLaunchTimeout when a tensor-core kernel gave up waiting
     cudaError_t check_error(cudaStream_t st);
 

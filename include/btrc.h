@@ -375,7 +375,9 @@ typedef struct btrc_nrc_frame_stats
     uint64_t queries;          /* paths that ended in a cache query */
     uint64_t train_samples;    /* training samples produced */
     int32_t train_steps;
-    float loss;                /* mean training loss of the frame's steps */
+    float loss;                /* mean training loss of the previous frame's steps (a frame's
+                                  Adam steps run on the cache's own stream after the call
+                                  returns, beside the next frame's path tracing) */
     double render_ms;          /* GPU time of the wavefront loop */
     double wall_ms;            /* host wall time of the call */
 } btrc_nrc_frame_stats;
@@ -383,7 +385,10 @@ typedef struct btrc_nrc_frame_stats
 /* One frame of one path per pixel through the wavefront renderer with paths terminated
    into the radiance cache, training paths for 1 / train_stride of the pixels, cache
    inference and splatting, then the frame's Adam steps. rgb_out receives the frame's
-   width*height*3 image (radiance / weight). Scenes with participating media:
+   width*height*3 image (radiance / weight) when the call returns; the Adam steps run on
+   the cache's own stream and may still be running then, beside the next frame's path
+   tracing. The next frame's inference, btrc_nrc_infer, btrc_nrc_train, btrc_nrc_params
+   and btrc_nrc_destroy wait for them. Scenes with participating media:
    BTRC_ERR_UNSUPPORTED. */
 btrc_status btrc_render_nrc_frame(btrc_ctx *ctx, btrc_scene *scene, btrc_nrc *nrc, const btrc_nrc_render_opts *opts,
                                   float *rgb_out, btrc_nrc_frame_stats *stats);
