@@ -1522,6 +1522,7 @@ struct btrc_nrc
     cudaStream_t train_stream = nullptr;
     cudaEvent_t ready = nullptr;     // this frame's samples written and inference done
     cudaEvent_t trained = nullptr;   // the last frame's Adam steps done
+    cudaEvent_t paths_done = nullptr;  // this frame's training paths traced
     bool pending = false;
     float *loss_host = nullptr;      // pinned, one slot per frame parity (sum over the frame's steps)
     int loss_steps[2] = {};          // Adam steps behind each slot
@@ -1539,6 +1540,8 @@ struct btrc_nrc
             cudaEventDestroy(ready);
         if(trained)
             cudaEventDestroy(trained);
+        if(paths_done)
+            cudaEventDestroy(paths_done);
         if(train_stream)
             cudaStreamDestroy(train_stream);
         if(loss_host)
@@ -1614,26 +1617,36 @@ btrc_status btrc_render_nrc_frame(btrc_ctx *ctx, btrc_scene *scene, btrc_nrc *nr
             check_cuda(cudaStreamCreateWithFlags(&nrc->train_stream, cudaStreamNonBlocking), "training stream");
             check_cuda(cudaEventCreateWithFlags(&nrc->ready, cudaEventDisableTiming), "training event");
             check_cuda(cudaEventCreateWithFlags(&nrc->trained, cudaEventDisableTiming), "training event");
+            check_cuda(cudaEventCreateWithFlags(&nrc->paths_done, cudaEventDisableTiming), "training event");
             check_cuda(cudaMallocHost(&nrc->loss_host, 2 * sizeof(float)), "loss buffer");
             nrc->loss_host[0] = nrc->loss_host[1] = 0.0f;
         }
         // this frame's samples: the buffer the last frame's training (maybe still running)
         // does not read
         float *samples = ctx->nrc_parity ? ctx->nrc_samples2 : ctx->nrc_samples;
-        RenderStats rs{};
-        check_cuda(render_wavefront(scene->dev, R, ctx->buf, s, &ctx->cancel, true, 0, &rs, &cancelled),
-                   "wavefront render");
         const bool on_dev = opts->output_on_device != 0;
         float *rgb_dev = on_dev ? rgb_out : ctx_scratch_images(ctx, pixels, 1);
         uint32_t *err = ctx_scratch_err(ctx);
-        if(opts->train_stride > 0 && sample_cap > 0)
+        // training paths (they read no weights) on the cache's stream, beside this frame's
+        // path tracing, after the counter clear
+        const bool train_paths = opts->train_stride > 0 && sample_cap > 0;
+        if(train_paths)
         {
+            cudaStream_t ts = nrc->train_stream;
+            check_cuda(cudaEventRecord(nrc->ready, s), "training event");
+            check_cuda(cudaStreamWaitEvent(ts, nrc->ready, 0), "training wait");
             const uint32_t stride = static_cast<uint32_t>(opts->train_stride);
             const uint32_t phase = (opts->frame * 7u + 3u) % stride;
             check_cuda(launch_nrc_train_paths(scene->dev, R, stride, phase, opts->frame + (1u << 20), samples,
-                                              ctx->nrc_counts + 1, static_cast<uint32_t>(sample_cap), err, s),
+                                              ctx->nrc_counts + 1, static_cast<uint32_t>(sample_cap), err, ts),
                        "training paths");
+            check_cuda(cudaEventRecord(nrc->paths_done, ts), "training event");
         }
+        RenderStats rs{};
+        check_cuda(render_wavefront(scene->dev, R, ctx->buf, s, &ctx->cancel, true, 0, &rs, &cancelled),
+                   "wavefront render");
+        if(train_paths)
+            check_cuda(cudaStreamWaitEvent(s, nrc->paths_done, 0), "training wait");
         uint32_t counts[4] = {};
         check_cuda(cudaMemcpyAsync(counts, ctx->nrc_counts, sizeof(counts), cudaMemcpyDeviceToHost, s), "counters");
         check_cuda(cudaStreamSynchronize(s), "counters");
