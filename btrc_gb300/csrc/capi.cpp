@@ -95,9 +95,8 @@ struct btrc_ctx
     std::unique_ptr<MergedBatch> merged;                              // the last merged batch of scenes
     // radiance-cache frame buffers (queries, weights, predictions, training samples)
     std::vector<void *> nrc_allocs;
-    size_t nrc_pixels = 0, nrc_sample_cap = 0;
-    float *nrc_query = nullptr, *nrc_samples = nullptr, *nrc_samples2 = nullptr;  // samples by frame parity
-    int nrc_parity = 0;
+    size_t nrc_pixels = 0;
+    float *nrc_query = nullptr;
     float4 *nrc_weight = nullptr, *nrc_pred = nullptr;
     uint32_t *nrc_counts = nullptr;
     float2 *nrc_spread[2] = {};      // path-spread state per queue slot, by bounce parity
@@ -853,7 +852,7 @@ void btrc_ctx_destroy(btrc_ctx *ctx)
     if(ctx->stream)
         cudaStreamSynchronize(ctx->stream);
     if(!ctx->nrc_allocs.empty())
-        cudaDeviceSynchronize();  // a cache's training may still read the sample buffers
+        cudaDeviceSynchronize();  // a cache's training paths may still be using the context's scratch
     for(void *p : ctx->buf_allocs)
         cudaFree(p);
     for(void *p : ctx->nrc_allocs)
@@ -1512,38 +1511,60 @@ btrc_status btrc_image_save(btrc_ctx *ctx, const char *filename, const float *pi
     });
 }
 
-// A cache's frame training runs on a stream of its own, beside the next frame's path
-// tracing (which does not read the weights); whatever reads or writes the weights waits
-// for it first (wait_training).
+// A cache's frame work beside the path tracing: the training paths of a frame run on a
+// stream of their own beside its path tracing and fill one of three sample buffers; the
+// frame's Adam steps train on them on a second stream beside the next frame's path
+// tracing (the weights are read only by inference, which waits for the last Adam steps).
+// Whatever else reads or writes the weights or the samples waits first (wait_training).
 struct btrc_nrc
 {
     btrc_ctx *ctx;
     std::unique_ptr<bt::Nrc> impl;
-    cudaStream_t train_stream = nullptr;
-    cudaEvent_t ready = nullptr;     // this frame's samples written and inference done
-    cudaEvent_t trained = nullptr;   // the last frame's Adam steps done
-    cudaEvent_t paths_done = nullptr;  // this frame's training paths traced
+    cudaStream_t train_stream = nullptr;  // Adam steps
+    cudaStream_t path_stream = nullptr;   // training paths
+    cudaEvent_t ready = nullptr;          // a point of the frame's own stream to start from
+    cudaEvent_t trained = nullptr;        // the last Adam steps done
+    cudaEvent_t paths_done[3] = {};       // training paths of each sample buffer traced
     bool pending = false;
-    float *loss_host = nullptr;      // pinned, one slot per frame parity (sum over the frame's steps)
-    int loss_steps[2] = {};          // Adam steps behind each slot
+    float *samples[3] = {};               // training samples, three frames in rotation
+    uint32_t *sample_count = nullptr;     // one counter per buffer
+    size_t sample_cap = 0;
+    int slot = 0;                         // buffer of the next frame
+    float *loss_host = nullptr;           // pinned, one slot per call parity (sum over steps)
+    int loss_steps[2] = {};               // Adam steps behind each slot
     int parity = 0;
     void wait_training()
     {
+        if(path_stream)
+            cudaStreamSynchronize(path_stream);
         if(pending && train_stream)
             cudaStreamSynchronize(train_stream);
         pending = false;
     }
+    void free_samples()
+    {
+        for(float *&p : samples)
+        {
+            if(p)
+                cudaFree(p);
+            p = nullptr;
+        }
+        if(sample_count)
+            cudaFree(sample_count);
+        sample_count = nullptr;
+        sample_cap = 0;
+    }
     ~btrc_nrc()
     {
         wait_training();
-        if(ready)
-            cudaEventDestroy(ready);
-        if(trained)
-            cudaEventDestroy(trained);
-        if(paths_done)
-            cudaEventDestroy(paths_done);
+        free_samples();
+        for(cudaEvent_t ev : { ready, trained, paths_done[0], paths_done[1], paths_done[2] })
+            if(ev)
+                cudaEventDestroy(ev);
         if(train_stream)
             cudaStreamDestroy(train_stream);
+        if(path_stream)
+            cudaStreamDestroy(path_stream);
         if(loss_host)
             cudaFreeHost(loss_host);
     }
@@ -1551,27 +1572,37 @@ struct btrc_nrc
 
 namespace {
 
-void ensure_nrc_buffers(btrc_ctx *ctx, size_t pixels, size_t sample_cap)
+void ensure_nrc_buffers(btrc_ctx *ctx, size_t pixels)
 {
-    if(ctx->nrc_pixels >= pixels && ctx->nrc_sample_cap >= sample_cap && ctx->nrc_counts)
+    if(ctx->nrc_pixels >= pixels && ctx->nrc_counts)
         return;
-    // a cache's training may still read the old sample buffers on its own stream
-    check_cuda(cudaDeviceSynchronize(), "device sync");
+    check_cuda(cudaStreamSynchronize(ctx->stream), "stream sync");
     for(void *p : ctx->nrc_allocs)
         cudaFree(p);
     ctx->nrc_allocs.clear();
-    ctx->nrc_pixels = ctx->nrc_sample_cap = 0;
+    ctx->nrc_pixels = 0;
     auto A = [&](size_t bytes) { return dev_alloc(ctx->nrc_allocs, bytes); };
     ctx->nrc_query = static_cast<float *>(A(sizeof(float) * NRC_QUERY_FLOATS * pixels));
     ctx->nrc_weight = static_cast<float4 *>(A(sizeof(float4) * pixels));
     ctx->nrc_pred = static_cast<float4 *>(A(sizeof(float4) * pixels));
-    ctx->nrc_samples = static_cast<float *>(A(sizeof(float) * NRC_SAMPLE_FLOATS * std::max<size_t>(sample_cap, 1)));
-    ctx->nrc_samples2 = static_cast<float *>(A(sizeof(float) * NRC_SAMPLE_FLOATS * std::max<size_t>(sample_cap, 1)));
     ctx->nrc_counts = static_cast<uint32_t *>(A(sizeof(uint32_t) * 4));
     for(auto &sp : ctx->nrc_spread)
         sp = static_cast<float2 *>(A(sizeof(float2) * pixels));
     ctx->nrc_pixels = pixels;
-    ctx->nrc_sample_cap = sample_cap;
+}
+
+void ensure_nrc_samples(btrc_nrc *nrc, size_t sample_cap)
+{
+    if(nrc->sample_cap >= sample_cap && nrc->sample_count)
+        return;
+    nrc->wait_training();
+    nrc->free_samples();
+    for(float *&p : nrc->samples)
+        check_cuda(cudaMalloc(&p, sizeof(float) * NRC_SAMPLE_FLOATS * std::max<size_t>(sample_cap, 1)),
+                   "training samples");
+    check_cuda(cudaMalloc(&nrc->sample_count, sizeof(uint32_t) * 3), "training samples");
+    check_cuda(cudaMemset(nrc->sample_count, 0, sizeof(uint32_t) * 3), "training samples");
+    nrc->sample_cap = sample_cap;
 }
 
 } // namespace
@@ -1597,10 +1628,23 @@ btrc_status btrc_render_nrc_frame(btrc_ctx *ctx, btrc_scene *scene, btrc_nrc *nr
             std::min<uint64_t>(static_cast<uint64_t>(H.params.state_count), std::max<size_t>(pixels, 1)));
         const size_t sample_cap = static_cast<size_t>(opts->train_steps) * static_cast<size_t>(opts->train_batch);
         ensure_render_buffers(ctx, capacity, pixels);
-        ensure_nrc_buffers(ctx, pixels, sample_cap);
+        ensure_nrc_buffers(ctx, pixels);
+        ensure_nrc_samples(nrc, sample_cap);
+        if(!nrc->train_stream)
+        {
+            check_cuda(cudaStreamCreateWithFlags(&nrc->train_stream, cudaStreamNonBlocking), "training stream");
+            check_cuda(cudaStreamCreateWithFlags(&nrc->path_stream, cudaStreamNonBlocking), "training stream");
+            for(cudaEvent_t *ev : { &nrc->ready, &nrc->trained, &nrc->paths_done[0], &nrc->paths_done[1],
+                                    &nrc->paths_done[2] })
+                check_cuda(cudaEventCreateWithFlags(ev, cudaEventDisableTiming), "training event");
+            check_cuda(cudaMallocHost(&nrc->loss_host, 2 * sizeof(float)), "loss buffer");
+            nrc->loss_host[0] = nrc->loss_host[1] = 0.0f;
+        }
         cudaStream_t s = ctx->stream;
+        const int slot = nrc->slot;
         check_cuda(cudaMemsetAsync(ctx->buf.film, 0, sizeof(float4) * pixels, s), "film clear");
         check_cuda(cudaMemsetAsync(ctx->nrc_counts, 0, sizeof(uint32_t) * 4, s), "counter clear");
+        check_cuda(cudaMemsetAsync(nrc->sample_count + slot, 0, sizeof(uint32_t), s), "counter clear");
         DevRender R = make_render_params(scene, 1, capacity);
         R.sample_offset = opts->frame;
         R.nrc_terminate = opts->terminate_vertex;
@@ -1612,46 +1656,43 @@ btrc_status btrc_render_nrc_frame(btrc_ctx *ctx, btrc_scene *scene, btrc_nrc *nr
         R.nrc_count = ctx->nrc_counts;
         R.nrc_cap = static_cast<uint32_t>(pixels);
         ctx->buf.capacity = capacity;
-        if(!nrc->train_stream)
-        {
-            check_cuda(cudaStreamCreateWithFlags(&nrc->train_stream, cudaStreamNonBlocking), "training stream");
-            check_cuda(cudaEventCreateWithFlags(&nrc->ready, cudaEventDisableTiming), "training event");
-            check_cuda(cudaEventCreateWithFlags(&nrc->trained, cudaEventDisableTiming), "training event");
-            check_cuda(cudaEventCreateWithFlags(&nrc->paths_done, cudaEventDisableTiming), "training event");
-            check_cuda(cudaMallocHost(&nrc->loss_host, 2 * sizeof(float)), "loss buffer");
-            nrc->loss_host[0] = nrc->loss_host[1] = 0.0f;
-        }
-        // this frame's samples: the buffer the last frame's training (maybe still running)
-        // does not read
-        float *samples = ctx->nrc_parity ? ctx->nrc_samples2 : ctx->nrc_samples;
         const bool on_dev = opts->output_on_device != 0;
         float *rgb_dev = on_dev ? rgb_out : ctx_scratch_images(ctx, pixels, 1);
         uint32_t *err = ctx_scratch_err(ctx);
-        // training paths (they read no weights) on the cache's stream, beside this frame's
-        // path tracing, after the counter clear
+        // this frame's training paths (they read no weights) on their own stream, beside
+        // this frame's path tracing, into this frame's sample buffer. That buffer was last
+        // read by the Adam steps of three calls back, which finished before the inference
+        // of two calls back, which this stream has passed.
         const bool train_paths = opts->train_stride > 0 && sample_cap > 0;
         if(train_paths)
         {
-            cudaStream_t ts = nrc->train_stream;
+            cudaStream_t ps = nrc->path_stream;
             check_cuda(cudaEventRecord(nrc->ready, s), "training event");
-            check_cuda(cudaStreamWaitEvent(ts, nrc->ready, 0), "training wait");
+            check_cuda(cudaStreamWaitEvent(ps, nrc->ready, 0), "training wait");
             const uint32_t stride = static_cast<uint32_t>(opts->train_stride);
             const uint32_t phase = (opts->frame * 7u + 3u) % stride;
-            check_cuda(launch_nrc_train_paths(scene->dev, R, stride, phase, opts->frame + (1u << 20), samples,
-                                              ctx->nrc_counts + 1, static_cast<uint32_t>(sample_cap), err, ts),
+            check_cuda(launch_nrc_train_paths(scene->dev, R, stride, phase, opts->frame + (1u << 20), nrc->samples[slot],
+                                              nrc->sample_count + slot, static_cast<uint32_t>(sample_cap), err, ps),
                        "training paths");
-            check_cuda(cudaEventRecord(nrc->paths_done, ts), "training event");
+            check_cuda(cudaEventRecord(nrc->paths_done[slot], ps), "training event");
         }
         RenderStats rs{};
         check_cuda(render_wavefront(scene->dev, R, ctx->buf, s, &ctx->cancel, true, 0, &rs, &cancelled),
                    "wavefront render");
-        if(train_paths)
-            check_cuda(cudaStreamWaitEvent(s, nrc->paths_done, 0), "training wait");
-        uint32_t counts[4] = {};
+        // the queries and training samples of this frame
+        uint32_t counts[4] = {}, ns_frame = 0;
         check_cuda(cudaMemcpyAsync(counts, ctx->nrc_counts, sizeof(counts), cudaMemcpyDeviceToHost, s), "counters");
+        if(train_paths)
+        {
+            check_cuda(cudaStreamWaitEvent(s, nrc->paths_done[slot], 0), "training wait");
+            check_cuda(cudaMemcpyAsync(&ns_frame, nrc->sample_count + slot, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                       s),
+                       "counters");
+        }
         check_cuda(cudaStreamSynchronize(s), "counters");
         const uint32_t nq = std::min<uint32_t>(counts[0], static_cast<uint32_t>(pixels));
-        // inference reads the weights the last frame's training writes
+        const uint32_t ns = std::min<uint32_t>(ns_frame, static_cast<uint32_t>(sample_cap));
+        // inference reads the weights the last Adam steps write
         if(nrc->pending)
             check_cuda(cudaStreamWaitEvent(s, nrc->trained, 0), "training wait");
         if(nq > 0 && opts->terminate_vertex >= 0)
@@ -1663,13 +1704,12 @@ btrc_status btrc_render_nrc_frame(btrc_ctx *ctx, btrc_scene *scene, btrc_nrc *nr
                        "cache splat");
         }
         check_cuda(launch_resolve(ctx->buf.film, rgb_dev, static_cast<uint32_t>(pixels), s), "resolve");
-        // train on this frame's samples, on the cache's own stream after this frame's
-        // inference: the call returns without waiting for it, and the next frame's path
-        // tracing runs beside it
-        const uint32_t ns = std::min<uint32_t>(counts[1], static_cast<uint32_t>(sample_cap));
-        // the last frame's loss slot: final once this frame's stream work (which waited for
-        // that training) has completed, read after the frame sync below
-        const int prev_slot = nrc->parity ^ 1;
+        // Adam steps on this frame's samples, on the training stream after this frame's
+        // inference: the call returns without waiting for them, and the next frame's path
+        // tracing runs beside them
+        // the last call's loss slot: final once this call's stream work (which waited for
+        // those steps) has completed, read after the frame sync below
+        const int loss_prev = nrc->parity ^ 1;
         int steps = 0;
         for(int k = 0; k < opts->train_steps; ++k)
             if(static_cast<uint32_t>(k) * static_cast<uint32_t>(opts->train_batch) < ns)
@@ -1684,8 +1724,9 @@ btrc_status btrc_render_nrc_frame(btrc_ctx *ctx, btrc_scene *scene, btrc_nrc *nr
             {
                 const uint32_t b0 = static_cast<uint32_t>(k) * static_cast<uint32_t>(opts->train_batch);
                 const uint32_t nb = std::min<uint32_t>(static_cast<uint32_t>(opts->train_batch), ns - b0);
-                check_cuda(nrc->impl->train(samples + static_cast<size_t>(b0) * NRC_SAMPLE_FLOATS, nb, true, ts),
-                           "cache training");
+                check_cuda(
+                    nrc->impl->train(nrc->samples[slot] + static_cast<size_t>(b0) * NRC_SAMPLE_FLOATS, nb, true, ts),
+                    "cache training");
             }
             check_cuda(nrc->impl->copy_loss_async(nrc->loss_host + nrc->parity, ts), "cache training");
             check_cuda(cudaEventRecord(nrc->trained, ts), "training event");
@@ -1695,7 +1736,7 @@ btrc_status btrc_render_nrc_frame(btrc_ctx *ctx, btrc_scene *scene, btrc_nrc *nr
             nrc->loss_host[nrc->parity] = 0.0f;
         nrc->loss_steps[nrc->parity] = steps;
         nrc->parity ^= 1;
-        ctx->nrc_parity ^= 1;
+        nrc->slot = (slot + 1) % 3;
         if(!on_dev)
             check_cuda(cudaMemcpyAsync(rgb_out, rgb_dev, pixels * 3 * sizeof(float), cudaMemcpyDeviceToHost, s),
                        "image download");
@@ -1709,7 +1750,7 @@ btrc_status btrc_render_nrc_frame(btrc_ctx *ctx, btrc_scene *scene, btrc_nrc *nr
             fstats->train_steps = steps;
             // the last frame's training has finished by now (this frame's stream waited for
             // it before inference); this frame's finishes after the call returns
-            fstats->loss = nrc->loss_steps[prev_slot] ? nrc->loss_host[prev_slot] / nrc->loss_steps[prev_slot] : 0.0f;
+            fstats->loss = nrc->loss_steps[loss_prev] ? nrc->loss_host[loss_prev] / nrc->loss_steps[loss_prev] : 0.0f;
             fstats->render_ms = rs.device_ms;
             fstats->wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
         }

@@ -1141,8 +1141,11 @@ __global__ void __launch_bounds__(BLOCK) k_order(const uint32_t *__restrict__ fl
     }
 }
 
-// MediumPipeline (builtin/btrc/builtin/renderer/wavefront/medium.cpp:28-249)
-__global__ void __launch_bounds__(BLOCK) k_medium(DevScene S, DevRender R, PathSoA P, PathSoA N, ShadowSoA SH, int shq,
+// MediumPipeline (builtin/btrc/builtin/renderer/wavefront/medium.cpp:28-249). Four blocks
+// per SM (64 registers, a few hundred bytes of spills): the tracking loop waits on
+// dependent density fetches, and the volume frame (256^3 grid, 1024^2, 64 spp) ran in
+// 832 ms against 856 ms at three blocks (80 registers) and 841-858 ms at five
+__global__ void __launch_bounds__(BLOCK, 4) k_medium(DevScene S, DevRender R, PathSoA P, PathSoA N, ShadowSoA SH, int shq,
                                                   uint32_t *flags, const HitDetail *hits, float4 *film, Counters *cnt)
 {
     const uint32_t n = cnt->active;

@@ -385,11 +385,12 @@ typedef struct btrc_nrc_frame_stats
 /* One frame of one path per pixel through the wavefront renderer with paths terminated
    into the radiance cache, training paths for 1 / train_stride of the pixels, cache
    inference and splatting, then the frame's Adam steps. rgb_out receives the frame's
-   width*height*3 image (radiance / weight) when the call returns; the Adam steps run on
-   the cache's own stream and may still be running then, beside the next frame's path
-   tracing. The next frame's inference, btrc_nrc_infer, btrc_nrc_train, btrc_nrc_params
-   and btrc_nrc_destroy wait for them. Scenes with participating media:
-   BTRC_ERR_UNSUPPORTED. */
+   width*height*3 image (radiance / weight) when the call returns. The training paths
+   run on a stream of the cache's own beside the frame's path tracing, and the frame's
+   Adam steps on a second such stream that may still be running when the call returns,
+   beside the next frame's path tracing. The next frame's inference, btrc_nrc_infer,
+   btrc_nrc_train, btrc_nrc_params and btrc_nrc_destroy wait for them. Scenes with
+   participating media: BTRC_ERR_UNSUPPORTED. */
 btrc_status btrc_render_nrc_frame(btrc_ctx *ctx, btrc_scene *scene, btrc_nrc *nrc, const btrc_nrc_render_opts *opts,
                                   float *rgb_out, btrc_nrc_frame_stats *stats);
 
