@@ -853,6 +853,7 @@ void btrc_ctx_destroy(btrc_ctx *ctx)
         cudaStreamSynchronize(ctx->stream);
     if(!ctx->nrc_allocs.empty())
         cudaDeviceSynchronize();  // a cache's training paths may still be using the context's scratch
+    release_render_graph(ctx->buf);
     for(void *p : ctx->buf_allocs)
         cudaFree(p);
     for(void *p : ctx->nrc_allocs)
@@ -1850,6 +1851,7 @@ BatchLane::~BatchLane()
 {
     if(stream)
         cudaStreamSynchronize(stream);
+    release_render_graph(buf);
     for(void *p : allocs)
         cudaFree(p);
     if(buf.host_counters)

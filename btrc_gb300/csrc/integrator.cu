@@ -1806,6 +1806,63 @@ cudaError_t upload_primes()
     return e;
 }
 
+// What render_wavefront keeps with its buffers between calls: the side stream and the
+// events of the bounce graph, the instantiated graph (updated in place when only kernel
+// arguments change, instantiated anew when the launches differ) and the timing events.
+struct RenderGraph
+{
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, odd_done = nullptr, even_shaded = nullptr, even_done = nullptr;
+    cudaEvent_t ring[RING_SLOTS] = {};
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+void release_render_graph(RenderBuffers &B)
+{
+    RenderGraph *G = B.graph;
+    if(!G)
+        return;
+    if(G->exec)
+        cudaGraphExecDestroy(G->exec);
+    for(cudaEvent_t ev : { G->fork, G->odd_done, G->even_shaded, G->even_done, G->t0, G->t1 })
+        if(ev)
+            cudaEventDestroy(ev);
+    for(cudaEvent_t ev : G->ring)
+        if(ev)
+            cudaEventDestroy(ev);
+    if(G->side)
+        cudaStreamDestroy(G->side);
+    delete G;
+    B.graph = nullptr;
+}
+
+namespace {
+
+cudaError_t render_graph_setup(RenderBuffers &B)
+{
+    if(B.graph)
+        return cudaSuccess;
+    RenderGraph *G = new RenderGraph();
+    B.graph = G;
+    cudaError_t e = cudaStreamCreateWithFlags(&G->side, cudaStreamNonBlocking);
+    for(cudaEvent_t *ev : { &G->fork, &G->odd_done, &G->even_shaded, &G->even_done })
+        if(e == cudaSuccess)
+            e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    for(cudaEvent_t &ev : G->ring)
+        if(e == cudaSuccess)
+            e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if(e == cudaSuccess)
+        e = cudaEventCreate(&G->t0);
+    if(e == cudaSuccess)
+        e = cudaEventCreate(&G->t1);
+    if(e != cudaSuccess)
+        release_render_graph(B);
+    return e;
+}
+
+} // namespace
+
 cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffers &B, cudaStream_t st,
                              const std::atomic<bool> *cancel, bool use_graphs, int profile, RenderStats *stats,
                              bool *cancelled, std::vector<std::pair<double, uint64_t>> *progress,
@@ -1835,31 +1892,17 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
     // launch, beside its even bounce, and once more after the last launch. A bounce that
     // reuses a shadow queue (its control kernel resets the queue's counters) waits for the
     // shadow kernel that reads it.
+    if((e = render_graph_setup(B)) != cudaSuccess)
+        return e;
+    RenderGraph &G = *B.graph;
     cudaGraphExec_t exec = nullptr;
-    cudaStream_t side = nullptr;
-    cudaEvent_t fork = nullptr, odd_done = nullptr, even_shaded = nullptr, even_done = nullptr;
-    auto release = [&] {
-        if(exec)
-            cudaGraphExecDestroy(exec);
-        for(cudaEvent_t ev : { fork, odd_done, even_shaded, even_done })
-            if(ev)
-                cudaEventDestroy(ev);
-        if(side)
-            cudaStreamDestroy(side);
-    };
+    cudaStream_t side = G.side;
+    cudaEvent_t fork = G.fork, odd_done = G.odd_done, even_shaded = G.even_shaded, even_done = G.even_done;
     if(use_graphs)
     {
-        e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
-        for(cudaEvent_t *ev : { &fork, &odd_done, &even_shaded, &even_done })
-            if(e == cudaSuccess)
-                e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
-        if(e == cudaSuccess)
-            e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+        e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
         if(e != cudaSuccess)
-        {
-            release();
             return e;
-        }
         uint64_t dummy[STAGE_COUNT] = {};
         cudaEventRecord(fork, st);
         cudaStreamWaitEvent(side, fork, 0);
@@ -1877,22 +1920,34 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
         e = cudaStreamEndCapture(st, &graph);
         if(e == cudaSuccess)
         {
-            e = cudaGraphInstantiate(&exec, graph, 0);
+            // the kept graph takes the new arguments in place when the launches are the
+            // same ones; otherwise it is instantiated anew
+            if(G.exec)
+            {
+                cudaGraphExecUpdateResultInfo info{};
+                if(cudaGraphExecUpdate(G.exec, graph, &info) != cudaSuccess)
+                {
+                    cudaGetLastError();
+                    cudaGraphExecDestroy(G.exec);
+                    G.exec = nullptr;
+                }
+            }
+            if(!G.exec)
+                e = cudaGraphInstantiate(&G.exec, graph, 0);
             cudaGraphDestroy(graph);
         }
         if(e != cudaSuccess)
         {
-            release();
+            if(G.exec)
+                cudaGraphExecDestroy(G.exec);
+            G.exec = nullptr;
             return e;
         }
+        exec = G.exec;
     }
 
-    cudaEvent_t ev[RING_SLOTS];
-    for(int k = 0; k < RING_SLOTS; ++k)
-        cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming);
-    cudaEvent_t t0, t1;
-    cudaEventCreate(&t0);
-    cudaEventCreate(&t1);
+    cudaEvent_t *ev = G.ring;
+    cudaEvent_t t0 = G.t0, t1 = G.t1;
     // progress log: one timing event and one copy of the generated-path counter per launch
     std::vector<cudaEvent_t> prog_ev;
     uint64_t *prog_gen = nullptr;
@@ -2011,11 +2066,6 @@ cudaError_t render_wavefront(const DevScene &S, const DevRender &R, RenderBuffer
     }
     Counters fin{};
     cudaMemcpy(&fin, B.counters, sizeof(Counters), cudaMemcpyDeviceToHost);
-    for(int k = 0; k < RING_SLOTS; ++k)
-        cudaEventDestroy(ev[k]);
-    cudaEventDestroy(t0);
-    cudaEventDestroy(t1);
-    release();
     if(stats)
     {
         *stats = RenderStats{};

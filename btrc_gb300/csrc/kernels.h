@@ -36,7 +36,11 @@ struct RenderBuffers
     Counters *counters;
     Counters *host_counters;  // pinned, ring of RING_SLOTS
     uint32_t capacity;
+    struct RenderGraph *graph = nullptr;  // bounce graph, side stream and events kept across renders
 };
+
+// Destroys the bounce graph, side stream and events render_wavefront keeps with B.
+void release_render_graph(RenderBuffers &B);
 
 constexpr int RING_SLOTS = 4;
 
