@@ -51,12 +51,14 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched uneven-scenes measurement")
     ap.add_argument("--nrc-frames", type=int, default=1000, help="frames of the radiance-cache study")
     ap.add_argument("--ref-spp", type=int, default=4096, help="spp of the converged reference image")
-    ap.add_argument("--probe", choices=["nrc", "medium", "generate", "trace", "trace-two-level", "build-device"],
+    ap.add_argument("--probe", choices=["nrc", "nrc-frames", "medium", "generate", "trace", "trace-two-level",
+                                        "build-device"],
                     help="run one small profiling case and exit: nrc (cache inference on 2^20 queries and "
                          "training steps of 16,384 samples), medium (volume workload at 256x256, 4 spp), "
                          "generate / trace (terrain at 1920x1080, 1 spp, 2 M-state queue), trace-two-level "
                          "(the same through the two-level acceleration structure), build-device (the "
-                         "terrain's BVH built on the device)")
+                         "terrain's BVH built on the device), nrc-frames (25 radiance-cache frames of the "
+                         "Cornell box at 512x512)")
     ap.add_argument("--trace-probe", action="store_true",
                     help="trace the workload's camera rays, then one diffuse bounce ray per camera hit, "
                          "through btrc_trace_closest (two launches, for DRAM-traffic captures) and exit")
@@ -832,6 +834,25 @@ def probe(args):
     import btrc_gb300 as B
     from btrc_gb300 import scenes
     ctx = B.Context(0)
+    if args.probe == "nrc-frames":
+        p = scenes.cornell(width=512, height=512, spp=16)
+        sc = ctx.load_scene(p).build()
+        info = sc.info()
+        img = torch.empty((info.height, info.width, 3), dtype=torch.float32, device="cuda")
+        cache = B.RadianceCache(ctx, info.world_min, info.world_max, seed=1)
+        cur = torch.cuda.current_stream()
+        walls, st = [], {}
+        for f in range(25):
+            t = time.perf_counter()
+            cache.render_frame(sc, f, out=img, terminate_vertex=1, train_stride=16, train_steps=4,
+                               train_batch=16384, stats=st)
+            cur.synchronize()
+            walls.append((time.perf_counter() - t) * 1000)
+        torch.cuda.synchronize()
+        print(json.dumps({"wall_ms": walls[5:], "render_ms": st["render_ms"], "queries": st["queries"]}), flush=True)
+        cache.close()
+        ctx.close()
+        return
     if args.probe == "build-device":
         p = scenes.terrain(width=1920, height=1080, spp=1, state_count=1 << 21)
         sc = ctx.load_scene(p).build(builder="device")
