@@ -80,3 +80,26 @@ def test_merged_batch_refuses_media(gpu_ctx, scene_dir):
         gpu_ctx.render_batch([sc], [out], merged=True)
     assert e.value.status == 8
     sc.close()
+
+
+def test_batches_of_device_built_and_two_level_scenes(gpu_ctx, scene_dir):
+    """Device-built BVHs go through the merged pass and two-level scenes through the lanes,
+    each giving the image of the scene's own render."""
+    paths = scenes.batch(count=4, seed=79, out_dir=scene_dir / "batch-forms")
+    dev = gpu_ctx.load_build_scenes([str(p) for p in paths], builder="device")
+    infos = [s.info() for s in dev]
+    assert all(i.bvh_builder == 1 for i in infos)
+    refs = [gpu_ctx.render(s) for s in dev]
+    outs = [np.zeros((i.height, i.width, 3), np.float32) for i in infos]
+    gpu_ctx.render_batch(dev, outs, autotune=False, merged=True)
+    for o, r in zip(outs, refs):
+        assert np.allclose(o, r, rtol=1e-4, atol=1e-5)
+    two = gpu_ctx.load_build_scenes([str(p) for p in paths], two_level=True)
+    assert all(s.info().two_level == 1 for s in two)
+    refs2 = [gpu_ctx.render(s) for s in two]
+    outs2 = [np.zeros((i.height, i.width, 3), np.float32) for i in infos]
+    gpu_ctx.render_batch(two, outs2, lanes=2, autotune=False)
+    for o, r in zip(outs2, refs2):
+        assert np.allclose(o, r, rtol=1e-4, atol=1e-5)
+    for s in dev + two:
+        s.close()
